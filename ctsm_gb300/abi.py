@@ -1,0 +1,122 @@
+"""ctypes mirror of include/ctsm_gpu.h and the field manifest of the soil path.
+
+The manifest records, for every derived-type component the C-ABI carries, its
+level kind (which fixes its Fortran lower bound and level count), its element
+type and whether the call reads it, writes it, or both.  The same manifest
+drives the host state container, the device buffers of the batched engine and
+the algorithmic-byte count used for the roofline.
+"""
+import ctypes as C
+
+NLEVSNO = 12
+NLEVSOI = 20
+NLEVGRND = 25
+
+# level kind -> (lower bound, number of levels); the C-ABI stores element
+# (c, j) at base[(c - begc) + (j - lb) * ld]  (src/main/ColumnType.F90:137-155)
+LEVELS = {
+    "C": (None, 1),                       # scalar per column (1-D)
+    "P": (None, 1),                       # scalar per patch (1-D)
+    "SS": (-NLEVSNO + 1, NLEVSNO + NLEVGRND),
+    "ZI": (-NLEVSNO, NLEVSNO + NLEVGRND + 1),
+    "G": (1, NLEVGRND),
+    "S": (1, NLEVSOI),
+    "SN": (-NLEVSNO + 1, NLEVSNO),
+    "PL": (-NLEVSNO + 1, NLEVSNO + 1),    # patch, snow levels + top soil
+}
+
+F64, I32 = "f8", "i4"
+
+# (name, kind, dtype, use) in the order of the C structs; use: in / out / inout
+SOILWATER_FIELDS = [
+    ("z", "SS", F64, "in"), ("zi", "ZI", F64, "in"), ("dz", "SS", F64, "in"),
+    ("zwt", "C", F64, "in"), ("qcharge", "C", F64, "out"), ("icefrac", "G", F64, "out"),
+    ("qin", "S", F64, "out"), ("qout", "S", F64, "out"),
+    ("smpmin", "C", F64, "in"), ("watsat", "G", F64, "in"), ("hksat", "G", F64, "in"),
+    ("bsw", "G", F64, "in"), ("sucsat", "G", F64, "in"),
+    ("smp_l", "G", F64, "out"), ("hk_l", "G", F64, "out"),
+    ("h2osoi_ice", "SS", F64, "in"), ("h2osoi_liq", "SS", F64, "inout"),
+    ("h2osoi_vol", "G", F64, "in"),
+    ("qflx_deficit", "C", F64, "out"), ("qflx_infl", "C", F64, "in"),
+    ("qflx_rootsoi", "S", F64, "in"),
+    ("t_soisno", "SS", F64, "in"),
+]
+
+SOILTEMP_FIELDS = [
+    ("snl", "C", I32, "in"), ("nbedrock", "C", I32, "in"),
+    ("z", "SS", F64, "in"), ("zi", "ZI", F64, "in"), ("dz", "SS", F64, "in"),
+    ("col_patchi", "C", I32, "in"), ("col_npatches", "C", I32, "in"),
+    ("wtcol", "P", F64, "in"), ("frac_veg_nosno", "P", I32, "in"),
+    ("forc_lwrad", "C", F64, "in"), ("sabg", "P", F64, "in"), ("sabg_soil", "P", F64, "in"),
+    ("sabg_snow", "P", F64, "in"), ("sabg_lyr", "PL", F64, "in"), ("sabg_chk", "P", F64, "out"),
+    ("htvp", "C", F64, "in"), ("cgrnd", "P", F64, "in"), ("dlrad", "P", F64, "in"),
+    ("eflx_sh_grnd", "P", F64, "in"), ("eflx_sh_snow", "P", F64, "in"),
+    ("eflx_sh_soil", "P", F64, "in"), ("eflx_sh_h2osfc", "P", F64, "in"),
+    ("qflx_evap_soi", "P", F64, "in"), ("qflx_ev_snow", "P", F64, "in"),
+    ("qflx_ev_soil", "P", F64, "in"), ("qflx_ev_h2osfc", "P", F64, "in"),
+    ("eflx_bot", "C", F64, "in"),
+    ("eflx_gnet", "P", F64, "out"), ("dgnetdT", "P", F64, "out"),
+    ("eflx_fgr12", "C", F64, "out"), ("eflx_fgr", "G", F64, "out"),
+    ("eflx_snomelt", "C", F64, "out"), ("eflx_h2osfc_to_snow", "C", F64, "out"),
+    ("emg", "C", F64, "in"), ("t_soisno", "SS", F64, "inout"), ("t_h2osfc", "C", F64, "inout"),
+    ("t_grnd", "C", F64, "inout"), ("fact", "SS", F64, "out"), ("c_h2osfc", "C", F64, "out"),
+    ("xmf", "C", F64, "out"), ("xmf_h2osfc", "C", F64, "out"), ("imelt", "SS", I32, "out"),
+    ("watsat", "G", F64, "in"), ("bsw", "G", F64, "in"), ("sucsat", "G", F64, "in"),
+    ("tkmg", "G", F64, "in"), ("tkdry", "G", F64, "in"), ("csol", "G", F64, "in"),
+    ("thk", "SS", F64, "out"),
+    ("h2osoi_liq", "SS", F64, "inout"), ("h2osoi_ice", "SS", F64, "inout"),
+    ("h2osfc", "C", F64, "inout"), ("h2osno_no_layers", "C", F64, "inout"),
+    ("int_snow", "C", F64, "inout"), ("snow_depth", "C", F64, "inout"),
+    ("snomelt_accum", "C", F64, "inout"),
+    ("frac_sno_eff", "C", F64, "in"), ("frac_h2osfc", "C", F64, "in"),
+    ("bw", "SN", F64, "out"), ("qflx_snomelt", "C", F64, "out"), ("qflx_snofrz", "C", F64, "out"),
+    ("qflx_snow_drain", "C", F64, "out"), ("qflx_snomelt_lyr", "SN", F64, "out"),
+    ("qflx_snofrz_lyr", "SN", F64, "out"), ("qflx_h2osfc_to_ice", "C", F64, "out"),
+]
+
+
+def _ptr_type(dtype):
+    return C.POINTER(C.c_double) if dtype == F64 else C.POINTER(C.c_int32)
+
+
+class Bounds(C.Structure):
+    _fields_ = [("begc", C.c_int32), ("endc", C.c_int32), ("begp", C.c_int32), ("endp", C.c_int32)]
+
+
+class Options(C.Structure):
+    _fields_ = [("soilwater_movement_method", C.c_int32), ("snow_thermal_cond_method", C.c_int32),
+                ("itmax_canopy_fluxes", C.c_int32), ("stomatalcond_method", C.c_int32),
+                ("nlevsno", C.c_int32), ("nlevsoi", C.c_int32), ("nlevgrnd", C.c_int32)]
+
+
+class SoilWaterParams(C.Structure):
+    _fields_ = [("e_ice", C.c_double)]
+
+
+class SoilWaterIO(C.Structure):
+    _fields_ = [("ldc", C.c_int32)] + [(n, _ptr_type(t)) for (n, _, t, _) in SOILWATER_FIELDS]
+
+
+class SoilTempIO(C.Structure):
+    _fields_ = [("ldc", C.c_int32), ("ldp", C.c_int32)] + \
+               [(n, _ptr_type(t)) for (n, _, t, _) in SOILTEMP_FIELDS]
+
+
+def field_shape(kind, ncol, npatch):
+    """numpy shape (levels, columns-or-patches) of a manifest field."""
+    n = npatch if kind in ("P", "PL") else ncol
+    nlev = LEVELS[kind][1]
+    return (n,) if kind in ("C", "P") else (nlev, n)
+
+
+def make_io(cls, fields, arrays, ldc, ldp=None):
+    """Fill a ctypes io struct with pointers into the numpy arrays of `arrays`."""
+    io = cls()
+    io.ldc = ldc
+    if ldp is not None:
+        io.ldp = ldp
+    for (n, _, t, _) in fields:
+        a = arrays[n]
+        assert a.flags.c_contiguous, n
+        setattr(io, n, a.ctypes.data_as(_ptr_type(t)))
+    return io

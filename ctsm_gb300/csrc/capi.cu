@@ -1,0 +1,346 @@
+// capi.cu -- extern "C" entry points of libctsm_gpu.so (declared in
+// include/ctsm_gpu.h).  Plain drop-in mode: every call copies the clump's
+// arrays to the device, runs the kernel over the filter and copies the
+// written components back, on a CUDA stream owned by the calling host thread.
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+#include "ctsm_gpu.h"
+#include "ctsm_device.cuh"
+#include "soil_kernels.cuh"
+#include "capi_internal.h"
+
+namespace ctsmg {
+
+// ------------------------------------------------------------ global state
+static std::mutex g_mu;
+static bool g_init = false;
+static ctsmg_options g_opt;
+static ctsmg_soilwater_params g_swp = {6.0};
+
+// ------------------------------------------------------------ per-thread context
+struct ThreadCtx {
+    cudaStream_t stream = nullptr;
+    char* arena = nullptr;
+    size_t arena_cap = 0, arena_top = 0;
+    DevError* err = nullptr;
+    std::string msg;
+    int err_index = 0, err_level = 0;
+    ~ThreadCtx() {
+        if (arena) cudaFree(arena);
+        if (err) cudaFree(err);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+static thread_local ThreadCtx* t_ctx = nullptr;
+static thread_local unsigned t_gen = 0;
+static unsigned g_gen = 1;               // bumped by ctsmg_finalize
+static std::vector<ThreadCtx*> g_ctxs;
+
+static thread_local std::string t_msg;
+static thread_local int t_idx = 0, t_lev = 0;
+
+int set_error(int code, const char* what, int index, int level) {
+    char buf[512];
+    std::snprintf(buf, sizeof buf, "%s", what);
+    t_msg = buf;
+    t_idx = index;
+    t_lev = level;
+    return code;
+}
+
+static int cuda_fail(cudaError_t e, const char* where) {
+    std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+    return set_error(CTSMG_E_CUDA, m.c_str(), 0, 0);
+}
+
+static int ctx_get(ThreadCtx** out) {
+    if (!g_init) return set_error(CTSMG_E_NOT_INIT, "ctsmg_init has not been called", 0, 0);
+    if (t_gen != g_gen) t_ctx = nullptr;   // contexts were freed by ctsmg_finalize
+    if (!t_ctx) {
+        ThreadCtx* c = new ThreadCtx();
+        cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaStreamCreate"); }
+        e = cudaMalloc(&c->err, sizeof(DevError));
+        if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaMalloc(err)"); }
+        t_ctx = c;
+        std::lock_guard<std::mutex> lk(g_mu);
+        t_gen = g_gen;
+        g_ctxs.push_back(c);
+    }
+    *out = t_ctx;
+    return 0;
+}
+
+// bump allocator over one device arena; grows (and invalidates) between calls
+static int arena_reserve(ThreadCtx* c, size_t bytes) {
+    if (bytes <= c->arena_cap) { c->arena_top = 0; return 0; }
+    if (c->arena) { cudaStreamSynchronize(c->stream); cudaFree(c->arena); c->arena = nullptr; }
+    size_t cap = bytes + bytes / 4 + (1 << 20);
+    cudaError_t e = cudaMalloc(&c->arena, cap);
+    if (e != cudaSuccess) { c->arena_cap = 0; return cuda_fail(e, "cudaMalloc(arena)"); }
+    c->arena_cap = cap;
+    c->arena_top = 0;
+    return 0;
+}
+static void* arena_take(ThreadCtx* c, size_t bytes) {
+    size_t off = (c->arena_top + 255) & ~(size_t)255;
+    c->arena_top = off + bytes;
+    return c->arena + off;
+}
+
+// ------------------------------------------------------------ field tables
+int kind_levels(int kind) {
+    switch (kind) {
+        case K_C: case K_P: return 1;
+        case K_SS: return NLEVSNO + NLEVGRND;
+        case K_ZI: return NLEVSNO + NLEVGRND + 1;
+        case K_G: return NLEVGRND;
+        case K_S: return NLEVSOI;
+        case K_SN: return NLEVSNO;
+        case K_PL: return NLEVSNO + 1;
+    }
+    return 0;
+}
+
+#define FW(S, name, kind, esz, use) {offsetof(S, name), kind, esz, use, #name}
+const FieldDesc SOILWATER_TABLE[] = {
+    FW(ctsmg_soilwater_io, z, K_SS, 8, U_IN), FW(ctsmg_soilwater_io, zi, K_ZI, 8, U_IN),
+    FW(ctsmg_soilwater_io, dz, K_SS, 8, U_IN), FW(ctsmg_soilwater_io, zwt, K_C, 8, U_IN),
+    FW(ctsmg_soilwater_io, qcharge, K_C, 8, U_OUT), FW(ctsmg_soilwater_io, icefrac, K_G, 8, U_OUT),
+    FW(ctsmg_soilwater_io, qin, K_S, 8, U_OUT), FW(ctsmg_soilwater_io, qout, K_S, 8, U_OUT),
+    FW(ctsmg_soilwater_io, smpmin, K_C, 8, U_IN), FW(ctsmg_soilwater_io, watsat, K_G, 8, U_IN),
+    FW(ctsmg_soilwater_io, hksat, K_G, 8, U_IN), FW(ctsmg_soilwater_io, bsw, K_G, 8, U_IN),
+    FW(ctsmg_soilwater_io, sucsat, K_G, 8, U_IN), FW(ctsmg_soilwater_io, smp_l, K_G, 8, U_OUT),
+    FW(ctsmg_soilwater_io, hk_l, K_G, 8, U_OUT), FW(ctsmg_soilwater_io, h2osoi_ice, K_SS, 8, U_IN),
+    FW(ctsmg_soilwater_io, h2osoi_liq, K_SS, 8, U_INOUT), FW(ctsmg_soilwater_io, h2osoi_vol, K_G, 8, U_IN),
+    FW(ctsmg_soilwater_io, qflx_deficit, K_C, 8, U_OUT), FW(ctsmg_soilwater_io, qflx_infl, K_C, 8, U_IN),
+    FW(ctsmg_soilwater_io, qflx_rootsoi, K_S, 8, U_IN), FW(ctsmg_soilwater_io, t_soisno, K_SS, 8, U_IN),
+};
+const int SOILWATER_NFIELDS = sizeof(SOILWATER_TABLE) / sizeof(SOILWATER_TABLE[0]);
+
+#define FT(name, kind, esz, use) FW(ctsmg_soiltemp_io, name, kind, esz, use)
+const FieldDesc SOILTEMP_TABLE[] = {
+    FT(snl, K_C, 4, U_IN), FT(nbedrock, K_C, 4, U_IN), FT(z, K_SS, 8, U_IN), FT(zi, K_ZI, 8, U_IN),
+    FT(dz, K_SS, 8, U_IN), FT(col_patchi, K_C, 4, U_IN), FT(col_npatches, K_C, 4, U_IN),
+    FT(wtcol, K_P, 8, U_IN), FT(frac_veg_nosno, K_P, 4, U_IN), FT(forc_lwrad, K_C, 8, U_IN),
+    FT(sabg, K_P, 8, U_IN), FT(sabg_soil, K_P, 8, U_IN), FT(sabg_snow, K_P, 8, U_IN),
+    FT(sabg_lyr, K_PL, 8, U_IN), FT(sabg_chk, K_P, 8, U_OUT), FT(htvp, K_C, 8, U_IN),
+    FT(cgrnd, K_P, 8, U_IN), FT(dlrad, K_P, 8, U_IN), FT(eflx_sh_grnd, K_P, 8, U_IN),
+    FT(eflx_sh_snow, K_P, 8, U_IN), FT(eflx_sh_soil, K_P, 8, U_IN), FT(eflx_sh_h2osfc, K_P, 8, U_IN),
+    FT(qflx_evap_soi, K_P, 8, U_IN), FT(qflx_ev_snow, K_P, 8, U_IN), FT(qflx_ev_soil, K_P, 8, U_IN),
+    FT(qflx_ev_h2osfc, K_P, 8, U_IN), FT(eflx_bot, K_C, 8, U_IN), FT(eflx_gnet, K_P, 8, U_OUT),
+    FT(dgnetdT, K_P, 8, U_OUT), FT(eflx_fgr12, K_C, 8, U_OUT), FT(eflx_fgr, K_G, 8, U_OUT),
+    FT(eflx_snomelt, K_C, 8, U_OUT), FT(eflx_h2osfc_to_snow, K_C, 8, U_OUT), FT(emg, K_C, 8, U_IN),
+    FT(t_soisno, K_SS, 8, U_INOUT), FT(t_h2osfc, K_C, 8, U_INOUT), FT(t_grnd, K_C, 8, U_INOUT),
+    FT(fact, K_SS, 8, U_OUT), FT(c_h2osfc, K_C, 8, U_OUT), FT(xmf, K_C, 8, U_OUT),
+    FT(xmf_h2osfc, K_C, 8, U_OUT), FT(imelt, K_SS, 4, U_OUT), FT(watsat, K_G, 8, U_IN),
+    FT(bsw, K_G, 8, U_IN), FT(sucsat, K_G, 8, U_IN), FT(tkmg, K_G, 8, U_IN), FT(tkdry, K_G, 8, U_IN),
+    FT(csol, K_G, 8, U_IN), FT(thk, K_SS, 8, U_OUT), FT(h2osoi_liq, K_SS, 8, U_INOUT),
+    FT(h2osoi_ice, K_SS, 8, U_INOUT), FT(h2osfc, K_C, 8, U_INOUT), FT(h2osno_no_layers, K_C, 8, U_INOUT),
+    FT(int_snow, K_C, 8, U_INOUT), FT(snow_depth, K_C, 8, U_INOUT), FT(snomelt_accum, K_C, 8, U_INOUT),
+    FT(frac_sno_eff, K_C, 8, U_IN), FT(frac_h2osfc, K_C, 8, U_IN), FT(bw, K_SN, 8, U_OUT),
+    FT(qflx_snomelt, K_C, 8, U_OUT), FT(qflx_snofrz, K_C, 8, U_OUT), FT(qflx_snow_drain, K_C, 8, U_OUT),
+    FT(qflx_snomelt_lyr, K_SN, 8, U_OUT), FT(qflx_snofrz_lyr, K_SN, 8, U_OUT),
+    FT(qflx_h2osfc_to_ice, K_C, 8, U_OUT),
+};
+const int SOILTEMP_NFIELDS = sizeof(SOILTEMP_TABLE) / sizeof(SOILTEMP_TABLE[0]);
+
+static inline void*& field_ptr(void* io, const FieldDesc& f) {
+    return *reinterpret_cast<void**>(reinterpret_cast<char*>(io) + f.offset);
+}
+
+size_t field_bytes(const FieldDesc& f, int ldc, int ldp) {
+    int ld = (f.kind == K_P || f.kind == K_PL) ? ldp : ldc;
+    return (size_t)ld * kind_levels(f.kind) * f.esize;
+}
+
+// Copy the host struct's arrays into the arena; fill dio with device pointers.
+static int stage_in(ThreadCtx* c, const void* hio, void* dio, size_t io_size, const FieldDesc* tab, int nf,
+                    int ldc, int ldp) {
+    std::memcpy(dio, hio, io_size);
+    for (int i = 0; i < nf; ++i) {
+        const void* hp = field_ptr(const_cast<void*>(hio), tab[i]);
+        if (!hp) {
+            std::string m = std::string("null pointer for component ") + tab[i].name;
+            return set_error(CTSMG_E_ARG, m.c_str(), 0, 0);
+        }
+        size_t nb = field_bytes(tab[i], ldc, ldp);
+        void* dp = arena_take(c, nb);
+        cudaError_t e = cudaMemcpyAsync(dp, hp, nb, cudaMemcpyHostToDevice, c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync H2D");
+        field_ptr(dio, tab[i]) = dp;
+    }
+    return 0;
+}
+
+static int stage_out(ThreadCtx* c, const void* hio, const void* dio, const FieldDesc* tab, int nf,
+                     int ldc, int ldp) {
+    for (int i = 0; i < nf; ++i) {
+        if (tab[i].use == U_IN) continue;
+        void* hp = field_ptr(const_cast<void*>(hio), tab[i]);
+        const void* dp = field_ptr(const_cast<void*>(dio), tab[i]);
+        cudaError_t e = cudaMemcpyAsync(hp, dp, field_bytes(tab[i], ldc, ldp), cudaMemcpyDeviceToHost, c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync D2H");
+    }
+    return 0;
+}
+
+static size_t table_bytes(const FieldDesc* tab, int nf, int ldc, int ldp) {
+    size_t s = 0;
+    for (int i = 0; i < nf; ++i) s += ((field_bytes(tab[i], ldc, ldp) + 255) & ~(size_t)255);
+    return s;
+}
+
+int check_filter(const ctsmg_bounds* b, int nf, const int32_t* filt) {
+    if (!b) return set_error(CTSMG_E_ARG, "null bounds", 0, 0);
+    if (b->endc < b->begc) return set_error(CTSMG_E_ARG, "endc < begc", 0, 0);
+    if (nf < 0) return set_error(CTSMG_E_ARG, "negative filter length", 0, 0);
+    if (nf > 0 && !filt) return set_error(CTSMG_E_ARG, "null filter", 0, 0);
+    for (int i = 0; i < nf; ++i)
+        if (filt[i] < b->begc || filt[i] > b->endc)
+            return set_error(CTSMG_E_ARG, "filter index outside bounds", filt[i], 0);
+    return 0;
+}
+
+static int read_error(ThreadCtx* c, int* code, int* index, int* level) {
+    DevError h;
+    cudaError_t e = cudaMemcpy(&h, c->err, sizeof h, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(err)");
+    if (h.key == ~0ull) { *code = 0; return 0; }
+    *code = (int)(h.key & 0xff);
+    *index = (int)(h.key >> 32);
+    *level = (int)((h.key >> 8) & 0xffffff) - 1024;
+    return 0;
+}
+
+} // namespace ctsmg
+
+using namespace ctsmg;
+
+// ============================================================ C-ABI
+extern "C" int32_t ctsmg_init(const ctsmg_options* opt) {
+    if (!opt) return set_error(CTSMG_E_ARG, "null options", 0, 0);
+    if (opt->nlevsno != NLEVSNO || opt->nlevsoi != NLEVSOI || opt->nlevgrnd != NLEVGRND)
+        return set_error(CTSMG_E_UNSUPPORTED, "only nlevsno=12, nlevsoi=20, nlevgrnd=25 (20SL_8.5m) are built", 0, 0);
+    if (opt->soilwater_movement_method != 0)
+        return set_error(CTSMG_E_UNSUPPORTED, "only soilwater_movement_method=0 (Zeng-Decker 2009) is built", 0, 0);
+    if (opt->snow_thermal_cond_method != 0 && opt->snow_thermal_cond_method != 1)
+        return set_error(CTSMG_E_ARG, "snow_thermal_cond_method must be 0 (Jordan1991) or 1 (Sturm1997)", 0, 0);
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev < 1) return cuda_fail(e == cudaSuccess ? cudaErrorNoDevice : e, "cudaGetDeviceCount");
+    e = cudaSetDevice(0);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_opt = *opt;
+    g_init = true;
+    return 0;
+}
+
+extern "C" int32_t ctsmg_set_soilwater_params(const ctsmg_soilwater_params* p) {
+    if (!p) return set_error(CTSMG_E_ARG, "null params", 0, 0);
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_swp = *p;
+    return 0;
+}
+
+extern "C" int32_t ctsmg_finalize(void) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    for (ThreadCtx* c : g_ctxs) delete c;
+    g_ctxs.clear();
+    t_ctx = nullptr;
+    ++g_gen;
+    g_init = false;
+    return 0;
+}
+
+extern "C" const char* ctsmg_last_error(void) { return t_msg.c_str(); }
+
+extern "C" int32_t ctsmg_last_error_index(int32_t* index, int32_t* level) {
+    if (index) *index = t_idx;
+    if (level) *level = t_lev;
+    return 0;
+}
+
+extern "C" int32_t ctsmg_soilwater(const ctsmg_bounds* bounds, int32_t num_hydrologyc,
+                                   const int32_t* filter_hydrologyc, const ctsmg_soilwater_io* io,
+                                   double dtime) {
+    ThreadCtx* c;
+    int rc = ctx_get(&c);
+    if (rc) return rc;
+    if (!io) return set_error(CTSMG_E_ARG, "null io", 0, 0);
+    if ((rc = check_filter(bounds, num_hydrologyc, filter_hydrologyc))) return rc;
+    const int ncol = bounds->endc - bounds->begc + 1;
+    if (io->ldc < ncol) return set_error(CTSMG_E_ARG, "ldc smaller than endc-begc+1", 0, 0);
+    if (!(dtime > 0.0)) return set_error(CTSMG_E_ARG, "dtime must be positive", 0, 0);
+    if (num_hydrologyc == 0) return 0;
+    const int ldc = io->ldc;
+    size_t need = table_bytes(SOILWATER_TABLE, SOILWATER_NFIELDS, ldc, 0) + (size_t)num_hydrologyc * 4 + 4096;
+    if ((rc = arena_reserve(c, need))) return rc;
+    ctsmg_soilwater_io dio;
+    if ((rc = stage_in(c, io, &dio, sizeof dio, SOILWATER_TABLE, SOILWATER_NFIELDS, ldc, 0))) return rc;
+    int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_hydrologyc * 4);
+    cudaError_t e = cudaMemcpyAsync(dfilt, filter_hydrologyc, (size_t)num_hydrologyc * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
+    double e_ice;
+    { std::lock_guard<std::mutex> lk(g_mu); e_ice = g_swp.e_ice; }
+    e = launch_soilwater(dio, bounds->begc, num_hydrologyc, dfilt, e_ice, dtime, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "soilwater kernel launch");
+    if ((rc = stage_out(c, io, &dio, SOILWATER_TABLE, SOILWATER_NFIELDS, ldc, 0))) return rc;
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "soilwater");
+    return 0;
+}
+
+extern "C" int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds, int32_t num_nolakec,
+                                         const int32_t* filter_nolakec, const ctsmg_soiltemp_io* io,
+                                         double dtime) {
+    ThreadCtx* c;
+    int rc = ctx_get(&c);
+    if (rc) return rc;
+    if (!io) return set_error(CTSMG_E_ARG, "null io", 0, 0);
+    if ((rc = check_filter(bounds, num_nolakec, filter_nolakec))) return rc;
+    const int ncol = bounds->endc - bounds->begc + 1;
+    const int npat = bounds->endp - bounds->begp + 1;
+    if (io->ldc < ncol || io->ldp < npat || npat < 0)
+        return set_error(CTSMG_E_ARG, "ldc/ldp smaller than the bounds", 0, 0);
+    if (!(dtime > 0.0)) return set_error(CTSMG_E_ARG, "dtime must be positive", 0, 0);
+    for (int i = 0; i < num_nolakec; ++i) {
+        const int cc = filter_nolakec[i] - bounds->begc;
+        const int s = io->snl[cc], pi = io->col_patchi[cc], np = io->col_npatches[cc];
+        if (s > 0 || s < -NLEVSNO) return set_error(CTSMG_E_ARG, "snl outside -nlevsno..0", filter_nolakec[i], 0);
+        if (np < 0 || pi < bounds->begp || pi + np - 1 > bounds->endp)
+            return set_error(CTSMG_E_ARG, "column patches outside begp..endp", filter_nolakec[i], 0);
+    }
+    if (num_nolakec == 0) return 0;
+    const int ldc = io->ldc, ldp = io->ldp;
+    const size_t ws_bytes = (size_t)SOILTEMP_WS_DOUBLES_PER_COL * num_nolakec * 8;
+    size_t need = table_bytes(SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp) + ws_bytes + (size_t)num_nolakec * 4 + 8192;
+    if ((rc = arena_reserve(c, need))) return rc;
+    ctsmg_soiltemp_io dio;
+    if ((rc = stage_in(c, io, &dio, sizeof dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp))) return rc;
+    int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_nolakec * 4);
+    double* ws = (double*)arena_take(c, ws_bytes);
+    cudaError_t e = cudaMemcpyAsync(dfilt, filter_nolakec, (size_t)num_nolakec * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
+    e = cudaMemsetAsync(c->err, 0xff, sizeof(DevError), c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(err)");
+    int snow_method;
+    { std::lock_guard<std::mutex> lk(g_mu); snow_method = g_opt.snow_thermal_cond_method; }
+    e = launch_soiltemp(dio, bounds->begc, bounds->begp, num_nolakec, dfilt, dtime, snow_method, ws,
+                        num_nolakec, c->err, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "soiltemperature kernel launch");
+    if ((rc = stage_out(c, io, &dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp))) return rc;
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "soiltemperature");
+    int code = 0, idx = 0, lev = 0;
+    if ((rc = read_error(c, &code, &idx, &lev))) return rc;
+    if (code) return set_error(code, "BandDiagonal ERROR: dgbsv returned error code", idx, lev);
+    return 0;
+}

@@ -1,0 +1,21 @@
+// capi_internal.h -- field tables and helpers shared by the C-ABI sources.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include "ctsm_gpu.h"
+
+namespace ctsmg {
+enum Kind { K_C, K_P, K_SS, K_ZI, K_G, K_S, K_SN, K_PL };
+enum Use { U_IN, U_OUT, U_INOUT };
+struct FieldDesc { size_t offset; int kind; int esize; int use; const char* name; };
+
+extern const FieldDesc SOILWATER_TABLE[];
+extern const int SOILWATER_NFIELDS;
+extern const FieldDesc SOILTEMP_TABLE[];
+extern const int SOILTEMP_NFIELDS;
+
+int kind_levels(int kind);
+size_t field_bytes(const FieldDesc& f, int ldc, int ldp);
+int set_error(int code, const char* what, int index, int level);
+int check_filter(const ctsmg_bounds* b, int nf, const int32_t* filt);
+} // namespace ctsmg

@@ -1,0 +1,866 @@
+// soil_kernels.cu -- sm_103a FP64 kernels for SoilWater (Zeng-Decker 2009) and
+// SoilTemperature (snow + surface water + soil + bedrock heat solve with phase
+// change).  One thread owns one column; every level array is read and written
+// level-major with consecutive columns in consecutive lanes, so each warp-wide
+// access is one coalesced 256-byte transaction.
+//
+// The banded heat system is factored with a streaming form of LAPACK dgbtf2
+// (partial pivoting, kl = ku = 2) that keeps a 3 x 5 window of the matrix in
+// registers, folds dgbtrs' forward substitution into the factorisation, and
+// stores each finished U row plus its forward-substituted right-hand side in a
+// per-column slot of a device scratch buffer (6 doubles per row, rows-major,
+// columns innermost).  The back substitution (dtbsv) then streams those rows
+// from the bottom up.  The sequence of floating-point operations on every
+// matrix and vector element is the one dgbtf2 + dgbtrs + dtbsv perform.
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "ctsm_device.cuh"
+#include "soil_kernels.cuh"
+
+namespace ctsmg {
+
+__device__ __forceinline__ double ipow4(double x) { double x2 = x * x; return x2 * x2; }
+__device__ __forceinline__ double ipow3(double x) { double x2 = x * x; return x2 * x; }
+
+// ============================================================ SoilWater (ZD09)
+// src/biogeophys/SoilWaterMovementMod.F90:414-972 for one column.
+__device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, double dtime) {
+    const int ld = io.ldc;
+    auto SS = [&](const double* p, int j) { return p[c + (size_t)(j - LS) * ld]; };
+    auto G = [&](const double* p, int j) { return p[c + (size_t)(j - 1) * ld]; };
+    auto ZI = [&](int j) { return io.zi[c + (size_t)(j + NLEVSNO) * ld]; };
+
+    constexpr int N1 = NLEVSOI + 2;
+    double zmm[N1], dzmm[N1], zimm[N1], vwc_liq[N1], zq[N1];
+    double hk[N1], dhkdw[N1], smp[N1], dsmpdw[N1], imped[N1], icef[N1];
+    double amx[N1], bmx[N1], cmx[N1], rmx[N1];
+
+    const double zwt = io.zwt[c], smpmin = io.smpmin[c];
+#pragma unroll 1
+    for (int j = 1; j <= NLEVSOI; ++j) {
+        const double dzj = SS(io.dz, j), ws = G(io.watsat, j);
+        zmm[j] = SS(io.z, j) * 1.e3;
+        dzmm[j] = dzj * 1.e3;
+        zimm[j] = ZI(j) * 1.e3;
+        double vol_ice = fmin(ws, SS(io.h2osoi_ice, j) / (dzj * DENICE));
+        icef[j] = fmin(1.0, vol_ice / ws);
+        io.icefrac[c + (size_t)(j - 1) * ld] = icef[j];
+        vwc_liq[j] = fmax(SS(io.h2osoi_liq, j), 1.0e-6) / (dzj * DENH2O);
+    }
+    zimm[0] = 0.0;
+    const double zwtmm = zwt * 1.e3;
+
+    int jwt = NLEVSOI;
+#pragma unroll 1
+    for (int j = 1; j <= NLEVSOI; ++j) {
+        if (zwt <= ZI(j)) { jwt = j - 1; break; }
+    }
+    double vwc_zwt = G(io.watsat, NLEVSOI);
+    if (SS(io.t_soisno, jwt + 1) < TFRZ) {
+        vwc_zwt = vwc_liq[NLEVSOI];
+#pragma unroll 1
+        for (int j = NLEVSOI; j <= NLEVGRND; ++j) {
+            if (zwt <= ZI(j)) {
+                const double t = SS(io.t_soisno, j);
+                double smp1 = HFUS * (TFRZ - t) / (GRAV * t) * 1000.0;
+                smp1 = fmax(G(io.sucsat, NLEVSOI), smp1);
+                vwc_zwt = G(io.watsat, NLEVSOI) * pow(smp1 / G(io.sucsat, NLEVSOI), -1.0 / G(io.bsw, NLEVSOI));
+                vwc_zwt = fmin(vwc_zwt, sp(0.5f) * (G(io.watsat, NLEVSOI) + G(io.h2osoi_vol, NLEVSOI)));
+                break;
+            }
+        }
+    }
+#pragma unroll 1
+    for (int j = 1; j <= NLEVSOI; ++j) {
+        const double ss = G(io.sucsat, j), ws = G(io.watsat, j), bb = G(io.bsw, j);
+        double veq;
+        if (zwtmm <= zimm[j - 1]) {
+            veq = ws;
+        } else if ((zwtmm < zimm[j]) && (zwtmm > zimm[j - 1])) {
+            double tempi = 1.0;
+            double temp0 = pow(((ss + zwtmm - zimm[j - 1]) / ss), 1.0 - 1.0 / bb);
+            double voleq1 = -ss * ws / (1.0 - 1.0 / bb) / (zwtmm - zimm[j - 1]) * (tempi - temp0);
+            veq = (voleq1 * (zwtmm - zimm[j - 1]) + ws * (zimm[j] - zwtmm)) / (zimm[j] - zimm[j - 1]);
+            veq = fmin(ws, veq);
+            veq = fmax(veq, 0.0);
+        } else {
+            double tempi = pow(((ss + zwtmm - zimm[j]) / ss), 1.0 - 1.0 / bb);
+            double temp0 = pow(((ss + zwtmm - zimm[j - 1]) / ss), 1.0 - 1.0 / bb);
+            veq = -ss * ws / (1.0 - 1.0 / bb) / (zimm[j] - zimm[j - 1]) * (tempi - temp0);
+            veq = fmax(veq, 0.0);
+            veq = fmin(ws, veq);
+        }
+        double q = -ss * pow(fmax(veq / ws, 0.01), -bb);
+        zq[j] = fmax(smpmin, q);
+    }
+    if (jwt == NLEVSOI) {
+        const int j = NLEVSOI;
+        const double ss = G(io.sucsat, j), ws = G(io.watsat, j), bb = G(io.bsw, j);
+        double tempi = 1.0;
+        double temp0 = pow(((ss + zwtmm - zimm[j]) / ss), 1.0 - 1.0 / bb);
+        double veq = -ss * ws / (1.0 - 1.0 / bb) / (zwtmm - zimm[j]) * (tempi - temp0);
+        veq = fmax(veq, 0.0);
+        veq = fmin(ws, veq);
+        double q = -ss * pow(fmax(veq / ws, 0.01), -bb);
+        zq[j + 1] = fmax(smpmin, q);
+    }
+#pragma unroll 1
+    for (int j = 1; j <= NLEVSOI; ++j) {
+        const int jp = min(NLEVSOI, j + 1);
+        const double wsj = G(io.watsat, j), wsp = G(io.watsat, jp), bb = G(io.bsw, j);
+        double s1 = 0.5 * (vwc_liq[j] + vwc_liq[jp]) / (0.5 * (wsj + wsp));
+        s1 = fmin(1.0, s1);
+        double s2 = G(io.hksat, j) * pow(s1, 2.0 * bb + 2.0);
+        imped[j] = pow(10.0, -e_ice * (0.5 * (icef[j] + icef[jp])));
+        hk[j] = imped[j] * s1 * s2;
+        dhkdw[j] = imped[j] * (2.0 * bb + 3.0) * s2 * (1.0 / (wsj + wsp));
+        double s_node = fmax(vwc_liq[j] / wsj, 0.01);
+        s_node = fmin(1.0, s_node);
+        double sm = -G(io.sucsat, j) * pow(s_node, -bb);
+        sm = fmax(smpmin, sm);
+        smp[j] = sm;
+        dsmpdw[j] = -bb * sm / vwc_liq[j];
+        io.smp_l[c + (size_t)(j - 1) * ld] = sm;
+        io.hk_l[c + (size_t)(j - 1) * ld] = hk[j];
+    }
+    zmm[NLEVSOI + 1] = sp(0.5f) * (1.e3 * zwt + zmm[NLEVSOI]);
+    dzmm[NLEVSOI + 1] = (jwt < NLEVSOI) ? dzmm[NLEVSOI] : (1.e3 * zwt - zmm[NLEVSOI]);
+
+    auto ROOT = [&](int j) { return io.qflx_rootsoi[c + (size_t)(j - 1) * ld]; };
+    auto setq = [&](int j, double qi, double qo) {
+        io.qin[c + (size_t)(j - 1) * ld] = qi;
+        io.qout[c + (size_t)(j - 1) * ld] = qo;
+    };
+    {   // top node
+        const int j = 1;
+        double qin = io.qflx_infl[c];
+        double den = (zmm[j + 1] - zmm[j]);
+        double dzq = (zq[j + 1] - zq[j]);
+        double num = (smp[j + 1] - smp[j]) - dzq;
+        double qout = -hk[j] * num / den;
+        double dqodw1 = -(-hk[j] * dsmpdw[j] + num * dhkdw[j]) / den;
+        double dqodw2 = -(hk[j] * dsmpdw[j + 1] + num * dhkdw[j]) / den;
+        rmx[j] = qin - qout - ROOT(j);
+        amx[j] = 0.0;
+        bmx[j] = dzmm[j] * (0.0 + 1.0 / dtime) + dqodw1;
+        cmx[j] = dqodw2;
+        setq(j, qin, qout);
+    }
+#pragma unroll 1
+    for (int j = 2; j <= NLEVSOI - 1; ++j) {
+        double den = (zmm[j] - zmm[j - 1]);
+        double dzq = (zq[j] - zq[j - 1]);
+        double num = (smp[j] - smp[j - 1]) - dzq;
+        double qin = -hk[j - 1] * num / den;
+        double dqidw0 = -(-hk[j - 1] * dsmpdw[j - 1] + num * dhkdw[j - 1]) / den;
+        double dqidw1 = -(hk[j - 1] * dsmpdw[j] + num * dhkdw[j - 1]) / den;
+        den = (zmm[j + 1] - zmm[j]);
+        dzq = (zq[j + 1] - zq[j]);
+        num = (smp[j + 1] - smp[j]) - dzq;
+        double qout = -hk[j] * num / den;
+        double dqodw1 = -(-hk[j] * dsmpdw[j] + num * dhkdw[j]) / den;
+        double dqodw2 = -(hk[j] * dsmpdw[j + 1] + num * dhkdw[j]) / den;
+        rmx[j] = qin - qout - ROOT(j);
+        amx[j] = -dqidw0;
+        bmx[j] = dzmm[j] / dtime - dqidw1 + dqodw1;
+        cmx[j] = dqodw2;
+        setq(j, qin, qout);
+    }
+    {   // bottom node and aquifer layer
+        const int j = NLEVSOI;
+        double den = (zmm[j] - zmm[j - 1]);
+        double dzq = (zq[j] - zq[j - 1]);
+        double num = (smp[j] - smp[j - 1]) - dzq;
+        double qin = -hk[j - 1] * num / den;
+        double dqidw0 = -(-hk[j - 1] * dsmpdw[j - 1] + num * dhkdw[j - 1]) / den;
+        double dqidw1 = -(hk[j - 1] * dsmpdw[j] + num * dhkdw[j - 1]) / den;
+        if (j > jwt) {
+            rmx[j] = qin - 0.0 - ROOT(j);
+            amx[j] = -dqidw0;
+            bmx[j] = dzmm[j] / dtime - dqidw1 + 0.0;
+            cmx[j] = 0.0;
+            setq(j, qin, 0.0);
+            rmx[j + 1] = 0.0;
+            amx[j + 1] = 0.0;
+            bmx[j + 1] = dzmm[j + 1] / dtime;
+            cmx[j + 1] = 0.0;
+        } else {
+            const double ws = G(io.watsat, j), bb = G(io.bsw, j);
+            double s_node = fmax(sp(0.5f) * ((vwc_zwt + vwc_liq[j]) / ws), 0.01);
+            s_node = fmin(1.0, s_node);
+            double smp1 = -G(io.sucsat, j) * pow(s_node, -bb);
+            smp1 = fmax(smpmin, smp1);
+            double dsmpdw1 = -bb * smp1 / (s_node * ws);
+            den = (zmm[j + 1] - zmm[j]);
+            dzq = (zq[j + 1] - zq[j]);
+            num = (smp1 - smp[j]) - dzq;
+            double qout = -hk[j] * num / den;
+            double dqodw1 = -(-hk[j] * dsmpdw[j] + num * dhkdw[j]) / den;
+            double dqodw2 = -(hk[j] * dsmpdw1 + num * dhkdw[j]) / den;
+            rmx[j] = qin - qout - ROOT(j);
+            amx[j] = -dqidw0;
+            bmx[j] = dzmm[j] / dtime - dqidw1 + dqodw1;
+            cmx[j] = dqodw2;
+            double dqidw0a = -(-hk[j] * dsmpdw[j] + num * dhkdw[j]) / den;
+            double dqidw1a = -(hk[j] * dsmpdw1 + num * dhkdw[j]) / den;
+            rmx[j + 1] = qout - 0.0;
+            amx[j + 1] = -dqidw0a;
+            bmx[j + 1] = dzmm[j + 1] / dtime - dqidw1a + 0.0;
+            cmx[j + 1] = 0.0;
+            setq(j, qin, qout);
+        }
+    }
+    // Tridiagonal (TridiagonalMod.F90:60-89), jtop = 1, levels 1..nlevsoi+1;
+    // gam overwrites amx, the solution overwrites rmx
+    {
+        double bet = bmx[1];
+        rmx[1] = rmx[1] / bet;
+#pragma unroll 1
+        for (int j = 2; j <= NLEVSOI + 1; ++j) {
+            double gam = cmx[j - 1] / bet;
+            bet = bmx[j] - amx[j] * gam;
+            rmx[j] = (rmx[j] - amx[j] * rmx[j - 1]) / bet;
+            amx[j] = gam;
+        }
+#pragma unroll 1
+        for (int j = NLEVSOI; j >= 1; --j) rmx[j] = rmx[j] - amx[j + 1] * rmx[j + 1];
+    }
+    const double* dwat2 = rmx;
+    double deficit = 0.0;
+#pragma unroll 1
+    for (int j = 1; j <= NLEVSOI; ++j) {
+        double& liq = io.h2osoi_liq[c + (size_t)(j - LS) * ld];
+        double v = liq + dwat2[j] * dzmm[j];
+        liq = v;
+        if (v < 0.0) deficit = deficit - v;
+    }
+    double qcharge;
+    if (jwt < NLEVSOI) {
+        const int jq = jwt + 1;
+        double s_node = fmax(G(io.h2osoi_vol, jq) / G(io.watsat, jq), 0.01);
+        double s1 = fmin(1.0, s_node);
+        double ka = imped[jq] * G(io.hksat, jq) * pow(s1, 2.0 * G(io.bsw, jq) + 3.0);
+        const int jm = max(1, jwt);
+        double smp1 = fmax(smpmin, smp[jm]);
+        double wh = smp1 - zq[jm];
+        if (jwt == 0) qcharge = -ka * (0.0 - wh) / ((zwt + sp(1.e-3f)) * 1000.0);
+        else qcharge = -ka * (0.0 - wh) / ((zwt - SS(io.z, jwt)) * 1000.0 * sp(2.0f));
+        qcharge = fmax(-10.0 / dtime, qcharge);
+        qcharge = fmin(10.0 / dtime, qcharge);
+    } else {
+        qcharge = dwat2[NLEVSOI + 1] * dzmm[NLEVSOI + 1] / dtime;
+    }
+    io.qcharge[c] = qcharge;
+    io.qflx_deficit[c] = deficit;
+}
+
+// ============================================================ SoilTemperature
+// Scratch slot of one column: row i (1-based, i = 1..n) occupies 6 doubles
+// U(i,i..i+4), y(i) at ws[((i-1)*6 + k) * ws_ld + slot].
+struct Scratch {
+    double* ws; int ld; int slot;
+    __device__ __forceinline__ double& at(int i, int k) const {
+        return ws[((size_t)(i - 1) * 6 + k) * ld + slot];
+    }
+};
+
+// src/biogeophys/SoilTemperatureMod.F90:92-508 (and the routines it calls) for
+// one natural-vegetation column.  Returns the dgbsv info (0 = success).
+__device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, double dtime,
+                               int snow_method, const Scratch& S) {
+    const int ld = io.ldc;
+    auto ssi = [&](int j) { return c + (size_t)(j - LS) * ld; };
+    auto gi = [&](int j) { return c + (size_t)(j - 1) * ld; };
+    auto Z = [&](int j) { return io.z[ssi(j)]; };
+    auto ZI = [&](int j) { return io.zi[c + (size_t)(j + NLEVSNO) * ld]; };
+    auto DZ = [&](int j) { return io.dz[ssi(j)]; };
+    double* __restrict__ T = io.t_soisno;
+    double* __restrict__ LIQ = io.h2osoi_liq;
+    double* __restrict__ ICE = io.h2osoi_ice;
+
+    const int snl = io.snl[c];
+    const int nbedrock = io.nbedrock[c];
+    const double frac_sno = io.frac_sno_eff[c];
+    const double frac_h2osfc = io.frac_h2osfc[c];
+    const double emg = io.emg[c];
+
+    constexpr int NL = NLEVSNO + NLEVGRND + 2;
+    auto L = [](int j) { return j + NLEVSNO; };
+    double tk[NL], fact[NL], fn[NL];
+
+    // ---------------- SoilThermProp (:664-896): thk, tk, cv -> fact
+    double thk_prev = 0.0;
+    double cvv[NL];
+#pragma unroll 1
+    for (int j = snl + 1; j <= NLEVGRND; ++j) {
+        double t;
+        if (j >= 1) {
+            const double liq = LIQ[ssi(j)], ice = ICE[ssi(j)], dzj = DZ(j), ws = io.watsat[gi(j)];
+            double satw = (liq / DENH2O + ice / DENICE + 0.0 / DENICE) / (dzj * ws);
+            satw = fmin(1.0, satw);
+            if (satw > .1e-6) {
+                double dke = (T[ssi(j)] >= TFRZ) ? fmax(0.0, log10(satw) + 1.0) : satw;
+                double fl = (liq / (DENH2O * dzj)) / (liq / (DENH2O * dzj) + ice / (DENICE * dzj) + 0.0 / (DENICE * dzj));
+                double dksat = io.tkmg[gi(j)] * pow(TKWAT, fl * ws) * pow(TKICE, (1.0 - fl) * ws);
+                t = dke * dksat + (1.0 - dke) * io.tkdry[gi(j)];
+            } else {
+                t = io.tkdry[gi(j)];
+            }
+            if (j > nbedrock) t = THK_BEDROCK;
+            double cv = io.csol[gi(j)] * (1.0 - ws) * dzj + (ice * CPICE + liq * CPLIQ) + 0.0 * CPICE;
+            if (j > nbedrock) cv = CSOL_BEDROCK * dzj;
+            if (j == 1 && io.h2osno_no_layers[c] > 0.0) cv = cv + CPICE * io.h2osno_no_layers[c];
+            cvv[L(j)] = cv;
+        } else {
+            const double liq = LIQ[ssi(j)], ice = ICE[ssi(j)];
+            double b = (ice + liq) / (frac_sno * DZ(j));
+            io.bw[ssi(j)] = b;
+            if (snow_method == 0) {
+                t = TKAIR + (7.75e-5 * b + 1.105e-6 * b * b) * (TKICE - TKAIR);
+            } else {
+                if (b <= 156) t = sp(0.023f) + sp(0.234f) * (b / 1000);
+                else t = sp(0.138f) - sp(1.01f) * (b / 1000) + (sp(3.233f) * ((b / 1000) * (b / 1000)));
+            }
+            cvv[L(j)] = (frac_sno > 0.0) ? fmax(THIN_SFCLAYER, (CPLIQ * liq + CPICE * ice) / frac_sno) : THIN_SFCLAYER;
+        }
+        io.thk[ssi(j)] = t;
+        if (j > snl + 1) {
+            const int jm = j - 1;
+            tk[L(jm)] = thk_prev * t * (Z(j) - Z(jm)) / (thk_prev * (Z(j) - ZI(jm)) + t * (ZI(jm) - Z(jm)));
+        }
+        thk_prev = t;
+    }
+    tk[L(NLEVGRND)] = 0.0;
+    const double thk1 = io.thk[ssi(1)];
+    const double z1 = Z(1);
+    double tk_h2osfc;
+    {
+        double zh2osfc = sp(1.0e-3f) * (sp(0.5f) * io.h2osfc[c]);
+        tk_h2osfc = TKWAT * thk1 * (z1 + zh2osfc) / (TKWAT * z1 + thk1 * zh2osfc);
+    }
+
+    // ---------------- ComputeGroundHeatFluxAndDeriv (:1655-1792)
+    const double t_grnd = io.t_grnd[c];
+    const double t_top0 = T[ssi(snl + 1)], t_soi1 = T[ssi(1)], t_h2osfc0 = io.t_h2osfc[c];
+    const double lwrad_emit = emg * SB * ipow4(t_grnd);
+    const double dlwrad_emit = 4.0 * emg * SB * ipow3(t_grnd);
+    const double lwrad_emit_snow = emg * SB * ipow4(t_top0);
+    const double lwrad_emit_soil = emg * SB * ipow4(t_soi1);
+    const double lwrad_emit_h2osfc = emg * SB * ipow4(t_h2osfc0);
+    const int p0 = io.col_patchi[c] - begp, np = io.col_npatches[c];
+    const double forc_lwrad = io.forc_lwrad[c], htvp = io.htvp[c];
+    const int lyr_top = snl + 1;
+    double hs_soil = 0.0, hs_h2osfc = 0.0, dhsdT = 0.0, hs_top_snow = 0.0;
+#pragma unroll 1
+    for (int p = p0; p < p0 + np; ++p) {
+        const double fv = (double)io.frac_veg_nosno[p];
+        const double dl = io.dlrad[p], lw = (1.0 - fv) * emg * forc_lwrad;
+        double gnet = io.sabg[p] + dl + lw - lwrad_emit - (io.eflx_sh_grnd[p] + io.qflx_evap_soi[p] * htvp);
+        io.eflx_gnet[p] = gnet;
+        io.sabg_chk[p] = frac_sno * io.sabg_snow[p] + (1.0 - frac_sno) * io.sabg_soil[p];
+        double gsoil = io.sabg_soil[p] + dl + lw - lwrad_emit_soil - (io.eflx_sh_soil[p] + io.qflx_ev_soil[p] * htvp);
+        double gh2o = io.sabg_soil[p] + dl + lw - lwrad_emit_h2osfc - (io.eflx_sh_h2osfc[p] + io.qflx_ev_h2osfc[p] * htvp);
+        double dg = -io.cgrnd[p] - dlwrad_emit;
+        io.dgnetdT[p] = dg;
+        const double w = io.wtcol[p];
+        dhsdT = dhsdT + dg * w;
+        hs_soil = hs_soil + gsoil * w;
+        hs_h2osfc = hs_h2osfc + gh2o * w;
+    }
+#pragma unroll 1
+    for (int p = p0; p < p0 + np; ++p) {
+        const double fv = (double)io.frac_veg_nosno[p];
+        const double w = io.wtcol[p];
+        const double* sl = io.sabg_lyr;
+        const size_t ldp = io.ldp;
+        double stop = sl[p + (size_t)(lyr_top - LS) * ldp];
+        double gsnow = stop + io.dlrad[p] + (1.0 - fv) * emg * forc_lwrad - lwrad_emit_snow -
+                       (io.eflx_sh_snow[p] + io.qflx_ev_snow[p] * htvp);
+        hs_top_snow = hs_top_snow + gsnow * w;
+    }
+    // sabg_lyr_col for levels lyr_top..1 is summed per level over patches when
+    // the RHS needs it (same order of summation as the reference's patch loop)
+    auto sabg_lyr_col = [&](int j) {
+        double s = 0.0;
+        for (int p = p0; p < p0 + np; ++p)
+            s = s + io.sabg_lyr[p + (size_t)(j - LS) * io.ldp] * io.wtcol[p];
+        return s;
+    };
+
+    // ---------------- ComputeHeatDiffFluxAndFactor (:1876-1906)
+#pragma unroll 1
+    for (int j = snl + 1; j <= NLEVGRND; ++j) {
+        double f, flux;
+        if (j == snl + 1) {
+            f = dtime / cvv[L(j)] * DZ(j) / (0.5 * (Z(j) - ZI(j - 1) + CAPR * (Z(j + 1) - ZI(j - 1))));
+            flux = tk[L(j)] * (T[ssi(j + 1)] - T[ssi(j)]) / (Z(j + 1) - Z(j));
+        } else if (j <= NLEVGRND - 1) {
+            f = dtime / cvv[L(j)];
+            flux = tk[L(j)] * (T[ssi(j + 1)] - T[ssi(j)]) / (Z(j + 1) - Z(j));
+        } else {
+            f = dtime / cvv[L(j)];
+            flux = io.eflx_bot[c];
+        }
+        fact[L(j)] = f;
+        fn[L(j)] = flux;
+        io.fact[ssi(j)] = f;
+    }
+    double c_h2osfc, dz_h2osfc;
+    if ((io.h2osfc[c] > THIN_SFCLAYER) && (frac_h2osfc > THIN_SFCLAYER)) {
+        c_h2osfc = fmax(THIN_SFCLAYER, CPLIQ * io.h2osfc[c] / frac_h2osfc);
+        dz_h2osfc = fmax(THIN_SFCLAYER, sp(1.0e-3f) * io.h2osfc[c] / frac_h2osfc);
+    } else {
+        c_h2osfc = THIN_SFCLAYER;
+        dz_h2osfc = THIN_SFCLAYER;
+    }
+    io.c_h2osfc[c] = c_h2osfc;
+    const double dzm_ssw = (sp(0.5f) * dz_h2osfc + z1);
+    const double fn_h2osfc = tk_h2osfc * (t_soi1 - t_h2osfc0) / dzm_ssw;
+
+    // ---------------- matrix row + RHS generator (SetRHSVec* :1913-2353,
+    // SetMatrix* :2356-2926).  Row r: -nlevsno..nlevgrnd; returns the five
+    // bands B(1..5, r) (band k couples row r to row r + 3 - k) and rhs(r).
+    auto make_row = [&](int r, double* bnd, double& rhs) {
+        bnd[0] = bnd[1] = bnd[2] = bnd[3] = bnd[4] = 0.0;
+        if (r < 0) {                                   // snow layer j = r + 1
+            const int j = r + 1;
+            const double dzp = Z(j + 1) - Z(j);
+            const double fj = fact[L(j)], tj = T[ssi(j)];
+            if (j == snl + 1) {
+                bnd[2] = 1.0 + (1.0 - CNFAC) * fj * tk[L(j)] / dzp - fj * dhsdT;
+                rhs = tj + fj * (hs_top_snow - dhsdT * tj + CNFAC * fn[L(j)]);
+            } else {
+                const double dzm = (Z(j) - Z(j - 1));
+                bnd[3] = -(1.0 - CNFAC) * fj * tk[L(j - 1)] / dzm;
+                bnd[2] = 1.0 + (1.0 - CNFAC) * fj * (tk[L(j)] / dzp + tk[L(j - 1)] / dzm);
+                double rr = tj + CNFAC * fj * (fn[L(j)] - fn[L(j - 1)]);
+                rhs = rr + fj * sabg_lyr_col(j);
+            }
+            if (j != 0) bnd[1] = -(1.0 - CNFAC) * fj * tk[L(j)] / dzp;
+            else bnd[0] = -(1.0 - CNFAC) * fj * tk[L(j)] / dzp;
+        } else if (r == 0) {                           // standing surface water
+            bnd[2] = 1.0 + (1.0 - CNFAC) * (dtime / c_h2osfc) * tk_h2osfc / dzm_ssw - (dtime / c_h2osfc) * dhsdT;
+            bnd[1] = -(1.0 - CNFAC) * (dtime / c_h2osfc) * tk_h2osfc / dzm_ssw;
+            rhs = t_h2osfc0 + (dtime / c_h2osfc) * (hs_h2osfc - dhsdT * t_h2osfc0 + CNFAC * fn_h2osfc);
+        } else {                                       // soil / bedrock layer j = r
+            const int j = r;
+            const double fj = fact[L(j)], tj = T[ssi(j)];
+            if (j == snl + 1) {
+                const double dzp = Z(j + 1) - Z(j);
+                bnd[2] = 1.0 + (1.0 - CNFAC) * fj * tk[L(j)] / dzp - fj * dhsdT;
+                bnd[1] = -(1.0 - CNFAC) * fj * tk[L(j)] / dzp;
+                rhs = tj + fj * (hs_top_snow - dhsdT * tj + CNFAC * fn[L(j)]);
+            } else if (j == 1) {
+                const double dzm = (Z(j) - Z(j - 1));
+                const double dzp = (Z(j + 1) - Z(j));
+                bnd[1] = -(1.0 - CNFAC) * fj * tk[L(j)] / dzp;
+                bnd[2] = 1.0 + (1.0 - CNFAC) * fj * (tk[L(j)] / dzp + frac_sno * tk[L(j - 1)] / dzm) -
+                         (1.0 - frac_sno) * fj * dhsdT;
+                bnd[4] = -frac_sno * (1.0 - CNFAC) * fj * tk[L(j - 1)] / dzm;
+                double rr = tj + fj * ((1.0 - frac_sno) * (hs_soil - dhsdT * tj) + CNFAC * (fn[L(j)] - frac_sno * fn[L(j - 1)]));
+                rhs = rr + frac_sno * fj * sabg_lyr_col(j);
+            } else if (j <= NLEVGRND - 1) {
+                const double dzm = (Z(j) - Z(j - 1));
+                const double dzp = (Z(j + 1) - Z(j));
+                bnd[1] = -(1.0 - CNFAC) * fj * tk[L(j)] / dzp;
+                bnd[2] = 1.0 + (1.0 - CNFAC) * fj * (tk[L(j)] / dzp + tk[L(j - 1)] / dzm);
+                bnd[3] = -(1.0 - CNFAC) * fj * tk[L(j - 1)] / dzm;
+                rhs = tj + CNFAC * fj * (fn[L(j)] - fn[L(j - 1)]);
+            } else {
+                const double dzm = (Z(j) - Z(j - 1));
+                bnd[2] = 1.0 + (1.0 - CNFAC) * fj * tk[L(j - 1)] / dzm;
+                bnd[3] = -(1.0 - CNFAC) * fj * tk[L(j - 1)] / dzm;
+                rhs = tj - CNFAC * fj * fn[L(j - 1)] + fj * fn[L(j)];
+            }
+            if (j == 1 && frac_h2osfc != 0.0) {
+                bnd[2] = bnd[2] + frac_h2osfc * ((1.0 - CNFAC) * fj * tk_h2osfc / dzm_ssw + fj * dhsdT);
+                bnd[3] = -frac_h2osfc * (1.0 - CNFAC) * fj * tk_h2osfc / dzm_ssw;
+                rhs = rhs - frac_h2osfc * fj * ((hs_soil - dhsdT * tj) + CNFAC * fn_h2osfc);
+            }
+        }
+    };
+
+    // ---------------- banded LU with partial pivoting + forward substitution
+    const int jtop = snl, n = NLEVGRND - jtop + 1;
+    // window W[a][b] = A(j+a, j+b), a = 0..2, b = 0..4;  rhs window y[a] = b(j+a)
+    double W[3][5], y[3];
+    {
+        double bnd[5], rr;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            make_row(jtop + a, bnd, rr);
+            // row i = 1 + a: A(i, i-2..i+2) = bands 5,4,3,2,1 ; window col b = i + (b - a) - 1
+#pragma unroll
+            for (int b = 0; b < 5; ++b) {
+                const int off = b - a;            // column offset from the row's diagonal
+                W[a][b] = (off >= -2 && off <= 2) ? bnd[2 - off] : 0.0;
+            }
+            y[a] = rr;
+        }
+    }
+    int info = 0;
+#pragma unroll 1
+    for (int j = 1; j <= n; ++j) {
+        const int km = min(2, n - j);
+        int jp = 0;
+        double dmax = fabs(W[0][0]);
+        if (km >= 1 && fabs(W[1][0]) > dmax) { jp = 1; dmax = fabs(W[1][0]); }
+        if (km >= 2 && fabs(W[2][0]) > dmax) { jp = 2; }
+        if (jp == 1) {
+#pragma unroll
+            for (int b = 0; b < 5; ++b) { double t = W[0][b]; W[0][b] = W[1][b]; W[1][b] = t; }
+            double t = y[0]; y[0] = y[1]; y[1] = t;
+        } else if (jp == 2) {
+#pragma unroll
+            for (int b = 0; b < 5; ++b) { double t = W[0][b]; W[0][b] = W[2][b]; W[2][b] = t; }
+            double t = y[0]; y[0] = y[2]; y[2] = t;
+        }
+        if (W[0][0] != 0.0) {
+            if (km > 0) {
+                const double rp = 1.0 / W[0][0];
+                W[1][0] = W[1][0] * rp;
+                if (km > 1) W[2][0] = W[2][0] * rp;
+#pragma unroll
+                for (int b = 1; b < 5; ++b) {
+                    const double yk = W[0][b];
+                    if (yk != 0.0) {
+                        const double temp = -1.0 * yk;
+                        W[1][b] = W[1][b] + W[1][0] * temp;
+                        if (km > 1) W[2][b] = W[2][b] + W[2][0] * temp;
+                    }
+                }
+            }
+        } else if (info == 0) {
+            info = j;
+        }
+        // dgbtrs forward step j (no-op for j = n)
+        if (j < n && y[0] != 0.0) {
+            const double temp = -1.0 * y[0];
+            y[1] = y[1] + W[1][0] * temp;
+            if (km > 1) y[2] = y[2] + W[2][0] * temp;
+        }
+        // finished row j -> scratch
+#pragma unroll
+        for (int b = 0; b < 5; ++b) S.at(j, b) = W[0][b];
+        S.at(j, 5) = y[0];
+        // shift the window down one row / right one column
+#pragma unroll
+        for (int b = 0; b < 4; ++b) { W[0][b] = W[1][b + 1]; W[1][b] = W[2][b + 1]; }
+        W[0][4] = 0.0; W[1][4] = 0.0;
+        y[0] = y[1]; y[1] = y[2];
+        if (j + 3 <= n) {
+            double bnd[5], rr;
+            make_row(jtop + j + 2, bnd, rr);
+            // row j+3 in window cols j+1..j+5: offsets -2..+2
+            W[2][0] = bnd[4]; W[2][1] = bnd[3]; W[2][2] = bnd[2];
+            W[2][3] = (j + 4 <= n) ? bnd[1] : 0.0;
+            W[2][4] = (j + 5 <= n) ? bnd[0] : 0.0;
+            y[2] = rr;
+        } else {
+#pragma unroll
+            for (int b = 0; b < 5; ++b) W[2][b] = 0.0;
+            y[2] = 0.0;
+        }
+    }
+    if (info != 0) return info;
+
+    // ---------------- dtbsv: back substitution, x(i) overwrites y(i)
+    // window x[k] = x(j - k), k = 0..4 (x(j) final once divided)
+    double x[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) x[k] = (n - k >= 1) ? S.at(n - k, 5) : 0.0;
+#pragma unroll 1
+    for (int j = n; j >= 1; --j) {
+        if (x[0] != 0.0) {
+            x[0] = x[0] / S.at(j, 0);
+            const double temp = x[0];
+#pragma unroll
+            for (int k = 1; k <= 4; ++k)
+                if (j - k >= 1) x[k] = x[k] - temp * S.at(j - k, k);   // U(j-k, j)
+        }
+        S.at(j, 5) = x[0];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) x[k] = x[k + 1];
+        x[4] = (j - 5 >= 1) ? S.at(j - 5, 5) : 0.0;
+    }
+    auto TV = [&](int r) { return S.at(r - jtop + 1, 5); };
+
+    // unpack (:422-434) and fn1 (:438-483) -- fn1 needs the new temperatures
+#pragma unroll 1
+    for (int j = snl + 1; j <= NLEVGRND; ++j) T[ssi(j)] = TV(j <= 0 ? j - 1 : j);
+    double t_h2osfc = (frac_h2osfc == 0.0) ? T[ssi(1)] : TV(0);
+    io.t_h2osfc[c] = t_h2osfc;
+    const double fn1_1 = tk[L(1)] * (T[ssi(2)] - T[ssi(1)]) / (Z(2) - Z(1));
+    io.eflx_fgr12[c] = -CNFAC * fn[L(1)] - (1.0 - CNFAC) * fn1_1;
+#pragma unroll 1
+    for (int j = 1; j <= NLEVGRND; ++j) {
+        double v;
+        if (j < NLEVGRND) {
+            double fn1 = tk[L(j)] * (T[ssi(j + 1)] - T[ssi(j)]) / (Z(j + 1) - Z(j));
+            v = -CNFAC * fn[L(j)] - (1.0 - CNFAC) * fn1;
+        } else {
+            v = 0.0;
+        }
+        io.eflx_fgr[gi(j)] = v;
+    }
+
+    // ---------------- PhaseChangeH2osfc (:960-1127)
+    io.xmf_h2osfc[c] = 0.0;
+    io.qflx_h2osfc_to_ice[c] = 0.0;
+    io.eflx_h2osfc_to_snow[c] = 0.0;
+    if (frac_h2osfc > 0.0 && t_h2osfc <= TFRZ) {
+        double h2osno_total = io.h2osno_no_layers[c];
+        for (int j = snl + 1; j <= 0; ++j) h2osno_total = h2osno_total + ICE[ssi(j)] + LIQ[ssi(j)];
+        double h2osfc = io.h2osfc[c];
+        double tinc = TFRZ - t_h2osfc;
+        t_h2osfc = TFRZ;
+        double hm = frac_h2osfc * (dhsdT * tinc - tinc * c_h2osfc / dtime);
+        double xm = hm * dtime / HFUS;
+        double temp1 = h2osfc + xm;
+        double z_avg = frac_sno * io.snow_depth[c];
+        double rho_avg = (z_avg > 0.0) ? fmin(800.0, h2osno_total / z_avg) : 200.0;
+        const double fact0 = fact[L(0)];
+        if (temp1 >= 0.0) {
+            io.int_snow[c] = io.int_snow[c] - xm;
+            if (snl == 0) io.h2osno_no_layers[c] = io.h2osno_no_layers[c] - xm;
+            else ICE[ssi(0)] = ICE[ssi(0)] - xm;
+            h2osno_total = h2osno_total - xm;
+            io.h2osfc[c] = h2osfc + xm;
+            io.xmf_h2osfc[c] = hm;
+            io.qflx_h2osfc_to_ice[c] = -xm / dtime;
+            if (frac_sno > 0 && snl < 0) io.snow_depth[c] = h2osno_total / (rho_avg * frac_sno);
+            else io.snow_depth[c] = h2osno_total / DENICE;
+            if (snl == 0) {
+                T[ssi(0)] = t_h2osfc;
+                io.eflx_h2osfc_to_snow[c] = 0.;
+            } else {
+                double c1 = (snl == -1) ? frac_sno * (dtime / fact0 - dhsdT * dtime) : frac_sno / fact0 * dtime;
+                double c2 = (frac_h2osfc != 0.0) ? (-CPLIQ * xm - frac_h2osfc * dhsdT * dtime) : 0.0;
+                double t0 = (c1 * T[ssi(0)] + c2 * t_h2osfc) / (c1 + c2);
+                T[ssi(0)] = t0;
+                io.eflx_h2osfc_to_snow[c] = (t_h2osfc - t0) * c2 / dtime;
+            }
+        } else {
+            rho_avg = (h2osno_total * rho_avg + h2osfc * DENICE) / (h2osno_total + h2osfc);
+            io.int_snow[c] = io.int_snow[c] + h2osfc;
+            if (snl == 0) io.h2osno_no_layers[c] = io.h2osno_no_layers[c] + h2osfc;
+            else ICE[ssi(0)] = ICE[ssi(0)] + h2osfc;
+            h2osno_total = h2osno_total + h2osfc;
+            io.qflx_h2osfc_to_ice[c] = h2osfc / dtime;
+            t_h2osfc = t_h2osfc - temp1 * HFUS / (dtime * dhsdT - c_h2osfc);
+            io.xmf_h2osfc[c] = (hm - frac_h2osfc * temp1 * HFUS / dtime);
+            if (snl == 0) {
+                T[ssi(0)] = t_h2osfc;
+            } else {
+                double c1 = (snl == -1) ? frac_sno * (dtime / fact0 - dhsdT * dtime) : frac_sno / fact0 * dtime;
+                double c2 = (frac_h2osfc != 0.0) ? frac_h2osfc * (c_h2osfc - dtime * dhsdT) : 0.0;
+                double t0 = (c1 * T[ssi(0)] + c2 * t_h2osfc) / (c1 + c2);
+                T[ssi(0)] = t0;
+                t_h2osfc = t0;
+            }
+            io.h2osfc[c] = 0.0;
+            if (frac_sno > 0 && snl < 0) io.snow_depth[c] = h2osno_total / (rho_avg * frac_sno);
+            else io.snow_depth[c] = h2osno_total / DENICE;
+        }
+        io.t_h2osfc[c] = t_h2osfc;
+    }
+
+    // ---------------- Phasechange (:1214-1527), one level at a time: the
+    // identification, energy and mass updates of level j only read level j.
+    double xmf = 0.0, qflx_snomelt = 0.0, qflx_snofrz = 0.0, qflx_snow_drain = 0.0;
+#pragma unroll 1
+    for (int j = LS; j <= 0; ++j) {
+        io.qflx_snomelt_lyr[ssi(j)] = 0.0;
+        io.qflx_snofrz_lyr[ssi(j)] = 0.0;
+    }
+#pragma unroll 1
+    for (int j = snl + 1; j <= NLEVGRND; ++j) {
+        const size_t ix = ssi(j);
+        const double wice0 = ICE[ix], wliq0 = LIQ[ix];
+        const double wmass0 = wice0 + wliq0 + 0.0;
+        double tj = T[ix];
+        int imelt = 0;
+        double tinc = 0.0, supercool = 0.0;
+        if (j <= 0) {
+            if (wice0 > 0.0 && tj > TFRZ) { imelt = 1; tinc = TFRZ - tj; tj = TFRZ; }
+            if (wliq0 > 0.0 && tj < TFRZ) { imelt = 2; tinc = TFRZ - tj; tj = TFRZ; }
+        } else {
+            if (wice0 > 0. && tj > TFRZ) { imelt = 1; tinc = TFRZ - tj; tj = TFRZ; }
+            if (tj < TFRZ) {
+                double smp = HFUS * (TFRZ - tj) / (GRAV * tj) * 1000.0;
+                supercool = io.watsat[gi(j)] * pow(smp / io.sucsat[gi(j)], -1.0 / io.bsw[gi(j)]);
+                supercool = supercool * DZ(j) * 1000.0;
+            }
+            if (wliq0 > supercool && tj < TFRZ) { imelt = 2; tinc = TFRZ - tj; tj = TFRZ; }
+            if (io.h2osno_no_layers[c] > 0.0 && j == 1) {
+                if (tj > TFRZ) { imelt = 1; tinc = TFRZ - tj; tj = TFRZ; }
+            }
+        }
+        const double fj = fact[L(j)];
+        double hm = 0.0;
+        if (imelt > 0) {
+            if (j == snl + 1) {
+                if (j > 0) hm = dhsdT * tinc - tinc / fj;
+                else hm = frac_sno * (dhsdT * tinc - tinc / fj);
+                if (j == 1 && frac_h2osfc != 0.0) hm = hm - frac_h2osfc * (dhsdT * tinc);
+            } else if (j == 1) {
+                hm = (1.0 - frac_sno - frac_h2osfc) * dhsdT * tinc - tinc / fj;
+            } else {
+                if (j < 1) hm = -frac_sno * (tinc / fj);
+                else hm = -tinc / fj;
+            }
+        }
+        if (imelt == 1 && hm < 0.0) { hm = 0.0; imelt = 0; }
+        if (imelt == 2 && hm > 0.0) { hm = 0.0; imelt = 0; }
+        double ice = wice0, liq = wliq0;
+        if (imelt > 0 && fabs(hm) > 0.0) {
+            double xm = hm * dtime / HFUS;
+            if (j == 1) {
+                if (io.h2osno_no_layers[c] > 0.0 && xm > 0.0) {
+                    double temp1 = io.h2osno_no_layers[c];
+                    double nl = fmax(0.0, temp1 - xm);
+                    io.h2osno_no_layers[c] = nl;
+                    double propor = nl / temp1;
+                    io.snow_depth[c] = propor * io.snow_depth[c];
+                    double heatr = hm - HFUS * (temp1 - nl) / dtime;
+                    if (heatr > 0.0) { xm = heatr * dtime / HFUS; hm = heatr; }
+                    else { xm = 0.0; hm = 0.0; }
+                    qflx_snomelt = fmax(0.0, (temp1 - nl)) / dtime;
+                    xmf = HFUS * qflx_snomelt;
+                    qflx_snow_drain = qflx_snomelt;
+                }
+            }
+            double heatr = 0.0;
+            if (xm > 0.0) {
+                ice = fmax(0.0, wice0 - xm);
+                if (j >= 1) heatr = hm - HFUS * (0.0 - 0.0 + wice0 - ice) / dtime;
+                else heatr = hm - HFUS * (wice0 - ice) / dtime;
+            } else if (xm < 0.0) {
+                if (j <= 0) ice = fmin(wmass0, wice0 - xm);
+                else ice = (wmass0 - 0.0 < supercool) ? 0.0 : fmin(wmass0 - 0.0 - supercool, wice0 - xm);
+                heatr = hm - HFUS * (wice0 - ice) / dtime;
+            }
+            liq = fmax(0.0, wmass0 - ice - 0.0);
+            if (fabs(heatr) > 0.0) {
+                if (j == snl + 1) {
+                    if (j == 1) tj = tj + fj * heatr / (1.0 - (1.0 - frac_h2osfc) * fj * dhsdT);
+                    else tj = tj + (fj / frac_sno) * heatr / (1.0 - fj * dhsdT);
+                } else if (j == 1) {
+                    tj = tj + fj * heatr / (1.0 - (1.0 - frac_sno - frac_h2osfc) * fj * dhsdT);
+                } else {
+                    if (j > 0) tj = tj + fj * heatr;
+                    else if (frac_sno > 0.0) tj = tj + (fj / frac_sno) * heatr;
+                }
+                if (j <= 0) {
+                    if (liq * ice > 0.0) tj = TFRZ;
+                }
+            }
+            if (j >= 1) xmf = xmf + HFUS * (wice0 - ice) / dtime + HFUS * (0.0 - 0.0) / dtime;
+            else xmf = xmf + HFUS * (wice0 - ice) / dtime;
+            if (imelt == 1 && j < 1) {
+                double m = fmax(0.0, (wice0 - ice)) / dtime;
+                io.qflx_snomelt_lyr[ix] = m;
+                qflx_snomelt = qflx_snomelt + m;
+                io.snomelt_accum[c] = io.snomelt_accum[c] + m * dtime * 1.e-3;
+            }
+            if (imelt == 2 && j < 1) {
+                double f = fmax(0.0, (ice - wice0)) / dtime;
+                io.qflx_snofrz_lyr[ix] = f;
+                qflx_snofrz = qflx_snofrz + f;
+            }
+            ICE[ix] = ice;
+            LIQ[ix] = liq;
+        }
+        T[ix] = tj;
+        io.imelt[ix] = imelt;
+    }
+    io.xmf[c] = xmf;
+    io.qflx_snomelt[c] = qflx_snomelt;
+    io.qflx_snofrz[c] = qflx_snofrz;
+    io.qflx_snow_drain[c] = qflx_snow_drain;
+    io.eflx_snomelt[c] = qflx_snomelt * HFUS;
+
+    // ---------------- t_grnd (:457-477)
+    double tg;
+    const double ts1 = T[ssi(1)];
+    if (snl < 0) {
+        if (frac_h2osfc != 0.0)
+            tg = frac_sno * T[ssi(snl + 1)] + (1.0 - frac_sno - frac_h2osfc) * ts1 + frac_h2osfc * io.t_h2osfc[c];
+        else
+            tg = frac_sno * T[ssi(snl + 1)] + (1.0 - frac_sno) * ts1;
+    } else {
+        if (frac_h2osfc != 0.0) tg = (1.0 - frac_h2osfc) * ts1 + frac_h2osfc * io.t_h2osfc[c];
+        else tg = ts1;
+    }
+    io.t_grnd[c] = tg;
+    return 0;
+}
+
+// ============================================================ kernels
+__global__ void __launch_bounds__(128)
+soilwater_kernel(ctsmg_soilwater_io io, int begc, int nfilt, const int32_t* __restrict__ filt,
+                 double e_ice, double dtime) {
+    const int fc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fc >= nfilt) return;
+    const int c = (filt ? filt[fc] : fc + 1) - begc;
+    zd09_column(io, c, e_ice, dtime);
+}
+
+__global__ void __launch_bounds__(128)
+soiltemp_kernel(ctsmg_soiltemp_io io, int begc, int begp, int nfilt, const int32_t* __restrict__ filt,
+                double dtime, int snow_method, double* ws, int ws_ld, DevError* err) {
+    const int fc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fc >= nfilt) return;
+    const int c = (filt ? filt[fc] : fc + 1) - begc;
+    Scratch S{ws, ws_ld, fc};
+    int info = soiltemp_column(io, c, begp, dtime, snow_method, S);
+    if (info != 0) report_error(err, filt ? filt[fc] : fc + begc, info, CTSMG_E_SINGULAR);
+}
+
+// SoilWater followed by SoilTemperature on the same column, then the
+// between-step refresh of h2osoi_vol (HydrologyNoDrainageMod.F90:580,590).
+__global__ void __launch_bounds__(128)
+soilstep_kernel(ctsmg_soilwater_io wio, ctsmg_soiltemp_io tio, int ncol, double e_ice, double dtime,
+                int snow_method, double* ws, int ws_ld, DevError* err) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncol) return;
+    zd09_column(wio, c, e_ice, dtime);
+    Scratch S{ws, ws_ld, c};
+    int info = soiltemp_column(tio, c, 1, dtime, snow_method, S);
+    if (info != 0) report_error(err, c + 1, info, CTSMG_E_SINGULAR);
+    const int ld = wio.ldc;
+#pragma unroll 1
+    for (int j = 1; j <= NLEVSOI; ++j) {
+        const size_t ix = c + (size_t)(j - LS) * ld;
+        const double dz = wio.dz[ix];
+        ((double*)wio.h2osoi_vol)[c + (size_t)(j - 1) * ld] =
+            tio.h2osoi_liq[ix] / (dz * DENH2O) + tio.h2osoi_ice[ix] / (dz * DENICE);
+    }
+}
+
+// ------------------------------------------------------------ launchers
+cudaError_t launch_soilwater(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt,
+                             double e_ice, double dtime, cudaStream_t s) {
+    if (nfilt <= 0) return cudaSuccess;
+    soilwater_kernel<<<(nfilt + 127) / 128, 128, 0, s>>>(io, begc, nfilt, d_filt, e_ice, dtime);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_soiltemp(const ctsmg_soiltemp_io& io, int begc, int begp, int nfilt, const int32_t* d_filt,
+                            double dtime, int snow_method, double* ws, int ws_ld, DevError* err, cudaStream_t s) {
+    if (nfilt <= 0) return cudaSuccess;
+    soiltemp_kernel<<<(nfilt + 127) / 128, 128, 0, s>>>(io, begc, begp, nfilt, d_filt, dtime, snow_method,
+                                                        ws, ws_ld, err);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_soilstep(const ctsmg_soilwater_io& wio, const ctsmg_soiltemp_io& tio, int ncol,
+                            double e_ice, double dtime, int snow_method, double* ws, int ws_ld,
+                            DevError* err, cudaStream_t s, int block) {
+    if (ncol <= 0) return cudaSuccess;
+    soilstep_kernel<<<(ncol + block - 1) / block, block, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method,
+                                                                 ws, ws_ld, err);
+    return cudaGetLastError();
+}
+
+} // namespace ctsmg

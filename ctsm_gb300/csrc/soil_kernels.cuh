@@ -1,0 +1,17 @@
+// soil_kernels.cuh -- launchers of the soil-path kernels (internal C++ API).
+#pragma once
+#include <cuda_runtime.h>
+#include "ctsm_device.cuh"
+
+namespace ctsmg {
+// rows of heat-system scratch per column (6 doubles per row)
+constexpr int SOILTEMP_WS_DOUBLES_PER_COL = 6 * NROW_MAX;
+
+cudaError_t launch_soilwater(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt,
+                             double e_ice, double dtime, cudaStream_t s);
+cudaError_t launch_soiltemp(const ctsmg_soiltemp_io& io, int begc, int begp, int nfilt, const int32_t* d_filt,
+                            double dtime, int snow_method, double* ws, int ws_ld, DevError* err, cudaStream_t s);
+cudaError_t launch_soilstep(const ctsmg_soilwater_io& wio, const ctsmg_soiltemp_io& tio, int ncol,
+                            double e_ice, double dtime, int snow_method, double* ws, int ws_ld,
+                            DevError* err, cudaStream_t s, int block);
+} // namespace ctsmg

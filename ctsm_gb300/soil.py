@@ -1,0 +1,51 @@
+"""Host-side mirror of the reference's SoilWater / SoilTemperature interface.
+
+The functions keep the reference's names and argument meaning (bounds,
+filter length, 1-based filter, the derived-type components, dtime) and its
+error behaviour (endrun becomes CtsmError carrying the same context).  The
+derived types are represented by one dict of numpy arrays keyed by component
+name, laid out as the Fortran arrays are: (levels, columns) C-contiguous, i.e.
+columns fastest.  Every call goes through the C-ABI of libctsm_gpu.so."""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+from ._lib import load, check
+
+_INIT = {}
+
+
+def init(snow_thermal_cond_method=0, stomatalcond_method=1, itmax_canopy_fluxes=40, e_ice=6.0):
+    """ctsmg_init + ctsmg_set_soilwater_params (the namelist and readParams
+    steps of SoilWaterMovementMod.F90:89-216 and CanopyFluxesMod.F90:92-188)."""
+    L = load()
+    opt = abi.Options(0, snow_thermal_cond_method, itmax_canopy_fluxes, stomatalcond_method,
+                      abi.NLEVSNO, abi.NLEVSOI, abi.NLEVGRND)
+    check(L.ctsmg_init(C.byref(opt)))
+    check(L.ctsmg_set_soilwater_params(C.byref(abi.SoilWaterParams(e_ice))))
+    _INIT.update(snow_thermal_cond_method=snow_thermal_cond_method, e_ice=e_ice)
+
+
+def _filter(filt):
+    f = np.ascontiguousarray(filt, dtype=np.int32)
+    return f, f.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def SoilWater(bounds, num_hydrologyc, filter_hydrologyc, state, dtime):
+    """SoilWater (SoilWaterMovementMod.F90:240), Zeng-Decker 2009 form."""
+    L = load()
+    f, fp = _filter(filter_hydrologyc)
+    ncol = bounds.endc - bounds.begc + 1
+    io = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS, state, ncol)
+    check(L.ctsmg_soilwater(C.byref(bounds), int(num_hydrologyc), fp, C.byref(io), float(dtime)))
+
+
+def SoilTemperature(bounds, num_nolakec, filter_nolakec, state, dtime):
+    """SoilTemperature (SoilTemperatureMod.F90:92) for natural-vegetation columns."""
+    L = load()
+    f, fp = _filter(filter_nolakec)
+    ncol = bounds.endc - bounds.begc + 1
+    npat = bounds.endp - bounds.begp + 1
+    io = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, state, ncol, npat)
+    check(L.ctsmg_soiltemperature(C.byref(bounds), int(num_nolakec), fp, C.byref(io), float(dtime)))

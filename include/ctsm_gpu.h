@@ -1,0 +1,255 @@
+/*
+ * ctsm_gpu.h -- C-ABI of the GB300 (sm_103a) column biogeophysics library.
+ *
+ * This is the boundary a CTSM host binds through ISO_C_BINDING in place of the
+ * three column-parallel calls of the land driver:
+ *
+ *   SoilWater        src/biogeophys/SoilWaterMovementMod.F90:240-243
+ *                    (called from src/biogeophys/HydrologyNoDrainageMod.F90:346)
+ *   SoilTemperature  src/biogeophys/SoilTemperatureMod.F90:92-95
+ *                    (called from src/main/clm_driver.F90:900)
+ *   CanopyFluxes     src/biogeophys/CanopyFluxesMod.F90:191-198
+ *                    (called from src/main/clm_driver.F90:766)
+ *
+ * Array convention (identical to the Fortran storage of the derived types):
+ *   every 2-D column field is declared (begc:endc, lb:ub) in Fortran, so
+ *   element (c, j) lives at  base[(c - begc) + (j - lb) * ldc].
+ *   The Fortran side passes  c_loc(inst%field(begc, lb))  and  ldc = endc-begc+1.
+ *   Patch fields use (p - begp) + (j - lb) * ldp the same way.
+ *   Lower bounds used below (nlevsno = 12, nlevsoi = 20, nlevgrnd = 25):
+ *     [SS] (c, -nlevsno+1 : nlevgrnd)   snow + soil levels (t_soisno, dz, ...)
+ *     [ZI] (c, -nlevsno   : nlevgrnd)   interfaces (col%zi)
+ *     [G ] (c, 1 : nlevgrnd)            soil + bedrock levels (watsat, ...)
+ *     [S ] (c, 1 : nlevsoi)             hydrologically active levels
+ *     [SN] (c, -nlevsno+1 : 0)          snow levels only
+ *     [PL] (p, -nlevsno+1 : 1)          patch snow levels + top soil (sabg_lyr)
+ *   Filters are the reference's 1-based global indices (filter_hydrologyc(fc)
+ *   holds c with begc <= c <= endc).
+ *
+ * Error behaviour: the reference calls endrun (abort).  Every entry point here
+ * returns 0 on success or a CTSMG_E* code; ctsmg_last_error() returns the
+ * message and ctsmg_last_error_index() the (column or patch, level) context, so
+ * the Fortran wrapper can call endrun(subgrid_index=..., subgrid_level=...)
+ * exactly where the reference would.
+ *
+ * All entry points are host-pointer, copy-in / copy-out calls that may be made
+ * concurrently from several host threads (one per clump, as the
+ * !$OMP PARALLEL DO of src/main/clm_driver.F90:525 does): each calling thread
+ * gets its own CUDA stream and device workspace.
+ */
+#ifndef CTSM_GPU_H
+#define CTSM_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- sizes */
+#define CTSMG_NLEVSNO   12
+#define CTSMG_NLEVSOI   20
+#define CTSMG_NLEVGRND  25
+#define CTSMG_NLEV_SS   (CTSMG_NLEVSNO + CTSMG_NLEVGRND)      /* 37 */
+#define CTSMG_NLEV_ZI   (CTSMG_NLEVSNO + CTSMG_NLEVGRND + 1)  /* 38 */
+
+/* ---------------------------------------------------------------- status */
+#define CTSMG_OK               0
+#define CTSMG_E_ARG            1   /* bad argument / size (host check)            */
+#define CTSMG_E_CUDA           2   /* CUDA runtime error                          */
+#define CTSMG_E_NOT_INIT       3   /* ctsmg_init not called                       */
+#define CTSMG_E_SINGULAR       4   /* band solve: dgbsv info /= 0
+                                      (src/biogeophys/BandDiagonalMod.F90:200-213) */
+#define CTSMG_E_DISCRIMINANT   5   /* quadratic: negative discriminant
+                                      (src/utils/quadraticMod.F90:50-58)          */
+#define CTSMG_E_NOT_BRACKETED  6   /* brent: root not bracketed
+                                      (src/biogeophys/PhotosynthesisMod.F90:2412-2415) */
+#define CTSMG_E_FORCING_HEIGHT 7   /* forcing height below canopy
+                                      (src/biogeophys/CanopyFluxesMod.F90:997-1002) */
+#define CTSMG_E_BALANCE        8   /* water / energy balance above stop threshold
+                                      (src/biogeophys/BalanceCheckMod.F90:626,1111) */
+#define CTSMG_E_TIMEOUT        9   /* a bounded device wait ran out                */
+#define CTSMG_E_UNSUPPORTED   10   /* option not built (e.g. urban columns)        */
+
+/* ---------------------------------------------------------------- bounds */
+/* src/main/decompMod.F90:58-70 (bounds_type: begg/endg, begl/endl, begc/endc, begp/endp) */
+typedef struct {
+    int32_t begc, endc;
+    int32_t begp, endp;
+} ctsmg_bounds;
+
+/* ---------------------------------------------------------------- options */
+/* Namelist values the reference keeps as module state:
+ *   soilwater_movement_method, lower_boundary_condition
+ *     (src/biogeophys/SoilWaterMovementMod.F90:67-78, defaults
+ *      bld/namelist_files/namelist_defaults_ctsm.xml:471-477)
+ *   snow_thermal_cond_method (src/main/clm_varctl.F90; default Jordan1991,
+ *      Sturm1997 for clm6_0: namelist_defaults_ctsm.xml:555-556)
+ *   itmax_canopy_fluxes (src/biogeophys/CanopyFluxesMod.F90:83)             */
+typedef struct {
+    int32_t soilwater_movement_method;   /* 0 = Zeng-Decker 2009 (only form built)  */
+    int32_t snow_thermal_cond_method;    /* 0 = Jordan1991, 1 = Sturm1997           */
+    int32_t itmax_canopy_fluxes;         /* 40                                      */
+    int32_t stomatalcond_method;         /* 0 = Ball-Berry 1987, 1 = Medlyn 2011    */
+    int32_t nlevsno, nlevsoi, nlevgrnd;  /* must equal the CTSMG_NLEV* constants    */
+} ctsmg_options;
+
+/* Scalar parameters read from the parameter file by readParams:
+ *   e_ice  src/biogeophys/SoilWaterMovementMod.F90:89-106                       */
+typedef struct {
+    double e_ice;
+} ctsmg_soilwater_params;
+
+/* ---------------------------------------------------------------- SoilWater */
+/* Components of the derived types that soilwater_zengdecker2009 reads and
+ * writes (src/biogeophys/SoilWaterMovementMod.F90:537-566).                  */
+typedef struct {
+    int32_t ldc;                 /* leading dimension of every column array       */
+    /* col (ColumnType) */
+    const double* z;             /* [SS] layer depth (m)                          */
+    const double* zi;            /* [ZI] interface depth (m)                      */
+    const double* dz;            /* [SS] layer thickness (m)                      */
+    /* soilhydrology_inst */
+    const double* zwt;           /* (c)  water table depth (m)                    */
+    double*       qcharge;       /* (c)  out: aquifer recharge (mm/s)             */
+    double*       icefrac;       /* [G]  out: ice fraction, levels 1..nlevsoi     */
+    double*       qin;           /* [S]  out: flux into layer (mm/s)              */
+    double*       qout;          /* [S]  out: flux out of layer (mm/s)            */
+    /* soilstate_inst */
+    const double* smpmin;        /* (c)  minimum soil potential (mm)              */
+    const double* watsat;        /* [G]  porosity                                 */
+    const double* hksat;         /* [G]  saturated conductivity (mm/s)            */
+    const double* bsw;           /* [G]  Clapp-Hornberger b                       */
+    const double* sucsat;        /* [G]  saturated suction (mm)                   */
+    double*       smp_l;         /* [G]  out: matric potential (mm)               */
+    double*       hk_l;          /* [G]  out: conductivity (mm/s)                 */
+    /* waterstatebulk_inst */
+    const double* h2osoi_ice;    /* [SS] ice (kg/m2)                              */
+    double*       h2osoi_liq;    /* [SS] inout: liquid (kg/m2)                    */
+    const double* h2osoi_vol;    /* [G]  volumetric water (previous step)         */
+    /* waterfluxbulk_inst */
+    double*       qflx_deficit;  /* (c)  out: deficit to keep liquid >= 0 (mm/s)  */
+    const double* qflx_infl;     /* (c)  infiltration (mm/s)                      */
+    const double* qflx_rootsoi;  /* [S]  root water sink (mm/s)                   */
+    /* temperature_inst */
+    const double* t_soisno;      /* [SS] soil temperature (K)                     */
+} ctsmg_soilwater_io;
+
+/* ---------------------------------------------------------------- SoilTemperature */
+/* Components read and written by SoilTemperature and the routines it calls
+ * (SoilThermProp, ComputeGroundHeatFluxAndDeriv, ComputeHeatDiffFluxAndFactor,
+ *  SetRHSVec*, SetMatrix*, BandDiagonal, PhaseChangeH2osfc, Phasechange):
+ *  src/biogeophys/SoilTemperatureMod.F90:184-256, 661-688, 960-981, 1191-1219,
+ *  1603-1653.  Natural-vegetation (soil/crop) columns only; urban, lake,
+ *  glacier, wetland and excess-ice branches are not built.                    */
+typedef struct {
+    int32_t ldc, ldp;
+    /* col (ColumnType) and patch (PatchType) */
+    const int32_t* snl;          /* (c)  number of snow layers (<= 0)             */
+    const int32_t* nbedrock;     /* (c)  index of deepest soil layer              */
+    const double*  z;            /* [SS] */
+    const double*  zi;           /* [ZI] */
+    const double*  dz;           /* [SS] */
+    const int32_t* col_patchi;   /* (c)  first patch of column (global index)     */
+    const int32_t* col_npatches; /* (c)  patches in column                        */
+    const double*  wtcol;        /* (p)  patch weight on column                   */
+    const int32_t* frac_veg_nosno; /* (p) 0/1                                     */
+    /* atm2lnd / solarabs (patch) */
+    const double* forc_lwrad;    /* (c)  downward longwave (W/m2)                 */
+    const double* sabg;          /* (p) */
+    const double* sabg_soil;     /* (p) */
+    const double* sabg_snow;     /* (p) */
+    const double* sabg_lyr;      /* [PL] */
+    double*       sabg_chk;      /* (p)  out */
+    /* energyflux_inst (patch inputs, patch/col outputs) */
+    const double* htvp;          /* (c) */
+    const double* cgrnd;         /* (p) */
+    const double* dlrad;         /* (p) */
+    const double* eflx_sh_grnd;  /* (p) */
+    const double* eflx_sh_snow;  /* (p) */
+    const double* eflx_sh_soil;  /* (p) */
+    const double* eflx_sh_h2osfc;/* (p) */
+    const double* qflx_evap_soi; /* (p) */
+    const double* qflx_ev_snow;  /* (p) */
+    const double* qflx_ev_soil;  /* (p) */
+    const double* qflx_ev_h2osfc;/* (p) */
+    const double* eflx_bot;      /* (c) */
+    double*       eflx_gnet;     /* (p)  out */
+    double*       dgnetdT;       /* (p)  out */
+    double*       eflx_fgr12;    /* (c)  out */
+    double*       eflx_fgr;      /* [G]  out */
+    double*       eflx_snomelt;  /* (c)  out */
+    double*       eflx_h2osfc_to_snow; /* (c) out */
+    /* temperature_inst */
+    const double* emg;           /* (c) */
+    double*       t_soisno;      /* [SS] inout */
+    double*       t_h2osfc;      /* (c)  inout */
+    double*       t_grnd;        /* (c)  inout (input: previous ground T)         */
+    double*       fact;          /* [SS] out */
+    double*       c_h2osfc;      /* (c)  out */
+    double*       xmf;           /* (c)  out */
+    double*       xmf_h2osfc;    /* (c)  out */
+    int32_t*      imelt;         /* [SS] out */
+    /* soilstate_inst */
+    const double* watsat;        /* [G] */
+    const double* bsw;           /* [G] */
+    const double* sucsat;        /* [G] */
+    const double* tkmg;          /* [G] */
+    const double* tkdry;         /* [G] */
+    const double* csol;          /* [G] */
+    double*       thk;           /* [SS] out */
+    /* waterstatebulk / waterdiagnosticbulk / waterfluxbulk */
+    double*       h2osoi_liq;    /* [SS] inout */
+    double*       h2osoi_ice;    /* [SS] inout */
+    double*       h2osfc;        /* (c)  inout */
+    double*       h2osno_no_layers; /* (c) inout */
+    double*       int_snow;      /* (c)  inout */
+    double*       snow_depth;    /* (c)  inout */
+    double*       snomelt_accum; /* (c)  inout */
+    const double* frac_sno_eff;  /* (c) */
+    const double* frac_h2osfc;   /* (c) */
+    double*       bw;            /* [SN] out */
+    double*       qflx_snomelt;  /* (c)  out */
+    double*       qflx_snofrz;   /* (c)  out */
+    double*       qflx_snow_drain; /* (c) out */
+    double*       qflx_snomelt_lyr; /* [SN] out */
+    double*       qflx_snofrz_lyr;  /* [SN] out */
+    double*       qflx_h2osfc_to_ice; /* (c) out */
+} ctsmg_soiltemp_io;
+
+/* ---------------------------------------------------------------- lifecycle */
+/* Replaces the namelist reads init_soilwater_movement
+ * (src/biogeophys/SoilWaterMovementMod.F90:110-216), CanopyFluxesReadNML
+ * (src/biogeophys/CanopyFluxesMod.F90:92-157) and Photosynthesis ReadNML
+ * (src/biogeophys/PhotosynthesisMod.F90:939-1015).  Selects device 0.       */
+int32_t ctsmg_init(const ctsmg_options* opt);
+
+/* Replaces readParams of SoilWaterMovementMod (src/biogeophys/SoilWaterMovementMod.F90:89-106). */
+int32_t ctsmg_set_soilwater_params(const ctsmg_soilwater_params* p);
+
+/* Frees every device buffer and stream. */
+int32_t ctsmg_finalize(void);
+
+/* Message and (index, level) context of the last error on the calling thread. */
+const char* ctsmg_last_error(void);
+int32_t ctsmg_last_error_index(int32_t* index, int32_t* level);
+
+/* ---------------------------------------------------------------- drop-in calls */
+/* SoilWater, Zeng-Decker 2009 form:
+ *   src/biogeophys/SoilWaterMovementMod.F90:240-243 (dispatch :297-329) and
+ *   soilwater_zengdecker2009 :414-972.  num_urbanc/filter_urbanc are unused by
+ *   that form and omitted. */
+int32_t ctsmg_soilwater(const ctsmg_bounds* bounds,
+                        int32_t num_hydrologyc, const int32_t* filter_hydrologyc,
+                        const ctsmg_soilwater_io* io, double dtime);
+
+/* SoilTemperature: src/biogeophys/SoilTemperatureMod.F90:92-508 (urban
+ * filters omitted: urban columns are not built). */
+int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds,
+                              int32_t num_nolakec, const int32_t* filter_nolakec,
+                              const ctsmg_soiltemp_io* io, double dtime);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CTSM_GPU_H */

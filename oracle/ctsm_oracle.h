@@ -1,0 +1,25 @@
+/* ctsm_oracle.h -- CPU oracle entry points (test infrastructure only; never
+ * linked into the product library).  Each restates a reference routine; see
+ * the comments in the .cpp files for the file:line each one follows. */
+#ifndef CTSM_ORACLE_H
+#define CTSM_ORACLE_H
+#include <stdint.h>
+#include "ctsm_gpu.h"
+#ifdef __cplusplus
+extern "C" {
+#endif
+void oracle_tridiagonal(int n, const double* a, const double* b, const double* c,
+                        const double* r, double* u);
+int  oracle_dgbsv(int n, int kl, int ku, double* ab, int ldab, int* ipiv, double* b);
+int  oracle_soilwater(const ctsmg_bounds* bounds, int num_hydrologyc,
+                      const int32_t* filter_hydrologyc, const ctsmg_soilwater_io* io,
+                      double e_ice, double dtime);
+int  oracle_soiltemperature(const ctsmg_bounds* bounds, int num_nolakec,
+                            const int32_t* filter_nolakec, const ctsmg_soiltemp_io* io,
+                            double dtime, int snow_method);
+int  oracle_last_error(int* idx, int* lev);
+void oracle_set_libm_noise(int ulps, unsigned long long seed);
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,37 @@
+"""ctypes loader for oracle/liboracle.so (built by oracle/Makefile)."""
+import ctypes as C
+import os
+import subprocess
+
+from ctsm_gb300 import abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+
+def build(force=False):
+    so = os.path.join(_HERE, "liboracle.so")
+    if force or not os.path.exists(so) or any(
+            os.path.getmtime(os.path.join(_HERE, f)) > os.path.getmtime(so)
+            for f in os.listdir(_HERE) if f.endswith((".cpp", ".h"))):
+        subprocess.run(["make", "-s", "-C", _HERE, "-B" if force else "all"], check=True)
+    return so
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        _LIB = C.CDLL(build())
+        P, I = C.POINTER, C.c_int
+        _LIB.oracle_soilwater.argtypes = [P(abi.Bounds), I, P(C.c_int32), P(abi.SoilWaterIO), C.c_double, C.c_double]
+        _LIB.oracle_soiltemperature.argtypes = [P(abi.Bounds), I, P(C.c_int32), P(abi.SoilTempIO), C.c_double, I]
+        _LIB.oracle_dgbsv.argtypes = [I, I, I, P(C.c_double), I, P(C.c_int), P(C.c_double)]
+        _LIB.oracle_tridiagonal.argtypes = [I] + [P(C.c_double)] * 5
+        _LIB.oracle_tridiagonal.restype = None
+        _LIB.oracle_set_libm_noise.argtypes = [I, C.c_ulonglong]
+        _LIB.oracle_set_libm_noise.restype = None
+    return _LIB
+
+
+def set_threads(n):
+    os.environ["OMP_NUM_THREADS"] = str(n)

@@ -1,0 +1,21 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a) and the built libctsm_gpu.so")
+
+
+@pytest.fixture(scope="session")
+def gpu_lib():
+    """The built CUDA library, initialised once per session."""
+    from ctsm_gb300 import build, soil
+    build.build()
+    soil.init()
+    return soil
