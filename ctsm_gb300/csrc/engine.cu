@@ -1,0 +1,295 @@
+// engine.cu -- batched resident mode: many columns of uneven depth kept in
+// HBM across model steps, bucketed by level count, each step replayed as one
+// CUDA graph (SoilWater + SoilTemperature + the h2osoi_vol refresh).
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <string>
+#include <vector>
+#include "ctsm_gpu.h"
+#include "ctsm_device.cuh"
+#include "soil_kernels.cuh"
+#include "capi_internal.h"
+
+namespace ctsmg {
+
+struct UField {              // one resident component (shared by both io structs)
+    std::string name;
+    int kind, esize, use;
+    void* dptr = nullptr;
+    size_t bytes = 0;
+};
+
+struct Batch {
+    int ncol = 0, npatch = 0;
+    double dtime = 1800.0, e_ice = 6.0;
+    int snow_method = 0;
+    int block = 128;
+    std::vector<UField> fields;
+    ctsmg_soilwater_io dsw{};
+    ctsmg_soiltemp_io dst{};
+    int32_t* d_perm = nullptr;     // sorted position -> original column index (0-based)
+    double* ws = nullptr;
+    DevError* err = nullptr;
+    void* snapshot = nullptr;
+    size_t state_bytes = 0;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+static int cuda_err(cudaError_t e, const char* where) {
+    std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+    return set_error(CTSMG_E_CUDA, m.c_str(), 0, 0);
+}
+#define CK(call, where) do { cudaError_t _e = (call); if (_e != cudaSuccess) return cuda_err(_e, where); } while (0)
+
+static void* io_ptr(const void* io, const FieldDesc& f) {
+    return *reinterpret_cast<void* const*>(reinterpret_cast<const char*>(io) + f.offset);
+}
+static void set_io_ptr(void* io, const FieldDesc& f, void* p) {
+    *reinterpret_cast<void**>(reinterpret_cast<char*>(io) + f.offset) = p;
+}
+
+static int build_graph(Batch* b) {
+    if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    cudaError_t le = launch_soilstep(b->dsw, b->dst, b->ncol, b->e_ice, b->dtime, b->snow_method, b->ws,
+                                     b->ncol, b->err, b->stream, b->block);
+    cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+    if (le != cudaSuccess) return cuda_err(le, "soilstep capture");
+    if (ce != cudaSuccess) return cuda_err(ce, "cudaStreamEndCapture");
+    cudaError_t ie = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) return cuda_err(ie, "cudaGraphInstantiate");
+    return 0;
+}
+
+static void batch_free(Batch* b) {
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    for (auto& f : b->fields) if (f.dptr) cudaFree(f.dptr);
+    if (b->d_perm) cudaFree(b->d_perm);
+    if (b->ws) cudaFree(b->ws);
+    if (b->err) cudaFree(b->err);
+    if (b->snapshot) cudaFree(b->snapshot);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+} // namespace ctsmg
+
+using namespace ctsmg;
+
+struct ctsmg_batch_s { Batch* b; };
+
+extern "C" int32_t ctsmg_batch_create(ctsmg_batch* out, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
+                                      int32_t ncol, int32_t npatch, double dtime, double e_ice,
+                                      int32_t snow_thermal_cond_method) {
+    if (!out || !sw || !st) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
+    if (ncol <= 0 || npatch < 0) return set_error(CTSMG_E_ARG, "ncol must be positive", 0, 0);
+    if (sw->ldc != ncol || st->ldc != ncol || st->ldp != npatch)
+        return set_error(CTSMG_E_ARG, "batch arrays must be dense: ldc = ncol, ldp = npatch", 0, 0);
+    if (!(dtime > 0.0)) return set_error(CTSMG_E_ARG, "dtime must be positive", 0, 0);
+    for (int c = 0; c < ncol; ++c) {
+        const int s = st->snl[c], pi = st->col_patchi[c], np = st->col_npatches[c];
+        if (s > 0 || s < -NLEVSNO) return set_error(CTSMG_E_ARG, "snl outside -nlevsno..0", c + 1, 0);
+        if (np < 0 || pi < 1 || pi + np - 1 > npatch)
+            return set_error(CTSMG_E_ARG, "column patches outside 1..npatch", c + 1, 0);
+    }
+    Batch* b = new Batch();
+    b->ncol = ncol; b->npatch = npatch; b->dtime = dtime; b->e_ice = e_ice;
+    b->snow_method = snow_thermal_cond_method;
+    auto fail = [&](int rc) { batch_free(b); return rc; };
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(cuda_err(e, "stream"));
+    if ((e = cudaEventCreate(&b->ev0)) != cudaSuccess) return fail(cuda_err(e, "event"));
+    if ((e = cudaEventCreate(&b->ev1)) != cudaSuccess) return fail(cuda_err(e, "event"));
+
+    // bucket columns: more snow layers first, then shallower bedrock
+    std::vector<int32_t> perm(ncol);
+    std::iota(perm.begin(), perm.end(), 0);
+    std::stable_sort(perm.begin(), perm.end(), [&](int a, int c) {
+        if (st->snl[a] != st->snl[c]) return st->snl[a] < st->snl[c];
+        return st->nbedrock[a] < st->nbedrock[c];
+    });
+    if ((e = cudaMalloc(&b->d_perm, (size_t)ncol * 4)) != cudaSuccess) return fail(cuda_err(e, "perm"));
+    if ((e = cudaMemcpy(b->d_perm, perm.data(), (size_t)ncol * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
+        return fail(cuda_err(e, "perm H2D"));
+
+    // the union of both component tables, one resident buffer per component
+    std::map<std::string, int> index;
+    auto add = [&](const FieldDesc* tab, int nf, const void* hio, void* dio) -> int {
+        for (int i = 0; i < nf; ++i) {
+            const FieldDesc& f = tab[i];
+            auto it = index.find(f.name);
+            if (it == index.end()) {
+                UField u;
+                u.name = f.name; u.kind = f.kind; u.esize = f.esize; u.use = f.use;
+                u.bytes = field_bytes(f, ncol, npatch);
+                cudaError_t ee = cudaMalloc(&u.dptr, u.bytes);
+                if (ee != cudaSuccess) return cuda_err(ee, "cudaMalloc(field)");
+                const void* hp = io_ptr(hio, f);
+                if (!hp) return set_error(CTSMG_E_ARG, (std::string("null component ") + f.name).c_str(), 0, 0);
+                // upload, then gather columns into bucket order (patch arrays stay in place)
+                if (f.kind == K_P || f.kind == K_PL) {
+                    ee = cudaMemcpy(u.dptr, hp, u.bytes, cudaMemcpyHostToDevice);
+                } else {
+                    void* tmp = nullptr;
+                    ee = cudaMalloc(&tmp, u.bytes);
+                    if (ee == cudaSuccess) ee = cudaMemcpy(tmp, hp, u.bytes, cudaMemcpyHostToDevice);
+                    if (ee == cudaSuccess) ee = launch_permute(u.dptr, tmp, b->d_perm, ncol, kind_levels(f.kind), f.esize, 0, b->stream);
+                    if (ee == cudaSuccess) ee = cudaStreamSynchronize(b->stream);
+                    if (tmp) cudaFree(tmp);
+                }
+                if (ee != cudaSuccess) return cuda_err(ee, "upload");
+                index[f.name] = (int)b->fields.size();
+                b->fields.push_back(u);
+                it = index.find(f.name);
+            }
+            set_io_ptr(dio, f, b->fields[it->second].dptr);
+        }
+        return 0;
+    };
+    std::memcpy(&b->dsw, sw, sizeof b->dsw);
+    std::memcpy(&b->dst, st, sizeof b->dst);
+    int rc;
+    if ((rc = add(SOILWATER_TABLE, SOILWATER_NFIELDS, sw, &b->dsw))) return fail(rc);
+    if ((rc = add(SOILTEMP_TABLE, SOILTEMP_NFIELDS, st, &b->dst))) return fail(rc);
+    for (auto& f : b->fields) b->state_bytes += f.bytes;
+    if ((e = cudaMalloc(&b->ws, (size_t)SOILTEMP_WS_DOUBLES_PER_COL * ncol * 8)) != cudaSuccess) return fail(cuda_err(e, "ws"));
+    if ((e = cudaMalloc(&b->err, sizeof(DevError))) != cudaSuccess) return fail(cuda_err(e, "err"));
+    if ((e = cudaMemset(b->err, 0xff, sizeof(DevError))) != cudaSuccess) return fail(cuda_err(e, "err"));
+    if ((rc = build_graph(b))) return fail(rc);
+    *out = new ctsmg_batch_s{b};
+    return 0;
+}
+
+extern "C" int32_t ctsmg_batch_run(ctsmg_batch bh, int32_t nsteps, float* step_ms) {
+    if (!bh || nsteps < 0) return set_error(CTSMG_E_ARG, "bad batch or nsteps", 0, 0);
+    Batch* b = bh->b;
+    for (int s = 0; s < nsteps; ++s) {
+        if (step_ms) CK(cudaEventRecord(b->ev0, b->stream), "event");
+        CK(cudaGraphLaunch(b->graph, b->stream), "cudaGraphLaunch");
+        if (step_ms) {
+            CK(cudaEventRecord(b->ev1, b->stream), "event");
+            CK(cudaEventSynchronize(b->ev1), "event sync");
+            CK(cudaEventElapsedTime(&step_ms[s], b->ev0, b->ev1), "elapsed");
+        }
+    }
+    return 0;
+}
+
+extern "C" int32_t ctsmg_batch_sync(ctsmg_batch bh) {
+    if (!bh) return set_error(CTSMG_E_ARG, "null batch", 0, 0);
+    Batch* b = bh->b;
+    CK(cudaStreamSynchronize(b->stream), "batch sync");
+    DevError h;
+    CK(cudaMemcpy(&h, b->err, sizeof h, cudaMemcpyDeviceToHost), "err D2H");
+    if (h.key != ~0ull) {
+        int pos = (int)(h.key >> 32) - 1;
+        int32_t orig = 0;
+        cudaMemcpy(&orig, b->d_perm + pos, 4, cudaMemcpyDeviceToHost);
+        return set_error((int)(h.key & 0xff), "BandDiagonal ERROR: dgbsv returned error code", orig + 1,
+                         (int)((h.key >> 8) & 0xffffff) - 1024);
+    }
+    return 0;
+}
+
+extern "C" int32_t ctsmg_batch_download(ctsmg_batch bh, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st) {
+    if (!bh || !sw || !st) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
+    Batch* b = bh->b;
+    CK(cudaStreamSynchronize(b->stream), "sync");
+    auto down = [&](const FieldDesc* tab, int nf, const void* hio) -> int {
+        for (int i = 0; i < nf; ++i) {
+            const FieldDesc& f = tab[i];
+            void* hp = io_ptr(hio, f);
+            const UField* u = nullptr;
+            for (auto& x : b->fields) if (x.name == f.name) { u = &x; break; }
+            if (!u || !hp) continue;
+            if (f.kind == K_P || f.kind == K_PL) {
+                CK(cudaMemcpy(hp, u->dptr, u->bytes, cudaMemcpyDeviceToHost), "D2H");
+            } else {
+                void* tmp = nullptr;
+                CK(cudaMalloc(&tmp, u->bytes), "tmp");
+                cudaError_t e = launch_permute(tmp, u->dptr, b->d_perm, b->ncol, kind_levels(f.kind), f.esize, 1, b->stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+                if (e == cudaSuccess) e = cudaMemcpy(hp, tmp, u->bytes, cudaMemcpyDeviceToHost);
+                cudaFree(tmp);
+                if (e != cudaSuccess) return cuda_err(e, "download");
+            }
+        }
+        return 0;
+    };
+    int rc;
+    if ((rc = down(SOILWATER_TABLE, SOILWATER_NFIELDS, sw))) return rc;
+    if ((rc = down(SOILTEMP_TABLE, SOILTEMP_NFIELDS, st))) return rc;
+    return 0;
+}
+
+// Times `trial_steps` graph replays per candidate block size on the batch's
+// own data and keeps the fastest; the state is restored afterwards.
+extern "C" int32_t ctsmg_batch_autotune(ctsmg_batch bh, int32_t trial_steps, int32_t* block_out) {
+    if (!bh) return set_error(CTSMG_E_ARG, "null batch", 0, 0);
+    Batch* b = bh->b;
+    if (trial_steps < 1) trial_steps = 1;
+    if (!b->snapshot) CK(cudaMalloc(&b->snapshot, b->state_bytes), "snapshot");
+    size_t off = 0;
+    for (auto& f : b->fields) {
+        CK(cudaMemcpyAsync((char*)b->snapshot + off, f.dptr, f.bytes, cudaMemcpyDeviceToDevice, b->stream), "snap");
+        off += f.bytes;
+    }
+    const int cands[3] = {64, 128, 256};
+    int best = b->block;
+    float best_ms = 1e30f;
+    for (int k = 0; k < 3; ++k) {
+        b->block = cands[k];
+        int rc = build_graph(b);
+        if (rc) return rc;
+        CK(cudaGraphLaunch(b->graph, b->stream), "warm");
+        CK(cudaEventRecord(b->ev0, b->stream), "ev");
+        for (int s = 0; s < trial_steps; ++s) CK(cudaGraphLaunch(b->graph, b->stream), "trial");
+        CK(cudaEventRecord(b->ev1, b->stream), "ev");
+        CK(cudaEventSynchronize(b->ev1), "ev sync");
+        float ms;
+        CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1), "elapsed");
+        if (ms < best_ms) { best_ms = ms; best = cands[k]; }
+    }
+    off = 0;
+    for (auto& f : b->fields) {
+        CK(cudaMemcpyAsync(f.dptr, (char*)b->snapshot + off, f.bytes, cudaMemcpyDeviceToDevice, b->stream), "restore");
+        off += f.bytes;
+    }
+    CK(cudaMemsetAsync(b->err, 0xff, sizeof(DevError), b->stream), "err reset");
+    CK(cudaStreamSynchronize(b->stream), "sync");
+    cudaFree(b->snapshot);
+    b->snapshot = nullptr;
+    b->block = best;
+    int rc = build_graph(b);
+    if (rc) return rc;
+    if (block_out) *block_out = best;
+    return 0;
+}
+
+extern "C" int32_t ctsmg_batch_set_block(ctsmg_batch bh, int32_t block) {
+    if (!bh || (block != 64 && block != 128 && block != 256))
+        return set_error(CTSMG_E_ARG, "block must be 64, 128 or 256", 0, 0);
+    bh->b->block = block;
+    return build_graph(bh->b);
+}
+
+extern "C" int64_t ctsmg_batch_state_bytes(ctsmg_batch bh) { return bh ? (int64_t)bh->b->state_bytes : 0; }
+
+extern "C" int32_t ctsmg_batch_destroy(ctsmg_batch bh) {
+    if (!bh) return 0;
+    batch_free(bh->b);
+    delete bh;
+    return 0;
+}

@@ -819,10 +819,11 @@ soiltemp_kernel(ctsmg_soiltemp_io io, int begc, int begp, int nfilt, const int32
 
 // SoilWater followed by SoilTemperature on the same column, then the
 // between-step refresh of h2osoi_vol (HydrologyNoDrainageMod.F90:580,590).
-__global__ void __launch_bounds__(128)
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK)
 soilstep_kernel(ctsmg_soilwater_io wio, ctsmg_soiltemp_io tio, int ncol, double e_ice, double dtime,
                 int snow_method, double* ws, int ws_ld, DevError* err) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.x * BLOCK + threadIdx.x;
     if (c >= ncol) return;
     zd09_column(wio, c, e_ice, dtime);
     Scratch S{ws, ws_ld, c};
@@ -858,8 +859,43 @@ cudaError_t launch_soilstep(const ctsmg_soilwater_io& wio, const ctsmg_soiltemp_
                             double e_ice, double dtime, int snow_method, double* ws, int ws_ld,
                             DevError* err, cudaStream_t s, int block) {
     if (ncol <= 0) return cudaSuccess;
-    soilstep_kernel<<<(ncol + block - 1) / block, block, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method,
-                                                                 ws, ws_ld, err);
+    switch (block) {
+        case 64:
+            soilstep_kernel<64><<<(ncol + 63) / 64, 64, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err);
+            break;
+        case 256:
+            soilstep_kernel<256><<<(ncol + 255) / 256, 256, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err);
+            break;
+        default:
+            soilstep_kernel<128><<<(ncol + 127) / 128, 128, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err);
+            break;
+    }
+    return cudaGetLastError();
+}
+
+// column gather / scatter of one level-major field: dst[l*ld + i] = src[l*ld + perm[i]]
+// (gather) or dst[l*ld + perm[i]] = src[l*ld + i] (scatter); esize 4 or 8 bytes.
+template <typename T>
+__global__ void permute_kernel(T* __restrict__ dst, const T* __restrict__ src, const int32_t* __restrict__ perm,
+                               int ncol, int nlev, int scatter) {
+    const long long n = (long long)ncol * nlev;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const int l = (int)(k / ncol), i = (int)(k % ncol);
+        const size_t base = (size_t)l * ncol;
+        if (scatter) dst[base + perm[i]] = src[base + i];
+        else dst[base + i] = src[base + perm[i]];
+    }
+}
+
+cudaError_t launch_permute(void* dst, const void* src, const int32_t* perm, int ncol, int nlev, int esize,
+                           int scatter, cudaStream_t s) {
+    const long long n = (long long)ncol * nlev;
+    int blocks = (int)((n + 255) / 256);
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    if (esize == 8)
+        permute_kernel<double><<<blocks, 256, 0, s>>>((double*)dst, (const double*)src, perm, ncol, nlev, scatter);
+    else
+        permute_kernel<int32_t><<<blocks, 256, 0, s>>>((int32_t*)dst, (const int32_t*)src, perm, ncol, nlev, scatter);
     return cudaGetLastError();
 }
 

@@ -14,4 +14,6 @@ cudaError_t launch_soiltemp(const ctsmg_soiltemp_io& io, int begc, int begp, int
 cudaError_t launch_soilstep(const ctsmg_soilwater_io& wio, const ctsmg_soiltemp_io& tio, int ncol,
                             double e_ice, double dtime, int snow_method, double* ws, int ws_ld,
                             DevError* err, cudaStream_t s, int block);
+cudaError_t launch_permute(void* dst, const void* src, const int32_t* perm, int ncol, int nlev, int esize,
+                           int scatter, cudaStream_t s);
 } // namespace ctsmg

@@ -1,0 +1,56 @@
+"""Algorithmic bytes per column-step of the fused soil step, from the ABI
+manifest (ctsm_gb300/abi.py): every component the step reads is counted once,
+every component it writes once, on the levels the column actually uses
+(snow arrays on its |snl| active layers only)."""
+from . import abi
+
+NLEVSNO, NLEVSOI, NLEVGRND = abi.NLEVSNO, abi.NLEVSOI, abi.NLEVGRND
+
+# FP64 floating-point operations per column-step of soilstep_kernel on the
+# uneven-column workload (DADD + DMUL + 2 x DFMA executed, libm included),
+# and DRAM bytes per column-step, from the ncu capture of 65,536 columns of
+# the same workload summarised in profiles/soilstep_kernel_uneven_columns.md.
+FLOPS_PER_COLUMN_STEP = (424136267 + 219978292 + 2 * 961139171) / 65536.0
+TRAFFIC_PER_COLUMN_STEP = (733.809408e6 + 492.769792e6) / 65536.0
+
+
+def _active_levels(kind, nsnow):
+    return {"C": 1, "P": 1, "SS": nsnow + NLEVGRND, "ZI": nsnow + NLEVGRND + 1, "G": NLEVGRND,
+            "S": NLEVSOI, "SN": nsnow, "PL": nsnow + 1}[kind]
+
+
+def step_bytes_per_column(mean_snow_layers, patches_per_column=1.0):
+    """(bytes read, bytes written) per column for one SoilWater + SoilTemperature
+    step with the between-step h2osoi_vol refresh."""
+    fields = {}
+    for (n, k, t, u) in abi.SOILWATER_FIELDS + abi.SOILTEMP_FIELDS:
+        r, w = fields.get(n, (False, False, k, t))[:2]
+        fields[n] = (r or u in ("in", "inout"), w or u in ("out", "inout"), k, t)
+    fields["h2osoi_vol"] = (True, True, "G", "f8")  # refreshed at the end of the step
+    rd = wr = 0.0
+    for n, (r, w, k, t) in fields.items():
+        size = 8 if t == "f8" else 4
+        lev = _active_levels(k, mean_snow_layers)
+        if k == "G" and n == "h2osoi_vol":
+            lev = NLEVSOI
+        mult = patches_per_column if k in ("P", "PL") else 1.0
+        if r:
+            rd += lev * size * mult
+        if w:
+            wr += lev * size * mult
+    return rd, wr
+
+
+def dropin_copy_bytes_per_column(patches_per_column=1.0):
+    """(H2D, D2H) bytes per column of one plain SoilWater + SoilTemperature call
+    pair: the C-ABI copies every component's full level extent in and the
+    written components back."""
+    h2d = d2h = 0.0
+    for table in (abi.SOILWATER_FIELDS, abi.SOILTEMP_FIELDS):
+        for (n, k, t, u) in table:
+            size = 8 if t == "f8" else 4
+            b = abi.LEVELS[k][1] * size * (patches_per_column if k in ("P", "PL") else 1.0)
+            h2d += b
+            if u != "in":
+                d2h += b
+    return h2d, d2h

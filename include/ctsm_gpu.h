@@ -249,6 +249,40 @@ int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds,
                               int32_t num_nolakec, const int32_t* filter_nolakec,
                               const ctsmg_soiltemp_io* io, double dtime);
 
+/* ---------------------------------------------------------------- batched resident mode */
+/* Many columns kept resident in HBM across model steps.  The reference has no
+ * counterpart object: it is the clump loop of src/main/clm_driver.F90:525-1346
+ * restricted to the three scoped calls, with state kept on the device.  Each
+ * step is SoilWater (ZD09), then SoilTemperature, then the between-step
+ * refresh h2osoi_vol = liq/(dz denh2o) + ice/(dz denice) on levels 1..nlevsoi
+ * that the driver makes in src/biogeophys/HydrologyNoDrainageMod.F90:580,590.
+ * Host arrays are dense (begc = begp = 1, ldc = ncol, ldp = npatch); columns
+ * are reordered on the device by (snl, nbedrock) so that warps see uniform
+ * level counts, and restored to the caller's order by ctsmg_batch_download. */
+typedef struct ctsmg_batch_s* ctsmg_batch;
+int32_t ctsmg_batch_create(ctsmg_batch* out, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
+                           int32_t ncol, int32_t npatch, double dtime, double e_ice,
+                           int32_t snow_thermal_cond_method);
+/* Enqueue nsteps steps (one CUDA graph replay each).  If step_ms is not NULL
+ * each step is timed with CUDA events on the batch's stream (synchronising). */
+int32_t ctsmg_batch_run(ctsmg_batch b, int32_t nsteps, float* step_ms);
+/* Wait for the batch's stream; returns CTSMG_E_SINGULAR with the column if a
+ * band solve failed in any step since creation. */
+int32_t ctsmg_batch_sync(ctsmg_batch b);
+/* Copy the resident state back into the caller's host arrays (caller order). */
+int32_t ctsmg_batch_download(ctsmg_batch b, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st);
+/* Time trial_steps steps for each candidate threads-per-block (64, 128, 256)
+ * on the batch's own data, keep the fastest, restore the state. */
+int32_t ctsmg_batch_autotune(ctsmg_batch b, int32_t trial_steps, int32_t* block_out);
+int32_t ctsmg_batch_set_block(ctsmg_batch b, int32_t block);
+int64_t ctsmg_batch_state_bytes(ctsmg_batch b);
+int32_t ctsmg_batch_destroy(ctsmg_batch b);
+
+/* ---------------------------------------------------------------- measurement */
+/* FP64 FMA throughput of the current GPU in TFLOP/s (a DFMA loop over every
+ * SM); the denominator of the FP64 roofline fraction.  No reference counterpart. */
+int32_t ctsmg_measure_fp64_tflops(double* tflops);
+
 #ifdef __cplusplus
 }
 #endif
