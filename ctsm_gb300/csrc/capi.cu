@@ -219,6 +219,11 @@ static int read_error(ThreadCtx* c, int* code, int* index, int* level) {
     return 0;
 }
 
+int current_snow_method() {
+    std::lock_guard<std::mutex> lk(g_mu);
+    return g_init ? g_opt.snow_thermal_cond_method : 0;
+}
+
 } // namespace ctsmg
 
 using namespace ctsmg;

@@ -18,4 +18,5 @@ int kind_levels(int kind);
 size_t field_bytes(const FieldDesc& f, int ldc, int ldp);
 int set_error(int code, const char* what, int index, int level);
 int check_filter(const ctsmg_bounds* b, int nf, const int32_t* filt);
+int current_snow_method();
 } // namespace ctsmg

@@ -15,7 +15,9 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include "ctsm_device.cuh"
+#include <mutex>
 #include "soil_kernels.cuh"
+#include "capi_internal.h"
 
 namespace ctsmg {
 
@@ -900,3 +902,115 @@ cudaError_t launch_permute(void* dst, const void* src, const int32_t* perm, int 
 }
 
 } // namespace ctsmg
+
+// ============================================================ allocation-free SoilTemperature
+// For callers that must not allocate device memory: the host model's device
+// memory is owned by another runtime (an OpenACC or OpenMP-offload build of the
+// Fortran host that keeps the derived types resident and budgets every byte of
+// device memory itself), or the caller runs where cudaMalloc is not acceptable
+// (cudaMalloc can synchronise the device, so latency-bound callers avoid it).
+// Such a caller passes device pointers for every input and output and this
+// entry point uses a fixed scratch array compiled into the library instead of
+// allocating one.  The array is sized for NOALLOC_MAX_COLUMNS columns (6 * 38
+// doubles each, 29.9 MB); every GPU that loads the library holds it until the
+// process exits.
+namespace ctsmg {
+constexpr int NOALLOC_MAX_COLUMNS = 16384;
+static __device__ __align__(256) double g_noalloc_ws[(size_t)SOILTEMP_WS_DOUBLES_PER_COL * NOALLOC_MAX_COLUMNS];
+static __device__ __align__(256) DevError g_noalloc_err;
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static std::mutex g_noalloc_mu;
+static double* g_noalloc_ws_addr[NOALLOC_MAX_DEVICES];
+static DevError* g_noalloc_err_addr[NOALLOC_MAX_DEVICES];
+
+// Same work as soiltemp_kernel, with the filter and patch indices checked on
+// the device (the caller's filter is in device memory, so the host cannot
+// check it without a staging copy): a bad index is recorded as CTSMG_E_ARG and
+// that column is skipped.
+__global__ void __launch_bounds__(128)
+soiltemp_noalloc_kernel(ctsmg_soiltemp_io io, int begc, int endc, int begp, int endp, int nfilt,
+                        const int32_t* __restrict__ filt, double dtime, int snow_method, double* ws,
+                        DevError* err) {
+    const int fc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fc >= nfilt) return;
+    const int cg = filt ? filt[fc] : begc + fc;
+    if (cg < begc || cg > endc) { report_error(err, fc + 1, 0, CTSMG_E_ARG); return; }
+    const int c = cg - begc;
+    const int snl = io.snl[c], pi = io.col_patchi[c], np = io.col_npatches[c];
+    if (snl > 0 || snl < -NLEVSNO || np < 0 || pi < begp || pi + np - 1 > endp) {
+        report_error(err, cg, 0, CTSMG_E_ARG);
+        return;
+    }
+    Scratch S{ws, NOALLOC_MAX_COLUMNS, fc};
+    int info = soiltemp_column(io, c, begp, dtime, snow_method, S);
+    if (info != 0) report_error(err, cg, info, CTSMG_E_SINGULAR);
+}
+
+// Looks up the device addresses of the scratch array and the error record
+// once per device, with that device current.
+static int noalloc_setup(int dev, double** ws, DevError** err) {
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+        return set_error(CTSMG_E_UNSUPPORTED, "device ordinal beyond the allocation-free table", dev, 0);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ws_addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_ws);
+        if (e != cudaSuccess) return set_error(CTSMG_E_CUDA, cudaGetErrorString(e), dev, 0);
+        void* q = nullptr;
+        e = cudaGetSymbolAddress(&q, g_noalloc_err);
+        if (e != cudaSuccess) return set_error(CTSMG_E_CUDA, cudaGetErrorString(e), dev, 0);
+        g_noalloc_ws_addr[dev] = static_cast<double*>(p);
+        g_noalloc_err_addr[dev] = static_cast<DevError*>(q);
+    }
+    *ws = g_noalloc_ws_addr[dev];
+    *err = g_noalloc_err_addr[dev];
+    return 0;
+}
+} // namespace ctsmg
+
+extern "C" int32_t ctsmg_soiltemperature_noalloc(const ctsmg_bounds* bounds, int32_t num_nolakec,
+                                                 const int32_t* filter_nolakec_dev,
+                                                 const ctsmg_soiltemp_io* io_dev, double dtime, void* stream) {
+    using namespace ctsmg;
+    if (!bounds || !io_dev) return set_error(CTSMG_E_ARG, "null bounds or io", 0, 0);
+    if (bounds->endc < bounds->begc || bounds->endp < bounds->begp - 1)
+        return set_error(CTSMG_E_ARG, "empty or inverted bounds", 0, 0);
+    if (num_nolakec < 0) return set_error(CTSMG_E_ARG, "negative filter length", 0, 0);
+    if (num_nolakec > NOALLOC_MAX_COLUMNS)
+        return set_error(CTSMG_E_ARG,
+                         "ctsmg_soiltemperature_noalloc: num_nolakec exceeds the built-in scratch "
+                         "(16384 columns); split the filter or use ctsmg_soiltemperature",
+                         num_nolakec, 0);
+    if (io_dev->ldc < bounds->endc - bounds->begc + 1 || io_dev->ldp < bounds->endp - bounds->begp + 1)
+        return set_error(CTSMG_E_ARG, "ldc/ldp smaller than the bounds", 0, 0);
+    if (!(dtime > 0.0)) return set_error(CTSMG_E_ARG, "dtime must be positive", 0, 0);
+    if (num_nolakec == 0) return 0;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_error(CTSMG_E_CUDA, cudaGetErrorString(e), 0, 0);
+    double* ws = nullptr;
+    DevError* err = nullptr;
+    int rc = noalloc_setup(dev, &ws, &err);
+    if (rc) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // the error record must start at "no error" (all ones) on every call
+    e = cudaMemsetAsync(err, 0xff, sizeof(DevError), s);
+    if (e != cudaSuccess) return set_error(CTSMG_E_CUDA, cudaGetErrorString(e), 0, 0);
+    soiltemp_noalloc_kernel<<<(num_nolakec + 127) / 128, 128, 0, s>>>(
+        *io_dev, bounds->begc, bounds->endc, bounds->begp, bounds->endp, num_nolakec, filter_nolakec_dev, dtime,
+        current_snow_method(), ws, err);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return set_error(CTSMG_E_CUDA, cudaGetErrorString(e), 0, 0);
+    DevError h;
+    e = cudaMemcpyAsync(&h, err, sizeof h, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return set_error(CTSMG_E_CUDA, cudaGetErrorString(e), 0, 0);
+    if (h.key != ~0ull) {
+        const int code = (int)(h.key & 0xff);
+        const int idx = (int)(h.key >> 32), lev = (int)((h.key >> 8) & 0xffffff) - 1024;
+        return set_error(code, code == CTSMG_E_SINGULAR ? "BandDiagonal ERROR: dgbsv returned error code"
+                                                        : "filter or patch index outside the bounds", idx, lev);
+    }
+    return 0;
+}

@@ -249,6 +249,23 @@ int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds,
                               int32_t num_nolakec, const int32_t* filter_nolakec,
                               const ctsmg_soiltemp_io* io, double dtime);
 
+/* Allocation-free SoilTemperature.  No counterpart in the reference: it is an
+ * extra entry point for callers that cannot allocate device memory -- a host
+ * whose device memory belongs to another runtime (an OpenACC or OpenMP-offload
+ * Fortran build that keeps the derived types resident and budgets device
+ * memory itself) or one that must not call cudaMalloc on this path.  Every
+ * pointer in io_dev and filter_nolakec_dev is DEVICE memory owned by the
+ * caller (filter NULL = begc..begc+num_nolakec-1); the call allocates nothing:
+ * the band-solve scratch is a fixed array inside the library, sized for at
+ * most 16384 columns per call (larger filters return CTSMG_E_ARG).  The first
+ * call on a device looks up that array's address (make it before any stream
+ * capture).  All calls share the one array, so calls that overlap on the GPU
+ * (other streams, other host threads) race: serialise them.  stream is a
+ * cudaStream_t (NULL = default stream); the call waits for it to finish. */
+int32_t ctsmg_soiltemperature_noalloc(const ctsmg_bounds* bounds, int32_t num_nolakec,
+                                      const int32_t* filter_nolakec_dev, const ctsmg_soiltemp_io* io_dev,
+                                      double dtime, void* stream);
+
 /* ---------------------------------------------------------------- batched resident mode */
 /* Many columns kept resident in HBM across model steps.  The reference has no
  * counterpart object: it is the clump loop of src/main/clm_driver.F90:525-1346
