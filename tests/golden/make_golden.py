@@ -1,0 +1,98 @@
+"""Regenerates the golden fixtures in this directory from the reference's own
+tests and technical-note tables (read as text; run in the build container,
+where the reference checkout is mounted at /root/reference):
+
+  layer_table_20sl.json  doc/source/tech_note/Ecosystem/CLM50_Tech_Note_Ecosystem.rst:164-219
+  skip_steps.json        src/biogeophys/test/Balance_test/test_Balance.pf:40-105
+  quadratic_kat.json     src/utils/test/quadratic_test/test_quadratic.pf
+  qsat_coeffs.json       src/biogeophys/QSatMod.F90:16-54
+
+    python tests/golden/make_golden.py [/root/reference]
+"""
+import json
+import os
+import re
+import sys
+
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def read(rel):
+    with open(os.path.join(REF, rel)) as f:
+        return f.read()
+
+
+def layer_table():
+    txt = read("doc/source/tech_note/Ecosystem/CLM50_Tech_Note_Ecosystem.rst")
+    start = txt.index(".. _Table Soil layer structure:")
+    rows = []
+    for line in txt[start:].splitlines():
+        m = re.match(r"\s*\|\s*(\d+)\s*\|\s*([\d.]+)\s*\|\s*([\d.]+)\s*\|\s*([\d.]+)\s*\|", line)
+        if m:
+            rows.append([int(m.group(1)), float(m.group(2)), float(m.group(3)), float(m.group(4))])
+        if len(rows) == 25:
+            break
+    return {"source": "CLM50_Tech_Note_Ecosystem.rst, Table Soil layer structure",
+            "columns": ["layer", "z", "dz", "zh"], "rows": rows, "decimals": 3}
+
+
+def skip_steps():
+    txt = read("src/biogeophys/test/Balance_test/test_Balance.pf")
+    cases = []
+    for block in txt.split("@Test")[1:]:
+        d = re.search(r"dtime\s*=\s*(\d+)", block)
+        a = re.search(r"@assertEqual\(\s*(\d+)\s*,\s*nskip", block)
+        if d and a:
+            cases.append([int(d.group(1)), int(a.group(1))])
+    return {"source": "test_Balance.pf", "skip_size_s": 3600.0, "cases": cases}
+
+
+def _arr(block, name):
+    m = re.search(name + r"\s*=\s*\(/(.*?)/\)", block, re.S)
+    return [float(x.replace("_r8", "").strip()) for x in m.group(1).split(",")]
+
+
+def quadratic():
+    txt = read("src/utils/test/quadratic_test/test_quadratic.pf")
+    sub = {m.group(1): m.group(2) for m in re.finditer(r"subroutine (\w+)\(this\)(.*?)end subroutine", txt, re.S)}
+    zr = sub["zero_root"]
+    sr = sub["simple_roots"]
+    return {
+        "source": "test_quadratic.pf",
+        "tol": 1e-15, "tol_big": 1e-6,
+        "zero_root": {"a": _arr(zr, r"\ba"), "b": 0.0, "c": 0.0, "r1": 0.0, "r2": 1e36},
+        "simple_roots": {"a": _arr(sr, r"\ba"), "b": _arr(sr, r"\bb"), "c": _arr(sr, r"\bc"),
+                         "r1": _arr(sr, "expectedr1"), "r2": _arr(sr, "expectedr2")},
+        "near_zero_sqrts": {"a": 1.0, "b": 4.0, "c": 4.0, "pert_eps": [0.0, 0.5, 2.0], "r1": -2.0},
+        "errors": [{"a": 0.0, "b": 0.0, "c": 0.0, "msg": "quadratic ERROR: Quadratic solution error"},
+                   {"a": 1.0, "b": 2.0, "c": 5.0,
+                    "msg": "quadratic ERROR: Quadratic solution error: b^2 - 4ac is negative"},
+                   {"a": 1.0, "b": 4.0, "c_plus_eps": 100.0,
+                    "msg": "quadratic ERROR: Quadratic solution error: b^2 - 4ac is negative"}],
+    }
+
+
+def qsat():
+    txt = read("src/biogeophys/QSatMod.F90")
+    out = {}
+    for name in ("a", "b", "c", "d"):
+        vals = []
+        for i in range(0, 9):
+            m = re.search(r"\b%s%d\s*=\s*([-+0-9.eE]+)_r8" % (name, i), txt)
+            if m:
+                vals.append(float(m.group(1)))
+        out[name] = vals
+    return {"source": "QSatMod.F90 (Flatau et al. 1992 coefficients)", "coeffs": out}
+
+
+def main():
+    for fname, fn in (("layer_table_20sl.json", layer_table), ("skip_steps.json", skip_steps),
+                      ("quadratic_kat.json", quadratic), ("qsat_coeffs.json", qsat)):
+        with open(os.path.join(OUT, fname), "w") as f:
+            json.dump(fn(), f, indent=1)
+        print("wrote", fname)
+
+
+if __name__ == "__main__":
+    main()
