@@ -23,6 +23,7 @@ LEVELS = {
     "S": (1, NLEVSOI),
     "SN": (-NLEVSNO + 1, NLEVSNO),
     "PL": (-NLEVSNO + 1, NLEVSNO + 1),    # patch, snow levels + top soil
+    "GR": (None, 1),                      # scalar per gridcell (1-D)
 }
 
 F64, I32 = "f8", "i4"
@@ -75,6 +76,31 @@ SOILTEMP_FIELDS = [
 ]
 
 
+_P_IN = ["elai", "esai", "htop", "emv", "fwet", "fdry", "laisun", "laisha", "btran", "sabv", "thm", "t_a10",
+         "parsun_z", "parsha_z", "vcmaxcintsun", "vcmaxcintsha"]
+_P_INOUT = ["displa", "z0mv", "t_veg", "liqcan", "snocan", "cgrnds", "cgrndl"]
+_P_OUT = ["z0hv", "z0qv", "forc_hgt_u_patch", "forc_hgt_t_patch", "forc_hgt_q_patch", "taf", "qaf", "ustar", "um",
+          "obu", "zeta", "ram1", "rah1", "raw1", "rah2", "raw2", "rb1", "uaf", "vpd", "rhaf",
+          "eflx_sh_veg", "qflx_evap_veg", "qflx_tran_veg", "eflx_sh_grnd", "eflx_sh_snow", "eflx_sh_soil",
+          "eflx_sh_h2osfc", "qflx_evap_soi", "qflx_ev_snow", "qflx_ev_soil", "qflx_ev_h2osfc",
+          "t_ref2m", "q_ref2m", "rh_ref2m", "vpd_ref2m", "dlrad", "ulrad", "t_skin", "cgrnd", "taux", "tauy",
+          "err_canopy", "rssun", "rssha", "psnsun", "psnsha", "lmrsun", "lmrsha", "cisun", "cisha", "gs_mol_sun",
+          "gs_mol_sha", "rh_leaf", "vpd_can", "u10_clm", "u10", "fv", "vds", "fm"]
+CANOPY_FIELDS = (
+    [("itype", "P", I32, "in"), ("patch_column", "P", I32, "in"), ("patch_gridcell", "P", I32, "in")] +
+    [(n, "GR", F64, "in") for n in ("forc_u", "forc_v", "forc_hgt_u", "forc_hgt_t", "forc_hgt_q", "forc_pco2",
+                                      "forc_po2", "dayl", "max_dayl")] +
+    [("snl", "C", I32, "in")] +
+    [(n, "C", F64, "in") for n in ("forc_pbot", "forc_th", "forc_q", "forc_rho", "forc_lwrad", "thv", "t_grnd",
+                                     "qg", "qg_snow", "qg_soil", "qg_h2osfc", "dqgdT", "emg", "htvp", "z0mg",
+                                     "snow_depth", "frac_sno_eff", "frac_h2osfc", "soilresis", "t_h2osfc")] +
+    [("t_soisno", "SS", F64, "in"), ("frac_veg_nosno", "P", I32, "in")] +
+    [(n, "P", F64, "in") for n in _P_IN] +
+    [(n, "P", F64, "inout") for n in _P_INOUT] +
+    [(n, "P", F64, "out") for n in _P_OUT] +
+    [("num_iter", "P", I32, "out")])
+
+
 def _ptr_type(dtype):
     return C.POINTER(C.c_double) if dtype == F64 else C.POINTER(C.c_int32)
 
@@ -102,19 +128,48 @@ class SoilTempIO(C.Structure):
                [(n, _ptr_type(t)) for (n, _, t, _) in SOILTEMP_FIELDS]
 
 
-def field_shape(kind, ncol, npatch):
+class CanopyParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "lai_dl", "z_dl", "a_coef", "a_exp", "csoilc", "cv", "wind_min", "zetamaxstable",
+        "kc25_coef", "ko25_coef", "cp25_yr2000", "kcha", "koha", "cpha",
+        "vcmaxha", "jmaxha", "tpuha", "lmrha", "vcmaxhd", "jmaxhd", "tpuhd", "lmrhd", "lmrse",
+        "vcmaxse_sf", "jmaxse_sf", "tpuse_sf", "jmax25top_sf",
+        "fnr", "act25", "theta_psii", "theta_ip", "tpu25ratio", "kp25ratio", "fnps", "leaf_mr_vcm")] + \
+        [("light_inhibit", C.c_int32)]
+
+
+MAX_PFT = 80
+
+
+class Pftcon(C.Structure):
+    _fields_ = [("npft", C.c_int32)] + [(n, C.c_double * MAX_PFT) for n in (
+        "c3psn", "slatop", "leafcn", "flnr", "fnitr", "dleaf", "medlynslope", "medlynintercept", "theta_cj",
+        "mbbopt")]
+
+
+class CanopyIO(C.Structure):
+    _fields_ = [("ldp", C.c_int32), ("ldc", C.c_int32), ("ldg", C.c_int32), ("begg", C.c_int32)] + \
+               [(n, _ptr_type(t)) for (n, _, t, _) in CANOPY_FIELDS]
+
+
+def field_shape(kind, ncol, npatch, ngrid=None):
     """numpy shape (levels, columns-or-patches) of a manifest field."""
+    if kind == "GR":
+        return (ngrid if ngrid is not None else ncol,)
     n = npatch if kind in ("P", "PL") else ncol
     nlev = LEVELS[kind][1]
     return (n,) if kind in ("C", "P") else (nlev, n)
 
 
-def make_io(cls, fields, arrays, ldc, ldp=None):
+def make_io(cls, fields, arrays, ldc, ldp=None, ldg=None, begg=1):
     """Fill a ctypes io struct with pointers into the numpy arrays of `arrays`."""
     io = cls()
     io.ldc = ldc
     if ldp is not None:
         io.ldp = ldp
+    if ldg is not None:
+        io.ldg = ldg
+        io.begg = begg
     for (n, _, t, _) in fields:
         a = arrays[n]
         assert a.flags.c_contiguous, n

@@ -1,0 +1,40 @@
+"""Host-side mirror of the reference's CanopyFluxes interface (one dict of
+numpy arrays stands for the derived types; every call goes through the C-ABI
+of libctsm_gpu.so)."""
+import ctypes as C
+
+import numpy as np
+
+from . import abi, canopy_inputs
+from ._lib import load, check
+
+
+def _bind(L):
+    if getattr(L, "_canopy_bound", False):
+        return
+    L.ctsmg_set_canopy_params.argtypes = [C.POINTER(abi.CanopyParams), C.POINTER(abi.Pftcon)]
+    L.ctsmg_canopyfluxes.argtypes = [C.POINTER(abi.Bounds), C.c_int32, C.POINTER(C.c_int32),
+                                     C.POINTER(abi.CanopyIO), C.c_double]
+    L._canopy_bound = True
+
+
+def set_params(params=None, pftcon=None):
+    """ctsmg_set_canopy_params: readParams of CanopyFluxesMod / PhotosynthesisMod
+    and the pftcon arrays (defaults: ctsm_gb300.canopy_inputs)."""
+    L = load()
+    _bind(L)
+    p = params if params is not None else canopy_inputs.make_params()
+    f = pftcon if pftcon is not None else canopy_inputs.make_pftcon()
+    check(L.ctsmg_set_canopy_params(C.byref(p), C.byref(f)))
+
+
+def CanopyFluxes(bounds, num_exposedvegp, filter_exposedvegp, state, dtime, ngrid, begg=1):
+    """CanopyFluxes (CanopyFluxesMod.F90:191) over the exposed-vegetation filter."""
+    L = load()
+    _bind(L)
+    f = np.ascontiguousarray(filter_exposedvegp, dtype=np.int32)
+    ncol = bounds.endc - bounds.begc + 1
+    npat = bounds.endp - bounds.begp + 1
+    io = abi.make_io(abi.CanopyIO, abi.CANOPY_FIELDS, state, ncol, npat, ngrid, begg)
+    check(L.ctsmg_canopyfluxes(C.byref(bounds), int(num_exposedvegp), f.ctypes.data_as(C.POINTER(C.c_int32)),
+                               C.byref(io), float(dtime)))

@@ -1,0 +1,753 @@
+// canopy_kernels.cu -- sm_103a FP64 kernel for CanopyFluxes (leaf temperature
+// / Monin-Obukhov stability iteration) with Photosynthesis sun + shade.
+//
+// One thread owns one patch at a time.  The reference removes converged
+// patches from its filter after every pass (CanopyFluxesMod.F90:1448-1456);
+// here a lane whose patch has converged (or reached itmax) finalises it and
+// takes the next patch from a global work counter, then rejoins the warp for
+// the next pass.  The pass body -- FrictionVelocity, the resistances, two
+// Photosynthesis calls and the energy-balance Newton step -- is therefore
+// executed with the warp's lanes on different patches but the same code,
+// which is the GPU form of the reference's filter compaction.  Per-patch
+// results do not depend on which lane or pass slot served them.
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "ctsm_device.cuh"
+#include "canopy_kernels.cuh"
+
+namespace ctsmg {
+namespace canopy {
+
+constexpr double PI = 3.14159265358979323846;
+constexpr double VKC = 0.4;
+constexpr double CPAIR = 1.00464e3;
+constexpr double HVAP = 2.501e6;
+constexpr double RGAS = 6.02214e26 * 1.38065e-23;
+constexpr double NU_PARAM = 1.5e-5;
+constexpr double TLSAI_CRIT = 2.0;
+
+__device__ __forceinline__ double ipow4(double x) { double x2 = x * x; return x2 * x2; }
+__device__ __forceinline__ double ipow3(double x) { double x2 = x * x; return x2 * x; }
+
+struct Err { int code, idx; };
+__device__ __forceinline__ void flag(Err& e, int code, int idx) { if (!e.code) { e.code = code; e.idx = idx; } }
+
+// QSatMod.F90:61-127
+__device__ void qsat(double T, double p, double& qs, double& es, double* qsdT) {
+    double td = fmin(100.0, fmax(-75.0, T - TFRZ));
+    double esl;
+    if (td >= 0.0)
+        esl = 6.11213476 + td * (0.444007856 + td * (0.143064234e-01 + td * (0.264461437e-03 + td * (0.305903558e-05 +
+              td * (0.196237241e-07 + td * (0.892344772e-10 + td * (-0.373208410e-12 + td * 0.209339997e-15)))))));
+    else
+        esl = 6.11123516 + td * (0.503109514 + td * (0.188369801e-01 + td * (0.420547422e-03 + td * (0.614396778e-05 +
+              td * (0.602780717e-07 + td * (0.387940929e-09 + td * (0.149436277e-11 + td * 0.262655803e-14)))))));
+    esl = esl * 100.0;
+    const double vp = 1.0 / (p - 0.378 * esl);
+    const double vp1 = 0.622 * vp;
+    qs = esl * vp1;
+    es = esl;
+    if (qsdT) {
+        double esdT;
+        if (td >= 0.0)
+            esdT = 0.444017302 + td * (0.286064092e-01 + td * (0.794683137e-03 + td * (0.121211669e-04 + td * (0.103354611e-06 +
+                   td * (0.404125005e-09 + td * (-0.788037859e-12 + td * (-0.114596802e-13 + td * 0.381294516e-16)))))));
+        else
+            esdT = 0.503277922 + td * (0.377289173e-01 + td * (0.126801703e-02 + td * (0.249468427e-04 + td * (0.313703411e-06 +
+                   td * (0.257180651e-08 + td * (0.133268878e-10 + td * (0.394116744e-13 + td * 0.498070196e-16)))))));
+        esdT = esdT * 100.0;
+        *qsdT = esdT * (vp1 * vp) * p;
+    }
+}
+
+// quadraticMod.F90:17-74
+__device__ __forceinline__ bool quadratic(double a, double b, double c, double& r1, double& r2) {
+    if (a == 0.0) { r1 = r2 = 0.0; return false; }
+    double root = b * b - 4.0 * a * c;
+    if (root < 0.0) {
+        if (-root < 3.0 * 2.220446049250313e-16) root = 0.0;
+        else { r1 = r2 = 0.0; return false; }
+    }
+    const double q = (b >= 0.0) ? -0.5 * (b + sqrt(root)) : -0.5 * (b - sqrt(root));
+    r1 = q / a;
+    r2 = (q != 0.0) ? c / q : 1.e36;
+    return true;
+}
+
+// FrictionVelocityMod.F90:1120-1155
+__device__ __forceinline__ double stab1(double zeta) {
+    const double chik2 = sqrt(1.0 - 16.0 * zeta);
+    const double chik = sqrt(chik2);
+    return 2.0 * log((1.0 + chik) * 0.5) + log((1.0 + chik2) * 0.5) - 2.0 * atan(chik) + PI * 0.5;
+}
+__device__ __forceinline__ double stab2(double zeta) {
+    return 2.0 * log((1.0 + sqrt(1.0 - 16.0 * zeta)) * 0.5);
+}
+
+struct PsnState { double ac, aj, ap, ag, an, gs_mol; };
+struct PsnCtx {
+    bool c3;
+    double vcmax_z, cp, kc, ko, qe, tpu_z, kp_z, theta_cj, theta_ip, forc_pbot, medlynslope, medlynintercept;
+    double bbb, mbb;
+    int method;
+    double gb_mol, je, cair, oair, lmr_z, par_z, rh_can;
+};
+
+// PhotosynthesisMod.F90:2564-2701
+__device__ double ci_func(double ci, const PsnCtx& x, PsnState& s, Err& e, int pidx) {
+    double r1, r2;
+    if (x.c3) {
+        s.ac = x.vcmax_z * fmax(ci - x.cp, 0.0) / (ci + x.kc * (1.0 + x.oair / x.ko));
+        s.aj = x.je * fmax(ci - x.cp, 0.0) / (4.0 * ci + 8.0 * x.cp);
+        s.ap = 3.0 * x.tpu_z;
+    } else {
+        s.ac = x.vcmax_z;
+        s.aj = x.qe * x.par_z * 4.6;
+        s.ap = x.kp_z * fmax(ci, 0.0) / x.forc_pbot;
+    }
+    if (!quadratic(x.theta_cj, -(s.ac + s.aj), s.ac * s.aj, r1, r2)) flag(e, CTSMG_E_DISCRIMINANT, pidx);
+    const double ai = fmin(r1, r2);
+    if (!quadratic(x.theta_ip, -(ai + s.ap), ai * s.ap, r1, r2)) flag(e, CTSMG_E_DISCRIMINANT, pidx);
+    s.ag = fmax(0.0, fmin(r1, r2));
+    s.an = s.ag - x.lmr_z;
+    if (s.an < 0.0) return 0.0;
+    double cs = x.cair - 1.4 / x.gb_mol * s.an * x.forc_pbot;
+    cs = fmax(cs, 1.e-06);
+    if (x.method == 1) {
+        const double term = 1.6 * s.an / (cs / x.forc_pbot * 1.e06);
+        const double st = x.medlynslope * term;
+        const double bquad = -(2.0 * (x.medlynintercept * 1.e-06 + term) + st * st / (x.gb_mol * 1.e-06 * x.rh_can));
+        const double cquad = x.medlynintercept * x.medlynintercept * 1.e-12 +
+                             (2.0 * x.medlynintercept * 1.e-06 + term * (1.0 - x.medlynslope * x.medlynslope / x.rh_can)) * term;
+        if (!quadratic(1.0, bquad, cquad, r1, r2)) flag(e, CTSMG_E_DISCRIMINANT, pidx);
+        s.gs_mol = fmax(r1, r2) * 1.e06;
+    } else {
+        const double bquad = cs * (x.gb_mol - x.bbb) - x.mbb * s.an * x.forc_pbot;
+        const double cquad = -x.gb_mol * (cs * x.bbb + x.mbb * s.an * x.forc_pbot * x.rh_can);
+        if (!quadratic(cs, bquad, cquad, r1, r2)) flag(e, CTSMG_E_DISCRIMINANT, pidx);
+        s.gs_mol = fmax(r1, r2);
+    }
+    return ci - x.cair + s.an * x.forc_pbot * (1.4 * s.gs_mol + 1.6 * x.gb_mol) / (x.gb_mol * s.gs_mol);
+}
+
+// PhotosynthesisMod.F90:2371-2485
+__device__ double brent(double x1, double x2, double f1, double f2, double tol, const PsnCtx& ctx, PsnState& st,
+                        Err& err, int pidx) {
+    const double eps = 1.e-2;
+    double a = x1, b = x2, fa = f1, fb = f2;
+    if ((fa > 0.0 && fb > 0.0) || (fa < 0.0 && fb < 0.0)) { flag(err, CTSMG_E_NOT_BRACKETED, pidx); return b; }
+    double c = b, fc = fb, d = 0.0, e = 0.0;
+#pragma unroll 1
+    for (int iter = 0; iter < 20; ++iter) {
+        if ((fb > 0.0 && fc > 0.0) || (fb < 0.0 && fc < 0.0)) { c = a; fc = fa; d = b - a; e = d; }
+        if (fabs(fc) < fabs(fb)) { a = b; b = c; c = a; fa = fb; fb = fc; fc = fa; }
+        const double tol1 = 2.0 * eps * fabs(b) + 0.5 * tol;
+        const double xm = 0.5 * (c - b);
+        if (fabs(xm) <= tol1 || fb == 0.) return b;
+        if (fabs(e) >= tol1 && fabs(fa) > fabs(fb)) {
+            const double s = fb / fa;
+            double p, q;
+            if (a == c) {
+                p = 2.0 * xm * s;
+                q = 1.0 - s;
+            } else {
+                q = fa / fc;
+                const double r = fb / fc;
+                p = s * (2.0 * xm * q * (q - r) - (b - a) * (r - 1.0));
+                q = (q - 1.0) * (r - 1.0) * (s - 1.0);
+            }
+            if (p > 0.0) q = -q;
+            p = fabs(p);
+            if (2.0 * p < fmin(3.0 * xm * q - fabs(tol1 * q), fabs(e * q))) { e = d; d = p / q; }
+            else { d = xm; e = d; }
+        } else {
+            d = xm;
+            e = d;
+        }
+        a = b;
+        fa = fb;
+        if (fabs(d) > tol1) b = b + d;
+        else b = b + copysign(fabs(tol1), xm);
+        fb = ci_func(b, ctx, st, err, pidx);
+        if (fb == 0.0) break;
+    }
+    return b;
+}
+
+// PhotosynthesisMod.F90:2251-2368
+__device__ void hybrid(double x0, const PsnCtx& ctx, PsnState& st, Err& err, int pidx) {
+    const double eps = 1.e-2, eps1 = 1.e-4;
+    double f0 = ci_func(x0, ctx, st, err, pidx);
+    if (f0 == 0.0) return;
+    double minx = x0, minf = f0;
+    double x1 = x0 * 0.99;
+    double f1 = ci_func(x1, ctx, st, err, pidx);
+    if (f1 == 0.0) return;
+    if (f1 < minf) { minx = x1; minf = f1; }
+#pragma unroll 1
+    for (int iter = 1;; ++iter) {
+        const double dx = -f1 * (x1 - x0) / (f1 - f0);
+        const double x = x1 + dx;
+        const double tol = fabs(x) * eps;
+        if (fabs(dx) < tol) return;
+        x0 = x1;
+        f0 = f1;
+        x1 = x;
+        f1 = ci_func(x1, ctx, st, err, pidx);
+        if (f1 < minf) { minx = x1; minf = f1; }
+        if (fabs(f1) <= eps1) return;
+        if (f1 * f0 < 0.0) { brent(x0, x1, f0, f1, tol, ctx, st, err, pidx); return; }
+        if (iter > 40) { ci_func(minx, ctx, st, err, pidx); return; }
+    }
+}
+
+__device__ __forceinline__ double ft(double tl, double ha) {
+    return exp(ha / (RGAS * 1.e-3 * (TFRZ + 25.0)) * (1.0 - (TFRZ + 25.0) / tl));
+}
+__device__ __forceinline__ double fth(double tl, double hd, double se, double sf) {
+    return sf / (1.0 + exp((-hd + se * tl) / (RGAS * 1.e-3 * tl)));
+}
+__device__ __forceinline__ double fth25(double hd, double se) {
+    return 1.0 + exp((-hd + se * (TFRZ + 25.0)) / (RGAS * 1.e-3 * (TFRZ + 25.0)));
+}
+
+struct PhaseOut { double rs, psn, lmr, ci, gs_mol_phase; };
+
+// PhotosynthesisMod.F90:1243-2062, one phase, nlevcan = nrad = 1
+__device__ PhaseOut photosynthesis(const CanopyArgs& A, int pidx, int ivt, double t_veg, double t10, double tgcm,
+                                   double forc_pbot, double esat_tv, double eair, double oair, double cair, double rb,
+                                   double btran, double dayl_factor, double par_z, double lai_z, double vcmaxcint,
+                                   PsnState& st, double& vpd_can, double& rh_leaf, Err& err) {
+    const ctsmg_canopy_params& P = A.par;
+    const ctsmg_pftcon& F = A.pft;
+    const int method = A.method;
+    const bool c3 = (llround(F.c3psn[ivt]) == 1);
+    const double qe = c3 ? 0.0 : 0.05;
+    double bbb = 0.0, mbb = 0.0;
+    if (method == 0) { bbb = fmax((c3 ? 10000.0 : 40000.0) * btran, 1.0); mbb = F.mbbopt[ivt]; }
+    const double kc = P.kc25_coef * forc_pbot * ft(t_veg, P.kcha);
+    const double ko = P.ko25_coef * forc_pbot * ft(t_veg, P.koha);
+    const double sco = 0.5 * 0.209 / P.cp25_yr2000;
+    const double cp = 0.5 * oair / sco * ft(t_veg, P.cpha);
+    const double lnc = 1.0 / (F.slatop[ivt] * F.leafcn[ivt]);
+    double vcmax25top = lnc * F.flnr[ivt] * P.fnr * P.act25 * dayl_factor;
+    vcmax25top = vcmax25top * F.fnitr[ivt];
+    const double t10c = fmin(fmax((t10 - TFRZ), 11.0), 35.0);
+    const double jmax25top = ((2.59 - 0.035 * t10c) * vcmax25top) * P.jmax25top_sf;
+    const double nscaler = vcmaxcint;
+    const double lmr25 = (c3 ? vcmax25top * P.leaf_mr_vcm : vcmax25top * 0.025) * nscaler;
+    double lmr_z;
+    if (c3) {
+        lmr_z = lmr25 * ft(t_veg, P.lmrha) * fth(t_veg, P.lmrhd, P.lmrse, fth25(P.lmrhd, P.lmrse));
+    } else {
+        lmr_z = lmr25 * pow(2.0, (t_veg - (TFRZ + 25.0)) / 10.0);
+        lmr_z = lmr_z / (1.0 + exp(1.3 * (t_veg - (TFRZ + 55.0))));
+    }
+    double vcmax_z = 0.0, jmax_z = 0.0, tpu_z = 0.0, kp_z = 0.0;
+    if (par_z > 0.0) {
+        const double vcmax25 = vcmax25top * nscaler, jmax25 = jmax25top * nscaler;
+        const double tpu25 = P.tpu25ratio * vcmax25top * nscaler, kp25 = P.kp25ratio * vcmax25top * nscaler;
+        const double vcmaxse = (668.39 - 1.07 * t10c) * P.vcmaxse_sf;
+        const double jmaxse = (659.70 - 0.75 * t10c) * P.jmaxse_sf;
+        const double tpuse = (668.39 - 1.07 * t10c) * P.tpuse_sf;
+        if (c3) {
+            vcmax_z = vcmax25 * ft(t_veg, P.vcmaxha) * fth(t_veg, P.vcmaxhd, vcmaxse, fth25(P.vcmaxhd, vcmaxse));
+        } else {
+            vcmax_z = vcmax25 * pow(2.0, (t_veg - (TFRZ + 25.0)) / 10.0);
+            vcmax_z = vcmax_z / (1.0 + exp(0.2 * ((TFRZ + 15.0) - t_veg)));
+            vcmax_z = vcmax_z / (1.0 + exp(0.3 * (t_veg - (TFRZ + 40.0))));
+        }
+        jmax_z = jmax25 * ft(t_veg, P.jmaxha) * fth(t_veg, P.jmaxhd, jmaxse, fth25(P.jmaxhd, jmaxse));
+        tpu_z = tpu25 * ft(t_veg, P.tpuha) * fth(t_veg, P.tpuhd, tpuse, fth25(P.tpuhd, tpuse));
+        kp_z = kp25 * pow(2.0, (t_veg - (TFRZ + 25.0)) / 10.0);
+    }
+    vcmax_z = vcmax_z * btran;
+    lmr_z = lmr_z * btran;
+    if (P.light_inhibit && par_z > 0.0) lmr_z = lmr_z * 0.67;
+
+    const double rsmax0 = 2.e4;
+    const double cf = forc_pbot / (RGAS * 1.e-3 * tgcm) * 1.e06;
+    const double gb_mol = 1.0 / rb * cf;
+    PhaseOut out;
+    double rs_z, psn_z, ci_z;
+    if (par_z <= 0.0) {
+        st.ac = st.aj = st.ap = st.ag = 0.0;
+        st.an = 0.0 - lmr_z;
+        psn_z = 0.0;
+        rs_z = (method == 0) ? fmin(rsmax0, 1.0 / bbb * cf) : fmin(rsmax0, 1.0 / F.medlynintercept[ivt] * cf);
+        ci_z = 0.0;
+        rh_leaf = 0.0;
+        out.gs_mol_phase = cf / rs_z;
+    } else {
+        const double ceair = fmin(eair, esat_tv);
+        double rh_can;
+        if (method == 0) {
+            rh_can = ceair / esat_tv;
+        } else {
+            rh_can = fmax((esat_tv - ceair), 50.0) * 0.001;
+            vpd_can = rh_can;
+        }
+        const double qabs = 0.5 * (1.0 - P.fnps) * par_z * 4.6;
+        double r1, r2;
+        if (!quadratic(P.theta_psii, -(qabs + jmax_z), qabs * jmax_z, r1, r2)) flag(err, CTSMG_E_DISCRIMINANT, pidx);
+        PsnCtx ctx{c3, vcmax_z, cp, kc, ko, qe, tpu_z, kp_z, F.theta_cj[ivt], P.theta_ip, forc_pbot,
+                   F.medlynslope[ivt], F.medlynintercept[ivt], bbb, mbb, method, gb_mol, fmin(r1, r2), cair, oair,
+                   lmr_z, par_z, rh_can};
+        hybrid(c3 ? 0.7 * cair : 0.4 * cair, ctx, st, err, pidx);
+        if (st.an < 0.0) st.gs_mol = (method == 0) ? bbb : F.medlynintercept[ivt];
+        out.gs_mol_phase = st.gs_mol;
+        ci_z = cair - st.an * forc_pbot * (1.4 * st.gs_mol + 1.6 * gb_mol) / (gb_mol * st.gs_mol);
+        ci_z = fmax(ci_z, 1.e-06);
+        rs_z = fmin(1.0 / (st.gs_mol / cf), rsmax0);
+        psn_z = st.ag;
+        if (st.gs_mol < 0.0) flag(err, CTSMG_E_ARG, pidx);
+        if (method == 0) rh_leaf = (gb_mol * ceair + st.gs_mol * esat_tv) / ((gb_mol + st.gs_mol) * esat_tv);
+    }
+    if (lai_z > 0.0) {
+        out.psn = psn_z * lai_z / lai_z;
+        out.lmr = lmr_z * lai_z / lai_z;
+        out.rs = lai_z / (lai_z / (rb + rs_z)) - rb;
+    } else {
+        out.psn = 0.0; out.lmr = 0.0; out.rs = 0.0;
+    }
+    out.ci = ci_z;
+    return out;
+}
+
+// everything one patch carries from pass to pass
+struct Patch {
+    int p, c, g, ivt, itlef, nmozsgn, num_iter;
+    double displa, z0mv, hgt_u, hgt_t, hgt_q, zldis, ur, um, obu, obuold, fm;
+    double t_veg, tl_ini, qsatl, el, qsatldT, taf, qaf, dth, dqh, delq;
+    double del, efeb, air, bir, cir, dayl_factor, liqcan, snocan;
+    // last-pass values used after the iteration
+    double tlbef, dt_veg, err, eflx_sh_veg, qflx_evap_veg, qflx_tran_veg, lw_leaf, zeta;
+    double ustar, temp1, temp2, temp12m, temp22m, ram1, rah_a, raw_a, rah_b, uaf, rb;
+    double wtl0, wta0, wtg, wtal, wtgq, wtlq0, wtaq0, wtalq, efe;
+    double u10_clm, u10, vds, vpd_can, rh_leaf, rhaf_last, vpd_last;
+    PhaseOut sun, sha;
+    PsnState st;
+};
+
+__device__ void friction_velocity(const Patch& s, int iter, double& fm, double& ustar, double& temp1, double& temp2,
+                                  double& temp12m, double& temp22m, double& u10_clm, double& u10, double& vds) {
+    const double zetam = 1.574, zetat = 0.465;
+    const double obu = s.obu, z0m = s.z0mv, um = s.um;
+    double zldis = s.hgt_u - s.displa;
+    double zeta = zldis / obu;
+    if (zeta < -zetam)
+        ustar = VKC * um / (log(-zetam * obu / z0m) - stab1(-zetam) + stab1(z0m / obu) +
+                            1.14 * (pow(-zeta, 0.333) - pow(zetam, 0.333)));
+    else if (zeta < 0.0)
+        ustar = VKC * um / (log(zldis / z0m) - stab1(zeta) + stab1(z0m / obu));
+    else if (zeta <= 1.0)
+        ustar = VKC * um / (log(zldis / z0m) + 5.0 * zeta - 5.0 * z0m / obu);
+    else
+        ustar = VKC * um / (log(obu / z0m) + 5.0 - 5.0 * z0m / obu + (5.0 * log(zeta) + zeta - 1.0));
+    vds = (zeta < 0.0) ? 2.e-3 * ustar * (1.0 + pow(300.0 / (-obu), 0.666)) : 2.e-3 * ustar;
+    if (zldis - z0m <= 10.0) {
+        u10_clm = um;
+    } else {
+        const double z10 = 10.0 + z0m;
+        if (zeta < -zetam)
+            u10_clm = um - (ustar / VKC * (log(-zetam * obu / z10) - stab1(-zetam) + stab1(z10 / obu) +
+                                            1.14 * (pow(-zeta, 0.333) - pow(zetam, 0.333))));
+        else if (zeta < 0.0)
+            u10_clm = um - (ustar / VKC * (log(zldis / z10) - stab1(zeta) + stab1(z10 / obu)));
+        else if (zeta <= 1.0)
+            u10_clm = um - (ustar / VKC * (log(zldis / z10) + 5.0 * zeta - 5.0 * z10 / obu));
+        else
+            u10_clm = um - (ustar / VKC * (log(obu / z10) + 5.0 - 5.0 * z10 / obu + (5.0 * log(zeta) + zeta - 1.0)));
+    }
+    auto tprof = [&](double zl, double z0) {
+        const double zt = zl / obu;
+        if (zt < -zetat)
+            return VKC / (log(-zetat * obu / z0) - stab2(-zetat) + stab2(z0 / obu) +
+                          0.8 * (pow(zetat, -0.333) - pow(-zt, -0.333)));
+        else if (zt < 0.0)
+            return VKC / (log(zl / z0) - stab2(zt) + stab2(z0 / obu));
+        else if (zt <= 1.0)
+            return VKC / (log(zl / z0) + 5.0 * zt - 5.0 * z0 / obu);
+        return VKC / (log(obu / z0) + 5.0 - 5.0 * z0 / obu + (5.0 * log(zt) + zt - 1.0));
+    };
+    temp1 = tprof(s.hgt_t - s.displa, s.z0mv);
+    temp2 = (s.hgt_q == s.hgt_t) ? temp1 : tprof(s.hgt_q - s.displa, s.z0mv);   // z0qv == z0hv here
+    temp12m = tprof(2.0 + s.z0mv, s.z0mv);
+    temp22m = temp12m;
+    double fmnew;
+    if (fmin(zeta, 1.0) < 0.0) {
+        const double tmp1 = pow(1.0 - 16.0 * fmin(zeta, 1.0), 0.25);
+        fmnew = 2.0 * log((1.0 + tmp1) / 2.0) + log((1.0 + tmp1 * tmp1) / 2.0) - 2.0 * atan(tmp1) + 1.5707963;
+    } else {
+        fmnew = -5.0 * fmin(zeta, 1.0);
+    }
+    fm = (iter == 1) ? fmnew : 0.5 * (fm + fmnew);
+    double zeta10 = fmin(10.0 / obu, 1.0);
+    if (zeta == 0.0) zeta10 = 0.0;
+    double fm10;
+    if (zeta10 < 0.0) {
+        const double tmp1 = pow(1.0 - 16.0 * zeta10, 0.25);
+        fm10 = 2.0 * log((1.0 + tmp1) / 2.0) + log((1.0 + tmp1 * tmp1) / 2.0) - 2.0 * atan(tmp1) + 1.5707963;
+    } else {
+        fm10 = -5.0 * zeta10;
+    }
+    u10 = s.ur - ustar / VKC * (log(fmax(1.0, s.hgt_u / 10.0)) - fm + fm10);
+}
+
+// initialisation before the iteration (CanopyFluxesMod.F90:642-1025)
+__device__ void setup(const CanopyArgs& A, Patch& s, int p, Err& err) {
+    const ctsmg_canopy_io& io = A.io;
+    s.p = p;
+    s.c = io.patch_column[p] - A.begc;
+    s.g = io.patch_gridcell[p] - io.begg;
+    s.ivt = io.itype[p];
+    const int c = s.c, g = s.g;
+    const double elai = io.elai[p], esai = io.esai[p], emv = io.emv[p], emg = io.emg[c];
+    s.del = 0.0; s.efeb = 0.0; s.obuold = 0.0;
+    s.wtgq = 0.0; s.wtlq0 = 0.0; s.wtaq0 = 0.0; s.wtalq = 0.0;
+    s.dayl_factor = fmin(1.0, fmax(0.01, (io.dayl[g] * io.dayl[g]) / (io.max_dayl[g] * io.max_dayl[g])));
+    io.rb1[p] = 0.0;
+    const double lt = fmin(elai + esai, TLSAI_CRIT);
+    const double egvf = (1.0 - exp(-lt)) / (1.0 - exp(-TLSAI_CRIT));
+    s.displa = egvf * io.displa[p];
+    s.z0mv = exp(egvf * log(io.z0mv[p]) + (1.0 - egvf) * log(io.z0mg[c]));
+    s.hgt_u = io.forc_hgt_u[g] + s.z0mv + s.displa;
+    s.hgt_t = io.forc_hgt_t[g] + s.z0mv + s.displa;
+    s.hgt_q = io.forc_hgt_q[g] + s.z0mv + s.displa;
+    s.air = emv * (1.0 + (1.0 - emv) * (1.0 - emg)) * io.forc_lwrad[c];
+    s.bir = -(2.0 - emv * (1.0 - emg)) * emv * SB;
+    s.cir = emv * emg * SB;
+    s.t_veg = io.t_veg[p];
+    qsat(s.t_veg, io.forc_pbot[c], s.qsatl, s.el, &s.qsatldT);
+    s.nmozsgn = 0;
+    const double thm = io.thm[p], forc_q = io.forc_q[c], qg = io.qg[c];
+    s.taf = (io.t_grnd[c] + thm) / 2.0;
+    s.qaf = (forc_q + qg) / 2.0;
+    s.ur = fmax(A.par.wind_min, sqrt(io.forc_u[g] * io.forc_u[g] + io.forc_v[g] * io.forc_v[g]));
+    s.dth = thm - s.taf;
+    s.dqh = forc_q - s.qaf;
+    s.delq = qg - s.qaf;
+    const double dthv = s.dth * (1.0 + 0.61 * forc_q) + 0.61 * io.forc_th[c] * s.dqh;
+    s.zldis = s.hgt_u - s.displa;
+    if (s.zldis < 0.0) flag(err, CTSMG_E_FORCING_HEIGHT, p + A.begp);
+    const double thv = io.thv[c];
+    s.um = (dthv >= 0.0) ? fmax(s.ur, 0.1) : sqrt(s.ur * s.ur + 0.5 * 0.5);
+    const double rib = GRAV * s.zldis * dthv / (thv * s.um * s.um);
+    double zeta;
+    if (rib >= 0.0) {
+        zeta = rib * log(s.zldis / s.z0mv) / (1.0 - 5.0 * fmin(rib, 0.19));
+        zeta = fmin(A.par.zetamaxstable, fmax(zeta, 0.01));
+    } else {
+        zeta = rib * log(s.zldis / s.z0mv);
+        zeta = fmax(-100.0, fmin(zeta, -0.01));
+    }
+    s.obu = s.zldis / zeta;
+    s.num_iter = 0;
+    s.tl_ini = s.t_veg;
+    s.liqcan = io.liqcan[p];
+    s.snocan = io.snocan[p];
+    s.fm = 0.0;
+    s.itlef = 0;
+    s.st = PsnState{0, 0, 0, 0, 0, 0};
+    s.vpd_can = 0.0;
+    s.rh_leaf = 0.0;
+}
+
+// one pass of the stability iteration (CanopyFluxesMod.F90:1028-1456);
+// returns true when the patch leaves the iteration
+__device__ bool pass(const CanopyArgs& A, Patch& s, Err& err, double dtime) {
+    const ctsmg_canopy_io& io = A.io;
+    const ctsmg_canopy_params& P = A.par;
+    const int p = s.p, c = s.c, g = s.g;
+    const int pg = p + A.begp;
+    friction_velocity(s, s.itlef + 1, s.fm, s.ustar, s.temp1, s.temp2, s.temp12m, s.temp22m, s.u10_clm, s.u10, s.vds);
+    const double ustar = s.ustar;
+    s.tlbef = s.t_veg;
+    const double del2 = s.del;
+    s.ram1 = 1.0 / (ustar * ustar / s.um);
+    s.rah_a = 1.0 / (s.temp1 * ustar);
+    s.raw_a = 1.0 / (s.temp2 * ustar);
+    s.uaf = s.um * sqrt(1.0 / (s.ram1 * s.um));
+    const double elai = io.elai[p], esai = io.esai[p];
+    const double cfl = P.cv / (sqrt(s.uaf) * sqrt(A.pft.dleaf[s.ivt]));
+    s.rb = 1.0 / (cfl * s.uaf);
+    const double rb = s.rb;
+    const double w = exp(-(elai + esai));
+    const double csoilb = VKC / (P.a_coef * pow(io.z0mg[c] * s.uaf / NU_PARAM, P.a_exp));
+    const double csoilcn = csoilb * w + P.csoilc * (1.0 - w);
+    s.rah_b = 1.0 / (csoilcn * s.uaf);
+    const double raw_b = s.rah_b;
+    const double forc_pbot = io.forc_pbot[c];
+    const double svpts = s.el;
+    const double eah = forc_pbot * s.qaf / 0.622;
+    s.rhaf_last = eah / svpts;
+    s.vpd_last = fmax((svpts - eah), 50.0) * 0.001;
+    const double thm = io.thm[p], btran = io.btran[p];
+    const double laisun = io.laisun[p], laisha = io.laisha[p];
+    s.sun = photosynthesis(A, pg, s.ivt, s.t_veg, io.t_a10[p], thm, forc_pbot, svpts, eah, io.forc_po2[g],
+                           io.forc_pco2[g], rb, btran, s.dayl_factor, io.parsun_z[p], laisun, io.vcmaxcintsun[p],
+                           s.st, s.vpd_can, s.rh_leaf, err);
+    s.sha = photosynthesis(A, pg, s.ivt, s.t_veg, io.t_a10[p], thm, forc_pbot, svpts, eah, io.forc_po2[g],
+                           io.forc_pco2[g], rb, btran, s.dayl_factor, io.parsha_z[p], laisha, io.vcmaxcintsha[p],
+                           s.st, s.vpd_can, s.rh_leaf, err);
+    const double sa_leaf = elai + esai;
+    const double wta = 1.0 / s.rah_a;
+    const double wtl = sa_leaf / rb;
+    s.wtg = 1.0 / s.rah_b;
+    const double wtshi = 1.0 / (wta + wtl + 0.0 + s.wtg);
+    s.wtl0 = wtl * wtshi;
+    const double wtg0 = s.wtg * wtshi;
+    s.wta0 = wta * wtshi;
+    const double wtga = s.wta0 + wtg0 + 0.0;
+    s.wtal = s.wta0 + s.wtl0 + 0.0;
+    const double fdry = io.fdry[p], fwet = io.fwet[p];
+    const double rppdry = (fdry > 0.0) ? fdry * rb * (laisun / (rb + s.sun.rs) + laisha / (rb + s.sha.rs)) / elai : 0.0;
+    const double forc_rho = io.forc_rho[c], forc_q = io.forc_q[c], qg = io.qg[c], t_grnd = io.t_grnd[c];
+    double efpot = forc_rho * ((elai + esai) / rb) * (s.qsatl - s.qaf);
+    const double h2ocan = s.liqcan + s.snocan;
+    double rpp;
+    if (efpot > 0.0) {
+        if (btran > 0.0) { s.qflx_tran_veg = efpot * rppdry; rpp = rppdry + fwet; }
+        else { rpp = fwet; s.qflx_tran_veg = 0.0; }
+        rpp = fmin(rpp, (s.qflx_tran_veg + h2ocan / dtime) / efpot);
+    } else {
+        rpp = 1.0;
+        s.qflx_tran_veg = 0.0;
+    }
+    const double fv = (double)io.frac_veg_nosno[p];
+    const double wtaq = fv / s.raw_a;
+    const double wtlq = fv * (elai + esai) / rb * rpp;
+    const double fsno_dl = io.snow_depth[c] / P.z_dl;
+    const double elai_dl = P.lai_dl * (1.0 - fmin(fsno_dl, 1.0));
+    const double rdl = (1.0 - exp(-elai_dl)) / (0.004 * s.uaf);
+    s.wtgq = (s.delq < 0.0) ? fv / (raw_b + rdl) : fv / (raw_b + io.soilresis[c]);
+    const double wtsqi = 1.0 / (wtaq + wtlq + s.wtgq);
+    const double wtgq0 = s.wtgq * wtsqi;
+    s.wtlq0 = wtlq * wtsqi;
+    s.wtaq0 = wtaq * wtsqi;
+    const double wtgaq = s.wtaq0 + wtgq0;
+    s.wtalq = s.wtaq0 + s.wtlq0;
+    const double dc1 = forc_rho * CPAIR * wtl;
+    const double dc2 = HVAP * forc_rho * wtlq;
+    const double efsh = dc1 * (wtga * s.t_veg - wtg0 * t_grnd - s.wta0 * thm - 0.0);
+    s.efe = dc2 * (wtgaq * s.qsatl - wtgq0 * qg - s.wtaq0 * forc_q);
+    double erre = 0.0;
+    if (s.efe * s.efeb < 0.0) {
+        const double efeold = s.efe;
+        s.efe = 0.1 * efeold;
+        erre = s.efe - efeold;
+    }
+    const int ldc = io.ldc;
+    const int snl = io.snl[c];
+    const double frac_sno = io.frac_sno_eff[c], frac_h2osfc = io.frac_h2osfc[c];
+    const double lw_grnd = (frac_sno * ipow4(io.t_soisno[c + (size_t)(snl + NLEVSNO) * ldc]) +
+                            (1.0 - frac_sno - frac_h2osfc) * ipow4(io.t_soisno[c + (size_t)NLEVSNO * ldc]) +
+                            frac_h2osfc * ipow4(io.t_h2osfc[c]));
+    const double sabv = io.sabv[p];
+    const double t_veg = s.t_veg;
+    double dt_veg = ((1.0 - 0.0) * (sabv + s.air + s.bir * ipow4(t_veg) + s.cir * lw_grnd) - efsh - s.efe - 0.0 + 0.0 -
+                     (0.0 / dtime) * (t_veg - s.tl_ini)) /
+                    ((1.0 - 0.0) * (-4.0 * s.bir * ipow3(t_veg)) + 4.0 * 0.0 * io.emv[p] * SB * ipow3(t_veg) + dc1 * wtga +
+                     dc2 * wtgaq * s.qsatldT + 0.0 / dtime);
+    s.t_veg = s.tlbef + dt_veg;
+    const double dels = dt_veg;
+    s.del = fabs(dels);
+    s.err = 0.0;
+    if (s.del > 1.0) {
+        dt_veg = 1.0 * dels / s.del;
+        s.t_veg = s.tlbef + dt_veg;
+        const double tb3 = ipow3(s.tlbef);
+        s.err = (1.0 - 0.0) * (sabv + s.air + s.bir * tb3 * (s.tlbef + 4.0 * dt_veg) + s.cir * lw_grnd) -
+                0.0 * io.emv[p] * SB * tb3 * (s.tlbef + 4.0 * dt_veg) + 0.0 - (efsh + dc1 * wtga * dt_veg) -
+                (s.efe + dc2 * wtgaq * s.qsatldT * dt_veg) - (0.0 / dtime) * (s.t_veg - s.tl_ini);
+    }
+    s.dt_veg = dt_veg;
+    efpot = forc_rho * ((elai + esai) / rb) * (wtgaq * (s.qsatl + s.qsatldT * dt_veg) - wtgq0 * qg - s.wtaq0 * forc_q);
+    s.qflx_evap_veg = rpp * efpot;
+    s.qflx_tran_veg = (efpot > 0.0 && btran > 0.0) ? efpot * rppdry : 0.0;
+    const double ecidif = fmax(0.0, s.qflx_evap_veg - s.qflx_tran_veg - h2ocan / dtime);
+    s.qflx_evap_veg = fmin(s.qflx_evap_veg, s.qflx_tran_veg + h2ocan / dtime);
+    s.eflx_sh_veg = efsh + dc1 * wtga * dt_veg + s.err + erre + HVAP * ecidif;
+    s.lw_leaf = 0.0 * io.emv[p] * SB * ipow3(s.tlbef) * (s.tlbef + 4.0 * dt_veg);
+    qsat(s.t_veg, forc_pbot, s.qsatl, s.el, &s.qsatldT);
+    s.taf = wtg0 * t_grnd + s.wta0 * thm + s.wtl0 * s.t_veg + 0.0;
+    s.qaf = s.wtlq0 * s.qsatl + wtgq0 * qg + forc_q * s.wtaq0;
+    s.dth = thm - s.taf;
+    s.dqh = forc_q - s.qaf;
+    s.delq = s.wtalq * qg - s.wtlq0 * s.qsatl - s.wtaq0 * forc_q;
+    const double tstar = s.temp1 * s.dth;
+    const double qstar = s.temp2 * s.dqh;
+    const double forc_th = io.forc_th[c], thv = io.thv[c];
+    const double thvstar = tstar * (1.0 + 0.61 * forc_q) + 0.61 * forc_th * qstar;
+    double zeta = s.zldis * VKC * GRAV * thvstar / ((ustar * ustar) * thv);
+    if (zeta >= 0.0) {
+        zeta = fmin(P.zetamaxstable, fmax(zeta, 0.01));
+        s.um = fmax(s.ur, 0.1);
+    } else {
+        zeta = fmax(-100.0, fmin(zeta, -0.01));
+        const double wc = (ustar * thvstar > 0.0) ? 0.0 : 1.0 * pow(-GRAV * ustar * thvstar * 1000.0 / thv, 0.333);
+        s.um = sqrt(s.ur * s.ur + wc * wc);
+    }
+    s.zeta = zeta;
+    s.obu = s.zldis / zeta;
+    if (s.obuold * s.obu < 0.0) s.nmozsgn = s.nmozsgn + 1;
+    if (s.nmozsgn >= 4) s.obu = s.zldis / (-0.01);
+    s.obuold = s.obu;
+    s.itlef = s.itlef + 1;
+    if (s.itlef > 2) {
+        const double dele = fabs(s.efe - s.efeb);
+        s.efeb = s.efe;
+        const double det = fmax(s.del, del2);
+        s.num_iter = s.itlef;
+        if (det < 0.01 && dele < 0.1) return true;
+    }
+    return s.itlef > A.itmax;
+}
+
+// after the iteration (CanopyFluxesMod.F90:1461-1655)
+__device__ void finalize(const CanopyArgs& A, const Patch& s, double dtime) {
+    const ctsmg_canopy_io& io = A.io;
+    const int p = s.p, c = s.c, g = s.g;
+    const int ldc = io.ldc;
+    const int snl = io.snl[c];
+    const double frac_sno = io.frac_sno_eff[c], frac_h2osfc = io.frac_h2osfc[c];
+    const double ts_top = io.t_soisno[c + (size_t)(snl + NLEVSNO) * ldc];
+    const double ts_1 = io.t_soisno[c + (size_t)NLEVSNO * ldc];
+    const double lw_grnd = (frac_sno * ipow4(ts_top) + (1.0 - frac_sno - frac_h2osfc) * ipow4(ts_1) +
+                            frac_h2osfc * ipow4(io.t_h2osfc[c]));
+    const double tb3 = ipow3(s.tlbef);
+    const double emv = io.emv[p], emg = io.emg[c];
+    io.err_canopy[p] = (1.0 - 0.0) * (io.sabv[p] + s.air + s.bir * tb3 * (s.tlbef + 4.0 * s.dt_veg) + s.cir * lw_grnd) -
+                       s.lw_leaf + 0.0 - s.eflx_sh_veg - HVAP * s.qflx_evap_veg - ((s.t_veg - s.tl_ini) * 0.0 / dtime);
+    const double thm = io.thm[p], forc_rho = io.forc_rho[c], forc_q = io.forc_q[c];
+    const double t_veg = s.t_veg;
+    const double delt = s.wtal * io.t_grnd[c] - s.wtl0 * t_veg - s.wta0 * thm - 0.0;
+    io.taux[p] = -forc_rho * io.forc_u[g] / s.ram1;
+    io.tauy[p] = -forc_rho * io.forc_v[g] / s.ram1;
+    io.eflx_sh_grnd[p] = CPAIR * forc_rho * s.wtg * delt;
+    io.eflx_sh_snow[p] = CPAIR * forc_rho * s.wtg * (s.wtal * ts_top - s.wtl0 * t_veg - s.wta0 * thm - 0.0);
+    io.eflx_sh_soil[p] = CPAIR * forc_rho * s.wtg * (s.wtal * ts_1 - s.wtl0 * t_veg - s.wta0 * thm - 0.0);
+    io.eflx_sh_h2osfc[p] = CPAIR * forc_rho * s.wtg * (s.wtal * io.t_h2osfc[c] - s.wtl0 * t_veg - s.wta0 * thm - 0.0);
+    io.qflx_evap_soi[p] = forc_rho * s.wtgq * s.delq;
+    io.qflx_ev_snow[p] = forc_rho * s.wtgq * (s.wtalq * io.qg_snow[c] - s.wtlq0 * s.qsatl - s.wtaq0 * forc_q);
+    io.qflx_ev_soil[p] = forc_rho * s.wtgq * (s.wtalq * io.qg_soil[c] - s.wtlq0 * s.qsatl - s.wtaq0 * forc_q);
+    io.qflx_ev_h2osfc[p] = forc_rho * s.wtgq * (s.wtalq * io.qg_h2osfc[c] - s.wtlq0 * s.qsatl - s.wtaq0 * forc_q);
+    const double t_ref2m = thm + s.temp1 * s.dth * (1.0 / s.temp12m - 1.0 / s.temp1);
+    const double q_ref2m = forc_q + s.temp2 * s.dqh * (1.0 / s.temp22m - 1.0 / s.temp2);
+    double qsat_ref2m, e_ref2m;
+    qsat(t_ref2m, io.forc_pbot[c], qsat_ref2m, e_ref2m, nullptr);
+    const double rh_ref2m = fmin(100.0, q_ref2m / qsat_ref2m * 100.0);
+    io.t_ref2m[p] = t_ref2m;
+    io.q_ref2m[p] = q_ref2m;
+    io.rh_ref2m[p] = rh_ref2m;
+    io.vpd_ref2m[p] = e_ref2m * (1.0 - rh_ref2m / 100.0);
+    const double forc_lwrad = io.forc_lwrad[c];
+    io.dlrad[p] = (1.0 - emv) * emg * forc_lwrad + emv * emg * SB * tb3 * (s.tlbef + 4.0 * s.dt_veg) * (1.0 - 0.0) +
+                  emv * emg * SB * 0.0 * (0.0 + 4.0 * 0.0) * 0.0;
+    io.ulrad[p] = ((1.0 - emg) * (1.0 - emv) * (1.0 - emv) * forc_lwrad +
+                   emv * (1.0 + (1.0 - emg) * (1.0 - emv)) * SB * tb3 * (s.tlbef + 4.0 * s.dt_veg) * (1.0 - 0.0) +
+                   emv * (1.0 + (1.0 - emg) * (1.0 - emv)) * SB * 0.0 * (0.0 + 4.0 * 0.0) * 0.0 +
+                   emg * (1.0 - emv) * SB * lw_grnd);
+    io.t_skin[p] = emv * t_veg + (1.0 - emv) * sqrt(sqrt(lw_grnd));
+    const double cgrnds = io.cgrnds[p] + CPAIR * forc_rho * s.wtg * s.wtal;
+    const double cgrndl = io.cgrndl[p] + forc_rho * s.wtgq * s.wtalq * io.dqgdT[c];
+    io.cgrnds[p] = cgrnds;
+    io.cgrndl[p] = cgrndl;
+    io.cgrnd[p] = cgrnds + cgrndl * io.htvp[c];
+    double liqcan = s.liqcan, snocan = s.snocan;
+    const double snocan_baseline = snocan;
+    const double net = (s.qflx_tran_veg - s.qflx_evap_veg) * dtime;
+    if (t_veg > TFRZ) {
+        if ((s.qflx_evap_veg - s.qflx_tran_veg) * dtime > liqcan) snocan = fmax(0.0, snocan + liqcan + net);
+        liqcan = fmax(0.0, liqcan + net);
+    } else if (t_veg <= TFRZ) {
+        if ((s.qflx_evap_veg - s.qflx_tran_veg) * dtime > snocan) liqcan = liqcan + snocan + net;
+        snocan = fmax(0.0, snocan + net);
+    }
+    if (fabs(snocan) < 1.e-10 * fabs(snocan_baseline)) snocan = 0.0;
+    io.liqcan[p] = liqcan;
+    io.snocan[p] = snocan;
+    io.displa[p] = s.displa;
+    io.z0mv[p] = s.z0mv;
+    io.z0hv[p] = s.z0mv;
+    io.z0qv[p] = s.z0mv;
+    io.forc_hgt_u_patch[p] = s.hgt_u;
+    io.forc_hgt_t_patch[p] = s.hgt_t;
+    io.forc_hgt_q_patch[p] = s.hgt_q;
+    io.t_veg[p] = t_veg;
+    io.taf[p] = s.taf;
+    io.qaf[p] = s.qaf;
+    io.ustar[p] = s.ustar;
+    io.um[p] = s.um;
+    io.obu[p] = s.obu;
+    io.zeta[p] = s.zeta;
+    io.ram1[p] = s.ram1;
+    io.rah1[p] = s.rah_a;
+    io.raw1[p] = s.raw_a;
+    io.rah2[p] = s.rah_b;
+    io.raw2[p] = s.rah_b;
+    io.rb1[p] = s.rb;
+    io.uaf[p] = s.uaf;
+    io.rhaf[p] = s.rhaf_last;
+    io.vpd[p] = s.vpd_last;
+    io.eflx_sh_veg[p] = s.eflx_sh_veg;
+    io.qflx_evap_veg[p] = s.qflx_evap_veg;
+    io.qflx_tran_veg[p] = s.qflx_tran_veg;
+    io.num_iter[p] = s.num_iter;
+    io.rssun[p] = s.sun.rs; io.rssha[p] = s.sha.rs;
+    io.psnsun[p] = s.sun.psn; io.psnsha[p] = s.sha.psn;
+    io.lmrsun[p] = s.sun.lmr; io.lmrsha[p] = s.sha.lmr;
+    io.cisun[p] = s.sun.ci; io.cisha[p] = s.sha.ci;
+    io.gs_mol_sun[p] = s.sun.gs_mol_phase; io.gs_mol_sha[p] = s.sha.gs_mol_phase;
+    io.rh_leaf[p] = s.rh_leaf;
+    io.vpd_can[p] = s.vpd_can;
+    io.u10_clm[p] = s.u10_clm;
+    io.u10[p] = s.u10;
+    io.fv[p] = s.ustar;
+    io.vds[p] = s.vds;
+    io.fm[p] = s.fm;
+}
+
+__global__ void __launch_bounds__(128)
+canopy_kernel(CanopyArgs A, int nfilt, const int32_t* __restrict__ filt, double dtime, int* __restrict__ next,
+              DevError* derr) {
+    Err err{0, 0};
+    Patch s;
+    int f = atomicAdd(next, 1);
+    bool active = f < nfilt;
+    if (active) setup(A, s, (filt ? filt[f] : f + A.begp) - A.begp, err);
+#pragma unroll 1
+    while (active) {
+        const bool done = pass(A, s, err, dtime);
+        if (done) {
+            finalize(A, s, dtime);
+            if (err.code) report_error(derr, err.idx, 0, err.code);
+            err = Err{0, 0};
+            f = atomicAdd(next, 1);
+            active = f < nfilt;
+            if (active) setup(A, s, (filt ? filt[f] : f + A.begp) - A.begp, err);
+        }
+    }
+}
+
+} // namespace canopy
+
+cudaError_t launch_canopy(const CanopyArgs& a, int nfilt, const int32_t* d_filt, double dtime, int* d_counter,
+                          DevError* err, cudaStream_t s) {
+    if (nfilt <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    int nsm = 152;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, canopy::canopy_kernel, 128, 0);
+    if (per_sm < 1) per_sm = 1;
+    long long want = (long long)nsm * per_sm;
+    long long need = (nfilt + 127) / 128;
+    int blocks = (int)(want < need ? want : need);
+    canopy::canopy_kernel<<<blocks, 128, 0, s>>>(a, nfilt, d_filt, dtime, d_counter, err);
+    return cudaGetLastError();
+}
+
+} // namespace ctsmg

@@ -13,6 +13,7 @@
 #include "ctsm_gpu.h"
 #include "ctsm_device.cuh"
 #include "soil_kernels.cuh"
+#include "canopy_kernels.cuh"
 #include "capi_internal.h"
 
 namespace ctsmg {
@@ -22,6 +23,9 @@ static std::mutex g_mu;
 static bool g_init = false;
 static ctsmg_options g_opt;
 static ctsmg_soilwater_params g_swp = {6.0};
+static ctsmg_canopy_params g_cpar;
+static ctsmg_pftcon g_pft;
+static bool g_cpar_set = false;
 
 // ------------------------------------------------------------ per-thread context
 struct ThreadCtx {
@@ -97,7 +101,7 @@ static void* arena_take(ThreadCtx* c, size_t bytes) {
 // ------------------------------------------------------------ field tables
 int kind_levels(int kind) {
     switch (kind) {
-        case K_C: case K_P: return 1;
+        case K_C: case K_P: case K_GR: return 1;
         case K_SS: return NLEVSNO + NLEVGRND;
         case K_ZI: return NLEVSNO + NLEVGRND + 1;
         case K_G: return NLEVGRND;
@@ -151,18 +155,141 @@ const FieldDesc SOILTEMP_TABLE[] = {
 };
 const int SOILTEMP_NFIELDS = sizeof(SOILTEMP_TABLE) / sizeof(SOILTEMP_TABLE[0]);
 
+#define FC(name, kind, esz, use) FW(ctsmg_canopy_io, name, kind, esz, use)
+const FieldDesc CANOPY_TABLE[] = {
+    FC(itype, K_P, 4, U_IN),
+    FC(patch_column, K_P, 4, U_IN),
+    FC(patch_gridcell, K_P, 4, U_IN),
+    FC(forc_u, K_GR, 8, U_IN),
+    FC(forc_v, K_GR, 8, U_IN),
+    FC(forc_hgt_u, K_GR, 8, U_IN),
+    FC(forc_hgt_t, K_GR, 8, U_IN),
+    FC(forc_hgt_q, K_GR, 8, U_IN),
+    FC(forc_pco2, K_GR, 8, U_IN),
+    FC(forc_po2, K_GR, 8, U_IN),
+    FC(dayl, K_GR, 8, U_IN),
+    FC(max_dayl, K_GR, 8, U_IN),
+    FC(snl, K_C, 4, U_IN),
+    FC(forc_pbot, K_C, 8, U_IN),
+    FC(forc_th, K_C, 8, U_IN),
+    FC(forc_q, K_C, 8, U_IN),
+    FC(forc_rho, K_C, 8, U_IN),
+    FC(forc_lwrad, K_C, 8, U_IN),
+    FC(thv, K_C, 8, U_IN),
+    FC(t_grnd, K_C, 8, U_IN),
+    FC(qg, K_C, 8, U_IN),
+    FC(qg_snow, K_C, 8, U_IN),
+    FC(qg_soil, K_C, 8, U_IN),
+    FC(qg_h2osfc, K_C, 8, U_IN),
+    FC(dqgdT, K_C, 8, U_IN),
+    FC(emg, K_C, 8, U_IN),
+    FC(htvp, K_C, 8, U_IN),
+    FC(z0mg, K_C, 8, U_IN),
+    FC(snow_depth, K_C, 8, U_IN),
+    FC(frac_sno_eff, K_C, 8, U_IN),
+    FC(frac_h2osfc, K_C, 8, U_IN),
+    FC(soilresis, K_C, 8, U_IN),
+    FC(t_h2osfc, K_C, 8, U_IN),
+    FC(t_soisno, K_SS, 8, U_IN),
+    FC(frac_veg_nosno, K_P, 4, U_IN),
+    FC(elai, K_P, 8, U_IN),
+    FC(esai, K_P, 8, U_IN),
+    FC(htop, K_P, 8, U_IN),
+    FC(emv, K_P, 8, U_IN),
+    FC(fwet, K_P, 8, U_IN),
+    FC(fdry, K_P, 8, U_IN),
+    FC(laisun, K_P, 8, U_IN),
+    FC(laisha, K_P, 8, U_IN),
+    FC(btran, K_P, 8, U_IN),
+    FC(sabv, K_P, 8, U_IN),
+    FC(thm, K_P, 8, U_IN),
+    FC(t_a10, K_P, 8, U_IN),
+    FC(parsun_z, K_P, 8, U_IN),
+    FC(parsha_z, K_P, 8, U_IN),
+    FC(vcmaxcintsun, K_P, 8, U_IN),
+    FC(vcmaxcintsha, K_P, 8, U_IN),
+    FC(displa, K_P, 8, U_INOUT),
+    FC(z0mv, K_P, 8, U_INOUT),
+    FC(t_veg, K_P, 8, U_INOUT),
+    FC(liqcan, K_P, 8, U_INOUT),
+    FC(snocan, K_P, 8, U_INOUT),
+    FC(cgrnds, K_P, 8, U_INOUT),
+    FC(cgrndl, K_P, 8, U_INOUT),
+    FC(z0hv, K_P, 8, U_OUT),
+    FC(z0qv, K_P, 8, U_OUT),
+    FC(forc_hgt_u_patch, K_P, 8, U_OUT),
+    FC(forc_hgt_t_patch, K_P, 8, U_OUT),
+    FC(forc_hgt_q_patch, K_P, 8, U_OUT),
+    FC(taf, K_P, 8, U_OUT),
+    FC(qaf, K_P, 8, U_OUT),
+    FC(ustar, K_P, 8, U_OUT),
+    FC(um, K_P, 8, U_OUT),
+    FC(obu, K_P, 8, U_OUT),
+    FC(zeta, K_P, 8, U_OUT),
+    FC(ram1, K_P, 8, U_OUT),
+    FC(rah1, K_P, 8, U_OUT),
+    FC(raw1, K_P, 8, U_OUT),
+    FC(rah2, K_P, 8, U_OUT),
+    FC(raw2, K_P, 8, U_OUT),
+    FC(rb1, K_P, 8, U_OUT),
+    FC(uaf, K_P, 8, U_OUT),
+    FC(vpd, K_P, 8, U_OUT),
+    FC(rhaf, K_P, 8, U_OUT),
+    FC(eflx_sh_veg, K_P, 8, U_OUT),
+    FC(qflx_evap_veg, K_P, 8, U_OUT),
+    FC(qflx_tran_veg, K_P, 8, U_OUT),
+    FC(eflx_sh_grnd, K_P, 8, U_OUT),
+    FC(eflx_sh_snow, K_P, 8, U_OUT),
+    FC(eflx_sh_soil, K_P, 8, U_OUT),
+    FC(eflx_sh_h2osfc, K_P, 8, U_OUT),
+    FC(qflx_evap_soi, K_P, 8, U_OUT),
+    FC(qflx_ev_snow, K_P, 8, U_OUT),
+    FC(qflx_ev_soil, K_P, 8, U_OUT),
+    FC(qflx_ev_h2osfc, K_P, 8, U_OUT),
+    FC(t_ref2m, K_P, 8, U_OUT),
+    FC(q_ref2m, K_P, 8, U_OUT),
+    FC(rh_ref2m, K_P, 8, U_OUT),
+    FC(vpd_ref2m, K_P, 8, U_OUT),
+    FC(dlrad, K_P, 8, U_OUT),
+    FC(ulrad, K_P, 8, U_OUT),
+    FC(t_skin, K_P, 8, U_OUT),
+    FC(cgrnd, K_P, 8, U_OUT),
+    FC(taux, K_P, 8, U_OUT),
+    FC(tauy, K_P, 8, U_OUT),
+    FC(err_canopy, K_P, 8, U_OUT),
+    FC(rssun, K_P, 8, U_OUT),
+    FC(rssha, K_P, 8, U_OUT),
+    FC(psnsun, K_P, 8, U_OUT),
+    FC(psnsha, K_P, 8, U_OUT),
+    FC(lmrsun, K_P, 8, U_OUT),
+    FC(lmrsha, K_P, 8, U_OUT),
+    FC(cisun, K_P, 8, U_OUT),
+    FC(cisha, K_P, 8, U_OUT),
+    FC(gs_mol_sun, K_P, 8, U_OUT),
+    FC(gs_mol_sha, K_P, 8, U_OUT),
+    FC(rh_leaf, K_P, 8, U_OUT),
+    FC(vpd_can, K_P, 8, U_OUT),
+    FC(u10_clm, K_P, 8, U_OUT),
+    FC(u10, K_P, 8, U_OUT),
+    FC(fv, K_P, 8, U_OUT),
+    FC(vds, K_P, 8, U_OUT),
+    FC(fm, K_P, 8, U_OUT),
+    FC(num_iter, K_P, 4, U_OUT),
+};
+const int CANOPY_NFIELDS = sizeof(CANOPY_TABLE) / sizeof(CANOPY_TABLE[0]);
+
 static inline void*& field_ptr(void* io, const FieldDesc& f) {
     return *reinterpret_cast<void**>(reinterpret_cast<char*>(io) + f.offset);
 }
 
-size_t field_bytes(const FieldDesc& f, int ldc, int ldp) {
-    int ld = (f.kind == K_P || f.kind == K_PL) ? ldp : ldc;
+size_t field_bytes(const FieldDesc& f, int ldc, int ldp, int ldg) {
+    int ld = (f.kind == K_P || f.kind == K_PL) ? ldp : (f.kind == K_GR ? ldg : ldc);
     return (size_t)ld * kind_levels(f.kind) * f.esize;
 }
 
 // Copy the host struct's arrays into the arena; fill dio with device pointers.
 static int stage_in(ThreadCtx* c, const void* hio, void* dio, size_t io_size, const FieldDesc* tab, int nf,
-                    int ldc, int ldp) {
+                    int ldc, int ldp, int ldg = 0) {
     std::memcpy(dio, hio, io_size);
     for (int i = 0; i < nf; ++i) {
         const void* hp = field_ptr(const_cast<void*>(hio), tab[i]);
@@ -170,7 +297,7 @@ static int stage_in(ThreadCtx* c, const void* hio, void* dio, size_t io_size, co
             std::string m = std::string("null pointer for component ") + tab[i].name;
             return set_error(CTSMG_E_ARG, m.c_str(), 0, 0);
         }
-        size_t nb = field_bytes(tab[i], ldc, ldp);
+        size_t nb = field_bytes(tab[i], ldc, ldp, ldg);
         void* dp = arena_take(c, nb);
         cudaError_t e = cudaMemcpyAsync(dp, hp, nb, cudaMemcpyHostToDevice, c->stream);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync H2D");
@@ -180,20 +307,20 @@ static int stage_in(ThreadCtx* c, const void* hio, void* dio, size_t io_size, co
 }
 
 static int stage_out(ThreadCtx* c, const void* hio, const void* dio, const FieldDesc* tab, int nf,
-                     int ldc, int ldp) {
+                     int ldc, int ldp, int ldg = 0) {
     for (int i = 0; i < nf; ++i) {
         if (tab[i].use == U_IN) continue;
         void* hp = field_ptr(const_cast<void*>(hio), tab[i]);
         const void* dp = field_ptr(const_cast<void*>(dio), tab[i]);
-        cudaError_t e = cudaMemcpyAsync(hp, dp, field_bytes(tab[i], ldc, ldp), cudaMemcpyDeviceToHost, c->stream);
+        cudaError_t e = cudaMemcpyAsync(hp, dp, field_bytes(tab[i], ldc, ldp, ldg), cudaMemcpyDeviceToHost, c->stream);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync D2H");
     }
     return 0;
 }
 
-static size_t table_bytes(const FieldDesc* tab, int nf, int ldc, int ldp) {
+static size_t table_bytes(const FieldDesc* tab, int nf, int ldc, int ldp, int ldg = 0) {
     size_t s = 0;
-    for (int i = 0; i < nf; ++i) s += ((field_bytes(tab[i], ldc, ldp) + 255) & ~(size_t)255);
+    for (int i = 0; i < nf; ++i) s += ((field_bytes(tab[i], ldc, ldp, ldg) + 255) & ~(size_t)255);
     return s;
 }
 
@@ -347,5 +474,80 @@ extern "C" int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds, int32_t num
     int code = 0, idx = 0, lev = 0;
     if ((rc = read_error(c, &code, &idx, &lev))) return rc;
     if (code) return set_error(code, "BandDiagonal ERROR: dgbsv returned error code", idx, lev);
+    return 0;
+}
+
+extern "C" int32_t ctsmg_set_canopy_params(const ctsmg_canopy_params* p, const ctsmg_pftcon* pft) {
+    if (!p || !pft) return set_error(CTSMG_E_ARG, "null params", 0, 0);
+    if (pft->npft < 1 || pft->npft > CTSMG_MAX_PFT) return set_error(CTSMG_E_ARG, "npft outside 1..CTSMG_MAX_PFT", 0, 0);
+    for (int i = 0; i < pft->npft; ++i)
+        if (pft->slatop[i] * pft->leafcn[i] <= 0.0)
+            return set_error(CTSMG_E_ARG, "ERROR: slatop or leafcn is zero", i, 0);
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_cpar = *p;
+    g_pft = *pft;
+    g_cpar_set = true;
+    return 0;
+}
+
+extern "C" int32_t ctsmg_canopyfluxes(const ctsmg_bounds* bounds, int32_t num_exposedvegp,
+                                      const int32_t* filter_exposedvegp, const ctsmg_canopy_io* io, double dtime) {
+    ThreadCtx* c;
+    int rc = ctx_get(&c);
+    if (rc) return rc;
+    if (!io) return set_error(CTSMG_E_ARG, "null io", 0, 0);
+    if (!g_cpar_set) return set_error(CTSMG_E_NOT_INIT, "ctsmg_set_canopy_params has not been called", 0, 0);
+    if (!bounds || bounds->endp < bounds->begp) return set_error(CTSMG_E_ARG, "bad patch bounds", 0, 0);
+    if (num_exposedvegp < 0 || (num_exposedvegp > 0 && !filter_exposedvegp))
+        return set_error(CTSMG_E_ARG, "bad patch filter", 0, 0);
+    const int npat = bounds->endp - bounds->begp + 1, ncol = bounds->endc - bounds->begc + 1;
+    if (io->ldp < npat || io->ldc < ncol || io->ldg < 1) return set_error(CTSMG_E_ARG, "ldp/ldc/ldg too small", 0, 0);
+    if (!(dtime > 0.0)) return set_error(CTSMG_E_ARG, "dtime must be positive", 0, 0);
+    for (int i = 0; i < num_exposedvegp; ++i) {
+        const int pg = filter_exposedvegp[i];
+        if (pg < bounds->begp || pg > bounds->endp) return set_error(CTSMG_E_ARG, "filter index outside bounds", pg, 0);
+        const int p = pg - bounds->begp;
+        const int cc = io->patch_column[p], gg = io->patch_gridcell[p], it = io->itype[p];
+        if (cc < bounds->begc || cc > bounds->endc) return set_error(CTSMG_E_ARG, "patch column outside bounds", pg, 0);
+        if (gg < io->begg || gg > io->begg + io->ldg - 1) return set_error(CTSMG_E_ARG, "patch gridcell outside ldg", pg, 0);
+        if (it < 0 || it >= g_pft.npft) return set_error(CTSMG_E_ARG, "patch itype outside pftcon", pg, 0);
+        const int s = io->snl[cc - bounds->begc];
+        if (s > 0 || s < -NLEVSNO) return set_error(CTSMG_E_ARG, "snl outside -nlevsno..0", cc, 0);
+    }
+    if (num_exposedvegp == 0) return 0;
+    const int ldc = io->ldc, ldp = io->ldp, ldg = io->ldg;
+    size_t need = table_bytes(CANOPY_TABLE, CANOPY_NFIELDS, ldc, ldp, ldg) + (size_t)num_exposedvegp * 4 + 8192;
+    if ((rc = arena_reserve(c, need))) return rc;
+    CanopyArgs a;
+    if ((rc = stage_in(c, io, &a.io, sizeof a.io, CANOPY_TABLE, CANOPY_NFIELDS, ldc, ldp, ldg))) return rc;
+    int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_exposedvegp * 4);
+    int* counter = (int*)arena_take(c, 256);
+    cudaError_t e = cudaMemcpyAsync(dfilt, filter_exposedvegp, (size_t)num_exposedvegp * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
+    e = cudaMemsetAsync(c->err, 0xff, sizeof(DevError), c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(err)");
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        a.par = g_cpar;
+        a.pft = g_pft;
+        a.method = g_opt.stomatalcond_method;
+        a.itmax = g_opt.itmax_canopy_fluxes;
+    }
+    a.begc = bounds->begc;
+    a.begp = bounds->begp;
+    e = launch_canopy(a, num_exposedvegp, dfilt, dtime, counter, c->err, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "canopy kernel launch");
+    if ((rc = stage_out(c, io, &a.io, CANOPY_TABLE, CANOPY_NFIELDS, ldc, ldp, ldg))) return rc;
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "canopyfluxes");
+    int code = 0, idx = 0, lev = 0;
+    if ((rc = read_error(c, &code, &idx, &lev))) return rc;
+    if (code) {
+        const char* m = code == CTSMG_E_DISCRIMINANT ? "quadratic ERROR: Quadratic solution error: b^2 - 4ac is negative"
+                      : code == CTSMG_E_NOT_BRACKETED ? "root must be bracketed for brent"
+                      : code == CTSMG_E_FORCING_HEIGHT ? "Error: Forcing height is below canopy height for patch index"
+                      : "CanopyFluxes error";
+        return set_error(code, m, idx, lev);
+    }
     return 0;
 }

@@ -5,7 +5,7 @@
 #include "ctsm_gpu.h"
 
 namespace ctsmg {
-enum Kind { K_C, K_P, K_SS, K_ZI, K_G, K_S, K_SN, K_PL };
+enum Kind { K_C, K_P, K_SS, K_ZI, K_G, K_S, K_SN, K_PL, K_GR };
 enum Use { U_IN, U_OUT, U_INOUT };
 struct FieldDesc { size_t offset; int kind; int esize; int use; const char* name; };
 
@@ -13,9 +13,11 @@ extern const FieldDesc SOILWATER_TABLE[];
 extern const int SOILWATER_NFIELDS;
 extern const FieldDesc SOILTEMP_TABLE[];
 extern const int SOILTEMP_NFIELDS;
+extern const FieldDesc CANOPY_TABLE[];
+extern const int CANOPY_NFIELDS;
 
 int kind_levels(int kind);
-size_t field_bytes(const FieldDesc& f, int ldc, int ldp);
+size_t field_bytes(const FieldDesc& f, int ldc, int ldp, int ldg = 0);
 int set_error(int code, const char* what, int index, int level);
 int check_filter(const ctsmg_bounds* b, int nf, const int32_t* filt);
 int current_snow_method();

@@ -217,6 +217,71 @@ typedef struct {
     double*       qflx_h2osfc_to_ice; /* (c) out */
 } ctsmg_soiltemp_io;
 
+/* ---------------------------------------------------------------- CanopyFluxes */
+/* Scalar parameters of CanopyFluxes (readParams, src/biogeophys/CanopyFluxesMod.F90:159-188),
+ * FrictionVelocity (zetamaxstable, FrictionVelocityMod.F90:136,511) and
+ * Photosynthesis (params_type, src/biogeophys/PhotosynthesisMod.F90:92-140;
+ * module constants :85-89).  Values of the parameter file are not shipped
+ * with the reference; ctsm_gb300/canopy_inputs.py records the ones used.   */
+typedef struct {
+    /* CanopyFluxes */
+    double lai_dl, z_dl, a_coef, a_exp, csoilc, cv, wind_min, zetamaxstable;
+    /* Photosynthesis */
+    double kc25_coef, ko25_coef, cp25_yr2000, kcha, koha, cpha;
+    double vcmaxha, jmaxha, tpuha, lmrha, vcmaxhd, jmaxhd, tpuhd, lmrhd, lmrse;
+    double vcmaxse_sf, jmaxse_sf, tpuse_sf, jmax25top_sf;
+    double fnr, act25, theta_psii, theta_ip, tpu25ratio, kp25ratio, fnps, leaf_mr_vcm;
+    int32_t light_inhibit;                 /* 1 = respiration x 0.67 in light (:1828-1830) */
+} ctsmg_canopy_params;
+
+/* pftcon arrays used on the path, indexed by patch%itype (0 .. npft-1)
+ * (src/main/pftconMod.F90): c3psn, slatop, leafcn, flnr, fnitr, dleaf,
+ * medlynslope, medlynintercept, mbbopt and Photosynthesis' theta_cj.     */
+#define CTSMG_MAX_PFT 80
+typedef struct {
+    int32_t npft;
+    double c3psn[CTSMG_MAX_PFT], slatop[CTSMG_MAX_PFT], leafcn[CTSMG_MAX_PFT];
+    double flnr[CTSMG_MAX_PFT], fnitr[CTSMG_MAX_PFT], dleaf[CTSMG_MAX_PFT];
+    double medlynslope[CTSMG_MAX_PFT], medlynintercept[CTSMG_MAX_PFT], theta_cj[CTSMG_MAX_PFT];
+    double mbbopt[CTSMG_MAX_PFT];
+} ctsmg_pftcon;
+
+/* Components CanopyFluxes reads and writes on the natural-vegetation,
+ * satellite-phenology path (associate block src/biogeophys/CanopyFluxesMod.F90:420-640):
+ * ZengWang2007 roughness, no biomass heat storage, no FATES / LUNA / hydraulic
+ * stress / ozone, soil resistance by sl14 (soilresis given).  Patch arrays
+ * (p) use ldp, column arrays (c) ldc, gridcell arrays (g) ldg; patch_column
+ * and patch_gridcell hold the reference's global indices (patch%column,
+ * patch%gridcell).  btran comes from calc_root_moist_stress, the sun/shade
+ * PAR, lai and vcmaxcint from SurfaceRadiation / SurfaceAlbedo.           */
+typedef struct {
+    int32_t ldp, ldc, ldg, begg;
+    /* patch (PatchType) */
+    const int32_t* itype; const int32_t* patch_column; const int32_t* patch_gridcell;
+    /* gridcell forcing (atm2lnd_inst) */
+    const double *forc_u, *forc_v, *forc_hgt_u, *forc_hgt_t, *forc_hgt_q, *forc_pco2, *forc_po2, *dayl, *max_dayl;
+    /* column inputs */
+    const int32_t* snl;
+    const double *forc_pbot, *forc_th, *forc_q, *forc_rho, *forc_lwrad, *thv, *t_grnd, *qg, *qg_snow, *qg_soil,
+        *qg_h2osfc, *dqgdT, *emg, *htvp, *z0mg, *snow_depth, *frac_sno_eff, *frac_h2osfc, *soilresis, *t_h2osfc;
+    const double* t_soisno;                /* [SS] */
+    /* patch inputs */
+    const int32_t* frac_veg_nosno;
+    const double *elai, *esai, *htop, *emv, *fwet, *fdry, *laisun, *laisha, *btran, *sabv, *thm, *t_a10,
+        *parsun_z, *parsha_z, *vcmaxcintsun, *vcmaxcintsha;
+    /* patch in/out */
+    double *displa, *z0mv, *t_veg, *liqcan, *snocan, *cgrnds, *cgrndl;
+    /* patch outputs */
+    double *z0hv, *z0qv, *forc_hgt_u_patch, *forc_hgt_t_patch, *forc_hgt_q_patch, *taf, *qaf, *ustar, *um, *obu,
+        *zeta, *ram1, *rah1, *raw1, *rah2, *raw2, *rb1, *uaf, *vpd, *rhaf;
+    double *eflx_sh_veg, *qflx_evap_veg, *qflx_tran_veg, *eflx_sh_grnd, *eflx_sh_snow, *eflx_sh_soil,
+        *eflx_sh_h2osfc, *qflx_evap_soi, *qflx_ev_snow, *qflx_ev_soil, *qflx_ev_h2osfc;
+    double *t_ref2m, *q_ref2m, *rh_ref2m, *vpd_ref2m, *dlrad, *ulrad, *t_skin, *cgrnd, *taux, *tauy, *err_canopy;
+    double *rssun, *rssha, *psnsun, *psnsha, *lmrsun, *lmrsha, *cisun, *cisha, *gs_mol_sun, *gs_mol_sha,
+        *rh_leaf, *vpd_can, *u10_clm, *u10, *fv, *vds, *fm;
+    int32_t* num_iter;
+} ctsmg_canopy_io;
+
 /* ---------------------------------------------------------------- lifecycle */
 /* Replaces the namelist reads init_soilwater_movement
  * (src/biogeophys/SoilWaterMovementMod.F90:110-216), CanopyFluxesReadNML
@@ -226,6 +291,10 @@ int32_t ctsmg_init(const ctsmg_options* opt);
 
 /* Replaces readParams of SoilWaterMovementMod (src/biogeophys/SoilWaterMovementMod.F90:89-106). */
 int32_t ctsmg_set_soilwater_params(const ctsmg_soilwater_params* p);
+
+/* Replaces readParams of CanopyFluxesMod / PhotosynthesisMod and the pftcon
+ * reads (src/biogeophys/CanopyFluxesMod.F90:159-188, PhotosynthesisMod.F90:809-912). */
+int32_t ctsmg_set_canopy_params(const ctsmg_canopy_params* p, const ctsmg_pftcon* pft);
 
 /* Frees every device buffer and stream. */
 int32_t ctsmg_finalize(void);
@@ -248,6 +317,14 @@ int32_t ctsmg_soilwater(const ctsmg_bounds* bounds,
 int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds,
                               int32_t num_nolakec, const int32_t* filter_nolakec,
                               const ctsmg_soiltemp_io* io, double dtime);
+
+/* CanopyFluxes: src/biogeophys/CanopyFluxesMod.F90:191-1768 with
+ * FrictionVelocity / MoninObukIni (FrictionVelocityMod.F90:754-1209), QSat
+ * (QSatMod.F90:61-127) and Photosynthesis sun + shade with hybrid / brent /
+ * ci_func / quadratic (PhotosynthesisMod.F90:1243-2701, quadraticMod.F90:17-74),
+ * over the exposed-vegetation patch filter (1-based patch indices).       */
+int32_t ctsmg_canopyfluxes(const ctsmg_bounds* bounds, int32_t num_exposedvegp,
+                           const int32_t* filter_exposedvegp, const ctsmg_canopy_io* io, double dtime);
 
 /* Allocation-free SoilTemperature.  No counterpart in the reference: it is an
  * extra entry point for callers that cannot allocate device memory -- a host

@@ -19,6 +19,11 @@ int  oracle_soiltemperature(const ctsmg_bounds* bounds, int num_nolakec,
                             double dtime, int snow_method);
 int  oracle_last_error(int* idx, int* lev);
 void oracle_set_libm_noise(int ulps, unsigned long long seed);
+void oracle_set_canopy_params(const ctsmg_canopy_params* p, const ctsmg_pftcon* pft, int method, int itmax);
+int  oracle_quadratic(double a, double b, double c, double* r1, double* r2);
+void oracle_qsat(double T, double p, double* qs, double* es, double* qsdT);
+int  oracle_canopyfluxes(const ctsmg_bounds* b, int num_exposedvegp, const int32_t* filter_exposedvegp,
+                         const ctsmg_canopy_io* io, double dtime, int* err_index);
 #ifdef __cplusplus
 }
 #endif

@@ -20,6 +20,12 @@
 #include <algorithm>
 #include "ctsm_gpu.h"
 #include "ctsm_oracle.h"
+#include "oracle_libm.h"
+
+namespace oracle_libm {
+int g_noise_ulps = 0;
+uint64_t g_noise_seed = 0;
+}
 
 namespace {
 
@@ -68,37 +74,21 @@ struct IW {
 
 thread_local int g_err = 0, g_err_idx = 0, g_err_lev = 0;
 
-// Optional libm noise for conditioning studies: when g_noise_ulps > 0 every
-// pow / log10 result is scaled by (1 + k eps) with k in [-ulps, ulps] drawn
-// from a hash of the call's arguments and g_noise_seed (deterministic and
-// thread-safe).  Off (0) for every parity run.
-int g_noise_ulps = 0;
-uint64_t g_noise_seed = 0;
-inline uint64_t mix64(uint64_t z) {
-    z += 0x9e3779b97f4a7c15ull;
-    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
-    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
-    return z ^ (z >> 31);
-}
-inline double noisy(double r, double a, double b) {
-    if (g_noise_ulps <= 0) return r;
-    uint64_t ua, ub;
-    std::memcpy(&ua, &a, 8); std::memcpy(&ub, &b, 8);
-    uint64_t h = mix64(ua ^ mix64(ub ^ g_noise_seed));
-    int k = (int)(h % (uint64_t)(2 * g_noise_ulps + 1)) - g_noise_ulps;
-    return r * (1.0 + k * 2.220446049250313e-16);
-}
-inline double o_pow(double x, double y) { return noisy(std::pow(x, y), x, y); }
-inline double o_log10(double x) { return noisy(std::log10(x), x, 1.0); }
+using oracle_libm::o_pow;
+using oracle_libm::o_log10;
 void set_err(int code, int idx, int lev) {
     if (g_err == 0) { g_err = code; g_err_idx = idx; g_err_lev = lev; }
 }
 
 } // namespace
 
+// Optional libm noise for conditioning studies: when ulps > 0 every pow /
+// log10 / exp / log / atan result is scaled by (1 + k eps) with k in
+// [-ulps, ulps] drawn from a hash of the call's arguments and the seed
+// (deterministic and thread-safe).  Off (0) for every parity run.
 extern "C" void oracle_set_libm_noise(int ulps, unsigned long long seed) {
-    g_noise_ulps = ulps;
-    g_noise_seed = seed;
+    oracle_libm::g_noise_ulps = ulps;
+    oracle_libm::g_noise_seed = seed;
 }
 
 // ============================================================ Tridiagonal

@@ -30,6 +30,12 @@ def lib():
         _LIB.oracle_tridiagonal.restype = None
         _LIB.oracle_set_libm_noise.argtypes = [I, C.c_ulonglong]
         _LIB.oracle_set_libm_noise.restype = None
+        _LIB.oracle_set_canopy_params.argtypes = [P(abi.CanopyParams), P(abi.Pftcon), I, I]
+        _LIB.oracle_set_canopy_params.restype = None
+        _LIB.oracle_quadratic.argtypes = [C.c_double] * 3 + [P(C.c_double)] * 2
+        _LIB.oracle_qsat.argtypes = [C.c_double, C.c_double] + [P(C.c_double)] * 3
+        _LIB.oracle_qsat.restype = None
+        _LIB.oracle_canopyfluxes.argtypes = [P(abi.Bounds), I, P(C.c_int32), P(abi.CanopyIO), C.c_double, P(C.c_int)]
     return _LIB
 
 

@@ -36,10 +36,25 @@ def max_rel_err(a, b, floor_frac=1e-12):
     return float(np.nanmax(d / (np.abs(b) + floor))) if d.size else 0.0
 
 
-def noise_spread(run, A, R, fields=CANCELLATION):
-    """Per-element spread of the oracle's outputs `fields` under libm noise.
-    run(B) runs the oracle in place on a copy B of the inputs A; R is the
-    noise-free result."""
+def perturb_inputs(A, ulps, seed, skip=()):
+    """Copy of A with every float64 array scaled elementwise by (1 + k eps),
+    k uniform in [-ulps, ulps]: a stand-in for the rounding differences of
+    the intermediate operations (FMA contraction on the device)."""
+    import copy
+    r = np.random.Generator(np.random.Philox(10_000 + seed))
+    B = copy.deepcopy(A)
+    eps = np.finfo(np.float64).eps
+    for k, v in B.items():
+        if v.dtype == np.float64 and k not in skip:
+            B[k] = v * (1.0 + eps * r.integers(-ulps, ulps + 1, size=v.shape))
+    return B
+
+
+def noise_spread(run, A, R, fields=CANCELLATION, input_ulps=0):
+    """Per-element spread of the oracle's outputs `fields` under libm noise
+    (and, if input_ulps > 0, an independent +-input_ulps perturbation of every
+    floating-point input).  run(B) runs the oracle in place on a copy B of the
+    inputs A; R is the noise-free result."""
     import copy
     from oracle import oracle as orc
     L = orc.lib()
@@ -47,7 +62,7 @@ def noise_spread(run, A, R, fields=CANCELLATION):
     try:
         for seed in range(1, NOISE_RUNS + 1):
             L.oracle_set_libm_noise(NOISE_ULPS, seed)
-            B = copy.deepcopy(A)
+            B = perturb_inputs(A, input_ulps, seed) if input_ulps else copy.deepcopy(A)
             run(B)
             for k in fields:
                 out[k] = np.maximum(out[k], np.abs(B[k] - R[k]))
