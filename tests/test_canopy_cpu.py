@@ -53,9 +53,14 @@ def test_qsat_polynomials_match_coefficient_table():
         L.oracle_qsat(T, 101325.0, C.byref(qs), C.byref(es), C.byref(qd))
         td = min(100.0, max(-75.0, T - 273.15))
         co, cd = (g["a"], g["b"]) if td >= 0 else (g["c"], g["d"])
-        ref = sum(co[k] * td ** k for k in range(9)) * 100.0
-        assert es.value == pytest.approx(ref, rel=1e-13)
-        refd = sum(cd[k] * td ** k for k in range(9)) * 100.0
+        def horner(cs):
+            v = cs[8]
+            for k in range(7, -1, -1):
+                v = cs[k] + td * v
+            return v
+        ref = horner(co) * 100.0
+        assert es.value == pytest.approx(ref, rel=1e-15)
+        refd = horner(cd) * 100.0
         vp = 1.0 / (101325.0 - 0.378 * ref)
         assert qs.value == pytest.approx(ref * 0.622 * vp, rel=1e-13)
         assert qd.value == pytest.approx(refd * 0.622 * vp * vp * 101325.0, rel=1e-12)
