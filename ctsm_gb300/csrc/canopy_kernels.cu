@@ -214,13 +214,14 @@ __device__ __forceinline__ double fth25(double hd, double se) {
 struct PhaseOut { double rs, psn, lmr, ci, gs_mol_phase; };
 
 // PhotosynthesisMod.F90:1243-2062, one phase, nlevcan = nrad = 1
-__device__ PhaseOut photosynthesis(const CanopyArgs& A, int pidx, int ivt, double t_veg, double t10, double tgcm,
+__device__ PhaseOut photosynthesis(const CanopyArgs& A, int p, int pidx, int ivt, double t_veg, double t10, double tgcm,
                                    double forc_pbot, double esat_tv, double eair, double oair, double cair, double rb,
                                    double btran, double dayl_factor, double par_z, double lai_z, double vcmaxcint,
                                    PsnState& st, double& vpd_can, double& rh_leaf, Err& err) {
     const ctsmg_canopy_params& P = A.par;
     const ctsmg_pftcon& F = A.pft;
     const int method = A.method;
+    const double medlyn_int = A.medlynintercept_p ? A.medlynintercept_p[p] : F.medlynintercept[ivt];
     const bool c3 = (llround(F.c3psn[ivt]) == 1);
     const double qe = c3 ? 0.0 : 0.05;
     double bbb = 0.0, mbb = 0.0;
@@ -274,7 +275,7 @@ __device__ PhaseOut photosynthesis(const CanopyArgs& A, int pidx, int ivt, doubl
         st.ac = st.aj = st.ap = st.ag = 0.0;
         st.an = 0.0 - lmr_z;
         psn_z = 0.0;
-        rs_z = (method == 0) ? fmin(rsmax0, 1.0 / bbb * cf) : fmin(rsmax0, 1.0 / F.medlynintercept[ivt] * cf);
+        rs_z = (method == 0) ? fmin(rsmax0, 1.0 / bbb * cf) : fmin(rsmax0, 1.0 / medlyn_int * cf);
         ci_z = 0.0;
         rh_leaf = 0.0;
         out.gs_mol_phase = cf / rs_z;
@@ -290,11 +291,12 @@ __device__ PhaseOut photosynthesis(const CanopyArgs& A, int pidx, int ivt, doubl
         const double qabs = 0.5 * (1.0 - P.fnps) * par_z * 4.6;
         double r1, r2;
         if (!quadratic(P.theta_psii, -(qabs + jmax_z), qabs * jmax_z, r1, r2)) flag(err, CTSMG_E_DISCRIMINANT, pidx);
+        const double mslope = A.medlynslope_p ? A.medlynslope_p[p] : F.medlynslope[ivt];
         PsnCtx ctx{c3, vcmax_z, cp, kc, ko, qe, tpu_z, kp_z, F.theta_cj[ivt], P.theta_ip, forc_pbot,
-                   F.medlynslope[ivt], F.medlynintercept[ivt], bbb, mbb, method, gb_mol, fmin(r1, r2), cair, oair,
+                   mslope, medlyn_int, bbb, mbb, method, gb_mol, fmin(r1, r2), cair, oair,
                    lmr_z, par_z, rh_can};
         hybrid(c3 ? 0.7 * cair : 0.4 * cair, ctx, st, err, pidx);
-        if (st.an < 0.0) st.gs_mol = (method == 0) ? bbb : F.medlynintercept[ivt];
+        if (st.an < 0.0) st.gs_mol = (method == 0) ? bbb : medlyn_int;
         out.gs_mol_phase = st.gs_mol;
         ci_z = cair - st.an * forc_pbot * (1.4 * st.gs_mol + 1.6 * gb_mol) / (gb_mol * st.gs_mol);
         ci_z = fmax(ci_z, 1.e-06);
@@ -484,10 +486,10 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, Err& err, double dtime) {
     s.vpd_last = fmax((svpts - eah), 50.0) * 0.001;
     const double thm = io.thm[p], btran = io.btran[p];
     const double laisun = io.laisun[p], laisha = io.laisha[p];
-    s.sun = photosynthesis(A, pg, s.ivt, s.t_veg, io.t_a10[p], thm, forc_pbot, svpts, eah, io.forc_po2[g],
+    s.sun = photosynthesis(A, p, pg, s.ivt, s.t_veg, io.t_a10[p], thm, forc_pbot, svpts, eah, io.forc_po2[g],
                            io.forc_pco2[g], rb, btran, s.dayl_factor, io.parsun_z[p], laisun, io.vcmaxcintsun[p],
                            s.st, s.vpd_can, s.rh_leaf, err);
-    s.sha = photosynthesis(A, pg, s.ivt, s.t_veg, io.t_a10[p], thm, forc_pbot, svpts, eah, io.forc_po2[g],
+    s.sha = photosynthesis(A, p, pg, s.ivt, s.t_veg, io.t_a10[p], thm, forc_pbot, svpts, eah, io.forc_po2[g],
                            io.forc_pco2[g], rb, btran, s.dayl_factor, io.parsha_z[p], laisha, io.vcmaxcintsha[p],
                            s.st, s.vpd_can, s.rh_leaf, err);
     const double sa_leaf = elai + esai;
@@ -649,8 +651,8 @@ __device__ void finalize(const CanopyArgs& A, const Patch& s, double dtime) {
                    emv * (1.0 + (1.0 - emg) * (1.0 - emv)) * SB * 0.0 * (0.0 + 4.0 * 0.0) * 0.0 +
                    emg * (1.0 - emv) * SB * lw_grnd);
     io.t_skin[p] = emv * t_veg + (1.0 - emv) * sqrt(sqrt(lw_grnd));
-    const double cgrnds = io.cgrnds[p] + CPAIR * forc_rho * s.wtg * s.wtal;
-    const double cgrndl = io.cgrndl[p] + forc_rho * s.wtgq * s.wtalq * io.dqgdT[c];
+    const double cgrnds = (A.engine ? 0.0 : io.cgrnds[p]) + CPAIR * forc_rho * s.wtg * s.wtal;
+    const double cgrndl = (A.engine ? 0.0 : io.cgrndl[p]) + forc_rho * s.wtgq * s.wtalq * io.dqgdT[c];
     io.cgrnds[p] = cgrnds;
     io.cgrndl[p] = cgrndl;
     io.cgrnd[p] = cgrnds + cgrndl * io.htvp[c];
@@ -667,8 +669,10 @@ __device__ void finalize(const CanopyArgs& A, const Patch& s, double dtime) {
     if (fabs(snocan) < 1.e-10 * fabs(snocan_baseline)) snocan = 0.0;
     io.liqcan[p] = liqcan;
     io.snocan[p] = snocan;
-    io.displa[p] = s.displa;
-    io.z0mv[p] = s.z0mv;
+    if (!A.engine) {
+        io.displa[p] = s.displa;
+        io.z0mv[p] = s.z0mv;
+    }
     io.z0hv[p] = s.z0mv;
     io.z0qv[p] = s.z0mv;
     io.forc_hgt_u_patch[p] = s.hgt_u;

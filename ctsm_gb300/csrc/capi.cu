@@ -105,7 +105,7 @@ int kind_levels(int kind) {
         case K_SS: return NLEVSNO + NLEVGRND;
         case K_ZI: return NLEVSNO + NLEVGRND + 1;
         case K_G: return NLEVGRND;
-        case K_S: return NLEVSOI;
+        case K_S: case K_PS: return NLEVSOI;
         case K_SN: return NLEVSNO;
         case K_PL: return NLEVSNO + 1;
     }
@@ -283,7 +283,7 @@ static inline void*& field_ptr(void* io, const FieldDesc& f) {
 }
 
 size_t field_bytes(const FieldDesc& f, int ldc, int ldp, int ldg) {
-    int ld = (f.kind == K_P || f.kind == K_PL) ? ldp : (f.kind == K_GR ? ldg : ldc);
+    int ld = (f.kind == K_P || f.kind == K_PL || f.kind == K_PS) ? ldp : (f.kind == K_GR ? ldg : ldc);
     return (size_t)ld * kind_levels(f.kind) * f.esize;
 }
 
@@ -535,6 +535,9 @@ extern "C" int32_t ctsmg_canopyfluxes(const ctsmg_bounds* bounds, int32_t num_ex
     }
     a.begc = bounds->begc;
     a.begp = bounds->begp;
+    a.engine = 0;
+    a.medlynslope_p = nullptr;
+    a.medlynintercept_p = nullptr;
     e = launch_canopy(a, num_exposedvegp, dfilt, dtime, counter, c->err, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "canopy kernel launch");
     if ((rc = stage_out(c, io, &a.io, CANOPY_TABLE, CANOPY_NFIELDS, ldc, ldp, ldg))) return rc;

@@ -5,7 +5,7 @@
 #include "ctsm_gpu.h"
 
 namespace ctsmg {
-enum Kind { K_C, K_P, K_SS, K_ZI, K_G, K_S, K_SN, K_PL, K_GR };
+enum Kind { K_C, K_P, K_SS, K_ZI, K_G, K_S, K_SN, K_PL, K_GR, K_PS };
 enum Use { U_IN, U_OUT, U_INOUT };
 struct FieldDesc { size_t offset; int kind; int esize; int use; const char* name; };
 

@@ -1,6 +1,7 @@
-// engine.cu -- batched resident mode: many columns of uneven depth kept in
-// HBM across model steps, bucketed by level count, each step replayed as one
-// CUDA graph (SoilWater + SoilTemperature + the h2osoi_vol refresh).
+// engine.cu -- batched resident mode: many columns (and their patches) kept in
+// HBM across model steps, columns bucketed by level count, each step replayed
+// as one CUDA graph: [CanopyFluxes -> root sink ->] SoilWater / SoilTemperature
+// -> h2osoi_vol refresh.
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cstdint>
@@ -12,11 +13,12 @@
 #include "ctsm_gpu.h"
 #include "ctsm_device.cuh"
 #include "soil_kernels.cuh"
+#include "canopy_kernels.cuh"
 #include "capi_internal.h"
 
 namespace ctsmg {
 
-struct UField {              // one resident component (shared by both io structs)
+struct UField {              // one resident component (shared by every io struct naming it)
     std::string name;
     int kind, esize, use;
     void* dptr = nullptr;
@@ -24,13 +26,17 @@ struct UField {              // one resident component (shared by both io struct
 };
 
 struct Batch {
-    int ncol = 0, npatch = 0;
-    double dtime = 1800.0, e_ice = 6.0;
-    int snow_method = 0;
+    ctsmg_batch_config cfg{};
     int block = 128;
     std::vector<UField> fields;
+    std::map<std::string, int> index;
     ctsmg_soilwater_io dsw{};
     ctsmg_soiltemp_io dst{};
+    CanopyArgs cargs{};
+    double* rootr = nullptr;
+    double* mslope = nullptr;
+    double* mint = nullptr;
+    int* counter = nullptr;
     int32_t* d_perm = nullptr;     // sorted position -> original column index (0-based)
     double* ws = nullptr;
     DevError* err = nullptr;
@@ -54,14 +60,27 @@ static void set_io_ptr(void* io, const FieldDesc& f, void* p) {
     *reinterpret_cast<void**>(reinterpret_cast<char*>(io) + f.offset) = p;
 }
 
+static cudaError_t enqueue_step(Batch* b) {
+    cudaError_t e = cudaSuccess;
+    const int ncol = b->cfg.ncol;
+    if (b->cfg.with_canopy) {
+        e = launch_canopy(b->cargs, b->cfg.npatch, nullptr, b->cfg.dtime, b->counter, b->err, b->stream);
+        if (e != cudaSuccess) return e;
+        e = launch_rootsink(b->dst.col_patchi, b->dst.col_npatches, b->dst.wtcol, b->cargs.io.qflx_tran_veg,
+                            b->rootr, b->cfg.npatch, (double*)b->dsw.qflx_rootsoi, ncol, b->stream);
+        if (e != cudaSuccess) return e;
+    }
+    return launch_soilstep(b->dsw, b->dst, ncol, b->cfg.e_ice, b->cfg.dtime, b->cfg.snow_thermal_cond_method, b->ws,
+                           ncol, b->err, b->stream, b->block, b->cfg.order);
+}
+
 static int build_graph(Batch* b) {
     if (b->graph) { cudaGraphExecDestroy(b->graph); b->graph = nullptr; }
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
-    cudaError_t le = launch_soilstep(b->dsw, b->dst, b->ncol, b->e_ice, b->dtime, b->snow_method, b->ws,
-                                     b->ncol, b->err, b->stream, b->block);
+    cudaError_t le = enqueue_step(b);
     cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
-    if (le != cudaSuccess) return cuda_err(le, "soilstep capture");
+    if (le != cudaSuccess) return cuda_err(le, "step capture");
     if (ce != cudaSuccess) return cuda_err(ce, "cudaStreamEndCapture");
     cudaError_t ie = cudaGraphInstantiate(&b->graph, g, 0);
     cudaGraphDestroy(g);
@@ -74,15 +93,16 @@ static void batch_free(Batch* b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->graph) cudaGraphExecDestroy(b->graph);
     for (auto& f : b->fields) if (f.dptr) cudaFree(f.dptr);
-    if (b->d_perm) cudaFree(b->d_perm);
-    if (b->ws) cudaFree(b->ws);
-    if (b->err) cudaFree(b->err);
-    if (b->snapshot) cudaFree(b->snapshot);
+    for (void* p : {(void*)b->d_perm, (void*)b->ws, (void*)b->err, b->snapshot, (void*)b->rootr, (void*)b->mslope,
+                    (void*)b->mint, (void*)b->counter})
+        if (p) cudaFree(p);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }
+
+static bool is_column_kind(int k) { return !(k == K_P || k == K_PL || k == K_PS || k == K_GR); }
 
 } // namespace ctsmg
 
@@ -90,14 +110,26 @@ using namespace ctsmg;
 
 struct ctsmg_batch_s { Batch* b; };
 
-extern "C" int32_t ctsmg_batch_create(ctsmg_batch* out, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
-                                      int32_t ncol, int32_t npatch, double dtime, double e_ice,
-                                      int32_t snow_thermal_cond_method) {
-    if (!out || !sw || !st) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
+extern "C" int32_t ctsmg_batch_create2(ctsmg_batch* out, const ctsmg_batch_config* cfg, const ctsmg_soilwater_io* sw,
+                                       const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio, const double* rootr,
+                                       const double* medlynslope_p, const double* medlynintercept_p,
+                                       const ctsmg_canopy_params* cpar, const ctsmg_pftcon* pft) {
+    if (!out || !cfg || !sw || !st) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
+    const int ncol = cfg->ncol, npatch = cfg->npatch;
     if (ncol <= 0 || npatch < 0) return set_error(CTSMG_E_ARG, "ncol must be positive", 0, 0);
     if (sw->ldc != ncol || st->ldc != ncol || st->ldp != npatch)
         return set_error(CTSMG_E_ARG, "batch arrays must be dense: ldc = ncol, ldp = npatch", 0, 0);
-    if (!(dtime > 0.0)) return set_error(CTSMG_E_ARG, "dtime must be positive", 0, 0);
+    if (!(cfg->dtime > 0.0)) return set_error(CTSMG_E_ARG, "dtime must be positive", 0, 0);
+    if (cfg->with_canopy) {
+        if (!cio || !rootr || !cpar || !pft) return set_error(CTSMG_E_ARG, "with_canopy needs cio, rootr, params", 0, 0);
+        if (cio->ldc != ncol || cio->ldp != npatch || cio->ldg != cfg->ngrid || cio->begg != 1)
+            return set_error(CTSMG_E_ARG, "canopy arrays must be dense (ldg = ngrid, begg = 1)", 0, 0);
+        for (int p = 0; p < npatch; ++p) {
+            const int cc = cio->patch_column[p], gg = cio->patch_gridcell[p], it = cio->itype[p];
+            if (cc < 1 || cc > ncol || gg < 1 || gg > cfg->ngrid || it < 0 || it >= pft->npft)
+                return set_error(CTSMG_E_ARG, "patch column / gridcell / itype out of range", p + 1, 0);
+        }
+    }
     for (int c = 0; c < ncol; ++c) {
         const int s = st->snl[c], pi = st->col_patchi[c], np = st->col_npatches[c];
         if (s > 0 || s < -NLEVSNO) return set_error(CTSMG_E_ARG, "snl outside -nlevsno..0", c + 1, 0);
@@ -105,8 +137,7 @@ extern "C" int32_t ctsmg_batch_create(ctsmg_batch* out, const ctsmg_soilwater_io
             return set_error(CTSMG_E_ARG, "column patches outside 1..npatch", c + 1, 0);
     }
     Batch* b = new Batch();
-    b->ncol = ncol; b->npatch = npatch; b->dtime = dtime; b->e_ice = e_ice;
-    b->snow_method = snow_thermal_cond_method;
+    b->cfg = *cfg;
     auto fail = [&](int rc) { batch_free(b); return rc; };
     cudaError_t e;
     if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(cuda_err(e, "stream"));
@@ -114,32 +145,37 @@ extern "C" int32_t ctsmg_batch_create(ctsmg_batch* out, const ctsmg_soilwater_io
     if ((e = cudaEventCreate(&b->ev1)) != cudaSuccess) return fail(cuda_err(e, "event"));
 
     // bucket columns: more snow layers first, then shallower bedrock
-    std::vector<int32_t> perm(ncol);
+    std::vector<int32_t> perm(ncol), inv(ncol);
     std::iota(perm.begin(), perm.end(), 0);
-    std::stable_sort(perm.begin(), perm.end(), [&](int a, int c) {
-        if (st->snl[a] != st->snl[c]) return st->snl[a] < st->snl[c];
-        return st->nbedrock[a] < st->nbedrock[c];
-    });
+    if (cfg->bucket)
+        std::stable_sort(perm.begin(), perm.end(), [&](int a, int c) {
+            if (st->snl[a] != st->snl[c]) return st->snl[a] < st->snl[c];
+            return st->nbedrock[a] < st->nbedrock[c];
+        });
+    for (int i = 0; i < ncol; ++i) inv[perm[i]] = i;
     if ((e = cudaMalloc(&b->d_perm, (size_t)ncol * 4)) != cudaSuccess) return fail(cuda_err(e, "perm"));
     if ((e = cudaMemcpy(b->d_perm, perm.data(), (size_t)ncol * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
         return fail(cuda_err(e, "perm H2D"));
+    std::vector<int32_t> pcol_new;
+    if (cfg->with_canopy) {
+        pcol_new.resize(npatch);
+        for (int p = 0; p < npatch; ++p) pcol_new[p] = inv[cio->patch_column[p] - 1] + 1;
+    }
 
-    // the union of both component tables, one resident buffer per component
-    std::map<std::string, int> index;
     auto add = [&](const FieldDesc* tab, int nf, const void* hio, void* dio) -> int {
         for (int i = 0; i < nf; ++i) {
             const FieldDesc& f = tab[i];
-            auto it = index.find(f.name);
-            if (it == index.end()) {
+            auto it = b->index.find(f.name);
+            if (it == b->index.end()) {
                 UField u;
                 u.name = f.name; u.kind = f.kind; u.esize = f.esize; u.use = f.use;
-                u.bytes = field_bytes(f, ncol, npatch);
+                u.bytes = field_bytes(f, ncol, npatch, cfg->ngrid);
                 cudaError_t ee = cudaMalloc(&u.dptr, u.bytes);
                 if (ee != cudaSuccess) return cuda_err(ee, "cudaMalloc(field)");
                 const void* hp = io_ptr(hio, f);
                 if (!hp) return set_error(CTSMG_E_ARG, (std::string("null component ") + f.name).c_str(), 0, 0);
-                // upload, then gather columns into bucket order (patch arrays stay in place)
-                if (f.kind == K_P || f.kind == K_PL) {
+                if (std::string(f.name) == "patch_column") hp = pcol_new.data();
+                if (!is_column_kind(f.kind)) {
                     ee = cudaMemcpy(u.dptr, hp, u.bytes, cudaMemcpyHostToDevice);
                 } else {
                     void* tmp = nullptr;
@@ -150,9 +186,11 @@ extern "C" int32_t ctsmg_batch_create(ctsmg_batch* out, const ctsmg_soilwater_io
                     if (tmp) cudaFree(tmp);
                 }
                 if (ee != cudaSuccess) return cuda_err(ee, "upload");
-                index[f.name] = (int)b->fields.size();
+                b->index[f.name] = (int)b->fields.size();
                 b->fields.push_back(u);
-                it = index.find(f.name);
+                it = b->index.find(f.name);
+            } else if (b->fields[it->second].use == U_IN && f.use != U_IN) {
+                b->fields[it->second].use = f.use;      // written by some call of the step
             }
             set_io_ptr(dio, f, b->fields[it->second].dptr);
         }
@@ -163,6 +201,31 @@ extern "C" int32_t ctsmg_batch_create(ctsmg_batch* out, const ctsmg_soilwater_io
     int rc;
     if ((rc = add(SOILWATER_TABLE, SOILWATER_NFIELDS, sw, &b->dsw))) return fail(rc);
     if ((rc = add(SOILTEMP_TABLE, SOILTEMP_NFIELDS, st, &b->dst))) return fail(rc);
+    if (cfg->with_canopy) {
+        std::memcpy(&b->cargs.io, cio, sizeof b->cargs.io);
+        if ((rc = add(CANOPY_TABLE, CANOPY_NFIELDS, cio, &b->cargs.io))) return fail(rc);
+        b->cargs.par = *cpar;
+        b->cargs.pft = *pft;
+        b->cargs.method = cfg->stomatalcond_method;
+        b->cargs.itmax = cfg->itmax_canopy_fluxes;
+        b->cargs.begc = 1;
+        b->cargs.begp = 1;
+        b->cargs.engine = 1;
+        const size_t pb = (size_t)npatch * 8;
+        if ((e = cudaMalloc(&b->rootr, pb * NLEVSOI)) != cudaSuccess) return fail(cuda_err(e, "rootr"));
+        if ((e = cudaMemcpy(b->rootr, rootr, pb * NLEVSOI, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(cuda_err(e, "rootr"));
+        if (medlynslope_p) {
+            if ((e = cudaMalloc(&b->mslope, pb)) != cudaSuccess) return fail(cuda_err(e, "mslope"));
+            if ((e = cudaMemcpy(b->mslope, medlynslope_p, pb, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(cuda_err(e, "mslope"));
+        }
+        if (medlynintercept_p) {
+            if ((e = cudaMalloc(&b->mint, pb)) != cudaSuccess) return fail(cuda_err(e, "mint"));
+            if ((e = cudaMemcpy(b->mint, medlynintercept_p, pb, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(cuda_err(e, "mint"));
+        }
+        b->cargs.medlynslope_p = b->mslope;
+        b->cargs.medlynintercept_p = b->mint;
+        if ((e = cudaMalloc(&b->counter, 256)) != cudaSuccess) return fail(cuda_err(e, "counter"));
+    }
     for (auto& f : b->fields) b->state_bytes += f.bytes;
     if ((e = cudaMalloc(&b->ws, (size_t)SOILTEMP_WS_DOUBLES_PER_COL * ncol * 8)) != cudaSuccess) return fail(cuda_err(e, "ws"));
     if ((e = cudaMalloc(&b->err, sizeof(DevError))) != cudaSuccess) return fail(cuda_err(e, "err"));
@@ -170,6 +233,18 @@ extern "C" int32_t ctsmg_batch_create(ctsmg_batch* out, const ctsmg_soilwater_io
     if ((rc = build_graph(b))) return fail(rc);
     *out = new ctsmg_batch_s{b};
     return 0;
+}
+
+extern "C" int32_t ctsmg_batch_create(ctsmg_batch* out, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
+                                      int32_t ncol, int32_t npatch, double dtime, double e_ice,
+                                      int32_t snow_thermal_cond_method) {
+    ctsmg_batch_config cfg{};
+    cfg.ncol = ncol; cfg.npatch = npatch; cfg.ngrid = 0;
+    cfg.dtime = dtime; cfg.e_ice = e_ice;
+    cfg.snow_thermal_cond_method = snow_thermal_cond_method;
+    cfg.stomatalcond_method = 1; cfg.itmax_canopy_fluxes = 40;
+    cfg.order = 0; cfg.with_canopy = 0; cfg.bucket = 1;
+    return ctsmg_batch_create2(out, &cfg, sw, st, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
 }
 
 extern "C" int32_t ctsmg_batch_run(ctsmg_batch bh, int32_t nsteps, float* step_ms) {
@@ -194,48 +269,61 @@ extern "C" int32_t ctsmg_batch_sync(ctsmg_batch bh) {
     DevError h;
     CK(cudaMemcpy(&h, b->err, sizeof h, cudaMemcpyDeviceToHost), "err D2H");
     if (h.key != ~0ull) {
-        int pos = (int)(h.key >> 32) - 1;
-        int32_t orig = 0;
-        cudaMemcpy(&orig, b->d_perm + pos, 4, cudaMemcpyDeviceToHost);
-        return set_error((int)(h.key & 0xff), "BandDiagonal ERROR: dgbsv returned error code", orig + 1,
+        const int code = (int)(h.key & 0xff);
+        int idx = (int)(h.key >> 32);
+        if (code == CTSMG_E_SINGULAR && idx >= 1 && idx <= b->cfg.ncol) {
+            int32_t orig = 0;
+            cudaMemcpy(&orig, b->d_perm + idx - 1, 4, cudaMemcpyDeviceToHost);
+            idx = orig + 1;
+        }
+        return set_error(code, code == CTSMG_E_SINGULAR ? "BandDiagonal ERROR: dgbsv returned error code"
+                                                        : "CanopyFluxes error", idx,
                          (int)((h.key >> 8) & 0xffffff) - 1024);
     }
     return 0;
 }
 
-extern "C" int32_t ctsmg_batch_download(ctsmg_batch bh, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st) {
-    if (!bh || !sw || !st) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
-    Batch* b = bh->b;
-    CK(cudaStreamSynchronize(b->stream), "sync");
-    auto down = [&](const FieldDesc* tab, int nf, const void* hio) -> int {
-        for (int i = 0; i < nf; ++i) {
-            const FieldDesc& f = tab[i];
-            void* hp = io_ptr(hio, f);
-            const UField* u = nullptr;
-            for (auto& x : b->fields) if (x.name == f.name) { u = &x; break; }
-            if (!u || !hp) continue;
-            if (f.kind == K_P || f.kind == K_PL) {
-                CK(cudaMemcpy(hp, u->dptr, u->bytes, cudaMemcpyDeviceToHost), "D2H");
-            } else {
-                void* tmp = nullptr;
-                CK(cudaMalloc(&tmp, u->bytes), "tmp");
-                cudaError_t e = launch_permute(tmp, u->dptr, b->d_perm, b->ncol, kind_levels(f.kind), f.esize, 1, b->stream);
-                if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
-                if (e == cudaSuccess) e = cudaMemcpy(hp, tmp, u->bytes, cudaMemcpyDeviceToHost);
-                cudaFree(tmp);
-                if (e != cudaSuccess) return cuda_err(e, "download");
-            }
+static int download_table(Batch* b, const FieldDesc* tab, int nf, const void* hio) {
+    for (int i = 0; i < nf; ++i) {
+        const FieldDesc& f = tab[i];
+        void* hp = io_ptr(hio, f);
+        auto it = b->index.find(f.name);
+        if (it == b->index.end() || !hp) continue;
+        const UField& u = b->fields[it->second];
+        if (u.use == U_IN && u.name != "h2osoi_vol" && u.name != "qflx_rootsoi") continue;
+        if (!is_column_kind(u.kind)) {
+            CK(cudaMemcpy(hp, u.dptr, u.bytes, cudaMemcpyDeviceToHost), "D2H");
+        } else {
+            void* tmp = nullptr;
+            CK(cudaMalloc(&tmp, u.bytes), "tmp");
+            cudaError_t e = launch_permute(tmp, u.dptr, b->d_perm, b->cfg.ncol, kind_levels(u.kind), u.esize, 1, b->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+            if (e == cudaSuccess) e = cudaMemcpy(hp, tmp, u.bytes, cudaMemcpyDeviceToHost);
+            cudaFree(tmp);
+            if (e != cudaSuccess) return cuda_err(e, "download");
         }
-        return 0;
-    };
-    int rc;
-    if ((rc = down(SOILWATER_TABLE, SOILWATER_NFIELDS, sw))) return rc;
-    if ((rc = down(SOILTEMP_TABLE, SOILTEMP_NFIELDS, st))) return rc;
+    }
     return 0;
 }
 
-// Times `trial_steps` graph replays per candidate block size on the batch's
-// own data and keeps the fastest; the state is restored afterwards.
+extern "C" int32_t ctsmg_batch_download2(ctsmg_batch bh, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
+                                         const ctsmg_canopy_io* cio) {
+    if (!bh || !sw || !st) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
+    Batch* b = bh->b;
+    CK(cudaStreamSynchronize(b->stream), "sync");
+    int rc;
+    if ((rc = download_table(b, SOILWATER_TABLE, SOILWATER_NFIELDS, sw))) return rc;
+    if ((rc = download_table(b, SOILTEMP_TABLE, SOILTEMP_NFIELDS, st))) return rc;
+    if (cio && b->cfg.with_canopy && (rc = download_table(b, CANOPY_TABLE, CANOPY_NFIELDS, cio))) return rc;
+    return 0;
+}
+
+extern "C" int32_t ctsmg_batch_download(ctsmg_batch bh, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st) {
+    return ctsmg_batch_download2(bh, sw, st, nullptr);
+}
+
+// Times `trial_steps` graph replays per candidate threads-per-block on the
+// batch's own data and keeps the fastest; the state is restored afterwards.
 extern "C" int32_t ctsmg_batch_autotune(ctsmg_batch bh, int32_t trial_steps, int32_t* block_out) {
     if (!bh) return set_error(CTSMG_E_ARG, "null batch", 0, 0);
     Batch* b = bh->b;

@@ -819,18 +819,21 @@ soiltemp_kernel(ctsmg_soiltemp_io io, int begc, int begp, int nfilt, const int32
     if (info != 0) report_error(err, filt ? filt[fc] : fc + begc, info, CTSMG_E_SINGULAR);
 }
 
-// SoilWater followed by SoilTemperature on the same column, then the
+// One model step on one column: SoilWater then SoilTemperature (ORDER 0, the
+// pairing of the plain workloads) or SoilTemperature then SoilWater (ORDER 1,
+// the driver's order after CanopyFluxes, clm_driver.F90:900,950), then the
 // between-step refresh of h2osoi_vol (HydrologyNoDrainageMod.F90:580,590).
-template <int BLOCK>
+template <int BLOCK, int ORDER>
 __global__ void __launch_bounds__(BLOCK)
 soilstep_kernel(ctsmg_soilwater_io wio, ctsmg_soiltemp_io tio, int ncol, double e_ice, double dtime,
                 int snow_method, double* ws, int ws_ld, DevError* err) {
     const int c = blockIdx.x * BLOCK + threadIdx.x;
     if (c >= ncol) return;
-    zd09_column(wio, c, e_ice, dtime);
     Scratch S{ws, ws_ld, c};
+    if (ORDER == 0) zd09_column(wio, c, e_ice, dtime);
     int info = soiltemp_column(tio, c, 1, dtime, snow_method, S);
     if (info != 0) report_error(err, c + 1, info, CTSMG_E_SINGULAR);
+    if (ORDER == 1) zd09_column(wio, c, e_ice, dtime);
     const int ld = wio.ldc;
 #pragma unroll 1
     for (int j = 1; j <= NLEVSOI; ++j) {
@@ -838,6 +841,28 @@ soilstep_kernel(ctsmg_soilwater_io wio, ctsmg_soiltemp_io tio, int ncol, double 
         const double dz = wio.dz[ix];
         ((double*)wio.h2osoi_vol)[c + (size_t)(j - 1) * ld] =
             tio.h2osoi_liq[ix] / (dz * DENH2O) + tio.h2osoi_ice[ix] / (dz * DENICE);
+    }
+}
+
+// Compute_EffecRootFrac_And_VertTranSink_Default
+// (src/biogeophys/SoilWaterPlantSinkMod.F90:332-420): the column root water
+// sink from the patches' transpiration and root fractions.
+__global__ void rootsink_kernel(const int32_t* __restrict__ col_patchi, const int32_t* __restrict__ col_npatches,
+                                const double* __restrict__ wtcol, const double* __restrict__ qflx_tran_veg,
+                                const double* __restrict__ rootr, int ldp, double* __restrict__ qflx_rootsoi,
+                                int ncol) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncol) return;
+    const int p0 = col_patchi[c] - 1, np = col_npatches[c];
+    double temp = 0.0, tran_col = 0.0;
+    for (int p = p0; p < p0 + np; ++p) temp = temp + qflx_tran_veg[p] * wtcol[p];
+    tran_col = temp;
+#pragma unroll 1
+    for (int j = 1; j <= NLEVSOI; ++j) {
+        double rc = 0.0;
+        for (int p = p0; p < p0 + np; ++p) rc = rc + rootr[p + (size_t)(j - 1) * ldp] * qflx_tran_veg[p] * wtcol[p];
+        if (temp != 0.0) rc = rc / temp;
+        qflx_rootsoi[c + (size_t)(j - 1) * ncol] = rc * tran_col;
     }
 }
 
@@ -857,21 +882,38 @@ cudaError_t launch_soiltemp(const ctsmg_soiltemp_io& io, int begc, int begp, int
     return cudaGetLastError();
 }
 
-cudaError_t launch_soilstep(const ctsmg_soilwater_io& wio, const ctsmg_soiltemp_io& tio, int ncol,
-                            double e_ice, double dtime, int snow_method, double* ws, int ws_ld,
-                            DevError* err, cudaStream_t s, int block) {
-    if (ncol <= 0) return cudaSuccess;
+template <int ORDER>
+static void launch_soilstep_order(const ctsmg_soilwater_io& wio, const ctsmg_soiltemp_io& tio, int ncol,
+                                  double e_ice, double dtime, int snow_method, double* ws, int ws_ld,
+                                  DevError* err, cudaStream_t s, int block) {
     switch (block) {
         case 64:
-            soilstep_kernel<64><<<(ncol + 63) / 64, 64, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err);
+            soilstep_kernel<64, ORDER><<<(ncol + 63) / 64, 64, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err);
             break;
         case 256:
-            soilstep_kernel<256><<<(ncol + 255) / 256, 256, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err);
+            soilstep_kernel<256, ORDER><<<(ncol + 255) / 256, 256, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err);
             break;
         default:
-            soilstep_kernel<128><<<(ncol + 127) / 128, 128, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err);
+            soilstep_kernel<128, ORDER><<<(ncol + 127) / 128, 128, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err);
             break;
     }
+}
+
+cudaError_t launch_soilstep(const ctsmg_soilwater_io& wio, const ctsmg_soiltemp_io& tio, int ncol,
+                            double e_ice, double dtime, int snow_method, double* ws, int ws_ld,
+                            DevError* err, cudaStream_t s, int block, int order) {
+    if (ncol <= 0) return cudaSuccess;
+    if (order == 1) launch_soilstep_order<1>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err, s, block);
+    else launch_soilstep_order<0>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err, s, block);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_rootsink(const int32_t* col_patchi, const int32_t* col_npatches, const double* wtcol,
+                            const double* qflx_tran_veg, const double* rootr, int ldp, double* qflx_rootsoi,
+                            int ncol, cudaStream_t s) {
+    if (ncol <= 0) return cudaSuccess;
+    rootsink_kernel<<<(ncol + 127) / 128, 128, 0, s>>>(col_patchi, col_npatches, wtcol, qflx_tran_veg, rootr, ldp,
+                                                       qflx_rootsoi, ncol);
     return cudaGetLastError();
 }
 

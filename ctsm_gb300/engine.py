@@ -21,23 +21,56 @@ def _bind(L):
     L.ctsmg_batch_state_bytes.argtypes = [C.c_void_p]
     L.ctsmg_batch_state_bytes.restype = C.c_int64
     L.ctsmg_batch_destroy.argtypes = [C.c_void_p]
+    L.ctsmg_batch_create2.argtypes = [P(C.c_void_p), P(BatchConfig), P(abi.SoilWaterIO), P(abi.SoilTempIO),
+                                      P(abi.CanopyIO), P(C.c_double), P(C.c_double), P(C.c_double),
+                                      P(abi.CanopyParams), P(abi.Pftcon)]
+    L.ctsmg_batch_download2.argtypes = [C.c_void_p, P(abi.SoilWaterIO), P(abi.SoilTempIO), P(abi.CanopyIO)]
     L._batch_bound = True
 
 
-class SoilBatch:
-    """Resident batch of columns advanced by SoilWater + SoilTemperature steps."""
+class BatchConfig(C.Structure):
+    _fields_ = [("ncol", C.c_int32), ("npatch", C.c_int32), ("ngrid", C.c_int32), ("dtime", C.c_double),
+                ("e_ice", C.c_double), ("snow_thermal_cond_method", C.c_int32), ("stomatalcond_method", C.c_int32),
+                ("itmax_canopy_fluxes", C.c_int32), ("order", C.c_int32), ("with_canopy", C.c_int32),
+                ("bucket", C.c_int32)]
 
-    def __init__(self, state, npatch, dtime=1800.0, e_ice=6.0, snow_thermal_cond_method=0):
+
+class SoilBatch:
+    """Resident batch of columns advanced by model steps: SoilWater +
+    SoilTemperature (order 0), or, with canopy=True, CanopyFluxes + root sink +
+    SoilTemperature + SoilWater in the driver's order (order 1)."""
+
+    def __init__(self, state, npatch, dtime=1800.0, e_ice=6.0, snow_thermal_cond_method=0, canopy=False,
+                 ngrid=None, rootr=None, order=None, bucket=True, stomatalcond_method=1, itmax=40,
+                 params=None, pftcon=None, per_patch_medlyn=False):
+        from . import canopy_inputs
         self.L = load()
         _bind(self.L)
         self.state = state
         self.ncol = state["zwt"].shape[0]
         self.npatch = npatch
+        self.canopy = canopy
+        self.ngrid = ngrid if ngrid is not None else self.ncol
         self._sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS, state, self.ncol)
         self._st = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, state, self.ncol, npatch)
+        cfg = BatchConfig(self.ncol, npatch, self.ngrid, dtime, e_ice, snow_thermal_cond_method, stomatalcond_method,
+                          itmax, (1 if canopy else 0) if order is None else order, 1 if canopy else 0,
+                          1 if bucket else 0)
         self.h = C.c_void_p()
-        check(self.L.ctsmg_batch_create(C.byref(self.h), C.byref(self._sw), C.byref(self._st), self.ncol, npatch,
-                                        dtime, e_ice, snow_thermal_cond_method))
+        if canopy:
+            self._ci = abi.make_io(abi.CanopyIO, abi.CANOPY_FIELDS, state, self.ncol, npatch, self.ngrid, 1)
+            self._rootr = np.ascontiguousarray(rootr, dtype=np.float64)
+            dp = C.POINTER(C.c_double)
+            ms = state["medlynslope_p"].ctypes.data_as(dp) if per_patch_medlyn else None
+            mi = state["medlynintercept_p"].ctypes.data_as(dp) if per_patch_medlyn else None
+            self._par = params if params is not None else canopy_inputs.make_params()
+            self._pft = pftcon if pftcon is not None else canopy_inputs.make_pftcon()
+            check(self.L.ctsmg_batch_create2(C.byref(self.h), C.byref(cfg), C.byref(self._sw), C.byref(self._st),
+                                             C.byref(self._ci), self._rootr.ctypes.data_as(dp), ms, mi,
+                                             C.byref(self._par), C.byref(self._pft)))
+        else:
+            check(self.L.ctsmg_batch_create2(C.byref(self.h), C.byref(cfg), C.byref(self._sw), C.byref(self._st),
+                                             None, None, None, None, None, None))
 
     def run(self, nsteps, timed=False):
         if timed:
@@ -54,7 +87,11 @@ class SoilBatch:
         st = state if state is not None else self.state
         sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS, st, self.ncol)
         tt = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, st, self.ncol, self.npatch)
-        check(self.L.ctsmg_batch_download(self.h, C.byref(sw), C.byref(tt)))
+        if self.canopy:
+            ci = abi.make_io(abi.CanopyIO, abi.CANOPY_FIELDS, st, self.ncol, self.npatch, self.ngrid, 1)
+            check(self.L.ctsmg_batch_download2(self.h, C.byref(sw), C.byref(tt), C.byref(ci)))
+        else:
+            check(self.L.ctsmg_batch_download(self.h, C.byref(sw), C.byref(tt)))
         return st
 
     def autotune(self, trial_steps=2):

@@ -1,0 +1,138 @@
+"""Seeded inputs for the full soil + canopy step (CanopyFluxes, SoilTemperature,
+SoilWater) and for the perturbed-parameter ensemble.
+
+One consistent state: the columns come from inputs.soil_columns (snow, uneven
+bedrock, 1-4 patches per column, every ground flux drawn), their patches
+from canopy_inputs.canopy_patches, and every component the two share
+(snl, t_soisno, t_grnd, t_h2osfc, frac_sno_eff, frac_h2osfc, snow_depth, emg,
+htvp, forc_lwrad, frac_veg_nosno, the patch/column maps) is taken from the
+soil state.  The air temperature of a column is its ground temperature plus
+U(-5,5) K.  Root fractions of every patch follow the fixed profile
+dz_j exp(-3 z_j) (normalised) that the plain workloads use for the sink.
+
+Ensemble members perturb 8 parameters by a factor drawn log-uniformly in
+[0.5, 1.5] (baseflow_scalar, fff, medlynslope, medlynintercept, jmaxb1, kmax,
+om_frac_sf, d_max).  On the scoped path medlynslope and medlynintercept enter
+Photosynthesis (per patch) and om_frac_sf the soil-property preparation; the
+other five act only in routines outside the path (drainage, runoff, LUNA,
+hydraulic stress, soil resistance) and are stored per member without effect.
+"""
+import numpy as np
+
+from . import abi, inputs, canopy_inputs
+
+ENSEMBLE_PARAMS = ("baseflow_scalar", "fff", "medlynslope", "medlynintercept", "jmaxb1", "kmax", "om_frac_sf",
+                   "d_max")
+
+
+def full_state(ncol, seed=0, npatch_max=4, om_frac_sf=1.0, rng=None):
+    """Returns (A, npatch, ngrid, rootr): A holds every soil and canopy
+    component; rootr is (nlevsoi, npatch)."""
+    r = rng if rng is not None else np.random.Generator(np.random.Philox(seed))
+    A, npatch = inputs.soil_columns(ncol, snow=True, nbedrock=(3, 20), forcing="full", npatch_max=npatch_max,
+                                    rng=r)
+    if om_frac_sf != 1.0:
+        _reprep_soil(A, r, om_frac_sf)
+    Cn, _, _, _ = canopy_inputs.canopy_patches(npatch, npatch_max=1, rng=r)
+    ngrid = ncol
+    pcol = np.repeat(np.arange(ncol), A["col_npatches"])
+    # patch -> column / gridcell maps from the soil state
+    Cn["patch_column"] = (pcol + 1).astype(np.int32)
+    Cn["patch_gridcell"] = (pcol + 1).astype(np.int32)
+    # columns: the canopy generator drew one column per patch; draw the
+    # atmosphere per column again, tied to the ground temperature
+    tg = A["t_grnd"]
+    forc_t = tg + r.uniform(-5.0, 5.0, ncol)
+    pbot = r.uniform(86000.0, 101325.0, ncol)
+    qs, _, _ = canopy_inputs.qsat(forc_t, pbot)
+    rh = r.uniform(0.10, 1.00, ncol)
+    forc_q = rh * qs
+    forc_th = forc_t * (100000.0 / pbot) ** (canopy_inputs.RAIR / canopy_inputs.CPAIR)
+    e = forc_q * pbot / (0.622 + 0.378 * forc_q)
+    col = dict(forc_pbot=pbot, forc_q=forc_q, forc_th=forc_th,
+               forc_rho=(pbot - 0.378 * e) / (canopy_inputs.RAIR * forc_t),
+               thv=forc_th * (1.0 + 0.61 * forc_q))
+    qg, _, dqg = canopy_inputs.qsat(tg, pbot)
+    wet = r.uniform(0.5, 1.0, ncol)
+    col.update(qg=qg * wet, qg_snow=qg, qg_soil=qg * wet, qg_h2osfc=qg, dqgdT=dqg * wet,
+               z0mg=np.full(ncol, 0.01), soilresis=r.uniform(50.0, 5000.0, ncol))
+    grid = dict(forc_u=r.uniform(0.5, 20.0, ngrid), forc_v=np.zeros(ngrid), forc_hgt_u=np.full(ngrid, 30.0),
+                forc_hgt_t=np.full(ngrid, 30.0), forc_hgt_q=np.full(ngrid, 30.0), forc_pco2=400.e-6 * pbot,
+                forc_po2=0.209 * pbot, dayl=r.uniform(28800.0, 57600.0, ngrid), max_dayl=np.full(ngrid, 57600.0))
+    for k, v in list(col.items()) + list(grid.items()):
+        A[k] = np.ascontiguousarray(v)
+    A["thm"] = forc_t[pcol] + 0.0098 * 30.0
+    A["t_a10"] = forc_t[pcol] + r.uniform(-3.0, 3.0, npatch)
+    A["t_veg"] = forc_t[pcol] + r.uniform(-2.0, 2.0, npatch)
+    A["snocan"] = np.where(A["t_veg"] < canopy_inputs.TFRZ, Cn["snocan"], 0.0)
+    # remaining canopy components (vegetation, radiation, outputs)
+    for (n, kind, dt, use) in abi.CANOPY_FIELDS:
+        if n not in A:
+            A[n] = Cn[n]
+    A["frac_veg_nosno"][:] = 1
+    # absorbed ground solar consistent with the soil's sabg_lyr (sum over layers)
+    dzs, zs, _ = inputs.layer_structure_20sl()
+    prof = np.array([dzs[j] * np.exp(-3.0 * zs[j]) for j in range(abi.NLEVSOI)])
+    prof = prof / prof.sum()
+    rootr = np.ascontiguousarray(np.repeat(prof[:, None], npatch, axis=1))
+    return A, npatch, ngrid, rootr
+
+
+def _reprep_soil(A, r, om_frac_sf):
+    """Soil properties with the organic-matter scale factor om_frac_sf
+    (SoilStateInitTimeConstMod.F90:452: om_frac = min(om_frac_sf*om/organic_max, 1))."""
+    ncol = A["zwt"].shape[0]
+    sand = r.uniform(5.0, 80.0, ncol)
+    clay = np.minimum(r.uniform(5.0, 85.0, ncol), 95.0 - sand)
+    om = np.minimum(r.uniform(0.0, 130.0, ncol) * om_frac_sf, inputs.ORGANIC_MAX)
+    _, zs, _ = inputs.layer_structure_20sl()
+    props = inputs.pedotransfer(sand, clay, om, zs)
+    for k in ("watsat", "bsw", "sucsat", "hksat", "tkmg", "tkdry", "csol"):
+        A[k][:] = props[k]
+
+
+def ensemble(nmembers, seed=0, cols=(512, 8192), npatch_max=4):
+    """Pack `nmembers` members (column counts U{cols}) into one state.
+    Returns (A, npatch, ngrid, rootr, member_of_column, params) with params a
+    dict name -> (nmembers,) factors and per-patch Medlyn arrays in A."""
+    r = np.random.Generator(np.random.Philox(seed))
+    factors = {k: np.exp(r.uniform(np.log(0.5), np.log(1.5), nmembers)) for k in ENSEMBLE_PARAMS}
+    ncols = r.integers(cols[0], cols[1] + 1, nmembers)
+    parts = []
+    for m in range(nmembers):
+        rm = np.random.Generator(np.random.Philox(seed * 1000003 + m + 1))
+        parts.append(full_state(int(ncols[m]), npatch_max=npatch_max, om_frac_sf=float(factors["om_frac_sf"][m]),
+                                rng=rm))
+    A, npatch, ngrid, rootr = concat(parts)
+    member_col = np.repeat(np.arange(nmembers), ncols).astype(np.int32)
+    member_patch = np.repeat(np.arange(nmembers), [p[1] for p in parts]).astype(np.int32)
+    pft = canopy_inputs.DEFAULT_PFT
+    it = A["itype"]
+    base_slope = np.array([row[6] for row in pft])[it]
+    base_int = np.array([row[7] for row in pft])[it]
+    A["medlynslope_p"] = np.ascontiguousarray(base_slope * factors["medlynslope"][member_patch])
+    A["medlynintercept_p"] = np.ascontiguousarray(base_int * factors["medlynintercept"][member_patch])
+    return A, npatch, ngrid, rootr, member_col, factors
+
+
+def concat(parts):
+    """Concatenate full states along columns / patches / gridcells, fixing the
+    1-based index maps."""
+    out = {}
+    ncol_off = npat_off = 0
+    pieces = {}
+    for (A, npatch, ngrid, rootr) in parts:
+        ncol = A["zwt"].shape[0]
+        B = dict(A)
+        B["col_patchi"] = A["col_patchi"] + npat_off
+        B["patch_column"] = A["patch_column"] + ncol_off
+        B["patch_gridcell"] = A["patch_gridcell"] + ncol_off
+        B["_rootr"] = rootr
+        for k, v in B.items():
+            pieces.setdefault(k, []).append(v)
+        ncol_off += ncol
+        npat_off += npatch
+    for k, vs in pieces.items():
+        out[k] = np.ascontiguousarray(np.concatenate(vs, axis=-1))
+    rootr = out.pop("_rootr")
+    return out, npat_off, ncol_off, rootr

@@ -354,6 +354,28 @@ int32_t ctsmg_soiltemperature_noalloc(const ctsmg_bounds* bounds, int32_t num_no
  * are reordered on the device by (snl, nbedrock) so that warps see uniform
  * level counts, and restored to the caller's order by ctsmg_batch_download. */
 typedef struct ctsmg_batch_s* ctsmg_batch;
+
+/* Full configuration of a batch.  with_canopy = 1 adds CanopyFluxes over all
+ * npatch patches before the soil step and the root water sink that couples
+ * transpiration into SoilWater (Compute_EffecRootFrac_And_VertTranSink_Default,
+ * src/biogeophys/SoilWaterPlantSinkMod.F90:332-420); order = 1 is the driver's
+ * order CanopyFluxes, SoilTemperature, SoilWater (src/main/clm_driver.F90:766,900,950),
+ * order = 0 is SoilWater then SoilTemperature.  bucket = 1 reorders the
+ * columns by (snl, nbedrock) on the device.                               */
+typedef struct {
+    int32_t ncol, npatch, ngrid;
+    double dtime, e_ice;
+    int32_t snow_thermal_cond_method, stomatalcond_method, itmax_canopy_fluxes;
+    int32_t order, with_canopy, bucket;
+} ctsmg_batch_config;
+
+/* cio/rootr/medlyn*_p may be NULL when with_canopy = 0.  rootr is (p, 1:nlevsoi)
+ * with ldp = npatch; medlynslope_p / medlynintercept_p (p) override the pftcon
+ * values per patch (perturbed-parameter ensemble members) or are NULL.     */
+int32_t ctsmg_batch_create2(ctsmg_batch* out, const ctsmg_batch_config* cfg, const ctsmg_soilwater_io* sw,
+                            const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio, const double* rootr,
+                            const double* medlynslope_p, const double* medlynintercept_p,
+                            const ctsmg_canopy_params* cpar, const ctsmg_pftcon* pft);
 int32_t ctsmg_batch_create(ctsmg_batch* out, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
                            int32_t ncol, int32_t npatch, double dtime, double e_ice,
                            int32_t snow_thermal_cond_method);
@@ -365,6 +387,9 @@ int32_t ctsmg_batch_run(ctsmg_batch b, int32_t nsteps, float* step_ms);
 int32_t ctsmg_batch_sync(ctsmg_batch b);
 /* Copy the resident state back into the caller's host arrays (caller order). */
 int32_t ctsmg_batch_download(ctsmg_batch b, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st);
+/* Same, and the canopy components as well when the batch runs CanopyFluxes. */
+int32_t ctsmg_batch_download2(ctsmg_batch b, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
+                              const ctsmg_canopy_io* cio);
 /* Time trial_steps steps for each candidate threads-per-block (64, 128, 256)
  * on the batch's own data, keep the fastest, restore the state. */
 int32_t ctsmg_batch_autotune(ctsmg_batch b, int32_t trial_steps, int32_t* block_out);

@@ -18,8 +18,11 @@ int  oracle_soiltemperature(const ctsmg_bounds* bounds, int num_nolakec,
                             const int32_t* filter_nolakec, const ctsmg_soiltemp_io* io,
                             double dtime, int snow_method);
 int  oracle_last_error(int* idx, int* lev);
+void oracle_rootsink(int ncol, int ldp, const int32_t* col_patchi, const int32_t* col_npatches,
+                     const double* wtcol, const double* qflx_tran_veg, const double* rootr, double* qflx_rootsoi);
 void oracle_set_libm_noise(int ulps, unsigned long long seed);
 void oracle_set_canopy_params(const ctsmg_canopy_params* p, const ctsmg_pftcon* pft, int method, int itmax);
+void oracle_set_patch_medlyn(const double* slope, const double* intercept);
 int  oracle_quadratic(double a, double b, double c, double* r1, double* r2);
 void oracle_qsat(double T, double p, double* qs, double* es, double* qsdT);
 int  oracle_canopyfluxes(const ctsmg_bounds* b, int num_exposedvegp, const int32_t* filter_exposedvegp,

@@ -257,6 +257,10 @@ void hybrid(double& x0, const PsnCtx& ctx, PsnState& st) {
 
 struct Params { ctsmg_canopy_params c; ctsmg_pftcon pft; int method; int itmax; };
 Params g_par;
+// optional per-patch Medlyn parameters (ensemble members), indexed by the
+// 1-based global patch index minus 1
+const double* g_mslope_p = nullptr;
+const double* g_mint_p = nullptr;
 
 double ft(double tl, double ha) { return o_exp(ha / (RGAS * 1.e-3 * (TFRZ + 25.0)) * (1.0 - (TFRZ + 25.0) / tl)); }
 double fth(double tl, double hd, double se, double sf) { return sf / (1.0 + o_exp((-hd + se * tl) / (RGAS * 1.e-3 * tl))); }
@@ -273,6 +277,7 @@ PhaseOut photosynthesis(int pidx, int ivt, double t_veg, double t10, double tgcm
     const ctsmg_canopy_params& P = g_par.c;
     const ctsmg_pftcon& F = g_par.pft;
     const int method = g_par.method;
+    const double medlyn_int = g_mint_p ? g_mint_p[pidx - 1] : F.medlynintercept[ivt];
     const double lmrc = fth25(P.lmrhd, P.lmrse);
     const bool c3 = (std::lround(F.c3psn[ivt]) == 1);
     const double qe = c3 ? 0.0 : 0.05;
@@ -342,7 +347,7 @@ PhaseOut photosynthesis(int pidx, int ivt, double t_veg, double t10, double tgcm
         st.an = st.ag - lmr_z;
         psn_z = 0.0;
         if (method == 0) rs_z = std::min(rsmax0, 1.0 / bbb * cf);
-        else rs_z = std::min(rsmax0, 1.0 / F.medlynintercept[ivt] * cf);
+        else rs_z = std::min(rsmax0, 1.0 / medlyn_int * cf);
         ci_z = 0.0;
         *rh_leaf = 0.0;
         out.gs_mol_phase = cf / rs_z;
@@ -361,11 +366,11 @@ PhaseOut photosynthesis(int pidx, int ivt, double t_veg, double t10, double tgcm
         const double je = std::min(r1, r2);
         ci_z = c3 ? 0.7 * cair : 0.4 * cair;
         PsnCtx ctx{c3, vcmax_z, cp, kc, ko, qe, tpu_z, kp_z, F.theta_cj[ivt], P.theta_ip, forc_pbot,
-                   F.medlynslope[ivt], F.medlynintercept[ivt], bbb, mbb, method, gb_mol, je, cair, oair,
-                   lmr_z, par_z, rh_can, pidx};
+                   g_mslope_p ? g_mslope_p[pidx - 1] : F.medlynslope[ivt], medlyn_int, bbb, mbb, method, gb_mol, je,
+                   cair, oair, lmr_z, par_z, rh_can, pidx};
         double ciold = ci_z;
         hybrid(ciold, ctx, st);
-        if (st.an < 0.0) st.gs_mol = (method == 0) ? bbb : F.medlynintercept[ivt];
+        if (st.an < 0.0) st.gs_mol = (method == 0) ? bbb : medlyn_int;
         out.gs_mol_phase = st.gs_mol;
         double cs = cair - 1.4 / gb_mol * st.an * forc_pbot;
         cs = std::max(cs, 1.e-06);
@@ -809,6 +814,11 @@ extern "C" void oracle_set_canopy_params(const ctsmg_canopy_params* p, const cts
     g_par.pft = *pft;
     g_par.method = method;
     g_par.itmax = itmax;
+}
+
+extern "C" void oracle_set_patch_medlyn(const double* slope, const double* intercept) {
+    g_mslope_p = slope;
+    g_mint_p = intercept;
 }
 
 extern "C" int oracle_quadratic(double a, double b, double c, double* r1, double* r2) {

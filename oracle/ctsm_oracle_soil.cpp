@@ -1001,3 +1001,25 @@ extern "C" int oracle_last_error(int* idx, int* lev) {
     if (lev) *lev = g_err_lev;
     return g_err;
 }
+
+// Compute_EffecRootFrac_And_VertTranSink_Default
+// (src/biogeophys/SoilWaterPlantSinkMod.F90:332-420) for dense arrays
+// (columns 1..ncol, patches col_patchi..col_patchi+npatches-1, 1-based).
+extern "C" void oracle_rootsink(int ncol, int ldp, const int32_t* col_patchi, const int32_t* col_npatches,
+                                const double* wtcol, const double* qflx_tran_veg, const double* rootr,
+                                double* qflx_rootsoi) {
+    for (int c = 0; c < ncol; ++c) {
+        const int p0 = col_patchi[c] - 1, np = col_npatches[c];
+        double rc[NLEVSOI + 1];
+        for (int j = 1; j <= NLEVSOI; ++j) rc[j] = 0.0;
+        for (int j = 1; j <= NLEVSOI; ++j)
+            for (int p = p0; p < p0 + np; ++p) rc[j] = rc[j] + rootr[p + (size_t)(j - 1) * ldp] * qflx_tran_veg[p] * wtcol[p];
+        double temp = 0.0;
+        for (int p = p0; p < p0 + np; ++p) temp = temp + qflx_tran_veg[p] * wtcol[p];
+        const double tran_col = temp;
+        for (int j = 1; j <= NLEVSOI; ++j) {
+            if (temp != 0.0) rc[j] = rc[j] / temp;
+            qflx_rootsoi[c + (size_t)(j - 1) * ncol] = rc[j] * tran_col;
+        }
+    }
+}

@@ -35,6 +35,10 @@ def lib():
         _LIB.oracle_quadratic.argtypes = [C.c_double] * 3 + [P(C.c_double)] * 2
         _LIB.oracle_qsat.argtypes = [C.c_double, C.c_double] + [P(C.c_double)] * 3
         _LIB.oracle_qsat.restype = None
+        _LIB.oracle_set_patch_medlyn.argtypes = [P(C.c_double), P(C.c_double)]
+        _LIB.oracle_set_patch_medlyn.restype = None
+        _LIB.oracle_rootsink.argtypes = [I, I, P(C.c_int32), P(C.c_int32)] + [P(C.c_double)] * 4
+        _LIB.oracle_rootsink.restype = None
         _LIB.oracle_canopyfluxes.argtypes = [P(abi.Bounds), I, P(C.c_int32), P(abi.CanopyIO), C.c_double, P(C.c_int)]
     return _LIB
 

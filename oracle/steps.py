@@ -1,0 +1,53 @@
+"""Multi-step drivers of the oracle (test infrastructure): the sequences the
+batched engine runs, stepped on the CPU."""
+import ctypes as C
+
+import numpy as np
+
+from ctsm_gb300 import abi, inputs, canopy_inputs
+from oracle import oracle as orc
+
+DT = 1800.0
+
+
+def _p(a, t=C.c_double):
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def full_steps(A, npatch, ngrid, rootr, nsteps, medlyn_per_patch=False, method=1, itmax=40, snow_method=0):
+    """nsteps x (CanopyFluxes, root sink, SoilTemperature, SoilWater, h2osoi_vol
+    refresh) in place on A.  displa / z0mv keep their SatellitePhenology values
+    and cgrnds / cgrndl restart from zero every step."""
+    L = orc.lib()
+    ncol = A["zwt"].shape[0]
+    L.oracle_set_canopy_params(C.byref(canopy_inputs.make_params()), C.byref(canopy_inputs.make_pftcon()), method,
+                               itmax)
+    if medlyn_per_patch:
+        L.oracle_set_patch_medlyn(_p(A["medlynslope_p"]), _p(A["medlynintercept_p"]))
+    b = abi.Bounds(1, ncol, 1, npatch)
+    filt_c = np.arange(1, ncol + 1, dtype=np.int32)
+    filt_p = np.arange(1, npatch + 1, dtype=np.int32)
+    displa0, z0mv0 = A["displa"].copy(), A["z0mv"].copy()
+    rootr = np.ascontiguousarray(rootr)
+    try:
+        for _ in range(nsteps):
+            A["displa"][:] = displa0
+            A["z0mv"][:] = z0mv0
+            A["cgrnds"][:] = 0.0
+            A["cgrndl"][:] = 0.0
+            ci = abi.make_io(abi.CanopyIO, abi.CANOPY_FIELDS, A, ncol, npatch, ngrid, 1)
+            e = C.c_int(0)
+            rc = L.oracle_canopyfluxes(C.byref(b), npatch, _p(filt_p, C.c_int32), C.byref(ci), DT, C.byref(e))
+            assert rc == 0, (rc, e.value)
+            L.oracle_rootsink(ncol, npatch, _p(A["col_patchi"], C.c_int32), _p(A["col_npatches"], C.c_int32),
+                              _p(A["wtcol"]), _p(A["qflx_tran_veg"]), _p(rootr), _p(A["qflx_rootsoi"]))
+            st = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, A, ncol, npatch)
+            assert L.oracle_soiltemperature(C.byref(b), ncol, _p(filt_c, C.c_int32), C.byref(st), DT, snow_method) == 0
+            sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS, A, ncol)
+            assert L.oracle_soilwater(C.byref(b), ncol, _p(filt_c, C.c_int32), C.byref(sw), 6.0, DT) == 0
+            inputs.refresh_h2osoi_vol(A)
+    finally:
+        A["displa"][:] = displa0
+        A["z0mv"][:] = z0mv0
+        if medlyn_per_patch:
+            L.oracle_set_patch_medlyn(None, None)

@@ -1,0 +1,80 @@
+"""The full soil + canopy step (driver order) and the perturbed-parameter
+ensemble in the batched engine, against the oracle stepped the same way."""
+import copy
+
+import numpy as np
+import pytest
+
+from ctsm_gb300 import full_inputs as fi
+from oracle.steps import full_steps
+from tests.parity import compare, noise_spread
+
+pytestmark = pytest.mark.gpu
+STATE = ["h2osoi_liq", "h2osoi_ice", "t_soisno", "t_grnd", "h2osoi_vol", "t_veg", "eflx_sh_veg", "qflx_evap_veg",
+         "qflx_tran_veg", "cgrnd", "dlrad", "psnsun", "psnsha", "rssun", "rssha", "liqcan", "snocan", "qcharge",
+         "eflx_sh_grnd", "qflx_evap_soi", "xmf", "num_iter"]
+CANCEL = ("liqcan", "snocan", "eflx_sh_grnd", "qflx_evap_soi", "xmf")
+
+
+def _run(A, npatch, ngrid, rootr, nsteps, per_patch=False):
+    from ctsm_gb300.engine import SoilBatch
+    G = copy.deepcopy(A)
+    b = SoilBatch(G, npatch, canopy=True, ngrid=ngrid, rootr=rootr, per_patch_medlyn=per_patch)
+    b.run(nsteps)
+    b.sync()
+    b.download()
+    b.close()
+    return G
+
+
+@pytest.mark.parametrize("nsteps", [1, 3])
+def test_full_step_matches_oracle(gpu_lib, nsteps):
+    A, npatch, ngrid, rootr = fi.full_state(2500, seed=31)
+    R = copy.deepcopy(A)
+    full_steps(R, npatch, ngrid, rootr, nsteps)
+    G = _run(A, npatch, ngrid, rootr, nsteps)
+    spread = noise_spread(lambda B: full_steps(B, npatch, ngrid, rootr, nsteps), A, R, fields=CANCEL, input_ulps=4)
+    for k in ("liqcan", "snocan"):
+        spread[k] = spread[k] + 1e-9 * (np.abs(A["liqcan"]) + np.abs(A["snocan"]))
+    errs, bad = compare(G, R, STATE, 1e-9, spread)
+    assert not bad, {k: errs[k] for k in bad}
+
+
+def test_ensemble_members_match_oracle(gpu_lib):
+    """Several members with perturbed Medlyn slope/intercept and organic-matter
+    scale packed into one batch: each member's result equals the oracle's."""
+    A, npatch, ngrid, rootr, member_col, factors = fi.ensemble(6, seed=4, cols=(200, 700))
+    R = copy.deepcopy(A)
+    full_steps(R, npatch, ngrid, rootr, 2, medlyn_per_patch=True)
+    G = _run(A, npatch, ngrid, rootr, 2, per_patch=True)
+    spread = noise_spread(lambda B: full_steps(B, npatch, ngrid, rootr, 2, medlyn_per_patch=True), A, R,
+                          fields=CANCEL, input_ulps=4)
+    for k in ("liqcan", "snocan"):
+        spread[k] = spread[k] + 1e-9 * (np.abs(A["liqcan"]) + np.abs(A["snocan"]))
+    errs, bad = compare(G, R, STATE, 1e-9, spread)
+    assert not bad, {k: errs[k] for k in bad}
+    assert len(np.unique(factors["medlynslope"])) == 6
+
+
+def test_member_alone_equals_member_in_ensemble(gpu_lib):
+    """A member run by itself gives bit-identical results to the same member
+    packed with others (results do not depend on the batch around them)."""
+    A, npatch, ngrid, rootr, member_col, factors = fi.ensemble(3, seed=9, cols=(150, 400))
+    G = _run(A, npatch, ngrid, rootr, 2, per_patch=True)
+    m = 1
+    cols = np.nonzero(member_col == m)[0]
+    pmask = np.isin(A["patch_column"] - 1, cols)
+    pidx = np.nonzero(pmask)[0]
+    S = {}
+    for k, v in A.items():
+        if v.shape[-1] == A["zwt"].shape[0]:
+            S[k] = np.ascontiguousarray(v[..., cols])
+        elif v.shape[-1] == npatch:
+            S[k] = np.ascontiguousarray(v[..., pidx])
+    S["col_patchi"] = (A["col_patchi"][cols] - pidx[0]).astype(np.int32)
+    S["patch_column"] = (A["patch_column"][pidx] - cols[0]).astype(np.int32)
+    S["patch_gridcell"] = S["patch_column"].copy()
+    Gs = _run(S, len(pidx), len(cols), np.ascontiguousarray(rootr[:, pidx]), 2, per_patch=True)
+    for k in ("t_soisno", "h2osoi_liq", "t_veg", "psnsun", "qcharge"):
+        g = G[k][..., cols] if G[k].shape[-1] == A["zwt"].shape[0] else G[k][..., pidx]
+        np.testing.assert_array_equal(Gs[k], g)
