@@ -14,6 +14,7 @@
 #include "ctsm_device.cuh"
 #include "soil_kernels.cuh"
 #include "canopy_kernels.cuh"
+#include "balance_kernels.cuh"
 #include "capi_internal.h"
 
 namespace ctsmg {
@@ -45,6 +46,8 @@ struct Batch {
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    BalanceState bal{};
+    void* bal_mem = nullptr;
 };
 
 static int cuda_err(cudaError_t e, const char* where) {
@@ -63,6 +66,10 @@ static void set_io_ptr(void* io, const FieldDesc& f, void* p) {
 static cudaError_t enqueue_step(Batch* b) {
     cudaError_t e = cudaSuccess;
     const int ncol = b->cfg.ncol;
+    if (b->cfg.balance) {
+        e = launch_prestep(b->dst, ncol, b->bal, b->stream);
+        if (e != cudaSuccess) return e;
+    }
     if (b->cfg.with_canopy) {
         e = launch_canopy(b->cargs, b->cfg.npatch, nullptr, b->cfg.dtime, b->counter, b->err, b->stream);
         if (e != cudaSuccess) return e;
@@ -70,8 +77,10 @@ static cudaError_t enqueue_step(Batch* b) {
                             b->rootr, b->cfg.npatch, (double*)b->dsw.qflx_rootsoi, ncol, b->stream);
         if (e != cudaSuccess) return e;
     }
-    return launch_soilstep(b->dsw, b->dst, ncol, b->cfg.e_ice, b->cfg.dtime, b->cfg.snow_thermal_cond_method, b->ws,
-                           ncol, b->err, b->stream, b->block, b->cfg.order);
+    e = launch_soilstep(b->dsw, b->dst, ncol, b->cfg.e_ice, b->cfg.dtime, b->cfg.snow_thermal_cond_method, b->ws,
+                        ncol, b->err, b->stream, b->block, b->cfg.order);
+    if (e != cudaSuccess || !b->cfg.balance) return e;
+    return launch_balance(b->dsw, b->dst, ncol, b->cfg.dtime, b->bal, b->stream);
 }
 
 static int build_graph(Batch* b) {
@@ -94,7 +103,7 @@ static void batch_free(Batch* b) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
     for (auto& f : b->fields) if (f.dptr) cudaFree(f.dptr);
     for (void* p : {(void*)b->d_perm, (void*)b->ws, (void*)b->err, b->snapshot, (void*)b->rootr, (void*)b->mslope,
-                    (void*)b->mint, (void*)b->counter})
+                    (void*)b->mint, (void*)b->counter, b->bal_mem})
         if (p) cudaFree(p);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
@@ -226,6 +235,21 @@ extern "C" int32_t ctsmg_batch_create2(ctsmg_batch* out, const ctsmg_batch_confi
         b->cargs.medlynintercept_p = b->mint;
         if ((e = cudaMalloc(&b->counter, 256)) != cudaSuccess) return fail(cuda_err(e, "counter"));
     }
+    if (cfg->balance) {
+        const size_t ssb = (size_t)ncol * (NLEVSNO + NLEVGRND) * 8, cb = (size_t)ncol * 8;
+        if ((e = cudaMalloc(&b->bal_mem, ssb + 6 * cb + 256)) != cudaSuccess) return fail(cuda_err(e, "balance"));
+        if ((e = cudaMemset(b->bal_mem, 0, ssb + 6 * cb + 256)) != cudaSuccess) return fail(cuda_err(e, "balance"));
+        char* m = (char*)b->bal_mem;
+        b->bal.tssbef = (double*)m; m += ssb;
+        b->bal.th2osfc_bef = (double*)m; m += cb;
+        b->bal.w_bef = (double*)m; m += cb;
+        b->bal.errh2o = (double*)m; m += cb;
+        b->bal.errsoi = (double*)m; m += cb;
+        b->bal.errh2o_max = (double*)m; m += cb;
+        b->bal.errsoi_max = (double*)m; m += cb;
+        b->bal.step = (int*)m;
+        b->bal.skip_steps = cfg->skip_steps;
+    }
     for (auto& f : b->fields) b->state_bytes += f.bytes;
     if ((e = cudaMalloc(&b->ws, (size_t)SOILTEMP_WS_DOUBLES_PER_COL * ncol * 8)) != cudaSuccess) return fail(cuda_err(e, "ws"));
     if ((e = cudaMalloc(&b->err, sizeof(DevError))) != cudaSuccess) return fail(cuda_err(e, "err"));
@@ -244,6 +268,7 @@ extern "C" int32_t ctsmg_batch_create(ctsmg_batch* out, const ctsmg_soilwater_io
     cfg.snow_thermal_cond_method = snow_thermal_cond_method;
     cfg.stomatalcond_method = 1; cfg.itmax_canopy_fluxes = 40;
     cfg.order = 0; cfg.with_canopy = 0; cfg.bucket = 1;
+    cfg.balance = 0; cfg.skip_steps = 0;
     return ctsmg_batch_create2(out, &cfg, sw, st, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
 }
 
@@ -322,6 +347,28 @@ extern "C" int32_t ctsmg_batch_download(ctsmg_batch bh, const ctsmg_soilwater_io
     return ctsmg_batch_download2(bh, sw, st, nullptr);
 }
 
+extern "C" int32_t ctsmg_batch_balance(ctsmg_batch bh, double* errh2o_max, double* errsoi_max, double* errh2o_last,
+                                       double* errsoi_last) {
+    if (!bh) return set_error(CTSMG_E_ARG, "null batch", 0, 0);
+    Batch* b = bh->b;
+    if (!b->cfg.balance) return set_error(CTSMG_E_ARG, "batch was created without balance = 1", 0, 0);
+    CK(cudaStreamSynchronize(b->stream), "sync");
+    const int ncol = b->cfg.ncol;
+    double* outs[4] = {errh2o_max, errsoi_max, errh2o_last, errsoi_last};
+    double* srcs[4] = {b->bal.errh2o_max, b->bal.errsoi_max, b->bal.errh2o, b->bal.errsoi};
+    for (int k = 0; k < 4; ++k) {
+        if (!outs[k]) continue;
+        double* tmp = nullptr;
+        CK(cudaMalloc(&tmp, (size_t)ncol * 8), "tmp");
+        cudaError_t e = launch_permute(tmp, srcs[k], b->d_perm, ncol, 1, 8, 1, b->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+        if (e == cudaSuccess) e = cudaMemcpy(outs[k], tmp, (size_t)ncol * 8, cudaMemcpyDeviceToHost);
+        cudaFree(tmp);
+        if (e != cudaSuccess) return cuda_err(e, "balance download");
+    }
+    return 0;
+}
+
 // Times `trial_steps` graph replays per candidate threads-per-block on the
 // batch's own data and keeps the fastest; the state is restored afterwards.
 extern "C" int32_t ctsmg_batch_autotune(ctsmg_batch bh, int32_t trial_steps, int32_t* block_out) {
@@ -356,6 +403,11 @@ extern "C" int32_t ctsmg_batch_autotune(ctsmg_batch bh, int32_t trial_steps, int
         off += f.bytes;
     }
     CK(cudaMemsetAsync(b->err, 0xff, sizeof(DevError), b->stream), "err reset");
+    if (b->cfg.balance) {
+        const int ncol = b->cfg.ncol;
+        const size_t ssb = (size_t)ncol * (NLEVSNO + NLEVGRND) * 8, cb = (size_t)ncol * 8;
+        CK(cudaMemsetAsync(b->bal_mem, 0, ssb + 6 * cb + 256, b->stream), "balance reset");
+    }
     CK(cudaStreamSynchronize(b->stream), "sync");
     cudaFree(b->snapshot);
     b->snapshot = nullptr;

@@ -25,6 +25,7 @@ def _bind(L):
                                       P(abi.CanopyIO), P(C.c_double), P(C.c_double), P(C.c_double),
                                       P(abi.CanopyParams), P(abi.Pftcon)]
     L.ctsmg_batch_download2.argtypes = [C.c_void_p, P(abi.SoilWaterIO), P(abi.SoilTempIO), P(abi.CanopyIO)]
+    L.ctsmg_batch_balance.argtypes = [C.c_void_p] + [P(C.c_double)] * 4
     L._batch_bound = True
 
 
@@ -32,7 +33,7 @@ class BatchConfig(C.Structure):
     _fields_ = [("ncol", C.c_int32), ("npatch", C.c_int32), ("ngrid", C.c_int32), ("dtime", C.c_double),
                 ("e_ice", C.c_double), ("snow_thermal_cond_method", C.c_int32), ("stomatalcond_method", C.c_int32),
                 ("itmax_canopy_fluxes", C.c_int32), ("order", C.c_int32), ("with_canopy", C.c_int32),
-                ("bucket", C.c_int32)]
+                ("bucket", C.c_int32), ("balance", C.c_int32), ("skip_steps", C.c_int32)]
 
 
 class SoilBatch:
@@ -42,7 +43,7 @@ class SoilBatch:
 
     def __init__(self, state, npatch, dtime=1800.0, e_ice=6.0, snow_thermal_cond_method=0, canopy=False,
                  ngrid=None, rootr=None, order=None, bucket=True, stomatalcond_method=1, itmax=40,
-                 params=None, pftcon=None, per_patch_medlyn=False):
+                 params=None, pftcon=None, per_patch_medlyn=False, balance=False, skip_steps=None):
         from . import canopy_inputs
         self.L = load()
         _bind(self.L)
@@ -53,9 +54,12 @@ class SoilBatch:
         self.ngrid = ngrid if ngrid is not None else self.ncol
         self._sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS, state, self.ncol)
         self._st = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, state, self.ncol, npatch)
+        from .balance import skip_steps as _skip
+        self.balance_on = balance
         cfg = BatchConfig(self.ncol, npatch, self.ngrid, dtime, e_ice, snow_thermal_cond_method, stomatalcond_method,
                           itmax, (1 if canopy else 0) if order is None else order, 1 if canopy else 0,
-                          1 if bucket else 0)
+                          1 if bucket else 0, 1 if balance else 0,
+                          _skip(dtime) if skip_steps is None else skip_steps)
         self.h = C.c_void_p()
         if canopy:
             self._ci = abi.make_io(abi.CanopyIO, abi.CANOPY_FIELDS, state, self.ncol, npatch, self.ngrid, 1)
@@ -93,6 +97,13 @@ class SoilBatch:
         else:
             check(self.L.ctsmg_batch_download(self.h, C.byref(sw), C.byref(tt)))
         return st
+
+    def balance(self):
+        """(errh2o_max, errsoi_max, errh2o_last, errsoi_last) per column."""
+        out = [np.zeros(self.ncol) for _ in range(4)]
+        dp = C.POINTER(C.c_double)
+        check(self.L.ctsmg_batch_balance(self.h, *[o.ctypes.data_as(dp) for o in out]))
+        return tuple(out)
 
     def autotune(self, trial_steps=2):
         b = C.c_int32()

@@ -7,7 +7,8 @@ from canopy_inputs.canopy_patches, and every component the two share
 (snl, t_soisno, t_grnd, t_h2osfc, frac_sno_eff, frac_h2osfc, snow_depth, emg,
 htvp, forc_lwrad, frac_veg_nosno, the patch/column maps) is taken from the
 soil state.  The air temperature of a column is its ground temperature plus
-U(-5,5) K.  Root fractions of every patch follow the fixed profile
+U(-5,5) K; the ground humidities follow SurfaceHumidityMod.F90:185-216 (qg_snow =
+qg_soil on snow-free columns, qg their fraction-weighted mix).  Root fractions of every patch follow the fixed profile
 dz_j exp(-3 z_j) (normalised) that the plain workloads use for the sink.
 
 Ensemble members perturb 8 parameters by a factor drawn log-uniformly in
@@ -52,9 +53,21 @@ def full_state(ncol, seed=0, npatch_max=4, om_frac_sf=1.0, rng=None):
     col = dict(forc_pbot=pbot, forc_q=forc_q, forc_th=forc_th,
                forc_rho=(pbot - 0.378 * e) / (canopy_inputs.RAIR * forc_t),
                thv=forc_th * (1.0 + 0.61 * forc_q))
-    qg, _, dqg = canopy_inputs.qsat(tg, pbot)
-    wet = r.uniform(0.5, 1.0, ncol)
-    col.update(qg=qg * wet, qg_snow=qg, qg_soil=qg * wet, qg_h2osfc=qg, dqgdT=dqg * wet,
+    # ground humidities by the rules of SurfaceHumidityMod.F90:185-216
+    LS = -abi.NLEVSNO + 1
+    snl = A["snl"]
+    t1 = A["t_soisno"][1 - LS]
+    ttop = A["t_soisno"][snl + 1 - LS, np.arange(ncol)]
+    fsno, fh2o = A["frac_sno_eff"], A["frac_h2osfc"]
+    q_soil, _, dq_soil = canopy_inputs.qsat(t1, pbot)
+    q_snow, _, dq_snow = canopy_inputs.qsat(ttop, pbot)
+    hr = r.uniform(0.5, 1.0, ncol)
+    qg_soil = hr * q_soil
+    qg_snow = np.where(snl < 0, q_snow, qg_soil)
+    dqgdT = np.where(snl < 0, fsno * dq_snow + (1.0 - fsno - fh2o) * hr * dq_soil, (1.0 - fh2o) * hr * dq_soil)
+    qg_h2osfc = qg_soil
+    qg = fsno * qg_snow + (1.0 - fsno - fh2o) * qg_soil + fh2o * qg_h2osfc
+    col.update(qg=qg, qg_snow=qg_snow, qg_soil=qg_soil, qg_h2osfc=qg_h2osfc, dqgdT=dqgdT,
                z0mg=np.full(ncol, 0.01), soilresis=r.uniform(50.0, 5000.0, ncol))
     grid = dict(forc_u=r.uniform(0.5, 20.0, ngrid), forc_v=np.zeros(ngrid), forc_hgt_u=np.full(ngrid, 30.0),
                 forc_hgt_t=np.full(ngrid, 30.0), forc_hgt_q=np.full(ngrid, 30.0), forc_pco2=400.e-6 * pbot,
@@ -70,6 +83,7 @@ def full_state(ncol, seed=0, npatch_max=4, om_frac_sf=1.0, rng=None):
         if n not in A:
             A[n] = Cn[n]
     A["frac_veg_nosno"][:] = 1
+    A["eflx_bot"][:] = 0.0            # no heat flux from beneath the column, as for CTSM's soil columns
     # absorbed ground solar consistent with the soil's sabg_lyr (sum over layers)
     dzs, zs, _ = inputs.layer_structure_20sl()
     prof = np.array([dzs[j] * np.exp(-3.0 * zs[j]) for j in range(abi.NLEVSOI)])

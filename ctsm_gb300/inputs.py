@@ -27,7 +27,9 @@ the builder are stated here and nowhere else:
   over the 20 soil layers by the fixed profile dz_j exp(-3 z_j) (normalised);
   zwt U(0.5,8) m; the ground heat flux G ~ U(-50,150) W/m2 enters as one patch
   per column with wtcol = 1, emg = 0, sabg = sabg_soil = sabg_snow = G, all of it
-  absorbed in the top layer, the turbulent fluxes at zero and cgrnd = 5 W/m2/K;
+  absorbed in the top layer, the turbulent fluxes at zero and cgrnd = 5 W/m2/K
+  (forcing="full": sabg = sabg_soil = sabg_snow drawn per patch and split over
+  the exposed layers, every other patch flux drawn independently);
   eflx_bot = 0, h2osfc = frac_h2osfc = 0.
 """
 import numpy as np
@@ -243,8 +245,9 @@ def soil_columns(ncol, seed=0, snow=False, nbedrock=(20, 20), zwt=(0.5, 8.0),
         A["frac_veg_nosno"][:] = r.integers(0, 2, size=npatch)
         A["emg"][:] = r.uniform(0.9, 0.99, size=ncol)
         A["forc_lwrad"][:] = r.uniform(150.0, 450.0, size=ncol)
-        for k in ("sabg", "sabg_soil", "sabg_snow"):
-            A[k][:] = r.uniform(0.0, 400.0, size=npatch)
+        A["sabg"][:] = r.uniform(0.0, 400.0, size=npatch)
+        A["sabg_soil"][:] = A["sabg"]
+        A["sabg_snow"][:] = A["sabg"]
         frac = r.uniform(0.0, 1.0, size=(NLEVSNO + 1, npatch))
         ptop = top[pcol]
         for j in range(LS, 2):

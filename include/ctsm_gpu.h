@@ -367,6 +367,12 @@ typedef struct {
     double dtime, e_ice;
     int32_t snow_thermal_cond_method, stomatalcond_method, itmax_canopy_fluxes;
     int32_t order, with_canopy, bucket;
+    /* balance = 1 evaluates every step's column water error (mm) and soil
+     * energy error errsoi (W/m2) as BalanceCheck does
+     * (src/biogeophys/BalanceCheckMod.F90:592-658, 1103-1113; errsoi from
+     * src/biogeophys/SoilFluxesMod.F90:399-445) and keeps their maxima over
+     * the steps after the first skip_steps (BalanceCheckMod.F90:91).       */
+    int32_t balance, skip_steps;
 } ctsmg_batch_config;
 
 /* cio/rootr/medlyn*_p may be NULL when with_canopy = 0.  rootr is (p, 1:nlevsoi)
@@ -392,6 +398,11 @@ int32_t ctsmg_batch_download2(ctsmg_batch b, const ctsmg_soilwater_io* sw, const
                               const ctsmg_canopy_io* cio);
 /* Time trial_steps steps for each candidate threads-per-block (64, 128, 256)
  * on the batch's own data, keep the fastest, restore the state. */
+/* Per-column balance results in the caller's column order (any pointer may be
+ * NULL): maxima of |errh2o| and |errsoi| over the checked steps, and the last
+ * step's signed errors. */
+int32_t ctsmg_batch_balance(ctsmg_batch b, double* errh2o_max, double* errsoi_max, double* errh2o_last,
+                            double* errsoi_last);
 int32_t ctsmg_batch_autotune(ctsmg_batch b, int32_t trial_steps, int32_t* block_out);
 int32_t ctsmg_batch_set_block(ctsmg_batch b, int32_t block);
 int64_t ctsmg_batch_state_bytes(ctsmg_batch b);
