@@ -102,14 +102,10 @@ def canopy_patches(npatch, seed=0, npatch_max=4, night_frac=0.1, rng=None):
     """Allocate and fill every canopy manifest field for about `npatch`
     patches (1..npatch_max per column).  Returns (arrays, npatch, ncol, ngrid)."""
     r = rng if rng is not None else np.random.Generator(np.random.Philox(seed))
-    per = []
-    tot = 0
-    while tot < npatch:
-        k = int(r.integers(1, npatch_max + 1))
-        k = min(k, npatch - tot)
-        per.append(k)
-        tot += k
-    per = np.array(per, dtype=np.int32)
+    per = r.integers(1, npatch_max + 1, npatch).astype(np.int32)
+    ncut = int(np.searchsorted(np.cumsum(per), npatch)) + 1      # first prefix reaching npatch
+    per = per[:ncut]
+    per[-1] -= int(per.sum()) - npatch
     ncol = len(per)
     ngrid = ncol
     A = {}

@@ -1,19 +1,25 @@
 // canopy_kernels.cu -- sm_103a FP64 kernel for CanopyFluxes (leaf temperature
 // / Monin-Obukhov stability iteration) with Photosynthesis sun + shade.
 //
-// One thread owns one patch at a time.  The reference removes converged
-// patches from its filter after every pass (CanopyFluxesMod.F90:1448-1456);
-// here a lane whose patch has converged (or reached itmax) finalises it and
-// takes the next patch from a global work counter, then rejoins the warp for
-// the next pass.  The pass body -- FrictionVelocity, the resistances, two
-// Photosynthesis calls and the energy-balance Newton step -- is therefore
-// executed with the warp's lanes on different patches but the same code,
-// which is the GPU form of the reference's filter compaction.  Per-patch
+// Three kernels per call.  canopy_setup_kernel prepares every patch of the
+// filter (CanopyFluxesMod.F90:700-1017) and writes its iteration state to a
+// per-patch record in HBM.  canopy_iterate_kernel is persistent: one thread
+// owns one patch at a time and runs its passes (:1028-1458); the reference
+// removes converged patches from its filter after every pass (:1448-1456),
+// and here a lane whose patch has converged (or reached itmax) stores the
+// record and takes the next patch from a global work counter, then rejoins
+// the warp for the next pass -- the GPU form of the reference's filter
+// compaction.  canopy_finalize_kernel reads the records and computes the
+// post-iteration fluxes (:1461-1655).  Keeping setup and finalize out of the
+// iterating kernel keeps its code (one pass, one Ci root finder, one out-of-
+// line copy of each libm function) small enough for the instruction cache,
+// and its lanes never wait on another lane's setup or finalize.  Per-patch
 // results do not depend on which lane or pass slot served them.
 #include <cuda_runtime.h>
 #include <cstdint>
 #include "ctsm_device.cuh"
 #include "canopy_kernels.cuh"
+#include "rootfind.cuh"
 
 namespace ctsmg {
 namespace canopy {
@@ -74,35 +80,50 @@ __device__ __forceinline__ bool quadratic(double a, double b, double c, double& 
     return true;
 }
 
+// One out-of-line body of each libm function that the pass calls at several
+// sites (FrictionVelocity, the stability functions, Photosynthesis): the
+// iterating kernel holds one copy of each instead of an inline expansion per
+// call site.  The functions are CUDA's own; only where their code sits changes.
+__device__ __noinline__ double xlog(double x) { return log(x); }
+__device__ __noinline__ double xexp(double x) { return exp(x); }
+__device__ __noinline__ double xpow(double x, double y) { return pow(x, y); }
+__device__ __noinline__ double xatan(double x) { return atan(x); }
+
 // FrictionVelocityMod.F90:1120-1155
 __device__ __forceinline__ double stab1(double zeta) {
     const double chik2 = sqrt(1.0 - 16.0 * zeta);
     const double chik = sqrt(chik2);
-    return 2.0 * log((1.0 + chik) * 0.5) + log((1.0 + chik2) * 0.5) - 2.0 * atan(chik) + PI * 0.5;
+    return 2.0 * xlog((1.0 + chik) * 0.5) + xlog((1.0 + chik2) * 0.5) - 2.0 * xatan(chik) + PI * 0.5;
 }
 __device__ __forceinline__ double stab2(double zeta) {
-    return 2.0 * log((1.0 + sqrt(1.0 - 16.0 * zeta)) * 0.5);
+    return 2.0 * xlog((1.0 + sqrt(1.0 - 16.0 * zeta)) * 0.5);
 }
 
 struct PsnState { double ac, aj, ap, ag, an, gs_mol; };
+
+// Inputs of ci_func for one patch and phase.  The ones that do not change
+// while Ci is iterated are evaluated once, with the operations in the order
+// ci_func writes them (kco = kc (1 + oair/ko), c14gb = 1.4/gb_mol, gbrh =
+// gb_mol 1e-6 rh_can and the Medlyn constants).
 struct PsnCtx {
     bool c3;
-    double vcmax_z, cp, kc, ko, qe, tpu_z, kp_z, theta_cj, theta_ip, forc_pbot, medlynslope, medlynintercept;
-    double bbb, mbb;
     int method;
-    double gb_mol, je, cair, oair, lmr_z, par_z, rh_can;
+    double vcmax_z, cp, kco, ap3, aj4, kp_z, theta_cj, theta_ip, forc_pbot;
+    double m_slope, m_i6, m_i2_12, m_2i6, m_s;
+    double bbb, mbb;
+    double gb_mol, c14gb, gbrh, je, cair, lmr_z, rh_can;
 };
 
 // PhotosynthesisMod.F90:2564-2701
 __device__ double ci_func(double ci, const PsnCtx& x, PsnState& s, Err& e, int pidx) {
     double r1, r2;
     if (x.c3) {
-        s.ac = x.vcmax_z * fmax(ci - x.cp, 0.0) / (ci + x.kc * (1.0 + x.oair / x.ko));
+        s.ac = x.vcmax_z * fmax(ci - x.cp, 0.0) / (ci + x.kco);
         s.aj = x.je * fmax(ci - x.cp, 0.0) / (4.0 * ci + 8.0 * x.cp);
-        s.ap = 3.0 * x.tpu_z;
+        s.ap = x.ap3;
     } else {
         s.ac = x.vcmax_z;
-        s.aj = x.qe * x.par_z * 4.6;
+        s.aj = x.aj4;
         s.ap = x.kp_z * fmax(ci, 0.0) / x.forc_pbot;
     }
     if (!quadratic(x.theta_cj, -(s.ac + s.aj), s.ac * s.aj, r1, r2)) flag(e, CTSMG_E_DISCRIMINANT, pidx);
@@ -111,14 +132,13 @@ __device__ double ci_func(double ci, const PsnCtx& x, PsnState& s, Err& e, int p
     s.ag = fmax(0.0, fmin(r1, r2));
     s.an = s.ag - x.lmr_z;
     if (s.an < 0.0) return 0.0;
-    double cs = x.cair - 1.4 / x.gb_mol * s.an * x.forc_pbot;
+    double cs = x.cair - x.c14gb * s.an * x.forc_pbot;
     cs = fmax(cs, 1.e-06);
     if (x.method == 1) {
         const double term = 1.6 * s.an / (cs / x.forc_pbot * 1.e06);
-        const double st = x.medlynslope * term;
-        const double bquad = -(2.0 * (x.medlynintercept * 1.e-06 + term) + st * st / (x.gb_mol * 1.e-06 * x.rh_can));
-        const double cquad = x.medlynintercept * x.medlynintercept * 1.e-12 +
-                             (2.0 * x.medlynintercept * 1.e-06 + term * (1.0 - x.medlynslope * x.medlynslope / x.rh_can)) * term;
+        const double st = x.m_slope * term;
+        const double bquad = -(2.0 * (x.m_i6 + term) + st * st / x.gbrh);
+        const double cquad = x.m_i2_12 + (x.m_2i6 + term * x.m_s) * term;
         if (!quadratic(1.0, bquad, cquad, r1, r2)) flag(e, CTSMG_E_DISCRIMINANT, pidx);
         s.gs_mol = fmax(r1, r2) * 1.e06;
     } else {
@@ -130,144 +150,174 @@ __device__ double ci_func(double ci, const PsnCtx& x, PsnState& s, Err& e, int p
     return ci - x.cair + s.an * x.forc_pbot * (1.4 * s.gs_mol + 1.6 * x.gb_mol) / (x.gb_mol * s.gs_mol);
 }
 
-// PhotosynthesisMod.F90:2371-2485
-__device__ double brent(double x1, double x2, double f1, double f2, double tol, const PsnCtx& ctx, PsnState& st,
-                        Err& err, int pidx) {
-    const double eps = 1.e-2;
-    double a = x1, b = x2, fa = f1, fb = f2;
-    if ((fa > 0.0 && fb > 0.0) || (fa < 0.0 && fb < 0.0)) { flag(err, CTSMG_E_NOT_BRACKETED, pidx); return b; }
-    double c = b, fc = fb, d = 0.0, e = 0.0;
-#pragma unroll 1
-    for (int iter = 0; iter < 20; ++iter) {
-        if ((fb > 0.0 && fc > 0.0) || (fb < 0.0 && fc < 0.0)) { c = a; fc = fa; d = b - a; e = d; }
-        if (fabs(fc) < fabs(fb)) { a = b; b = c; c = a; fa = fb; fb = fc; fc = fa; }
-        const double tol1 = 2.0 * eps * fabs(b) + 0.5 * tol;
-        const double xm = 0.5 * (c - b);
-        if (fabs(xm) <= tol1 || fb == 0.) return b;
-        if (fabs(e) >= tol1 && fabs(fa) > fabs(fb)) {
-            const double s = fb / fa;
-            double p, q;
-            if (a == c) {
-                p = 2.0 * xm * s;
-                q = 1.0 - s;
-            } else {
-                q = fa / fc;
-                const double r = fb / fc;
-                p = s * (2.0 * xm * q * (q - r) - (b - a) * (r - 1.0));
-                q = (q - 1.0) * (r - 1.0) * (s - 1.0);
-            }
-            if (p > 0.0) q = -q;
-            p = fabs(p);
-            if (2.0 * p < fmin(3.0 * xm * q - fabs(tol1 * q), fabs(e * q))) { e = d; d = p / q; }
-            else { d = xm; e = d; }
-        } else {
-            d = xm;
-            e = d;
-        }
-        a = b;
-        fa = fb;
-        if (fabs(d) > tol1) b = b + d;
-        else b = b + copysign(fabs(tol1), xm);
-        fb = ci_func(b, ctx, st, err, pidx);
-        if (fb == 0.0) break;
-    }
-    return b;
-}
-
-// PhotosynthesisMod.F90:2251-2368
-__device__ void hybrid(double x0, const PsnCtx& ctx, PsnState& st, Err& err, int pidx) {
-    const double eps = 1.e-2, eps1 = 1.e-4;
-    double f0 = ci_func(x0, ctx, st, err, pidx);
-    if (f0 == 0.0) return;
-    double minx = x0, minf = f0;
-    double x1 = x0 * 0.99;
-    double f1 = ci_func(x1, ctx, st, err, pidx);
-    if (f1 == 0.0) return;
-    if (f1 < minf) { minx = x1; minf = f1; }
-#pragma unroll 1
-    for (int iter = 1;; ++iter) {
-        const double dx = -f1 * (x1 - x0) / (f1 - f0);
-        const double x = x1 + dx;
-        const double tol = fabs(x) * eps;
-        if (fabs(dx) < tol) return;
-        x0 = x1;
-        f0 = f1;
-        x1 = x;
-        f1 = ci_func(x1, ctx, st, err, pidx);
-        if (f1 < minf) { minx = x1; minf = f1; }
-        if (fabs(f1) <= eps1) return;
-        if (f1 * f0 < 0.0) { brent(x0, x1, f0, f1, tol, ctx, st, err, pidx); return; }
-        if (iter > 40) { ci_func(minx, ctx, st, err, pidx); return; }
-    }
-}
-
 __device__ __forceinline__ double ft(double tl, double ha) {
-    return exp(ha / (RGAS * 1.e-3 * (TFRZ + 25.0)) * (1.0 - (TFRZ + 25.0) / tl));
+    return xexp(ha / (RGAS * 1.e-3 * (TFRZ + 25.0)) * (1.0 - (TFRZ + 25.0) / tl));
 }
 __device__ __forceinline__ double fth(double tl, double hd, double se, double sf) {
-    return sf / (1.0 + exp((-hd + se * tl) / (RGAS * 1.e-3 * tl)));
+    return sf / (1.0 + xexp((-hd + se * tl) / (RGAS * 1.e-3 * tl)));
 }
 __device__ __forceinline__ double fth25(double hd, double se) {
-    return 1.0 + exp((-hd + se * (TFRZ + 25.0)) / (RGAS * 1.e-3 * (TFRZ + 25.0)));
+    return 1.0 + xexp((-hd + se * (TFRZ + 25.0)) / (RGAS * 1.e-3 * (TFRZ + 25.0)));
 }
 
 struct PhaseOut { double rs, psn, lmr, ci, gs_mol_phase; };
 
-// PhotosynthesisMod.F90:1243-2062, one phase, nlevcan = nrad = 1
-__device__ PhaseOut photosynthesis(const CanopyArgs& A, int p, int pidx, int ivt, double t_veg, double t10, double tgcm,
-                                   double forc_pbot, double esat_tv, double eair, double oair, double cair, double rb,
-                                   double btran, double dayl_factor, double par_z, double lai_z, double vcmaxcint,
-                                   PsnState& st, double& vpd_can, double& rh_leaf, Err& err) {
+// Photosynthesis quantities of a patch that stay fixed while CanopyFluxes
+// iterates (PhotosynthesisMod.F90:1555-1830 with nlevcan = 1): canopy-top
+// vcmax25 / jmax25, the acclimation entropies from the 10-day temperature,
+// the high-temperature normalisers fth25, the conductance factor cf and the
+// stomatal parameters.
+struct PsnPatch {
+    double vcmax25top, jmax25top, vcmaxse, jmaxse, tpuse, f25_lmr, f25_vc, f25_j, f25_tpu, cf, mslope, mint, mbb;
+};
+
+// Temperature factors of a pass: they depend on t_veg only, so the sunlit and
+// shaded phases share them.  C3: ft and fth of lmr, vcmax, jmax, tpu; C4: the
+// Q10 factor and the 1 + exp(...) divisors (PhotosynthesisMod.F90:1555-1562,
+// 1722-1817).
+struct PsnTemp { double kc, ko, cp, lmr1, lmr2, vc1, vc2, j1, j2, tpu1, tpu2, q10; };
+
+// everything one patch carries from setup to the passes and on to finalize
+struct Patch {
+    int p, c, g, ivt, itlef, nmozsgn, num_iter, c3, err_code, err_idx;
+    double displa, z0mv, hgt_u, hgt_t, hgt_q, zldis, ur, um, obu, obuold, fm;
+    double t_veg, tl_ini, qsatl, el, qsatldT, taf, qaf, dth, dqh, delq;
+    double del, efeb, air, bir, cir, dayl_factor, liqcan, snocan;
+    // last-pass values used after the iteration
+    double tlbef, dt_veg, err, eflx_sh_veg, qflx_evap_veg, qflx_tran_veg, lw_leaf, zeta;
+    double ustar, temp1, temp2, temp12m, temp22m, ram1, rah_a, raw_a, rah_b, uaf, rb;
+    double wtl0, wta0, wtg, wtal, wtgq, wtlq0, wtaq0, wtalq, efe;
+    double u10_clm, u10, vds, vpd_can, rh_leaf, rhaf_last, vpd_last;
+    // quantities of the pass that do not change between passes: logarithms of
+    // the fixed heights over z0m in FrictionVelocity, (zetam)^0.333 and
+    // (zetat)^-0.333, exp(-(elai+esai)), sqrt(dleaf), 1 - exp(-elai_dl) and
+    // the ground's emitted longwave factor lw_grnd
+    double lg_u, lg_u10, lg_t, lg_q, lg_2m, lg_u10m, pz_m, pz_t, w_sai, sqrt_dleaf, one_m_edl, lw_grnd;
+    PsnPatch q;
+    PhaseOut sun, sha;
+    PsnState st;
+};
+
+// The record of a patch in HBM: one plane per component, indexed by the
+// patch's filter position (level-major like the model arrays).
+#define PATCH_INTS(X) X(p) X(c) X(g) X(ivt) X(itlef) X(nmozsgn) X(num_iter) X(c3) X(err_code) X(err_idx)
+#define PATCH_DOUBLES(X)                                                                                              \
+    X(displa) X(z0mv) X(hgt_u) X(hgt_t) X(hgt_q) X(zldis) X(ur) X(um) X(obu) X(obuold) X(fm)                          \
+    X(t_veg) X(tl_ini) X(qsatl) X(el) X(qsatldT) X(taf) X(qaf) X(dth) X(dqh) X(delq)                                  \
+    X(del) X(efeb) X(air) X(bir) X(cir) X(dayl_factor) X(liqcan) X(snocan)                                            \
+    X(tlbef) X(dt_veg) X(err) X(eflx_sh_veg) X(qflx_evap_veg) X(qflx_tran_veg) X(lw_leaf) X(zeta)                     \
+    X(ustar) X(temp1) X(temp2) X(temp12m) X(temp22m) X(ram1) X(rah_a) X(raw_a) X(rah_b) X(uaf) X(rb)                  \
+    X(wtl0) X(wta0) X(wtg) X(wtal) X(wtgq) X(wtlq0) X(wtaq0) X(wtalq) X(efe)                                          \
+    X(u10_clm) X(u10) X(vds) X(vpd_can) X(rh_leaf) X(rhaf_last) X(vpd_last)                                           \
+    X(lg_u) X(lg_u10) X(lg_t) X(lg_q) X(lg_2m) X(lg_u10m) X(pz_m) X(pz_t) X(w_sai) X(sqrt_dleaf) X(one_m_edl)         \
+    X(lw_grnd)                                                                                                        \
+    X(q.vcmax25top) X(q.jmax25top) X(q.vcmaxse) X(q.jmaxse) X(q.tpuse) X(q.f25_lmr) X(q.f25_vc) X(q.f25_j)            \
+    X(q.f25_tpu) X(q.cf) X(q.mslope) X(q.mint) X(q.mbb)                                                               \
+    X(sun.rs) X(sun.psn) X(sun.lmr) X(sun.ci) X(sun.gs_mol_phase)                                                     \
+    X(sha.rs) X(sha.psn) X(sha.lmr) X(sha.ci) X(sha.gs_mol_phase)                                                     \
+    X(st.ac) X(st.aj) X(st.ap) X(st.ag) X(st.an) X(st.gs_mol)
+#define PATCH_COUNT(m) +1
+constexpr int NPI = 0 PATCH_INTS(PATCH_COUNT);
+constexpr int NPD = 0 PATCH_DOUBLES(PATCH_COUNT);
+static_assert(sizeof(Patch) == NPI * 4 + NPD * 8, "every Patch component must be listed in PATCH_INTS / PATCH_DOUBLES");
+
+__device__ __forceinline__ void store_patch(double* ws, int ld, int f, const Patch& s) {
+    int* wi = reinterpret_cast<int*>(ws + (size_t)NPD * ld);
+    int k = 0;
+#define ST_D(m) ws[(size_t)(k++) * ld + f] = s.m;
+    PATCH_DOUBLES(ST_D)
+#undef ST_D
+    k = 0;
+#define ST_I(m) wi[(size_t)(k++) * ld + f] = s.m;
+    PATCH_INTS(ST_I)
+#undef ST_I
+}
+
+__device__ __forceinline__ void load_patch(const double* __restrict__ ws, int ld, int f, Patch& s) {
+    const int* wi = reinterpret_cast<const int*>(ws + (size_t)NPD * ld);
+    int k = 0;
+#define LD_D(m) s.m = ws[(size_t)(k++) * ld + f];
+    PATCH_DOUBLES(LD_D)
+#undef LD_D
+    k = 0;
+#define LD_I(m) s.m = wi[(size_t)(k++) * ld + f];
+    PATCH_INTS(LD_I)
+#undef LD_I
+}
+
+// PhotosynthesisMod.F90:1555-1830: the factors of the pass's t_veg.  The
+// day-time ones (kc, ko, cp, vcmax, jmax, tpu) only when a phase has light.
+__device__ void psn_temp(const CanopyArgs& A, const Patch& s, double forc_pbot, double oair, bool day, PsnTemp& T) {
     const ctsmg_canopy_params& P = A.par;
-    const ctsmg_pftcon& F = A.pft;
+    const double t_veg = s.t_veg;
+    if (s.c3) {
+        T.lmr1 = ft(t_veg, P.lmrha);
+        T.lmr2 = fth(t_veg, P.lmrhd, P.lmrse, s.q.f25_lmr);
+    } else {
+        T.q10 = xpow(2.0, (t_veg - (TFRZ + 25.0)) / 10.0);
+        T.lmr2 = 1.0 + xexp(1.3 * (t_veg - (TFRZ + 55.0)));
+    }
+    if (!day) return;
+    T.kc = P.kc25_coef * forc_pbot * ft(t_veg, P.kcha);
+    T.ko = P.ko25_coef * forc_pbot * ft(t_veg, P.koha);
+    const double sco = 0.5 * 0.209 / P.cp25_yr2000;
+    T.cp = 0.5 * oair / sco * ft(t_veg, P.cpha);
+    if (s.c3) {
+        T.vc1 = ft(t_veg, P.vcmaxha);
+        T.vc2 = fth(t_veg, P.vcmaxhd, s.q.vcmaxse, s.q.f25_vc);
+    } else {
+        T.vc1 = 1.0 + xexp(0.2 * ((TFRZ + 15.0) - t_veg));
+        T.vc2 = 1.0 + xexp(0.3 * (t_veg - (TFRZ + 40.0)));
+    }
+    T.j1 = ft(t_veg, P.jmaxha);
+    T.j2 = fth(t_veg, P.jmaxhd, s.q.jmaxse, s.q.f25_j);
+    T.tpu1 = ft(t_veg, P.tpuha);
+    T.tpu2 = fth(t_veg, P.tpuhd, s.q.tpuse, s.q.f25_tpu);
+}
+
+// PhotosynthesisMod.F90:1243-2062, one phase, nlevcan = nrad = 1
+__device__ PhaseOut photosynthesis(const CanopyArgs& A, const Patch& s, const PsnTemp& T, int pidx, double forc_pbot,
+                                   double esat_tv, double eair, double oair, double cair, double rb, double btran,
+                                   double par_z, double lai_z, double vcmaxcint, PsnState& st, double& vpd_can,
+                                   double& rh_leaf, Err& err) {
+    const ctsmg_canopy_params& P = A.par;
     const int method = A.method;
-    const double medlyn_int = A.medlynintercept_p ? A.medlynintercept_p[p] : F.medlynintercept[ivt];
-    const bool c3 = (llround(F.c3psn[ivt]) == 1);
+    const PsnPatch& q = s.q;
+    const double medlyn_int = q.mint;
+    const bool c3 = s.c3 != 0;
     const double qe = c3 ? 0.0 : 0.05;
     double bbb = 0.0, mbb = 0.0;
-    if (method == 0) { bbb = fmax((c3 ? 10000.0 : 40000.0) * btran, 1.0); mbb = F.mbbopt[ivt]; }
-    const double kc = P.kc25_coef * forc_pbot * ft(t_veg, P.kcha);
-    const double ko = P.ko25_coef * forc_pbot * ft(t_veg, P.koha);
-    const double sco = 0.5 * 0.209 / P.cp25_yr2000;
-    const double cp = 0.5 * oair / sco * ft(t_veg, P.cpha);
-    const double lnc = 1.0 / (F.slatop[ivt] * F.leafcn[ivt]);
-    double vcmax25top = lnc * F.flnr[ivt] * P.fnr * P.act25 * dayl_factor;
-    vcmax25top = vcmax25top * F.fnitr[ivt];
-    const double t10c = fmin(fmax((t10 - TFRZ), 11.0), 35.0);
-    const double jmax25top = ((2.59 - 0.035 * t10c) * vcmax25top) * P.jmax25top_sf;
+    if (method == 0) { bbb = fmax((c3 ? 10000.0 : 40000.0) * btran, 1.0); mbb = q.mbb; }
     const double nscaler = vcmaxcint;
-    const double lmr25 = (c3 ? vcmax25top * P.leaf_mr_vcm : vcmax25top * 0.025) * nscaler;
+    const double lmr25 = (c3 ? q.vcmax25top * P.leaf_mr_vcm : q.vcmax25top * 0.025) * nscaler;
     double lmr_z;
     if (c3) {
-        lmr_z = lmr25 * ft(t_veg, P.lmrha) * fth(t_veg, P.lmrhd, P.lmrse, fth25(P.lmrhd, P.lmrse));
+        lmr_z = lmr25 * T.lmr1 * T.lmr2;
     } else {
-        lmr_z = lmr25 * pow(2.0, (t_veg - (TFRZ + 25.0)) / 10.0);
-        lmr_z = lmr_z / (1.0 + exp(1.3 * (t_veg - (TFRZ + 55.0))));
+        lmr_z = lmr25 * T.q10;
+        lmr_z = lmr_z / T.lmr2;
     }
     double vcmax_z = 0.0, jmax_z = 0.0, tpu_z = 0.0, kp_z = 0.0;
     if (par_z > 0.0) {
-        const double vcmax25 = vcmax25top * nscaler, jmax25 = jmax25top * nscaler;
-        const double tpu25 = P.tpu25ratio * vcmax25top * nscaler, kp25 = P.kp25ratio * vcmax25top * nscaler;
-        const double vcmaxse = (668.39 - 1.07 * t10c) * P.vcmaxse_sf;
-        const double jmaxse = (659.70 - 0.75 * t10c) * P.jmaxse_sf;
-        const double tpuse = (668.39 - 1.07 * t10c) * P.tpuse_sf;
+        const double vcmax25 = q.vcmax25top * nscaler, jmax25 = q.jmax25top * nscaler;
+        const double tpu25 = P.tpu25ratio * q.vcmax25top * nscaler, kp25 = P.kp25ratio * q.vcmax25top * nscaler;
         if (c3) {
-            vcmax_z = vcmax25 * ft(t_veg, P.vcmaxha) * fth(t_veg, P.vcmaxhd, vcmaxse, fth25(P.vcmaxhd, vcmaxse));
+            vcmax_z = vcmax25 * T.vc1 * T.vc2;
         } else {
-            vcmax_z = vcmax25 * pow(2.0, (t_veg - (TFRZ + 25.0)) / 10.0);
-            vcmax_z = vcmax_z / (1.0 + exp(0.2 * ((TFRZ + 15.0) - t_veg)));
-            vcmax_z = vcmax_z / (1.0 + exp(0.3 * (t_veg - (TFRZ + 40.0))));
+            vcmax_z = vcmax25 * T.q10;
+            vcmax_z = vcmax_z / T.vc1;
+            vcmax_z = vcmax_z / T.vc2;
+            kp_z = kp25 * T.q10;
         }
-        jmax_z = jmax25 * ft(t_veg, P.jmaxha) * fth(t_veg, P.jmaxhd, jmaxse, fth25(P.jmaxhd, jmaxse));
-        tpu_z = tpu25 * ft(t_veg, P.tpuha) * fth(t_veg, P.tpuhd, tpuse, fth25(P.tpuhd, tpuse));
-        kp_z = kp25 * pow(2.0, (t_veg - (TFRZ + 25.0)) / 10.0);
+        jmax_z = jmax25 * T.j1 * T.j2;
+        tpu_z = tpu25 * T.tpu1 * T.tpu2;
     }
     vcmax_z = vcmax_z * btran;
     lmr_z = lmr_z * btran;
     if (P.light_inhibit && par_z > 0.0) lmr_z = lmr_z * 0.67;
 
     const double rsmax0 = 2.e4;
-    const double cf = forc_pbot / (RGAS * 1.e-3 * tgcm) * 1.e06;
+    const double cf = q.cf;
     const double gb_mol = 1.0 / rb * cf;
     PhaseOut out;
     double rs_z, psn_z, ci_z;
@@ -291,11 +341,16 @@ __device__ PhaseOut photosynthesis(const CanopyArgs& A, int p, int pidx, int ivt
         const double qabs = 0.5 * (1.0 - P.fnps) * par_z * 4.6;
         double r1, r2;
         if (!quadratic(P.theta_psii, -(qabs + jmax_z), qabs * jmax_z, r1, r2)) flag(err, CTSMG_E_DISCRIMINANT, pidx);
-        const double mslope = A.medlynslope_p ? A.medlynslope_p[p] : F.medlynslope[ivt];
-        PsnCtx ctx{c3, vcmax_z, cp, kc, ko, qe, tpu_z, kp_z, F.theta_cj[ivt], P.theta_ip, forc_pbot,
-                   mslope, medlyn_int, bbb, mbb, method, gb_mol, fmin(r1, r2), cair, oair,
-                   lmr_z, par_z, rh_can};
-        hybrid(c3 ? 0.7 * cair : 0.4 * cair, ctx, st, err, pidx);
+        const double ms = q.mslope, mi = medlyn_int;
+        const PsnCtx ctx{c3, method, vcmax_z, T.cp, T.kc * (1.0 + oair / T.ko), 3.0 * tpu_z, qe * par_z * 4.6, kp_z,
+                         A.pft.theta_cj[s.ivt], P.theta_ip, forc_pbot,
+                         ms, mi * 1.e-06, mi * mi * 1.e-12, 2.0 * mi * 1.e-06, 1.0 - ms * ms / rh_can,
+                         bbb, mbb, gb_mol, 1.4 / gb_mol, gb_mol * 1.e-06 * rh_can, fmin(r1, r2), cair, lmr_z, rh_can};
+        RootFind rf;                                   // hybrid + brent, one evaluation site
+        rf.start(c3 ? 0.7 * cair : 0.4 * cair);
+#pragma unroll 1
+        while (rf.next(ci_func(rf.x, ctx, st, err, pidx))) {}
+        if (rf.not_bracketed) flag(err, CTSMG_E_NOT_BRACKETED, pidx);
         if (st.an < 0.0) st.gs_mol = (method == 0) ? bbb : medlyn_int;
         out.gs_mol_phase = st.gs_mol;
         ci_z = cair - st.an * forc_pbot * (1.4 * st.gs_mol + 1.6 * gb_mol) / (gb_mol * st.gs_mol);
@@ -316,21 +371,8 @@ __device__ PhaseOut photosynthesis(const CanopyArgs& A, int p, int pidx, int ivt
     return out;
 }
 
-// everything one patch carries from pass to pass
-struct Patch {
-    int p, c, g, ivt, itlef, nmozsgn, num_iter;
-    double displa, z0mv, hgt_u, hgt_t, hgt_q, zldis, ur, um, obu, obuold, fm;
-    double t_veg, tl_ini, qsatl, el, qsatldT, taf, qaf, dth, dqh, delq;
-    double del, efeb, air, bir, cir, dayl_factor, liqcan, snocan;
-    // last-pass values used after the iteration
-    double tlbef, dt_veg, err, eflx_sh_veg, qflx_evap_veg, qflx_tran_veg, lw_leaf, zeta;
-    double ustar, temp1, temp2, temp12m, temp22m, ram1, rah_a, raw_a, rah_b, uaf, rb;
-    double wtl0, wta0, wtg, wtal, wtgq, wtlq0, wtaq0, wtalq, efe;
-    double u10_clm, u10, vds, vpd_can, rh_leaf, rhaf_last, vpd_last;
-    PhaseOut sun, sha;
-    PsnState st;
-};
-
+// FrictionVelocityMod.F90:754-1117 for one patch (z0h = z0q = z0m), with the
+// logarithms of the fixed heights taken from the patch record.
 __device__ void friction_velocity(const Patch& s, int iter, double& fm, double& ustar, double& temp1, double& temp2,
                                   double& temp12m, double& temp22m, double& u10_clm, double& u10, double& vds) {
     const double zetam = 1.574, zetat = 0.465;
@@ -338,48 +380,48 @@ __device__ void friction_velocity(const Patch& s, int iter, double& fm, double& 
     double zldis = s.hgt_u - s.displa;
     double zeta = zldis / obu;
     if (zeta < -zetam)
-        ustar = VKC * um / (log(-zetam * obu / z0m) - stab1(-zetam) + stab1(z0m / obu) +
-                            1.14 * (pow(-zeta, 0.333) - pow(zetam, 0.333)));
+        ustar = VKC * um / (xlog(-zetam * obu / z0m) - stab1(-zetam) + stab1(z0m / obu) +
+                            1.14 * (xpow(-zeta, 0.333) - s.pz_m));
     else if (zeta < 0.0)
-        ustar = VKC * um / (log(zldis / z0m) - stab1(zeta) + stab1(z0m / obu));
+        ustar = VKC * um / (s.lg_u - stab1(zeta) + stab1(z0m / obu));
     else if (zeta <= 1.0)
-        ustar = VKC * um / (log(zldis / z0m) + 5.0 * zeta - 5.0 * z0m / obu);
+        ustar = VKC * um / (s.lg_u + 5.0 * zeta - 5.0 * z0m / obu);
     else
-        ustar = VKC * um / (log(obu / z0m) + 5.0 - 5.0 * z0m / obu + (5.0 * log(zeta) + zeta - 1.0));
-    vds = (zeta < 0.0) ? 2.e-3 * ustar * (1.0 + pow(300.0 / (-obu), 0.666)) : 2.e-3 * ustar;
+        ustar = VKC * um / (xlog(obu / z0m) + 5.0 - 5.0 * z0m / obu + (5.0 * xlog(zeta) + zeta - 1.0));
+    vds = (zeta < 0.0) ? 2.e-3 * ustar * (1.0 + xpow(300.0 / (-obu), 0.666)) : 2.e-3 * ustar;
     if (zldis - z0m <= 10.0) {
         u10_clm = um;
     } else {
         const double z10 = 10.0 + z0m;
         if (zeta < -zetam)
-            u10_clm = um - (ustar / VKC * (log(-zetam * obu / z10) - stab1(-zetam) + stab1(z10 / obu) +
-                                            1.14 * (pow(-zeta, 0.333) - pow(zetam, 0.333))));
+            u10_clm = um - (ustar / VKC * (xlog(-zetam * obu / z10) - stab1(-zetam) + stab1(z10 / obu) +
+                                            1.14 * (xpow(-zeta, 0.333) - s.pz_m)));
         else if (zeta < 0.0)
-            u10_clm = um - (ustar / VKC * (log(zldis / z10) - stab1(zeta) + stab1(z10 / obu)));
+            u10_clm = um - (ustar / VKC * (s.lg_u10 - stab1(zeta) + stab1(z10 / obu)));
         else if (zeta <= 1.0)
-            u10_clm = um - (ustar / VKC * (log(zldis / z10) + 5.0 * zeta - 5.0 * z10 / obu));
+            u10_clm = um - (ustar / VKC * (s.lg_u10 + 5.0 * zeta - 5.0 * z10 / obu));
         else
-            u10_clm = um - (ustar / VKC * (log(obu / z10) + 5.0 - 5.0 * z10 / obu + (5.0 * log(zeta) + zeta - 1.0)));
+            u10_clm = um - (ustar / VKC * (xlog(obu / z10) + 5.0 - 5.0 * z10 / obu + (5.0 * xlog(zeta) + zeta - 1.0)));
     }
-    auto tprof = [&](double zl, double z0) {
+    auto tprof = [&](double zl, double z0, double lgz) {
         const double zt = zl / obu;
         if (zt < -zetat)
-            return VKC / (log(-zetat * obu / z0) - stab2(-zetat) + stab2(z0 / obu) +
-                          0.8 * (pow(zetat, -0.333) - pow(-zt, -0.333)));
+            return VKC / (xlog(-zetat * obu / z0) - stab2(-zetat) + stab2(z0 / obu) +
+                          0.8 * (s.pz_t - xpow(-zt, -0.333)));
         else if (zt < 0.0)
-            return VKC / (log(zl / z0) - stab2(zt) + stab2(z0 / obu));
+            return VKC / (lgz - stab2(zt) + stab2(z0 / obu));
         else if (zt <= 1.0)
-            return VKC / (log(zl / z0) + 5.0 * zt - 5.0 * z0 / obu);
-        return VKC / (log(obu / z0) + 5.0 - 5.0 * z0 / obu + (5.0 * log(zt) + zt - 1.0));
+            return VKC / (lgz + 5.0 * zt - 5.0 * z0 / obu);
+        return VKC / (xlog(obu / z0) + 5.0 - 5.0 * z0 / obu + (5.0 * xlog(zt) + zt - 1.0));
     };
-    temp1 = tprof(s.hgt_t - s.displa, s.z0mv);
-    temp2 = (s.hgt_q == s.hgt_t) ? temp1 : tprof(s.hgt_q - s.displa, s.z0mv);   // z0qv == z0hv here
-    temp12m = tprof(2.0 + s.z0mv, s.z0mv);
+    temp1 = tprof(s.hgt_t - s.displa, s.z0mv, s.lg_t);
+    temp2 = (s.hgt_q == s.hgt_t) ? temp1 : tprof(s.hgt_q - s.displa, s.z0mv, s.lg_q);   // z0qv == z0hv here
+    temp12m = tprof(2.0 + s.z0mv, s.z0mv, s.lg_2m);
     temp22m = temp12m;
     double fmnew;
     if (fmin(zeta, 1.0) < 0.0) {
-        const double tmp1 = pow(1.0 - 16.0 * fmin(zeta, 1.0), 0.25);
-        fmnew = 2.0 * log((1.0 + tmp1) / 2.0) + log((1.0 + tmp1 * tmp1) / 2.0) - 2.0 * atan(tmp1) + 1.5707963;
+        const double tmp1 = xpow(1.0 - 16.0 * fmin(zeta, 1.0), 0.25);
+        fmnew = 2.0 * xlog((1.0 + tmp1) / 2.0) + xlog((1.0 + tmp1 * tmp1) / 2.0) - 2.0 * xatan(tmp1) + 1.5707963;
     } else {
         fmnew = -5.0 * fmin(zeta, 1.0);
     }
@@ -388,15 +430,14 @@ __device__ void friction_velocity(const Patch& s, int iter, double& fm, double& 
     if (zeta == 0.0) zeta10 = 0.0;
     double fm10;
     if (zeta10 < 0.0) {
-        const double tmp1 = pow(1.0 - 16.0 * zeta10, 0.25);
-        fm10 = 2.0 * log((1.0 + tmp1) / 2.0) + log((1.0 + tmp1 * tmp1) / 2.0) - 2.0 * atan(tmp1) + 1.5707963;
+        const double tmp1 = xpow(1.0 - 16.0 * zeta10, 0.25);
+        fm10 = 2.0 * xlog((1.0 + tmp1) / 2.0) + xlog((1.0 + tmp1 * tmp1) / 2.0) - 2.0 * xatan(tmp1) + 1.5707963;
     } else {
         fm10 = -5.0 * zeta10;
     }
-    u10 = s.ur - ustar / VKC * (log(fmax(1.0, s.hgt_u / 10.0)) - fm + fm10);
+    u10 = s.ur - ustar / VKC * (s.lg_u10m - fm + fm10);
 }
 
-// initialisation before the iteration (CanopyFluxesMod.F90:642-1025)
 __device__ void setup(const CanopyArgs& A, Patch& s, int p, Err& err) {
     const ctsmg_canopy_io& io = A.io;
     s.p = p;
@@ -410,9 +451,9 @@ __device__ void setup(const CanopyArgs& A, Patch& s, int p, Err& err) {
     s.dayl_factor = fmin(1.0, fmax(0.01, (io.dayl[g] * io.dayl[g]) / (io.max_dayl[g] * io.max_dayl[g])));
     io.rb1[p] = 0.0;
     const double lt = fmin(elai + esai, TLSAI_CRIT);
-    const double egvf = (1.0 - exp(-lt)) / (1.0 - exp(-TLSAI_CRIT));
+    const double egvf = (1.0 - xexp(-lt)) / (1.0 - xexp(-TLSAI_CRIT));
     s.displa = egvf * io.displa[p];
-    s.z0mv = exp(egvf * log(io.z0mv[p]) + (1.0 - egvf) * log(io.z0mg[c]));
+    s.z0mv = xexp(egvf * xlog(io.z0mv[p]) + (1.0 - egvf) * xlog(io.z0mg[c]));
     s.hgt_u = io.forc_hgt_u[g] + s.z0mv + s.displa;
     s.hgt_t = io.forc_hgt_t[g] + s.z0mv + s.displa;
     s.hgt_q = io.forc_hgt_q[g] + s.z0mv + s.displa;
@@ -437,13 +478,59 @@ __device__ void setup(const CanopyArgs& A, Patch& s, int p, Err& err) {
     const double rib = GRAV * s.zldis * dthv / (thv * s.um * s.um);
     double zeta;
     if (rib >= 0.0) {
-        zeta = rib * log(s.zldis / s.z0mv) / (1.0 - 5.0 * fmin(rib, 0.19));
+        zeta = rib * xlog(s.zldis / s.z0mv) / (1.0 - 5.0 * fmin(rib, 0.19));
         zeta = fmin(A.par.zetamaxstable, fmax(zeta, 0.01));
     } else {
-        zeta = rib * log(s.zldis / s.z0mv);
+        zeta = rib * xlog(s.zldis / s.z0mv);
         zeta = fmax(-100.0, fmin(zeta, -0.01));
     }
     s.obu = s.zldis / zeta;
+    // fixed during the iteration: FrictionVelocity's logarithms of the
+    // heights over z0m, the pass's vegetation / snow factors, lw_grnd
+    s.lg_u = xlog(s.zldis / s.z0mv);
+    s.lg_u10 = xlog(s.zldis / (10.0 + s.z0mv));
+    s.lg_t = xlog((s.hgt_t - s.displa) / s.z0mv);
+    s.lg_q = xlog((s.hgt_q - s.displa) / s.z0mv);
+    s.lg_2m = xlog((2.0 + s.z0mv) / s.z0mv);
+    s.lg_u10m = xlog(fmax(1.0, s.hgt_u / 10.0));
+    s.pz_m = xpow(1.574, 0.333);
+    s.pz_t = xpow(0.465, -0.333);
+    s.w_sai = xexp(-(elai + esai));
+    s.sqrt_dleaf = sqrt(A.pft.dleaf[s.ivt]);
+    {
+        const double fsno_dl = io.snow_depth[c] / A.par.z_dl;
+        const double elai_dl = A.par.lai_dl * (1.0 - fmin(fsno_dl, 1.0));
+        s.one_m_edl = 1.0 - xexp(-elai_dl);
+        const int ldc = io.ldc, snl = io.snl[c];
+        const double frac_sno = io.frac_sno_eff[c], frac_h2osfc = io.frac_h2osfc[c];
+        s.lw_grnd = (frac_sno * ipow4(io.t_soisno[c + (size_t)(snl + NLEVSNO) * ldc]) +
+                     (1.0 - frac_sno - frac_h2osfc) * ipow4(io.t_soisno[c + (size_t)NLEVSNO * ldc]) +
+                     frac_h2osfc * ipow4(io.t_h2osfc[c]));
+    }
+    // Photosynthesis constants of the patch (PhotosynthesisMod.F90:1555-1830)
+    {
+        const ctsmg_canopy_params& P = A.par;
+        const ctsmg_pftcon& F = A.pft;
+        const int ivt = s.ivt;
+        s.c3 = (llround(F.c3psn[ivt]) == 1) ? 1 : 0;
+        const double lnc = 1.0 / (F.slatop[ivt] * F.leafcn[ivt]);
+        double vcmax25top = lnc * F.flnr[ivt] * P.fnr * P.act25 * s.dayl_factor;
+        vcmax25top = vcmax25top * F.fnitr[ivt];
+        const double t10c = fmin(fmax((io.t_a10[p] - TFRZ), 11.0), 35.0);
+        s.q.vcmax25top = vcmax25top;
+        s.q.jmax25top = ((2.59 - 0.035 * t10c) * vcmax25top) * P.jmax25top_sf;
+        s.q.vcmaxse = (668.39 - 1.07 * t10c) * P.vcmaxse_sf;
+        s.q.jmaxse = (659.70 - 0.75 * t10c) * P.jmaxse_sf;
+        s.q.tpuse = (668.39 - 1.07 * t10c) * P.tpuse_sf;
+        s.q.f25_lmr = fth25(P.lmrhd, P.lmrse);
+        s.q.f25_vc = fth25(P.vcmaxhd, s.q.vcmaxse);
+        s.q.f25_j = fth25(P.jmaxhd, s.q.jmaxse);
+        s.q.f25_tpu = fth25(P.tpuhd, s.q.tpuse);
+        s.q.cf = io.forc_pbot[c] / (RGAS * 1.e-3 * thm) * 1.e06;
+        s.q.mslope = A.medlynslope_p ? A.medlynslope_p[p] : F.medlynslope[ivt];
+        s.q.mint = A.medlynintercept_p ? A.medlynintercept_p[p] : F.medlynintercept[ivt];
+        s.q.mbb = F.mbbopt[ivt];
+    }
     s.num_iter = 0;
     s.tl_ini = s.t_veg;
     s.liqcan = io.liqcan[p];
@@ -471,11 +558,11 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, Err& err, double dtime) {
     s.raw_a = 1.0 / (s.temp2 * ustar);
     s.uaf = s.um * sqrt(1.0 / (s.ram1 * s.um));
     const double elai = io.elai[p], esai = io.esai[p];
-    const double cfl = P.cv / (sqrt(s.uaf) * sqrt(A.pft.dleaf[s.ivt]));
+    const double cfl = P.cv / (sqrt(s.uaf) * s.sqrt_dleaf);
     s.rb = 1.0 / (cfl * s.uaf);
     const double rb = s.rb;
-    const double w = exp(-(elai + esai));
-    const double csoilb = VKC / (P.a_coef * pow(io.z0mg[c] * s.uaf / NU_PARAM, P.a_exp));
+    const double w = s.w_sai;
+    const double csoilb = VKC / (P.a_coef * xpow(io.z0mg[c] * s.uaf / NU_PARAM, P.a_exp));
     const double csoilcn = csoilb * w + P.csoilc * (1.0 - w);
     s.rah_b = 1.0 / (csoilcn * s.uaf);
     const double raw_b = s.rah_b;
@@ -486,12 +573,22 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, Err& err, double dtime) {
     s.vpd_last = fmax((svpts - eah), 50.0) * 0.001;
     const double thm = io.thm[p], btran = io.btran[p];
     const double laisun = io.laisun[p], laisha = io.laisha[p];
-    s.sun = photosynthesis(A, p, pg, s.ivt, s.t_veg, io.t_a10[p], thm, forc_pbot, svpts, eah, io.forc_po2[g],
-                           io.forc_pco2[g], rb, btran, s.dayl_factor, io.parsun_z[p], laisun, io.vcmaxcintsun[p],
-                           s.st, s.vpd_can, s.rh_leaf, err);
-    s.sha = photosynthesis(A, p, pg, s.ivt, s.t_veg, io.t_a10[p], thm, forc_pbot, svpts, eah, io.forc_po2[g],
-                           io.forc_pco2[g], rb, btran, s.dayl_factor, io.parsha_z[p], laisha, io.vcmaxcintsha[p],
-                           s.st, s.vpd_can, s.rh_leaf, err);
+    const double oair = io.forc_po2[g], cair = io.forc_pco2[g];
+    const double parsun = io.parsun_z[p], parsha = io.parsha_z[p];
+    PsnTemp T;
+    psn_temp(A, s, forc_pbot, oair, parsun > 0.0 || parsha > 0.0, T);
+    // sunlit then shaded phase (PhotosynthesisMod called with phase='sun' and
+    // 'sha', CanopyFluxesMod.F90:1143-1169); a loop, so the phase body and
+    // its root finder are compiled once
+#pragma unroll 1
+    for (int ph = 0; ph < 2; ++ph) {
+        const PhaseOut o = photosynthesis(A, s, T, pg, forc_pbot, svpts, eah, oair, cair, rb, btran,
+                                          ph ? parsha : parsun, ph ? laisha : laisun,
+                                          ph ? io.vcmaxcintsha[p] : io.vcmaxcintsun[p], s.st, s.vpd_can, s.rh_leaf,
+                                          err);
+        if (ph) s.sha = o;
+        else s.sun = o;
+    }
     const double sa_leaf = elai + esai;
     const double wta = 1.0 / s.rah_a;
     const double wtl = sa_leaf / rb;
@@ -519,9 +616,7 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, Err& err, double dtime) {
     const double fv = (double)io.frac_veg_nosno[p];
     const double wtaq = fv / s.raw_a;
     const double wtlq = fv * (elai + esai) / rb * rpp;
-    const double fsno_dl = io.snow_depth[c] / P.z_dl;
-    const double elai_dl = P.lai_dl * (1.0 - fmin(fsno_dl, 1.0));
-    const double rdl = (1.0 - exp(-elai_dl)) / (0.004 * s.uaf);
+    const double rdl = s.one_m_edl / (0.004 * s.uaf);
     s.wtgq = (s.delq < 0.0) ? fv / (raw_b + rdl) : fv / (raw_b + io.soilresis[c]);
     const double wtsqi = 1.0 / (wtaq + wtlq + s.wtgq);
     const double wtgq0 = s.wtgq * wtsqi;
@@ -539,12 +634,7 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, Err& err, double dtime) {
         s.efe = 0.1 * efeold;
         erre = s.efe - efeold;
     }
-    const int ldc = io.ldc;
-    const int snl = io.snl[c];
-    const double frac_sno = io.frac_sno_eff[c], frac_h2osfc = io.frac_h2osfc[c];
-    const double lw_grnd = (frac_sno * ipow4(io.t_soisno[c + (size_t)(snl + NLEVSNO) * ldc]) +
-                            (1.0 - frac_sno - frac_h2osfc) * ipow4(io.t_soisno[c + (size_t)NLEVSNO * ldc]) +
-                            frac_h2osfc * ipow4(io.t_h2osfc[c]));
+    const double lw_grnd = s.lw_grnd;
     const double sabv = io.sabv[p];
     const double t_veg = s.t_veg;
     double dt_veg = ((1.0 - 0.0) * (sabv + s.air + s.bir * ipow4(t_veg) + s.cir * lw_grnd) - efsh - s.efe - 0.0 + 0.0 -
@@ -587,7 +677,7 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, Err& err, double dtime) {
         s.um = fmax(s.ur, 0.1);
     } else {
         zeta = fmax(-100.0, fmin(zeta, -0.01));
-        const double wc = (ustar * thvstar > 0.0) ? 0.0 : 1.0 * pow(-GRAV * ustar * thvstar * 1000.0 / thv, 0.333);
+        const double wc = (ustar * thvstar > 0.0) ? 0.0 : 1.0 * xpow(-GRAV * ustar * thvstar * 1000.0 / thv, 0.333);
         s.um = sqrt(s.ur * s.ur + wc * wc);
     }
     s.zeta = zeta;
@@ -712,45 +802,147 @@ __device__ void finalize(const CanopyArgs& A, const Patch& s, double dtime) {
     io.fm[p] = s.fm;
 }
 
+// Work order of the iterating kernel: patches grouped by the branches their
+// passes are expected to take -- the surface-layer regime (FrictionVelocity's
+// zeta < -zetam, < -zetat, < 0 or stable, from the bulk Richardson number of
+// setup), C4 photosynthesis, no PAR in either phase -- so that the lanes of a
+// warp mostly follow the same path; in the resident modes the patches that
+// needed many passes in the previous step go first, so that long iterations
+// do not start at the end of the queue.  Only the schedule changes.
+constexpr int NKEY = 64;
+struct Order {
+    int* key;       // [nfilt] bucket of each filter position
+    int* order;     // [nfilt] filter positions in bucket order
+    int* hist;      // [NKEY] patches per bucket
+    int* fill;      // [NKEY] positions handed out per bucket
+};
+
+__device__ __forceinline__ Order order_of(double* ws, int nfilt) {
+    int* b = reinterpret_cast<int*>(ws + (size_t)NPD * nfilt) + (size_t)NPI * nfilt;
+    return Order{b, b + nfilt, b + 2 * (size_t)nfilt, b + 2 * (size_t)nfilt + NKEY};
+}
+
 __global__ void __launch_bounds__(128)
-canopy_kernel(CanopyArgs A, int nfilt, const int32_t* __restrict__ filt, double dtime, int* __restrict__ next,
-              DevError* derr) {
-    Err err{0, 0};
+canopy_setup_kernel(CanopyArgs A, int nfilt, const int32_t* __restrict__ filt, double* __restrict__ ws) {
+    __shared__ int bh[NKEY];
+    if (threadIdx.x < NKEY) bh[threadIdx.x] = 0;
+    __syncthreads();
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    const Order O = order_of(ws, nfilt);
+    if (f < nfilt) {
+        Patch s{};
+        Err err{0, 0};
+        setup(A, s, (filt ? filt[f] : f + A.begp) - A.begp, err);
+        s.err_code = err.code;
+        s.err_idx = err.idx;
+        store_patch(ws, nfilt, f, s);
+        const double zeta0 = s.zldis / s.obu;
+        const bool dark = !(A.io.parsun_z[s.p] > 0.0 || A.io.parsha_z[s.p] > 0.0);
+        const int regime = zeta0 < -1.574 ? 3 : zeta0 < -0.465 ? 2 : zeta0 < 0.0 ? 1 : 0;
+        int heavy = 2;
+        if (A.engine) {
+            const int ni = A.io.num_iter[s.p];
+            heavy = ni >= 16 ? 0 : ni >= 8 ? 1 : 2;
+        }
+        const int k = heavy * 16 + regime + (s.c3 ? 0 : 4) + (dark ? 8 : 0);
+        O.key[f] = k;
+        atomicAdd(&bh[k], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x < NKEY && bh[threadIdx.x]) atomicAdd(&O.hist[threadIdx.x], bh[threadIdx.x]);
+}
+
+// Counting-sort scatter of the filter positions by bucket (block-aggregated
+// reservations; the order within a bucket is immaterial).
+__global__ void __launch_bounds__(128) canopy_order_kernel(int nfilt, double* __restrict__ ws) {
+    __shared__ int bh[NKEY], base[NKEY];
+    const Order O = order_of(ws, nfilt);
+    if (threadIdx.x < NKEY) bh[threadIdx.x] = 0;
+    __syncthreads();
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    int k = 0, r = 0;
+    if (f < nfilt) {
+        k = O.key[f];
+        r = atomicAdd(&bh[k], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x < NKEY) {
+        int start = 0;
+        for (int j = 0; j < (int)threadIdx.x; ++j) start += O.hist[j];
+        base[threadIdx.x] = bh[threadIdx.x] ? start + atomicAdd(&O.fill[threadIdx.x], bh[threadIdx.x]) : 0;
+    }
+    __syncthreads();
+    if (f < nfilt) O.order[base[k] + r] = f;
+}
+
+#ifndef CTSMG_CANOPY_MIN_BLOCKS
+#define CTSMG_CANOPY_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(128, CTSMG_CANOPY_MIN_BLOCKS)
+canopy_iterate_kernel(CanopyArgs A, int nfilt, double* __restrict__ ws, double dtime, int* __restrict__ next) {
     Patch s;
-    int f = atomicAdd(next, 1);
-    bool active = f < nfilt;
-    if (active) setup(A, s, (filt ? filt[f] : f + A.begp) - A.begp, err);
+    Err err{0, 0};
+    const int* __restrict__ order = order_of(ws, nfilt).order;
+    int f = -1;                        // filter position of the patch this lane holds
 #pragma unroll 1
-    while (active) {
-        const bool done = pass(A, s, err, dtime);
-        if (done) {
-            finalize(A, s, dtime);
-            if (err.code) report_error(derr, err.idx, 0, err.code);
-            err = Err{0, 0};
-            f = atomicAdd(next, 1);
-            active = f < nfilt;
-            if (active) setup(A, s, (filt ? filt[f] : f + A.begp) - A.begp, err);
+    for (;;) {
+        if (f < 0) {
+            const int i = atomicAdd(next, 1);
+            if (i >= nfilt) break;
+            f = order[i];
+            load_patch(ws, nfilt, f, s);
+            err = Err{s.err_code, s.err_idx};
+        }
+        if (pass(A, s, err, dtime)) {
+            s.err_code = err.code;
+            s.err_idx = err.idx;
+            store_patch(ws, nfilt, f, s);
+            f = -1;
         }
     }
 }
 
+__global__ void __launch_bounds__(128)
+canopy_finalize_kernel(CanopyArgs A, int nfilt, const double* __restrict__ ws, double dtime, DevError* derr) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nfilt) return;
+    Patch s;
+    load_patch(ws, nfilt, f, s);
+    finalize(A, s, dtime);
+    if (s.err_code) report_error(derr, s.err_idx, 0, s.err_code);
+}
+
 } // namespace canopy
 
+// per patch: the record (NPD doubles, NPI ints), its bucket key and its slot
+// in the work order; plus the bucket counters
+size_t canopy_ws_bytes_per_patch() { return (size_t)canopy::NPD * 8 + (size_t)canopy::NPI * 4 + 8; }
+
+size_t canopy_ws_bytes(int nfilt) {
+    return canopy_ws_bytes_per_patch() * (size_t)(nfilt > 0 ? nfilt : 0) + 2 * canopy::NKEY * 4 + 256;
+}
+
 cudaError_t launch_canopy(const CanopyArgs& a, int nfilt, const int32_t* d_filt, double dtime, int* d_counter,
-                          DevError* err, cudaStream_t s) {
+                          DevError* err, double* ws, cudaStream_t s) {
     if (nfilt <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(int), s);
     if (e != cudaSuccess) return e;
+    int* counters = reinterpret_cast<int*>(ws + (size_t)canopy::NPD * nfilt) + (size_t)(canopy::NPI + 2) * nfilt;
+    e = cudaMemsetAsync(counters, 0, 2 * canopy::NKEY * sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    const int nb = (nfilt + 127) / 128;
+    canopy::canopy_setup_kernel<<<nb, 128, 0, s>>>(a, nfilt, d_filt, ws);
+    canopy::canopy_order_kernel<<<nb, 128, 0, s>>>(nfilt, ws);
     int nsm = 152;
     int dev = 0;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, canopy::canopy_kernel, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, canopy::canopy_iterate_kernel, 128, 0);
     if (per_sm < 1) per_sm = 1;
-    long long want = (long long)nsm * per_sm;
-    long long need = (nfilt + 127) / 128;
-    int blocks = (int)(want < need ? want : need);
-    canopy::canopy_kernel<<<blocks, 128, 0, s>>>(a, nfilt, d_filt, dtime, d_counter, err);
+    const long long want = (long long)nsm * per_sm;
+    const int blocks = (int)(want < nb ? want : nb);
+    canopy::canopy_iterate_kernel<<<blocks, 128, 0, s>>>(a, nfilt, ws, dtime, d_counter);
+    canopy::canopy_finalize_kernel<<<nb, 128, 0, s>>>(a, nfilt, ws, dtime, err);
     return cudaGetLastError();
 }
 

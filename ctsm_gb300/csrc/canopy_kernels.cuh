@@ -18,6 +18,10 @@ struct CanopyArgs {
     const double* medlynslope_p;
     const double* medlynintercept_p;
 };
+// Device bytes of the per-patch iteration records of a call over nfilt patches.
+size_t canopy_ws_bytes(int nfilt);
+size_t canopy_ws_bytes_per_patch();
+// ws: canopy_ws_bytes(nfilt) bytes of device memory, 8-byte aligned.
 cudaError_t launch_canopy(const CanopyArgs& a, int nfilt, const int32_t* d_filt, double dtime, int* d_counter,
-                          DevError* err, cudaStream_t s);
+                          DevError* err, double* ws, cudaStream_t s);
 } // namespace ctsmg

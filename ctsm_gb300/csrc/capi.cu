@@ -516,12 +516,14 @@ extern "C" int32_t ctsmg_canopyfluxes(const ctsmg_bounds* bounds, int32_t num_ex
     }
     if (num_exposedvegp == 0) return 0;
     const int ldc = io->ldc, ldp = io->ldp, ldg = io->ldg;
-    size_t need = table_bytes(CANOPY_TABLE, CANOPY_NFIELDS, ldc, ldp, ldg) + (size_t)num_exposedvegp * 4 + 8192;
+    size_t need = table_bytes(CANOPY_TABLE, CANOPY_NFIELDS, ldc, ldp, ldg) + (size_t)num_exposedvegp * 4 +
+                  canopy_ws_bytes(num_exposedvegp) + 8192;
     if ((rc = arena_reserve(c, need))) return rc;
     CanopyArgs a;
     if ((rc = stage_in(c, io, &a.io, sizeof a.io, CANOPY_TABLE, CANOPY_NFIELDS, ldc, ldp, ldg))) return rc;
     int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_exposedvegp * 4);
     int* counter = (int*)arena_take(c, 256);
+    double* cws = (double*)arena_take(c, canopy_ws_bytes(num_exposedvegp));
     cudaError_t e = cudaMemcpyAsync(dfilt, filter_exposedvegp, (size_t)num_exposedvegp * 4, cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
     e = cudaMemsetAsync(c->err, 0xff, sizeof(DevError), c->stream);
@@ -538,7 +540,7 @@ extern "C" int32_t ctsmg_canopyfluxes(const ctsmg_bounds* bounds, int32_t num_ex
     a.engine = 0;
     a.medlynslope_p = nullptr;
     a.medlynintercept_p = nullptr;
-    e = launch_canopy(a, num_exposedvegp, dfilt, dtime, counter, c->err, c->stream);
+    e = launch_canopy(a, num_exposedvegp, dfilt, dtime, counter, c->err, cws, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "canopy kernel launch");
     if ((rc = stage_out(c, io, &a.io, CANOPY_TABLE, CANOPY_NFIELDS, ldc, ldp, ldg))) return rc;
     e = cudaStreamSynchronize(c->stream);

@@ -38,6 +38,7 @@ struct Batch {
     double* mslope = nullptr;
     double* mint = nullptr;
     int* counter = nullptr;
+    double* cws = nullptr;         // CanopyFluxes iteration records
     int32_t* d_perm = nullptr;     // sorted position -> original column index (0-based)
     double* ws = nullptr;
     DevError* err = nullptr;
@@ -71,8 +72,8 @@ static cudaError_t enqueue_step(Batch* b) {
         if (e != cudaSuccess) return e;
     }
     if (b->cfg.with_canopy) {
-        e = launch_canopy(b->cargs, b->cfg.npatch, nullptr, b->cfg.dtime, b->counter, b->err, b->stream);
-        if (e != cudaSuccess) return e;
+        e = launch_canopy(b->cargs, b->cfg.npatch, nullptr, b->cfg.dtime, b->counter, b->err, b->cws, b->stream);
+        if (e != cudaSuccess || b->cfg.order == 2) return e;
         e = launch_rootsink(b->dst.col_patchi, b->dst.col_npatches, b->dst.wtcol, b->cargs.io.qflx_tran_veg,
                             b->rootr, b->cfg.npatch, (double*)b->dsw.qflx_rootsoi, ncol, b->stream);
         if (e != cudaSuccess) return e;
@@ -103,7 +104,7 @@ static void batch_free(Batch* b) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
     for (auto& f : b->fields) if (f.dptr) cudaFree(f.dptr);
     for (void* p : {(void*)b->d_perm, (void*)b->ws, (void*)b->err, b->snapshot, (void*)b->rootr, (void*)b->mslope,
-                    (void*)b->mint, (void*)b->counter, b->bal_mem})
+                    (void*)b->mint, (void*)b->counter, (void*)b->cws, b->bal_mem})
         if (p) cudaFree(p);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
@@ -123,14 +124,18 @@ extern "C" int32_t ctsmg_batch_create2(ctsmg_batch* out, const ctsmg_batch_confi
                                        const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio, const double* rootr,
                                        const double* medlynslope_p, const double* medlynintercept_p,
                                        const ctsmg_canopy_params* cpar, const ctsmg_pftcon* pft) {
-    if (!out || !cfg || !sw || !st) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
+    const bool canopy_only = cfg && cfg->order == 2;
+    if (!out || !cfg || (!canopy_only && (!sw || !st))) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
     const int ncol = cfg->ncol, npatch = cfg->npatch;
     if (ncol <= 0 || npatch < 0) return set_error(CTSMG_E_ARG, "ncol must be positive", 0, 0);
-    if (sw->ldc != ncol || st->ldc != ncol || st->ldp != npatch)
+    if (!canopy_only && (sw->ldc != ncol || st->ldc != ncol || st->ldp != npatch))
         return set_error(CTSMG_E_ARG, "batch arrays must be dense: ldc = ncol, ldp = npatch", 0, 0);
     if (!(cfg->dtime > 0.0)) return set_error(CTSMG_E_ARG, "dtime must be positive", 0, 0);
+    if (cfg->order < 0 || cfg->order > 2 || (cfg->order == 2 && (!cfg->with_canopy || cfg->balance)))
+        return set_error(CTSMG_E_ARG, "order must be 0, 1, or 2 (CanopyFluxes only: with_canopy, no balance)", 0, 0);
     if (cfg->with_canopy) {
-        if (!cio || !rootr || !cpar || !pft) return set_error(CTSMG_E_ARG, "with_canopy needs cio, rootr, params", 0, 0);
+        if (!cio || (!rootr && !canopy_only) || !cpar || !pft)
+            return set_error(CTSMG_E_ARG, "with_canopy needs cio, rootr, params", 0, 0);
         if (cio->ldc != ncol || cio->ldp != npatch || cio->ldg != cfg->ngrid || cio->begg != 1)
             return set_error(CTSMG_E_ARG, "canopy arrays must be dense (ldg = ngrid, begg = 1)", 0, 0);
         for (int p = 0; p < npatch; ++p) {
@@ -139,7 +144,7 @@ extern "C" int32_t ctsmg_batch_create2(ctsmg_batch* out, const ctsmg_batch_confi
                 return set_error(CTSMG_E_ARG, "patch column / gridcell / itype out of range", p + 1, 0);
         }
     }
-    for (int c = 0; c < ncol; ++c) {
+    for (int c = 0; c < (canopy_only ? 0 : ncol); ++c) {
         const int s = st->snl[c], pi = st->col_patchi[c], np = st->col_npatches[c];
         if (s > 0 || s < -NLEVSNO) return set_error(CTSMG_E_ARG, "snl outside -nlevsno..0", c + 1, 0);
         if (np < 0 || pi < 1 || pi + np - 1 > npatch)
@@ -156,7 +161,7 @@ extern "C" int32_t ctsmg_batch_create2(ctsmg_batch* out, const ctsmg_batch_confi
     // bucket columns: more snow layers first, then shallower bedrock
     std::vector<int32_t> perm(ncol), inv(ncol);
     std::iota(perm.begin(), perm.end(), 0);
-    if (cfg->bucket)
+    if (cfg->bucket && !canopy_only)
         std::stable_sort(perm.begin(), perm.end(), [&](int a, int c) {
             if (st->snl[a] != st->snl[c]) return st->snl[a] < st->snl[c];
             return st->nbedrock[a] < st->nbedrock[c];
@@ -205,11 +210,13 @@ extern "C" int32_t ctsmg_batch_create2(ctsmg_batch* out, const ctsmg_batch_confi
         }
         return 0;
     };
-    std::memcpy(&b->dsw, sw, sizeof b->dsw);
-    std::memcpy(&b->dst, st, sizeof b->dst);
     int rc;
-    if ((rc = add(SOILWATER_TABLE, SOILWATER_NFIELDS, sw, &b->dsw))) return fail(rc);
-    if ((rc = add(SOILTEMP_TABLE, SOILTEMP_NFIELDS, st, &b->dst))) return fail(rc);
+    if (!canopy_only) {
+        std::memcpy(&b->dsw, sw, sizeof b->dsw);
+        std::memcpy(&b->dst, st, sizeof b->dst);
+        if ((rc = add(SOILWATER_TABLE, SOILWATER_NFIELDS, sw, &b->dsw))) return fail(rc);
+        if ((rc = add(SOILTEMP_TABLE, SOILTEMP_NFIELDS, st, &b->dst))) return fail(rc);
+    }
     if (cfg->with_canopy) {
         std::memcpy(&b->cargs.io, cio, sizeof b->cargs.io);
         if ((rc = add(CANOPY_TABLE, CANOPY_NFIELDS, cio, &b->cargs.io))) return fail(rc);
@@ -221,8 +228,11 @@ extern "C" int32_t ctsmg_batch_create2(ctsmg_batch* out, const ctsmg_batch_confi
         b->cargs.begp = 1;
         b->cargs.engine = 1;
         const size_t pb = (size_t)npatch * 8;
-        if ((e = cudaMalloc(&b->rootr, pb * NLEVSOI)) != cudaSuccess) return fail(cuda_err(e, "rootr"));
-        if ((e = cudaMemcpy(b->rootr, rootr, pb * NLEVSOI, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(cuda_err(e, "rootr"));
+        if (!canopy_only) {
+            if ((e = cudaMalloc(&b->rootr, pb * NLEVSOI)) != cudaSuccess) return fail(cuda_err(e, "rootr"));
+            if ((e = cudaMemcpy(b->rootr, rootr, pb * NLEVSOI, cudaMemcpyHostToDevice)) != cudaSuccess)
+                return fail(cuda_err(e, "rootr"));
+        }
         if (medlynslope_p) {
             if ((e = cudaMalloc(&b->mslope, pb)) != cudaSuccess) return fail(cuda_err(e, "mslope"));
             if ((e = cudaMemcpy(b->mslope, medlynslope_p, pb, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(cuda_err(e, "mslope"));
@@ -234,6 +244,7 @@ extern "C" int32_t ctsmg_batch_create2(ctsmg_batch* out, const ctsmg_batch_confi
         b->cargs.medlynslope_p = b->mslope;
         b->cargs.medlynintercept_p = b->mint;
         if ((e = cudaMalloc(&b->counter, 256)) != cudaSuccess) return fail(cuda_err(e, "counter"));
+        if ((e = cudaMalloc(&b->cws, canopy_ws_bytes(npatch))) != cudaSuccess) return fail(cuda_err(e, "canopy ws"));
     }
     if (cfg->balance) {
         const size_t ssb = (size_t)ncol * (NLEVSNO + NLEVGRND) * 8, cb = (size_t)ncol * 8;
@@ -333,12 +344,13 @@ static int download_table(Batch* b, const FieldDesc* tab, int nf, const void* hi
 
 extern "C" int32_t ctsmg_batch_download2(ctsmg_batch bh, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
                                          const ctsmg_canopy_io* cio) {
-    if (!bh || !sw || !st) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
+    if (!bh) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
     Batch* b = bh->b;
+    if (b->cfg.order != 2 && (!sw || !st)) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
     CK(cudaStreamSynchronize(b->stream), "sync");
     int rc;
-    if ((rc = download_table(b, SOILWATER_TABLE, SOILWATER_NFIELDS, sw))) return rc;
-    if ((rc = download_table(b, SOILTEMP_TABLE, SOILTEMP_NFIELDS, st))) return rc;
+    if (sw && (rc = download_table(b, SOILWATER_TABLE, SOILWATER_NFIELDS, sw))) return rc;
+    if (st && (rc = download_table(b, SOILTEMP_TABLE, SOILTEMP_NFIELDS, st))) return rc;
     if (cio && b->cfg.with_canopy && (rc = download_table(b, CANOPY_TABLE, CANOPY_NFIELDS, cio))) return rc;
     return 0;
 }

@@ -826,10 +826,11 @@ soiltemp_kernel(ctsmg_soiltemp_io io, int begc, int begp, int nfilt, const int32
 template <int BLOCK, int ORDER>
 __global__ void __launch_bounds__(BLOCK)
 soilstep_kernel(ctsmg_soilwater_io wio, ctsmg_soiltemp_io tio, int ncol, double e_ice, double dtime,
-                int snow_method, double* ws, int ws_ld, DevError* err) {
-    const int c = blockIdx.x * BLOCK + threadIdx.x;
-    if (c >= ncol) return;
-    Scratch S{ws, ws_ld, c};
+                int snow_method, double* ws, int ws_ld, DevError* err, const int32_t* __restrict__ filt) {
+    const int fc = blockIdx.x * BLOCK + threadIdx.x;
+    if (fc >= ncol) return;
+    const int c = filt ? filt[fc] - 1 : fc;     // filt: 1-based column positions (pool mode)
+    Scratch S{ws, ws_ld, fc};
     if (ORDER == 0) zd09_column(wio, c, e_ice, dtime);
     int info = soiltemp_column(tio, c, 1, dtime, snow_method, S);
     if (info != 0) report_error(err, c + 1, info, CTSMG_E_SINGULAR);
@@ -850,9 +851,10 @@ soilstep_kernel(ctsmg_soilwater_io wio, ctsmg_soiltemp_io tio, int ncol, double 
 __global__ void rootsink_kernel(const int32_t* __restrict__ col_patchi, const int32_t* __restrict__ col_npatches,
                                 const double* __restrict__ wtcol, const double* __restrict__ qflx_tran_veg,
                                 const double* __restrict__ rootr, int ldp, double* __restrict__ qflx_rootsoi,
-                                int ncol) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncol) return;
+                                int ncol, int ldc, const int32_t* __restrict__ filt) {
+    const int fc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fc >= ncol) return;
+    const int c = filt ? filt[fc] - 1 : fc;
     const int p0 = col_patchi[c] - 1, np = col_npatches[c];
     double temp = 0.0, tran_col = 0.0;
     for (int p = p0; p < p0 + np; ++p) temp = temp + qflx_tran_veg[p] * wtcol[p];
@@ -862,7 +864,7 @@ __global__ void rootsink_kernel(const int32_t* __restrict__ col_patchi, const in
         double rc = 0.0;
         for (int p = p0; p < p0 + np; ++p) rc = rc + rootr[p + (size_t)(j - 1) * ldp] * qflx_tran_veg[p] * wtcol[p];
         if (temp != 0.0) rc = rc / temp;
-        qflx_rootsoi[c + (size_t)(j - 1) * ncol] = rc * tran_col;
+        qflx_rootsoi[c + (size_t)(j - 1) * ldc] = rc * tran_col;
     }
 }
 
@@ -885,35 +887,38 @@ cudaError_t launch_soiltemp(const ctsmg_soiltemp_io& io, int begc, int begp, int
 template <int ORDER>
 static void launch_soilstep_order(const ctsmg_soilwater_io& wio, const ctsmg_soiltemp_io& tio, int ncol,
                                   double e_ice, double dtime, int snow_method, double* ws, int ws_ld,
-                                  DevError* err, cudaStream_t s, int block) {
+                                  DevError* err, cudaStream_t s, int block, const int32_t* filt) {
     switch (block) {
         case 64:
-            soilstep_kernel<64, ORDER><<<(ncol + 63) / 64, 64, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err);
+            soilstep_kernel<64, ORDER><<<(ncol + 63) / 64, 64, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method, ws,
+                                                                       ws_ld, err, filt);
             break;
         case 256:
-            soilstep_kernel<256, ORDER><<<(ncol + 255) / 256, 256, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err);
+            soilstep_kernel<256, ORDER><<<(ncol + 255) / 256, 256, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method,
+                                                                          ws, ws_ld, err, filt);
             break;
         default:
-            soilstep_kernel<128, ORDER><<<(ncol + 127) / 128, 128, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err);
+            soilstep_kernel<128, ORDER><<<(ncol + 127) / 128, 128, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method,
+                                                                          ws, ws_ld, err, filt);
             break;
     }
 }
 
 cudaError_t launch_soilstep(const ctsmg_soilwater_io& wio, const ctsmg_soiltemp_io& tio, int ncol,
                             double e_ice, double dtime, int snow_method, double* ws, int ws_ld,
-                            DevError* err, cudaStream_t s, int block, int order) {
+                            DevError* err, cudaStream_t s, int block, int order, const int32_t* filt) {
     if (ncol <= 0) return cudaSuccess;
-    if (order == 1) launch_soilstep_order<1>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err, s, block);
-    else launch_soilstep_order<0>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err, s, block);
+    if (order == 1) launch_soilstep_order<1>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err, s, block, filt);
+    else launch_soilstep_order<0>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err, s, block, filt);
     return cudaGetLastError();
 }
 
 cudaError_t launch_rootsink(const int32_t* col_patchi, const int32_t* col_npatches, const double* wtcol,
                             const double* qflx_tran_veg, const double* rootr, int ldp, double* qflx_rootsoi,
-                            int ncol, cudaStream_t s) {
+                            int ncol, cudaStream_t s, int ldc, const int32_t* filt) {
     if (ncol <= 0) return cudaSuccess;
     rootsink_kernel<<<(ncol + 127) / 128, 128, 0, s>>>(col_patchi, col_npatches, wtcol, qflx_tran_veg, rootr, ldp,
-                                                       qflx_rootsoi, ncol);
+                                                       qflx_rootsoi, ncol, ldc > 0 ? ldc : ncol, filt);
     return cudaGetLastError();
 }
 

@@ -29,6 +29,10 @@ def _bind(L):
     L._batch_bound = True
 
 
+def _ref(x):
+    return None if x is None else C.byref(x)
+
+
 class BatchConfig(C.Structure):
     _fields_ = [("ncol", C.c_int32), ("npatch", C.c_int32), ("ngrid", C.c_int32), ("dtime", C.c_double),
                 ("e_ice", C.c_double), ("snow_thermal_cond_method", C.c_int32), ("stomatalcond_method", C.c_int32),
@@ -39,7 +43,9 @@ class BatchConfig(C.Structure):
 class SoilBatch:
     """Resident batch of columns advanced by model steps: SoilWater +
     SoilTemperature (order 0), or, with canopy=True, CanopyFluxes + root sink +
-    SoilTemperature + SoilWater in the driver's order (order 1)."""
+    SoilTemperature + SoilWater in the driver's order (order 1), or
+    CanopyFluxes alone (order 2; `state` then needs only the canopy
+    components)."""
 
     def __init__(self, state, npatch, dtime=1800.0, e_ice=6.0, snow_thermal_cond_method=0, canopy=False,
                  ngrid=None, rootr=None, order=None, bucket=True, stomatalcond_method=1, itmax=40,
@@ -48,12 +54,16 @@ class SoilBatch:
         self.L = load()
         _bind(self.L)
         self.state = state
-        self.ncol = state["zwt"].shape[0]
+        self.canopy_only = order == 2
+        self.ncol = state["forc_pbot" if self.canopy_only else "zwt"].shape[0]
         self.npatch = npatch
         self.canopy = canopy
         self.ngrid = ngrid if ngrid is not None else self.ncol
-        self._sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS, state, self.ncol)
-        self._st = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, state, self.ncol, npatch)
+        if self.canopy_only:
+            self._sw = self._st = None
+        else:
+            self._sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS, state, self.ncol)
+            self._st = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, state, self.ncol, npatch)
         from .balance import skip_steps as _skip
         self.balance_on = balance
         cfg = BatchConfig(self.ncol, npatch, self.ngrid, dtime, e_ice, snow_thermal_cond_method, stomatalcond_method,
@@ -63,15 +73,16 @@ class SoilBatch:
         self.h = C.c_void_p()
         if canopy:
             self._ci = abi.make_io(abi.CanopyIO, abi.CANOPY_FIELDS, state, self.ncol, npatch, self.ngrid, 1)
-            self._rootr = np.ascontiguousarray(rootr, dtype=np.float64)
             dp = C.POINTER(C.c_double)
             ms = state["medlynslope_p"].ctypes.data_as(dp) if per_patch_medlyn else None
             mi = state["medlynintercept_p"].ctypes.data_as(dp) if per_patch_medlyn else None
             self._par = params if params is not None else canopy_inputs.make_params()
             self._pft = pftcon if pftcon is not None else canopy_inputs.make_pftcon()
-            check(self.L.ctsmg_batch_create2(C.byref(self.h), C.byref(cfg), C.byref(self._sw), C.byref(self._st),
-                                             C.byref(self._ci), self._rootr.ctypes.data_as(dp), ms, mi,
-                                             C.byref(self._par), C.byref(self._pft)))
+            self._rootr = None if rootr is None else np.ascontiguousarray(rootr, dtype=np.float64)
+            check(self.L.ctsmg_batch_create2(C.byref(self.h), C.byref(cfg), _ref(self._sw), _ref(self._st),
+                                             C.byref(self._ci),
+                                             None if self._rootr is None else self._rootr.ctypes.data_as(dp), ms,
+                                             mi, C.byref(self._par), C.byref(self._pft)))
         else:
             check(self.L.ctsmg_batch_create2(C.byref(self.h), C.byref(cfg), C.byref(self._sw), C.byref(self._st),
                                              None, None, None, None, None, None))
@@ -89,11 +100,14 @@ class SoilBatch:
 
     def download(self, state=None):
         st = state if state is not None else self.state
-        sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS, st, self.ncol)
-        tt = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, st, self.ncol, self.npatch)
+        if self.canopy_only:
+            sw = tt = None
+        else:
+            sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS, st, self.ncol)
+            tt = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, st, self.ncol, self.npatch)
         if self.canopy:
             ci = abi.make_io(abi.CanopyIO, abi.CANOPY_FIELDS, st, self.ncol, self.npatch, self.ngrid, 1)
-            check(self.L.ctsmg_batch_download2(self.h, C.byref(sw), C.byref(tt), C.byref(ci)))
+            check(self.L.ctsmg_batch_download2(self.h, _ref(sw), _ref(tt), C.byref(ci)))
         else:
             check(self.L.ctsmg_batch_download(self.h, C.byref(sw), C.byref(tt)))
         return st

@@ -360,7 +360,8 @@ typedef struct ctsmg_batch_s* ctsmg_batch;
  * transpiration into SoilWater (Compute_EffecRootFrac_And_VertTranSink_Default,
  * src/biogeophys/SoilWaterPlantSinkMod.F90:332-420); order = 1 is the driver's
  * order CanopyFluxes, SoilTemperature, SoilWater (src/main/clm_driver.F90:766,900,950),
- * order = 0 is SoilWater then SoilTemperature.  bucket = 1 reorders the
+ * order = 0 is SoilWater then SoilTemperature, order = 2 runs CanopyFluxes
+ * alone (the soil state is then read but not advanced).  bucket = 1 reorders the
  * columns by (snl, nbedrock) on the device.                               */
 typedef struct {
     int32_t ncol, npatch, ngrid;
@@ -396,17 +397,80 @@ int32_t ctsmg_batch_download(ctsmg_batch b, const ctsmg_soilwater_io* sw, const 
 /* Same, and the canopy components as well when the batch runs CanopyFluxes. */
 int32_t ctsmg_batch_download2(ctsmg_batch b, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
                               const ctsmg_canopy_io* cio);
-/* Time trial_steps steps for each candidate threads-per-block (64, 128, 256)
- * on the batch's own data, keep the fastest, restore the state. */
 /* Per-column balance results in the caller's column order (any pointer may be
  * NULL): maxima of |errh2o| and |errsoi| over the checked steps, and the last
  * step's signed errors. */
 int32_t ctsmg_batch_balance(ctsmg_batch b, double* errh2o_max, double* errsoi_max, double* errh2o_last,
                             double* errsoi_last);
+/* Time trial_steps steps for each candidate threads-per-block (64, 128, 256)
+ * on the batch's own data, keep the fastest, restore the state. */
 int32_t ctsmg_batch_autotune(ctsmg_batch b, int32_t trial_steps, int32_t* block_out);
 int32_t ctsmg_batch_set_block(ctsmg_batch b, int32_t block);
 int64_t ctsmg_batch_state_bytes(ctsmg_batch b);
 int32_t ctsmg_batch_destroy(ctsmg_batch b);
+
+/* ---------------------------------------------------------------- serving pool */
+/* A device-resident pool of column, patch and gridcell slots that independent
+ * run requests (a single point or a region: their own columns, patches,
+ * gridcells and step count) are admitted into while others are running.  No
+ * reference counterpart: CTSM runs one configuration per executable.  Each
+ * tick advances every admitted, unfinished request by one model step -- the
+ * same step as a batch with with_canopy (CanopyFluxes, root sink,
+ * SoilTemperature, SoilWater, h2osoi_vol refresh) or, with_canopy = 0,
+ * SoilWater then SoilTemperature -- through one CUDA graph whose kernels run
+ * over filters of the active slots (1-based positions, sorted by (snl,
+ * nbedrock)).  Columns never interact, so a request's results do not depend
+ * on what else is in the pool.  Calls on one pool must come from one host
+ * thread at a time. */
+typedef struct ctsmg_pool_s* ctsmg_pool;
+
+typedef struct {
+    int32_t col_capacity, patch_capacity, grid_capacity;   /* slots of each kind  */
+    double dtime, e_ice;
+    int32_t snow_thermal_cond_method, stomatalcond_method, itmax_canopy_fluxes;
+    int32_t with_canopy;
+    int32_t max_inflight;     /* ticks queued ahead of the device (>= 1)      */
+} ctsmg_pool_config;
+
+#define CTSMG_E_FULL          11   /* pool: no free range large enough (nothing changed) */
+
+/* Device bytes one slot of each kind takes in a pool (resident fields, band
+ * scratch, filters, root fractions, per-patch Medlyn parameters), for sizing
+ * the capacities from a memory budget.                                      */
+int32_t ctsmg_pool_slot_bytes(int32_t with_canopy, int64_t* col_bytes, int64_t* patch_bytes, int64_t* grid_bytes);
+/* cpar / pft may be NULL when with_canopy = 0. */
+int32_t ctsmg_pool_create(ctsmg_pool* out, const ctsmg_pool_config* cfg, const ctsmg_canopy_params* cpar,
+                          const ctsmg_pftcon* pft);
+/* Admit one request: its host arrays are dense (begc = begp = begg = 1, ldc =
+ * ncol, ldp = npatch, ldg = ngrid, 1-based col_patchi / patch_column /
+ * patch_gridcell within the request), copied to free slot ranges before the
+ * call returns.  rootr is (p, 1:nlevsoi) with ldp = npatch; medlynslope_p /
+ * medlynintercept_p (p) may be NULL (pftcon values).  Returns CTSMG_E_FULL,
+ * changing nothing, when a range of the needed size is not free.  nsteps >= 1
+ * model steps run from the next tick on; *slot_out identifies the request. */
+int32_t ctsmg_pool_admit(ctsmg_pool p, int32_t ncol, int32_t npatch, int32_t ngrid, int32_t nsteps,
+                         const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio,
+                         const double* rootr, const double* medlynslope_p, const double* medlynintercept_p,
+                         int32_t* slot_out);
+/* Enqueue one step of every running request (returns at once unless
+ * max_inflight ticks are already queued).  *ncol_stepped (may be NULL) is
+ * the number of columns the tick advances. */
+int32_t ctsmg_pool_tick(ctsmg_pool p, int64_t* ncol_stepped);
+/* Requests whose last step has completed on the device (up to cap slots). */
+int32_t ctsmg_pool_poll(ctsmg_pool p, int32_t* slots, int32_t cap, int32_t* n);
+/* Copy a request's state to the host arrays (dense, as for admit; the index
+ * components are not written back) and free its slots.  A request that has
+ * not finished is stopped after the steps already enqueued.  *steps_done
+ * (may be NULL) is the number of steps it ran. */
+int32_t ctsmg_pool_evict(ctsmg_pool p, int32_t slot, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
+                         const ctsmg_canopy_io* cio, int32_t* steps_done);
+/* Wait for the device; reports a band-solve or CanopyFluxes failure as its
+ * status with the request slot in ctsmg_last_error_index and the column (or
+ * patch) within the request in the level slot. */
+int32_t ctsmg_pool_sync(ctsmg_pool p);
+/* Free slots of each kind (largest free range in *_largest; any may be NULL). */
+int32_t ctsmg_pool_free(ctsmg_pool p, int32_t* cols_largest, int32_t* patches_largest, int32_t* grids_largest);
+int32_t ctsmg_pool_destroy(ctsmg_pool p);
 
 /* ---------------------------------------------------------------- measurement */
 /* FP64 FMA throughput of the current GPU in TFLOP/s (a DFMA loop over every

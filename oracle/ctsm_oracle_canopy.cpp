@@ -15,6 +15,7 @@
 #include "ctsm_gpu.h"
 #include "ctsm_oracle.h"
 #include "oracle_libm.h"
+#include "rootfind_testfns.h"
 
 using oracle_libm::o_pow;
 using oracle_libm::o_exp;
@@ -161,13 +162,15 @@ double ci_func(double ci, const PsnCtx& x, PsnState& s) {
     return ci - x.cair + s.an * x.forc_pbot * (1.4 * s.gs_mol + 1.6 * x.gb_mol) / (x.gb_mol * s.gs_mol);
 }
 
-// PhotosynthesisMod.F90:2371-2485
-double brent(double x1, double x2, double f1, double f2, double tol, const PsnCtx& ctx, PsnState& st) {
+// PhotosynthesisMod.F90:2371-2485, for any evaluated function fn(x);
+// *not_bracketed is the endrun condition of :2412-2415.
+template <class F>
+double brent_t(double x1, double x2, double f1, double f2, double tol, F&& fn, bool* not_bracketed) {
     const int itmax = 20;
     const double eps = 1.e-2;
     double a = x1, b = x2, fa = f1, fb = f2;
     if ((fa > 0.0 && fb > 0.0) || (fa < 0.0 && fb < 0.0)) {
-        flag(CTSMG_E_NOT_BRACKETED, ctx.pidx);
+        *not_bracketed = true;
         return b;
     }
     double c = b, fc = fb, d = 0.0, e = 0.0;
@@ -198,7 +201,7 @@ double brent(double x1, double x2, double f1, double f2, double tol, const PsnCt
             }
             if (p > 0.0) q = -q;
             p = std::fabs(p);
-            if (2.0 * p < std::min(3.0 * xm * q - std::fabs(tol1 * q), std::fabs(e * q))) {
+            if (2.0 * p < std::fmin(3.0 * xm * q - std::fabs(tol1 * q), std::fabs(e * q))) {
                 e = d;
                 d = p / q;
             } else {
@@ -213,21 +216,22 @@ double brent(double x1, double x2, double f1, double f2, double tol, const PsnCt
         fa = fb;
         if (std::fabs(d) > tol1) b = b + d;
         else b = b + std::copysign(std::fabs(tol1), xm);
-        fb = ci_func(b, ctx, st);
+        fb = fn(b);
         if (fb == 0.0) break;
     }
     return b;
 }
 
 // PhotosynthesisMod.F90:2251-2368; x0 in/out
-void hybrid(double& x0, const PsnCtx& ctx, PsnState& st) {
+template <class F>
+void hybrid_t(double& x0, F&& fn, bool* not_bracketed) {
     const double eps = 1.e-2, eps1 = 1.e-4;
     const int itmax = 40;
-    double f0 = ci_func(x0, ctx, st);
+    double f0 = fn(x0);
     if (f0 == 0.0) return;
     double minx = x0, minf = f0;
     double x1 = x0 * 0.99;
-    double f1 = ci_func(x1, ctx, st);
+    double f1 = fn(x1);
     if (f1 == 0.0) { x0 = x1; return; }
     if (f1 < minf) { minx = x1; minf = f1; }
     int iter = 0;
@@ -240,19 +244,25 @@ void hybrid(double& x0, const PsnCtx& ctx, PsnState& st) {
         x0 = x1;
         f0 = f1;
         x1 = x;
-        f1 = ci_func(x1, ctx, st);
+        f1 = fn(x1);
         if (f1 < minf) { minx = x1; minf = f1; }
         if (std::fabs(f1) <= eps1) { x0 = x1; break; }
         if (f1 * f0 < 0.0) {
-            x = brent(x0, x1, f0, f1, tol, ctx, st);
+            x = brent_t(x0, x1, f0, f1, tol, fn, not_bracketed);
             x0 = x;
             break;
         }
         if (iter > itmax) {
-            f1 = ci_func(minx, ctx, st);
+            f1 = fn(minx);
             break;
         }
     }
+}
+
+void hybrid(double& x0, const PsnCtx& ctx, PsnState& st) {
+    bool nb = false;
+    hybrid_t(x0, [&](double x) { return ci_func(x, ctx, st); }, &nb);
+    if (nb) flag(CTSMG_E_NOT_BRACKETED, ctx.pidx);
 }
 
 struct Params { ctsmg_canopy_params c; ctsmg_pftcon pft; int method; int itmax; };
@@ -819,6 +829,16 @@ extern "C" void oracle_set_canopy_params(const ctsmg_canopy_params* p, const cts
 extern "C" void oracle_set_patch_medlyn(const double* slope, const double* intercept) {
     g_mslope_p = slope;
     g_mint_p = intercept;
+}
+
+// The points hybrid evaluates for one of the synthetic functions of
+// rootfind_testfns.h (test support: pins the device root finder's control flow).
+extern "C" int oracle_rootfind_trace(int k, const double* prm, double x0, double* xs, int cap, int* not_bracketed) {
+    int n = 0;
+    bool nb = false;
+    hybrid_t(x0, [&](double x) { if (n < cap) xs[n] = x; ++n; return rf_testfn(k, prm, x); }, &nb);
+    *not_bracketed = nb ? 1 : 0;
+    return n;
 }
 
 extern "C" int oracle_quadratic(double a, double b, double c, double* r1, double* r2) {
