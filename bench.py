@@ -13,6 +13,15 @@ Lines reported:
          pinned host buffers, host<->device copies inside the timed region
   cpu_baseline / --impl reference   the CPU oracle (C++ restatement of the
          reference Fortran, OpenMP over clumps of columns) on the host cores
+Extra keys on the same line (rank 0, N = 1):
+  canopy    CanopyFluxes + Photosynthesis over 2,097,152 patches (1-4 per
+            column): device-resident steps and the plain drop-in call
+  ensemble  256 perturbed-parameter members (columns U{512..8192} each) through
+            the full soil + canopy step, batched vs one set of plain drop-in
+            calls per member
+  serving   a Poisson stream of run requests (columns log-uniform 1..50,000,
+            lengths U{48..17,520} steps) through the device pool with a 150 GB
+            admission budget, bounded in wall time
 Under torchrun each rank advances its own 524,288-column shard (no
 collective on the data path; weak scaling); time is the max over ranks.
 """
@@ -47,6 +56,17 @@ def parse():
     p.add_argument("--seed", type=int, default=2026)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-canopy", action="store_true")
+    p.add_argument("--no-ensemble", action="store_true")
+    p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--canopy-patches", type=int, default=2097152)
+    p.add_argument("--canopy-steps", type=int, default=8)
+    p.add_argument("--ens-members", type=int, default=256)
+    p.add_argument("--ens-steps", type=int, default=48)
+    p.add_argument("--serve-requests", type=int, default=64)
+    p.add_argument("--serve-rate", type=float, default=2.0)
+    p.add_argument("--serve-seconds", type=float, default=60.0)
+    p.add_argument("--serve-budget-gb", type=float, default=150.0)
     return p.parse_args()
 
 
@@ -184,6 +204,142 @@ def reference_arm(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+
+# ---------------------------------------------------------------- extra workloads
+def canopy_leg(args, barrier):
+    """CanopyFluxes + Photosynthesis over the canopy workload: resident steps
+    (inputs in HBM, CUDA events) and the plain drop-in call on pinned host
+    arrays (copies in the timed region)."""
+    import torch
+    from ctsm_gb300 import abi, canopy, canopy_inputs as ci, roofline
+    from ctsm_gb300.engine import SoilBatch
+    A, npatch, ncol, ngrid = ci.canopy_patches(args.canopy_patches, seed=args.seed)
+    A0 = copy.deepcopy(A)
+    b = SoilBatch(A, npatch, canopy=True, ngrid=ngrid, order=2)
+    b.run(args.warmup)
+    b.sync()
+    barrier()
+    ms = b.run(args.canopy_steps, timed=True)
+    b.sync()
+    b.download()
+    b.close()
+    mean_ms = float(ms.mean())
+    passes = float(A["num_iter"].mean())
+    flops = roofline.CANOPY_FLOPS_PER_PASS * passes * npatch
+    out = {"workload": "CanopyFluxes+Photosynthesis, %d patches, 1-4 per column, itmax 40" % npatch,
+           "patches": npatch, "steps": args.canopy_steps, "ms_per_step": mean_ms,
+           "patch_steps_per_s": npatch / (mean_ms * 1e-3), "mean_passes": passes,
+           "gpu_launches_per_step": 4,
+           "fp64": {"achieved": flops / (mean_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
+                    "flops_per_pass": roofline.CANOPY_FLOPS_PER_PASS}}
+    if not args.no_e2e:
+        H = {}
+        for k, v in A0.items():
+            t = torch.empty(v.shape, dtype=torch.float64 if v.dtype == np.float64 else torch.int32).pin_memory()
+            h = t.numpy()
+            h[...] = v
+            H[k] = h
+        canopy.set_params()
+        bnd = abi.Bounds(1, ncol, 1, npatch)
+        filt = np.arange(1, npatch + 1, dtype=np.int32)
+        canopy.CanopyFluxes(bnd, npatch, filt, H, DT, ngrid)
+        barrier()
+        k = 3
+        t0 = time.perf_counter()
+        for _ in range(k):
+            canopy.CanopyFluxes(bnd, npatch, filt, H, DT, ngrid)
+        barrier()
+        te = (time.perf_counter() - t0) / k
+        h2d = sum(H[n].nbytes for (n, kk, t, u) in abi.CANOPY_FIELDS)
+        d2h = sum(H[n].nbytes for (n, kk, t, u) in abi.CANOPY_FIELDS if u != "in")
+        out["e2e"] = {"value": npatch / te, "unit": "patch-steps/s", "ms_per_call": 1e3 * te,
+                      "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                      "path": "ctsmg_canopyfluxes (plain drop-in, pinned host arrays)"}
+    return out
+
+
+def ensemble_leg(args, barrier):
+    """The perturbed-parameter ensemble through the full step: all members in
+    one resident batch (one CUDA graph per step) against the plain form, one
+    set of drop-in calls per member (timed on a sample of members)."""
+    from ctsm_gb300 import full_inputs as fi, plain_step, canopy
+    from ctsm_gb300.engine import SoilBatch
+    A, npatch, ngrid, rootr, member_col, factors = fi.ensemble(args.ens_members, seed=args.seed)
+    ncol = A["zwt"].shape[0]
+    b = SoilBatch(copy.deepcopy(A), npatch, canopy=True, ngrid=ngrid, rootr=rootr, per_patch_medlyn=True)
+    block = b.autotune(trial_steps=1)
+    b.run(args.warmup)
+    b.sync()
+    barrier()
+    ms = b.run(args.ens_steps, timed=True)
+    b.sync()
+    b.close()
+    batched = ncol * args.ens_steps / (float(ms.sum()) * 1e-3)
+    # plain form on the first members, two steps each
+    nm = min(8, args.ens_members)
+    cols_done = 0
+    t_plain = 0.0
+    for m in range(nm):
+        cols = np.nonzero(member_col == m)[0]
+        pmask = np.isin(A["patch_column"] - 1, cols)
+        pidx = np.nonzero(pmask)[0]
+        S = {}
+        for k, v in A.items():
+            if v.shape[-1] == ncol:
+                S[k] = np.ascontiguousarray(v[..., cols])
+            elif v.shape[-1] == npatch:
+                S[k] = np.ascontiguousarray(v[..., pidx])
+        S["col_patchi"] = (A["col_patchi"][cols] - pidx[0]).astype(np.int32)
+        S["patch_column"] = (A["patch_column"][pidx] - cols[0]).astype(np.int32)
+        S["patch_gridcell"] = S["patch_column"].copy()
+        rr = np.ascontiguousarray(rootr[:, pidx])
+        d0, z0 = S["displa"].copy(), S["z0mv"].copy()
+        med = (float(factors["medlynslope"][m]), float(factors["medlynintercept"][m]))
+        plain_step.full_step(S, len(pidx), len(cols), rr, d0, z0, med)          # warm-up
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(2):
+            plain_step.full_step(S, len(pidx), len(cols), rr, d0, z0, med)
+        barrier()
+        t_plain += time.perf_counter() - t0
+        cols_done += 2 * len(cols)
+    canopy.set_params()
+    plain = cols_done / t_plain
+    return {"workload": "%d members, columns U{512..8192} each (%d columns, %d patches), full soil+canopy step, "
+                        "8 parameters log-uniform x[0.5,1.5]" % (args.ens_members, ncol, npatch),
+            "columns": ncol, "patches": npatch, "steps": args.ens_steps, "ms_per_step": float(ms.mean()),
+            "batched_column_steps_per_s": batched, "block": block,
+            "plain_column_steps_per_s": plain,
+            "plain_sample": "%d members x 2 steps, one set of drop-in calls per member" % nm,
+            "batched_over_plain": batched / plain}
+
+
+def serving_leg(args):
+    """A Poisson stream of run requests through the device pool, bounded in
+    wall time: requests still running at the limit are stopped (their steps
+    count in the throughput; their pace -- wall seconds per simulated day
+    since arrival -- is reported beside the completed requests' latency)."""
+    from ctsm_gb300 import serving
+    reqs = serving.request_stream(args.serve_requests, args.serve_rate, seed=args.seed)
+    pool = serving.Pool(budget_bytes=args.serve_budget_gb * 1e9)
+    cap = pool.capacity
+    st = serving.serve(pool, reqs, time_limit=args.serve_seconds)
+    pool.close()
+    pace = []
+    for q in reqs:
+        if q.steps_done > 0:
+            end = q.t_done if q.t_done == q.t_done else st["wall_s"]
+            pace.append((end - q.arrival) / (q.steps_done / serving.STEPS_PER_DAY))
+    st.update({"workload": "Poisson arrivals at %.2f/s, %d requests, columns log-uniform 1..50000, "
+                           "lengths U{48..17520} steps, full soil+canopy step" % (args.serve_rate, args.serve_requests),
+               "budget_gb": args.serve_budget_gb, "capacity_columns": cap[0], "time_limit_s": args.serve_seconds,
+               "offered_column_steps": int(sum(q.column_steps() for q in reqs)),
+               "p50_pace_s_per_day": serving.percentile(pace, 50), "p99_pace_s_per_day": serving.percentile(pace, 99),
+               "latency_note": "p50/p99_s_per_day: completed requests, (completion - arrival) / simulated days; "
+                               "pace: every request, (end or limit - arrival) / simulated days run"})
+    return st
+
+
 def ours_arm(args, ws, rank, local):
     import torch
     from ctsm_gb300 import abi, soil, roofline, _lib
@@ -298,6 +454,17 @@ def ours_arm(args, ws, rank, local):
                "sample": "first %d columns of the workload x %d steps (%.1f s)" % (n, steps, dt),
                "cpu": cpu_model()}
 
+    extra = {}
+    if rank == 0 and ws == 1:
+        for name, flag, fn in (("canopy", args.no_canopy, lambda: canopy_leg(args, barrier)),
+                               ("ensemble", args.no_ensemble, lambda: ensemble_leg(args, barrier)),
+                               ("serving", args.no_serving, lambda: serving_leg(args))):
+            if not flag:
+                try:
+                    extra[name] = fn()
+                except Exception as exc:          # a failed leg is reported, not hidden
+                    extra[name] = {"error": "%s: %s" % (type(exc).__name__, exc)}
+
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * t_rank / args.steps, "higher_is_better": True,
@@ -308,6 +475,7 @@ def ours_arm(args, ws, rank, local):
                            "l2": "inputs larger than L2 (resident state %.2f GB vs 129 MB L2)" % state_gb},
                 "gpu_launches": int(args.steps), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clk, "wall_s_timed": wall, "fp64_peak_tflops": fp64.value}
+        line.update(extra)
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist

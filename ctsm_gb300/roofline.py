@@ -13,6 +13,11 @@ NLEVSNO, NLEVSOI, NLEVGRND = abi.NLEVSNO, abi.NLEVSOI, abi.NLEVGRND
 FLOPS_PER_COLUMN_STEP = (424136267 + 219978292 + 2 * 961139171) / 65536.0
 TRAFFIC_PER_COLUMN_STEP = (733.809408e6 + 492.769792e6) / 65536.0
 
+# FP64 floating-point operations per CanopyFluxes pass of one patch
+# (canopy_iterate_kernel: DADD + DMUL + 2 x DFMA executed over 262,144 patches
+# of the canopy workload, 6.266 passes per patch on average).
+CANOPY_FLOPS_PER_PASS = (739121234 + 1058410707 + 2 * 3057904378) / (262144 * 6.266)
+
 
 def _active_levels(kind, nsnow):
     return {"C": 1, "P": 1, "SS": nsnow + NLEVGRND, "ZI": nsnow + NLEVGRND + 1, "G": NLEVGRND,

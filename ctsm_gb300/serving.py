@@ -267,13 +267,16 @@ def serve(pool, requests, time_limit=None, tick_clock=False, clock=time.perf_cou
     admission order reproducible; the recorded admission and completion
     times are then tick numbers too).  Requests still running when time_limit
     runs out are stopped and evicted with the steps they ran.  Returns a dict
-    of statistics; each request's record is on the request object."""
+    of statistics (steady_column_steps_per_s: the rate from the tick at which
+    the last request was admitted to the end); each request's record is on
+    the request object."""
     queue = sorted(requests, key=lambda q: (q.arrival, q.rid))
     running = {}
     nq = 0
     ticks = 0
     col_steps = 0
     max_running_cols = 0
+    t_all, cs_all = None, 0
     t0 = clock()
 
     def now():
@@ -307,6 +310,8 @@ def serve(pool, requests, time_limit=None, tick_clock=False, clock=time.perf_cou
         ticks += 1
         col_steps += n
         max_running_cols = max(max_running_cols, n)
+        if nq == len(queue) and t_all is None:      # every request admitted: steady part begins
+            t_all, cs_all = clock() - t0, col_steps - n
         for slot in pool.poll():
             finish(slot)
     for slot in list(running):          # stopped by the time limit
@@ -316,7 +321,11 @@ def serve(pool, requests, time_limit=None, tick_clock=False, clock=time.perf_cou
     done = [q for q in requests if q.steps_done == q.nsteps]
     per_day = [(q.t_done - q.arrival) / q.days for q in done]
     wait = [q.t_admit - q.arrival for q in requests if not math.isnan(q.t_admit)]
+    steady = None
+    if t_all is not None and wall - t_all > 1.0:
+        steady = (col_steps - cs_all) / (wall - t_all)
     return dict(wall_s=wall, ticks=ticks, column_steps=col_steps, column_steps_per_s=col_steps / wall if wall > 0 else 0.0,
+                steady_column_steps_per_s=steady, steady_from_s=t_all,
                 requests=len(requests), completed=len(done), stopped=len(requests) - len(done) - (len(queue) - nq),
                 never_admitted=len(queue) - nq, max_running_columns=max_running_cols,
                 p50_s_per_day=percentile(per_day, 50), p99_s_per_day=percentile(per_day, 99),
