@@ -21,6 +21,37 @@
 
 namespace ctsmg {
 
+// Powers with a constant base, as exp of a double-double exponent: the
+// product x*ln(base) is formed exactly as hi + lo (FMA error term, Dekker's
+// product; ln(base) split into its nearest double and the remainder), and
+// exp(hi + lo) = exp(hi) (1 + lo) + O(lo^2).  The result carries exp's
+// rounding only, within about 1 ulp of the exact power -- as close as pow
+// itself, for one exp instead of one pow per factor.
+constexpr double LN10_HI = 2.302585092994046, LN10_LO = -2.1707562233822494e-16;
+constexpr double LN_TKWAT_HI = -0.5621189181535413, LN_TKWAT_LO = 1.1409357209435452e-17;   // ln(0.57)
+constexpr double LN_TKICE_HI = 0.8285518175661483, LN_TKICE_LO = 3.2758189660989295e-17;    // ln(2.290)
+
+__device__ __forceinline__ double exp_dd(double hi, double lo) {
+    const double r = exp(hi);
+    return fma(r, lo, r);
+}
+
+// 10^x (IceImpedance, SoilWaterMovementMod.F90:2139-2160)
+__device__ __forceinline__ double pow10_dd(double x) {
+    const double p = x * LN10_HI;
+    return exp_dd(p, fma(x, LN10_HI, -p) + x * LN10_LO);
+}
+
+// tkwat^a * tkice^b (Johansen saturated conductivity, SoilTemperatureMod.F90:700-705)
+__device__ __forceinline__ double tkwat_tkice_pow(double a, double b) {
+    const double p1 = a * LN_TKWAT_HI, p2 = b * LN_TKICE_HI;
+    const double e1 = fma(a, LN_TKWAT_HI, -p1) + a * LN_TKWAT_LO;
+    const double e2 = fma(b, LN_TKICE_HI, -p2) + b * LN_TKICE_LO;
+    const double s = p1 + p2, bb = s - p1;                       // TwoSum
+    const double es = (p1 - (s - bb)) + (p2 - bb);
+    return exp_dd(s, es + e1 + e2);
+}
+
 __device__ __forceinline__ double ipow4(double x) { double x2 = x * x; return x2 * x2; }
 __device__ __forceinline__ double ipow3(double x) { double x2 = x * x; return x2 * x; }
 
@@ -75,19 +106,24 @@ __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, d
 #pragma unroll 1
     for (int j = 1; j <= NLEVSOI; ++j) {
         const double ss = G(io.sucsat, j), ws = G(io.watsat, j), bb = G(io.bsw, j);
+        // three cases (:674-706): water table above the layer, inside it, below
+        // it.  temp0 is the same expression in the last two and tempi is only
+        // needed in the last, so each power has one call site and a warp whose
+        // lanes are in different cases evaluates it once.
+        const bool above = zwtmm <= zimm[j - 1];
+        const bool inside = !above && (zwtmm < zimm[j]) && (zwtmm > zimm[j - 1]);
+        double temp0 = 0.0, tempi = 1.0;
+        if (!above) temp0 = pow(((ss + zwtmm - zimm[j - 1]) / ss), 1.0 - 1.0 / bb);
+        if (!above && !inside) tempi = pow(((ss + zwtmm - zimm[j]) / ss), 1.0 - 1.0 / bb);
         double veq;
-        if (zwtmm <= zimm[j - 1]) {
+        if (above) {
             veq = ws;
-        } else if ((zwtmm < zimm[j]) && (zwtmm > zimm[j - 1])) {
-            double tempi = 1.0;
-            double temp0 = pow(((ss + zwtmm - zimm[j - 1]) / ss), 1.0 - 1.0 / bb);
+        } else if (inside) {
             double voleq1 = -ss * ws / (1.0 - 1.0 / bb) / (zwtmm - zimm[j - 1]) * (tempi - temp0);
             veq = (voleq1 * (zwtmm - zimm[j - 1]) + ws * (zimm[j] - zwtmm)) / (zimm[j] - zimm[j - 1]);
             veq = fmin(ws, veq);
             veq = fmax(veq, 0.0);
         } else {
-            double tempi = pow(((ss + zwtmm - zimm[j]) / ss), 1.0 - 1.0 / bb);
-            double temp0 = pow(((ss + zwtmm - zimm[j - 1]) / ss), 1.0 - 1.0 / bb);
             veq = -ss * ws / (1.0 - 1.0 / bb) / (zimm[j] - zimm[j - 1]) * (tempi - temp0);
             veq = fmax(veq, 0.0);
             veq = fmin(ws, veq);
@@ -113,7 +149,7 @@ __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, d
         double s1 = 0.5 * (vwc_liq[j] + vwc_liq[jp]) / (0.5 * (wsj + wsp));
         s1 = fmin(1.0, s1);
         double s2 = G(io.hksat, j) * pow(s1, 2.0 * bb + 2.0);
-        imped[j] = pow(10.0, -e_ice * (0.5 * (icef[j] + icef[jp])));
+        imped[j] = pow10_dd(-e_ice * (0.5 * (icef[j] + icef[jp])));
         hk[j] = imped[j] * s1 * s2;
         dhkdw[j] = imped[j] * (2.0 * bb + 3.0) * s2 * (1.0 / (wsj + wsp));
         double s_node = fmax(vwc_liq[j] / wsj, 0.01);
@@ -298,17 +334,22 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
         double t;
         if (j >= 1) {
             const double liq = LIQ[ssi(j)], ice = ICE[ssi(j)], dzj = DZ(j), ws = io.watsat[gi(j)];
-            double satw = (liq / DENH2O + ice / DENICE + 0.0 / DENICE) / (dzj * ws);
-            satw = fmin(1.0, satw);
-            if (satw > .1e-6) {
-                double dke = (T[ssi(j)] >= TFRZ) ? fmax(0.0, log10(satw) + 1.0) : satw;
-                double fl = (liq / (DENH2O * dzj)) / (liq / (DENH2O * dzj) + ice / (DENICE * dzj) + 0.0 / (DENICE * dzj));
-                double dksat = io.tkmg[gi(j)] * pow(TKWAT, fl * ws) * pow(TKICE, (1.0 - fl) * ws);
-                t = dke * dksat + (1.0 - dke) * io.tkdry[gi(j)];
+            if (j > nbedrock) {
+                // the reference evaluates the soil formula here too and then
+                // overwrites it with thk_bedrock (:710-725); the value is unused
+                t = THK_BEDROCK;
             } else {
-                t = io.tkdry[gi(j)];
+                double satw = (liq / DENH2O + ice / DENICE + 0.0 / DENICE) / (dzj * ws);
+                satw = fmin(1.0, satw);
+                if (satw > .1e-6) {
+                    double dke = (T[ssi(j)] >= TFRZ) ? fmax(0.0, log10(satw) + 1.0) : satw;
+                    double fl = (liq / (DENH2O * dzj)) / (liq / (DENH2O * dzj) + ice / (DENICE * dzj) + 0.0 / (DENICE * dzj));
+                    double dksat = io.tkmg[gi(j)] * tkwat_tkice_pow(fl * ws, (1.0 - fl) * ws);
+                    t = dke * dksat + (1.0 - dke) * io.tkdry[gi(j)];
+                } else {
+                    t = io.tkdry[gi(j)];
+                }
             }
-            if (j > nbedrock) t = THK_BEDROCK;
             double cv = io.csol[gi(j)] * (1.0 - ws) * dzj + (ice * CPICE + liq * CPLIQ) + 0.0 * CPICE;
             if (j > nbedrock) cv = CSOL_BEDROCK * dzj;
             if (j == 1 && io.h2osno_no_layers[c] > 0.0) cv = cv + CPICE * io.h2osno_no_layers[c];
@@ -1059,5 +1100,36 @@ extern "C" int32_t ctsmg_soiltemperature_noalloc(const ctsmg_bounds* bounds, int
         return set_error(code, code == CTSMG_E_SINGULAR ? "BandDiagonal ERROR: dgbsv returned error code"
                                                         : "filter or patch index outside the bounds", idx, lev);
     }
+    return 0;
+}
+
+// ---------------------------------------------------------------- diagnostic
+namespace ctsmg {
+__global__ void diag_powers_kernel(int n, const double* __restrict__ a, const double* __restrict__ b,
+                                   double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = pow(10.0, a[i]);
+    out[n + i] = pow10_dd(a[i]);
+    out[2 * (size_t)n + i] = pow(TKWAT, a[i]) * pow(TKICE, b[i]);
+    out[3 * (size_t)n + i] = tkwat_tkice_pow(a[i], b[i]);
+}
+} // namespace ctsmg
+
+extern "C" int32_t ctsmg_diag_powers(int32_t n, const double* a, const double* b, double* out) {
+    using namespace ctsmg;
+    if (n <= 0 || !a || !b || !out) return set_error(CTSMG_E_ARG, "bad arguments", 0, 0);
+    double* d = nullptr;
+    const size_t nb = (size_t)n * 8;
+    cudaError_t e = cudaMalloc(&d, 6 * nb);
+    if (e == cudaSuccess) e = cudaMemcpy(d, a, nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d + n, b, nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        diag_powers_kernel<<<(n + 127) / 128, 128>>>(n, d, d + n, d + 2 * (size_t)n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * (size_t)n, 4 * nb, cudaMemcpyDeviceToHost);
+    if (d) cudaFree(d);
+    if (e != cudaSuccess) return set_error(CTSMG_E_CUDA, cudaGetErrorString(e), 0, 0);
     return 0;
 }

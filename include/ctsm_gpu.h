@@ -476,6 +476,11 @@ int32_t ctsmg_pool_destroy(ctsmg_pool p);
 /* FP64 FMA throughput of the current GPU in TFLOP/s (a DFMA loop over every
  * SM); the denominator of the FP64 roofline fraction.  No reference counterpart. */
 int32_t ctsmg_measure_fp64_tflops(double* tflops);
+/* Diagnostic for the tests (no reference counterpart): for each i, out[i] =
+ * pow(10, a[i]) and out[n+i] = the soil step's exp form of it; out[2n+i] =
+ * pow(tkwat, a[i]) * pow(tkice, b[i]) and out[3n+i] = the exp form of that
+ * product.  Host arrays; out holds 4n doubles. */
+int32_t ctsmg_diag_powers(int32_t n, const double* a, const double* b, double* out);
 
 #ifdef __cplusplus
 }
