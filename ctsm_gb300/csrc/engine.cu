@@ -158,13 +158,17 @@ extern "C" int32_t ctsmg_batch_create2(ctsmg_batch* out, const ctsmg_batch_confi
     if ((e = cudaEventCreate(&b->ev0)) != cudaSuccess) return fail(cuda_err(e, "event"));
     if ((e = cudaEventCreate(&b->ev1)) != cudaSuccess) return fail(cuda_err(e, "event"));
 
-    // bucket columns: more snow layers first, then shallower bedrock
+    // bucket columns: more snow layers first, then shallower bedrock, then a
+    // shallower water table (the water-table position selects the branches
+    // of the equilibrium profile and recharge in SoilWater); only the order
+    // in which threads take columns changes
     std::vector<int32_t> perm(ncol), inv(ncol);
     std::iota(perm.begin(), perm.end(), 0);
     if (cfg->bucket && !canopy_only)
         std::stable_sort(perm.begin(), perm.end(), [&](int a, int c) {
             if (st->snl[a] != st->snl[c]) return st->snl[a] < st->snl[c];
-            return st->nbedrock[a] < st->nbedrock[c];
+            if (st->nbedrock[a] != st->nbedrock[c]) return st->nbedrock[a] < st->nbedrock[c];
+            return sw->zwt[a] < sw->zwt[c];
         });
     for (int i = 0; i < ncol; ++i) inv[perm[i]] = i;
     if ((e = cudaMalloc(&b->d_perm, (size_t)ncol * 4)) != cudaSuccess) return fail(cuda_err(e, "perm"));

@@ -89,7 +89,7 @@ struct Pool {
     int32_t* h_cfilt = nullptr;               // pinned staging of the filters
     int32_t* h_pfilt = nullptr;
     cudaEvent_t filt_ev = nullptr;            // last filter upload
-    std::vector<uint16_t> key;                // per column position: bucket key
+    std::vector<uint16_t> key;                // per column position: bucket key (snl, nbedrock, jwt)
     int ncol_act = 0, npat_act = 0;
     bool dirty = true;
     RangeAlloc cols, pats, grids;
@@ -170,7 +170,7 @@ static cudaError_t enqueue_tick(Pool* P) {
 // patches in position order), uploaded in stream order, and the tick graph.
 static int rebuild(Pool* P) {
     PK(cudaEventSynchronize(P->filt_ev), "filter staging");
-    const int NKEY = 1 << 10;
+    const int NKEY = 1 << 14;
     std::vector<int> cnt(NKEY + 1, 0);
     int nc = 0, np = 0;
     for (auto& r : P->req) {
@@ -418,7 +418,12 @@ extern "C" int32_t ctsmg_pool_admit(ctsmg_pool ph, int32_t ncol, int32_t npatch,
     if (e == cudaSuccess) e = se;
     if (e != cudaSuccess) { release(); return e == cudaErrorInvalidValue ? set_error(CTSMG_E_ARG, "null component", 0, 0)
                                                                           : pcuda(e, "admit copy"); }
-    for (int c = 0; c < ncol; ++c) P->key[r.c0 + c] = (uint16_t)((st->snl[c] + NLEVSNO) * 32 + st->nbedrock[c]);
+    for (int c = 0; c < ncol; ++c) {             // jwt: layers above the water table (:638-647)
+        int jwt = NLEVSOI;
+        for (int j = 1; j <= NLEVSOI; ++j)
+            if (sw->zwt[c] <= sw->zi[c + (size_t)(j + NLEVSNO) * ncol]) { jwt = j - 1; break; }
+        P->key[r.c0 + c] = (uint16_t)(((st->snl[c] + NLEVSNO) * 32 + st->nbedrock[c]) * 32 + jwt);
+    }
     int slot = -1;
     for (size_t i = 0; i < P->req.size(); ++i) if (P->req[i].state == R_FREE) { slot = (int)i; break; }
     if (slot < 0) { slot = (int)P->req.size(); P->req.emplace_back(); }
