@@ -19,9 +19,9 @@ Extra keys on the same line (rank 0, N = 1):
   ensemble  256 perturbed-parameter members (columns U{512..8192} each) through
             the full soil + canopy step, batched vs one set of plain drop-in
             calls per member
-  serving   a Poisson stream of run requests (columns log-uniform 1..50,000,
-            lengths U{48..17,520} steps) through the device pool with a 150 GB
-            admission budget, bounded in wall time
+  serving   a Poisson stream of run requests (192 at 8/s; columns log-uniform
+            1..50,000, lengths U{48..17,520} steps) through the device pool
+            with a 150 GB admission budget, bounded in wall time
 Under torchrun each rank advances its own 524,288-column shard (no
 collective on the data path; weak scaling); time is the max over ranks.
 """
@@ -63,8 +63,8 @@ def parse():
     p.add_argument("--canopy-steps", type=int, default=8)
     p.add_argument("--ens-members", type=int, default=256)
     p.add_argument("--ens-steps", type=int, default=48)
-    p.add_argument("--serve-requests", type=int, default=64)
-    p.add_argument("--serve-rate", type=float, default=2.0)
+    p.add_argument("--serve-requests", type=int, default=192)
+    p.add_argument("--serve-rate", type=float, default=8.0)
     p.add_argument("--serve-seconds", type=float, default=60.0)
     p.add_argument("--serve-budget-gb", type=float, default=150.0)
     return p.parse_args()
@@ -231,7 +231,8 @@ def canopy_leg(args, barrier):
            "patch_steps_per_s": npatch / (mean_ms * 1e-3), "mean_passes": passes,
            "gpu_launches_per_step": 4,
            "fp64": {"achieved": flops / (mean_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
-                    "flops_per_pass": roofline.CANOPY_FLOPS_PER_PASS}}
+                    "flops_per_pass": roofline.CANOPY_FLOPS_PER_PASS},
+           "traffic_bytes_per_patch_step": roofline.CANOPY_TRAFFIC_PER_PATCH_STEP}
     if not args.no_e2e:
         H = {}
         for k, v in A0.items():

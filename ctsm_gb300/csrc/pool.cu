@@ -68,6 +68,7 @@ struct Request {
     int c0 = 0, nc = 0, p0 = 0, np = 0, g0 = 0, ng = 0;
     int nsteps = 0, enq = 0;
     cudaEvent_t done = nullptr;               // recorded after its last enqueued step
+    std::vector<int32_t> perm;                // pool position c0 + i holds the request's column perm[i]
 };
 
 struct Pool {
@@ -89,7 +90,6 @@ struct Pool {
     int32_t* h_cfilt = nullptr;               // pinned staging of the filters
     int32_t* h_pfilt = nullptr;
     cudaEvent_t filt_ev = nullptr;            // last filter upload
-    std::vector<uint16_t> key;                // per column position: bucket key (snl, nbedrock, jwt)
     int ncol_act = 0, npat_act = 0;
     bool dirty = true;
     RangeAlloc cols, pats, grids;
@@ -144,7 +144,7 @@ static void add_slot_bytes(const FieldDesc& f, void* ctx) {
 static void slot_bytes(int with_canopy, int64_t* cb, int64_t* pb, int64_t* gb) {
     SlotBytes s;
     for_tables(with_canopy, add_slot_bytes, &s);
-    s.c += (int64_t)SOILTEMP_WS_DOUBLES_PER_COL * 8 + 4 + 2;        // band scratch, filter entry, host key
+    s.c += (int64_t)SOILTEMP_WS_DOUBLES_PER_COL * 8 + 4;            // band scratch, filter entry
     if (with_canopy)       // rootr, Medlyn slope/intercept, filter, iteration record
         s.p += (int64_t)NLEVSOI * 8 + 2 * 8 + 4 + (int64_t)canopy_ws_bytes_per_patch();
     else s.p += 4;
@@ -166,23 +166,19 @@ static cudaError_t enqueue_tick(Pool* P) {
                            P->cfg.col_capacity, P->err, P->stream, P->block, P->cfg.with_canopy ? 1 : 0, P->d_cfilt);
 }
 
-// Filters of the running requests (columns counting-sorted by bucket key,
-// patches in position order), uploaded in stream order, and the tick graph.
+// Filters of the running requests in pool-position order (each request's
+// columns sit in its range sorted by (snl, nbedrock, water-table depth), so
+// consecutive threads read consecutive columns of the same bucket), uploaded
+// in stream order, and the tick graph.
 static int rebuild(Pool* P) {
     PK(cudaEventSynchronize(P->filt_ev), "filter staging");
-    const int NKEY = 1 << 14;
-    std::vector<int> cnt(NKEY + 1, 0);
+    std::vector<const Request*> run;
+    for (auto& r : P->req) if (r.state == R_RUNNING) run.push_back(&r);
+    std::sort(run.begin(), run.end(), [](const Request* a, const Request* b) { return a->c0 < b->c0; });
     int nc = 0, np = 0;
-    for (auto& r : P->req) {
-        if (r.state != R_RUNNING) continue;
-        for (int c = r.c0; c < r.c0 + r.nc; ++c) cnt[P->key[c] + 1]++;
-        for (int p = r.p0; p < r.p0 + r.np; ++p) P->h_pfilt[np++] = p + 1;
-        nc += r.nc;
-    }
-    for (int k = 0; k < NKEY; ++k) cnt[k + 1] += cnt[k];
-    for (auto& r : P->req) {
-        if (r.state != R_RUNNING) continue;
-        for (int c = r.c0; c < r.c0 + r.nc; ++c) P->h_cfilt[cnt[P->key[c]]++] = c + 1;
+    for (const Request* r : run) {
+        for (int c = r->c0; c < r->c0 + r->nc; ++c) P->h_cfilt[nc++] = c + 1;
+        for (int p = r->p0; p < r->p0 + r->np; ++p) P->h_pfilt[np++] = p + 1;
     }
     P->ncol_act = nc;
     P->npat_act = np;
@@ -328,7 +324,6 @@ extern "C" int32_t ctsmg_pool_create(ctsmg_pool* out, const ctsmg_pool_config* c
     if ((e = cudaMalloc(&P->d_pfilt, (size_t)PC * 4)) != cudaSuccess) return fail(pcuda(e, "filter"));
     if ((e = cudaHostAlloc(&P->h_pfilt, (size_t)PC * 4, cudaHostAllocDefault)) != cudaSuccess) return fail(pcuda(e, "filter"));
     if ((e = cudaEventRecord(P->filt_ev, P->stream)) != cudaSuccess) return fail(pcuda(e, "event"));
-    P->key.assign(CC, 0);
     P->cols.init(CC);
     P->pats.init(PC);
     P->grids.init(GC);
@@ -374,16 +369,30 @@ extern "C" int32_t ctsmg_pool_admit(ctsmg_pool ph, int32_t ncol, int32_t npatch,
     }
     r.nc = ncol; r.np = npatch; r.ng = ngrid; r.nsteps = nsteps; r.enq = 0;
     auto release = [&]() { P->cols.give(r.c0, r.nc); P->pats.give(r.p0, r.np); P->grids.give(r.g0, r.ng); };
+    // the request's columns in bucket order: more snow layers, shallower
+    // bedrock, shallower water table (the batch engine's order)
+    r.perm.resize(ncol);
+    std::vector<int32_t> inv(ncol);
+    for (int i = 0; i < ncol; ++i) r.perm[i] = i;
+    std::stable_sort(r.perm.begin(), r.perm.end(), [&](int a, int b) {
+        if (st->snl[a] != st->snl[b]) return st->snl[a] < st->snl[b];
+        if (st->nbedrock[a] != st->nbedrock[b]) return st->nbedrock[a] < st->nbedrock[b];
+        return sw->zwt[a] < sw->zwt[b];
+    });
+    bool identity = true;
+    for (int i = 0; i < ncol; ++i) { inv[r.perm[i]] = i; identity = identity && r.perm[i] == i; }
+    if (identity) r.perm.clear();
     // index components rebased to the pool positions
-    std::vector<int32_t> patchi(st->col_patchi, st->col_patchi + ncol), pcol, pgrid;
-    for (auto& v : patchi) v += r.p0;
+    std::vector<int32_t> patchi(ncol), pcol, pgrid;
+    for (int i = 0; i < ncol; ++i) patchi[i] = st->col_patchi[identity ? i : r.perm[i]] + r.p0;
     if (can) {
-        pcol.assign(cio->patch_column, cio->patch_column + npatch);
+        pcol.resize(npatch);
         pgrid.assign(cio->patch_gridcell, cio->patch_gridcell + npatch);
-        for (auto& v : pcol) v += r.c0;
+        for (int p = 0; p < npatch; ++p) pcol[p] = inv[cio->patch_column[p] - 1] + 1 + r.c0;
         for (auto& v : pgrid) v += r.g0;
     }
     std::vector<double> ms, mi;
+    std::vector<char> gathered;
     auto upload = [&](const FieldDesc* tab, int nf, const void* hio) -> cudaError_t {
         for (int i = 0; i < nf; ++i) {
             const FieldDesc& f = tab[i];
@@ -393,7 +402,17 @@ extern "C" int32_t ctsmg_pool_admit(ctsmg_pool ph, int32_t ncol, int32_t npatch,
             if (u.name == "col_patchi") hp = patchi.data();
             else if (u.name == "patch_column") hp = pcol.data();
             else if (u.name == "patch_gridcell") hp = pgrid.data();
+            else if (!identity && !patch_kind(u.kind) && u.kind != K_GR) {
+                const int lev = kind_levels(u.kind), es = u.esize;
+                gathered.resize((size_t)lev * ncol * es);
+                const char* src = static_cast<const char*>(hp);
+                for (int l = 0; l < lev; ++l)
+                    for (int c = 0; c < ncol; ++c)
+                        std::memcpy(&gathered[((size_t)l * ncol + c) * es], src + ((size_t)l * ncol + r.perm[c]) * es, es);
+                hp = gathered.data();
+            }
             cudaError_t ee = copy_field(P, u, r, const_cast<void*>(hp), true);
+            if (ee == cudaSuccess && hp == gathered.data()) ee = cudaStreamSynchronize(P->copy);   // buffer reused
             if (ee != cudaSuccess) return ee;
         }
         return cudaSuccess;
@@ -418,12 +437,6 @@ extern "C" int32_t ctsmg_pool_admit(ctsmg_pool ph, int32_t ncol, int32_t npatch,
     if (e == cudaSuccess) e = se;
     if (e != cudaSuccess) { release(); return e == cudaErrorInvalidValue ? set_error(CTSMG_E_ARG, "null component", 0, 0)
                                                                           : pcuda(e, "admit copy"); }
-    for (int c = 0; c < ncol; ++c) {             // jwt: layers above the water table (:638-647)
-        int jwt = NLEVSOI;
-        for (int j = 1; j <= NLEVSOI; ++j)
-            if (sw->zwt[c] <= sw->zi[c + (size_t)(j + NLEVSNO) * ncol]) { jwt = j - 1; break; }
-        P->key[r.c0 + c] = (uint16_t)(((st->snl[c] + NLEVSNO) * 32 + st->nbedrock[c]) * 32 + jwt);
-    }
     int slot = -1;
     for (size_t i = 0; i < P->req.size(); ++i) if (P->req[i].state == R_FREE) { slot = (int)i; break; }
     if (slot < 0) { slot = (int)P->req.size(); P->req.emplace_back(); }
@@ -496,12 +509,26 @@ extern "C" int32_t ctsmg_pool_evict(ctsmg_pool ph, int32_t slot, const ctsmg_soi
         P->dirty = true;
     }
     PK(cudaStreamWaitEvent(P->copy, r.done, 0), "evict wait");
+    std::vector<char> staged;
     auto download = [&](const FieldDesc* tab, int nf, const void* hio) -> cudaError_t {
         for (int i = 0; i < nf; ++i) {
             const FieldDesc& f = tab[i];
             void* hp = fptr(hio, f);
             const PField& u = P->fields[P->index[f.name]];
             if (!hp || (u.use == U_IN && u.name != "h2osoi_vol" && u.name != "qflx_rootsoi")) continue;
+            if (!r.perm.empty() && !patch_kind(u.kind) && u.kind != K_GR) {
+                // back to the request's column order
+                const int lev = kind_levels(u.kind), es = u.esize, nc = r.nc;
+                staged.resize((size_t)lev * nc * es);
+                cudaError_t ee = copy_field(P, u, r, staged.data(), false);
+                if (ee == cudaSuccess) ee = cudaStreamSynchronize(P->copy);
+                if (ee != cudaSuccess) return ee;
+                char* dst = static_cast<char*>(hp);
+                for (int l = 0; l < lev; ++l)
+                    for (int c = 0; c < nc; ++c)
+                        std::memcpy(dst + ((size_t)l * nc + r.perm[c]) * es, &staged[((size_t)l * nc + c) * es], es);
+                continue;
+            }
             cudaError_t ee = copy_field(P, u, r, hp, false);
             if (ee != cudaSuccess) return ee;
         }
@@ -537,7 +564,13 @@ extern "C" int32_t ctsmg_pool_sync(ctsmg_pool ph) {
         const Request& r = P->req[i];
         if (r.state == R_FREE) continue;
         const int s0 = col ? r.c0 : r.p0, n = col ? r.nc : r.np;
-        if (pos >= s0 && pos < s0 + n) { slot = (int)i; local = pos - s0 + 1; break; }
+        if (pos >= s0 && pos < s0 + n) {
+            slot = (int)i;
+            local = pos - s0;
+            if (col && !r.perm.empty()) local = r.perm[local];
+            local = local + 1;
+            break;
+        }
     }
     return set_error(code, col ? "BandDiagonal ERROR: dgbsv returned error code" : "CanopyFluxes error", slot, local);
 }

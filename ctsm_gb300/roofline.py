@@ -8,15 +8,19 @@ NLEVSNO, NLEVSOI, NLEVGRND = abi.NLEVSNO, abi.NLEVSOI, abi.NLEVGRND
 
 # FP64 floating-point operations per column-step of soilstep_kernel on the
 # uneven-column workload (DADD + DMUL + 2 x DFMA executed, libm included),
-# and DRAM bytes per column-step, from the ncu capture of 65,536 columns of
-# the same workload summarised in profiles/soilstep_kernel_uneven_columns.md.
-FLOPS_PER_COLUMN_STEP = (424136267 + 219978292 + 2 * 961139171) / 65536.0
-TRAFFIC_PER_COLUMN_STEP = (733.809408e6 + 492.769792e6) / 65536.0
+# from the ncu capture of 65,536 columns of the same workload, and DRAM bytes
+# per column-step from the 1-pass capture of the full 524,288-column launch;
+# both summarised in profiles/soilstep_kernel_uneven_columns.md.
+FLOPS_PER_COLUMN_STEP = (302494944 + 180903465 + 2 * 779430043) / 65536.0
+TRAFFIC_PER_COLUMN_STEP = (6585233152 + 4161359616) / 524288.0
 
 # FP64 floating-point operations per CanopyFluxes pass of one patch
 # (canopy_iterate_kernel: DADD + DMUL + 2 x DFMA executed over 262,144 patches
-# of the canopy workload, 6.266 passes per patch on average).
+# of the canopy workload, 6.266 passes per patch on average), and DRAM bytes
+# per patch-step of that kernel from the 1-pass capture of the full
+# 2,097,152-patch launch (profiles/canopy_iterate_kernel_canopy_workload.md).
 CANOPY_FLOPS_PER_PASS = (739121234 + 1058410707 + 2 * 3057904378) / (262144 * 6.266)
+CANOPY_TRAFFIC_PER_PATCH_STEP = (41889384704 + 15773437184) / 2097152.0
 
 
 def _active_levels(kind, nsnow):

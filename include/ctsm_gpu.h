@@ -418,8 +418,9 @@ int32_t ctsmg_batch_destroy(ctsmg_batch b);
  * same step as a batch with with_canopy (CanopyFluxes, root sink,
  * SoilTemperature, SoilWater, h2osoi_vol refresh) or, with_canopy = 0,
  * SoilWater then SoilTemperature -- through one CUDA graph whose kernels run
- * over filters of the active slots (1-based positions, sorted by (snl,
- * nbedrock)).  Columns never interact, so a request's results do not depend
+ * over filters of the active slots (1-based positions; each request's
+ * columns are stored sorted by (snl, nbedrock, water-table depth) and are
+ * returned in the caller's order).  Columns never interact, so a request's results do not depend
  * on what else is in the pool.  Calls on one pool must come from one host
  * thread at a time. */
 typedef struct ctsmg_pool_s* ctsmg_pool;

@@ -25,7 +25,7 @@ def test_slot_bytes_match_manifest():
             gb += b
         else:
             cb += b
-    assert c == cb + 6 * 38 * 8 + 4 + 2
+    assert c == cb + 6 * 38 * 8 + 4
     rec = p - (pb + 20 * 8 + 16 + 4)          # rootr, Medlyn pair, filter entry, CanopyFluxes iteration record
     assert rec % 4 == 0 and 0 < rec < 2048
     assert g == gb
