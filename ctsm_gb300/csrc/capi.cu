@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <algorithm>
 #include <string>
 #include <vector>
 #include "ctsm_gpu.h"
@@ -28,8 +29,13 @@ static ctsmg_pftcon g_pft;
 static bool g_cpar_set = false;
 
 // ------------------------------------------------------------ per-thread context
+constexpr int PIPE_CHUNKS = 8;           // chunks of a pipelined drop-in call
+constexpr int PIPE_MIN_COLUMNS = 32768;  // smaller calls run in one piece
+
 struct ThreadCtx {
     cudaStream_t stream = nullptr;
+    cudaStream_t h2d = nullptr, d2h = nullptr;      // copy streams of the pipelined calls
+    cudaEvent_t ev_in[PIPE_CHUNKS] = {}, ev_done[PIPE_CHUNKS] = {};
     char* arena = nullptr;
     size_t arena_cap = 0, arena_top = 0;
     DevError* err = nullptr;
@@ -38,6 +44,12 @@ struct ThreadCtx {
     ~ThreadCtx() {
         if (arena) cudaFree(arena);
         if (err) cudaFree(err);
+        for (int k = 0; k < PIPE_CHUNKS; ++k) {
+            if (ev_in[k]) cudaEventDestroy(ev_in[k]);
+            if (ev_done[k]) cudaEventDestroy(ev_done[k]);
+        }
+        if (h2d) cudaStreamDestroy(h2d);
+        if (d2h) cudaStreamDestroy(d2h);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -72,6 +84,16 @@ static int ctx_get(ThreadCtx** out) {
         if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaStreamCreate"); }
         e = cudaMalloc(&c->err, sizeof(DevError));
         if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaMalloc(err)"); }
+        if ((e = cudaStreamCreateWithFlags(&c->h2d, cudaStreamNonBlocking)) != cudaSuccess ||
+            (e = cudaStreamCreateWithFlags(&c->d2h, cudaStreamNonBlocking)) != cudaSuccess) {
+            delete c;
+            return cuda_fail(e, "cudaStreamCreate");
+        }
+        for (int k = 0; k < PIPE_CHUNKS && e == cudaSuccess; ++k) {
+            e = cudaEventCreateWithFlags(&c->ev_in[k], cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_done[k], cudaEventDisableTiming);
+        }
+        if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaEventCreate"); }
         t_ctx = c;
         std::lock_guard<std::mutex> lk(g_mu);
         t_gen = g_gen;
@@ -335,6 +357,94 @@ int check_filter(const ctsmg_bounds* b, int nf, const int32_t* filt) {
     return 0;
 }
 
+// ------------------------------------------------------------ pipelined calls
+// A call over an ascending filter is split into chunks of the filter; chunk k
+// copies the column range (and patch range) its filter entries span, its
+// kernel runs once those copies are in, and its outputs go back while later
+// chunks copy in and compute.  Columns of a range that are not in the filter
+// travel in and out unchanged.  Chunks whose patch ranges would overlap (a
+// patch order that does not follow the columns) run the call in one piece.
+struct Chunk { int f0, f1, c0, c1, p0, p1; };
+
+static bool plan_chunks(const ctsmg_bounds* b, int num, const int32_t* filt, const int32_t* col_patchi,
+                        const int32_t* col_npatches, std::vector<Chunk>& out) {
+    if (num < PIPE_MIN_COLUMNS || !filt) return false;
+    for (int i = 1; i < num; ++i)
+        if (filt[i] <= filt[i - 1]) return false;
+    out.clear();
+    for (int k = 0; k < PIPE_CHUNKS; ++k) {
+        Chunk ch;
+        ch.f0 = (int)((long long)num * k / PIPE_CHUNKS);
+        ch.f1 = (int)((long long)num * (k + 1) / PIPE_CHUNKS);
+        if (ch.f1 <= ch.f0) continue;
+        ch.c0 = filt[ch.f0] - b->begc;
+        ch.c1 = filt[ch.f1 - 1] - b->begc + 1;
+        ch.p0 = ch.p1 = 0;
+        if (col_patchi) {
+            int lo = 1 << 30, hi = -1;
+            for (int c = ch.c0; c < ch.c1; ++c) {
+                if (col_npatches[c] <= 0) continue;
+                lo = std::min(lo, col_patchi[c] - b->begp);
+                hi = std::max(hi, col_patchi[c] + col_npatches[c] - 1 - b->begp);
+            }
+            if (hi >= lo) { ch.p0 = lo; ch.p1 = hi + 1; }
+            if (!out.empty() && ch.p1 > ch.p0 && out.back().p1 > out.back().p0 && ch.p0 < out.back().p1) return false;
+        }
+        out.push_back(ch);
+    }
+    return out.size() > 1;
+}
+
+// Strided copy of the [lo, hi) column (or patch) slice of every level of one
+// field between the caller's array and its device copy (both with ld).
+static cudaError_t copy_slice(const FieldDesc& f, void* dst, const void* src, int ld, int lo, int hi,
+                              cudaMemcpyKind kind, cudaStream_t s) {
+    if (hi <= lo) return cudaSuccess;
+    const size_t es = f.esize, pitch = (size_t)ld * es, w = (size_t)(hi - lo) * es;
+    return cudaMemcpy2DAsync(static_cast<char*>(dst) + lo * es, pitch, static_cast<const char*>(src) + lo * es, pitch,
+                             w, kind_levels(f.kind), kind, s);
+}
+
+static bool patch_field(const FieldDesc& f) { return f.kind == K_P || f.kind == K_PL || f.kind == K_PS; }
+
+// Device copies of every component (arena), no data moved yet.
+static void stage_alloc(ThreadCtx* c, const void* hio, void* dio, size_t io_size, const FieldDesc* tab, int nf,
+                        int ldc, int ldp) {
+    std::memcpy(dio, hio, io_size);
+    for (int i = 0; i < nf; ++i) field_ptr(dio, tab[i]) = arena_take(c, field_bytes(tab[i], ldc, ldp, 0));
+}
+
+// Enqueue the copy-in of chunk k (h2d stream) and record ev_in[k].
+static int chunk_in(ThreadCtx* c, const Chunk& ch, int k, const void* hio, const void* dio, const FieldDesc* tab,
+                    int nf, int ldc, int ldp) {
+    for (int i = 0; i < nf; ++i) {
+        const FieldDesc& f = tab[i];
+        const bool pf = patch_field(f);
+        cudaError_t e = copy_slice(f, field_ptr(const_cast<void*>(dio), f), field_ptr(const_cast<void*>(hio), f),
+                                   pf ? ldp : ldc, pf ? ch.p0 : ch.c0, pf ? ch.p1 : ch.c1, cudaMemcpyHostToDevice,
+                                   c->h2d);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy2DAsync H2D");
+    }
+    cudaError_t e = cudaEventRecord(c->ev_in[k], c->h2d);
+    return e == cudaSuccess ? 0 : cuda_fail(e, "cudaEventRecord");
+}
+
+// After the kernel of chunk k (ev_done[k]), enqueue its copy-out (d2h stream).
+static int chunk_out(ThreadCtx* c, const Chunk& ch, int k, const void* hio, const void* dio, const FieldDesc* tab,
+                     int nf, int ldc, int ldp) {
+    cudaError_t e = cudaStreamWaitEvent(c->d2h, c->ev_done[k], 0);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamWaitEvent");
+    for (int i = 0; i < nf; ++i) {
+        const FieldDesc& f = tab[i];
+        if (f.use == U_IN) continue;
+        const bool pf = patch_field(f);
+        e = copy_slice(f, field_ptr(const_cast<void*>(hio), f), field_ptr(const_cast<void*>(dio), f), pf ? ldp : ldc,
+                       pf ? ch.p0 : ch.c0, pf ? ch.p1 : ch.c1, cudaMemcpyDeviceToHost, c->d2h);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy2DAsync D2H");
+    }
+    return 0;
+}
+
 static int read_error(ThreadCtx* c, int* code, int* index, int* level) {
     DevError h;
     cudaError_t e = cudaMemcpy(&h, c->err, sizeof h, cudaMemcpyDeviceToHost);
@@ -415,6 +525,32 @@ extern "C" int32_t ctsmg_soilwater(const ctsmg_bounds* bounds, int32_t num_hydro
     const int ldc = io->ldc;
     size_t need = table_bytes(SOILWATER_TABLE, SOILWATER_NFIELDS, ldc, 0) + (size_t)num_hydrologyc * 4 + 4096;
     if ((rc = arena_reserve(c, need))) return rc;
+    double e_ice_p;
+    { std::lock_guard<std::mutex> lk(g_mu); e_ice_p = g_swp.e_ice; }
+    std::vector<Chunk> chunks;
+    if (plan_chunks(bounds, num_hydrologyc, filter_hydrologyc, nullptr, nullptr, chunks)) {
+        ctsmg_soilwater_io dio;
+        stage_alloc(c, io, &dio, sizeof dio, SOILWATER_TABLE, SOILWATER_NFIELDS, ldc, 0);
+        int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_hydrologyc * 4);
+        cudaError_t e = cudaMemcpyAsync(dfilt, filter_hydrologyc, (size_t)num_hydrologyc * 4, cudaMemcpyHostToDevice,
+                                        c->h2d);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
+        const int K = (int)chunks.size();
+        if ((rc = chunk_in(c, chunks[0], 0, io, &dio, SOILWATER_TABLE, SOILWATER_NFIELDS, ldc, 0))) return rc;
+        for (int k = 0; k < K; ++k) {
+            const Chunk& ch = chunks[k];
+            if ((e = cudaStreamWaitEvent(c->stream, c->ev_in[k], 0)) != cudaSuccess) return cuda_fail(e, "wait");
+            e = launch_soilwater(dio, bounds->begc, ch.f1 - ch.f0, dfilt + ch.f0, e_ice_p, dtime, c->stream);
+            if (e != cudaSuccess) return cuda_fail(e, "soilwater kernel launch");
+            if ((e = cudaEventRecord(c->ev_done[k], c->stream)) != cudaSuccess) return cuda_fail(e, "record");
+            if (k + 1 < K && (rc = chunk_in(c, chunks[k + 1], k + 1, io, &dio, SOILWATER_TABLE, SOILWATER_NFIELDS, ldc, 0)))
+                return rc;
+            if ((rc = chunk_out(c, ch, k, io, &dio, SOILWATER_TABLE, SOILWATER_NFIELDS, ldc, 0))) return rc;
+        }
+        if ((e = cudaStreamSynchronize(c->d2h)) != cudaSuccess) return cuda_fail(e, "soilwater");
+        if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return cuda_fail(e, "soilwater");
+        return 0;
+    }
     ctsmg_soilwater_io dio;
     if ((rc = stage_in(c, io, &dio, sizeof dio, SOILWATER_TABLE, SOILWATER_NFIELDS, ldc, 0))) return rc;
     int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_hydrologyc * 4);
@@ -455,6 +591,38 @@ extern "C" int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds, int32_t num
     const size_t ws_bytes = (size_t)SOILTEMP_WS_DOUBLES_PER_COL * num_nolakec * 8;
     size_t need = table_bytes(SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp) + ws_bytes + (size_t)num_nolakec * 4 + 8192;
     if ((rc = arena_reserve(c, need))) return rc;
+    std::vector<Chunk> chunks;
+    if (plan_chunks(bounds, num_nolakec, filter_nolakec, io->col_patchi, io->col_npatches, chunks)) {
+        ctsmg_soiltemp_io dio;
+        stage_alloc(c, io, &dio, sizeof dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp);
+        int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_nolakec * 4);
+        double* ws = (double*)arena_take(c, ws_bytes);
+        cudaError_t e = cudaMemcpyAsync(dfilt, filter_nolakec, (size_t)num_nolakec * 4, cudaMemcpyHostToDevice, c->h2d);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
+        if ((e = cudaMemsetAsync(c->err, 0xff, sizeof(DevError), c->stream)) != cudaSuccess)
+            return cuda_fail(e, "cudaMemsetAsync(err)");
+        int snow_method;
+        { std::lock_guard<std::mutex> lk(g_mu); snow_method = g_opt.snow_thermal_cond_method; }
+        const int K = (int)chunks.size();
+        if ((rc = chunk_in(c, chunks[0], 0, io, &dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp))) return rc;
+        for (int k = 0; k < K; ++k) {
+            const Chunk& ch = chunks[k];
+            if ((e = cudaStreamWaitEvent(c->stream, c->ev_in[k], 0)) != cudaSuccess) return cuda_fail(e, "wait");
+            e = launch_soiltemp(dio, bounds->begc, bounds->begp, ch.f1 - ch.f0, dfilt + ch.f0, dtime, snow_method,
+                                ws + ch.f0, num_nolakec, c->err, c->stream);
+            if (e != cudaSuccess) return cuda_fail(e, "soiltemperature kernel launch");
+            if ((e = cudaEventRecord(c->ev_done[k], c->stream)) != cudaSuccess) return cuda_fail(e, "record");
+            if (k + 1 < K && (rc = chunk_in(c, chunks[k + 1], k + 1, io, &dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp)))
+                return rc;
+            if ((rc = chunk_out(c, ch, k, io, &dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp))) return rc;
+        }
+        if ((e = cudaStreamSynchronize(c->d2h)) != cudaSuccess) return cuda_fail(e, "soiltemperature");
+        if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return cuda_fail(e, "soiltemperature");
+        int code = 0, idx = 0, lev = 0;
+        if ((rc = read_error(c, &code, &idx, &lev))) return rc;
+        if (code) return set_error(code, "BandDiagonal ERROR: dgbsv returned error code", idx, lev);
+        return 0;
+    }
     ctsmg_soiltemp_io dio;
     if ((rc = stage_in(c, io, &dio, sizeof dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp))) return rc;
     int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_nolakec * 4);

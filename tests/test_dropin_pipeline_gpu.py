@@ -1,0 +1,35 @@
+"""Large drop-in calls over an ascending filter run pipelined (chunks of the
+filter copy in, compute and copy out on three streams); other filters run in
+one piece.  Both forms must give bit-identical results, including columns
+that are not in the filter (left as they were)."""
+import copy
+
+import numpy as np
+import pytest
+
+from ctsm_gb300 import abi, inputs, soil
+
+pytestmark = pytest.mark.gpu
+DT = 1800.0
+
+
+def test_pipelined_equals_single_shot(gpu_lib):
+    A, npatch = inputs.soil_columns(40000, seed=71, snow=True, nbedrock=(3, 20), forcing="full", npatch_max=3)
+    ncol = A["zwt"].shape[0]
+    keep = np.arange(1, ncol + 1, dtype=np.int32)
+    keep = keep[(keep % 7) != 3]                 # gaps: every 7th column stays out of the filter
+    asc = np.ascontiguousarray(keep)
+    desc = np.ascontiguousarray(keep[::-1])      # same set, not ascending: one-piece path
+    b = abi.Bounds(1, ncol, 1, npatch)
+    P, S = copy.deepcopy(A), copy.deepcopy(A)
+    soil.SoilWater(b, len(asc), asc, P, DT)
+    soil.SoilTemperature(b, len(asc), asc, P, DT)
+    soil.SoilWater(b, len(desc), desc, S, DT)
+    soil.SoilTemperature(b, len(desc), desc, S, DT)
+    out = [n for (n, k, t, u) in abi.SOILWATER_FIELDS + abi.SOILTEMP_FIELDS]
+    for k in out:
+        np.testing.assert_array_equal(P[k], S[k], err_msg=k)
+    skipped = np.setdiff1d(np.arange(ncol), asc - 1)
+    for k in ("t_soisno", "h2osoi_liq", "qin", "xmf", "eflx_fgr"):
+        np.testing.assert_array_equal(P[k][..., skipped], A[k][..., skipped], err_msg=k)
+    assert not np.array_equal(P["t_soisno"], A["t_soisno"])
