@@ -29,7 +29,10 @@ static ctsmg_pftcon g_pft;
 static bool g_cpar_set = false;
 
 // ------------------------------------------------------------ per-thread context
-constexpr int PIPE_CHUNKS = 8;           // chunks of a pipelined drop-in call
+#ifndef CTSMG_PIPE_CHUNKS
+#define CTSMG_PIPE_CHUNKS 16
+#endif
+constexpr int PIPE_CHUNKS = CTSMG_PIPE_CHUNKS;   // chunks of a pipelined drop-in call
 constexpr int PIPE_MIN_COLUMNS = 32768;  // smaller calls run in one piece
 
 struct ThreadCtx {
