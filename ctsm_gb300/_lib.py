@@ -34,6 +34,8 @@ def load():
     L.ctsmg_last_error_index.argtypes = [P(C.c_int32), P(C.c_int32)]
     L.ctsmg_soilwater.argtypes = [P(abi.Bounds), C.c_int32, P(C.c_int32), P(abi.SoilWaterIO), C.c_double]
     L.ctsmg_soiltemperature.argtypes = [P(abi.Bounds), C.c_int32, P(C.c_int32), P(abi.SoilTempIO), C.c_double]
+    L.ctsmg_soilfluxes.argtypes = [P(abi.Bounds), C.c_int32, P(C.c_int32), C.c_int32, P(C.c_int32),
+                                   P(abi.SoilFluxesIO), C.c_double]
     _LIB = L
     return L
 

@@ -101,6 +101,33 @@ CANOPY_FIELDS = (
     [("num_iter", "P", I32, "out")])
 
 
+# SoilFluxes (src/biogeophys/SoilFluxesMod.F90:36-518), natural-vegetation
+# columns and patches; tssbef / t_h2osfc_bef are the temperatures saved before
+# SoilTemperature.
+SOILFLUXES_FIELDS = [
+    ("snl", "C", I32, "in"), ("col_patchi", "C", I32, "in"), ("col_npatches", "C", I32, "in"),
+    ("frac_sno_eff", "C", F64, "in"), ("frac_h2osfc", "C", F64, "in"), ("t_grnd", "C", F64, "in"),
+    ("t_h2osfc", "C", F64, "in"), ("t_h2osfc_bef", "C", F64, "in"), ("c_h2osfc", "C", F64, "in"),
+    ("emg", "C", F64, "in"), ("forc_lwrad", "C", F64, "in"), ("htvp", "C", F64, "in"),
+    ("xmf", "C", F64, "in"), ("xmf_h2osfc", "C", F64, "in"), ("eflx_h2osfc_to_snow", "C", F64, "in"),
+    ("t_soisno", "SS", F64, "in"), ("tssbef", "SS", F64, "in"), ("fact", "SS", F64, "in"),
+    ("h2osoi_liq", "SS", F64, "in"), ("h2osoi_ice", "SS", F64, "in"),
+    ("errsoi_col", "C", F64, "out"),
+    ("patch_column", "P", I32, "in"), ("frac_veg_nosno", "P", I32, "in"), ("wtcol", "P", F64, "in"),
+    ("cgrnds", "P", F64, "in"), ("cgrndl", "P", F64, "in"), ("sabg_soil", "P", F64, "in"),
+    ("sabg_snow", "P", F64, "in"), ("dlrad", "P", F64, "in"), ("ulrad", "P", F64, "in"),
+    ("eflx_sh_veg", "P", F64, "in"), ("qflx_evap_veg", "P", F64, "in"), ("qflx_tran_veg", "P", F64, "in"),
+    ("eflx_sh_grnd", "P", F64, "inout"), ("qflx_evap_soi", "P", F64, "inout"),
+    ("qflx_ev_snow", "P", F64, "inout"), ("qflx_ev_soil", "P", F64, "inout"), ("qflx_ev_h2osfc", "P", F64, "inout"),
+    ("qflx_liqevap_from_top_layer", "P", F64, "out"), ("qflx_solidevap_from_top_layer", "P", F64, "out"),
+    ("qflx_soliddew_to_top_layer", "P", F64, "out"), ("qflx_liqdew_to_top_layer", "P", F64, "out"),
+    ("eflx_soil_grnd", "P", F64, "out"), ("eflx_sh_tot", "P", F64, "out"), ("qflx_evap_tot", "P", F64, "out"),
+    ("eflx_lh_tot", "P", F64, "out"), ("qflx_evap_can", "P", F64, "out"), ("eflx_lh_vege", "P", F64, "out"),
+    ("eflx_lh_vegt", "P", F64, "out"), ("eflx_lh_grnd", "P", F64, "out"), ("eflx_lwrad_out", "P", F64, "out"),
+    ("eflx_lwrad_net", "P", F64, "out"), ("errsoi_patch", "P", F64, "out"), ("t_skin", "P", F64, "inout"),
+]
+
+
 def _ptr_type(dtype):
     return C.POINTER(C.c_double) if dtype == F64 else C.POINTER(C.c_int32)
 
@@ -121,6 +148,11 @@ class SoilWaterParams(C.Structure):
 
 class SoilWaterIO(C.Structure):
     _fields_ = [("ldc", C.c_int32)] + [(n, _ptr_type(t)) for (n, _, t, _) in SOILWATER_FIELDS]
+
+
+class SoilFluxesIO(C.Structure):
+    _fields_ = [("ldc", C.c_int32), ("ldp", C.c_int32)] + \
+               [(n, _ptr_type(t)) for (n, _, t, _) in SOILFLUXES_FIELDS]
 
 
 class SoilTempIO(C.Structure):

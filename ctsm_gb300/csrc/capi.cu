@@ -15,6 +15,7 @@
 #include "ctsm_device.cuh"
 #include "soil_kernels.cuh"
 #include "canopy_kernels.cuh"
+#include "soilfluxes_kernels.cuh"
 #include "capi_internal.h"
 
 namespace ctsmg {
@@ -181,6 +182,65 @@ const FieldDesc SOILTEMP_TABLE[] = {
 const int SOILTEMP_NFIELDS = sizeof(SOILTEMP_TABLE) / sizeof(SOILTEMP_TABLE[0]);
 
 #define FC(name, kind, esz, use) FW(ctsmg_canopy_io, name, kind, esz, use)
+#define FF(name, kind, esz, use) FW(ctsmg_soilfluxes_io, name, kind, esz, use)
+const FieldDesc SOILFLUXES_TABLE[] = {
+    FF(snl, K_C, 4, U_IN),
+    FF(col_patchi, K_C, 4, U_IN),
+    FF(col_npatches, K_C, 4, U_IN),
+    FF(frac_sno_eff, K_C, 8, U_IN),
+    FF(frac_h2osfc, K_C, 8, U_IN),
+    FF(t_grnd, K_C, 8, U_IN),
+    FF(t_h2osfc, K_C, 8, U_IN),
+    FF(t_h2osfc_bef, K_C, 8, U_IN),
+    FF(c_h2osfc, K_C, 8, U_IN),
+    FF(emg, K_C, 8, U_IN),
+    FF(forc_lwrad, K_C, 8, U_IN),
+    FF(htvp, K_C, 8, U_IN),
+    FF(xmf, K_C, 8, U_IN),
+    FF(xmf_h2osfc, K_C, 8, U_IN),
+    FF(eflx_h2osfc_to_snow, K_C, 8, U_IN),
+    FF(t_soisno, K_SS, 8, U_IN),
+    FF(tssbef, K_SS, 8, U_IN),
+    FF(fact, K_SS, 8, U_IN),
+    FF(h2osoi_liq, K_SS, 8, U_IN),
+    FF(h2osoi_ice, K_SS, 8, U_IN),
+    FF(errsoi_col, K_C, 8, U_OUT),
+    FF(patch_column, K_P, 4, U_IN),
+    FF(frac_veg_nosno, K_P, 4, U_IN),
+    FF(wtcol, K_P, 8, U_IN),
+    FF(cgrnds, K_P, 8, U_IN),
+    FF(cgrndl, K_P, 8, U_IN),
+    FF(sabg_soil, K_P, 8, U_IN),
+    FF(sabg_snow, K_P, 8, U_IN),
+    FF(dlrad, K_P, 8, U_IN),
+    FF(ulrad, K_P, 8, U_IN),
+    FF(eflx_sh_veg, K_P, 8, U_IN),
+    FF(qflx_evap_veg, K_P, 8, U_IN),
+    FF(qflx_tran_veg, K_P, 8, U_IN),
+    FF(eflx_sh_grnd, K_P, 8, U_INOUT),
+    FF(qflx_evap_soi, K_P, 8, U_INOUT),
+    FF(qflx_ev_snow, K_P, 8, U_INOUT),
+    FF(qflx_ev_soil, K_P, 8, U_INOUT),
+    FF(qflx_ev_h2osfc, K_P, 8, U_INOUT),
+    FF(qflx_liqevap_from_top_layer, K_P, 8, U_OUT),
+    FF(qflx_solidevap_from_top_layer, K_P, 8, U_OUT),
+    FF(qflx_soliddew_to_top_layer, K_P, 8, U_OUT),
+    FF(qflx_liqdew_to_top_layer, K_P, 8, U_OUT),
+    FF(eflx_soil_grnd, K_P, 8, U_OUT),
+    FF(eflx_sh_tot, K_P, 8, U_OUT),
+    FF(qflx_evap_tot, K_P, 8, U_OUT),
+    FF(eflx_lh_tot, K_P, 8, U_OUT),
+    FF(qflx_evap_can, K_P, 8, U_OUT),
+    FF(eflx_lh_vege, K_P, 8, U_OUT),
+    FF(eflx_lh_vegt, K_P, 8, U_OUT),
+    FF(eflx_lh_grnd, K_P, 8, U_OUT),
+    FF(eflx_lwrad_out, K_P, 8, U_OUT),
+    FF(eflx_lwrad_net, K_P, 8, U_OUT),
+    FF(errsoi_patch, K_P, 8, U_OUT),
+    FF(t_skin, K_P, 8, U_INOUT),
+};
+const int SOILFLUXES_NFIELDS = sizeof(SOILFLUXES_TABLE) / sizeof(SOILFLUXES_TABLE[0]);
+
 const FieldDesc CANOPY_TABLE[] = {
     FC(itype, K_P, 4, U_IN),
     FC(patch_column, K_P, 4, U_IN),
@@ -725,5 +785,56 @@ extern "C" int32_t ctsmg_canopyfluxes(const ctsmg_bounds* bounds, int32_t num_ex
                       : "CanopyFluxes error";
         return set_error(code, m, idx, lev);
     }
+    return 0;
+}
+
+extern "C" int32_t ctsmg_soilfluxes(const ctsmg_bounds* bounds, int32_t num_nolakec, const int32_t* filter_nolakec,
+                                    int32_t num_nolakep, const int32_t* filter_nolakep, const ctsmg_soilfluxes_io* io,
+                                    double dtime) {
+    ThreadCtx* c;
+    int rc = ctx_get(&c);
+    if (rc) return rc;
+    if (!io) return set_error(CTSMG_E_ARG, "null io", 0, 0);
+    if ((rc = check_filter(bounds, num_nolakec, filter_nolakec))) return rc;
+    if (num_nolakep < 0 || (num_nolakep > 0 && !filter_nolakep)) return set_error(CTSMG_E_ARG, "bad patch filter", 0, 0);
+    const int ncol = bounds->endc - bounds->begc + 1;
+    const int npat = bounds->endp - bounds->begp + 1;
+    if (io->ldc < ncol || io->ldp < npat || npat < 0)
+        return set_error(CTSMG_E_ARG, "ldc/ldp smaller than the bounds", 0, 0);
+    if (!(dtime > 0.0)) return set_error(CTSMG_E_ARG, "dtime must be positive", 0, 0);
+    for (int i = 0; i < num_nolakep; ++i) {
+        const int pg = filter_nolakep[i];
+        if (pg < bounds->begp || pg > bounds->endp) return set_error(CTSMG_E_ARG, "patch filter outside bounds", pg, 0);
+        const int cc = io->patch_column[pg - bounds->begp];
+        if (cc < bounds->begc || cc > bounds->endc) return set_error(CTSMG_E_ARG, "patch column outside bounds", pg, 0);
+        const int s = io->snl[cc - bounds->begc];
+        if (s > 0 || s < -NLEVSNO) return set_error(CTSMG_E_ARG, "snl outside -nlevsno..0", cc, 0);
+    }
+    for (int i = 0; i < num_nolakec; ++i) {
+        const int cc = filter_nolakec[i] - bounds->begc;
+        const int pi = io->col_patchi[cc], np = io->col_npatches[cc];
+        if (np < 0 || (np > 0 && (pi < bounds->begp || pi + np - 1 > bounds->endp)))
+            return set_error(CTSMG_E_ARG, "column patches outside begp..endp", filter_nolakec[i], 0);
+    }
+    if (num_nolakec == 0 && num_nolakep == 0) return 0;
+    const int ldc = io->ldc, ldp = io->ldp;
+    size_t need = table_bytes(SOILFLUXES_TABLE, SOILFLUXES_NFIELDS, ldc, ldp) +
+                  ((size_t)num_nolakec + (size_t)num_nolakep) * 4 + 8192;
+    if ((rc = arena_reserve(c, need))) return rc;
+    ctsmg_soilfluxes_io dio;
+    if ((rc = stage_in(c, io, &dio, sizeof dio, SOILFLUXES_TABLE, SOILFLUXES_NFIELDS, ldc, ldp))) return rc;
+    int32_t* dfc = (int32_t*)arena_take(c, (size_t)num_nolakec * 4 + 4);
+    int32_t* dfp = (int32_t*)arena_take(c, (size_t)num_nolakep * 4 + 4);
+    cudaError_t e = cudaSuccess;
+    if (num_nolakec > 0)
+        e = cudaMemcpyAsync(dfc, filter_nolakec, (size_t)num_nolakec * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess && num_nolakep > 0)
+        e = cudaMemcpyAsync(dfp, filter_nolakep, (size_t)num_nolakep * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
+    e = launch_soilfluxes(dio, bounds->begc, bounds->begp, num_nolakec, dfc, num_nolakep, dfp, dtime, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "soilfluxes kernel launch");
+    if ((rc = stage_out(c, io, &dio, SOILFLUXES_TABLE, SOILFLUXES_NFIELDS, ldc, ldp))) return rc;
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "soilfluxes");
     return 0;
 }

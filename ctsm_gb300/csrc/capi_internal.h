@@ -15,6 +15,8 @@ extern const FieldDesc SOILTEMP_TABLE[];
 extern const int SOILTEMP_NFIELDS;
 extern const FieldDesc CANOPY_TABLE[];
 extern const int CANOPY_NFIELDS;
+extern const FieldDesc SOILFLUXES_TABLE[];
+extern const int SOILFLUXES_NFIELDS;
 
 int kind_levels(int kind);
 size_t field_bytes(const FieldDesc& f, int ldc, int ldp, int ldg = 0);

@@ -49,3 +49,16 @@ def SoilTemperature(bounds, num_nolakec, filter_nolakec, state, dtime):
     npat = bounds.endp - bounds.begp + 1
     io = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, state, ncol, npat)
     check(L.ctsmg_soiltemperature(C.byref(bounds), int(num_nolakec), fp, C.byref(io), float(dtime)))
+
+
+def SoilFluxes(bounds, num_nolakec, filter_nolakec, num_nolakep, filter_nolakep, state, dtime):
+    """SoilFluxes (SoilFluxesMod.F90:36) after SoilTemperature; `state` also
+    holds tssbef / t_h2osfc_bef, the temperatures saved before SoilTemperature."""
+    L = load()
+    fc, fcp = _filter(filter_nolakec)
+    fp, fpp = _filter(filter_nolakep)
+    ncol = bounds.endc - bounds.begc + 1
+    npat = bounds.endp - bounds.begp + 1
+    io = abi.make_io(abi.SoilFluxesIO, abi.SOILFLUXES_FIELDS, state, ncol, npat)
+    check(L.ctsmg_soilfluxes(C.byref(bounds), int(num_nolakec), fcp, int(num_nolakep), fpp, C.byref(io), float(dtime)))
+

@@ -326,6 +326,83 @@ int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds,
 int32_t ctsmg_canopyfluxes(const ctsmg_bounds* bounds, int32_t num_exposedvegp,
                            const int32_t* filter_exposedvegp, const ctsmg_canopy_io* io, double dtime);
 
+/* ---------------------------------------------------------------- SoilFluxes */
+/* Components SoilFluxes reads and writes for natural-vegetation columns and
+ * patches (src/biogeophys/SoilFluxesMod.F90:36-518; the urban branches and the
+ * _r/_u copies are not built).  tssbef and t_h2osfc_bef are the temperatures
+ * saved before SoilTemperature (temperature_inst%t_ssbef_col,
+ * t_h2osfc_bef_col); patch_column is 1-based (begc); eflx_sh_stem is zero
+ * (no biomass heat storage).                                                */
+typedef struct {
+    int32_t ldc, ldp;
+    /* columns */
+    const int32_t* snl;
+    const int32_t* col_patchi;       /* (c) first patch (1-based, begp)         */
+    const int32_t* col_npatches;
+    const double*  frac_sno_eff;
+    const double*  frac_h2osfc;
+    const double*  t_grnd;
+    const double*  t_h2osfc;
+    const double*  t_h2osfc_bef;
+    const double*  c_h2osfc;
+    const double*  emg;
+    const double*  forc_lwrad;
+    const double*  htvp;
+    const double*  xmf;
+    const double*  xmf_h2osfc;
+    const double*  eflx_h2osfc_to_snow;
+    const double*  t_soisno;         /* [SS] after SoilTemperature              */
+    const double*  tssbef;           /* [SS] before SoilTemperature             */
+    const double*  fact;             /* [SS] from SoilTemperature               */
+    const double*  h2osoi_liq;       /* [SS]                                    */
+    const double*  h2osoi_ice;       /* [SS]                                    */
+    double*        errsoi_col;       /* out: soil energy error (W/m2), p2c      */
+    /* patches */
+    const int32_t* patch_column;
+    const int32_t* frac_veg_nosno;
+    const double*  wtcol;
+    const double*  cgrnds;
+    const double*  cgrndl;
+    const double*  sabg_soil;
+    const double*  sabg_snow;
+    const double*  dlrad;
+    const double*  ulrad;
+    const double*  eflx_sh_veg;
+    const double*  qflx_evap_veg;
+    const double*  qflx_tran_veg;
+    double*        eflx_sh_grnd;     /* inout: updated for the T increment     */
+    double*        qflx_evap_soi;    /* inout                                   */
+    double*        qflx_ev_snow;     /* inout                                   */
+    double*        qflx_ev_soil;     /* inout                                   */
+    double*        qflx_ev_h2osfc;   /* inout                                   */
+    double*        qflx_liqevap_from_top_layer;
+    double*        qflx_solidevap_from_top_layer;
+    double*        qflx_soliddew_to_top_layer;
+    double*        qflx_liqdew_to_top_layer;
+    double*        eflx_soil_grnd;
+    double*        eflx_sh_tot;
+    double*        qflx_evap_tot;
+    double*        eflx_lh_tot;
+    double*        qflx_evap_can;
+    double*        eflx_lh_vege;
+    double*        eflx_lh_vegt;
+    double*        eflx_lh_grnd;
+    double*        eflx_lwrad_out;
+    double*        eflx_lwrad_net;
+    double*        errsoi_patch;
+    double*        t_skin;           /* inout: written where frac_veg_nosno = 0 */
+} ctsmg_soilfluxes_io;
+
+/* SoilFluxes (src/biogeophys/SoilFluxesMod.F90:36-518): the ground sensible
+ * and latent fluxes for the temperature increment of the step, top-layer
+ * evaporation / dew and its limits, eflx_soil_grnd, the total, latent and
+ * longwave fluxes and the soil energy error errsoi (patch, and column by
+ * p2c over filter_nolakec).  Called after SoilTemperature
+ * (src/main/clm_driver.F90:921).                                         */
+int32_t ctsmg_soilfluxes(const ctsmg_bounds* bounds, int32_t num_nolakec, const int32_t* filter_nolakec,
+                         int32_t num_nolakep, const int32_t* filter_nolakep, const ctsmg_soilfluxes_io* io,
+                         double dtime);
+
 /* Allocation-free SoilTemperature.  No counterpart in the reference: it is an
  * extra entry point for callers that cannot allocate device memory -- a host
  * whose device memory belongs to another runtime (an OpenACC or OpenMP-offload

@@ -54,6 +54,8 @@ def test_struct_layout_matches_ctypes(tmp_path):
     """Compile a C probe against the header and compare sizeof/offsetof."""
     fields = {"ctsmg_soilwater_io": (abi.SoilWaterIO, ["ldc"] + [f[0] for f in abi.SOILWATER_FIELDS]),
               "ctsmg_soiltemp_io": (abi.SoilTempIO, ["ldc", "ldp"] + [f[0] for f in abi.SOILTEMP_FIELDS]),
+              "ctsmg_soilfluxes_io": (abi.SoilFluxesIO, ["ldc", "ldp"] + [f[0] for f in abi.SOILFLUXES_FIELDS]),
+              "ctsmg_canopy_io": (abi.CanopyIO, ["ldp", "ldc", "ldg", "begg"] + [f[0] for f in abi.CANOPY_FIELDS]),
               "ctsmg_bounds": (abi.Bounds, ["begc", "endc", "begp", "endp"]),
               "ctsmg_options": (abi.Options, [f[0] for f in abi.Options._fields_])}
     src = ['#include <stdio.h>', '#include <stddef.h>', '#include "ctsm_gpu.h"', "int main(void){"]
