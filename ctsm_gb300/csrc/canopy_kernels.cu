@@ -35,6 +35,22 @@ constexpr double TLSAI_CRIT = 2.0;
 __device__ __forceinline__ double ipow4(double x) { double x2 = x * x; return x2 * x2; }
 __device__ __forceinline__ double ipow3(double x) { double x2 = x * x; return x2 * x; }
 
+// Lane-occupancy probes for tuning builds (-DCTSMG_LANE_PROBE): per probe
+// point, the number of warp-level executions and the sum of active lanes.
+#ifdef CTSMG_LANE_PROBE
+__device__ unsigned long long g_lane_probe[64];
+#define LANE_PROBE(i)                                                                        \
+    do {                                                                                     \
+        const unsigned m_ = __activemask();                                                  \
+        if ((int)(threadIdx.x & 31) == __ffs(m_) - 1) {                                      \
+            atomicAdd(&g_lane_probe[2 * (i)], 1ull);                                         \
+            atomicAdd(&g_lane_probe[2 * (i) + 1], (unsigned long long)__popc(m_));           \
+        }                                                                                    \
+    } while (0)
+#else
+#define LANE_PROBE(i) do {} while (0)
+#endif
+
 struct Err { int code, idx; };
 __device__ __forceinline__ void flag(Err& e, int code, int idx) { if (!e.code) { e.code = code; e.idx = idx; } }
 
@@ -116,6 +132,7 @@ struct PsnCtx {
 
 // PhotosynthesisMod.F90:2564-2701
 __device__ double ci_func(double ci, const PsnCtx& x, PsnState& s, Err& e, int pidx) {
+    LANE_PROBE(4);
     double r1, r2;
     if (x.c3) {
         s.ac = x.vcmax_z * fmax(ci - x.cp, 0.0) / (ci + x.kco);
@@ -132,6 +149,7 @@ __device__ double ci_func(double ci, const PsnCtx& x, PsnState& s, Err& e, int p
     s.ag = fmax(0.0, fmin(r1, r2));
     s.an = s.ag - x.lmr_z;
     if (s.an < 0.0) return 0.0;
+    LANE_PROBE(5);
     double cs = x.cair - x.c14gb * s.an * x.forc_pbot;
     cs = fmax(cs, 1.e-06);
     if (x.method == 1) {
@@ -192,7 +210,8 @@ struct Patch {
     // the fixed heights over z0m in FrictionVelocity, (zetam)^0.333 and
     // (zetat)^-0.333, exp(-(elai+esai)), sqrt(dleaf), 1 - exp(-elai_dl) and
     // the ground's emitted longwave factor lw_grnd
-    double lg_u, lg_u10, lg_t, lg_q, lg_2m, lg_u10m, pz_m, pz_t, w_sai, sqrt_dleaf, one_m_edl, lw_grnd;
+    double lg_u, lg_u10, lg_t, lg_q, lg_2m, lg_u10m, pz_m, pz_t, s1_zetam, s2_zetat, w_sai, sqrt_dleaf, one_m_edl,
+        lw_grnd;
     PsnPatch q;
     PhaseOut sun, sha;
     PsnState st;
@@ -209,7 +228,8 @@ struct Patch {
     X(ustar) X(temp1) X(temp2) X(temp12m) X(temp22m) X(ram1) X(rah_a) X(raw_a) X(rah_b) X(uaf) X(rb)                  \
     X(wtl0) X(wta0) X(wtg) X(wtal) X(wtgq) X(wtlq0) X(wtaq0) X(wtalq) X(efe)                                          \
     X(u10_clm) X(u10) X(vds) X(vpd_can) X(rh_leaf) X(rhaf_last) X(vpd_last)                                           \
-    X(lg_u) X(lg_u10) X(lg_t) X(lg_q) X(lg_2m) X(lg_u10m) X(pz_m) X(pz_t) X(w_sai) X(sqrt_dleaf) X(one_m_edl)         \
+    X(lg_u) X(lg_u10) X(lg_t) X(lg_q) X(lg_2m) X(lg_u10m) X(pz_m) X(pz_t) X(s1_zetam) X(s2_zetat) X(w_sai)         \
+    X(sqrt_dleaf) X(one_m_edl)                                                                                        \
     X(lw_grnd)                                                                                                        \
     X(q.vcmax25top) X(q.jmax25top) X(q.vcmaxse) X(q.jmaxse) X(q.tpuse) X(q.f25_lmr) X(q.f25_vc) X(q.f25_j)            \
     X(q.f25_tpu) X(q.cf) X(q.mslope) X(q.mint) X(q.mbb)                                                               \
@@ -258,6 +278,7 @@ __device__ void psn_temp(const CanopyArgs& A, const Patch& s, double forc_pbot, 
         T.lmr2 = 1.0 + xexp(1.3 * (t_veg - (TFRZ + 55.0)));
     }
     if (!day) return;
+    LANE_PROBE(6);
     T.kc = P.kc25_coef * forc_pbot * ft(t_veg, P.kcha);
     T.ko = P.ko25_coef * forc_pbot * ft(t_veg, P.koha);
     const double sco = 0.5 * 0.209 / P.cp25_yr2000;
@@ -282,6 +303,7 @@ __device__ PhaseOut photosynthesis(const CanopyArgs& A, const Patch& s, const Ps
                                    double& rh_leaf, Err& err) {
     const ctsmg_canopy_params& P = A.par;
     const int method = A.method;
+    LANE_PROBE(3);
     const PsnPatch& q = s.q;
     const double medlyn_int = q.mint;
     const bool c3 = s.c3 != 0;
@@ -379,14 +401,22 @@ __device__ void friction_velocity(const Patch& s, int iter, double& fm, double& 
     const double obu = s.obu, z0m = s.z0mv, um = s.um;
     double zldis = s.hgt_u - s.displa;
     double zeta = zldis / obu;
-    if (zeta < -zetam)
-        ustar = VKC * um / (xlog(-zetam * obu / z0m) - stab1(-zetam) + stab1(z0m / obu) +
-                            1.14 * (xpow(-zeta, 0.333) - s.pz_m));
-    else if (zeta < 0.0)
+    // values several branches share, evaluated once: stab1(-zetam) and
+    // stab2(-zetat) (constants, kept in the record), (-zeta)^0.333, and
+    // stab2(z0m/obu), the same in all three scalar profiles
+    LANE_PROBE(1);
+    const double pz = (zeta < -zetam) ? xpow(-zeta, 0.333) : 0.0;
+    const double s2z0 = (obu < 0.0) ? stab2(z0m / obu) : 0.0;
+    if (zeta < -zetam) {
+        LANE_PROBE(8);
+        ustar = VKC * um / (xlog(-zetam * obu / z0m) - s.s1_zetam + stab1(z0m / obu) + 1.14 * (pz - s.pz_m));
+    } else if (zeta < 0.0) {
+        LANE_PROBE(9);
         ustar = VKC * um / (s.lg_u - stab1(zeta) + stab1(z0m / obu));
-    else if (zeta <= 1.0)
+    } else if (zeta <= 1.0) {
+        LANE_PROBE(10);
         ustar = VKC * um / (s.lg_u + 5.0 * zeta - 5.0 * z0m / obu);
-    else
+    } else
         ustar = VKC * um / (xlog(obu / z0m) + 5.0 - 5.0 * z0m / obu + (5.0 * xlog(zeta) + zeta - 1.0));
     vds = (zeta < 0.0) ? 2.e-3 * ustar * (1.0 + xpow(300.0 / (-obu), 0.666)) : 2.e-3 * ustar;
     if (zldis - z0m <= 10.0) {
@@ -394,8 +424,7 @@ __device__ void friction_velocity(const Patch& s, int iter, double& fm, double& 
     } else {
         const double z10 = 10.0 + z0m;
         if (zeta < -zetam)
-            u10_clm = um - (ustar / VKC * (xlog(-zetam * obu / z10) - stab1(-zetam) + stab1(z10 / obu) +
-                                            1.14 * (xpow(-zeta, 0.333) - s.pz_m)));
+            u10_clm = um - (ustar / VKC * (xlog(-zetam * obu / z10) - s.s1_zetam + stab1(z10 / obu) + 1.14 * (pz - s.pz_m)));
         else if (zeta < 0.0)
             u10_clm = um - (ustar / VKC * (s.lg_u10 - stab1(zeta) + stab1(z10 / obu)));
         else if (zeta <= 1.0)
@@ -403,13 +432,12 @@ __device__ void friction_velocity(const Patch& s, int iter, double& fm, double& 
         else
             u10_clm = um - (ustar / VKC * (xlog(obu / z10) + 5.0 - 5.0 * z10 / obu + (5.0 * xlog(zeta) + zeta - 1.0)));
     }
-    auto tprof = [&](double zl, double z0, double lgz) {
+    auto tprof = [&](double zl, double z0, double lgz) {   // z0 = z0m in every call
         const double zt = zl / obu;
         if (zt < -zetat)
-            return VKC / (xlog(-zetat * obu / z0) - stab2(-zetat) + stab2(z0 / obu) +
-                          0.8 * (s.pz_t - xpow(-zt, -0.333)));
+            return VKC / (xlog(-zetat * obu / z0) - s.s2_zetat + s2z0 + 0.8 * (s.pz_t - xpow(-zt, -0.333)));
         else if (zt < 0.0)
-            return VKC / (lgz - stab2(zt) + stab2(z0 / obu));
+            return VKC / (lgz - stab2(zt) + s2z0);
         else if (zt <= 1.0)
             return VKC / (lgz + 5.0 * zt - 5.0 * z0 / obu);
         return VKC / (xlog(obu / z0) + 5.0 - 5.0 * z0 / obu + (5.0 * xlog(zt) + zt - 1.0));
@@ -419,7 +447,9 @@ __device__ void friction_velocity(const Patch& s, int iter, double& fm, double& 
     temp12m = tprof(2.0 + s.z0mv, s.z0mv, s.lg_2m);
     temp22m = temp12m;
     double fmnew;
+    LANE_PROBE(2);
     if (fmin(zeta, 1.0) < 0.0) {
+        LANE_PROBE(11);
         const double tmp1 = xpow(1.0 - 16.0 * fmin(zeta, 1.0), 0.25);
         fmnew = 2.0 * xlog((1.0 + tmp1) / 2.0) + xlog((1.0 + tmp1 * tmp1) / 2.0) - 2.0 * xatan(tmp1) + 1.5707963;
     } else {
@@ -495,6 +525,8 @@ __device__ void setup(const CanopyArgs& A, Patch& s, int p, Err& err) {
     s.lg_u10m = xlog(fmax(1.0, s.hgt_u / 10.0));
     s.pz_m = xpow(1.574, 0.333);
     s.pz_t = xpow(0.465, -0.333);
+    s.s1_zetam = stab1(-1.574);
+    s.s2_zetat = stab2(-0.465);
     s.w_sai = xexp(-(elai + esai));
     s.sqrt_dleaf = sqrt(A.pft.dleaf[s.ivt]);
     {
@@ -549,6 +581,7 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, Err& err, double dtime) {
     const ctsmg_canopy_params& P = A.par;
     const int p = s.p, c = s.c, g = s.g;
     const int pg = p + A.begp;
+    LANE_PROBE(0);
     friction_velocity(s, s.itlef + 1, s.fm, s.ustar, s.temp1, s.temp2, s.temp12m, s.temp22m, s.u10_clm, s.u10, s.vds);
     const double ustar = s.ustar;
     s.tlbef = s.t_veg;
@@ -589,6 +622,7 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, Err& err, double dtime) {
         if (ph) s.sha = o;
         else s.sun = o;
     }
+    LANE_PROBE(7);
     const double sa_leaf = elai + esai;
     const double wta = 1.0 / s.rah_a;
     const double wtl = sa_leaf / rb;
@@ -884,21 +918,32 @@ canopy_iterate_kernel(CanopyArgs A, int nfilt, double* __restrict__ ws, double d
     Err err{0, 0};
     const int* __restrict__ order = order_of(ws, nfilt).order;
     int f = -1;                        // filter position of the patch this lane holds
+    bool have = true;                  // the work queue was not empty when this lane last looked
+    // The loop runs until every lane of the warp is out of work, and the
+    // lanes that took a new patch this round meet the others at __syncwarp()
+    // before the pass, so each pass is executed by the whole warp at once.
+    // (Block size is a multiple of 32 and no lane leaves the loop early.)
 #pragma unroll 1
-    for (;;) {
-        if (f < 0) {
+    while (__any_sync(0xffffffffu, have)) {
+        if (have && f < 0) {
             const int i = atomicAdd(next, 1);
-            if (i >= nfilt) break;
-            f = order[i];
-            load_patch(ws, nfilt, f, s);
-            err = Err{s.err_code, s.err_idx};
+            if (i >= nfilt) {
+                have = false;
+            } else {
+                f = order[i];
+                LANE_PROBE(12);
+                load_patch(ws, nfilt, f, s);
+                err = Err{s.err_code, s.err_idx};
+            }
         }
-        if (pass(A, s, err, dtime)) {
+        __syncwarp();
+        if (have && pass(A, s, err, dtime)) {
             s.err_code = err.code;
             s.err_idx = err.idx;
             store_patch(ws, nfilt, f, s);
             f = -1;
         }
+        __syncwarp();
     }
 }
 
@@ -947,3 +992,15 @@ cudaError_t launch_canopy(const CanopyArgs& a, int nfilt, const int32_t* d_filt,
 }
 
 } // namespace ctsmg
+
+#ifdef CTSMG_LANE_PROBE
+extern "C" int32_t ctsmg_lane_probe_read(unsigned long long* out, int32_t reset) {
+    cudaError_t e = cudaMemcpyFromSymbol(out, ctsmg::canopy::g_lane_probe, sizeof(unsigned long long) * 64);
+    if (reset) {
+        unsigned long long z[64] = {};
+        cudaMemcpyToSymbol(ctsmg::canopy::g_lane_probe, z, sizeof z);
+    }
+    return e == cudaSuccess ? 0 : 2;
+}
+#endif
+
