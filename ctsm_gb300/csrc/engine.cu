@@ -33,6 +33,7 @@ struct Batch {
     std::map<std::string, int> index;
     ctsmg_soilwater_io dsw{};
     ctsmg_soiltemp_io dst{};
+    ctsmg_soilfluxes_io dsf{};
     CanopyArgs cargs{};
     double* rootr = nullptr;
     double* mslope = nullptr;
@@ -67,7 +68,7 @@ static void set_io_ptr(void* io, const FieldDesc& f, void* p) {
 static cudaError_t enqueue_step(Batch* b) {
     cudaError_t e = cudaSuccess;
     const int ncol = b->cfg.ncol;
-    if (b->cfg.balance) {
+    if (b->cfg.balance || b->cfg.soilfluxes) {
         e = launch_prestep(b->dst, ncol, b->bal, b->stream);
         if (e != cudaSuccess) return e;
     }
@@ -79,7 +80,8 @@ static cudaError_t enqueue_step(Batch* b) {
         if (e != cudaSuccess) return e;
     }
     e = launch_soilstep(b->dsw, b->dst, ncol, b->cfg.e_ice, b->cfg.dtime, b->cfg.snow_thermal_cond_method, b->ws,
-                        ncol, b->err, b->stream, b->block, b->cfg.order);
+                        ncol, b->err, b->stream, b->block, b->cfg.soilfluxes ? 2 : b->cfg.order, nullptr,
+                        b->cfg.soilfluxes ? &b->dsf : nullptr);
     if (e != cudaSuccess || !b->cfg.balance) return e;
     return launch_balance(b->dsw, b->dst, ncol, b->cfg.dtime, b->bal, b->stream);
 }
@@ -120,8 +122,9 @@ using namespace ctsmg;
 
 struct ctsmg_batch_s { Batch* b; };
 
-extern "C" int32_t ctsmg_batch_create2(ctsmg_batch* out, const ctsmg_batch_config* cfg, const ctsmg_soilwater_io* sw,
-                                       const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio, const double* rootr,
+extern "C" int32_t ctsmg_batch_create3(ctsmg_batch* out, const ctsmg_batch_config* cfg, const ctsmg_soilwater_io* sw,
+                                       const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio,
+                                       const ctsmg_soilfluxes_io* sf, const double* rootr,
                                        const double* medlynslope_p, const double* medlynintercept_p,
                                        const ctsmg_canopy_params* cpar, const ctsmg_pftcon* pft) {
     const bool canopy_only = cfg && cfg->order == 2;
@@ -133,6 +136,10 @@ extern "C" int32_t ctsmg_batch_create2(ctsmg_batch* out, const ctsmg_batch_confi
     if (!(cfg->dtime > 0.0)) return set_error(CTSMG_E_ARG, "dtime must be positive", 0, 0);
     if (cfg->order < 0 || cfg->order > 2 || (cfg->order == 2 && (!cfg->with_canopy || cfg->balance)))
         return set_error(CTSMG_E_ARG, "order must be 0, 1, or 2 (CanopyFluxes only: with_canopy, no balance)", 0, 0);
+    if (cfg->soilfluxes && (!cfg->with_canopy || cfg->order != 1 || !sf))
+        return set_error(CTSMG_E_ARG, "soilfluxes needs with_canopy, order 1 and the SoilFluxes components", 0, 0);
+    if (cfg->soilfluxes && (sf->ldc != ncol || sf->ldp != npatch))
+        return set_error(CTSMG_E_ARG, "SoilFluxes arrays must be dense: ldc = ncol, ldp = npatch", 0, 0);
     if (cfg->with_canopy) {
         if (!cio || (!rootr && !canopy_only) || !cpar || !pft)
             return set_error(CTSMG_E_ARG, "with_canopy needs cio, rootr, params", 0, 0);
@@ -247,10 +254,14 @@ extern "C" int32_t ctsmg_batch_create2(ctsmg_batch* out, const ctsmg_batch_confi
         }
         b->cargs.medlynslope_p = b->mslope;
         b->cargs.medlynintercept_p = b->mint;
+        if (cfg->soilfluxes) {
+            std::memcpy(&b->dsf, sf, sizeof b->dsf);
+            if ((rc = add(SOILFLUXES_TABLE, SOILFLUXES_NFIELDS, sf, &b->dsf))) return fail(rc);
+        }
         if ((e = cudaMalloc(&b->counter, 256)) != cudaSuccess) return fail(cuda_err(e, "counter"));
         if ((e = cudaMalloc(&b->cws, canopy_ws_bytes(npatch))) != cudaSuccess) return fail(cuda_err(e, "canopy ws"));
     }
-    if (cfg->balance) {
+    if (cfg->balance || cfg->soilfluxes) {
         const size_t ssb = (size_t)ncol * (NLEVSNO + NLEVGRND) * 8, cb = (size_t)ncol * 8;
         if ((e = cudaMalloc(&b->bal_mem, ssb + 6 * cb + 256)) != cudaSuccess) return fail(cuda_err(e, "balance"));
         if ((e = cudaMemset(b->bal_mem, 0, ssb + 6 * cb + 256)) != cudaSuccess) return fail(cuda_err(e, "balance"));
@@ -264,6 +275,10 @@ extern "C" int32_t ctsmg_batch_create2(ctsmg_batch* out, const ctsmg_batch_confi
         b->bal.errsoi_max = (double*)m; m += cb;
         b->bal.step = (int*)m;
         b->bal.skip_steps = cfg->skip_steps;
+        if (cfg->soilfluxes) {                  // the prestep saves straight into SoilFluxes' inputs
+            b->bal.tssbef = const_cast<double*>(b->dsf.tssbef);
+            b->bal.th2osfc_bef = const_cast<double*>(b->dsf.t_h2osfc_bef);
+        }
     }
     for (auto& f : b->fields) b->state_bytes += f.bytes;
     if ((e = cudaMalloc(&b->ws, (size_t)SOILTEMP_WS_DOUBLES_PER_COL * ncol * 8)) != cudaSuccess) return fail(cuda_err(e, "ws"));
@@ -272,6 +287,14 @@ extern "C" int32_t ctsmg_batch_create2(ctsmg_batch* out, const ctsmg_batch_confi
     if ((rc = build_graph(b))) return fail(rc);
     *out = new ctsmg_batch_s{b};
     return 0;
+}
+
+extern "C" int32_t ctsmg_batch_create2(ctsmg_batch* out, const ctsmg_batch_config* cfg, const ctsmg_soilwater_io* sw,
+                                       const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio, const double* rootr,
+                                       const double* medlynslope_p, const double* medlynintercept_p,
+                                       const ctsmg_canopy_params* cpar, const ctsmg_pftcon* pft) {
+    if (cfg && cfg->soilfluxes) return set_error(CTSMG_E_ARG, "soilfluxes needs ctsmg_batch_create3", 0, 0);
+    return ctsmg_batch_create3(out, cfg, sw, st, cio, nullptr, rootr, medlynslope_p, medlynintercept_p, cpar, pft);
 }
 
 extern "C" int32_t ctsmg_batch_create(ctsmg_batch* out, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
@@ -283,7 +306,7 @@ extern "C" int32_t ctsmg_batch_create(ctsmg_batch* out, const ctsmg_soilwater_io
     cfg.snow_thermal_cond_method = snow_thermal_cond_method;
     cfg.stomatalcond_method = 1; cfg.itmax_canopy_fluxes = 40;
     cfg.order = 0; cfg.with_canopy = 0; cfg.bucket = 1;
-    cfg.balance = 0; cfg.skip_steps = 0;
+    cfg.balance = 0; cfg.skip_steps = 0; cfg.soilfluxes = 0;
     return ctsmg_batch_create2(out, &cfg, sw, st, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
 }
 
@@ -344,6 +367,13 @@ static int download_table(Batch* b, const FieldDesc* tab, int nf, const void* hi
         }
     }
     return 0;
+}
+
+extern "C" int32_t ctsmg_batch_download3(ctsmg_batch bh, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
+                                         const ctsmg_canopy_io* cio, const ctsmg_soilfluxes_io* sf) {
+    int rc = ctsmg_batch_download2(bh, sw, st, cio);
+    if (rc || !sf || !bh->b->cfg.soilfluxes) return rc;
+    return download_table(bh->b, SOILFLUXES_TABLE, SOILFLUXES_NFIELDS, sf);
 }
 
 extern "C" int32_t ctsmg_batch_download2(ctsmg_batch bh, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,

@@ -17,6 +17,7 @@
 #include "ctsm_device.cuh"
 #include <mutex>
 #include "soil_kernels.cuh"
+#include "soilfluxes_device.cuh"
 #include "capi_internal.h"
 
 namespace ctsmg {
@@ -861,13 +862,16 @@ soiltemp_kernel(ctsmg_soiltemp_io io, int begc, int begp, int nfilt, const int32
 }
 
 // One model step on one column: SoilWater then SoilTemperature (ORDER 0, the
-// pairing of the plain workloads) or SoilTemperature then SoilWater (ORDER 1,
-// the driver's order after CanopyFluxes, clm_driver.F90:900,950), then the
-// between-step refresh of h2osoi_vol (HydrologyNoDrainageMod.F90:580,590).
+// pairing of the plain workloads), SoilTemperature then SoilWater (ORDER 1,
+// the driver's order after CanopyFluxes, clm_driver.F90:900,950), or
+// SoilTemperature, SoilFluxes over the column's patches and SoilWater
+// (ORDER 2, clm_driver.F90:900,921,950; sf carries the SoilFluxes components
+// and the temperatures saved before the step), then the between-step refresh
+// of h2osoi_vol (HydrologyNoDrainageMod.F90:580,590).
 template <int BLOCK, int ORDER>
 __global__ void __launch_bounds__(BLOCK)
-soilstep_kernel(ctsmg_soilwater_io wio, ctsmg_soiltemp_io tio, int ncol, double e_ice, double dtime,
-                int snow_method, double* ws, int ws_ld, DevError* err, const int32_t* __restrict__ filt) {
+soilstep_kernel(ctsmg_soilwater_io wio, ctsmg_soiltemp_io tio, ctsmg_soilfluxes_io sf, int ncol, double e_ice,
+                double dtime, int snow_method, double* ws, int ws_ld, DevError* err, const int32_t* __restrict__ filt) {
     const int fc = blockIdx.x * BLOCK + threadIdx.x;
     if (fc >= ncol) return;
     const int c = filt ? filt[fc] - 1 : fc;     // filt: 1-based column positions (pool mode)
@@ -875,7 +879,13 @@ soilstep_kernel(ctsmg_soilwater_io wio, ctsmg_soiltemp_io tio, int ncol, double 
     if (ORDER == 0) zd09_column(wio, c, e_ice, dtime);
     int info = soiltemp_column(tio, c, 1, dtime, snow_method, S);
     if (info != 0) report_error(err, c + 1, info, CTSMG_E_SINGULAR);
-    if (ORDER == 1) zd09_column(wio, c, e_ice, dtime);
+    if (ORDER == 2) {
+        const int p0 = sf.col_patchi[c] - 1, np = sf.col_npatches[c];
+#pragma unroll 1
+        for (int p = p0; p < p0 + np; ++p) soilfluxes_patch(sf, p, c, dtime);
+        soilfluxes_p2c(sf, c, 1);
+    }
+    if (ORDER >= 1) zd09_column(wio, c, e_ice, dtime);
     const int ld = wio.ldc;
 #pragma unroll 1
     for (int j = 1; j <= NLEVSOI; ++j) {
@@ -926,31 +936,37 @@ cudaError_t launch_soiltemp(const ctsmg_soiltemp_io& io, int begc, int begp, int
 }
 
 template <int ORDER>
-static void launch_soilstep_order(const ctsmg_soilwater_io& wio, const ctsmg_soiltemp_io& tio, int ncol,
-                                  double e_ice, double dtime, int snow_method, double* ws, int ws_ld,
-                                  DevError* err, cudaStream_t s, int block, const int32_t* filt) {
+static void launch_soilstep_order(const ctsmg_soilwater_io& wio, const ctsmg_soiltemp_io& tio,
+                                  const ctsmg_soilfluxes_io& sf, int ncol, double e_ice, double dtime,
+                                  int snow_method, double* ws, int ws_ld, DevError* err, cudaStream_t s, int block,
+                                  const int32_t* filt) {
     switch (block) {
         case 64:
-            soilstep_kernel<64, ORDER><<<(ncol + 63) / 64, 64, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method, ws,
-                                                                       ws_ld, err, filt);
+            soilstep_kernel<64, ORDER><<<(ncol + 63) / 64, 64, 0, s>>>(wio, tio, sf, ncol, e_ice, dtime, snow_method,
+                                                                       ws, ws_ld, err, filt);
             break;
         case 256:
-            soilstep_kernel<256, ORDER><<<(ncol + 255) / 256, 256, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method,
-                                                                          ws, ws_ld, err, filt);
+            soilstep_kernel<256, ORDER><<<(ncol + 255) / 256, 256, 0, s>>>(wio, tio, sf, ncol, e_ice, dtime,
+                                                                          snow_method, ws, ws_ld, err, filt);
             break;
         default:
-            soilstep_kernel<128, ORDER><<<(ncol + 127) / 128, 128, 0, s>>>(wio, tio, ncol, e_ice, dtime, snow_method,
-                                                                          ws, ws_ld, err, filt);
+            soilstep_kernel<128, ORDER><<<(ncol + 127) / 128, 128, 0, s>>>(wio, tio, sf, ncol, e_ice, dtime,
+                                                                          snow_method, ws, ws_ld, err, filt);
             break;
     }
 }
 
 cudaError_t launch_soilstep(const ctsmg_soilwater_io& wio, const ctsmg_soiltemp_io& tio, int ncol,
                             double e_ice, double dtime, int snow_method, double* ws, int ws_ld,
-                            DevError* err, cudaStream_t s, int block, int order, const int32_t* filt) {
+                            DevError* err, cudaStream_t s, int block, int order, const int32_t* filt,
+                            const ctsmg_soilfluxes_io* sf) {
     if (ncol <= 0) return cudaSuccess;
-    if (order == 1) launch_soilstep_order<1>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err, s, block, filt);
-    else launch_soilstep_order<0>(wio, tio, ncol, e_ice, dtime, snow_method, ws, ws_ld, err, s, block, filt);
+    if (order == 2 && !sf) return cudaErrorInvalidValue;
+    const ctsmg_soilfluxes_io none{};
+    const ctsmg_soilfluxes_io& f = sf ? *sf : none;
+    if (order == 2) launch_soilstep_order<2>(wio, tio, f, ncol, e_ice, dtime, snow_method, ws, ws_ld, err, s, block, filt);
+    else if (order == 1) launch_soilstep_order<1>(wio, tio, f, ncol, e_ice, dtime, snow_method, ws, ws_ld, err, s, block, filt);
+    else launch_soilstep_order<0>(wio, tio, f, ncol, e_ice, dtime, snow_method, ws, ws_ld, err, s, block, filt);
     return cudaGetLastError();
 }
 

@@ -14,7 +14,7 @@ cudaError_t launch_soiltemp(const ctsmg_soiltemp_io& io, int begc, int begp, int
 cudaError_t launch_soilstep(const ctsmg_soilwater_io& wio, const ctsmg_soiltemp_io& tio, int ncol,
                             double e_ice, double dtime, int snow_method, double* ws, int ws_ld,
                             DevError* err, cudaStream_t s, int block, int order = 0,
-                            const int32_t* filt = nullptr);
+                            const int32_t* filt = nullptr, const ctsmg_soilfluxes_io* sf = nullptr);
 cudaError_t launch_rootsink(const int32_t* col_patchi, const int32_t* col_npatches, const double* wtcol,
                             const double* qflx_tran_veg, const double* rootr, int ldp, double* qflx_rootsoi,
                             int ncol, cudaStream_t s, int ldc = 0, const int32_t* filt = nullptr);

@@ -25,6 +25,11 @@ def _bind(L):
                                       P(abi.CanopyIO), P(C.c_double), P(C.c_double), P(C.c_double),
                                       P(abi.CanopyParams), P(abi.Pftcon)]
     L.ctsmg_batch_download2.argtypes = [C.c_void_p, P(abi.SoilWaterIO), P(abi.SoilTempIO), P(abi.CanopyIO)]
+    L.ctsmg_batch_create3.argtypes = [P(C.c_void_p), P(BatchConfig), P(abi.SoilWaterIO), P(abi.SoilTempIO),
+                                      P(abi.CanopyIO), P(abi.SoilFluxesIO), P(C.c_double), P(C.c_double),
+                                      P(C.c_double), P(abi.CanopyParams), P(abi.Pftcon)]
+    L.ctsmg_batch_download3.argtypes = [C.c_void_p, P(abi.SoilWaterIO), P(abi.SoilTempIO), P(abi.CanopyIO),
+                                        P(abi.SoilFluxesIO)]
     L.ctsmg_batch_balance.argtypes = [C.c_void_p] + [P(C.c_double)] * 4
     L._batch_bound = True
 
@@ -37,7 +42,7 @@ class BatchConfig(C.Structure):
     _fields_ = [("ncol", C.c_int32), ("npatch", C.c_int32), ("ngrid", C.c_int32), ("dtime", C.c_double),
                 ("e_ice", C.c_double), ("snow_thermal_cond_method", C.c_int32), ("stomatalcond_method", C.c_int32),
                 ("itmax_canopy_fluxes", C.c_int32), ("order", C.c_int32), ("with_canopy", C.c_int32),
-                ("bucket", C.c_int32), ("balance", C.c_int32), ("skip_steps", C.c_int32)]
+                ("bucket", C.c_int32), ("balance", C.c_int32), ("skip_steps", C.c_int32), ("soilfluxes", C.c_int32)]
 
 
 class SoilBatch:
@@ -49,7 +54,8 @@ class SoilBatch:
 
     def __init__(self, state, npatch, dtime=1800.0, e_ice=6.0, snow_thermal_cond_method=0, canopy=False,
                  ngrid=None, rootr=None, order=None, bucket=True, stomatalcond_method=1, itmax=40,
-                 params=None, pftcon=None, per_patch_medlyn=False, balance=False, skip_steps=None):
+                 params=None, pftcon=None, per_patch_medlyn=False, balance=False, skip_steps=None,
+                 soilfluxes=False):
         from . import canopy_inputs
         self.L = load()
         _bind(self.L)
@@ -69,7 +75,8 @@ class SoilBatch:
         cfg = BatchConfig(self.ncol, npatch, self.ngrid, dtime, e_ice, snow_thermal_cond_method, stomatalcond_method,
                           itmax, (1 if canopy else 0) if order is None else order, 1 if canopy else 0,
                           1 if bucket else 0, 1 if balance else 0,
-                          _skip(dtime) if skip_steps is None else skip_steps)
+                          _skip(dtime) if skip_steps is None else skip_steps, 1 if soilfluxes else 0)
+        self.soilfluxes = soilfluxes
         self.h = C.c_void_p()
         if canopy:
             self._ci = abi.make_io(abi.CanopyIO, abi.CANOPY_FIELDS, state, self.ncol, npatch, self.ngrid, 1)
@@ -79,8 +86,10 @@ class SoilBatch:
             self._par = params if params is not None else canopy_inputs.make_params()
             self._pft = pftcon if pftcon is not None else canopy_inputs.make_pftcon()
             self._rootr = None if rootr is None else np.ascontiguousarray(rootr, dtype=np.float64)
-            check(self.L.ctsmg_batch_create2(C.byref(self.h), C.byref(cfg), _ref(self._sw), _ref(self._st),
-                                             C.byref(self._ci),
+            self._sf = abi.make_io(abi.SoilFluxesIO, abi.SOILFLUXES_FIELDS, state, self.ncol, npatch) \
+                if soilfluxes else None
+            check(self.L.ctsmg_batch_create3(C.byref(self.h), C.byref(cfg), _ref(self._sw), _ref(self._st),
+                                             C.byref(self._ci), _ref(self._sf),
                                              None if self._rootr is None else self._rootr.ctypes.data_as(dp), ms,
                                              mi, C.byref(self._par), C.byref(self._pft)))
         else:
@@ -107,7 +116,9 @@ class SoilBatch:
             tt = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, st, self.ncol, self.npatch)
         if self.canopy:
             ci = abi.make_io(abi.CanopyIO, abi.CANOPY_FIELDS, st, self.ncol, self.npatch, self.ngrid, 1)
-            check(self.L.ctsmg_batch_download2(self.h, _ref(sw), _ref(tt), C.byref(ci)))
+            sf = abi.make_io(abi.SoilFluxesIO, abi.SOILFLUXES_FIELDS, st, self.ncol, self.npatch) \
+                if self.soilfluxes else None
+            check(self.L.ctsmg_batch_download3(self.h, _ref(sw), _ref(tt), C.byref(ci), _ref(sf)))
         else:
             check(self.L.ctsmg_batch_download(self.h, C.byref(sw), C.byref(tt)))
         return st

@@ -150,3 +150,13 @@ def concat(parts):
         out[k] = np.ascontiguousarray(np.concatenate(vs, axis=-1))
     rootr = out.pop("_rootr")
     return out, npat_off, ncol_off, rootr
+
+
+def add_soilfluxes_fields(A, npatch, ngrid):
+    """Zero-filled arrays for the SoilFluxes components a full state lacks
+    (tssbef / t_h2osfc_bef are written by the step before SoilTemperature)."""
+    ncol = A["zwt"].shape[0]
+    for (n, kind, t, u) in abi.SOILFLUXES_FIELDS:
+        if n not in A:
+            A[n] = np.zeros(abi.field_shape(kind, ncol, npatch, ngrid), dtype=np.dtype(t))
+    return A

@@ -2,7 +2,7 @@
  * ctsm_gpu.h -- C-ABI of the GB300 (sm_103a) column biogeophysics library.
  *
  * This is the boundary a CTSM host binds through ISO_C_BINDING in place of the
- * three column-parallel calls of the land driver:
+ * column-parallel calls of the land driver:
  *
  *   SoilWater        src/biogeophys/SoilWaterMovementMod.F90:240-243
  *                    (called from src/biogeophys/HydrologyNoDrainageMod.F90:346)
@@ -10,6 +10,8 @@
  *                    (called from src/main/clm_driver.F90:900)
  *   CanopyFluxes     src/biogeophys/CanopyFluxesMod.F90:191-198
  *                    (called from src/main/clm_driver.F90:766)
+ *   SoilFluxes       src/biogeophys/SoilFluxesMod.F90:36-41
+ *                    (called from src/main/clm_driver.F90:921)
  *
  * Array convention (identical to the Fortran storage of the derived types):
  *   every 2-D column field is declared (begc:endc, lb:ub) in Fortran, so
@@ -451,6 +453,10 @@ typedef struct {
      * src/biogeophys/SoilFluxesMod.F90:399-445) and keeps their maxima over
      * the steps after the first skip_steps (BalanceCheckMod.F90:91).       */
     int32_t balance, skip_steps;
+    /* soilfluxes = 1 (with_canopy, order 1) runs SoilFluxes between
+     * SoilTemperature and SoilWater as the driver does (clm_driver.F90:921);
+     * sf (ctsmg_batch_create3) then carries its components.               */
+    int32_t soilfluxes;
 } ctsmg_batch_config;
 
 /* cio/rootr/medlyn*_p may be NULL when with_canopy = 0.  rootr is (p, 1:nlevsoi)
@@ -460,6 +466,15 @@ int32_t ctsmg_batch_create2(ctsmg_batch* out, const ctsmg_batch_config* cfg, con
                             const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio, const double* rootr,
                             const double* medlynslope_p, const double* medlynintercept_p,
                             const ctsmg_canopy_params* cpar, const ctsmg_pftcon* pft);
+/* As ctsmg_batch_create2, plus the SoilFluxes components when cfg->soilfluxes
+ * (sf->tssbef / t_h2osfc_bef are filled by the step itself).               */
+int32_t ctsmg_batch_create3(ctsmg_batch* out, const ctsmg_batch_config* cfg, const ctsmg_soilwater_io* sw,
+                            const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio, const ctsmg_soilfluxes_io* sf,
+                            const double* rootr, const double* medlynslope_p, const double* medlynintercept_p,
+                            const ctsmg_canopy_params* cpar, const ctsmg_pftcon* pft);
+/* As ctsmg_batch_download2, plus the SoilFluxes components (sf may be NULL). */
+int32_t ctsmg_batch_download3(ctsmg_batch b, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
+                              const ctsmg_canopy_io* cio, const ctsmg_soilfluxes_io* sf);
 int32_t ctsmg_batch_create(ctsmg_batch* out, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
                            int32_t ncol, int32_t npatch, double dtime, double e_ice,
                            int32_t snow_thermal_cond_method);

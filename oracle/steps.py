@@ -14,10 +14,13 @@ def _p(a, t=C.c_double):
     return a.ctypes.data_as(C.POINTER(t))
 
 
-def full_steps(A, npatch, ngrid, rootr, nsteps, medlyn_per_patch=False, method=1, itmax=40, snow_method=0):
-    """nsteps x (CanopyFluxes, root sink, SoilTemperature, SoilWater, h2osoi_vol
-    refresh) in place on A.  displa / z0mv keep their SatellitePhenology values
-    and cgrnds / cgrndl restart from zero every step."""
+def full_steps(A, npatch, ngrid, rootr, nsteps, medlyn_per_patch=False, method=1, itmax=40, snow_method=0,
+               soilfluxes=False):
+    """nsteps x (CanopyFluxes, root sink, SoilTemperature, [SoilFluxes,]
+    SoilWater, h2osoi_vol refresh) in place on A.  displa / z0mv keep their
+    SatellitePhenology values and cgrnds / cgrndl restart from zero every
+    step; with soilfluxes the temperatures before SoilTemperature go to
+    tssbef / t_h2osfc_bef."""
     L = orc.lib()
     ncol = A["zwt"].shape[0]
     L.oracle_set_canopy_params(C.byref(canopy_inputs.make_params()), C.byref(canopy_inputs.make_pftcon()), method,
@@ -41,8 +44,15 @@ def full_steps(A, npatch, ngrid, rootr, nsteps, medlyn_per_patch=False, method=1
             assert rc == 0, (rc, e.value)
             L.oracle_rootsink(ncol, npatch, _p(A["col_patchi"], C.c_int32), _p(A["col_npatches"], C.c_int32),
                               _p(A["wtcol"]), _p(A["qflx_tran_veg"]), _p(rootr), _p(A["qflx_rootsoi"]))
+            if soilfluxes:
+                A["tssbef"][:] = A["t_soisno"]
+                A["t_h2osfc_bef"][:] = A["t_h2osfc"]
             st = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, A, ncol, npatch)
             assert L.oracle_soiltemperature(C.byref(b), ncol, _p(filt_c, C.c_int32), C.byref(st), DT, snow_method) == 0
+            if soilfluxes:
+                sf = abi.make_io(abi.SoilFluxesIO, abi.SOILFLUXES_FIELDS, A, ncol, npatch)
+                assert L.oracle_soilfluxes(C.byref(b), ncol, _p(filt_c, C.c_int32), npatch, _p(filt_p, C.c_int32),
+                                           C.byref(sf), DT) == 0
             sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS, A, ncol)
             assert L.oracle_soilwater(C.byref(b), ncol, _p(filt_c, C.c_int32), C.byref(sw), 6.0, DT) == 0
             inputs.refresh_h2osoi_vol(A)

@@ -78,3 +78,32 @@ def test_member_alone_equals_member_in_ensemble(gpu_lib):
     for k in ("t_soisno", "h2osoi_liq", "t_veg", "psnsun", "qcharge"):
         g = G[k][..., cols] if G[k].shape[-1] == A["zwt"].shape[0] else G[k][..., pidx]
         np.testing.assert_array_equal(Gs[k], g)
+
+
+SF_OUT = ["eflx_soil_grnd", "eflx_sh_tot", "qflx_evap_tot", "eflx_lh_tot", "eflx_lwrad_out", "eflx_lwrad_net",
+          "qflx_liqevap_from_top_layer", "qflx_solidevap_from_top_layer", "eflx_lh_grnd"]
+
+
+def test_full_step_with_soilfluxes_matches_oracle(gpu_lib):
+    """Driver order with SoilFluxes between SoilTemperature and SoilWater
+    (clm_driver.F90:900,921,950) in the resident engine, against the oracle
+    stepped the same way."""
+    from ctsm_gb300.engine import SoilBatch
+    A, npatch, ngrid, rootr = fi.full_state(2500, seed=34)
+    fi.add_soilfluxes_fields(A, npatch, ngrid)
+    R = copy.deepcopy(A)
+    full_steps(R, npatch, ngrid, rootr, 3, soilfluxes=True)
+    G = copy.deepcopy(A)
+    b = SoilBatch(G, npatch, canopy=True, ngrid=ngrid, rootr=rootr, soilfluxes=True)
+    b.run(3)
+    b.sync()
+    b.download()
+    b.close()
+    spread = noise_spread(lambda B: full_steps(B, npatch, ngrid, rootr, 3, soilfluxes=True), A, R,
+                          fields=CANCEL + ("eflx_soil_grnd", "eflx_sh_tot", "eflx_lwrad_net"), input_ulps=4)
+    for k in ("liqcan", "snocan"):
+        spread[k] = spread[k] + 1e-9 * (np.abs(A["liqcan"]) + np.abs(A["snocan"]))
+    errs, bad = compare(G, R, STATE + SF_OUT, 1e-9, spread)
+    assert not bad, {k: errs[k] for k in bad}
+    assert np.abs(G["errsoi_col"] - R["errsoi_col"]).max() < 1e-8
+    assert np.abs(G["errsoi_col"]).max() < 1e-5          # the reference's errsoi warning threshold
