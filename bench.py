@@ -77,6 +77,30 @@ def dist_setup():
     return ws, rank, local
 
 
+def rank_seed(seed, rank):
+    """Each rank advances its own shard of columns (weak scaling): same size,
+    its own draws."""
+    return seed + rank
+
+
+def max_over_ranks(x, ws, device):
+    """The slowest rank's time (the job's time); all_reduce on `device` (cuda
+    with NCCL, cpu with gloo)."""
+    if ws == 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(ws, units_per_rank, steps, t_max):
+    """Whole-job throughput: the units all ranks processed over the slowest
+    rank's time."""
+    return ws * units_per_rank * steps / t_max
+
+
 def make_inputs(ncol, seed):
     from ctsm_gb300 import inputs
     return inputs.soil_columns(ncol, seed=seed, snow=True, nbedrock=(3, 20))
@@ -356,7 +380,7 @@ def ours_arm(args, ws, rank, local):
     fp64 = C.c_double(0.0)
     L.ctsmg_measure_fp64_tflops(C.byref(fp64))
 
-    A, npatch = make_inputs(args.ncol, args.seed + rank)
+    A, npatch = make_inputs(args.ncol, rank_seed(args.seed, rank))
     ncol = args.ncol
     mean_snow = float(-A["snl"].mean())
 
@@ -382,13 +406,8 @@ def ours_arm(args, ws, rank, local):
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     ev_total_s = float(step_ms.sum()) / 1e3
-    t_rank = max(ev_total_s, 0.0)
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([t_rank], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_rank = float(t.item())
-    value = ws * ncol * args.steps / t_rank
+    t_rank = max_over_ranks(max(ev_total_s, 0.0), ws, "cuda")
+    value = job_value(ws, ncol, args.steps, t_rank)
     mean_launch_s = float(step_ms.mean()) / 1e3
 
     rd, wr = roofline.step_bytes_per_column(mean_snow, 1.0)
@@ -436,14 +455,9 @@ def ours_arm(args, ws, rank, local):
             soil.SoilWater(bnd, ncol, filt, H, DT)
             soil.SoilTemperature(bnd, ncol, filt, H, DT)
         barrier()
-        te = time.perf_counter() - t0
-        if ws > 1:
-            import torch.distributed as dist
-            t = torch.tensor([te], device="cuda", dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            te = float(t.item())
+        te = max_over_ranks(time.perf_counter() - t0, ws, "cuda")
         h2d, d2h = roofline.dropin_copy_bytes_per_column(1.0)
-        e2e = {"value": ws * ncol * ke / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d * ncol),
+        e2e = {"value": job_value(ws, ncol, ke, te), "unit": UNIT, "h2d_bytes_per_step": int(h2d * ncol),
                "d2h_bytes_per_step": int(d2h * ncol), "steps": ke, "ms_per_step": 1e3 * te / ke,
                "path": "ctsmg_soilwater + ctsmg_soiltemperature (plain drop-in, pinned host arrays)"}
 
