@@ -24,6 +24,7 @@ LEVELS = {
     "SN": (-NLEVSNO + 1, NLEVSNO),
     "PL": (-NLEVSNO + 1, NLEVSNO + 1),    # patch, snow levels + top soil
     "GR": (None, 1),                      # scalar per gridcell (1-D)
+    "PG": (1, NLEVGRND),                  # patch, soil + bedrock levels
 }
 
 F64, I32 = "f8", "i4"
@@ -128,6 +129,17 @@ SOILFLUXES_FIELDS = [
 ]
 
 
+# Root moisture stress (SoilMoistStressMod.F90:70-217, 312-435) as run at the
+# start of CanopyFluxes (CanopyFluxesMod.F90:709, 833-895).
+ROOTMOIST_FIELDS = [
+    ("h2osoi_liq", "SS", F64, "in"), ("h2osoi_ice", "SS", F64, "in"), ("dz", "SS", F64, "in"),
+    ("t_soisno", "SS", F64, "in"), ("watsat", "G", F64, "in"), ("sucsat", "G", F64, "in"), ("bsw", "G", F64, "in"),
+    ("eff_porosity", "G", F64, "out"), ("h2osoi_liqvol", "G", F64, "out"),
+    ("patch_column", "P", I32, "in"), ("itype", "P", I32, "in"), ("rootfr", "PG", F64, "in"),
+    ("btran", "P", F64, "out"), ("rootr", "PG", F64, "out"), ("rresis", "PG", F64, "inout"),
+]
+
+
 def _ptr_type(dtype):
     return C.POINTER(C.c_double) if dtype == F64 else C.POINTER(C.c_int32)
 
@@ -148,6 +160,11 @@ class SoilWaterParams(C.Structure):
 
 class SoilWaterIO(C.Structure):
     _fields_ = [("ldc", C.c_int32)] + [(n, _ptr_type(t)) for (n, _, t, _) in SOILWATER_FIELDS]
+
+
+class RootMoistIO(C.Structure):
+    _fields_ = [("ldc", C.c_int32), ("ldp", C.c_int32)] + \
+               [(n, _ptr_type(t)) for (n, _, t, _) in ROOTMOIST_FIELDS]
 
 
 class SoilFluxesIO(C.Structure):
@@ -176,7 +193,7 @@ MAX_PFT = 80
 class Pftcon(C.Structure):
     _fields_ = [("npft", C.c_int32)] + [(n, C.c_double * MAX_PFT) for n in (
         "c3psn", "slatop", "leafcn", "flnr", "fnitr", "dleaf", "medlynslope", "medlynintercept", "theta_cj",
-        "mbbopt")]
+        "mbbopt", "smpso", "smpsc")]
 
 
 class CanopyIO(C.Structure):
@@ -188,7 +205,7 @@ def field_shape(kind, ncol, npatch, ngrid=None):
     """numpy shape (levels, columns-or-patches) of a manifest field."""
     if kind == "GR":
         return (ngrid if ngrid is not None else ncol,)
-    n = npatch if kind in ("P", "PL") else ncol
+    n = npatch if kind in ("P", "PL", "PS", "PG") else ncol
     nlev = LEVELS[kind][1]
     return (n,) if kind in ("C", "P") else (nlev, n)
 

@@ -38,3 +38,21 @@ def CanopyFluxes(bounds, num_exposedvegp, filter_exposedvegp, state, dtime, ngri
     io = abi.make_io(abi.CanopyIO, abi.CANOPY_FIELDS, state, ncol, npat, ngrid, begg)
     check(L.ctsmg_canopyfluxes(C.byref(bounds), int(num_exposedvegp), f.ctypes.data_as(C.POINTER(C.c_int32)),
                                C.byref(io), float(dtime)))
+
+
+def RootMoistStress(bounds, num_exposedvegp, filter_exposedvegp, state):
+    """The root moisture stress CanopyFluxes computes before its iteration
+    (CanopyFluxesMod.F90:833-895 -> calc_root_moist_stress,
+    SoilMoistStressMod.F90:438-514): eff_porosity, h2osoi_liqvol, btran,
+    rootr and rresis of `state` are written."""
+    L = load()
+    if not getattr(L, "_rootmoist_bound", False):
+        L.ctsmg_root_moist_stress.argtypes = [C.POINTER(abi.Bounds), C.c_int32, C.POINTER(C.c_int32),
+                                              C.POINTER(abi.RootMoistIO)]
+        L._rootmoist_bound = True
+    f = np.ascontiguousarray(filter_exposedvegp, dtype=np.int32)
+    ncol = bounds.endc - bounds.begc + 1
+    npat = bounds.endp - bounds.begp + 1
+    io = abi.make_io(abi.RootMoistIO, abi.ROOTMOIST_FIELDS, state, ncol, npat)
+    check(L.ctsmg_root_moist_stress(C.byref(bounds), int(num_exposedvegp), f.ctypes.data_as(C.POINTER(C.c_int32)),
+                                    C.byref(io)))

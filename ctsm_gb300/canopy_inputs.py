@@ -45,10 +45,13 @@ DEFAULT_PARAMS = dict(
     fnr=7.16, act25=3.6 * 1000.0 / 60.0, theta_psii=0.7, theta_ip=0.95, tpu25ratio=0.167, kp25ratio=20000.0,
     fnps=0.15, leaf_mr_vcm=0.015, light_inhibit=1)
 
-# (c3psn, slatop, leafcn, flnr, fnitr, dleaf, medlynslope, medlynintercept, theta_cj, mbbopt)
+# (c3psn, slatop, leafcn, flnr, fnitr, dleaf, medlynslope, medlynintercept, theta_cj, mbbopt, smpso, smpsc);
+# smpso / smpsc (soil water potential at full stomatal opening / closure, mm)
+# are the builder's choice for grasses: the parameter file is not in the
+# repository.
 DEFAULT_PFT = [
-    (1.0, 0.030, 25.0, 0.09, 0.90, 0.04, 4.45, 100.0, 0.9393, 9.0),   # C3
-    (0.0, 0.050, 25.0, 0.09, 0.80, 0.04, 1.62, 100.0, 0.80, 4.0),     # C4
+    (1.0, 0.030, 25.0, 0.09, 0.90, 0.04, 4.45, 100.0, 0.9393, 9.0, -74000.0, -275000.0),   # C3
+    (0.0, 0.050, 25.0, 0.09, 0.80, 0.04, 1.62, 100.0, 0.80, 4.0, -74000.0, -275000.0),     # C4
 ]
 
 
@@ -67,7 +70,7 @@ def make_pftcon(rows=None):
     f = abi.Pftcon()
     f.npft = len(rows)
     names = ["c3psn", "slatop", "leafcn", "flnr", "fnitr", "dleaf", "medlynslope", "medlynintercept", "theta_cj",
-             "mbbopt"]
+             "mbbopt", "smpso", "smpsc"]
     for i, row in enumerate(rows):
         for n, v in zip(names, row):
             getattr(f, n)[i] = v

@@ -16,6 +16,7 @@
 #include "soil_kernels.cuh"
 #include "canopy_kernels.cuh"
 #include "soilfluxes_kernels.cuh"
+#include "rootmoist_kernels.cuh"
 #include "capi_internal.h"
 
 namespace ctsmg {
@@ -130,7 +131,7 @@ int kind_levels(int kind) {
         case K_C: case K_P: case K_GR: return 1;
         case K_SS: return NLEVSNO + NLEVGRND;
         case K_ZI: return NLEVSNO + NLEVGRND + 1;
-        case K_G: return NLEVGRND;
+        case K_G: case K_PG: return NLEVGRND;
         case K_S: case K_PS: return NLEVSOI;
         case K_SN: return NLEVSNO;
         case K_PL: return NLEVSNO + 1;
@@ -182,6 +183,26 @@ const FieldDesc SOILTEMP_TABLE[] = {
 const int SOILTEMP_NFIELDS = sizeof(SOILTEMP_TABLE) / sizeof(SOILTEMP_TABLE[0]);
 
 #define FC(name, kind, esz, use) FW(ctsmg_canopy_io, name, kind, esz, use)
+#define FR(name, kind, esz, use) FW(ctsmg_rootmoist_io, name, kind, esz, use)
+const FieldDesc ROOTMOIST_TABLE[] = {
+    FR(h2osoi_liq, K_SS, 8, U_IN),
+    FR(h2osoi_ice, K_SS, 8, U_IN),
+    FR(dz, K_SS, 8, U_IN),
+    FR(t_soisno, K_SS, 8, U_IN),
+    FR(watsat, K_G, 8, U_IN),
+    FR(sucsat, K_G, 8, U_IN),
+    FR(bsw, K_G, 8, U_IN),
+    FR(eff_porosity, K_G, 8, U_OUT),
+    FR(h2osoi_liqvol, K_G, 8, U_OUT),
+    FR(patch_column, K_P, 4, U_IN),
+    FR(itype, K_P, 4, U_IN),
+    FR(rootfr, K_PG, 8, U_IN),
+    FR(btran, K_P, 8, U_OUT),
+    FR(rootr, K_PG, 8, U_OUT),
+    FR(rresis, K_PG, 8, U_INOUT),
+};
+const int ROOTMOIST_NFIELDS = sizeof(ROOTMOIST_TABLE) / sizeof(ROOTMOIST_TABLE[0]);
+
 #define FF(name, kind, esz, use) FW(ctsmg_soilfluxes_io, name, kind, esz, use)
 const FieldDesc SOILFLUXES_TABLE[] = {
     FF(snl, K_C, 4, U_IN),
@@ -368,7 +389,7 @@ static inline void*& field_ptr(void* io, const FieldDesc& f) {
 }
 
 size_t field_bytes(const FieldDesc& f, int ldc, int ldp, int ldg) {
-    int ld = (f.kind == K_P || f.kind == K_PL || f.kind == K_PS) ? ldp : (f.kind == K_GR ? ldg : ldc);
+    int ld = (f.kind == K_P || f.kind == K_PL || f.kind == K_PS || f.kind == K_PG) ? ldp : (f.kind == K_GR ? ldg : ldc);
     return (size_t)ld * kind_levels(f.kind) * f.esize;
 }
 
@@ -468,7 +489,7 @@ static cudaError_t copy_slice(const FieldDesc& f, void* dst, const void* src, in
                              w, kind_levels(f.kind), kind, s);
 }
 
-static bool patch_field(const FieldDesc& f) { return f.kind == K_P || f.kind == K_PL || f.kind == K_PS; }
+static bool patch_field(const FieldDesc& f) { return f.kind == K_P || f.kind == K_PL || f.kind == K_PS || f.kind == K_PG; }
 
 // Device copies of every component (arena), no data moved yet.
 static void stage_alloc(ThreadCtx* c, const void* hio, void* dio, size_t io_size, const FieldDesc* tab, int nf,
@@ -838,3 +859,45 @@ extern "C" int32_t ctsmg_soilfluxes(const ctsmg_bounds* bounds, int32_t num_nola
     if (e != cudaSuccess) return cuda_fail(e, "soilfluxes");
     return 0;
 }
+
+extern "C" int32_t ctsmg_root_moist_stress(const ctsmg_bounds* bounds, int32_t num_exposedvegp,
+                                           const int32_t* filter_exposedvegp, const ctsmg_rootmoist_io* io) {
+    ThreadCtx* c;
+    int rc = ctx_get(&c);
+    if (rc) return rc;
+    if (!io) return set_error(CTSMG_E_ARG, "null io", 0, 0);
+    if (!g_cpar_set) return set_error(CTSMG_E_NOT_INIT, "ctsmg_set_canopy_params has not been called", 0, 0);
+    if (!bounds || bounds->endp < bounds->begp || bounds->endc < bounds->begc)
+        return set_error(CTSMG_E_ARG, "bad bounds", 0, 0);
+    if (num_exposedvegp < 0 || (num_exposedvegp > 0 && !filter_exposedvegp))
+        return set_error(CTSMG_E_ARG, "bad patch filter", 0, 0);
+    const int ncol = bounds->endc - bounds->begc + 1, npat = bounds->endp - bounds->begp + 1;
+    if (io->ldc < ncol || io->ldp < npat) return set_error(CTSMG_E_ARG, "ldc/ldp smaller than the bounds", 0, 0);
+    ctsmg_pftcon pft;
+    { std::lock_guard<std::mutex> lk(g_mu); pft = g_pft; }
+    for (int i = 0; i < num_exposedvegp; ++i) {
+        const int pg = filter_exposedvegp[i];
+        if (pg < bounds->begp || pg > bounds->endp) return set_error(CTSMG_E_ARG, "filter index outside bounds", pg, 0);
+        const int p = pg - bounds->begp;
+        const int cc = io->patch_column[p], it = io->itype[p];
+        if (cc < bounds->begc || cc > bounds->endc) return set_error(CTSMG_E_ARG, "patch column outside bounds", pg, 0);
+        if (it < 0 || it >= pft.npft) return set_error(CTSMG_E_ARG, "patch itype outside pftcon", pg, 0);
+    }
+    if (num_exposedvegp == 0) return 0;
+    const int ldc = io->ldc, ldp = io->ldp;
+    size_t need = table_bytes(ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, ldc, ldp) + (size_t)num_exposedvegp * 4 + 4096;
+    if ((rc = arena_reserve(c, need))) return rc;
+    ctsmg_rootmoist_io dio;
+    if ((rc = stage_in(c, io, &dio, sizeof dio, ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, ldc, ldp))) return rc;
+    int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_exposedvegp * 4);
+    cudaError_t e = cudaMemcpyAsync(dfilt, filter_exposedvegp, (size_t)num_exposedvegp * 4, cudaMemcpyHostToDevice,
+                                    c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
+    e = launch_rootmoist(dio, pft, bounds->begc, bounds->begp, num_exposedvegp, dfilt, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "root moisture stress kernel launch");
+    if ((rc = stage_out(c, io, &dio, ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, ldc, ldp))) return rc;
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "root moisture stress");
+    return 0;
+}
+

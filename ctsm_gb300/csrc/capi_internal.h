@@ -5,7 +5,7 @@
 #include "ctsm_gpu.h"
 
 namespace ctsmg {
-enum Kind { K_C, K_P, K_SS, K_ZI, K_G, K_S, K_SN, K_PL, K_GR, K_PS };
+enum Kind { K_C, K_P, K_SS, K_ZI, K_G, K_S, K_SN, K_PL, K_GR, K_PS, K_PG };
 enum Use { U_IN, U_OUT, U_INOUT };
 struct FieldDesc { size_t offset; int kind; int esize; int use; const char* name; };
 
@@ -15,6 +15,8 @@ extern const FieldDesc SOILTEMP_TABLE[];
 extern const int SOILTEMP_NFIELDS;
 extern const FieldDesc CANOPY_TABLE[];
 extern const int CANOPY_NFIELDS;
+extern const FieldDesc ROOTMOIST_TABLE[];
+extern const int ROOTMOIST_NFIELDS;
 extern const FieldDesc SOILFLUXES_TABLE[];
 extern const int SOILFLUXES_NFIELDS;
 

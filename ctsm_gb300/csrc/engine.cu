@@ -15,6 +15,7 @@
 #include "soil_kernels.cuh"
 #include "canopy_kernels.cuh"
 #include "balance_kernels.cuh"
+#include "rootmoist_kernels.cuh"
 #include "capi_internal.h"
 
 namespace ctsmg {
@@ -34,6 +35,7 @@ struct Batch {
     ctsmg_soilwater_io dsw{};
     ctsmg_soiltemp_io dst{};
     ctsmg_soilfluxes_io dsf{};
+    ctsmg_rootmoist_io drm{};
     CanopyArgs cargs{};
     double* rootr = nullptr;
     double* mslope = nullptr;
@@ -72,11 +74,15 @@ static cudaError_t enqueue_step(Batch* b) {
         e = launch_prestep(b->dst, ncol, b->bal, b->stream);
         if (e != cudaSuccess) return e;
     }
+    if (b->cfg.rootmoist) {
+        e = launch_rootmoist(b->drm, b->cargs.pft, 1, 1, b->cfg.npatch, nullptr, b->stream);
+        if (e != cudaSuccess) return e;
+    }
     if (b->cfg.with_canopy) {
         e = launch_canopy(b->cargs, b->cfg.npatch, nullptr, b->cfg.dtime, b->counter, b->err, b->cws, b->stream);
         if (e != cudaSuccess || b->cfg.order == 2) return e;
         e = launch_rootsink(b->dst.col_patchi, b->dst.col_npatches, b->dst.wtcol, b->cargs.io.qflx_tran_veg,
-                            b->rootr, b->cfg.npatch, (double*)b->dsw.qflx_rootsoi, ncol, b->stream);
+                            b->cfg.rootmoist ? b->drm.rootr : b->rootr, b->cfg.npatch, (double*)b->dsw.qflx_rootsoi, ncol, b->stream);
         if (e != cudaSuccess) return e;
     }
     e = launch_soilstep(b->dsw, b->dst, ncol, b->cfg.e_ice, b->cfg.dtime, b->cfg.snow_thermal_cond_method, b->ws,
@@ -114,7 +120,7 @@ static void batch_free(Batch* b) {
     delete b;
 }
 
-static bool is_column_kind(int k) { return !(k == K_P || k == K_PL || k == K_PS || k == K_GR); }
+static bool is_column_kind(int k) { return !(k == K_P || k == K_PL || k == K_PS || k == K_PG || k == K_GR); }
 
 } // namespace ctsmg
 
@@ -122,11 +128,18 @@ using namespace ctsmg;
 
 struct ctsmg_batch_s { Batch* b; };
 
-extern "C" int32_t ctsmg_batch_create3(ctsmg_batch* out, const ctsmg_batch_config* cfg, const ctsmg_soilwater_io* sw,
-                                       const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio,
-                                       const ctsmg_soilfluxes_io* sf, const double* rootr,
-                                       const double* medlynslope_p, const double* medlynintercept_p,
-                                       const ctsmg_canopy_params* cpar, const ctsmg_pftcon* pft) {
+extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* cfg, const ctsmg_batch_inputs* in) {
+    if (!in) return set_error(CTSMG_E_ARG, "null inputs", 0, 0);
+    const ctsmg_soilwater_io* sw = in->sw;
+    const ctsmg_soiltemp_io* st = in->st;
+    const ctsmg_canopy_io* cio = in->cio;
+    const ctsmg_soilfluxes_io* sf = in->sf;
+    const ctsmg_rootmoist_io* rm = in->rm;
+    const double* rootr = in->rootr;
+    const double* medlynslope_p = in->medlynslope_p;
+    const double* medlynintercept_p = in->medlynintercept_p;
+    const ctsmg_canopy_params* cpar = in->cpar;
+    const ctsmg_pftcon* pft = in->pft;
     const bool canopy_only = cfg && cfg->order == 2;
     if (!out || !cfg || (!canopy_only && (!sw || !st))) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
     const int ncol = cfg->ncol, npatch = cfg->npatch;
@@ -140,8 +153,12 @@ extern "C" int32_t ctsmg_batch_create3(ctsmg_batch* out, const ctsmg_batch_confi
         return set_error(CTSMG_E_ARG, "soilfluxes needs with_canopy, order 1 and the SoilFluxes components", 0, 0);
     if (cfg->soilfluxes && (sf->ldc != ncol || sf->ldp != npatch))
         return set_error(CTSMG_E_ARG, "SoilFluxes arrays must be dense: ldc = ncol, ldp = npatch", 0, 0);
+    if (cfg->rootmoist && (!cfg->with_canopy || !rm))
+        return set_error(CTSMG_E_ARG, "rootmoist needs with_canopy and the root moisture stress components", 0, 0);
+    if (cfg->rootmoist && (rm->ldc != ncol || rm->ldp != npatch))
+        return set_error(CTSMG_E_ARG, "root moisture stress arrays must be dense: ldc = ncol, ldp = npatch", 0, 0);
     if (cfg->with_canopy) {
-        if (!cio || (!rootr && !canopy_only) || !cpar || !pft)
+        if (!cio || (!rootr && !canopy_only && !cfg->rootmoist) || !cpar || !pft)
             return set_error(CTSMG_E_ARG, "with_canopy needs cio, rootr, params", 0, 0);
         if (cio->ldc != ncol || cio->ldp != npatch || cio->ldg != cfg->ngrid || cio->begg != 1)
             return set_error(CTSMG_E_ARG, "canopy arrays must be dense (ldg = ngrid, begg = 1)", 0, 0);
@@ -239,7 +256,10 @@ extern "C" int32_t ctsmg_batch_create3(ctsmg_batch* out, const ctsmg_batch_confi
         b->cargs.begp = 1;
         b->cargs.engine = 1;
         const size_t pb = (size_t)npatch * 8;
-        if (!canopy_only) {
+        if (cfg->rootmoist) {
+            std::memcpy(&b->drm, rm, sizeof b->drm);
+            if ((rc = add(ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, rm, &b->drm))) return fail(rc);
+        } else if (!canopy_only) {
             if ((e = cudaMalloc(&b->rootr, pb * NLEVSOI)) != cudaSuccess) return fail(cuda_err(e, "rootr"));
             if ((e = cudaMemcpy(b->rootr, rootr, pb * NLEVSOI, cudaMemcpyHostToDevice)) != cudaSuccess)
                 return fail(cuda_err(e, "rootr"));
@@ -289,6 +309,16 @@ extern "C" int32_t ctsmg_batch_create3(ctsmg_batch* out, const ctsmg_batch_confi
     return 0;
 }
 
+extern "C" int32_t ctsmg_batch_create3(ctsmg_batch* out, const ctsmg_batch_config* cfg, const ctsmg_soilwater_io* sw,
+                                       const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio,
+                                       const ctsmg_soilfluxes_io* sf, const double* rootr,
+                                       const double* medlynslope_p, const double* medlynintercept_p,
+                                       const ctsmg_canopy_params* cpar, const ctsmg_pftcon* pft) {
+    if (cfg && cfg->rootmoist) return set_error(CTSMG_E_ARG, "rootmoist needs ctsmg_batch_open", 0, 0);
+    const ctsmg_batch_inputs in = {sw, st, cio, sf, nullptr, rootr, medlynslope_p, medlynintercept_p, cpar, pft};
+    return ctsmg_batch_open(out, cfg, &in);
+}
+
 extern "C" int32_t ctsmg_batch_create2(ctsmg_batch* out, const ctsmg_batch_config* cfg, const ctsmg_soilwater_io* sw,
                                        const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio, const double* rootr,
                                        const double* medlynslope_p, const double* medlynintercept_p,
@@ -306,7 +336,7 @@ extern "C" int32_t ctsmg_batch_create(ctsmg_batch* out, const ctsmg_soilwater_io
     cfg.snow_thermal_cond_method = snow_thermal_cond_method;
     cfg.stomatalcond_method = 1; cfg.itmax_canopy_fluxes = 40;
     cfg.order = 0; cfg.with_canopy = 0; cfg.bucket = 1;
-    cfg.balance = 0; cfg.skip_steps = 0; cfg.soilfluxes = 0;
+    cfg.balance = 0; cfg.skip_steps = 0; cfg.soilfluxes = 0; cfg.rootmoist = 0;
     return ctsmg_batch_create2(out, &cfg, sw, st, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
 }
 
@@ -367,6 +397,13 @@ static int download_table(Batch* b, const FieldDesc* tab, int nf, const void* hi
         }
     }
     return 0;
+}
+
+extern "C" int32_t ctsmg_batch_fetch(ctsmg_batch bh, const ctsmg_batch_inputs* in) {
+    if (!bh || !in) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
+    int rc = ctsmg_batch_download3(bh, in->sw, in->st, in->cio, in->sf);
+    if (rc || !in->rm || !bh->b->cfg.rootmoist) return rc;
+    return download_table(bh->b, ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, in->rm);
 }
 
 extern "C" int32_t ctsmg_batch_download3(ctsmg_batch bh, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,

@@ -113,7 +113,7 @@ static void* fptr(const void* io, const FieldDesc& f) {
 static void set_fptr(void* io, const FieldDesc& f, void* p) {
     *reinterpret_cast<void**>(reinterpret_cast<char*>(io) + f.offset) = p;
 }
-static bool patch_kind(int k) { return k == K_P || k == K_PL || k == K_PS; }
+static bool patch_kind(int k) { return k == K_P || k == K_PL || k == K_PS || k == K_PG; }
 
 // Capacity (leading dimension) and first position of a field's kind.
 static int kind_cap(const Pool* P, int k) {

@@ -31,6 +31,8 @@ def _bind(L):
     L.ctsmg_batch_download3.argtypes = [C.c_void_p, P(abi.SoilWaterIO), P(abi.SoilTempIO), P(abi.CanopyIO),
                                         P(abi.SoilFluxesIO)]
     L.ctsmg_batch_balance.argtypes = [C.c_void_p] + [P(C.c_double)] * 4
+    L.ctsmg_batch_open.argtypes = [P(C.c_void_p), P(BatchConfig), P(BatchInputs)]
+    L.ctsmg_batch_fetch.argtypes = [C.c_void_p, P(BatchInputs)]
     L._batch_bound = True
 
 
@@ -42,7 +44,20 @@ class BatchConfig(C.Structure):
     _fields_ = [("ncol", C.c_int32), ("npatch", C.c_int32), ("ngrid", C.c_int32), ("dtime", C.c_double),
                 ("e_ice", C.c_double), ("snow_thermal_cond_method", C.c_int32), ("stomatalcond_method", C.c_int32),
                 ("itmax_canopy_fluxes", C.c_int32), ("order", C.c_int32), ("with_canopy", C.c_int32),
-                ("bucket", C.c_int32), ("balance", C.c_int32), ("skip_steps", C.c_int32), ("soilfluxes", C.c_int32)]
+                ("bucket", C.c_int32), ("balance", C.c_int32), ("skip_steps", C.c_int32), ("soilfluxes", C.c_int32),
+                ("rootmoist", C.c_int32)]
+
+
+class BatchInputs(C.Structure):
+    _fields_ = [("sw", C.POINTER(abi.SoilWaterIO)), ("st", C.POINTER(abi.SoilTempIO)),
+                ("cio", C.POINTER(abi.CanopyIO)), ("sf", C.POINTER(abi.SoilFluxesIO)),
+                ("rm", C.POINTER(abi.RootMoistIO)), ("rootr", C.POINTER(C.c_double)),
+                ("medlynslope_p", C.POINTER(C.c_double)), ("medlynintercept_p", C.POINTER(C.c_double)),
+                ("cpar", C.POINTER(abi.CanopyParams)), ("pft", C.POINTER(abi.Pftcon))]
+
+
+def _pt(x):
+    return None if x is None else C.pointer(x)
 
 
 class SoilBatch:
@@ -55,7 +70,7 @@ class SoilBatch:
     def __init__(self, state, npatch, dtime=1800.0, e_ice=6.0, snow_thermal_cond_method=0, canopy=False,
                  ngrid=None, rootr=None, order=None, bucket=True, stomatalcond_method=1, itmax=40,
                  params=None, pftcon=None, per_patch_medlyn=False, balance=False, skip_steps=None,
-                 soilfluxes=False):
+                 soilfluxes=False, rootmoist=False):
         from . import canopy_inputs
         self.L = load()
         _bind(self.L)
@@ -75,8 +90,10 @@ class SoilBatch:
         cfg = BatchConfig(self.ncol, npatch, self.ngrid, dtime, e_ice, snow_thermal_cond_method, stomatalcond_method,
                           itmax, (1 if canopy else 0) if order is None else order, 1 if canopy else 0,
                           1 if bucket else 0, 1 if balance else 0,
-                          _skip(dtime) if skip_steps is None else skip_steps, 1 if soilfluxes else 0)
+                          _skip(dtime) if skip_steps is None else skip_steps, 1 if soilfluxes else 0,
+                          1 if rootmoist else 0)
         self.soilfluxes = soilfluxes
+        self.rootmoist = rootmoist
         self.h = C.c_void_p()
         if canopy:
             self._ci = abi.make_io(abi.CanopyIO, abi.CANOPY_FIELDS, state, self.ncol, npatch, self.ngrid, 1)
@@ -88,10 +105,12 @@ class SoilBatch:
             self._rootr = None if rootr is None else np.ascontiguousarray(rootr, dtype=np.float64)
             self._sf = abi.make_io(abi.SoilFluxesIO, abi.SOILFLUXES_FIELDS, state, self.ncol, npatch) \
                 if soilfluxes else None
-            check(self.L.ctsmg_batch_create3(C.byref(self.h), C.byref(cfg), _ref(self._sw), _ref(self._st),
-                                             C.byref(self._ci), _ref(self._sf),
-                                             None if self._rootr is None else self._rootr.ctypes.data_as(dp), ms,
-                                             mi, C.byref(self._par), C.byref(self._pft)))
+            self._rm = abi.make_io(abi.RootMoistIO, abi.ROOTMOIST_FIELDS, state, self.ncol, npatch) \
+                if rootmoist else None
+            self._in = BatchInputs(_pt(self._sw), _pt(self._st), C.pointer(self._ci), _pt(self._sf), _pt(self._rm),
+                                   None if self._rootr is None else self._rootr.ctypes.data_as(dp), ms, mi,
+                                   C.pointer(self._par), C.pointer(self._pft))
+            check(self.L.ctsmg_batch_open(C.byref(self.h), C.byref(cfg), C.byref(self._in)))
         else:
             check(self.L.ctsmg_batch_create2(C.byref(self.h), C.byref(cfg), C.byref(self._sw), C.byref(self._st),
                                              None, None, None, None, None, None))
@@ -118,7 +137,10 @@ class SoilBatch:
             ci = abi.make_io(abi.CanopyIO, abi.CANOPY_FIELDS, st, self.ncol, self.npatch, self.ngrid, 1)
             sf = abi.make_io(abi.SoilFluxesIO, abi.SOILFLUXES_FIELDS, st, self.ncol, self.npatch) \
                 if self.soilfluxes else None
-            check(self.L.ctsmg_batch_download3(self.h, _ref(sw), _ref(tt), C.byref(ci), _ref(sf)))
+            rm = abi.make_io(abi.RootMoistIO, abi.ROOTMOIST_FIELDS, st, self.ncol, self.npatch) \
+                if self.rootmoist else None
+            check(self.L.ctsmg_batch_fetch(self.h, C.byref(BatchInputs(_pt(sw), _pt(tt), C.pointer(ci), _pt(sf),
+                                                                       _pt(rm), None, None, None, None, None))))
         else:
             check(self.L.ctsmg_batch_download(self.h, C.byref(sw), C.byref(tt)))
         return st

@@ -160,3 +160,20 @@ def add_soilfluxes_fields(A, npatch, ngrid):
         if n not in A:
             A[n] = np.zeros(abi.field_shape(kind, ncol, npatch, ngrid), dtype=np.dtype(t))
     return A
+
+
+def add_rootmoist_fields(A, npatch, rootr, rng=None):
+    """Root fractions (levels 1..nlevgrnd, zero below nlevsoi as
+    RootBiophysMod leaves them) and zero-filled stress outputs.  rootfr is the
+    state's nlevsoi root profile, jittered per patch when rng is given."""
+    ncol = A["zwt"].shape[0]
+    fr = np.zeros((abi.NLEVGRND, npatch))
+    fr[:abi.NLEVSOI] = rootr[:, :npatch]
+    if rng is not None:
+        fr[:abi.NLEVSOI] *= rng.uniform(0.5, 1.5, (abi.NLEVSOI, npatch))
+        fr /= fr.sum(axis=0, keepdims=True)
+    A["rootfr"] = np.ascontiguousarray(fr)
+    for (n, kind, t, u) in abi.ROOTMOIST_FIELDS:
+        if n not in A:
+            A[n] = np.zeros(abi.field_shape(kind, ncol, npatch, ncol), dtype=np.dtype(t))
+    return A

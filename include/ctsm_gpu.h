@@ -25,6 +25,7 @@
  *     [S ] (c, 1 : nlevsoi)             hydrologically active levels
  *     [SN] (c, -nlevsno+1 : 0)          snow levels only
  *     [PL] (p, -nlevsno+1 : 1)          patch snow levels + top soil (sabg_lyr)
+ *     [PG] (p, 1 : nlevgrnd)            patch soil + bedrock levels (rootfr, rootr)
  *   Filters are the reference's 1-based global indices (filter_hydrologyc(fc)
  *   holds c with begc <= c <= endc).
  *
@@ -238,7 +239,9 @@ typedef struct {
 
 /* pftcon arrays used on the path, indexed by patch%itype (0 .. npft-1)
  * (src/main/pftconMod.F90): c3psn, slatop, leafcn, flnr, fnitr, dleaf,
- * medlynslope, medlynintercept, mbbopt and Photosynthesis' theta_cj.     */
+ * medlynslope, medlynintercept, mbbopt, Photosynthesis' theta_cj, and the
+ * soil water potentials at full stomatal opening / closure smpso, smpsc (mm)
+ * of the root moisture stress.                                            */
 #define CTSMG_MAX_PFT 80
 typedef struct {
     int32_t npft;
@@ -246,6 +249,7 @@ typedef struct {
     double flnr[CTSMG_MAX_PFT], fnitr[CTSMG_MAX_PFT], dleaf[CTSMG_MAX_PFT];
     double medlynslope[CTSMG_MAX_PFT], medlynintercept[CTSMG_MAX_PFT], theta_cj[CTSMG_MAX_PFT];
     double mbbopt[CTSMG_MAX_PFT];
+    double smpso[CTSMG_MAX_PFT], smpsc[CTSMG_MAX_PFT];
 } ctsmg_pftcon;
 
 /* Components CanopyFluxes reads and writes on the natural-vegetation,
@@ -327,6 +331,39 @@ int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds,
  * over the exposed-vegetation patch filter (1-based patch indices).       */
 int32_t ctsmg_canopyfluxes(const ctsmg_bounds* bounds, int32_t num_exposedvegp,
                            const int32_t* filter_exposedvegp, const ctsmg_canopy_io* io, double dtime);
+
+/* ---------------------------------------------------------------- root moisture stress */
+/* The first part of CanopyFluxes' setup (src/biogeophys/CanopyFluxesMod.F90:
+ * 709, 833-895): effective porosity and volumetric liquid water of the soil
+ * levels (SoilMoistStressMod.F90:70-114, 171-217) and the default root
+ * moisture stress (calc_root_moist_stress_clm45default, :312-435, with the
+ * Clapp-Hornberger suction): btran and the effective root fractions rootr
+ * that the root water sink uses.  [PG] = (p, 1:nlevgrnd).  The reference runs
+ * it inside CanopyFluxes; here it is its own call, made right before
+ * ctsmg_canopyfluxes, which takes btran as an input.                      */
+typedef struct {
+    int32_t ldc, ldp;
+    const double*  h2osoi_liq;       /* [SS]                                    */
+    const double*  h2osoi_ice;       /* [SS]                                    */
+    const double*  dz;               /* [SS]                                    */
+    const double*  t_soisno;         /* [SS]                                    */
+    const double*  watsat;           /* [G]                                     */
+    const double*  sucsat;           /* [G]                                     */
+    const double*  bsw;              /* [G]                                     */
+    double*        eff_porosity;     /* [G]  out                                */
+    double*        h2osoi_liqvol;    /* [G]  out                                */
+    const int32_t* patch_column;     /* (p)  1-based (begc)                     */
+    const int32_t* itype;            /* (p)                                     */
+    const double*  rootfr;           /* [PG] root fraction                      */
+    double*        btran;            /* (p)  out: transpiration wetness factor  */
+    double*        rootr;            /* [PG] out: effective root fraction       */
+    double*        rresis;           /* [PG] inout: root soil water stress      */
+} ctsmg_rootmoist_io;
+
+/* calc_root_moist_stress for the exposed-vegetation patch filter (pftcon
+ * smpso / smpsc from ctsmg_set_canopy_params).                             */
+int32_t ctsmg_root_moist_stress(const ctsmg_bounds* bounds, int32_t num_exposedvegp,
+                                const int32_t* filter_exposedvegp, const ctsmg_rootmoist_io* io);
 
 /* ---------------------------------------------------------------- SoilFluxes */
 /* Components SoilFluxes reads and writes for natural-vegetation columns and
@@ -457,7 +494,32 @@ typedef struct {
      * SoilTemperature and SoilWater as the driver does (clm_driver.F90:921);
      * sf (ctsmg_batch_create3) then carries its components.               */
     int32_t soilfluxes;
+    /* rootmoist = 1 (with_canopy) computes btran and rootr from the resident
+     * soil state at the start of every step, as CanopyFluxes does before its
+     * iteration (src/biogeophys/CanopyFluxesMod.F90:833-895); the root sink
+     * then uses that rootr.  The inputs' rm carries the components.       */
+    int32_t rootmoist;
 } ctsmg_batch_config;
+
+/* Everything a batch can hold, in one struct (NULL = not used).           */
+typedef struct {
+    const ctsmg_soilwater_io* sw;
+    const ctsmg_soiltemp_io* st;
+    const ctsmg_canopy_io* cio;
+    const ctsmg_soilfluxes_io* sf;
+    const ctsmg_rootmoist_io* rm;
+    const double* rootr;                 /* (p, 1:nlevsoi), ldp = npatch; unused with rootmoist */
+    const double* medlynslope_p;
+    const double* medlynintercept_p;
+    const ctsmg_canopy_params* cpar;
+    const ctsmg_pftcon* pft;
+} ctsmg_batch_inputs;
+
+/* Create a batch from `in` (the arrays are copied); ctsmg_batch_create*
+ * are shorthands for it.  ctsmg_batch_fetch copies the state the steps
+ * write back into every table `in` names, in the caller's column order.   */
+int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* cfg, const ctsmg_batch_inputs* in);
+int32_t ctsmg_batch_fetch(ctsmg_batch b, const ctsmg_batch_inputs* in);
 
 /* cio/rootr/medlyn*_p may be NULL when with_canopy = 0.  rootr is (p, 1:nlevsoi)
  * with ldp = npatch; medlynslope_p / medlynintercept_p (p) override the pftcon

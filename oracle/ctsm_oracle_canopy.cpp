@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdint>
 #include <algorithm>
+#include <vector>
 #include "ctsm_gpu.h"
 #include "ctsm_oracle.h"
 #include "oracle_libm.h"
@@ -862,3 +863,52 @@ extern "C" int oracle_canopyfluxes(const ctsmg_bounds* b, int num_exposedvegp, c
     if (err_index) *err_index = idx;
     return code;
 }
+
+// CanopyFluxesMod.F90:709, 833-895 -> SoilMoistStressMod.F90:70-114 (effective
+// porosity), 171-217 (volumetric liquid, jtop = 1), 312-435 (default stress,
+// perchroot off) with the Clapp-Hornberger suction.
+extern "C" int oracle_root_moist_stress(const ctsmg_bounds* b, int nump, const int32_t* filtp,
+                                        const ctsmg_rootmoist_io* io) {
+    const double TFRZ_ = 273.15, DENICE_ = 917.0, DENH2O_ = 1000.0;
+    const int NLEVSNO_ = 12, NLEVGRND_ = 25, LS_ = -NLEVSNO_ + 1;
+    const int ldc = io->ldc, ldp = io->ldp;
+    std::vector<int> cols;
+    for (int f = 0; f < nump; ++f) cols.push_back(io->patch_column[filtp[f] - b->begp] - b->begc);
+    for (int j = 1; j <= NLEVGRND_; ++j)
+        for (int c : cols) {
+            const size_t ss = c + (size_t)(j - LS_) * ldc, g = c + (size_t)(j - 1) * ldc;
+            const double vol_ice = std::min(io->watsat[g], io->h2osoi_ice[ss] / (DENICE_ * io->dz[ss]));
+            io->eff_porosity[g] = io->watsat[g] - vol_ice;
+        }
+    for (int j = 1; j <= NLEVGRND_; ++j)
+        for (int c : cols) {
+            const size_t ss = c + (size_t)(j - LS_) * ldc, g = c + (size_t)(j - 1) * ldc;
+            io->h2osoi_liqvol[g] = std::min(io->eff_porosity[g], io->h2osoi_liq[ss] / (io->dz[ss] * DENH2O_));
+        }
+    for (int f = 0; f < nump; ++f) io->btran[filtp[f] - b->begp] = 0.0;
+    for (int j = 1; j <= NLEVGRND_; ++j)
+        for (int f = 0; f < nump; ++f) {
+            const int p = filtp[f] - b->begp, c = io->patch_column[p] - b->begc, it = io->itype[p];
+            const size_t ss = c + (size_t)(j - LS_) * ldc, g = c + (size_t)(j - 1) * ldc, pg = p + (size_t)(j - 1) * ldp;
+            const double smpso = g_par.pft.smpso[it], smpsc = g_par.pft.smpsc[it];
+            if (io->h2osoi_liqvol[g] <= 0.0 || io->t_soisno[ss] <= TFRZ_ - 2.0) {
+                io->rootr[pg] = 0.0;
+            } else {
+                const double s_node = std::max(io->h2osoi_liqvol[g] / io->eff_porosity[g], 0.01);
+                double smp_node = -io->sucsat[g] * o_pow(s_node, -io->bsw[g]);
+                smp_node = std::max(smpsc, smp_node);
+                io->rresis[pg] = std::min((io->eff_porosity[g] / io->watsat[g]) * (smp_node - smpsc) / (smpso - smpsc), 1.0);
+                io->rootr[pg] = io->rootfr[pg] * io->rresis[pg];
+                io->btran[p] = io->btran[p] + std::max(io->rootr[pg], 0.0);
+            }
+        }
+    for (int j = 1; j <= NLEVGRND_; ++j)
+        for (int f = 0; f < nump; ++f) {
+            const int p = filtp[f] - b->begp;
+            const size_t pg = p + (size_t)(j - 1) * ldp;
+            if (io->btran[p] > 0.0) io->rootr[pg] = io->rootr[pg] / io->btran[p];
+            else io->rootr[pg] = 0.0;
+        }
+    return 0;
+}
+

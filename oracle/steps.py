@@ -15,12 +15,14 @@ def _p(a, t=C.c_double):
 
 
 def full_steps(A, npatch, ngrid, rootr, nsteps, medlyn_per_patch=False, method=1, itmax=40, snow_method=0,
-               soilfluxes=False):
+               soilfluxes=False, rootmoist=False):
     """nsteps x (CanopyFluxes, root sink, SoilTemperature, [SoilFluxes,]
     SoilWater, h2osoi_vol refresh) in place on A.  displa / z0mv keep their
     SatellitePhenology values and cgrnds / cgrndl restart from zero every
     step; with soilfluxes the temperatures before SoilTemperature go to
-    tssbef / t_h2osfc_bef."""
+    tssbef / t_h2osfc_bef; with rootmoist btran and rootr come from the root
+    moisture stress of the current soil state at the start of every step
+    (A then holds the ROOTMOIST components; `rootr` is not used)."""
     L = orc.lib()
     ncol = A["zwt"].shape[0]
     L.oracle_set_canopy_params(C.byref(canopy_inputs.make_params()), C.byref(canopy_inputs.make_pftcon()), method,
@@ -38,12 +40,16 @@ def full_steps(A, npatch, ngrid, rootr, nsteps, medlyn_per_patch=False, method=1
             A["z0mv"][:] = z0mv0
             A["cgrnds"][:] = 0.0
             A["cgrndl"][:] = 0.0
+            if rootmoist:
+                rm = abi.make_io(abi.RootMoistIO, abi.ROOTMOIST_FIELDS, A, ncol, npatch)
+                assert L.oracle_root_moist_stress(C.byref(b), npatch, _p(filt_p, C.c_int32), C.byref(rm)) == 0
             ci = abi.make_io(abi.CanopyIO, abi.CANOPY_FIELDS, A, ncol, npatch, ngrid, 1)
             e = C.c_int(0)
             rc = L.oracle_canopyfluxes(C.byref(b), npatch, _p(filt_p, C.c_int32), C.byref(ci), DT, C.byref(e))
             assert rc == 0, (rc, e.value)
             L.oracle_rootsink(ncol, npatch, _p(A["col_patchi"], C.c_int32), _p(A["col_npatches"], C.c_int32),
-                              _p(A["wtcol"]), _p(A["qflx_tran_veg"]), _p(rootr), _p(A["qflx_rootsoi"]))
+                              _p(A["wtcol"]), _p(A["qflx_tran_veg"]), _p(A["rootr"] if rootmoist else rootr),
+                              _p(A["qflx_rootsoi"]))
             if soilfluxes:
                 A["tssbef"][:] = A["t_soisno"]
                 A["t_h2osfc_bef"][:] = A["t_h2osfc"]

@@ -8,6 +8,7 @@ import subprocess
 import pytest
 
 from ctsm_gb300 import abi
+from ctsm_gb300.engine import BatchConfig, BatchInputs
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "ctsm_gpu.h")
@@ -55,7 +56,11 @@ def test_struct_layout_matches_ctypes(tmp_path):
     fields = {"ctsmg_soilwater_io": (abi.SoilWaterIO, ["ldc"] + [f[0] for f in abi.SOILWATER_FIELDS]),
               "ctsmg_soiltemp_io": (abi.SoilTempIO, ["ldc", "ldp"] + [f[0] for f in abi.SOILTEMP_FIELDS]),
               "ctsmg_soilfluxes_io": (abi.SoilFluxesIO, ["ldc", "ldp"] + [f[0] for f in abi.SOILFLUXES_FIELDS]),
+              "ctsmg_rootmoist_io": (abi.RootMoistIO, ["ldc", "ldp"] + [f[0] for f in abi.ROOTMOIST_FIELDS]),
+              "ctsmg_pftcon": (abi.Pftcon, [f[0] for f in abi.Pftcon._fields_]),
               "ctsmg_canopy_io": (abi.CanopyIO, ["ldp", "ldc", "ldg", "begg"] + [f[0] for f in abi.CANOPY_FIELDS]),
+              "ctsmg_batch_config": (BatchConfig, [f[0] for f in BatchConfig._fields_]),
+              "ctsmg_batch_inputs": (BatchInputs, [f[0] for f in BatchInputs._fields_]),
               "ctsmg_bounds": (abi.Bounds, ["begc", "endc", "begp", "endp"]),
               "ctsmg_options": (abi.Options, [f[0] for f in abi.Options._fields_])}
     src = ['#include <stdio.h>', '#include <stddef.h>', '#include "ctsm_gpu.h"', "int main(void){"]

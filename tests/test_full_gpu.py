@@ -107,3 +107,39 @@ def test_full_step_with_soilfluxes_matches_oracle(gpu_lib):
     assert not bad, {k: errs[k] for k in bad}
     assert np.abs(G["errsoi_col"] - R["errsoi_col"]).max() < 1e-8
     assert np.abs(G["errsoi_col"]).max() < 1e-5          # the reference's errsoi warning threshold
+
+
+def test_full_step_with_root_moisture_stress_matches_oracle(gpu_lib):
+    """btran and rootr computed from the resident soil state at the start of
+    every step (CanopyFluxesMod.F90:833-895) and fed to CanopyFluxes and the
+    root sink, with SoilFluxes, over 3 steps."""
+    from ctsm_gb300.engine import SoilBatch
+    A, npatch, ngrid, rootr = fi.full_state(2500, seed=35)
+    fi.add_soilfluxes_fields(A, npatch, ngrid)
+    fi.add_rootmoist_fields(A, npatch, rootr, rng=np.random.Generator(np.random.Philox(36)))
+    R = copy.deepcopy(A)
+    full_steps(R, npatch, ngrid, None, 3, soilfluxes=True, rootmoist=True)
+    G = copy.deepcopy(A)
+    b = SoilBatch(G, npatch, canopy=True, ngrid=ngrid, soilfluxes=True, rootmoist=True)
+    b.run(3)
+    b.sync()
+    b.download()
+    b.close()
+    assert (R["btran"] != A["btran"]).mean() > 0.9          # the stress really was recomputed
+    # rresis = (eff/watsat)*(smp - smpsc)/(smpso - smpsc) cancels where the
+    # suction nears smpsc, and smp ~ s^-bsw amplifies the state's rounding by
+    # bsw: those fields (and the transpiration they scale) get the
+    # conditioned test
+    spread = noise_spread(lambda B: full_steps(B, npatch, ngrid, None, 3, soilfluxes=True, rootmoist=True), A, R,
+                          fields=CANCEL + ("eflx_soil_grnd", "eflx_sh_tot", "eflx_lwrad_net", "rresis", "rootr",
+                                           "btran", "qflx_evap_veg", "qflx_tran_veg"), input_ulps=4)
+    for k in ("liqcan", "snocan"):
+        spread[k] = spread[k] + 1e-9 * (np.abs(A["liqcan"]) + np.abs(A["snocan"]))
+    # with btran = 0 (frozen or dry root zones) and a dry canopy,
+    # qflx_evap_veg = min(rpp*efpot, 0) and efpot is a difference of
+    # humidities (CanopyFluxesMod.F90:1336-1364) crossing zero at dew point:
+    # its rounding, ~eps*qsat/dq ~ 1e-14 of the field's scale, decides the sign
+    spread["qflx_evap_veg"] = spread["qflx_evap_veg"] + 1e-14 * np.abs(R["qflx_evap_veg"]).max()
+    errs, bad = compare(G, R, STATE + SF_OUT + ["btran", "rootr", "rresis", "eff_porosity", "h2osoi_liqvol"], 1e-9,
+                        spread)
+    assert not bad, {k: errs[k] for k in bad}
