@@ -30,6 +30,7 @@ def load():
     P = C.POINTER
     L.ctsmg_init.argtypes = [P(abi.Options)]
     L.ctsmg_set_soilwater_params.argtypes = [P(abi.SoilWaterParams)]
+    L.ctsmg_set_soilwater_movement.argtypes = [P(abi.SoilWaterMovementNml)]
     L.ctsmg_last_error.restype = C.c_char_p
     L.ctsmg_last_error_index.argtypes = [P(C.c_int32), P(C.c_int32)]
     L.ctsmg_soilwater.argtypes = [P(abi.Bounds), C.c_int32, P(C.c_int32), P(abi.SoilWaterIO), C.c_double]

@@ -44,6 +44,12 @@ SOILWATER_FIELDS = [
     ("t_soisno", "SS", F64, "in"),
 ]
 
+# components only the moisture form or the flexibleCN fix use (NULL otherwise)
+SOILWATER_EXTRA = [
+    ("nbedrock", "C", I32, "in"), ("eff_porosity", "G", F64, "in"), ("num_substeps", "C", F64, "out"),
+    ("wa", "C", F64, "inout"),
+]
+
 SOILTEMP_FIELDS = [
     ("snl", "C", I32, "in"), ("nbedrock", "C", I32, "in"),
     ("z", "SS", F64, "in"), ("zi", "ZI", F64, "in"), ("dz", "SS", F64, "in"),
@@ -159,7 +165,23 @@ class SoilWaterParams(C.Structure):
 
 
 class SoilWaterIO(C.Structure):
-    _fields_ = [("ldc", C.c_int32)] + [(n, _ptr_type(t)) for (n, _, t, _) in SOILWATER_FIELDS]
+    _fields_ = [("ldc", C.c_int32)] + [(n, _ptr_type(t)) for (n, _, t, _) in SOILWATER_FIELDS + SOILWATER_EXTRA]
+
+
+class SoilWaterMovementNml(C.Structure):
+    _fields_ = [("soilwater_movement_method", C.c_int32), ("upper_boundary_condition", C.c_int32),
+                ("lower_boundary_condition", C.c_int32), ("flux_calculation", C.c_int32),
+                ("use_flexibleCN", C.c_int32), ("use_bedrock", C.c_int32), ("dtmin", C.c_double),
+                ("verySmall", C.c_double), ("xTolerUpper", C.c_double), ("xTolerLower", C.c_double)]
+
+
+def soilwater_movement_nml(method=1, upper=1, lower=None, flux_calculation=1, use_flexibleCN=0, use_bedrock=1,
+                           dtmin=60.0, verySmall=1e-8, xTolerUpper=1e-1, xTolerLower=1e-2):
+    """The namelist with the reference's defaults (namelist_defaults_ctsm.xml:471-488)."""
+    if lower is None:
+        lower = 4 if method == 0 else 2
+    return SoilWaterMovementNml(method, upper, lower, flux_calculation, use_flexibleCN, use_bedrock, dtmin,
+                                verySmall, xTolerUpper, xTolerLower)
 
 
 class RootMoistIO(C.Structure):

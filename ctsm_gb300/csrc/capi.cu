@@ -17,6 +17,7 @@
 #include "canopy_kernels.cuh"
 #include "soilfluxes_kernels.cuh"
 #include "rootmoist_kernels.cuh"
+#include "moisture_form_kernels.cuh"
 #include "capi_internal.h"
 
 namespace ctsmg {
@@ -26,6 +27,8 @@ static std::mutex g_mu;
 static bool g_init = false;
 static ctsmg_options g_opt;
 static ctsmg_soilwater_params g_swp = {6.0};
+// soilwater_movement_inparm; defaults of the Zeng-Decker form until ctsmg_init
+static ctsmg_soilwater_movement_nml g_swm = {0, 1, 4, 1, 0, 0, 60.0, 1.e-8, 1.e-1, 1.e-2};
 static ctsmg_canopy_params g_cpar;
 static ctsmg_pftcon g_pft;
 static bool g_cpar_set = false;
@@ -154,6 +157,31 @@ const FieldDesc SOILWATER_TABLE[] = {
     FW(ctsmg_soilwater_io, qflx_rootsoi, K_S, 8, U_IN), FW(ctsmg_soilwater_io, t_soisno, K_SS, 8, U_IN),
 };
 const int SOILWATER_NFIELDS = sizeof(SOILWATER_TABLE) / sizeof(SOILWATER_TABLE[0]);
+
+// soilwater_moisture_form (SoilWaterMovementMod.F90:1172-1186, 1503-1508,
+// 1627-1635, 2085-2095): icefrac and eff_porosity are inputs here
+const FieldDesc SOILWATER_MF_TABLE[] = {
+    FW(ctsmg_soilwater_io, z, K_SS, 8, U_IN), FW(ctsmg_soilwater_io, zi, K_ZI, 8, U_IN),
+    FW(ctsmg_soilwater_io, dz, K_SS, 8, U_IN), FW(ctsmg_soilwater_io, nbedrock, K_C, 4, U_IN),
+    FW(ctsmg_soilwater_io, zwt, K_C, 8, U_IN), FW(ctsmg_soilwater_io, qcharge, K_C, 8, U_OUT),
+    FW(ctsmg_soilwater_io, icefrac, K_G, 8, U_IN), FW(ctsmg_soilwater_io, qin, K_S, 8, U_OUT),
+    FW(ctsmg_soilwater_io, qout, K_S, 8, U_OUT), FW(ctsmg_soilwater_io, smpmin, K_C, 8, U_IN),
+    FW(ctsmg_soilwater_io, watsat, K_G, 8, U_IN), FW(ctsmg_soilwater_io, hksat, K_G, 8, U_IN),
+    FW(ctsmg_soilwater_io, bsw, K_G, 8, U_IN), FW(ctsmg_soilwater_io, sucsat, K_G, 8, U_IN),
+    FW(ctsmg_soilwater_io, smp_l, K_G, 8, U_OUT), FW(ctsmg_soilwater_io, hk_l, K_G, 8, U_OUT),
+    FW(ctsmg_soilwater_io, h2osoi_liq, K_SS, 8, U_INOUT), FW(ctsmg_soilwater_io, qflx_infl, K_C, 8, U_IN),
+    FW(ctsmg_soilwater_io, qflx_rootsoi, K_S, 8, U_IN), FW(ctsmg_soilwater_io, eff_porosity, K_G, 8, U_IN),
+    FW(ctsmg_soilwater_io, num_substeps, K_C, 8, U_OUT),
+};
+const int SOILWATER_MF_NFIELDS = sizeof(SOILWATER_MF_TABLE) / sizeof(SOILWATER_MF_TABLE[0]);
+
+// the use_flexibleCN fix after either form (SoilWaterMovementMod.F90:331-368)
+const FieldDesc SOILWATER_FLEXCN_TABLE[] = {
+    FW(ctsmg_soilwater_io, h2osoi_liq, K_SS, 8, U_INOUT), FW(ctsmg_soilwater_io, h2osoi_ice, K_SS, 8, U_IN),
+    FW(ctsmg_soilwater_io, dz, K_SS, 8, U_IN), FW(ctsmg_soilwater_io, h2osoi_vol, K_G, 8, U_INOUT),
+    FW(ctsmg_soilwater_io, wa, K_C, 8, U_INOUT),
+};
+const int SOILWATER_FLEXCN_NFIELDS = sizeof(SOILWATER_FLEXCN_TABLE) / sizeof(SOILWATER_FLEXCN_TABLE[0]);
 
 #define FT(name, kind, esz, use) FW(ctsmg_soiltemp_io, name, kind, esz, use)
 const FieldDesc SOILTEMP_TABLE[] = {
@@ -554,8 +582,9 @@ extern "C" int32_t ctsmg_init(const ctsmg_options* opt) {
     if (!opt) return set_error(CTSMG_E_ARG, "null options", 0, 0);
     if (opt->nlevsno != NLEVSNO || opt->nlevsoi != NLEVSOI || opt->nlevgrnd != NLEVGRND)
         return set_error(CTSMG_E_UNSUPPORTED, "only nlevsno=12, nlevsoi=20, nlevgrnd=25 (20SL_8.5m) are built", 0, 0);
-    if (opt->soilwater_movement_method != 0)
-        return set_error(CTSMG_E_UNSUPPORTED, "only soilwater_movement_method=0 (Zeng-Decker 2009) is built", 0, 0);
+    if (opt->soilwater_movement_method != 0 && opt->soilwater_movement_method != 1)
+        return set_error(CTSMG_E_UNSUPPORTED,
+                         "soilwater_movement_method must be 0 (Zeng-Decker 2009) or 1 (moisture form)", 0, 0);
     if (opt->snow_thermal_cond_method != 0 && opt->snow_thermal_cond_method != 1)
         return set_error(CTSMG_E_ARG, "snow_thermal_cond_method must be 0 (Jordan1991) or 1 (Sturm1997)", 0, 0);
     int ndev = 0;
@@ -565,7 +594,36 @@ extern "C" int32_t ctsmg_init(const ctsmg_options* opt) {
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     std::lock_guard<std::mutex> lk(g_mu);
     g_opt = *opt;
+    // the namelist defaults for this method (namelist_defaults_ctsm.xml:471-488)
+    g_swm = ctsmg_soilwater_movement_nml{opt->soilwater_movement_method, 1,
+                                         opt->soilwater_movement_method == 0 ? 4 : 2, 1, 0,
+                                         opt->soilwater_movement_method == 0 ? 0 : 1, 60.0, 1.e-8, 1.e-1, 1.e-2};
     g_init = true;
+    return 0;
+}
+
+extern "C" int32_t ctsmg_set_soilwater_movement(const ctsmg_soilwater_movement_nml* nml) {
+    if (!nml) return set_error(CTSMG_E_ARG, "null namelist", 0, 0);
+    const int m = nml->soilwater_movement_method, ubc = nml->upper_boundary_condition,
+              lbc = nml->lower_boundary_condition;
+    if (m != 0 && m != 1)
+        return set_error(CTSMG_E_UNSUPPORTED, "soilwater_movement_method must be 0 or 1 (mixed and head forms are empty "
+                         "in the reference)", 0, 0);
+    if (m == 0 && lbc != 4)
+        return set_error(CTSMG_E_ARG, "ERROR inconsistent soilwater_movement namelist: ZD09 must use bc_aquifer lbc", 0, 0);
+    if (nml->use_bedrock && lbc != 2)
+        return set_error(CTSMG_E_ARG, "ERROR inconsistent soilwater_movement namelist: use_bedrock requires "
+                         "bc_zero_flux lbc", 0, 0);
+    if (ubc != 1)
+        return set_error(CTSMG_E_UNSUPPORTED, "upper_boundary_condition must be bc_flux (bc_head reads a boundary water "
+                         "content the reference never sets)", 0, 0);
+    if (m == 1 && (lbc < 1 || lbc > 3))
+        return set_error(CTSMG_E_UNSUPPORTED, "the moisture form supports lower_boundary_condition bc_flux, "
+                         "bc_zero_flux or bc_waterTable", 0, 0);
+    if (m == 1 && !(nml->dtmin > 0.0 && nml->verySmall > 0.0 && nml->xTolerUpper > 0.0 && nml->xTolerLower >= 0.0))
+        return set_error(CTSMG_E_ARG, "dtmin, verySmall, xTolerUpper must be positive", 0, 0);
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_swm = *nml;
     return 0;
 }
 
@@ -594,6 +652,48 @@ extern "C" int32_t ctsmg_last_error_index(int32_t* index, int32_t* level) {
     return 0;
 }
 
+// The fields one SoilWater call stages: the Zeng-Decker table, or the
+// moisture form's, plus what the use_flexibleCN fix reads and writes.
+static std::vector<FieldDesc> soilwater_fields(const ctsmg_soilwater_movement_nml& nml) {
+    std::vector<FieldDesc> t;
+    if (nml.soilwater_movement_method == 0) {
+        t.assign(SOILWATER_TABLE, SOILWATER_TABLE + SOILWATER_NFIELDS);
+    } else {
+        t.assign(SOILWATER_MF_TABLE, SOILWATER_MF_TABLE + SOILWATER_MF_NFIELDS);
+    }
+    if (nml.use_flexibleCN) {
+        auto put = [&](const FieldDesc& f) {
+            for (auto& g : t)
+                if (g.offset == f.offset) { g.use = f.use; return; }
+            t.push_back(f);
+        };
+        for (int i = 0; i < SOILWATER_FLEXCN_NFIELDS; ++i) put(SOILWATER_FLEXCN_TABLE[i]);
+    }
+    return t;
+}
+
+static cudaError_t launch_soilwater_call(const ctsmg_soilwater_io& dio, int begc, int n, const int32_t* dfilt,
+                                         const ctsmg_soilwater_movement_nml& nml, double e_ice, double dtime,
+                                         DevError* err, cudaStream_t s) {
+    cudaError_t e;
+    if (nml.soilwater_movement_method == 0) {
+        e = launch_soilwater(dio, begc, n, dfilt, e_ice, dtime, s);
+    } else {
+        MoistureFormArgs P{e_ice, dtime, nml.dtmin, nml.verySmall, nml.xTolerUpper, nml.xTolerLower,
+                           nml.lower_boundary_condition, nml.flux_calculation == 42 ? 1 : 0,
+                           moisture_form_max_trials(dtime, nml.dtmin)};
+        e = launch_moisture_form(dio, begc, n, dfilt, P, err, s);
+    }
+    if (e == cudaSuccess && nml.use_flexibleCN) e = launch_flexcn(dio, begc, n, dfilt, s);
+    return e;
+}
+
+static int soilwater_error(int code, int idx, int lev) {
+    if (code == CTSMG_E_SINGULAR)
+        return set_error(code, "soilwater_moisture_form:: problem with the lapack solver", idx, lev);
+    return set_error(code, "soilwater_moisture_form:: sub-step loop did not complete the time step", idx, lev);
+}
+
 extern "C" int32_t ctsmg_soilwater(const ctsmg_bounds* bounds, int32_t num_hydrologyc,
                                    const int32_t* filter_hydrologyc, const ctsmg_soilwater_io* io,
                                    double dtime) {
@@ -605,48 +705,73 @@ extern "C" int32_t ctsmg_soilwater(const ctsmg_bounds* bounds, int32_t num_hydro
     const int ncol = bounds->endc - bounds->begc + 1;
     if (io->ldc < ncol) return set_error(CTSMG_E_ARG, "ldc smaller than endc-begc+1", 0, 0);
     if (!(dtime > 0.0)) return set_error(CTSMG_E_ARG, "dtime must be positive", 0, 0);
+    ctsmg_soilwater_movement_nml nml;
+    double e_ice;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        nml = g_swm;
+        e_ice = g_swp.e_ice;
+    }
+    const std::vector<FieldDesc> tab = soilwater_fields(nml);
+    const FieldDesc* T = tab.data();
+    const int NT = (int)tab.size();
+    for (const FieldDesc& f : tab)
+        if (!field_ptr(const_cast<ctsmg_soilwater_io*>(io), f)) {
+            std::string m = std::string("null pointer for component ") + f.name;
+            return set_error(CTSMG_E_ARG, m.c_str(), 0, 0);
+        }
+    if (nml.soilwater_movement_method == 1) {
+        for (int i = 0; i < num_hydrologyc; ++i) {
+            const int nb = io->nbedrock[filter_hydrologyc[i] - bounds->begc];
+            if (nb < 2 || nb > NLEVSOI)
+                return set_error(CTSMG_E_ARG, "nbedrock outside 2..nlevsoi", filter_hydrologyc[i], 0);
+            if (nml.lower_boundary_condition == 3 && nb != NLEVSOI)
+                return set_error(CTSMG_E_ARG, "bc_waterTable needs nbedrock = nlevsoi (use_bedrock = .false.)",
+                                 filter_hydrologyc[i], 0);
+        }
+    }
     if (num_hydrologyc == 0) return 0;
     const int ldc = io->ldc;
-    size_t need = table_bytes(SOILWATER_TABLE, SOILWATER_NFIELDS, ldc, 0) + (size_t)num_hydrologyc * 4 + 4096;
+    size_t need = table_bytes(T, NT, ldc, 0) + (size_t)num_hydrologyc * 4 + 4096;
     if ((rc = arena_reserve(c, need))) return rc;
-    double e_ice_p;
-    { std::lock_guard<std::mutex> lk(g_mu); e_ice_p = g_swp.e_ice; }
+    cudaError_t e = cudaMemsetAsync(c->err, 0xff, sizeof(DevError), c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(err)");
     std::vector<Chunk> chunks;
     if (plan_chunks(bounds, num_hydrologyc, filter_hydrologyc, nullptr, nullptr, chunks)) {
         ctsmg_soilwater_io dio;
-        stage_alloc(c, io, &dio, sizeof dio, SOILWATER_TABLE, SOILWATER_NFIELDS, ldc, 0);
+        stage_alloc(c, io, &dio, sizeof dio, T, NT, ldc, 0);
         int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_hydrologyc * 4);
-        cudaError_t e = cudaMemcpyAsync(dfilt, filter_hydrologyc, (size_t)num_hydrologyc * 4, cudaMemcpyHostToDevice,
-                                        c->h2d);
+        e = cudaMemcpyAsync(dfilt, filter_hydrologyc, (size_t)num_hydrologyc * 4, cudaMemcpyHostToDevice, c->h2d);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
         const int K = (int)chunks.size();
-        if ((rc = chunk_in(c, chunks[0], 0, io, &dio, SOILWATER_TABLE, SOILWATER_NFIELDS, ldc, 0))) return rc;
+        if ((rc = chunk_in(c, chunks[0], 0, io, &dio, T, NT, ldc, 0))) return rc;
         for (int k = 0; k < K; ++k) {
             const Chunk& ch = chunks[k];
             if ((e = cudaStreamWaitEvent(c->stream, c->ev_in[k], 0)) != cudaSuccess) return cuda_fail(e, "wait");
-            e = launch_soilwater(dio, bounds->begc, ch.f1 - ch.f0, dfilt + ch.f0, e_ice_p, dtime, c->stream);
+            e = launch_soilwater_call(dio, bounds->begc, ch.f1 - ch.f0, dfilt + ch.f0, nml, e_ice, dtime, c->err,
+                                      c->stream);
             if (e != cudaSuccess) return cuda_fail(e, "soilwater kernel launch");
             if ((e = cudaEventRecord(c->ev_done[k], c->stream)) != cudaSuccess) return cuda_fail(e, "record");
-            if (k + 1 < K && (rc = chunk_in(c, chunks[k + 1], k + 1, io, &dio, SOILWATER_TABLE, SOILWATER_NFIELDS, ldc, 0)))
-                return rc;
-            if ((rc = chunk_out(c, ch, k, io, &dio, SOILWATER_TABLE, SOILWATER_NFIELDS, ldc, 0))) return rc;
+            if (k + 1 < K && (rc = chunk_in(c, chunks[k + 1], k + 1, io, &dio, T, NT, ldc, 0))) return rc;
+            if ((rc = chunk_out(c, ch, k, io, &dio, T, NT, ldc, 0))) return rc;
         }
         if ((e = cudaStreamSynchronize(c->d2h)) != cudaSuccess) return cuda_fail(e, "soilwater");
         if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return cuda_fail(e, "soilwater");
-        return 0;
+    } else {
+        ctsmg_soilwater_io dio;
+        if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, 0))) return rc;
+        int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_hydrologyc * 4);
+        e = cudaMemcpyAsync(dfilt, filter_hydrologyc, (size_t)num_hydrologyc * 4, cudaMemcpyHostToDevice, c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
+        e = launch_soilwater_call(dio, bounds->begc, num_hydrologyc, dfilt, nml, e_ice, dtime, c->err, c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "soilwater kernel launch");
+        if ((rc = stage_out(c, io, &dio, T, NT, ldc, 0))) return rc;
+        e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "soilwater");
     }
-    ctsmg_soilwater_io dio;
-    if ((rc = stage_in(c, io, &dio, sizeof dio, SOILWATER_TABLE, SOILWATER_NFIELDS, ldc, 0))) return rc;
-    int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_hydrologyc * 4);
-    cudaError_t e = cudaMemcpyAsync(dfilt, filter_hydrologyc, (size_t)num_hydrologyc * 4, cudaMemcpyHostToDevice, c->stream);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
-    double e_ice;
-    { std::lock_guard<std::mutex> lk(g_mu); e_ice = g_swp.e_ice; }
-    e = launch_soilwater(dio, bounds->begc, num_hydrologyc, dfilt, e_ice, dtime, c->stream);
-    if (e != cudaSuccess) return cuda_fail(e, "soilwater kernel launch");
-    if ((rc = stage_out(c, io, &dio, SOILWATER_TABLE, SOILWATER_NFIELDS, ldc, 0))) return rc;
-    e = cudaStreamSynchronize(c->stream);
-    if (e != cudaSuccess) return cuda_fail(e, "soilwater");
+    int code = 0, idx = 0, lev = 0;
+    if ((rc = read_error(c, &code, &idx, &lev))) return rc;
+    if (code) return soilwater_error(code, idx, lev);
     return 0;
 }
 

@@ -11,6 +11,10 @@ struct FieldDesc { size_t offset; int kind; int esize; int use; const char* name
 
 extern const FieldDesc SOILWATER_TABLE[];
 extern const int SOILWATER_NFIELDS;
+extern const FieldDesc SOILWATER_MF_TABLE[];
+extern const int SOILWATER_MF_NFIELDS;
+extern const FieldDesc SOILWATER_FLEXCN_TABLE[];
+extern const int SOILWATER_FLEXCN_NFIELDS;
 extern const FieldDesc SOILTEMP_TABLE[];
 extern const int SOILTEMP_NFIELDS;
 extern const FieldDesc CANOPY_TABLE[];

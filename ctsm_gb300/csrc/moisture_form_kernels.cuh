@@ -1,0 +1,35 @@
+// moisture_form_kernels.cuh -- launchers of SoilWater's moisture form and of
+// the use_flexibleCN fix (internal C++ API).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "ctsm_gpu.h"
+#include "ctsm_device.cuh"
+
+namespace ctsmg {
+
+struct MoistureFormArgs {
+    double e_ice, dtime, dtmin, verySmall, xTolerUpper, xTolerLower;
+    int lower_bc;        // 1 bc_flux, 2 bc_zero_flux, 3 bc_waterTable
+    int expensive;       // flux_calculation == expensive
+    int max_trials;      // bound on the sub-step loop (never reached by the reference's rule)
+};
+
+// Trials the halving/doubling rule can take at most: every accepted sub-step
+// is at least dtmin long (or the remainder) and is preceded by at most one
+// rejected doubling, after the initial halvings from dtime down to dtmin.
+inline int moisture_form_max_trials(double dtime, double dtmin) {
+    double n = dtime / (dtmin > 0.0 ? dtmin : dtime);
+    if (n > 1.0e6) n = 1.0e6;
+    return 2 * (int)n + 128;
+}
+
+__device__ int mf_column(const ctsmg_soilwater_io& io, int c, const MoistureFormArgs& P);
+__device__ void flexcn_column(const ctsmg_soilwater_io& io, int c);
+
+// d_filt: device copy of the 1-based column filter, or NULL for begc .. begc+nfilt-1.
+cudaError_t launch_moisture_form(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt,
+                                 const MoistureFormArgs& P, DevError* err, cudaStream_t s);
+cudaError_t launch_flexcn(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt, cudaStream_t s);
+
+} // namespace ctsmg

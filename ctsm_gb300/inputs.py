@@ -34,7 +34,7 @@ the builder are stated here and nowhere else:
 """
 import numpy as np
 
-from .abi import NLEVSNO, NLEVSOI, NLEVGRND, SOILWATER_FIELDS, SOILTEMP_FIELDS, field_shape
+from .abi import NLEVSNO, NLEVSOI, NLEVGRND, SOILWATER_FIELDS, SOILWATER_EXTRA, SOILTEMP_FIELDS, field_shape
 
 TFRZ = 273.15
 DENH2O = 1.000e3
@@ -47,7 +47,7 @@ PEDO = dict(tkd_sand=8.80, tkd_clay=2.92, tkm_om=0.25, tkd_om=0.05, csol_sand=2.
             csol_clay=2.385, csol_om=2.5, pd=2700.0, zsapric=0.5, pcalpha=0.5, pcbeta=0.139)
 
 ALL_FIELDS = {}
-for _f in SOILWATER_FIELDS + SOILTEMP_FIELDS:
+for _f in SOILWATER_FIELDS + SOILWATER_EXTRA + SOILTEMP_FIELDS:
     ALL_FIELDS[_f[0]] = _f
 
 
@@ -267,7 +267,22 @@ def soil_columns(ncol, seed=0, snow=False, nbedrock=(20, 20), zwt=(0.5, 8.0),
         A["frac_h2osfc"][:] = np.minimum(A["frac_h2osfc"], 1.0 - A["frac_sno_eff"])
         A["frac_sno_eff"][:] = np.where(has_snow, 1.0 - A["frac_h2osfc"], 0.0)
         A["t_h2osfc"][:] = r.uniform(268.0, 285.0, size=ncol)
+    A["wa"][:] = 5000.0      # aquifer water at aquifer_water_baseline (clm_varcon.F90:124)
+    set_soil_water_fractions(A)
     return A, npatch
+
+
+def set_soil_water_fractions(A):
+    """icefrac and eff_porosity on levels 1..nlevsoi as SetSoilWaterFractions
+    computes them before SoilWater (SoilHydrologyMod.F90:236-249, no excess
+    ice: dz_ext = dz)."""
+    LS = -NLEVSNO + 1
+    for j in range(1, NLEVSOI + 1):
+        row = j - LS
+        ws = A["watsat"][j - 1]
+        vol_ice = np.minimum(ws, (A["h2osoi_ice"][row] + 0.0) / ((A["dz"][row] + 0.0 / DENICE) * DENICE))
+        A["eff_porosity"][j - 1] = np.maximum(0.01, ws - vol_ice)
+        A["icefrac"][j - 1] = np.minimum(1.0, vol_ice / ws)
 
 
 def refresh_h2osoi_vol(A):

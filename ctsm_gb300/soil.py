@@ -16,15 +16,23 @@ from ._lib import load, check
 _INIT = {}
 
 
-def init(snow_thermal_cond_method=0, stomatalcond_method=1, itmax_canopy_fluxes=40, e_ice=6.0):
+def init(snow_thermal_cond_method=0, stomatalcond_method=1, itmax_canopy_fluxes=40, e_ice=6.0,
+         soilwater_movement_method=0):
     """ctsmg_init + ctsmg_set_soilwater_params (the namelist and readParams
     steps of SoilWaterMovementMod.F90:89-216 and CanopyFluxesMod.F90:92-188)."""
     L = load()
-    opt = abi.Options(0, snow_thermal_cond_method, itmax_canopy_fluxes, stomatalcond_method,
+    opt = abi.Options(soilwater_movement_method, snow_thermal_cond_method, itmax_canopy_fluxes, stomatalcond_method,
                       abi.NLEVSNO, abi.NLEVSOI, abi.NLEVGRND)
     check(L.ctsmg_init(C.byref(opt)))
     check(L.ctsmg_set_soilwater_params(C.byref(abi.SoilWaterParams(e_ice))))
     _INIT.update(snow_thermal_cond_method=snow_thermal_cond_method, e_ice=e_ice)
+
+
+def set_soilwater_movement(nml):
+    """ctsmg_set_soilwater_movement: the soilwater_movement_inparm namelist
+    (init_soilwater_movement, SoilWaterMovementMod.F90:108-216); build it with
+    abi.soilwater_movement_nml."""
+    check(load().ctsmg_set_soilwater_movement(C.byref(nml)))
 
 
 def _filter(filt):
@@ -33,11 +41,14 @@ def _filter(filt):
 
 
 def SoilWater(bounds, num_hydrologyc, filter_hydrologyc, state, dtime):
-    """SoilWater (SoilWaterMovementMod.F90:240), Zeng-Decker 2009 form."""
+    """SoilWater (SoilWaterMovementMod.F90:240) in the form the namelist
+    selects; the moisture form and the flexibleCN fix also take the
+    SOILWATER_EXTRA components of `state`."""
     L = load()
     f, fp = _filter(filter_hydrologyc)
     ncol = bounds.endc - bounds.begc + 1
-    io = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS, state, ncol)
+    fields = abi.SOILWATER_FIELDS + [x for x in abi.SOILWATER_EXTRA if x[0] in state]
+    io = abi.make_io(abi.SoilWaterIO, fields, state, ncol)
     check(L.ctsmg_soilwater(C.byref(bounds), int(num_hydrologyc), fp, C.byref(io), float(dtime)))
 
 

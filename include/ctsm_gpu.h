@@ -90,7 +90,7 @@ typedef struct {
  *      Sturm1997 for clm6_0: namelist_defaults_ctsm.xml:555-556)
  *   itmax_canopy_fluxes (src/biogeophys/CanopyFluxesMod.F90:83)             */
 typedef struct {
-    int32_t soilwater_movement_method;   /* 0 = Zeng-Decker 2009 (only form built)  */
+    int32_t soilwater_movement_method;   /* 0 = Zeng-Decker 2009, 1 = moisture form */
     int32_t snow_thermal_cond_method;    /* 0 = Jordan1991, 1 = Sturm1997           */
     int32_t itmax_canopy_fluxes;         /* 40                                      */
     int32_t stomatalcond_method;         /* 0 = Ball-Berry 1987, 1 = Medlyn 2011    */
@@ -136,7 +136,40 @@ typedef struct {
     const double* qflx_rootsoi;  /* [S]  root water sink (mm/s)                   */
     /* temperature_inst */
     const double* t_soisno;      /* [SS] soil temperature (K)                     */
+    /* Read or written only by the moisture form (soilwater_movement_method = 1,
+     * SoilWaterMovementMod.F90:1172-1186) or by the use_flexibleCN
+     * negative-liquid fix (:331-368); NULL otherwise.  With the moisture form
+     * icefrac is an INPUT (set by SetSoilWaterFractions,
+     * SoilHydrologyMod.F90:200-245, before SoilWater) and h2osoi_vol,
+     * qflx_deficit and t_soisno are not used.                                */
+    const int32_t* nbedrock;     /* (c)  index of the bottom soil layer (nlayers) */
+    const double* eff_porosity;  /* [G]  porosity - ice volume (over-saturation)  */
+    double*       num_substeps;  /* (c)  out: adaptive sub-steps taken (trials)   */
+    double*       wa;            /* (c)  inout: aquifer water, flexibleCN fix (mm)*/
 } ctsmg_soilwater_io;
+
+/* Namelist soilwater_movement_inparm (init_soilwater_movement,
+ * src/biogeophys/SoilWaterMovementMod.F90:108-216) and use_flexibleCN
+ * (clm_varctl).  Boundary conditions: 0 bc_head, 1 bc_flux, 2 bc_zero_flux,
+ * 3 bc_waterTable, 4 bc_aquifer (:47-51).  flux_calculation = 42 is the
+ * reference's `expensive` error estimate (:1321-1336), any other value the
+ * inexpensive one.  The same consistency checks as the reference apply
+ * (ZD09 needs bc_aquifer; use_bedrock needs bc_zero_flux), and the forms the
+ * reference cannot complete are refused: bc_head at either boundary (the
+ * boundary water contents are never set, and the lower one ends in endrun),
+ * bc_aquifer with the moisture form (:1764-1861 has no case for it).       */
+typedef struct {
+    int32_t soilwater_movement_method;   /* 0 ZD09, 1 moisture form              */
+    int32_t upper_boundary_condition;    /* 1                                     */
+    int32_t lower_boundary_condition;    /* 4 with ZD09, 2 with the moisture form */
+    int32_t flux_calculation;            /* 1 inexpensive, 42 expensive           */
+    int32_t use_flexibleCN;              /* 0 / 1                                 */
+    int32_t use_bedrock;                 /* 1 (namelist_defaults_ctsm.xml:259)   */
+    double  dtmin;                       /* 60 s                                  */
+    double  verySmall;                   /* 1e-8 s                                */
+    double  xTolerUpper;                 /* 1e-1: halve the sub-step above        */
+    double  xTolerLower;                 /* 1e-2: double the sub-step below       */
+} ctsmg_soilwater_movement_nml;
 
 /* ---------------------------------------------------------------- SoilTemperature */
 /* Components read and written by SoilTemperature and the routines it calls
@@ -294,6 +327,11 @@ typedef struct {
  * (src/biogeophys/CanopyFluxesMod.F90:92-157) and Photosynthesis ReadNML
  * (src/biogeophys/PhotosynthesisMod.F90:939-1015).  Selects device 0.       */
 int32_t ctsmg_init(const ctsmg_options* opt);
+
+/* Replaces init_soilwater_movement (SoilWaterMovementMod.F90:108-216).
+ * ctsmg_init sets the reference's defaults for its soilwater_movement_method;
+ * this call replaces all of them.                                          */
+int32_t ctsmg_set_soilwater_movement(const ctsmg_soilwater_movement_nml* nml);
 
 /* Replaces readParams of SoilWaterMovementMod (src/biogeophys/SoilWaterMovementMod.F90:89-106). */
 int32_t ctsmg_set_soilwater_params(const ctsmg_soilwater_params* p);

@@ -25,6 +25,12 @@ void oracle_set_canopy_params(const ctsmg_canopy_params* p, const ctsmg_pftcon* 
 void oracle_set_patch_medlyn(const double* slope, const double* intercept);
 int  oracle_quadratic(double a, double b, double c, double* r1, double* r2);
 void oracle_qsat(double T, double p, double* qs, double* es, double* qsdT);
+int  oracle_dgtsv(int n, double* dl, double* d, double* du, double* b);
+int  oracle_soilwater_mf(const ctsmg_bounds* bounds, int num_hydrologyc, const int32_t* filter_hydrologyc,
+                         const ctsmg_soilwater_io* io, double e_ice, double dtime,
+                         const ctsmg_soilwater_movement_nml* nml, int* err_col);
+void oracle_flexcn_fix(const ctsmg_bounds* bounds, int num_hydrologyc, const int32_t* filter_hydrologyc,
+                       const ctsmg_soilwater_io* io);
 int  oracle_root_moist_stress(const ctsmg_bounds* b, int nump, const int32_t* filtp, const ctsmg_rootmoist_io* io);
 int  oracle_soilfluxes(const ctsmg_bounds* b, int num_nolakec, const int32_t* filter_nolakec, int num_nolakep,
                        const int32_t* filter_nolakep, const ctsmg_soilfluxes_io* io, double dtime);

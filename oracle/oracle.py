@@ -40,6 +40,11 @@ def lib():
         _LIB.oracle_rootsink.argtypes = [I, I, P(C.c_int32), P(C.c_int32)] + [P(C.c_double)] * 4
         _LIB.oracle_rootsink.restype = None
         _LIB.oracle_canopyfluxes.argtypes = [P(abi.Bounds), I, P(C.c_int32), P(abi.CanopyIO), C.c_double, P(C.c_int)]
+        _LIB.oracle_dgtsv.argtypes = [I] + [P(C.c_double)] * 4
+        _LIB.oracle_soilwater_mf.argtypes = [P(abi.Bounds), I, P(C.c_int32), P(abi.SoilWaterIO), C.c_double,
+                                             C.c_double, P(abi.SoilWaterMovementNml), P(C.c_int)]
+        _LIB.oracle_flexcn_fix.argtypes = [P(abi.Bounds), I, P(C.c_int32), P(abi.SoilWaterIO)]
+        _LIB.oracle_flexcn_fix.restype = None
         _LIB.oracle_root_moist_stress.argtypes = [P(abi.Bounds), I, P(C.c_int32), P(abi.RootMoistIO)]
         _LIB.oracle_soilfluxes.argtypes = [P(abi.Bounds), I, P(C.c_int32), I, P(C.c_int32), P(abi.SoilFluxesIO),
                                            C.c_double]

@@ -47,7 +47,7 @@ def test_init_without_gpu_fails_cleanly(lib):
 
 def test_unsupported_options_rejected(lib):
     lib.ctsmg_init.argtypes = [C.POINTER(abi.Options)]
-    assert lib.ctsmg_init(C.byref(abi.Options(1, 0, 40, 1, 12, 20, 25))) == 10   # moisture form not built
+    assert lib.ctsmg_init(C.byref(abi.Options(2, 0, 40, 1, 12, 20, 25))) == 10   # mixed form is empty
     assert lib.ctsmg_init(C.byref(abi.Options(0, 0, 40, 1, 10, 20, 25))) == 10   # nlevsno must be 12
 
 
