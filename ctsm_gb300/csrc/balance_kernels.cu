@@ -36,10 +36,15 @@ __global__ void balance_kernel(ctsmg_soilwater_io w, ctsmg_soiltemp_io t, int nc
     if (c >= ncol) return;
     const int ld = t.ldc, snl = t.snl[c];
     // ---- water: change of column storage minus the scoped fluxes
+    // Zeng-Decker: the sink of every soil level, and recharge leaves the
+    // column only through the aquifer node (jwt == nlevsoi).  Moisture form:
+    // the sink of levels 1..nbedrock, and the bottom flux qcharge unless the
+    // boundary is zero-flux.
+    const int nl = bs.mf_lbc ? t.nbedrock[c] : NLEVSOI;
     double root = 0.0;
-    for (int j = 1; j <= NLEVSOI; ++j) root = root + w.qflx_rootsoi[c + (size_t)(j - 1) * ld];
-    const bool deep = w.zwt[c] > w.zi[c + (size_t)(NLEVSOI + NLEVSNO) * ld];   // jwt == nlevsoi
-    const double net = (w.qflx_infl[c] - root - (deep ? w.qcharge[c] : 0.0)) * dtime;
+    for (int j = 1; j <= nl; ++j) root = root + w.qflx_rootsoi[c + (size_t)(j - 1) * ld];
+    const bool out = bs.mf_lbc ? bs.mf_lbc != 2 : w.zwt[c] > w.zi[c + (size_t)(NLEVSOI + NLEVSNO) * ld];
+    const double net = (w.qflx_infl[c] - root - (out ? w.qcharge[c] : 0.0)) * dtime;
     const double errh2o = (column_water(t, c) - bs.w_bef[c]) - net;
     // ---- soil energy: SoilFluxesMod.F90:170-200 (t_grnd0, tinc), 340-370
     // (eflx_soil_grnd) and 399-430 (errsoi), p2c with wtcol

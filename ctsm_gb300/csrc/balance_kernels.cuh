@@ -14,6 +14,7 @@ struct BalanceState {
     double* errsoi_max;    // (c)
     int* step;             // steps completed
     int skip_steps;
+    int mf_lbc;            // 0: Zeng-Decker; else the moisture form's lower boundary condition
 };
 cudaError_t launch_prestep(const ctsmg_soiltemp_io& t, int ncol, const BalanceState& bs, cudaStream_t s);
 cudaError_t launch_balance(const ctsmg_soilwater_io& w, const ctsmg_soiltemp_io& t, int ncol, double dtime,

@@ -568,6 +568,11 @@ static int read_error(ThreadCtx* c, int* code, int* index, int* level) {
     return 0;
 }
 
+ctsmg_soilwater_movement_nml current_soilwater_nml() {
+    std::lock_guard<std::mutex> lk(g_mu);
+    return g_swm;
+}
+
 int current_snow_method() {
     std::lock_guard<std::mutex> lk(g_mu);
     return g_init ? g_opt.snow_thermal_cond_method : 0;

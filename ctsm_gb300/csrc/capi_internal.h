@@ -29,4 +29,6 @@ size_t field_bytes(const FieldDesc& f, int ldc, int ldp, int ldg = 0);
 int set_error(int code, const char* what, int index, int level);
 int check_filter(const ctsmg_bounds* b, int nf, const int32_t* filt);
 int current_snow_method();
+// the soilwater_movement_inparm namelist in force (ctsmg_init / ctsmg_set_soilwater_movement)
+ctsmg_soilwater_movement_nml current_soilwater_nml();
 } // namespace ctsmg

@@ -16,6 +16,7 @@
 #include "canopy_kernels.cuh"
 #include "balance_kernels.cuh"
 #include "rootmoist_kernels.cuh"
+#include "moisture_form_kernels.cuh"
 #include "capi_internal.h"
 
 namespace ctsmg {
@@ -36,6 +37,8 @@ struct Batch {
     ctsmg_soiltemp_io dst{};
     ctsmg_soilfluxes_io dsf{};
     ctsmg_rootmoist_io drm{};
+    ctsmg_soilwater_movement_nml swm{};   // the namelist when the batch was created
+    MoistureFormArgs mfa{};
     CanopyArgs cargs{};
     double* rootr = nullptr;
     double* mslope = nullptr;
@@ -85,9 +88,22 @@ static cudaError_t enqueue_step(Batch* b) {
                             b->cfg.rootmoist ? b->drm.rootr : b->rootr, b->cfg.npatch, (double*)b->dsw.qflx_rootsoi, ncol, b->stream);
         if (e != cudaSuccess) return e;
     }
+    // the moisture form runs in its own kernel: before the heat solve in
+    // order 0 (SoilWater first), after it (and SoilFluxes) otherwise
+    const int ord = b->cfg.soilfluxes ? 2 : b->cfg.order;
+    const bool mf = b->swm.soilwater_movement_method == 1;
+    if (mf && ord == 0) {
+        e = launch_mf_step(b->dsw, ncol, b->mfa, b->swm.use_flexibleCN, 0, b->err, nullptr, b->stream);
+        if (e != cudaSuccess) return e;
+    }
+    SoilStepFlags fl;
+    fl.water = mf ? 0 : 1;
+    fl.flexcn = b->swm.use_flexibleCN;
+    fl.refresh = (mf && ord >= 1) ? 0 : 1;
     e = launch_soilstep(b->dsw, b->dst, ncol, b->cfg.e_ice, b->cfg.dtime, b->cfg.snow_thermal_cond_method, b->ws,
-                        ncol, b->err, b->stream, b->block, b->cfg.soilfluxes ? 2 : b->cfg.order, nullptr,
-                        b->cfg.soilfluxes ? &b->dsf : nullptr);
+                        ncol, b->err, b->stream, b->block, ord, nullptr, b->cfg.soilfluxes ? &b->dsf : nullptr, fl);
+    if (e == cudaSuccess && mf && ord >= 1)
+        e = launch_mf_step(b->dsw, ncol, b->mfa, b->swm.use_flexibleCN, 1, b->err, nullptr, b->stream);
     if (e != cudaSuccess || !b->cfg.balance) return e;
     return launch_balance(b->dsw, b->dst, ncol, b->cfg.dtime, b->bal, b->stream);
 }
@@ -174,8 +190,28 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
         if (np < 0 || pi < 1 || pi + np - 1 > npatch)
             return set_error(CTSMG_E_ARG, "column patches outside 1..npatch", c + 1, 0);
     }
+    const ctsmg_soilwater_movement_nml swm = current_soilwater_nml();
+    if (!canopy_only && swm.soilwater_movement_method == 1) {
+        if (!sw->nbedrock || !sw->eff_porosity || !sw->num_substeps || (swm.use_flexibleCN && !sw->wa))
+            return set_error(CTSMG_E_ARG, "the moisture form needs nbedrock, eff_porosity, num_substeps (and wa with "
+                             "use_flexibleCN)", 0, 0);
+        for (int c = 0; c < ncol; ++c) {
+            const int nb = st->nbedrock[c];
+            if (nb < 2 || nb > NLEVSOI) return set_error(CTSMG_E_ARG, "nbedrock outside 2..nlevsoi", c + 1, 0);
+            if (swm.lower_boundary_condition == 3 && nb != NLEVSOI)
+                return set_error(CTSMG_E_ARG, "bc_waterTable needs nbedrock = nlevsoi", c + 1, 0);
+        }
+    }
+    if (!canopy_only && swm.use_flexibleCN && !sw->wa) return set_error(CTSMG_E_ARG, "use_flexibleCN needs wa", 0, 0);
+    if (cfg->balance && swm.use_flexibleCN)
+        return set_error(CTSMG_E_UNSUPPORTED, "the balance check does not count the aquifer water the flexibleCN fix "
+                         "moves", 0, 0);
     Batch* b = new Batch();
     b->cfg = *cfg;
+    b->swm = swm;
+    b->mfa = MoistureFormArgs{cfg->e_ice, cfg->dtime, swm.dtmin, swm.verySmall, swm.xTolerUpper, swm.xTolerLower,
+                              swm.lower_boundary_condition, swm.flux_calculation == 42 ? 1 : 0,
+                              moisture_form_max_trials(cfg->dtime, swm.dtmin)};
     auto fail = [&](int rc) { batch_free(b); return rc; };
     cudaError_t e;
     if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(cuda_err(e, "stream"));
@@ -244,6 +280,12 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
         std::memcpy(&b->dst, st, sizeof b->dst);
         if ((rc = add(SOILWATER_TABLE, SOILWATER_NFIELDS, sw, &b->dsw))) return fail(rc);
         if ((rc = add(SOILTEMP_TABLE, SOILTEMP_NFIELDS, st, &b->dst))) return fail(rc);
+        if (swm.soilwater_movement_method == 1) {
+            if ((rc = add(SOILWATER_MF_TABLE, SOILWATER_MF_NFIELDS, sw, &b->dsw))) return fail(rc);
+            b->fields[b->index["eff_porosity"]].use = U_OUT;     // SetSoilWaterFractions runs in the step
+        }
+        if (swm.use_flexibleCN && (rc = add(SOILWATER_FLEXCN_TABLE, SOILWATER_FLEXCN_NFIELDS, sw, &b->dsw)))
+            return fail(rc);
     }
     if (cfg->with_canopy) {
         std::memcpy(&b->cargs.io, cio, sizeof b->cargs.io);
@@ -295,6 +337,7 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
         b->bal.errsoi_max = (double*)m; m += cb;
         b->bal.step = (int*)m;
         b->bal.skip_steps = cfg->skip_steps;
+        b->bal.mf_lbc = swm.soilwater_movement_method == 1 ? swm.lower_boundary_condition : 0;
         if (cfg->soilfluxes) {                  // the prestep saves straight into SoilFluxes' inputs
             b->bal.tssbef = const_cast<double*>(b->dsf.tssbef);
             b->bal.th2osfc_bef = const_cast<double*>(b->dsf.t_h2osfc_bef);
@@ -421,6 +464,10 @@ extern "C" int32_t ctsmg_batch_download2(ctsmg_batch bh, const ctsmg_soilwater_i
     CK(cudaStreamSynchronize(b->stream), "sync");
     int rc;
     if (sw && (rc = download_table(b, SOILWATER_TABLE, SOILWATER_NFIELDS, sw))) return rc;
+    if (sw && b->swm.soilwater_movement_method == 1 &&
+        (rc = download_table(b, SOILWATER_MF_TABLE, SOILWATER_MF_NFIELDS, sw))) return rc;
+    if (sw && b->swm.use_flexibleCN &&
+        (rc = download_table(b, SOILWATER_FLEXCN_TABLE, SOILWATER_FLEXCN_NFIELDS, sw))) return rc;
     if (st && (rc = download_table(b, SOILTEMP_TABLE, SOILTEMP_NFIELDS, st))) return rc;
     if (cio && b->cfg.with_canopy && (rc = download_table(b, CANOPY_TABLE, CANOPY_NFIELDS, cio))) return rc;
     return 0;

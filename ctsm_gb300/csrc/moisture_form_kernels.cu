@@ -18,6 +18,7 @@
 #include "ctsm_device.cuh"
 #include "soil_math.cuh"
 #include "moisture_form_kernels.cuh"
+#include "moisture_form_device.cuh"
 
 namespace ctsmg {
 
@@ -262,32 +263,6 @@ __device__ int mf_column(const ctsmg_soilwater_io& io, int c, const MoistureForm
     return 0;
 }
 
-// SoilWater's use_flexibleCN fix (:331-368) for one column.
-__device__ void flexcn_column(const ctsmg_soilwater_io& io, int c) {
-    const int ld = io.ldc;
-    const double watmin = 0.001;
-    double* liq = io.h2osoi_liq;
-    double carry = liq[c + (size_t)(1 - LS) * ld];
-#pragma unroll 1
-    for (int j = 1; j <= NLEVSOI - 1; ++j) {
-        const size_t ix = c + (size_t)(j - LS) * ld, ixn = ix + ld;
-        const double xs = carry < 0.0 ? watmin - carry : 0.0;
-        liq[ix] = carry + xs;
-        carry = liq[ixn] - xs;
-        liq[ixn] = carry;
-    }
-    const size_t ib = c + (size_t)(NLEVSOI - LS) * ld;
-    const double xs = carry < watmin ? watmin - carry : 0.0;
-    liq[ib] = carry + xs;
-    io.wa[c] = io.wa[c] - xs;
-#pragma unroll 1
-    for (int j = 1; j <= NLEVSOI; ++j) {
-        const size_t ix = c + (size_t)(j - LS) * ld;
-        const double dz = io.dz[ix];
-        ((double*)io.h2osoi_vol)[c + (size_t)(j - 1) * ld] = liq[ix] / (dz * DENH2O) + io.h2osoi_ice[ix] / (dz * DENICE);
-    }
-}
-
 __global__ void __launch_bounds__(128)
 moisture_form_kernel(ctsmg_soilwater_io io, int begc, int nfilt, const int32_t* __restrict__ filt,
                      MoistureFormArgs P, DevError* err) {
@@ -304,6 +279,31 @@ flexcn_kernel(ctsmg_soilwater_io io, int begc, int nfilt, const int32_t* __restr
     const int fc = blockIdx.x * blockDim.x + threadIdx.x;
     if (fc >= nfilt) return;
     flexcn_column(io, (filt ? filt[fc] : fc + begc) - begc);
+}
+
+// One column's soil-water part of a resident model step with the moisture
+// form: SetSoilWaterFractions, SoilWater (moisture form), the flexibleCN fix
+// and, if refresh, the between-step h2osoi_vol refresh
+// (HydrologyNoDrainageMod.F90:302, 346, 580, 590).
+__global__ void __launch_bounds__(128)
+mf_step_kernel(ctsmg_soilwater_io io, int ncol, MoistureFormArgs P, int flexcn, int refresh, DevError* err,
+               const int32_t* __restrict__ filt) {
+    const int fc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fc >= ncol) return;
+    const int c = filt ? filt[fc] - 1 : fc;
+    set_soil_water_fractions(io, c);
+    const int info = mf_column(io, c, P);
+    if (info > 0) report_error(err, c + 1, info, CTSMG_E_SINGULAR);
+    else if (info < 0) report_error(err, c + 1, 0, CTSMG_E_TIMEOUT);
+    if (flexcn) flexcn_column(io, c);
+    if (refresh) refresh_h2osoi_vol(io, c);
+}
+
+cudaError_t launch_mf_step(const ctsmg_soilwater_io& io, int ncol, const MoistureFormArgs& P, int flexcn, int refresh,
+                           DevError* err, const int32_t* d_filt, cudaStream_t s) {
+    if (ncol <= 0) return cudaSuccess;
+    mf_step_kernel<<<(ncol + 127) / 128, 128, 0, s>>>(io, ncol, P, flexcn, refresh, err, d_filt);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_moisture_form(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt,

@@ -25,11 +25,13 @@ inline int moisture_form_max_trials(double dtime, double dtmin) {
 }
 
 __device__ int mf_column(const ctsmg_soilwater_io& io, int c, const MoistureFormArgs& P);
-__device__ void flexcn_column(const ctsmg_soilwater_io& io, int c);
 
 // d_filt: device copy of the 1-based column filter, or NULL for begc .. begc+nfilt-1.
 cudaError_t launch_moisture_form(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt,
                                  const MoistureFormArgs& P, DevError* err, cudaStream_t s);
+// Resident-step form over positions 0..ncol-1 (or the 1-based position filter).
+cudaError_t launch_mf_step(const ctsmg_soilwater_io& io, int ncol, const MoistureFormArgs& P, int flexcn, int refresh,
+                           DevError* err, const int32_t* d_filt, cudaStream_t s);
 cudaError_t launch_flexcn(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt, cudaStream_t s);
 
 } // namespace ctsmg

@@ -256,6 +256,10 @@ extern "C" int32_t ctsmg_pool_create(ctsmg_pool* out, const ctsmg_pool_config* c
     if (!(cfg->dtime > 0.0)) return set_error(CTSMG_E_ARG, "dtime must be positive", 0, 0);
     if (cfg->with_canopy && (!cpar || !pft || cfg->patch_capacity <= 0 || cfg->grid_capacity <= 0))
         return set_error(CTSMG_E_ARG, "with_canopy needs params, pftcon, patch and gridcell capacity", 0, 0);
+    const ctsmg_soilwater_movement_nml swm = current_soilwater_nml();
+    if (swm.soilwater_movement_method != 0 || swm.use_flexibleCN)
+        return set_error(CTSMG_E_UNSUPPORTED, "the serving pool steps the Zeng-Decker form without the flexibleCN fix",
+                         0, 0);
     Pool* P = new Pool();
     P->cfg = *cfg;
     if (P->cfg.max_inflight < 1) P->cfg.max_inflight = 1;

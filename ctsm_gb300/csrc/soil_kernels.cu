@@ -18,6 +18,7 @@
 #include <mutex>
 #include "soil_kernels.cuh"
 #include "soil_math.cuh"
+#include "moisture_form_device.cuh"
 #include "soilfluxes_device.cuh"
 #include "capi_internal.h"
 
@@ -841,12 +842,16 @@ soiltemp_kernel(ctsmg_soiltemp_io io, int begc, int begp, int nfilt, const int32
 template <int BLOCK, int ORDER>
 __global__ void __launch_bounds__(BLOCK)
 soilstep_kernel(ctsmg_soilwater_io wio, ctsmg_soiltemp_io tio, ctsmg_soilfluxes_io sf, int ncol, double e_ice,
-                double dtime, int snow_method, double* ws, int ws_ld, DevError* err, const int32_t* __restrict__ filt) {
+                double dtime, int snow_method, double* ws, int ws_ld, DevError* err, const int32_t* __restrict__ filt,
+                SoilStepFlags fl) {
     const int fc = blockIdx.x * BLOCK + threadIdx.x;
     if (fc >= ncol) return;
     const int c = filt ? filt[fc] - 1 : fc;     // filt: 1-based column positions (pool mode)
     Scratch S{ws, ws_ld, fc};
-    if (ORDER == 0) zd09_column(wio, c, e_ice, dtime);
+    if (ORDER == 0 && fl.water) {
+        zd09_column(wio, c, e_ice, dtime);
+        if (fl.flexcn) flexcn_column(wio, c);
+    }
     int info = soiltemp_column(tio, c, 1, dtime, snow_method, S);
     if (info != 0) report_error(err, c + 1, info, CTSMG_E_SINGULAR);
     if (ORDER == 2) {
@@ -855,15 +860,11 @@ soilstep_kernel(ctsmg_soilwater_io wio, ctsmg_soiltemp_io tio, ctsmg_soilfluxes_
         for (int p = p0; p < p0 + np; ++p) soilfluxes_patch(sf, p, c, dtime);
         soilfluxes_p2c(sf, c, 1);
     }
-    if (ORDER >= 1) zd09_column(wio, c, e_ice, dtime);
-    const int ld = wio.ldc;
-#pragma unroll 1
-    for (int j = 1; j <= NLEVSOI; ++j) {
-        const size_t ix = c + (size_t)(j - LS) * ld;
-        const double dz = wio.dz[ix];
-        ((double*)wio.h2osoi_vol)[c + (size_t)(j - 1) * ld] =
-            tio.h2osoi_liq[ix] / (dz * DENH2O) + tio.h2osoi_ice[ix] / (dz * DENICE);
+    if (ORDER >= 1 && fl.water) {
+        zd09_column(wio, c, e_ice, dtime);
+        if (fl.flexcn) flexcn_column(wio, c);
     }
+    if (fl.refresh) refresh_h2osoi_vol(wio, c);
 }
 
 // Compute_EffecRootFrac_And_VertTranSink_Default
@@ -909,19 +910,19 @@ template <int ORDER>
 static void launch_soilstep_order(const ctsmg_soilwater_io& wio, const ctsmg_soiltemp_io& tio,
                                   const ctsmg_soilfluxes_io& sf, int ncol, double e_ice, double dtime,
                                   int snow_method, double* ws, int ws_ld, DevError* err, cudaStream_t s, int block,
-                                  const int32_t* filt) {
+                                  const int32_t* filt, SoilStepFlags fl) {
     switch (block) {
         case 64:
             soilstep_kernel<64, ORDER><<<(ncol + 63) / 64, 64, 0, s>>>(wio, tio, sf, ncol, e_ice, dtime, snow_method,
-                                                                       ws, ws_ld, err, filt);
+                                                                       ws, ws_ld, err, filt, fl);
             break;
         case 256:
             soilstep_kernel<256, ORDER><<<(ncol + 255) / 256, 256, 0, s>>>(wio, tio, sf, ncol, e_ice, dtime,
-                                                                          snow_method, ws, ws_ld, err, filt);
+                                                                          snow_method, ws, ws_ld, err, filt, fl);
             break;
         default:
             soilstep_kernel<128, ORDER><<<(ncol + 127) / 128, 128, 0, s>>>(wio, tio, sf, ncol, e_ice, dtime,
-                                                                          snow_method, ws, ws_ld, err, filt);
+                                                                          snow_method, ws, ws_ld, err, filt, fl);
             break;
     }
 }
@@ -929,14 +930,14 @@ static void launch_soilstep_order(const ctsmg_soilwater_io& wio, const ctsmg_soi
 cudaError_t launch_soilstep(const ctsmg_soilwater_io& wio, const ctsmg_soiltemp_io& tio, int ncol,
                             double e_ice, double dtime, int snow_method, double* ws, int ws_ld,
                             DevError* err, cudaStream_t s, int block, int order, const int32_t* filt,
-                            const ctsmg_soilfluxes_io* sf) {
+                            const ctsmg_soilfluxes_io* sf, SoilStepFlags fl) {
     if (ncol <= 0) return cudaSuccess;
     if (order == 2 && !sf) return cudaErrorInvalidValue;
     const ctsmg_soilfluxes_io none{};
     const ctsmg_soilfluxes_io& f = sf ? *sf : none;
-    if (order == 2) launch_soilstep_order<2>(wio, tio, f, ncol, e_ice, dtime, snow_method, ws, ws_ld, err, s, block, filt);
-    else if (order == 1) launch_soilstep_order<1>(wio, tio, f, ncol, e_ice, dtime, snow_method, ws, ws_ld, err, s, block, filt);
-    else launch_soilstep_order<0>(wio, tio, f, ncol, e_ice, dtime, snow_method, ws, ws_ld, err, s, block, filt);
+    if (order == 2) launch_soilstep_order<2>(wio, tio, f, ncol, e_ice, dtime, snow_method, ws, ws_ld, err, s, block, filt, fl);
+    else if (order == 1) launch_soilstep_order<1>(wio, tio, f, ncol, e_ice, dtime, snow_method, ws, ws_ld, err, s, block, filt, fl);
+    else launch_soilstep_order<0>(wio, tio, f, ncol, e_ice, dtime, snow_method, ws, ws_ld, err, s, block, filt, fl);
     return cudaGetLastError();
 }
 

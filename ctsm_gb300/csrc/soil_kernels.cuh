@@ -11,10 +11,18 @@ cudaError_t launch_soilwater(const ctsmg_soilwater_io& io, int begc, int nfilt, 
                              double e_ice, double dtime, cudaStream_t s);
 cudaError_t launch_soiltemp(const ctsmg_soiltemp_io& io, int begc, int begp, int nfilt, const int32_t* d_filt,
                             double dtime, int snow_method, double* ws, int ws_ld, DevError* err, cudaStream_t s);
+// What the fused soil step does beside the heat solve: water = 1 runs the
+// Zeng-Decker SoilWater inside (0: the caller runs the moisture form in its
+// own kernel), flexcn = 1 applies the use_flexibleCN fix after it, refresh = 1
+// refreshes h2osoi_vol at the end.
+struct SoilStepFlags {
+    int water = 1, flexcn = 0, refresh = 1;
+};
 cudaError_t launch_soilstep(const ctsmg_soilwater_io& wio, const ctsmg_soiltemp_io& tio, int ncol,
                             double e_ice, double dtime, int snow_method, double* ws, int ws_ld,
                             DevError* err, cudaStream_t s, int block, int order = 0,
-                            const int32_t* filt = nullptr, const ctsmg_soilfluxes_io* sf = nullptr);
+                            const int32_t* filt = nullptr, const ctsmg_soilfluxes_io* sf = nullptr,
+                            SoilStepFlags fl = SoilStepFlags());
 cudaError_t launch_rootsink(const int32_t* col_patchi, const int32_t* col_npatches, const double* wtcol,
                             const double* qflx_tran_veg, const double* rootr, int ldp, double* qflx_rootsoi,
                             int ncol, cudaStream_t s, int ldc = 0, const int32_t* filt = nullptr);

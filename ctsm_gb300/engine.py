@@ -83,7 +83,8 @@ class SoilBatch:
         if self.canopy_only:
             self._sw = self._st = None
         else:
-            self._sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS, state, self.ncol)
+            self._sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS +
+                                   [x for x in abi.SOILWATER_EXTRA if x[0] in state], state, self.ncol)
             self._st = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, state, self.ncol, npatch)
         from .balance import skip_steps as _skip
         self.balance_on = balance
@@ -131,7 +132,8 @@ class SoilBatch:
         if self.canopy_only:
             sw = tt = None
         else:
-            sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS, st, self.ncol)
+            sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS +
+                             [x for x in abi.SOILWATER_EXTRA if x[0] in st], st, self.ncol)
             tt = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, st, self.ncol, self.npatch)
         if self.canopy:
             ci = abi.make_io(abi.CanopyIO, abi.CANOPY_FIELDS, st, self.ncol, self.npatch, self.ngrid, 1)

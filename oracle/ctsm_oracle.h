@@ -29,6 +29,8 @@ int  oracle_dgtsv(int n, double* dl, double* d, double* du, double* b);
 int  oracle_soilwater_mf(const ctsmg_bounds* bounds, int num_hydrologyc, const int32_t* filter_hydrologyc,
                          const ctsmg_soilwater_io* io, double e_ice, double dtime,
                          const ctsmg_soilwater_movement_nml* nml, int* err_col);
+void oracle_set_soil_water_fractions(const ctsmg_bounds* bounds, int num_hydrologyc, const int32_t* filter_hydrologyc,
+                                     const ctsmg_soilwater_io* io);
 void oracle_flexcn_fix(const ctsmg_bounds* bounds, int num_hydrologyc, const int32_t* filter_hydrologyc,
                        const ctsmg_soilwater_io* io);
 int  oracle_root_moist_stress(const ctsmg_bounds* b, int nump, const int32_t* filtp, const ctsmg_rootmoist_io* io);

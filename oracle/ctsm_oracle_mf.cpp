@@ -343,3 +343,19 @@ extern "C" void oracle_flexcn_fix(const ctsmg_bounds* bounds, int num_hydrologyc
                 k.ss(io->h2osoi_liq, j) / (k.ss(io->dz, j) * DENH2O) + k.ss(io->h2osoi_ice, j) / (k.ss(io->dz, j) * DENICE);
     }
 }
+
+// SetSoilWaterFractions (src/biogeophys/SoilHydrologyMod.F90:236-249) with no
+// excess ice: eff_porosity and icefrac on levels 1..nlevsoi.
+extern "C" void oracle_set_soil_water_fractions(const ctsmg_bounds* bounds, int num_hydrologyc,
+                                                const int32_t* filter_hydrologyc, const ctsmg_soilwater_io* io) {
+    const double excess_ice = 0.0;
+    for (int j = 1; j <= NLEVSOI; ++j)
+        for (int fc = 0; fc < num_hydrologyc; ++fc) {
+            Col k{io, filter_hydrologyc[fc] - bounds->begc, io->ldc};
+            const double dz_ext = k.ss(io->dz, j) + excess_ice / DENICE;
+            const double vol_ice = std::min(k.g(io->watsat, j), (k.ss(io->h2osoi_ice, j) + excess_ice) / (dz_ext * DENICE));
+            k.gw(const_cast<double*>(io->eff_porosity), j) = std::max(0.01, k.g(io->watsat, j) - vol_ice);
+            k.gw(io->icefrac, j) = std::min(1.0, vol_ice / k.g(io->watsat, j));
+        }
+}
+

@@ -45,6 +45,8 @@ def lib():
                                              C.c_double, P(abi.SoilWaterMovementNml), P(C.c_int)]
         _LIB.oracle_flexcn_fix.argtypes = [P(abi.Bounds), I, P(C.c_int32), P(abi.SoilWaterIO)]
         _LIB.oracle_flexcn_fix.restype = None
+        _LIB.oracle_set_soil_water_fractions.argtypes = [P(abi.Bounds), I, P(C.c_int32), P(abi.SoilWaterIO)]
+        _LIB.oracle_set_soil_water_fractions.restype = None
         _LIB.oracle_root_moist_stress.argtypes = [P(abi.Bounds), I, P(C.c_int32), P(abi.RootMoistIO)]
         _LIB.oracle_soilfluxes.argtypes = [P(abi.Bounds), I, P(C.c_int32), I, P(C.c_int32), P(abi.SoilFluxesIO),
                                            C.c_double]

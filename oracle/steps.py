@@ -15,14 +15,16 @@ def _p(a, t=C.c_double):
 
 
 def full_steps(A, npatch, ngrid, rootr, nsteps, medlyn_per_patch=False, method=1, itmax=40, snow_method=0,
-               soilfluxes=False, rootmoist=False):
+               soilfluxes=False, rootmoist=False, swm=None):
     """nsteps x (CanopyFluxes, root sink, SoilTemperature, [SoilFluxes,]
     SoilWater, h2osoi_vol refresh) in place on A.  displa / z0mv keep their
     SatellitePhenology values and cgrnds / cgrndl restart from zero every
     step; with soilfluxes the temperatures before SoilTemperature go to
     tssbef / t_h2osfc_bef; with rootmoist btran and rootr come from the root
     moisture stress of the current soil state at the start of every step
-    (A then holds the ROOTMOIST components; `rootr` is not used)."""
+    (A then holds the ROOTMOIST components; `rootr` is not used).  swm (an
+    abi.SoilWaterMovementNml) selects the SoilWater form and the flexibleCN
+    fix; None is the Zeng-Decker form."""
     L = orc.lib()
     ncol = A["zwt"].shape[0]
     L.oracle_set_canopy_params(C.byref(canopy_inputs.make_params()), C.byref(canopy_inputs.make_pftcon()), method,
@@ -59,11 +61,44 @@ def full_steps(A, npatch, ngrid, rootr, nsteps, medlyn_per_patch=False, method=1
                 sf = abi.make_io(abi.SoilFluxesIO, abi.SOILFLUXES_FIELDS, A, ncol, npatch)
                 assert L.oracle_soilfluxes(C.byref(b), ncol, _p(filt_c, C.c_int32), npatch, _p(filt_p, C.c_int32),
                                            C.byref(sf), DT) == 0
-            sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS, A, ncol)
-            assert L.oracle_soilwater(C.byref(b), ncol, _p(filt_c, C.c_int32), C.byref(sw), 6.0, DT) == 0
+            soilwater(L, A, b, filt_c, swm)
             inputs.refresh_h2osoi_vol(A)
     finally:
         A["displa"][:] = displa0
         A["z0mv"][:] = z0mv0
         if medlyn_per_patch:
             L.oracle_set_patch_medlyn(None, None)
+
+
+def soilwater(L, A, b, filt_c, swm=None, e_ice=6.0):
+    """HydrologyNoDrainage's SetSoilWaterFractions and SoilWater
+    (HydrologyNoDrainageMod.F90:302, 346) in the form swm selects."""
+    ncol = A["zwt"].shape[0]
+    n = len(filt_c)
+    fp = _p(filt_c, C.c_int32)
+    if swm is None or swm.soilwater_movement_method == 0:
+        fields = abi.SOILWATER_FIELDS + ([x for x in abi.SOILWATER_EXTRA if x[0] in A] if swm is not None else [])
+        sw = abi.make_io(abi.SoilWaterIO, fields, A, ncol)
+        assert L.oracle_soilwater(C.byref(b), n, fp, C.byref(sw), e_ice, DT) == 0
+    else:
+        sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS + abi.SOILWATER_EXTRA, A, ncol)
+        L.oracle_set_soil_water_fractions(C.byref(b), n, fp, C.byref(sw))
+        e = C.c_int(0)
+        assert L.oracle_soilwater_mf(C.byref(b), n, fp, C.byref(sw), e_ice, DT, C.byref(swm), C.byref(e)) == 0, e.value
+    if swm is not None and swm.use_flexibleCN:
+        L.oracle_flexcn_fix(C.byref(b), n, fp, C.byref(sw))
+
+
+def soil_steps(A, npatch, nsteps, swm=None, snow_method=0):
+    """nsteps x (SoilWater, SoilTemperature, h2osoi_vol refresh): the batched
+    engine's order 0."""
+    L = orc.lib()
+    ncol = A["zwt"].shape[0]
+    b = abi.Bounds(1, ncol, 1, npatch)
+    filt = np.arange(1, ncol + 1, dtype=np.int32)
+    st = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, A, ncol, npatch)
+    for _ in range(nsteps):
+        soilwater(L, A, b, filt, swm)
+        assert L.oracle_soiltemperature(C.byref(b), ncol, _p(filt, C.c_int32), C.byref(st), DT, snow_method) == 0
+        inputs.refresh_h2osoi_vol(A)
+

@@ -131,3 +131,65 @@ def test_flexible_cn_fix(soil_mf, method):
     assert (R["h2osoi_liq"][top] >= 0).all() and (G["h2osoi_liq"][top] >= 0).all()
     if method == 0:
         assert (R["wa"] != A["wa"]).any()
+
+
+STATE = ["h2osoi_liq", "h2osoi_ice", "t_soisno", "t_grnd", "h2osoi_vol", "qcharge", "xmf", "num_substeps",
+         "icefrac", "eff_porosity"]
+
+
+@pytest.mark.parametrize("lower,nbedrock", [(2, (3, 20)), (3, (20, 20))])
+def test_resident_steps_with_moisture_form(soil_mf, lower, nbedrock):
+    """The batched engine's order 0 (SoilWater then SoilTemperature) with the
+    moisture form in its own kernel, 4 steps, against the oracle stepped the
+    same way; column water closes with the zero-flux boundary."""
+    from ctsm_gb300.engine import SoilBatch
+    from oracle.steps import soil_steps
+    A, npatch = inputs.soil_columns(4000, seed=31, snow=True, nbedrock=nbedrock, forcing="full", npatch_max=3,
+                                    zwt=(0.5, 9.5))
+    r = np.random.Generator(np.random.Philox(32))
+    A["qflx_rootsoi"][:] = r.uniform(0.0, 2e-5, A["qflx_rootsoi"].shape)
+    nml = abi.soilwater_movement_nml(1, lower=lower, use_bedrock=1 if lower == 2 else 0)
+    soil_mf.set_soilwater_movement(nml)
+    R = copy.deepcopy(A)
+    soil_steps(R, npatch, 4, swm=nml)
+    G = copy.deepcopy(A)
+    b = SoilBatch(G, npatch, dtime=DT, balance=lower == 2, skip_steps=0)
+    b.run(4)
+    b.sync()
+    b.download()
+    bal = b.balance() if lower == 2 else None
+    b.close()
+    spread = noise_spread(lambda B: soil_steps(B, npatch, 4, swm=nml), A, R, fields=("xmf", "qcharge"))
+    errs, bad = compare(G, R, STATE, 1e-9, spread)
+    assert not bad, {k: errs[k] for k in bad}
+    assert (G["num_substeps"] == R["num_substeps"]).all()
+    if bal is not None:
+        assert np.abs(bal[0]).max() < 1e-8          # errh2o (mm) over the 4 steps
+
+
+def test_full_step_with_moisture_form(soil_mf):
+    """Driver order with SoilFluxes and the moisture form after the heat solve
+    (clm_driver.F90:900, 921, 950), 3 steps."""
+    from ctsm_gb300 import full_inputs as fi
+    from ctsm_gb300.engine import SoilBatch
+    from oracle.steps import full_steps
+    A, npatch, ngrid, rootr = fi.full_state(2500, seed=37)
+    fi.add_soilfluxes_fields(A, npatch, ngrid)
+    nml = abi.soilwater_movement_nml(1)
+    soil_mf.set_soilwater_movement(nml)
+    R = copy.deepcopy(A)
+    full_steps(R, npatch, ngrid, rootr, 3, soilfluxes=True, swm=nml)
+    G = copy.deepcopy(A)
+    b = SoilBatch(G, npatch, canopy=True, ngrid=ngrid, rootr=rootr, soilfluxes=True)
+    b.run(3)
+    b.sync()
+    b.download()
+    b.close()
+    cancel = ("liqcan", "snocan", "eflx_sh_grnd", "qflx_evap_soi", "xmf", "eflx_soil_grnd", "qcharge")
+    spread = noise_spread(lambda B: full_steps(B, npatch, ngrid, rootr, 3, soilfluxes=True, swm=nml), A, R,
+                          fields=cancel, input_ulps=4)
+    for k in ("liqcan", "snocan"):
+        spread[k] = spread[k] + 1e-9 * (np.abs(A["liqcan"]) + np.abs(A["snocan"]))
+    errs, bad = compare(G, R, ["h2osoi_liq", "h2osoi_ice", "t_soisno", "t_grnd", "h2osoi_vol", "t_veg",
+                               "qflx_tran_veg", "num_substeps", "eflx_soil_grnd"] + list(cancel), 1e-9, spread)
+    assert not bad, {k: errs[k] for k in bad}
