@@ -146,6 +146,15 @@ ROOTMOIST_FIELDS = [
 ]
 
 
+# calc_soilevap_resis (sl_14 uses dsl/soilresis, leepielke_1992 soilbeta)
+SOILRESIS_FIELDS = [
+    ("dz", "SS", F64, "in"), ("t_soisno", "SS", F64, "in"), ("h2osoi_liq", "SS", F64, "in"),
+    ("h2osoi_ice", "SS", F64, "in"), ("watsat", "G", F64, "in"), ("bsw", "G", F64, "in"), ("sucsat", "G", F64, "in"),
+    ("watfc", "G", F64, "in"), ("frac_sno", "C", F64, "in"), ("frac_h2osfc", "C", F64, "in"),
+    ("dsl", "C", F64, "out"), ("soilresis", "C", F64, "out"), ("soilbeta", "C", F64, "out"),
+]
+
+
 def _ptr_type(dtype):
     return C.POINTER(C.c_double) if dtype == F64 else C.POINTER(C.c_int32)
 
@@ -166,6 +175,14 @@ class SoilWaterParams(C.Structure):
 
 class SoilWaterIO(C.Structure):
     _fields_ = [("ldc", C.c_int32)] + [(n, _ptr_type(t)) for (n, _, t, _) in SOILWATER_FIELDS + SOILWATER_EXTRA]
+
+
+class SoilResisIO(C.Structure):
+    _fields_ = [("ldc", C.c_int32)] + [(n, _ptr_type(t)) for (n, _, t, _) in SOILRESIS_FIELDS]
+
+
+class SoilResistanceParams(C.Structure):
+    _fields_ = [("soil_resis_method", C.c_int32), ("d_max", C.c_double), ("frac_sat_soil_dsl_init", C.c_double)]
 
 
 class SoilWaterMovementNml(C.Structure):

@@ -18,6 +18,7 @@
 #include "soilfluxes_kernels.cuh"
 #include "rootmoist_kernels.cuh"
 #include "moisture_form_kernels.cuh"
+#include "surface_resistance.cuh"
 #include "capi_internal.h"
 
 namespace ctsmg {
@@ -27,6 +28,9 @@ static std::mutex g_mu;
 static bool g_init = false;
 static ctsmg_options g_opt;
 static ctsmg_soilwater_params g_swp = {6.0};
+// soil_resis_inparm and the two parameter-file values (the parameter file is
+// absent here: 15 mm and 0.8 stand in until ctsmg_set_soil_resistance)
+static ctsmg_soil_resistance_params g_sres = {1, 15.0, 0.8};
 // soilwater_movement_inparm; defaults of the Zeng-Decker form until ctsmg_init
 static ctsmg_soilwater_movement_nml g_swm = {0, 1, 4, 1, 0, 0, 60.0, 1.e-8, 1.e-1, 1.e-2};
 static ctsmg_canopy_params g_cpar;
@@ -182,6 +186,23 @@ const FieldDesc SOILWATER_FLEXCN_TABLE[] = {
     FW(ctsmg_soilwater_io, wa, K_C, 8, U_INOUT),
 };
 const int SOILWATER_FLEXCN_NFIELDS = sizeof(SOILWATER_FLEXCN_TABLE) / sizeof(SOILWATER_FLEXCN_TABLE[0]);
+
+// calc_soilevap_resis: sl_14 (dsl, soilresis) and leepielke_1992 (soilbeta)
+const FieldDesc SOILRESIS_SL14_TABLE[] = {
+    FW(ctsmg_soilresis_io, dz, K_SS, 8, U_IN), FW(ctsmg_soilresis_io, t_soisno, K_SS, 8, U_IN),
+    FW(ctsmg_soilresis_io, h2osoi_liq, K_SS, 8, U_IN), FW(ctsmg_soilresis_io, h2osoi_ice, K_SS, 8, U_IN),
+    FW(ctsmg_soilresis_io, watsat, K_G, 8, U_IN), FW(ctsmg_soilresis_io, bsw, K_G, 8, U_IN),
+    FW(ctsmg_soilresis_io, sucsat, K_G, 8, U_IN), FW(ctsmg_soilresis_io, dsl, K_C, 8, U_OUT),
+    FW(ctsmg_soilresis_io, soilresis, K_C, 8, U_OUT),
+};
+const int SOILRESIS_SL14_NFIELDS = sizeof(SOILRESIS_SL14_TABLE) / sizeof(SOILRESIS_SL14_TABLE[0]);
+const FieldDesc SOILRESIS_LP92_TABLE[] = {
+    FW(ctsmg_soilresis_io, dz, K_SS, 8, U_IN), FW(ctsmg_soilresis_io, h2osoi_liq, K_SS, 8, U_IN),
+    FW(ctsmg_soilresis_io, h2osoi_ice, K_SS, 8, U_IN), FW(ctsmg_soilresis_io, watfc, K_G, 8, U_IN),
+    FW(ctsmg_soilresis_io, frac_sno, K_C, 8, U_IN), FW(ctsmg_soilresis_io, frac_h2osfc, K_C, 8, U_IN),
+    FW(ctsmg_soilresis_io, soilbeta, K_C, 8, U_OUT),
+};
+const int SOILRESIS_LP92_NFIELDS = sizeof(SOILRESIS_LP92_TABLE) / sizeof(SOILRESIS_LP92_TABLE[0]);
 
 #define FT(name, kind, esz, use) FW(ctsmg_soiltemp_io, name, kind, esz, use)
 const FieldDesc SOILTEMP_TABLE[] = {
@@ -566,6 +587,11 @@ static int read_error(ThreadCtx* c, int* code, int* index, int* level) {
     *index = (int)(h.key >> 32);
     *level = (int)((h.key >> 8) & 0xffffff) - 1024;
     return 0;
+}
+
+ctsmg_soil_resistance_params current_soil_resistance() {
+    std::lock_guard<std::mutex> lk(g_mu);
+    return g_sres;
 }
 
 ctsmg_soilwater_movement_nml current_soilwater_nml() {
@@ -1028,6 +1054,44 @@ extern "C" int32_t ctsmg_root_moist_stress(const ctsmg_bounds* bounds, int32_t n
     if ((rc = stage_out(c, io, &dio, ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, ldc, ldp))) return rc;
     e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "root moisture stress");
+    return 0;
+}
+
+extern "C" int32_t ctsmg_set_soil_resistance(const ctsmg_soil_resistance_params* p) {
+    if (!p) return set_error(CTSMG_E_ARG, "null params", 0, 0);
+    if (p->soil_resis_method != 0 && p->soil_resis_method != 1)
+        return set_error(CTSMG_E_ARG, "calc_soilevap_resis:: a soilevap resis function must be specified!", 0, 0);
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_sres = *p;
+    return 0;
+}
+
+extern "C" int32_t ctsmg_soilevap_resis(const ctsmg_bounds* bounds, int32_t num_nolakec, const int32_t* filter_nolakec,
+                                        const ctsmg_soilresis_io* io) {
+    ThreadCtx* c;
+    int rc = ctx_get(&c);
+    if (rc) return rc;
+    if (!io) return set_error(CTSMG_E_ARG, "null io", 0, 0);
+    if ((rc = check_filter(bounds, num_nolakec, filter_nolakec))) return rc;
+    const int ncol = bounds->endc - bounds->begc + 1;
+    if (io->ldc < ncol) return set_error(CTSMG_E_ARG, "ldc smaller than endc-begc+1", 0, 0);
+    const ctsmg_soil_resistance_params par = current_soil_resistance();
+    const FieldDesc* T = par.soil_resis_method == 1 ? SOILRESIS_SL14_TABLE : SOILRESIS_LP92_TABLE;
+    const int NT = par.soil_resis_method == 1 ? SOILRESIS_SL14_NFIELDS : SOILRESIS_LP92_NFIELDS;
+    if (num_nolakec == 0) return 0;
+    const int ldc = io->ldc;
+    if ((rc = arena_reserve(c, table_bytes(T, NT, ldc, 0) + (size_t)num_nolakec * 4 + 4096))) return rc;
+    ctsmg_soilresis_io dio;
+    if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, 0))) return rc;
+    int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_nolakec * 4);
+    cudaError_t e = cudaMemcpyAsync(dfilt, filter_nolakec, (size_t)num_nolakec * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
+    const SoilResisArgs a{par.soil_resis_method, par.d_max, par.frac_sat_soil_dsl_init};
+    e = launch_soilevap_resis(dio, bounds->begc, num_nolakec, dfilt, a, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "soil resistance kernel launch");
+    if ((rc = stage_out(c, io, &dio, T, NT, ldc, 0))) return rc;
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "soil resistance");
     return 0;
 }
 

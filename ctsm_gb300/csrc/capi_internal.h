@@ -15,6 +15,8 @@ extern const FieldDesc SOILWATER_MF_TABLE[];
 extern const int SOILWATER_MF_NFIELDS;
 extern const FieldDesc SOILWATER_FLEXCN_TABLE[];
 extern const int SOILWATER_FLEXCN_NFIELDS;
+extern const FieldDesc SOILRESIS_SL14_TABLE[];
+extern const int SOILRESIS_SL14_NFIELDS;
 extern const FieldDesc SOILTEMP_TABLE[];
 extern const int SOILTEMP_NFIELDS;
 extern const FieldDesc CANOPY_TABLE[];
@@ -31,4 +33,5 @@ int check_filter(const ctsmg_bounds* b, int nf, const int32_t* filt);
 int current_snow_method();
 // the soilwater_movement_inparm namelist in force (ctsmg_init / ctsmg_set_soilwater_movement)
 ctsmg_soilwater_movement_nml current_soilwater_nml();
+ctsmg_soil_resistance_params current_soil_resistance();
 } // namespace ctsmg

@@ -24,6 +24,7 @@ constexpr double CNFAC = 0.5;
 constexpr double THK_BEDROCK = 3.0;
 constexpr double CSOL_BEDROCK = 2.0e6;
 constexpr double THIN_SFCLAYER = 1.0e-6;
+constexpr double CTSMG_PI = 3.14159265358979323846;     // SHR_CONST_PI
 
 constexpr int NLEVSNO = CTSMG_NLEVSNO;
 constexpr int NLEVSOI = CTSMG_NLEVSOI;

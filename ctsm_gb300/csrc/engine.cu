@@ -17,6 +17,7 @@
 #include "balance_kernels.cuh"
 #include "rootmoist_kernels.cuh"
 #include "moisture_form_kernels.cuh"
+#include "surface_resistance.cuh"
 #include "capi_internal.h"
 
 namespace ctsmg {
@@ -38,6 +39,8 @@ struct Batch {
     ctsmg_soilfluxes_io dsf{};
     ctsmg_rootmoist_io drm{};
     ctsmg_soilwater_movement_nml swm{};   // the namelist when the batch was created
+    ctsmg_soilresis_io dsr{};
+    SoilResisArgs sra{};
     MoistureFormArgs mfa{};
     CanopyArgs cargs{};
     double* rootr = nullptr;
@@ -75,6 +78,10 @@ static cudaError_t enqueue_step(Batch* b) {
     const int ncol = b->cfg.ncol;
     if (b->cfg.balance || b->cfg.soilfluxes) {
         e = launch_prestep(b->dst, ncol, b->bal, b->stream);
+        if (e != cudaSuccess) return e;
+    }
+    if (b->cfg.soilresis) {
+        e = launch_soilevap_resis(b->dsr, 1, ncol, nullptr, b->sra, b->stream);
         if (e != cudaSuccess) return e;
     }
     if (b->cfg.rootmoist) {
@@ -156,6 +163,7 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
     const double* medlynintercept_p = in->medlynintercept_p;
     const ctsmg_canopy_params* cpar = in->cpar;
     const ctsmg_pftcon* pft = in->pft;
+    const ctsmg_soilresis_io* sr = in->sr;
     const bool canopy_only = cfg && cfg->order == 2;
     if (!out || !cfg || (!canopy_only && (!sw || !st))) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
     const int ncol = cfg->ncol, npatch = cfg->npatch;
@@ -169,6 +177,11 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
         return set_error(CTSMG_E_ARG, "soilfluxes needs with_canopy, order 1 and the SoilFluxes components", 0, 0);
     if (cfg->soilfluxes && (sf->ldc != ncol || sf->ldp != npatch))
         return set_error(CTSMG_E_ARG, "SoilFluxes arrays must be dense: ldc = ncol, ldp = npatch", 0, 0);
+    const ctsmg_soil_resistance_params sres = current_soil_resistance();
+    if (cfg->soilresis && (!cfg->with_canopy || !sr || sres.soil_resis_method != 1))
+        return set_error(CTSMG_E_ARG, "soilresis needs with_canopy, the sl_14 method and its components", 0, 0);
+    if (cfg->soilresis && sr->ldc != ncol)
+        return set_error(CTSMG_E_ARG, "soil resistance arrays must be dense: ldc = ncol", 0, 0);
     if (cfg->rootmoist && (!cfg->with_canopy || !rm))
         return set_error(CTSMG_E_ARG, "rootmoist needs with_canopy and the root moisture stress components", 0, 0);
     if (cfg->rootmoist && (rm->ldc != ncol || rm->ldp != npatch))
@@ -298,6 +311,11 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
         b->cargs.begp = 1;
         b->cargs.engine = 1;
         const size_t pb = (size_t)npatch * 8;
+        if (cfg->soilresis) {
+            std::memcpy(&b->dsr, sr, sizeof b->dsr);
+            if ((rc = add(SOILRESIS_SL14_TABLE, SOILRESIS_SL14_NFIELDS, sr, &b->dsr))) return fail(rc);
+            b->sra = SoilResisArgs{1, sres.d_max, sres.frac_sat_soil_dsl_init};
+        }
         if (cfg->rootmoist) {
             std::memcpy(&b->drm, rm, sizeof b->drm);
             if ((rc = add(ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, rm, &b->drm))) return fail(rc);
@@ -358,7 +376,8 @@ extern "C" int32_t ctsmg_batch_create3(ctsmg_batch* out, const ctsmg_batch_confi
                                        const double* medlynslope_p, const double* medlynintercept_p,
                                        const ctsmg_canopy_params* cpar, const ctsmg_pftcon* pft) {
     if (cfg && cfg->rootmoist) return set_error(CTSMG_E_ARG, "rootmoist needs ctsmg_batch_open", 0, 0);
-    const ctsmg_batch_inputs in = {sw, st, cio, sf, nullptr, rootr, medlynslope_p, medlynintercept_p, cpar, pft};
+    if (cfg && cfg->soilresis) return set_error(CTSMG_E_ARG, "soilresis needs ctsmg_batch_open", 0, 0);
+    const ctsmg_batch_inputs in = {sw, st, cio, sf, nullptr, rootr, medlynslope_p, medlynintercept_p, cpar, pft, nullptr};
     return ctsmg_batch_open(out, cfg, &in);
 }
 
@@ -379,7 +398,7 @@ extern "C" int32_t ctsmg_batch_create(ctsmg_batch* out, const ctsmg_soilwater_io
     cfg.snow_thermal_cond_method = snow_thermal_cond_method;
     cfg.stomatalcond_method = 1; cfg.itmax_canopy_fluxes = 40;
     cfg.order = 0; cfg.with_canopy = 0; cfg.bucket = 1;
-    cfg.balance = 0; cfg.skip_steps = 0; cfg.soilfluxes = 0; cfg.rootmoist = 0;
+    cfg.balance = 0; cfg.skip_steps = 0; cfg.soilfluxes = 0; cfg.soilresis = 0; cfg.rootmoist = 0;
     return ctsmg_batch_create2(out, &cfg, sw, st, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
 }
 
@@ -445,8 +464,13 @@ static int download_table(Batch* b, const FieldDesc* tab, int nf, const void* hi
 extern "C" int32_t ctsmg_batch_fetch(ctsmg_batch bh, const ctsmg_batch_inputs* in) {
     if (!bh || !in) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
     int rc = ctsmg_batch_download3(bh, in->sw, in->st, in->cio, in->sf);
-    if (rc || !in->rm || !bh->b->cfg.rootmoist) return rc;
-    return download_table(bh->b, ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, in->rm);
+    if (rc) return rc;
+    if (in->rm && bh->b->cfg.rootmoist && (rc = download_table(bh->b, ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, in->rm)))
+        return rc;
+    if (in->sr && bh->b->cfg.soilresis &&
+        (rc = download_table(bh->b, SOILRESIS_SL14_TABLE, SOILRESIS_SL14_NFIELDS, in->sr)))
+        return rc;
+    return 0;
 }
 
 extern "C" int32_t ctsmg_batch_download3(ctsmg_batch bh, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,

@@ -45,7 +45,7 @@ class BatchConfig(C.Structure):
                 ("e_ice", C.c_double), ("snow_thermal_cond_method", C.c_int32), ("stomatalcond_method", C.c_int32),
                 ("itmax_canopy_fluxes", C.c_int32), ("order", C.c_int32), ("with_canopy", C.c_int32),
                 ("bucket", C.c_int32), ("balance", C.c_int32), ("skip_steps", C.c_int32), ("soilfluxes", C.c_int32),
-                ("rootmoist", C.c_int32)]
+                ("soilresis", C.c_int32), ("rootmoist", C.c_int32)]
 
 
 class BatchInputs(C.Structure):
@@ -53,7 +53,8 @@ class BatchInputs(C.Structure):
                 ("cio", C.POINTER(abi.CanopyIO)), ("sf", C.POINTER(abi.SoilFluxesIO)),
                 ("rm", C.POINTER(abi.RootMoistIO)), ("rootr", C.POINTER(C.c_double)),
                 ("medlynslope_p", C.POINTER(C.c_double)), ("medlynintercept_p", C.POINTER(C.c_double)),
-                ("cpar", C.POINTER(abi.CanopyParams)), ("pft", C.POINTER(abi.Pftcon))]
+                ("cpar", C.POINTER(abi.CanopyParams)), ("pft", C.POINTER(abi.Pftcon)),
+                ("sr", C.POINTER(abi.SoilResisIO))]
 
 
 def _pt(x):
@@ -70,7 +71,7 @@ class SoilBatch:
     def __init__(self, state, npatch, dtime=1800.0, e_ice=6.0, snow_thermal_cond_method=0, canopy=False,
                  ngrid=None, rootr=None, order=None, bucket=True, stomatalcond_method=1, itmax=40,
                  params=None, pftcon=None, per_patch_medlyn=False, balance=False, skip_steps=None,
-                 soilfluxes=False, rootmoist=False):
+                 soilfluxes=False, rootmoist=False, soilresis=False):
         from . import canopy_inputs
         self.L = load()
         _bind(self.L)
@@ -92,7 +93,8 @@ class SoilBatch:
                           itmax, (1 if canopy else 0) if order is None else order, 1 if canopy else 0,
                           1 if bucket else 0, 1 if balance else 0,
                           _skip(dtime) if skip_steps is None else skip_steps, 1 if soilfluxes else 0,
-                          1 if rootmoist else 0)
+                          1 if soilresis else 0, 1 if rootmoist else 0)
+        self.soilresis = soilresis
         self.soilfluxes = soilfluxes
         self.rootmoist = rootmoist
         self.h = C.c_void_p()
@@ -108,9 +110,10 @@ class SoilBatch:
                 if soilfluxes else None
             self._rm = abi.make_io(abi.RootMoistIO, abi.ROOTMOIST_FIELDS, state, self.ncol, npatch) \
                 if rootmoist else None
+            self._sr = abi.make_io(abi.SoilResisIO, abi.SOILRESIS_FIELDS, state, self.ncol) if soilresis else None
             self._in = BatchInputs(_pt(self._sw), _pt(self._st), C.pointer(self._ci), _pt(self._sf), _pt(self._rm),
                                    None if self._rootr is None else self._rootr.ctypes.data_as(dp), ms, mi,
-                                   C.pointer(self._par), C.pointer(self._pft))
+                                   C.pointer(self._par), C.pointer(self._pft), _pt(self._sr))
             check(self.L.ctsmg_batch_open(C.byref(self.h), C.byref(cfg), C.byref(self._in)))
         else:
             check(self.L.ctsmg_batch_create2(C.byref(self.h), C.byref(cfg), C.byref(self._sw), C.byref(self._st),
@@ -141,8 +144,10 @@ class SoilBatch:
                 if self.soilfluxes else None
             rm = abi.make_io(abi.RootMoistIO, abi.ROOTMOIST_FIELDS, st, self.ncol, self.npatch) \
                 if self.rootmoist else None
+            sr = abi.make_io(abi.SoilResisIO, abi.SOILRESIS_FIELDS, st, self.ncol) if self.soilresis else None
             check(self.L.ctsmg_batch_fetch(self.h, C.byref(BatchInputs(_pt(sw), _pt(tt), C.pointer(ci), _pt(sf),
-                                                                       _pt(rm), None, None, None, None, None))))
+                                                                       _pt(rm), None, None, None, None, None,
+                                                                       _pt(sr)))))
         else:
             check(self.L.ctsmg_batch_download(self.h, C.byref(sw), C.byref(tt)))
         return st

@@ -177,3 +177,18 @@ def add_rootmoist_fields(A, npatch, rootr, rng=None):
         if n not in A:
             A[n] = np.zeros(abi.field_shape(kind, ncol, npatch, ncol), dtype=np.dtype(t))
     return A
+
+
+def add_soilresis_fields(A):
+    """The calc_soilevap_resis components a full state lacks: watfc by the
+    field-capacity rule of SoilStateInitTimeConstMod.F90:596-600 (hk = 0.1
+    mm/day), frac_sno from frac_sno_eff, and zero-filled dsl / soilbeta."""
+    ncol = A["zwt"].shape[0]
+    secspday = 86400.0
+    A["watfc"] = np.ascontiguousarray(A["watsat"] * (0.1 / (A["hksat"] * secspday)) ** (1.0 / (2.0 * A["bsw"] + 3.0)))
+    A["frac_sno"] = np.ascontiguousarray(A["frac_sno_eff"].copy())
+    for n in ("dsl", "soilbeta"):
+        A[n] = np.zeros(ncol)
+    if "soilresis" not in A:
+        A["soilresis"] = np.zeros(ncol)
+    return A

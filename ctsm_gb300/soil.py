@@ -73,3 +73,23 @@ def SoilFluxes(bounds, num_nolakec, filter_nolakec, num_nolakep, filter_nolakep,
     io = abi.make_io(abi.SoilFluxesIO, abi.SOILFLUXES_FIELDS, state, ncol, npat)
     check(L.ctsmg_soilfluxes(C.byref(bounds), int(num_nolakec), fcp, int(num_nolakep), fpp, C.byref(io), float(dtime)))
 
+
+def set_soil_resistance(method=1, d_max=15.0, frac_sat_soil_dsl_init=0.8):
+    """ctsmg_set_soil_resistance: soil_resis_method (1 sl_14, 0 leepielke_1992)
+    and the parameter-file values d_max (mm) and frac_sat_soil_dsl_init
+    (SurfaceResistanceMod.F90:60-111)."""
+    L = load()
+    L.ctsmg_set_soil_resistance.argtypes = [C.POINTER(abi.SoilResistanceParams)]
+    check(L.ctsmg_set_soil_resistance(C.byref(abi.SoilResistanceParams(method, d_max, frac_sat_soil_dsl_init))))
+
+
+def calc_soilevap_resis(bounds, num_nolakec, filter_nolakec, state):
+    """calc_soilevap_resis (SurfaceResistanceMod.F90:190) over the column filter."""
+    L = load()
+    L.ctsmg_soilevap_resis.argtypes = [C.POINTER(abi.Bounds), C.c_int32, C.POINTER(C.c_int32),
+                                       C.POINTER(abi.SoilResisIO)]
+    f, fp = _filter(filter_nolakec)
+    ncol = bounds.endc - bounds.begc + 1
+    io = abi.make_io(abi.SoilResisIO, abi.SOILRESIS_FIELDS, state, ncol)
+    check(L.ctsmg_soilevap_resis(C.byref(bounds), int(num_nolakec), fp, C.byref(io)))
+

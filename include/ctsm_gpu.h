@@ -403,6 +403,45 @@ typedef struct {
 int32_t ctsmg_root_moist_stress(const ctsmg_bounds* bounds, int32_t num_exposedvegp,
                                 const int32_t* filter_exposedvegp, const ctsmg_rootmoist_io* io);
 
+/* ------------------------------------------------------- soil evaporative resistance */
+/* calc_soilevap_resis (src/biogeophys/SurfaceResistanceMod.F90:190-227),
+ * called from BiogeophysPreFluxCalcs before CanopyFluxes
+ * (BiogeophysPreFluxCalcsMod.F90:113), for natural-vegetation soil columns
+ * (the wetland, glacier and urban branches are not built).
+ * soil_resis_method 1 = sl_14 (dry surface layer: dsl, soilresis; the CLM5
+ * default, namelist_defaults_ctsm.xml:270), 0 = leepielke_1992 (soilbeta).
+ * d_max (mm) and frac_sat_soil_dsl_init come from the parameter file
+ * (readParams, :101-111).                                                   */
+typedef struct {
+    int32_t soil_resis_method;
+    double  d_max;
+    double  frac_sat_soil_dsl_init;
+} ctsmg_soil_resistance_params;
+
+typedef struct {
+    int32_t ldc;
+    const double* dz;             /* [SS] layer thickness (m)                    */
+    const double* t_soisno;       /* [SS] (K)                                    */
+    const double* h2osoi_liq;     /* [SS] (kg/m2)                                */
+    const double* h2osoi_ice;     /* [SS] (kg/m2)                                */
+    const double* watsat;         /* [G]                                         */
+    const double* bsw;            /* [G]                                         */
+    const double* sucsat;         /* [G]  (mm)                                   */
+    const double* watfc;          /* [G]  field capacity (leepielke_1992 only)   */
+    const double* frac_sno;       /* (c)  (leepielke_1992 only)                  */
+    const double* frac_h2osfc;    /* (c)  (leepielke_1992 only)                  */
+    double*       dsl;            /* (c)  out: dry surface layer thickness (mm)  */
+    double*       soilresis;      /* (c)  out: soil evaporative resistance (s/m) */
+    double*       soilbeta;       /* (c)  out: evaporation factor (leepielke)    */
+} ctsmg_soilresis_io;
+
+/* Replaces soil_resistance_readNL (:60-96) and readParams (:101-111). */
+int32_t ctsmg_set_soil_resistance(const ctsmg_soil_resistance_params* p);
+/* Replaces calc_soilevap_resis over the column filter; the components the
+ * method does not use may be NULL.                                          */
+int32_t ctsmg_soilevap_resis(const ctsmg_bounds* bounds, int32_t num_nolakec, const int32_t* filter_nolakec,
+                             const ctsmg_soilresis_io* io);
+
 /* ---------------------------------------------------------------- SoilFluxes */
 /* Components SoilFluxes reads and writes for natural-vegetation columns and
  * patches (src/biogeophys/SoilFluxesMod.F90:36-518; the urban branches and the
@@ -532,6 +571,12 @@ typedef struct {
      * SoilTemperature and SoilWater as the driver does (clm_driver.F90:921);
      * sf (ctsmg_batch_create3) then carries its components.               */
     int32_t soilfluxes;
+    /* soilresis = 1 (with_canopy) computes dsl and soilresis (sl_14, the
+     * parameters of ctsmg_set_soil_resistance) from the resident soil state
+     * at the start of every step, as BiogeophysPreFluxCalcs does before
+     * CanopyFluxes (BiogeophysPreFluxCalcsMod.F90:113); the inputs' sr
+     * carries the components.                                              */
+    int32_t soilresis;
     /* rootmoist = 1 (with_canopy) computes btran and rootr from the resident
      * soil state at the start of every step, as CanopyFluxes does before its
      * iteration (src/biogeophys/CanopyFluxesMod.F90:833-895); the root sink
@@ -551,6 +596,7 @@ typedef struct {
     const double* medlynintercept_p;
     const ctsmg_canopy_params* cpar;
     const ctsmg_pftcon* pft;
+    const ctsmg_soilresis_io* sr;
 } ctsmg_batch_inputs;
 
 /* Create a batch from `in` (the arrays are copied); ctsmg_batch_create*

@@ -53,7 +53,13 @@ def test_unsupported_options_rejected(lib):
 
 def test_struct_layout_matches_ctypes(tmp_path):
     """Compile a C probe against the header and compare sizeof/offsetof."""
-    fields = {"ctsmg_soilwater_io": (abi.SoilWaterIO, ["ldc"] + [f[0] for f in abi.SOILWATER_FIELDS]),
+    fields = {"ctsmg_soilwater_io": (abi.SoilWaterIO, ["ldc"] + [f[0] for f in abi.SOILWATER_FIELDS +
+                                                                    abi.SOILWATER_EXTRA]),
+              "ctsmg_soilwater_movement_nml": (abi.SoilWaterMovementNml,
+                                               [f[0] for f in abi.SoilWaterMovementNml._fields_]),
+              "ctsmg_soilresis_io": (abi.SoilResisIO, ["ldc"] + [f[0] for f in abi.SOILRESIS_FIELDS]),
+              "ctsmg_soil_resistance_params": (abi.SoilResistanceParams,
+                                               [f[0] for f in abi.SoilResistanceParams._fields_]),
               "ctsmg_soiltemp_io": (abi.SoilTempIO, ["ldc", "ldp"] + [f[0] for f in abi.SOILTEMP_FIELDS]),
               "ctsmg_soilfluxes_io": (abi.SoilFluxesIO, ["ldc", "ldp"] + [f[0] for f in abi.SOILFLUXES_FIELDS]),
               "ctsmg_rootmoist_io": (abi.RootMoistIO, ["ldc", "ldp"] + [f[0] for f in abi.ROOTMOIST_FIELDS]),
