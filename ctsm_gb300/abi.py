@@ -146,6 +146,26 @@ ROOTMOIST_FIELDS = [
 ]
 
 
+# BareGroundFluxes (BareGroundFluxesMod.F90:73-545), in the order of
+# ctsmg_baregrnd_io after ldp, ldc, ldg, begg
+BAREGRND_FIELDS = (
+    [("patch_column", "P", I32, "in"), ("patch_gridcell", "P", I32, "in")] +
+    [(n, "GR", F64, "in") for n in ("forc_u", "forc_v", "forc_hgt_u", "forc_hgt_t", "forc_hgt_q")] +
+    [("snl", "C", I32, "in")] +
+    [(n, "C", F64, "in") for n in ("forc_t", "forc_pbot", "forc_q", "forc_th", "forc_rho", "thv", "t_grnd", "qg",
+                                     "qg_snow", "qg_soil", "qg_h2osfc", "dqgdT", "htvp", "z0mg", "soilresis",
+                                     "soilbeta", "t_h2osfc")] +
+    [("t_soisno", "SS", F64, "in"), ("z0hg", "C", F64, "inout"), ("z0qg", "C", F64, "inout"),
+     ("thm", "P", F64, "in")] +
+    [(n, "P", F64, "inout") for n in ("forc_hgt_u_patch", "forc_hgt_t_patch", "forc_hgt_q_patch")] +
+    [(n, "P", F64, "out") for n in (
+        "btran", "t_veg", "rssun", "rssha", "displa", "z0mv", "z0hv", "z0qv", "dlrad", "ulrad", "dhsdt_canopy",
+        "eflx_sh_stem", "z0mg_patch", "z0hg_patch", "z0qg_patch", "zeta", "obu", "ram1", "cgrnds", "cgrndl", "cgrnd",
+        "taux", "tauy", "eflx_sh_grnd", "eflx_sh_tot", "eflx_sh_snow", "eflx_sh_soil", "eflx_sh_h2osfc",
+        "qflx_tran_veg", "qflx_evap_veg", "qflx_evap_soi", "qflx_evap_tot", "qflx_ev_snow", "qflx_ev_soil",
+        "qflx_ev_h2osfc", "t_ref2m", "q_ref2m", "rh_ref2m", "kbm1", "u10_clm", "u10", "va", "vds", "fv", "fm")] +
+    [("num_iter", "P", I32, "out"), ("rootr", "PG", F64, "out"), ("rresis", "PG", F64, "out")])
+
 # calc_soilevap_resis (sl_14 uses dsl/soilresis, leepielke_1992 soilbeta)
 SOILRESIS_FIELDS = [
     ("dz", "SS", F64, "in"), ("t_soisno", "SS", F64, "in"), ("h2osoi_liq", "SS", F64, "in"),
@@ -175,6 +195,11 @@ class SoilWaterParams(C.Structure):
 
 class SoilWaterIO(C.Structure):
     _fields_ = [("ldc", C.c_int32)] + [(n, _ptr_type(t)) for (n, _, t, _) in SOILWATER_FIELDS + SOILWATER_EXTRA]
+
+
+class BareGrndIO(C.Structure):
+    _fields_ = [("ldp", C.c_int32), ("ldc", C.c_int32), ("ldg", C.c_int32), ("begg", C.c_int32)] + \
+               [(n, _ptr_type(t)) for (n, _, t, _) in BAREGRND_FIELDS]
 
 
 class SoilResisIO(C.Structure):

@@ -56,3 +56,22 @@ def RootMoistStress(bounds, num_exposedvegp, filter_exposedvegp, state):
     io = abi.make_io(abi.RootMoistIO, abi.ROOTMOIST_FIELDS, state, ncol, npat)
     check(L.ctsmg_root_moist_stress(C.byref(bounds), int(num_exposedvegp), f.ctypes.data_as(C.POINTER(C.c_int32)),
                                     C.byref(io)))
+
+
+def BareGroundFluxes(bounds, num_noexposedvegp, filter_noexposedvegp, state, ngrid, begg=1):
+    """BareGroundFluxes (BareGroundFluxesMod.F90:73) over the patches without
+    exposed vegetation; the soil resistance method of soil.set_soil_resistance
+    selects soilresis (sl_14) or soilbeta."""
+    L = load()
+    _bind(L)
+    if not getattr(L, "_bare_bound", False):
+        L.ctsmg_baregroundfluxes.argtypes = [C.POINTER(abi.Bounds), C.c_int32, C.POINTER(C.c_int32),
+                                             C.POINTER(abi.BareGrndIO)]
+        L._bare_bound = True
+    f = np.ascontiguousarray(filter_noexposedvegp, dtype=np.int32)
+    ncol = bounds.endc - bounds.begc + 1
+    npat = bounds.endp - bounds.begp + 1
+    io = abi.make_io(abi.BareGrndIO, abi.BAREGRND_FIELDS, state, ncol, npat, ngrid, begg)
+    check(L.ctsmg_baregroundfluxes(C.byref(bounds), int(num_noexposedvegp), f.ctypes.data_as(C.POINTER(C.c_int32)),
+                                   C.byref(io)))
+

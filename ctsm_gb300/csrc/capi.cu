@@ -19,6 +19,7 @@
 #include "rootmoist_kernels.cuh"
 #include "moisture_form_kernels.cuh"
 #include "surface_resistance.cuh"
+#include "baregrnd_kernels.cuh"
 #include "capi_internal.h"
 
 namespace ctsmg {
@@ -203,6 +204,91 @@ const FieldDesc SOILRESIS_LP92_TABLE[] = {
     FW(ctsmg_soilresis_io, soilbeta, K_C, 8, U_OUT),
 };
 const int SOILRESIS_LP92_NFIELDS = sizeof(SOILRESIS_LP92_TABLE) / sizeof(SOILRESIS_LP92_TABLE[0]);
+
+// BareGroundFluxes (the soil resistance method adds soilresis or soilbeta)
+const FieldDesc BAREGRND_TABLE[] = {
+    FW(ctsmg_baregrnd_io, patch_column, K_P, 4, U_IN),
+    FW(ctsmg_baregrnd_io, patch_gridcell, K_P, 4, U_IN),
+    FW(ctsmg_baregrnd_io, forc_u, K_GR, 8, U_IN),
+    FW(ctsmg_baregrnd_io, forc_v, K_GR, 8, U_IN),
+    FW(ctsmg_baregrnd_io, forc_hgt_u, K_GR, 8, U_IN),
+    FW(ctsmg_baregrnd_io, forc_hgt_t, K_GR, 8, U_IN),
+    FW(ctsmg_baregrnd_io, forc_hgt_q, K_GR, 8, U_IN),
+    FW(ctsmg_baregrnd_io, snl, K_C, 4, U_IN),
+    FW(ctsmg_baregrnd_io, forc_t, K_C, 8, U_IN),
+    FW(ctsmg_baregrnd_io, forc_pbot, K_C, 8, U_IN),
+    FW(ctsmg_baregrnd_io, forc_q, K_C, 8, U_IN),
+    FW(ctsmg_baregrnd_io, forc_th, K_C, 8, U_IN),
+    FW(ctsmg_baregrnd_io, forc_rho, K_C, 8, U_IN),
+    FW(ctsmg_baregrnd_io, thv, K_C, 8, U_IN),
+    FW(ctsmg_baregrnd_io, t_grnd, K_C, 8, U_IN),
+    FW(ctsmg_baregrnd_io, qg, K_C, 8, U_IN),
+    FW(ctsmg_baregrnd_io, qg_snow, K_C, 8, U_IN),
+    FW(ctsmg_baregrnd_io, qg_soil, K_C, 8, U_IN),
+    FW(ctsmg_baregrnd_io, qg_h2osfc, K_C, 8, U_IN),
+    FW(ctsmg_baregrnd_io, dqgdT, K_C, 8, U_IN),
+    FW(ctsmg_baregrnd_io, htvp, K_C, 8, U_IN),
+    FW(ctsmg_baregrnd_io, z0mg, K_C, 8, U_IN),
+    FW(ctsmg_baregrnd_io, t_h2osfc, K_C, 8, U_IN),
+    FW(ctsmg_baregrnd_io, t_soisno, K_SS, 8, U_IN),
+    FW(ctsmg_baregrnd_io, z0hg, K_C, 8, U_INOUT),
+    FW(ctsmg_baregrnd_io, z0qg, K_C, 8, U_INOUT),
+    FW(ctsmg_baregrnd_io, thm, K_P, 8, U_IN),
+    FW(ctsmg_baregrnd_io, forc_hgt_u_patch, K_P, 8, U_INOUT),
+    FW(ctsmg_baregrnd_io, forc_hgt_t_patch, K_P, 8, U_INOUT),
+    FW(ctsmg_baregrnd_io, forc_hgt_q_patch, K_P, 8, U_INOUT),
+    FW(ctsmg_baregrnd_io, btran, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, t_veg, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, rssun, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, rssha, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, displa, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, z0mv, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, z0hv, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, z0qv, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, dlrad, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, ulrad, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, dhsdt_canopy, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, eflx_sh_stem, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, z0mg_patch, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, z0hg_patch, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, z0qg_patch, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, zeta, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, obu, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, ram1, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, cgrnds, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, cgrndl, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, cgrnd, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, taux, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, tauy, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, eflx_sh_grnd, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, eflx_sh_tot, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, eflx_sh_snow, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, eflx_sh_soil, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, eflx_sh_h2osfc, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, qflx_tran_veg, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, qflx_evap_veg, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, qflx_evap_soi, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, qflx_evap_tot, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, qflx_ev_snow, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, qflx_ev_soil, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, qflx_ev_h2osfc, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, t_ref2m, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, q_ref2m, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, rh_ref2m, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, kbm1, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, u10_clm, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, u10, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, va, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, vds, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, fv, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, fm, K_P, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, num_iter, K_P, 4, U_OUT),
+    FW(ctsmg_baregrnd_io, rootr, K_PG, 8, U_OUT),
+    FW(ctsmg_baregrnd_io, rresis, K_PG, 8, U_OUT),
+};
+const int BAREGRND_NFIELDS = sizeof(BAREGRND_TABLE) / sizeof(BAREGRND_TABLE[0]);
+const FieldDesc BAREGRND_SOILRESIS[] = {FW(ctsmg_baregrnd_io, soilresis, K_C, 8, U_IN)};
+const FieldDesc BAREGRND_SOILBETA[] = {FW(ctsmg_baregrnd_io, soilbeta, K_C, 8, U_IN)};
 
 #define FT(name, kind, esz, use) FW(ctsmg_soiltemp_io, name, kind, esz, use)
 const FieldDesc SOILTEMP_TABLE[] = {
@@ -1092,6 +1178,55 @@ extern "C" int32_t ctsmg_soilevap_resis(const ctsmg_bounds* bounds, int32_t num_
     if ((rc = stage_out(c, io, &dio, T, NT, ldc, 0))) return rc;
     e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "soil resistance");
+    return 0;
+}
+
+extern "C" int32_t ctsmg_baregroundfluxes(const ctsmg_bounds* bounds, int32_t num_noexposedvegp,
+                                          const int32_t* filter_noexposedvegp, const ctsmg_baregrnd_io* io) {
+    ThreadCtx* c;
+    int rc = ctx_get(&c);
+    if (rc) return rc;
+    if (!io) return set_error(CTSMG_E_ARG, "null io", 0, 0);
+    if (!g_cpar_set) return set_error(CTSMG_E_NOT_INIT, "ctsmg_set_canopy_params has not been called", 0, 0);
+    if (!bounds || bounds->endp < bounds->begp || bounds->endc < bounds->begc)
+        return set_error(CTSMG_E_ARG, "bad bounds", 0, 0);
+    if (num_noexposedvegp < 0 || (num_noexposedvegp > 0 && !filter_noexposedvegp))
+        return set_error(CTSMG_E_ARG, "bad patch filter", 0, 0);
+    const int ncol = bounds->endc - bounds->begc + 1, npat = bounds->endp - bounds->begp + 1;
+    if (io->ldp < npat || io->ldc < ncol || io->ldg < 1) return set_error(CTSMG_E_ARG, "ldp/ldc/ldg too small", 0, 0);
+    for (int i = 0; i < num_noexposedvegp; ++i) {
+        const int pg = filter_noexposedvegp[i];
+        if (pg < bounds->begp || pg > bounds->endp) return set_error(CTSMG_E_ARG, "filter index outside bounds", pg, 0);
+        const int cc = io->patch_column[pg - bounds->begp], gg = io->patch_gridcell[pg - bounds->begp];
+        if (cc < bounds->begc || cc > bounds->endc) return set_error(CTSMG_E_ARG, "patch column outside bounds", pg, 0);
+        if (gg < io->begg || gg > io->begg + io->ldg - 1) return set_error(CTSMG_E_ARG, "patch gridcell outside ldg", pg, 0);
+        const int s = io->snl[cc - bounds->begc];
+        if (s > 0 || s < -NLEVSNO) return set_error(CTSMG_E_ARG, "snl outside -nlevsno..0", cc, 0);
+    }
+    ctsmg_canopy_params cp;
+    { std::lock_guard<std::mutex> lk(g_mu); cp = g_cpar; }
+    const ctsmg_soil_resistance_params sres = current_soil_resistance();
+    std::vector<FieldDesc> tab(BAREGRND_TABLE, BAREGRND_TABLE + BAREGRND_NFIELDS);
+    tab.push_back(sres.soil_resis_method == 1 ? BAREGRND_SOILRESIS[0] : BAREGRND_SOILBETA[0]);
+    if (num_noexposedvegp == 0) return 0;
+    const int ldc = io->ldc, ldp = io->ldp, ldg = io->ldg;
+    const FieldDesc* T = tab.data();
+    const int NT = (int)tab.size();
+    size_t need = table_bytes(T, NT, ldc, ldp, ldg) + (size_t)num_noexposedvegp * 4 + (size_t)ldc * 4 + 8192;
+    if ((rc = arena_reserve(c, need))) return rc;
+    ctsmg_baregrnd_io dio;
+    if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, ldp, ldg))) return rc;
+    int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_noexposedvegp * 4);
+    int* dlast = (int*)arena_take(c, (size_t)ldc * 4);
+    cudaError_t e = cudaMemcpyAsync(dfilt, filter_noexposedvegp, (size_t)num_noexposedvegp * 4, cudaMemcpyHostToDevice,
+                                    c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
+    const BareArgs a{cp.a_coef, cp.a_exp, cp.wind_min, cp.zetamaxstable, sres.soil_resis_method};
+    e = launch_baregrnd(dio, bounds->begc, bounds->begp, num_noexposedvegp, dfilt, a, dlast, ldc, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "bare ground kernel launch");
+    if ((rc = stage_out(c, io, &dio, T, NT, ldc, ldp, ldg))) return rc;
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "bare ground fluxes");
     return 0;
 }
 

@@ -72,6 +72,7 @@ def full_state(ncol, seed=0, npatch_max=4, om_frac_sf=1.0, rng=None):
     grid = dict(forc_u=r.uniform(0.5, 20.0, ngrid), forc_v=np.zeros(ngrid), forc_hgt_u=np.full(ngrid, 30.0),
                 forc_hgt_t=np.full(ngrid, 30.0), forc_hgt_q=np.full(ngrid, 30.0), forc_pco2=400.e-6 * pbot,
                 forc_po2=0.209 * pbot, dayl=r.uniform(28800.0, 57600.0, ngrid), max_dayl=np.full(ngrid, 57600.0))
+    col["forc_t"] = forc_t
     for k, v in list(col.items()) + list(grid.items()):
         A[k] = np.ascontiguousarray(v)
     A["thm"] = forc_t[pcol] + 0.0098 * 30.0
@@ -192,3 +193,26 @@ def add_soilresis_fields(A):
     if "soilresis" not in A:
         A["soilresis"] = np.zeros(ncol)
     return A
+
+
+def add_baregrnd_fields(A, npatch, ngrid):
+    """The BareGroundFluxes components a full state lacks: the last step's
+    ground roughness for heat / moisture (z0hg = z0qg = z0mg/10, builder's
+    choice) and forcing heights at patch level (forc_hgt + roughness, as the
+    routine leaves them), soilbeta, and zero-filled outputs."""
+    ncol = A["zwt"].shape[0]
+    if "watfc" not in A:
+        add_soilresis_fields(A)
+    A["z0hg"] = np.ascontiguousarray(A["z0mg"] / 10.0)
+    A["z0qg"] = A["z0hg"].copy()
+    pc = A["patch_column"] - 1
+    pg = A["patch_gridcell"] - 1
+    A["forc_hgt_u_patch"] = np.ascontiguousarray(A["forc_hgt_u"][pg] + A["z0mg"][pc])
+    A["forc_hgt_t_patch"] = np.ascontiguousarray(A["forc_hgt_t"][pg] + A["z0hg"][pc])
+    A["forc_hgt_q_patch"] = np.ascontiguousarray(A["forc_hgt_q"][pg] + A["z0qg"][pc])
+    A["soilbeta"] = np.ascontiguousarray(np.clip(A["h2osoi_vol"][0] / A["watsat"][0], 0.0, 1.0))
+    for (n, kind, t, u) in abi.BAREGRND_FIELDS:
+        if n not in A:
+            A[n] = np.zeros(abi.field_shape(kind, ncol, npatch, ngrid), dtype=np.dtype(t))
+    return A
+

@@ -403,6 +403,44 @@ typedef struct {
 int32_t ctsmg_root_moist_stress(const ctsmg_bounds* bounds, int32_t num_exposedvegp,
                                 const int32_t* filter_exposedvegp, const ctsmg_rootmoist_io* io);
 
+/* ------------------------------------------------------------ BareGroundFluxes */
+/* Components BareGroundFluxes reads and writes for the patches without
+ * exposed vegetation (src/biogeophys/BareGroundFluxesMod.F90:73-545;
+ * called at clm_driver.F90:718): three Monin-Obukhov iterations with
+ * FrictionVelocity, ZengWang2007 roughness, the ground evaporation
+ * resistance of the soil resistance method in force (sl_14: soilresis,
+ * leepielke_1992: soilbeta), the 2 m diagnostics.  The human-stress
+ * indices, lch4 and the landunit-level reference-temperature copies are not
+ * built.  a_coef, a_exp, wind_min and zetamaxstable are taken from
+ * ctsmg_set_canopy_params (the reference reads the same parameter names).  */
+typedef struct {
+    int32_t ldp, ldc, ldg, begg;
+    const int32_t* patch_column; const int32_t* patch_gridcell;
+    /* gridcell forcing */
+    const double *forc_u, *forc_v, *forc_hgt_u, *forc_hgt_t, *forc_hgt_q;
+    /* column */
+    const int32_t* snl;
+    const double *forc_t, *forc_pbot, *forc_q, *forc_th, *forc_rho, *thv, *t_grnd, *qg, *qg_snow, *qg_soil,
+                 *qg_h2osfc, *dqgdT, *htvp, *z0mg, *soilresis, *soilbeta, *t_h2osfc;
+    const double* t_soisno;                        /* [SS]                              */
+    double *z0hg, *z0qg;                           /* (c) inout: the last step's roughness in, this step's out */
+    /* patch */
+    const double* thm;
+    double *forc_hgt_u_patch;                      /* (p) inout: the last step's height in */
+    double *forc_hgt_t_patch, *forc_hgt_q_patch;   /* (p) inout                         */
+    double *btran, *t_veg, *rssun, *rssha, *displa, *z0mv, *z0hv, *z0qv, *dlrad, *ulrad, *dhsdt_canopy,
+           *eflx_sh_stem, *z0mg_patch, *z0hg_patch, *z0qg_patch, *zeta, *obu, *ram1, *cgrnds, *cgrndl, *cgrnd,
+           *taux, *tauy, *eflx_sh_grnd, *eflx_sh_tot, *eflx_sh_snow, *eflx_sh_soil, *eflx_sh_h2osfc,
+           *qflx_tran_veg, *qflx_evap_veg, *qflx_evap_soi, *qflx_evap_tot, *qflx_ev_snow, *qflx_ev_soil,
+           *qflx_ev_h2osfc, *t_ref2m, *q_ref2m, *rh_ref2m, *kbm1, *u10_clm, *u10, *va, *vds, *fv, *fm;
+    int32_t* num_iter;
+    double *rootr, *rresis;                        /* [PG] out: zero                    */
+} ctsmg_baregrnd_io;
+
+/* Replaces BareGroundFluxes over filter_noexposedvegp (1-based patches). */
+int32_t ctsmg_baregroundfluxes(const ctsmg_bounds* bounds, int32_t num_noexposedvegp,
+                               const int32_t* filter_noexposedvegp, const ctsmg_baregrnd_io* io);
+
 /* ------------------------------------------------------- soil evaporative resistance */
 /* calc_soilevap_resis (src/biogeophys/SurfaceResistanceMod.F90:190-227),
  * called from BiogeophysPreFluxCalcs before CanopyFluxes

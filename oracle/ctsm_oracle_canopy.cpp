@@ -912,3 +912,147 @@ extern "C" int oracle_root_moist_stress(const ctsmg_bounds* b, int nump, const i
     return 0;
 }
 
+// BareGroundFluxes (src/biogeophys/BareGroundFluxesMod.F90:73-545) over
+// filter_noexposedvegp, statement by statement; soil_resis_method 1 (sl_14,
+// soilresis) or 0 (leepielke_1992, soilbeta).  The canopy parameters carry
+// a_coef, a_exp, wind_min and zetamaxstable.
+extern "C" int oracle_baregroundfluxes(const ctsmg_bounds* b, int nump, const int32_t* filtp,
+                                       const ctsmg_baregrnd_io* io, int soil_resis_method) {
+    const ctsmg_canopy_params& P = g_par.c;
+    const double zii = 1000.0, beta = 1.0;
+    const int ldp = io->ldp, ldc = io->ldc, LS_ = -CTSMG_NLEVSNO + 1;
+    std::vector<double> zldis(nump), ur(nump), dth(nump), dqh(nump), obu(nump), um(nump), fm(nump);
+    std::vector<FVOut> fvo(nump);
+    auto PC = [&](int f) { return io->patch_column[filtp[f] - b->begp] - b->begc; };
+    auto PG = [&](int f) { return io->patch_gridcell[filtp[f] - b->begp] - io->begg; };
+    for (int f = 0; f < nump; ++f) {
+        const int p = filtp[f] - b->begp, c = PC(f);
+        io->btran[p] = 0.0;
+        io->t_veg[p] = io->forc_t[c];
+        const double cf_bare = io->forc_pbot[c] / (RGAS * 0.001 * io->thm[p]) * 1.e06;
+        io->rssun[p] = 1.0 / 1.e15 * cf_bare;
+        io->rssha[p] = 1.0 / 1.e15 * cf_bare;
+        for (int j = 1; j <= CTSMG_NLEVGRND; ++j) {
+            io->rootr[p + (size_t)(j - 1) * ldp] = 0.0;
+            io->rresis[p + (size_t)(j - 1) * ldp] = 0.0;
+        }
+    }
+    for (int f = 0; f < nump; ++f) {
+        const int p = filtp[f] - b->begp, c = PC(f), g = PG(f);
+        io->displa[p] = 0.0; io->z0mv[p] = 0.0; io->z0hv[p] = 0.0; io->z0qv[p] = 0.0;
+        io->dlrad[p] = 0.0; io->ulrad[p] = 0.0; io->dhsdt_canopy[p] = 0.0; io->eflx_sh_stem[p] = 0.0;
+        ur[f] = std::max(P.wind_min, std::sqrt(io->forc_u[g] * io->forc_u[g] + io->forc_v[g] * io->forc_v[g]));
+        dth[f] = io->thm[p] - io->t_grnd[c];
+        dqh[f] = io->forc_q[c] - io->qg[c];
+        const double dthv = dth[f] * (1.0 + 0.61 * io->forc_q[c]) + 0.61 * io->forc_th[c] * dqh[f];
+        zldis[f] = io->forc_hgt_u_patch[p];
+        io->z0mg_patch[p] = io->z0mg[c];
+        io->z0hg_patch[p] = io->z0hg[c];
+        io->z0qg_patch[p] = io->z0qg[c];
+        // MoninObukIni (FrictionVelocityMod.F90:1158-1209)
+        const double wc = 0.5;
+        if (dthv >= 0.0) um[f] = std::max(ur[f], 0.1);
+        else um[f] = std::sqrt(ur[f] * ur[f] + wc * wc);
+        const double rib = GRAV * zldis[f] * dthv / (io->thv[c] * um[f] * um[f]);
+        double zeta;
+        if (rib >= 0.0) {
+            zeta = rib * o_log(zldis[f] / io->z0mg_patch[p]) / (1.0 - 5.0 * std::min(rib, 0.19));
+            zeta = std::min(P.zetamaxstable, std::max(zeta, 0.01));
+        } else {
+            zeta = rib * o_log(zldis[f] / io->z0mg_patch[p]);
+            zeta = std::max(-100.0, std::min(zeta, -0.01));
+        }
+        obu[f] = zldis[f] / zeta;
+        io->num_iter[p] = 0;
+    }
+    for (int iter = 1; iter <= 3; ++iter) {
+        for (int f = 0; f < nump; ++f) {
+            const int p = filtp[f] - b->begp;
+            friction_velocity(io->displa[p], io->z0mg_patch[p], io->z0hg_patch[p], io->z0qg_patch[p], obu[f], iter,
+                              ur[f], um[f], io->forc_hgt_u_patch[p], io->forc_hgt_t_patch[p], io->forc_hgt_q_patch[p],
+                              fm[f], fvo[f]);
+        }
+        for (int f = 0; f < nump; ++f) {
+            const int p = filtp[f] - b->begp, c = PC(f), g = PG(f);
+            const double ustar = fvo[f].ustar;
+            const double tstar = fvo[f].temp1 * dth[f];
+            const double qstar = fvo[f].temp2 * dqh[f];
+            io->z0hg_patch[p] = io->z0mg_patch[p] / o_exp(P.a_coef * o_pow(ustar * io->z0mg_patch[p] / NU_PARAM, P.a_exp));
+            io->z0qg_patch[p] = io->z0hg_patch[p];
+            io->forc_hgt_u_patch[p] = io->forc_hgt_u[g] + io->z0mg_patch[p] + io->displa[p];
+            io->forc_hgt_t_patch[p] = io->forc_hgt_t[g] + io->z0hg_patch[p] + io->displa[p];
+            io->forc_hgt_q_patch[p] = io->forc_hgt_q[g] + io->z0qg_patch[p] + io->displa[p];
+            const double thvstar = tstar * (1.0 + 0.61 * io->forc_q[c]) + 0.61 * io->forc_th[c] * qstar;
+            double zeta = zldis[f] * VKC * GRAV * thvstar / (ustar * ustar * io->thv[c]);
+            if (zeta >= 0.0) {
+                zeta = std::min(P.zetamaxstable, std::max(zeta, 0.01));
+                um[f] = std::max(ur[f], 0.1);
+            } else {
+                zeta = std::max(-100.0, std::min(zeta, -0.01));
+                const double wc = beta * o_pow(-GRAV * ustar * thvstar * zii / io->thv[c], 0.333);
+                um[f] = std::sqrt(ur[f] * ur[f] + wc * wc);
+            }
+            io->zeta[p] = zeta;
+            obu[f] = zldis[f] / zeta;
+            io->num_iter[p] = iter;
+        }
+    }
+    for (int f = 0; f < nump; ++f) {
+        const int p = filtp[f] - b->begp, c = PC(f), g = PG(f);
+        const FVOut& o = fvo[f];
+        io->obu[p] = obu[f]; io->fm[p] = fm[f];
+        io->u10_clm[p] = o.u10_clm; io->u10[p] = o.u10; io->va[p] = o.va; io->vds[p] = o.vds; io->fv[p] = o.fv;
+        const double ram = 1.0 / (o.ustar * o.ustar / um[f]);
+        const double rah = 1.0 / (o.temp1 * o.ustar);
+        const double raw = 1.0 / (o.temp2 * o.ustar);
+        const double raih = io->forc_rho[c] * CPAIR / rah;
+        double forc_qs, forc_esat;
+        qsat(io->forc_t[c], io->forc_pbot[c], &forc_qs, &forc_esat, nullptr);
+        const double forc_e = std::max((io->forc_q[c] * io->forc_pbot[c]) / (io->forc_q[c] + 0.622), 0.01 * forc_esat);
+        const double t = io->t_grnd[c];
+        double forc_dewpoint;            // dewpoint (:558-578)
+        if (t < TFRZ) forc_dewpoint = 273.86 * o_log(forc_e / 611.21) / (22.587 - o_log(forc_e / 611.21));
+        else forc_dewpoint = 243.04 * o_log(forc_e / 610.94) / (17.625 - o_log(forc_e / 610.94));
+        forc_dewpoint = forc_dewpoint + TFRZ;
+        double raiw = 0.0;
+        if (dqh[f] > 0.0) {
+            if (io->t_grnd[c] > forc_dewpoint) raiw = 0.0;
+            else raiw = io->forc_rho[c] / raw;
+        } else {
+            if (soil_resis_method == 0) {
+                if (io->t_grnd[c] > forc_dewpoint) raiw = 0.0;
+                else raiw = io->soilbeta[c] * io->forc_rho[c] / raw;
+            }
+            if (soil_resis_method == 1) raiw = io->forc_rho[c] / (raw + io->soilresis[c]);
+        }
+        io->ram1[p] = ram;
+        io->cgrnds[p] = raih;
+        io->cgrndl[p] = raiw * io->dqgdT[c];
+        io->cgrnd[p] = io->cgrnds[p] + io->htvp[c] * io->cgrndl[p];
+        io->taux[p] = -io->forc_rho[c] * io->forc_u[g] / ram;
+        io->tauy[p] = -io->forc_rho[c] * io->forc_v[g] / ram;
+        io->eflx_sh_grnd[p] = -raih * dth[f];
+        io->eflx_sh_tot[p] = io->eflx_sh_grnd[p];
+        const int snl = io->snl[c];
+        io->eflx_sh_snow[p] = -raih * (io->thm[p] - io->t_soisno[c + (size_t)(snl + 1 - LS_) * ldc]);
+        io->eflx_sh_soil[p] = -raih * (io->thm[p] - io->t_soisno[c + (size_t)(1 - LS_) * ldc]);
+        io->eflx_sh_h2osfc[p] = -raih * (io->thm[p] - io->t_h2osfc[c]);
+        io->qflx_tran_veg[p] = 0.0;
+        io->qflx_evap_veg[p] = 0.0;
+        io->qflx_evap_soi[p] = -raiw * dqh[f];
+        io->qflx_evap_tot[p] = io->qflx_evap_soi[p];
+        io->qflx_ev_snow[p] = -raiw * (io->forc_q[c] - io->qg_snow[c]);
+        io->qflx_ev_soil[p] = -raiw * (io->forc_q[c] - io->qg_soil[c]);
+        io->qflx_ev_h2osfc[p] = -raiw * (io->forc_q[c] - io->qg_h2osfc[c]);
+        io->t_ref2m[p] = io->thm[p] + o.temp1 * dth[f] * (1.0 / o.temp12m - 1.0 / o.temp1);
+        io->q_ref2m[p] = io->forc_q[c] + o.temp2 * dqh[f] * (1.0 / o.temp22m - 1.0 / o.temp2);
+        double qsat_ref2m, e_ref2m;
+        qsat(io->t_ref2m[p], io->forc_pbot[c], &qsat_ref2m, &e_ref2m, nullptr);
+        io->rh_ref2m[p] = std::min(100.0, io->q_ref2m[p] / qsat_ref2m * 100.0);
+        io->kbm1[p] = o_log(io->z0mg_patch[p] / io->z0hg_patch[p]);
+        io->z0hg[c] = io->z0hg_patch[p];
+        io->z0qg[c] = io->z0qg_patch[p];
+    }
+    return 0;
+}
+

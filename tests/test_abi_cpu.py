@@ -57,6 +57,8 @@ def test_struct_layout_matches_ctypes(tmp_path):
                                                                     abi.SOILWATER_EXTRA]),
               "ctsmg_soilwater_movement_nml": (abi.SoilWaterMovementNml,
                                                [f[0] for f in abi.SoilWaterMovementNml._fields_]),
+              "ctsmg_baregrnd_io": (abi.BareGrndIO, ["ldp", "ldc", "ldg", "begg"] +
+                                    [f[0] for f in abi.BAREGRND_FIELDS]),
               "ctsmg_soilresis_io": (abi.SoilResisIO, ["ldc"] + [f[0] for f in abi.SOILRESIS_FIELDS]),
               "ctsmg_soil_resistance_params": (abi.SoilResistanceParams,
                                                [f[0] for f in abi.SoilResistanceParams._fields_]),
