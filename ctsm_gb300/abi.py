@@ -166,6 +166,21 @@ BAREGRND_FIELDS = (
         "qflx_ev_h2osfc", "t_ref2m", "q_ref2m", "rh_ref2m", "kbm1", "u10_clm", "u10", "va", "vds", "fv", "fm")] +
     [("num_iter", "P", I32, "out"), ("rootr", "PG", F64, "out"), ("rresis", "PG", F64, "out")])
 
+# hydrology neighbours of SoilWater (ctsmg_hydrology_io order after ldc)
+HYDROLOGY_FIELDS = [
+    ("nbedrock", "C", I32, "in"), ("z", "SS", F64, "in"), ("zi", "ZI", F64, "in"), ("dz", "SS", F64, "in"),
+    ("t_soisno", "SS", F64, "in"), ("h2osoi_liq", "SS", F64, "inout"), ("h2osoi_ice", "SS", F64, "inout"),
+    ("h2osoi_vol", "G", F64, "inout"), ("h2osfc", "C", F64, "inout"), ("zwt", "C", F64, "inout"),
+    ("zwt_perched", "C", F64, "inout"), ("frost_table", "C", F64, "inout"), ("icefrac", "G", F64, "out"),
+    ("watsat", "G", F64, "in"), ("hksat", "G", F64, "in"), ("bsw", "G", F64, "in"), ("sucsat", "G", F64, "in"),
+    ("eff_porosity", "G", F64, "in"), ("topo_slope", "C", F64, "in"), ("wtfact", "C", F64, "in"),
+    ("qflx_rain_plus_snomelt", "C", F64, "in"), ("qflx_snwcp_liq", "C", F64, "in"),
+    ("fsat", "C", F64, "out"), ("fcov", "C", F64, "out"), ("qflx_sat_excess_surf", "C", F64, "out"),
+    ("qflx_drain_perched", "C", F64, "out"), ("qflx_latflow_out", "C", F64, "out"),
+    ("qflx_latflow_in", "C", F64, "out"), ("qflx_rsub_sat", "C", F64, "out"), ("qflx_drain", "C", F64, "out"),
+    ("qflx_qrgwl", "C", F64, "out"), ("qflx_ice_runoff_xs", "C", F64, "out"),
+]
+
 # calc_soilevap_resis (sl_14 uses dsl/soilresis, leepielke_1992 soilbeta)
 SOILRESIS_FIELDS = [
     ("dz", "SS", F64, "in"), ("t_soisno", "SS", F64, "in"), ("h2osoi_liq", "SS", F64, "in"),
@@ -200,6 +215,15 @@ class SoilWaterIO(C.Structure):
 class BareGrndIO(C.Structure):
     _fields_ = [("ldp", C.c_int32), ("ldc", C.c_int32), ("ldg", C.c_int32), ("begg", C.c_int32)] + \
                [(n, _ptr_type(t)) for (n, _, t, _) in BAREGRND_FIELDS]
+
+
+class HydrologyIO(C.Structure):
+    _fields_ = [("ldc", C.c_int32)] + [(n, _ptr_type(t)) for (n, _, t, _) in HYDROLOGY_FIELDS]
+
+
+class SoilHydrologyParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("aq_sp_yield_min", "n_baseflow", "baseflow_scalar",
+                                           "perched_baseflow_scalar", "e_ice", "fff")]
 
 
 class SoilResisIO(C.Structure):

@@ -20,6 +20,7 @@
 #include "moisture_form_kernels.cuh"
 #include "surface_resistance.cuh"
 #include "baregrnd_kernels.cuh"
+#include "hydrology_kernels.cuh"
 #include "capi_internal.h"
 
 namespace ctsmg {
@@ -32,6 +33,9 @@ static ctsmg_soilwater_params g_swp = {6.0};
 // soil_resis_inparm and the two parameter-file values (the parameter file is
 // absent here: 15 mm and 0.8 stand in until ctsmg_set_soil_resistance)
 static ctsmg_soil_resistance_params g_sres = {1, 15.0, 0.8};
+// SoilHydrologyMod / SaturatedExcessRunoffMod parameter-file values (absent
+// here; these stand in until ctsmg_set_soilhydrology_params)
+static ctsmg_soilhydrology_params g_shp = {0.01, 1.0, 1.0e-2, 1.0e-5, 6.0, 0.5};
 // soilwater_movement_inparm; defaults of the Zeng-Decker form until ctsmg_init
 static ctsmg_soilwater_movement_nml g_swm = {0, 1, 4, 1, 0, 0, 60.0, 1.e-8, 1.e-1, 1.e-2};
 static ctsmg_canopy_params g_cpar;
@@ -287,6 +291,85 @@ const FieldDesc BAREGRND_TABLE[] = {
     FW(ctsmg_baregrnd_io, rresis, K_PG, 8, U_OUT),
 };
 const int BAREGRND_NFIELDS = sizeof(BAREGRND_TABLE) / sizeof(BAREGRND_TABLE[0]);
+
+// SaturatedExcessRunoff, PerchedWaterTable, ThetaBasedWaterTable,
+// PerchedLateralFlow, SubsurfaceLateralFlow: the components each reads or writes
+const FieldDesc HYD_SAT_TABLE[] = {
+    FW(ctsmg_hydrology_io, zwt, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, zwt_perched, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, frost_table, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, wtfact, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, qflx_rain_plus_snomelt, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, fsat, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, fcov, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_sat_excess_surf, K_C, 8, U_OUT),
+};
+const int HYD_SAT_TABLE_N = sizeof(HYD_SAT_TABLE) / sizeof(HYD_SAT_TABLE[0]);
+const FieldDesc HYD_PWT_TABLE[] = {
+    FW(ctsmg_hydrology_io, z, K_SS, 8, U_IN),
+    FW(ctsmg_hydrology_io, zi, K_ZI, 8, U_IN),
+    FW(ctsmg_hydrology_io, dz, K_SS, 8, U_IN),
+    FW(ctsmg_hydrology_io, t_soisno, K_SS, 8, U_IN),
+    FW(ctsmg_hydrology_io, h2osoi_liq, K_SS, 8, U_IN),
+    FW(ctsmg_hydrology_io, h2osoi_ice, K_SS, 8, U_IN),
+    FW(ctsmg_hydrology_io, h2osoi_vol, K_G, 8, U_INOUT),
+    FW(ctsmg_hydrology_io, zwt, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, zwt_perched, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, frost_table, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, watsat, K_G, 8, U_IN),
+};
+const int HYD_PWT_TABLE_N = sizeof(HYD_PWT_TABLE) / sizeof(HYD_PWT_TABLE[0]);
+const FieldDesc HYD_TWT_TABLE[] = {
+    FW(ctsmg_hydrology_io, nbedrock, K_C, 4, U_IN),
+    FW(ctsmg_hydrology_io, z, K_SS, 8, U_IN),
+    FW(ctsmg_hydrology_io, zi, K_ZI, 8, U_IN),
+    FW(ctsmg_hydrology_io, dz, K_SS, 8, U_IN),
+    FW(ctsmg_hydrology_io, h2osoi_liq, K_SS, 8, U_IN),
+    FW(ctsmg_hydrology_io, h2osoi_ice, K_SS, 8, U_IN),
+    FW(ctsmg_hydrology_io, h2osoi_vol, K_G, 8, U_INOUT),
+    FW(ctsmg_hydrology_io, zwt, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, watsat, K_G, 8, U_IN),
+};
+const int HYD_TWT_TABLE_N = sizeof(HYD_TWT_TABLE) / sizeof(HYD_TWT_TABLE[0]);
+const FieldDesc HYD_PLF_TABLE[] = {
+    FW(ctsmg_hydrology_io, nbedrock, K_C, 4, U_IN),
+    FW(ctsmg_hydrology_io, zi, K_ZI, 8, U_IN),
+    FW(ctsmg_hydrology_io, dz, K_SS, 8, U_IN),
+    FW(ctsmg_hydrology_io, h2osoi_liq, K_SS, 8, U_INOUT),
+    FW(ctsmg_hydrology_io, zwt_perched, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, frost_table, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, watsat, K_G, 8, U_IN),
+    FW(ctsmg_hydrology_io, hksat, K_G, 8, U_IN),
+    FW(ctsmg_hydrology_io, bsw, K_G, 8, U_IN),
+    FW(ctsmg_hydrology_io, sucsat, K_G, 8, U_IN),
+    FW(ctsmg_hydrology_io, topo_slope, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, qflx_drain_perched, K_C, 8, U_OUT),
+};
+const int HYD_PLF_TABLE_N = sizeof(HYD_PLF_TABLE) / sizeof(HYD_PLF_TABLE[0]);
+const FieldDesc HYD_SLF_TABLE[] = {
+    FW(ctsmg_hydrology_io, nbedrock, K_C, 4, U_IN),
+    FW(ctsmg_hydrology_io, zi, K_ZI, 8, U_IN),
+    FW(ctsmg_hydrology_io, dz, K_SS, 8, U_IN),
+    FW(ctsmg_hydrology_io, h2osoi_liq, K_SS, 8, U_INOUT),
+    FW(ctsmg_hydrology_io, h2osoi_ice, K_SS, 8, U_INOUT),
+    FW(ctsmg_hydrology_io, h2osfc, K_C, 8, U_INOUT),
+    FW(ctsmg_hydrology_io, zwt, K_C, 8, U_INOUT),
+    FW(ctsmg_hydrology_io, frost_table, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, icefrac, K_G, 8, U_OUT),
+    FW(ctsmg_hydrology_io, watsat, K_G, 8, U_IN),
+    FW(ctsmg_hydrology_io, bsw, K_G, 8, U_IN),
+    FW(ctsmg_hydrology_io, sucsat, K_G, 8, U_IN),
+    FW(ctsmg_hydrology_io, eff_porosity, K_G, 8, U_IN),
+    FW(ctsmg_hydrology_io, topo_slope, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, qflx_snwcp_liq, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, qflx_latflow_out, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_latflow_in, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_rsub_sat, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_drain, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_qrgwl, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_ice_runoff_xs, K_C, 8, U_OUT),
+};
+const int HYD_SLF_TABLE_N = sizeof(HYD_SLF_TABLE) / sizeof(HYD_SLF_TABLE[0]);
 const FieldDesc BAREGRND_SOILRESIS[] = {FW(ctsmg_baregrnd_io, soilresis, K_C, 8, U_IN)};
 const FieldDesc BAREGRND_SOILBETA[] = {FW(ctsmg_baregrnd_io, soilbeta, K_C, 8, U_IN)};
 
@@ -1228,5 +1311,74 @@ extern "C" int32_t ctsmg_baregroundfluxes(const ctsmg_bounds* bounds, int32_t nu
     e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "bare ground fluxes");
     return 0;
+}
+
+extern "C" int32_t ctsmg_set_soilhydrology_params(const ctsmg_soilhydrology_params* p) {
+    if (!p) return set_error(CTSMG_E_ARG, "null params", 0, 0);
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_shp = *p;
+    return 0;
+}
+
+ctsmg_soilhydrology_params ctsmg::current_soilhydrology_params() {
+    std::lock_guard<std::mutex> lk(g_mu);
+    return g_shp;
+}
+
+// One hydrology routine over the column filter: stage the routine's
+// components, run its kernel, copy the outputs back.
+static int hydrology_call(const ctsmg_bounds* bounds, int32_t n, const int32_t* filt, const ctsmg_hydrology_io* io,
+                          double dtime, int which, const FieldDesc* T, int NT) {
+    ThreadCtx* c;
+    int rc = ctx_get(&c);
+    if (rc) return rc;
+    if (!io) return set_error(CTSMG_E_ARG, "null io", 0, 0);
+    if ((rc = check_filter(bounds, n, filt))) return rc;
+    const int ncol = bounds->endc - bounds->begc + 1;
+    if (io->ldc < ncol) return set_error(CTSMG_E_ARG, "ldc smaller than endc-begc+1", 0, 0);
+    if ((which == HYD_PERCHED_LAT || which == HYD_SUBSURFACE_LAT) && !(dtime > 0.0))
+        return set_error(CTSMG_E_ARG, "dtime must be positive", 0, 0);
+    for (int i = 0; i < NT; ++i)
+        if (T[i].offset == offsetof(ctsmg_hydrology_io, nbedrock)) {
+            for (int k = 0; k < n; ++k) {
+                const int nb = io->nbedrock[filt[k] - bounds->begc];
+                if (nb < 1 || nb > NLEVSOI) return set_error(CTSMG_E_ARG, "nbedrock outside 1..nlevsoi", filt[k], 0);
+            }
+        }
+    if (n == 0) return 0;
+    const int ldc = io->ldc;
+    if ((rc = arena_reserve(c, table_bytes(T, NT, ldc, 0) + (size_t)n * 4 + 4096))) return rc;
+    ctsmg_hydrology_io dio;
+    if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, 0))) return rc;
+    int32_t* dfilt = (int32_t*)arena_take(c, (size_t)n * 4);
+    cudaError_t e = cudaMemcpyAsync(dfilt, filt, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
+    e = launch_hydrology(dio, bounds->begc, n, dfilt, which, current_soilhydrology_params(), dtime, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "hydrology kernel launch");
+    if ((rc = stage_out(c, io, &dio, T, NT, ldc, 0))) return rc;
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "hydrology");
+    return 0;
+}
+
+extern "C" int32_t ctsmg_saturated_excess_runoff(const ctsmg_bounds* b, int32_t n, const int32_t* f,
+                                                 const ctsmg_hydrology_io* io) {
+    return hydrology_call(b, n, f, io, 0.0, HYD_SAT_EXCESS, HYD_SAT_TABLE, HYD_SAT_TABLE_N);
+}
+extern "C" int32_t ctsmg_perched_water_table(const ctsmg_bounds* b, int32_t n, const int32_t* f,
+                                             const ctsmg_hydrology_io* io) {
+    return hydrology_call(b, n, f, io, 0.0, HYD_PERCHED_WT, HYD_PWT_TABLE, HYD_PWT_TABLE_N);
+}
+extern "C" int32_t ctsmg_theta_based_water_table(const ctsmg_bounds* b, int32_t n, const int32_t* f,
+                                                 const ctsmg_hydrology_io* io) {
+    return hydrology_call(b, n, f, io, 0.0, HYD_THETA_WT, HYD_TWT_TABLE, HYD_TWT_TABLE_N);
+}
+extern "C" int32_t ctsmg_perched_lateral_flow(const ctsmg_bounds* b, int32_t n, const int32_t* f,
+                                              const ctsmg_hydrology_io* io, double dtime) {
+    return hydrology_call(b, n, f, io, dtime, HYD_PERCHED_LAT, HYD_PLF_TABLE, HYD_PLF_TABLE_N);
+}
+extern "C" int32_t ctsmg_subsurface_lateral_flow(const ctsmg_bounds* b, int32_t n, const int32_t* f,
+                                                 const ctsmg_hydrology_io* io, double dtime) {
+    return hydrology_call(b, n, f, io, dtime, HYD_SUBSURFACE_LAT, HYD_SLF_TABLE, HYD_SLF_TABLE_N);
 }
 

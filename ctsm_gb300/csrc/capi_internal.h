@@ -34,4 +34,5 @@ int current_snow_method();
 // the soilwater_movement_inparm namelist in force (ctsmg_init / ctsmg_set_soilwater_movement)
 ctsmg_soilwater_movement_nml current_soilwater_nml();
 ctsmg_soil_resistance_params current_soil_resistance();
+ctsmg_soilhydrology_params current_soilhydrology_params();
 } // namespace ctsmg

@@ -216,3 +216,24 @@ def add_baregrnd_fields(A, npatch, ngrid):
             A[n] = np.zeros(abi.field_shape(kind, ncol, npatch, ngrid), dtype=np.dtype(t))
     return A
 
+
+def add_hydrology_fields(A, rng=None):
+    """The water-table / drainage components a soil state lacks: topographic
+    slope U(0.1, 10) degrees, wtfact U(0.2, 0.6), rain plus snowmelt U(0, 1e-4)
+    mm/s, snow capping U(0, 1e-6) mm/s (builder's choices); zwt_perched and
+    frost_table start at the water table; zero-filled outputs."""
+    r = rng if rng is not None else np.random.Generator(np.random.Philox(7))
+    ncol = A["zwt"].shape[0]
+    A["topo_slope"] = r.uniform(0.1, 10.0, ncol)
+    A["wtfact"] = r.uniform(0.2, 0.6, ncol)
+    A["qflx_rain_plus_snomelt"] = r.uniform(0.0, 1e-4, ncol)
+    A["qflx_snwcp_liq"] = r.uniform(0.0, 1e-6, ncol)
+    A["zwt_perched"] = A["zwt"].copy()
+    A["frost_table"] = A["zwt"].copy()
+    if "h2osfc" not in A:
+        A["h2osfc"] = np.zeros(ncol)
+    for (n, kind, t, u) in abi.HYDROLOGY_FIELDS:
+        if n not in A:
+            A[n] = np.zeros(abi.field_shape(kind, ncol, 1, ncol), dtype=np.dtype(t))
+    return A
+

@@ -93,3 +93,38 @@ def calc_soilevap_resis(bounds, num_nolakec, filter_nolakec, state):
     io = abi.make_io(abi.SoilResisIO, abi.SOILRESIS_FIELDS, state, ncol)
     check(L.ctsmg_soilevap_resis(C.byref(bounds), int(num_nolakec), fp, C.byref(io)))
 
+
+HYDROLOGY_ROUTINES = ("SaturatedExcessRunoff", "PerchedWaterTable", "ThetaBasedWaterTable", "PerchedLateralFlow",
+                      "SubsurfaceLateralFlow")
+_HYD_ENTRY = {"SaturatedExcessRunoff": "ctsmg_saturated_excess_runoff",
+              "PerchedWaterTable": "ctsmg_perched_water_table",
+              "ThetaBasedWaterTable": "ctsmg_theta_based_water_table",
+              "PerchedLateralFlow": "ctsmg_perched_lateral_flow",
+              "SubsurfaceLateralFlow": "ctsmg_subsurface_lateral_flow"}
+
+
+def set_soilhydrology_params(aq_sp_yield_min=0.01, n_baseflow=1.0, baseflow_scalar=1.0e-2,
+                             perched_baseflow_scalar=1.0e-5, e_ice=6.0, fff=0.5):
+    """ctsmg_set_soilhydrology_params: readParams of SoilHydrologyMod
+    (SoilHydrologyMod.F90:174-199) and SaturatedExcessRunoffMod (fff)."""
+    L = load()
+    L.ctsmg_set_soilhydrology_params.argtypes = [C.POINTER(abi.SoilHydrologyParams)]
+    p = abi.SoilHydrologyParams(aq_sp_yield_min, n_baseflow, baseflow_scalar, perched_baseflow_scalar, e_ice, fff)
+    check(L.ctsmg_set_soilhydrology_params(C.byref(p)))
+
+
+def hydrology(routine, bounds, num_hydrologyc, filter_hydrologyc, state, dtime=None):
+    """One of the water-table / drainage routines (HYDROLOGY_ROUTINES, by the
+    reference's subroutine name) over the column filter."""
+    L = load()
+    name = _HYD_ENTRY[routine]
+    fn = getattr(L, name)
+    args = [C.POINTER(abi.Bounds), C.c_int32, C.POINTER(C.c_int32), C.POINTER(abi.HydrologyIO)]
+    lateral = routine in ("PerchedLateralFlow", "SubsurfaceLateralFlow")
+    fn.argtypes = args + ([C.c_double] if lateral else [])
+    f, fp = _filter(filter_hydrologyc)
+    ncol = bounds.endc - bounds.begc + 1
+    io = abi.make_io(abi.HydrologyIO, abi.HYDROLOGY_FIELDS, state, ncol)
+    extra = [float(dtime)] if lateral else []
+    check(fn(C.byref(bounds), int(num_hydrologyc), fp, C.byref(io), *extra))
+

@@ -403,6 +403,74 @@ typedef struct {
 int32_t ctsmg_root_moist_stress(const ctsmg_bounds* bounds, int32_t num_exposedvegp,
                                 const int32_t* filter_exposedvegp, const ctsmg_rootmoist_io* io);
 
+/* ------------------------------------------------------- hydrology neighbours of SoilWater */
+/* The water-table and drainage routines of the default (no aquifer layer)
+ * hydrology around SoilWater, for natural soil columns outside hillslopes
+ * (src/biogeophys/HydrologyNoDrainageMod.F90:302-372,
+ *  src/biogeophys/HydrologyDrainageMod.F90:132-146):
+ *   SaturatedExcessRunoff, TOPMODEL fsat (SaturatedExcessRunoffMod.F90:200-360)
+ *   PerchedWaterTable      (SoilHydrologyMod.F90:1525-1641)
+ *   ThetaBasedWaterTable   (SoilHydrologyMod.F90:1933-2025)
+ *   PerchedLateralFlow     (SoilHydrologyMod.F90:1645-1929)
+ *   SubsurfaceLateralFlow  (SoilHydrologyMod.F90:2029-2565)
+ * The parameter-file values are aq_sp_yield_min, n_baseflow, baseflow_scalar,
+ * perched_baseflow_scalar, e_ice (SoilHydrologyMod.F90:61-67, 174-199) and
+ * fff (SaturatedExcessRunoffMod.F90:56, 194).  The hillslope branches, the
+ * urban columns and the volumetric discharge diagnostics are not built.   */
+typedef struct {
+    double aq_sp_yield_min, n_baseflow, baseflow_scalar, perched_baseflow_scalar, e_ice, fff;
+} ctsmg_soilhydrology_params;
+
+typedef struct {
+    int32_t ldc;
+    const int32_t* nbedrock;          /* (c)                                        */
+    const double* z;                  /* [SS]                                       */
+    const double* zi;                 /* [ZI]                                       */
+    const double* dz;                 /* [SS]                                       */
+    const double* t_soisno;           /* [SS]                                       */
+    double* h2osoi_liq;               /* [SS] inout                                 */
+    double* h2osoi_ice;               /* [SS] inout                                 */
+    double* h2osoi_vol;               /* [G]  inout (the water tables refresh it)   */
+    double* h2osfc;                   /* (c)  inout (mm)                            */
+    double* zwt;                      /* (c)  inout: water table depth (m)          */
+    double* zwt_perched;              /* (c)  inout: perched water table depth (m)  */
+    double* frost_table;              /* (c)  inout: frost table depth (m)          */
+    double* icefrac;                  /* [G]  out                                   */
+    const double* watsat;             /* [G]                                        */
+    const double* hksat;              /* [G]  (mm/s)                                */
+    const double* bsw;                /* [G]                                        */
+    const double* sucsat;             /* [G]  (mm)                                  */
+    const double* eff_porosity;       /* [G]                                        */
+    const double* topo_slope;         /* (c)  (degrees)                             */
+    const double* wtfact;             /* (c)  maximum saturated fraction            */
+    const double* qflx_rain_plus_snomelt; /* (c) (mm/s)                             */
+    const double* qflx_snwcp_liq;     /* (c)  (mm/s)                                */
+    double* fsat;                     /* (c)  out: saturated fraction               */
+    double* fcov;                     /* (c)  out                                   */
+    double* qflx_sat_excess_surf;     /* (c)  out (mm/s)                            */
+    double* qflx_drain_perched;       /* (c)  out (mm/s)                            */
+    double* qflx_latflow_out;         /* (c)  out (mm/s)                            */
+    double* qflx_latflow_in;          /* (c)  out (mm/s)                            */
+    double* qflx_rsub_sat;            /* (c)  out (mm/s)                            */
+    double* qflx_drain;               /* (c)  out (mm/s)                            */
+    double* qflx_qrgwl;               /* (c)  out (mm/s)                            */
+    double* qflx_ice_runoff_xs;       /* (c)  out (mm/s)                            */
+} ctsmg_hydrology_io;
+
+/* readParams of SoilHydrologyMod and SaturatedExcessRunoffMod. */
+int32_t ctsmg_set_soilhydrology_params(const ctsmg_soilhydrology_params* p);
+/* One entry per reference routine, over filter_hydrologyc (1-based). */
+int32_t ctsmg_saturated_excess_runoff(const ctsmg_bounds* bounds, int32_t num_hydrologyc,
+                                      const int32_t* filter_hydrologyc, const ctsmg_hydrology_io* io);
+int32_t ctsmg_perched_water_table(const ctsmg_bounds* bounds, int32_t num_hydrologyc,
+                                  const int32_t* filter_hydrologyc, const ctsmg_hydrology_io* io);
+int32_t ctsmg_theta_based_water_table(const ctsmg_bounds* bounds, int32_t num_hydrologyc,
+                                      const int32_t* filter_hydrologyc, const ctsmg_hydrology_io* io);
+int32_t ctsmg_perched_lateral_flow(const ctsmg_bounds* bounds, int32_t num_hydrologyc,
+                                   const int32_t* filter_hydrologyc, const ctsmg_hydrology_io* io, double dtime);
+int32_t ctsmg_subsurface_lateral_flow(const ctsmg_bounds* bounds, int32_t num_hydrologyc,
+                                      const int32_t* filter_hydrologyc, const ctsmg_hydrology_io* io, double dtime);
+
 /* ------------------------------------------------------------ BareGroundFluxes */
 /* Components BareGroundFluxes reads and writes for the patches without
  * exposed vegetation (src/biogeophys/BareGroundFluxesMod.F90:73-545;

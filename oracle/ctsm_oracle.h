@@ -25,6 +25,8 @@ void oracle_set_canopy_params(const ctsmg_canopy_params* p, const ctsmg_pftcon* 
 void oracle_set_patch_medlyn(const double* slope, const double* intercept);
 int  oracle_quadratic(double a, double b, double c, double* r1, double* r2);
 void oracle_qsat(double T, double p, double* qs, double* es, double* qsdT);
+int  oracle_hydrology(const ctsmg_bounds* b, int n, const int32_t* filt, const ctsmg_hydrology_io* io, int which,
+                      const ctsmg_soilhydrology_params* P, double dtime);
 int  oracle_baregroundfluxes(const ctsmg_bounds* b, int nump, const int32_t* filtp, const ctsmg_baregrnd_io* io,
                              int soil_resis_method);
 int  oracle_soilevap_resis(const ctsmg_bounds* b, int num_nolakec, const int32_t* filter_nolakec,

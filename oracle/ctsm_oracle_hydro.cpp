@@ -1,0 +1,260 @@
+// ctsm_oracle_hydro.cpp -- CPU oracle (test infrastructure only) of the
+// water-table and drainage routines of the default hydrology, for natural
+// soil columns outside hillslopes, statement by statement:
+//   SaturatedExcessRunoff / ComputeFsatTopmodel  SaturatedExcessRunoffMod.F90:200-360
+//   PerchedWaterTable       SoilHydrologyMod.F90:1525-1641
+//   ThetaBasedWaterTable    SoilHydrologyMod.F90:1933-2025
+//   PerchedLateralFlow      SoilHydrologyMod.F90:1645-1929
+//   SubsurfaceLateralFlow   SoilHydrologyMod.F90:2029-2565
+// sat_lev = 0.9 is a default-real literal in the reference, reproduced as
+// (double)0.9f.  Parity unpinned: the reference ships no test of these.
+#include <cmath>
+#include <cstdint>
+#include <algorithm>
+#include "ctsm_gpu.h"
+#include "ctsm_oracle.h"
+#include "oracle_libm.h"
+
+namespace {
+const double TFRZ = 273.15, DENH2O = 1.000e3, DENICE = 0.917e3;
+const double WATMIN = 0.01, PONDMX = 0.0, RPI = 3.14159265358979323846;
+const int NLEVSNO = CTSMG_NLEVSNO, NLEVSOI = CTSMG_NLEVSOI, LS = -NLEVSNO + 1;
+using oracle_libm::o_pow;
+using oracle_libm::o_exp;
+
+struct K {
+    const ctsmg_hydrology_io* io;
+    int c, ld;
+    double& liq(int j) const { return io->h2osoi_liq[c + (size_t)(j - LS) * ld]; }
+    double& ice(int j) const { return io->h2osoi_ice[c + (size_t)(j - LS) * ld]; }
+    double dz(int j) const { return io->dz[c + (size_t)(j - LS) * ld]; }
+    double z(int j) const { return io->z[c + (size_t)(j - LS) * ld]; }
+    double t(int j) const { return io->t_soisno[c + (size_t)(j - LS) * ld]; }
+    double zi(int j) const { return io->zi[c + (size_t)(j + NLEVSNO) * ld]; }
+    double watsat(int j) const { return io->watsat[c + (size_t)(j - 1) * ld]; }
+    double hksat(int j) const { return io->hksat[c + (size_t)(j - 1) * ld]; }
+    double bsw(int j) const { return io->bsw[c + (size_t)(j - 1) * ld]; }
+    double sucsat(int j) const { return io->sucsat[c + (size_t)(j - 1) * ld]; }
+    double eff(int j) const { return io->eff_porosity[c + (size_t)(j - 1) * ld]; }
+    double& vol(int j) const { return io->h2osoi_vol[c + (size_t)(j - 1) * ld]; }
+    double& icefrac(int j) const { return io->icefrac[c + (size_t)(j - 1) * ld]; }
+};
+} // namespace
+
+extern "C" int oracle_hydrology(const ctsmg_bounds* b, int n, const int32_t* filt, const ctsmg_hydrology_io* io,
+                                int which, const ctsmg_soilhydrology_params* P, double dtime) {
+    const double sat_lev = (double)0.9f;
+    for (int fc = 0; fc < n; ++fc) {
+        const K k{io, filt[fc] - b->begc, io->ldc};
+        const int c = k.c;
+        if (which == 0) {                      // SaturatedExcessRunoff (TOPMODEL fsat)
+            double fsat;
+            if (io->frost_table[c] > io->zwt_perched[c] && io->frost_table[c] <= io->zwt[c])
+                fsat = io->wtfact[c] * o_exp(-0.5 * P->fff * io->zwt_perched[c]);
+            else
+                fsat = io->wtfact[c] * o_exp(-0.5 * P->fff * io->zwt[c]);
+            io->fsat[c] = fsat;
+            io->qflx_sat_excess_surf[c] = fsat * io->qflx_rain_plus_snomelt[c];
+            io->fcov[c] = fsat;
+        } else if (which == 1) {               // PerchedWaterTable
+            int k_frz = (k.t(1) > TFRZ) ? NLEVSOI : 1;
+            for (int kk = 2; kk <= NLEVSOI; ++kk)
+                if (k.t(kk - 1) > TFRZ && k.t(kk) <= TFRZ) { k_frz = kk; break; }
+            io->frost_table[c] = k.zi(k_frz - 1);
+            io->zwt_perched[c] = io->frost_table[c];
+            if (io->zwt[c] < io->frost_table[c] && k.t(k_frz) <= TFRZ) {
+            } else if (k_frz > 1) {
+                int k_perch = 1;
+                for (int kk = k_frz; kk >= 1; --kk) {
+                    k.vol(kk) = k.liq(kk) / (k.dz(kk) * DENH2O) + k.ice(kk) / (k.dz(kk) * DENICE);
+                    if (k.vol(kk) / k.watsat(kk) <= sat_lev) { k_perch = kk; break; }
+                }
+                if (k.t(k_frz) > TFRZ) k_perch = k_frz;
+                if (k_frz > k_perch) {
+                    const double s1 = (k.liq(k_perch) / (k.dz(k_perch) * DENH2O) + k.ice(k_perch) / (k.dz(k_perch) * DENICE)) /
+                                      k.watsat(k_perch);
+                    const double s2 = (k.liq(k_perch + 1) / (k.dz(k_perch + 1) * DENH2O) +
+                                       k.ice(k_perch + 1) / (k.dz(k_perch + 1) * DENICE)) / k.watsat(k_perch + 1);
+                    if (s1 > s2) {
+                        io->zwt_perched[c] = k.zi(k_perch - 1);
+                    } else {
+                        const double m = (k.z(k_perch + 1) - k.z(k_perch)) / (s2 - s1);
+                        const double bb = k.z(k_perch + 1) - m * s2;
+                        io->zwt_perched[c] = std::max(0.0, m * sat_lev + bb);
+                    }
+                }
+            }
+        } else if (which == 2) {               // ThetaBasedWaterTable
+            const int nb = io->nbedrock[c];
+            io->zwt[c] = k.zi(NLEVSOI);
+            int k_zwt = nb, sat_flag = 1;
+            for (int kk = nb; kk >= 1; --kk) {
+                k.vol(kk) = k.liq(kk) / (k.dz(kk) * DENH2O) + k.ice(kk) / (k.dz(kk) * DENICE);
+                if (k.vol(kk) / k.watsat(kk) <= sat_lev) { k_zwt = kk; sat_flag = 0; break; }
+            }
+            if (sat_flag == 1) k_zwt = 1;
+            if (k_zwt == 1) {
+                io->zwt[c] = k.zi(1);
+            } else if (k_zwt < nb) {
+                const double s1 = (k.liq(k_zwt) / (k.dz(k_zwt) * DENH2O) + k.ice(k_zwt) / (k.dz(k_zwt) * DENICE)) /
+                                  k.watsat(k_zwt);
+                const double s2 = (k.liq(k_zwt + 1) / (k.dz(k_zwt + 1) * DENH2O) +
+                                   k.ice(k_zwt + 1) / (k.dz(k_zwt + 1) * DENICE)) / k.watsat(k_zwt + 1);
+                const double m = (k.z(k_zwt + 1) - k.z(k_zwt)) / (s2 - s1);
+                const double bb = k.z(k_zwt + 1) - m * s2;
+                io->zwt[c] = std::max(0.0, m * sat_lev + bb);
+            } else {
+                io->zwt[c] = k.zi(nb);
+            }
+        } else if (which == 3) {               // PerchedLateralFlow
+            const int nb = io->nbedrock[c];
+            int k_frost = nb, k_perch = nb;
+            for (int kk = 1; kk <= nb; ++kk)
+                if (io->frost_table[c] >= k.zi(kk - 1) && io->frost_table[c] < k.zi(kk)) { k_frost = kk; break; }
+            for (int kk = 1; kk <= nb; ++kk)
+                if (io->zwt_perched[c] >= k.zi(kk - 1) && io->zwt_perched[c] < k.zi(kk)) { k_perch = kk; break; }
+            io->qflx_drain_perched[c] = 0.0;
+            double out = 0.0;
+            if (io->frost_table[c] > io->zwt_perched[c]) {
+                const double q_perch_max = P->perched_baseflow_scalar * std::sin(io->topo_slope[c] * (RPI / 180.0));
+                double wtsub = 0.0, q_perch = 0.0;
+                for (int kk = k_perch; kk <= k_frost - 1; ++kk) {
+                    q_perch = q_perch + k.hksat(kk) * k.dz(kk);
+                    wtsub = wtsub + k.dz(kk);
+                }
+                if (wtsub > 0.0) q_perch = q_perch / wtsub;
+                out = q_perch_max * q_perch * (io->frost_table[c] - io->zwt_perched[c]);
+            }
+            io->qflx_drain_perched[c] = io->qflx_drain_perched[c] + out;
+            double drainage_tot = io->qflx_drain_perched[c] * dtime;
+            for (int kk = k_perch; kk <= k_frost - 1; ++kk) {
+                double s_y = k.watsat(kk) * (1. - o_pow(1. + 1.e3 * io->zwt_perched[c] / k.sucsat(kk), -1. / k.bsw(kk)));
+                s_y = std::max(s_y, P->aq_sp_yield_min);
+                double dl;
+                if (kk == k_perch) dl = std::min(drainage_tot, (s_y * (k.zi(kk) - io->zwt_perched[c]) * 1.e3));
+                else dl = std::min(drainage_tot, (s_y * (k.dz(kk)) * 1.e3));
+                dl = std::max(dl, 0.0);
+                drainage_tot = drainage_tot - dl;
+                k.liq(kk) = k.liq(kk) - dl;
+            }
+            io->qflx_drain_perched[c] = io->qflx_drain_perched[c] - drainage_tot / dtime;
+        } else {                               // SubsurfaceLateralFlow
+            const int nb = io->nbedrock[c];
+            double dzmm[NLEVSOI + 1];
+            for (int j = 1; j <= NLEVSOI; ++j) {
+                dzmm[j] = k.dz(j) * 1.e3;
+                const double vol_ice = std::min(k.watsat(j), k.ice(j) / (k.dz(j) * DENICE));
+                k.icefrac(j) = std::min(1.0, vol_ice / k.watsat(j));
+            }
+            io->qflx_drain[c] = 0.0;
+            io->qflx_rsub_sat[c] = 0.0;
+            double drainage = 0.0;
+            io->qflx_latflow_in[c] = 0.0;
+            io->qflx_latflow_out[c] = 0.0;
+            int jwt = NLEVSOI;
+            for (int j = 1; j <= NLEVSOI; ++j)
+                if (io->zwt[c] <= k.zi(j)) { jwt = j - 1; break; }
+            double dzsum = 0.0, icefracsum = 0.0;
+            for (int j = std::max(jwt, 1); j <= NLEVSOI; ++j) {
+                dzsum = dzsum + dzmm[j];
+                icefracsum = icefracsum + k.icefrac(j) * dzmm[j];
+            }
+            const double ice_imped_col = o_pow(10.0, -P->e_ice * (icefracsum / dzsum));
+            if (io->zwt[c] <= k.zi(nb))
+                io->qflx_latflow_out[c] = ice_imped_col * P->baseflow_scalar * std::tan(RPI / 180.0 * io->topo_slope[c]) *
+                                          o_pow(k.zi(nb) - io->zwt[c], P->n_baseflow);
+            const double net = io->qflx_latflow_out[c] - io->qflx_latflow_in[c];
+            if (io->zwt[c] <= k.zi(nb)) drainage = net;
+            else drainage = 0.0;
+            double drainage_tot = -drainage * dtime;
+            if (drainage_tot > 0.) {
+                for (int j = jwt + 1; j >= 1; --j) {
+                    if (k.zi(j) < io->frost_table[c]) {
+                        double s_y = k.watsat(j) * (1. - o_pow(1. + 1.e3 * io->zwt[c] / k.sucsat(j), -1. / k.bsw(j)));
+                        s_y = std::max(s_y, P->aq_sp_yield_min);
+                        double dl = std::min(drainage_tot, (s_y * k.dz(j) * 1.e3));
+                        dl = std::max(dl, 0.0);
+                        k.liq(j) = k.liq(j) + dl;
+                        drainage_tot = drainage_tot - dl;
+                        if (drainage_tot <= 0.) {
+                            io->zwt[c] = io->zwt[c] - dl / s_y / 1000.0;
+                            break;
+                        } else {
+                            io->zwt[c] = k.zi(j - 1);
+                        }
+                    }
+                }
+                io->h2osfc[c] = io->h2osfc[c] + drainage_tot;
+            } else {
+                for (int j = jwt + 1; j <= nb; ++j) {
+                    double s_y = k.watsat(j) * (1. - o_pow(1. + 1.e3 * io->zwt[c] / k.sucsat(j), -1. / k.bsw(j)));
+                    s_y = std::max(s_y, P->aq_sp_yield_min);
+                    double dl = std::max(drainage_tot, -(s_y * (k.zi(j) - io->zwt[c]) * 1.e3));
+                    dl = std::min(dl, 0.0);
+                    k.liq(j) = k.liq(j) + dl;
+                    drainage_tot = drainage_tot - dl;
+                    if (drainage_tot >= 0.) {
+                        io->zwt[c] = io->zwt[c] - dl / s_y / 1000.0;
+                        break;
+                    } else {
+                        io->zwt[c] = k.zi(j);
+                    }
+                }
+                drainage = drainage + drainage_tot / dtime;
+            }
+            io->zwt[c] = std::max(0.0, io->zwt[c]);
+            io->zwt[c] = std::min(80.0, io->zwt[c]);
+            for (int j = NLEVSOI; j >= 2; --j) {
+                const double xsi = std::max(k.liq(j) - k.eff(j) * dzmm[j], 0.0);
+                k.liq(j) = std::min(k.eff(j) * dzmm[j], k.liq(j));
+                k.liq(j - 1) = k.liq(j - 1) + xsi;
+            }
+            double xs1 = std::max(std::max(k.liq(1) - WATMIN, 0.0) -
+                                  std::max(0.0, (PONDMX + k.watsat(1) * dzmm[1] - k.ice(1) - WATMIN)), 0.0);
+            k.liq(1) = k.liq(1) - xs1;
+            io->h2osfc[c] = io->h2osfc[c] + xs1;
+            io->qflx_rsub_sat[c] = 0.0;
+            xs1 = std::max(std::max(k.ice(1), 0.0) - std::max(0.0, (PONDMX + k.watsat(1) * dzmm[1] - k.liq(1))), 0.0);
+            k.ice(1) = std::min(std::max(0.0, PONDMX + k.watsat(1) * dzmm[1] - k.liq(1)), k.ice(1));
+            io->qflx_ice_runoff_xs[c] = xs1 / dtime;
+            for (int j = 1; j <= NLEVSOI - 1; ++j) {
+                double xs;
+                if (k.liq(j) < WATMIN) {
+                    xs = WATMIN - k.liq(j);
+                    if (j == jwt) io->zwt[c] = io->zwt[c] + xs / k.eff(j) / 1000.0;
+                } else {
+                    xs = 0.0;
+                }
+                k.liq(j) = k.liq(j) + xs;
+                k.liq(j + 1) = k.liq(j + 1) - xs;
+            }
+            {
+                const int j = NLEVSOI;
+                double xs;
+                if (k.liq(j) < WATMIN) {
+                    xs = WATMIN - k.liq(j);
+                    for (int i = NLEVSOI - 1; i >= 1; --i) {
+                        const double avail = std::max(k.liq(i) - WATMIN - xs, 0.0);
+                        if (avail >= xs) {
+                            k.liq(j) = k.liq(j) + xs;
+                            k.liq(i) = k.liq(i) - xs;
+                            xs = 0.0;
+                            break;
+                        } else {
+                            k.liq(j) = k.liq(j) + avail;
+                            k.liq(i) = k.liq(i) - avail;
+                            xs = xs - avail;
+                        }
+                    }
+                } else {
+                    xs = 0.0;
+                }
+                k.liq(j) = k.liq(j) + xs;
+                io->qflx_rsub_sat[c] = io->qflx_rsub_sat[c] - xs / dtime;
+            }
+            io->qflx_drain[c] = io->qflx_rsub_sat[c] + drainage;
+            io->qflx_qrgwl[c] = io->qflx_snwcp_liq[c];
+        }
+    }
+    return 0;
+}

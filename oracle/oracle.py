@@ -40,6 +40,8 @@ def lib():
         _LIB.oracle_rootsink.argtypes = [I, I, P(C.c_int32), P(C.c_int32)] + [P(C.c_double)] * 4
         _LIB.oracle_rootsink.restype = None
         _LIB.oracle_canopyfluxes.argtypes = [P(abi.Bounds), I, P(C.c_int32), P(abi.CanopyIO), C.c_double, P(C.c_int)]
+        _LIB.oracle_hydrology.argtypes = [P(abi.Bounds), I, P(C.c_int32), P(abi.HydrologyIO), I,
+                                          P(abi.SoilHydrologyParams), C.c_double]
         _LIB.oracle_baregroundfluxes.argtypes = [P(abi.Bounds), I, P(C.c_int32), P(abi.BareGrndIO), I]
         _LIB.oracle_soilevap_resis.argtypes = [P(abi.Bounds), I, P(C.c_int32), P(abi.SoilResisIO),
                                                P(abi.SoilResistanceParams)]

@@ -59,6 +59,9 @@ def test_struct_layout_matches_ctypes(tmp_path):
                                                [f[0] for f in abi.SoilWaterMovementNml._fields_]),
               "ctsmg_baregrnd_io": (abi.BareGrndIO, ["ldp", "ldc", "ldg", "begg"] +
                                     [f[0] for f in abi.BAREGRND_FIELDS]),
+              "ctsmg_hydrology_io": (abi.HydrologyIO, ["ldc"] + [f[0] for f in abi.HYDROLOGY_FIELDS]),
+              "ctsmg_soilhydrology_params": (abi.SoilHydrologyParams,
+                                             [f[0] for f in abi.SoilHydrologyParams._fields_]),
               "ctsmg_soilresis_io": (abi.SoilResisIO, ["ldc"] + [f[0] for f in abi.SOILRESIS_FIELDS]),
               "ctsmg_soil_resistance_params": (abi.SoilResistanceParams,
                                                [f[0] for f in abi.SoilResistanceParams._fields_]),

@@ -1,0 +1,94 @@
+"""The water-table and drainage routines around SoilWater (SaturatedExcessRunoff,
+PerchedWaterTable, ThetaBasedWaterTable, PerchedLateralFlow,
+SubsurfaceLateralFlow) through their drop-in entries, against the oracle:
+each alone and in the driver's sequence, on states where their branches act
+(frozen layers under a perched table, saturated columns, water tables below
+the bedrock, nearly dry layers, an over-full top layer)."""
+import copy
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from ctsm_gb300 import abi, inputs, full_inputs as fi
+from tests.parity import compare
+
+pytestmark = pytest.mark.gpu
+LS = -abi.NLEVSNO + 1
+DT = 1800.0
+PAR = dict(aq_sp_yield_min=0.01, n_baseflow=1.0, baseflow_scalar=1.0e-2, perched_baseflow_scalar=1.0e-5, e_ice=6.0,
+           fff=0.5)
+WHICH = {"SaturatedExcessRunoff": 0, "PerchedWaterTable": 1, "ThetaBasedWaterTable": 2, "PerchedLateralFlow": 3,
+         "SubsurfaceLateralFlow": 4}
+OUT = [n for (n, k, t, u) in abi.HYDROLOGY_FIELDS if u != "in"]
+
+
+def state(ncol, seed):
+    A, _ = inputs.soil_columns(ncol, seed=seed, snow=True, nbedrock=(3, 20), zwt=(0.1, 9.5))
+    r = np.random.Generator(np.random.Philox(seed + 1))
+    fi.add_hydrology_fields(A, r)
+    soil = slice(1 - LS, abi.NLEVSOI + 1 - LS)
+    sat = r.choice(ncol, ncol // 8, replace=False)          # saturated columns
+    A["h2osoi_liq"][soil, sat] = 0.97 * A["watsat"][:abi.NLEVSOI, sat] * A["dz"][soil, sat] * 1000.0
+    A["h2osoi_ice"][soil, sat] = 0.0
+    dry = r.choice(ncol, ncol // 8, replace=False)          # nearly dry layers
+    j = r.integers(1, abi.NLEVSOI + 1, size=len(dry))
+    A["h2osoi_liq"][j - LS, dry] = 0.001
+    full = r.choice(ncol, ncol // 8, replace=False)         # over-full top layer
+    A["h2osoi_liq"][1 - LS, full] = 2.0 * A["watsat"][0, full] * A["dz"][1 - LS, full] * 1000.0
+    from ctsm_gb300.inputs import set_soil_water_fractions
+    set_soil_water_fractions(A)
+    return A
+
+
+def oracle(A, routines, begc=1, filt=None):
+    from oracle import oracle as orc
+    ncol = A["zwt"].shape[0]
+    f = np.arange(begc, begc + ncol, dtype=np.int32) if filt is None else np.ascontiguousarray(filt, np.int32)
+    io = abi.make_io(abi.HydrologyIO, abi.HYDROLOGY_FIELDS, A, ncol)
+    P = abi.SoilHydrologyParams(*PAR.values())
+    for rt in routines:
+        assert orc.lib().oracle_hydrology(C.byref(abi.Bounds(begc, begc + ncol - 1, 1, 1)), len(f),
+                                          f.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(io), WHICH[rt],
+                                          C.byref(P), DT) == 0
+
+
+def gpu(soil, A, routines, begc=1, filt=None):
+    ncol = A["zwt"].shape[0]
+    f = np.arange(begc, begc + ncol, dtype=np.int32) if filt is None else filt
+    for rt in routines:
+        soil.hydrology(rt, abi.Bounds(begc, begc + ncol - 1, 1, 1), len(f), f, A, DT)
+
+
+@pytest.mark.parametrize("routine", list(WHICH))
+def test_each_routine_matches_oracle(gpu_lib, routine):
+    gpu_lib.set_soilhydrology_params(**PAR)
+    A = state(5000, seed=81)
+    oracle(A, ["PerchedWaterTable"])                  # a consistent frost table / perched table to start from
+    G, R = copy.deepcopy(A), copy.deepcopy(A)
+    oracle(R, [routine])
+    gpu(gpu_lib, G, [routine])
+    errs, bad = compare(G, R, OUT, 1e-12, {})
+    assert not bad, {k: errs[k] for k in bad}
+
+
+def test_driver_sequence_with_filter(gpu_lib):
+    """HydrologyNoDrainage's water tables then HydrologyDrainage's lateral
+    flows (HydrologyNoDrainageMod.F90:302-372, HydrologyDrainageMod.F90:132-146)
+    over a filter with gaps and an offset column range; the branches acted."""
+    gpu_lib.set_soilhydrology_params(**PAR)
+    A = state(6000, seed=82)
+    seq = ["SaturatedExcessRunoff", "PerchedWaterTable", "ThetaBasedWaterTable", "PerchedLateralFlow",
+           "SubsurfaceLateralFlow"]
+    r = np.random.Generator(np.random.Philox(83))
+    filt = np.sort(r.choice(np.arange(11, 6011, dtype=np.int32), 5000, replace=False))
+    G, R = copy.deepcopy(A), copy.deepcopy(A)
+    oracle(R, seq, begc=11, filt=filt)
+    gpu(gpu_lib, G, seq, begc=11, filt=filt)
+    errs, bad = compare(G, R, OUT, 1e-12, {})
+    assert not bad, {k: errs[k] for k in bad}
+    c = filt - 11
+    assert (R["qflx_drain_perched"][c] > 0).any() and (R["qflx_latflow_out"][c] > 0).any()
+    assert (R["qflx_latflow_out"][c] == 0).any()          # water table below the bedrock
+    assert (R["qflx_ice_runoff_xs"][c] >= 0).all() and (R["qflx_rsub_sat"][c] <= 0).all()
+    assert (R["h2osfc"][c] > A["h2osfc"][c]).any()        # top-layer excess went to the surface
