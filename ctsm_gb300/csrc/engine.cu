@@ -41,6 +41,8 @@ struct Batch {
     ctsmg_soilwater_movement_nml swm{};   // the namelist when the batch was created
     ctsmg_soilresis_io dsr{};
     SoilResisArgs sra{};
+    HydroStepArgs hya{};
+    double* hyd_params = nullptr;         // per-column baseflow_scalar / fff (positions order)
     MoistureFormArgs mfa{};
     CanopyArgs cargs{};
     double* rootr = nullptr;
@@ -99,8 +101,9 @@ static cudaError_t enqueue_step(Batch* b) {
     // order 0 (SoilWater first), after it (and SoilFluxes) otherwise
     const int ord = b->cfg.soilfluxes ? 2 : b->cfg.order;
     const bool mf = b->swm.soilwater_movement_method == 1;
+    const HydroStepArgs* hy = b->cfg.hydrology ? &b->hya : nullptr;
     if (mf && ord == 0) {
-        e = launch_mf_step(b->dsw, ncol, b->mfa, b->swm.use_flexibleCN, 0, b->err, nullptr, b->stream);
+        e = launch_mf_step(b->dsw, ncol, b->mfa, b->swm.use_flexibleCN, 0, b->err, nullptr, b->stream, hy);
         if (e != cudaSuccess) return e;
     }
     SoilStepFlags fl;
@@ -110,7 +113,7 @@ static cudaError_t enqueue_step(Batch* b) {
     e = launch_soilstep(b->dsw, b->dst, ncol, b->cfg.e_ice, b->cfg.dtime, b->cfg.snow_thermal_cond_method, b->ws,
                         ncol, b->err, b->stream, b->block, ord, nullptr, b->cfg.soilfluxes ? &b->dsf : nullptr, fl);
     if (e == cudaSuccess && mf && ord >= 1)
-        e = launch_mf_step(b->dsw, ncol, b->mfa, b->swm.use_flexibleCN, 1, b->err, nullptr, b->stream);
+        e = launch_mf_step(b->dsw, ncol, b->mfa, b->swm.use_flexibleCN, 1, b->err, nullptr, b->stream, hy);
     if (e != cudaSuccess || !b->cfg.balance) return e;
     return launch_balance(b->dsw, b->dst, ncol, b->cfg.dtime, b->bal, b->stream);
 }
@@ -135,7 +138,7 @@ static void batch_free(Batch* b) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
     for (auto& f : b->fields) if (f.dptr) cudaFree(f.dptr);
     for (void* p : {(void*)b->d_perm, (void*)b->ws, (void*)b->err, b->snapshot, (void*)b->rootr, (void*)b->mslope,
-                    (void*)b->mint, (void*)b->counter, (void*)b->cws, b->bal_mem})
+                    (void*)b->mint, (void*)b->counter, (void*)b->cws, b->bal_mem, (void*)b->hyd_params})
         if (p) cudaFree(p);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
@@ -164,6 +167,7 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
     const ctsmg_canopy_params* cpar = in->cpar;
     const ctsmg_pftcon* pft = in->pft;
     const ctsmg_soilresis_io* sr = in->sr;
+    const ctsmg_hydrology_io* hy = in->hy;
     const bool canopy_only = cfg && cfg->order == 2;
     if (!out || !cfg || (!canopy_only && (!sw || !st))) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
     const int ncol = cfg->ncol, npatch = cfg->npatch;
@@ -216,6 +220,11 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
         }
     }
     if (!canopy_only && swm.use_flexibleCN && !sw->wa) return set_error(CTSMG_E_ARG, "use_flexibleCN needs wa", 0, 0);
+    if (cfg->hydrology && (canopy_only || swm.soilwater_movement_method != 1 || !hy || hy->ldc != ncol))
+        return set_error(CTSMG_E_ARG, "hydrology needs the moisture form, the soil step and dense hydrology arrays", 0, 0);
+    if (cfg->hydrology && cfg->balance)
+        return set_error(CTSMG_E_UNSUPPORTED, "the balance check does not count the lateral and surface fluxes of the "
+                         "hydrology routines", 0, 0);
     if (cfg->balance && swm.use_flexibleCN)
         return set_error(CTSMG_E_UNSUPPORTED, "the balance check does not count the aquifer water the flexibleCN fix "
                          "moves", 0, 0);
@@ -299,6 +308,31 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
         }
         if (swm.use_flexibleCN && (rc = add(SOILWATER_FLEXCN_TABLE, SOILWATER_FLEXCN_NFIELDS, sw, &b->dsw)))
             return fail(rc);
+        if (cfg->hydrology) {
+            std::memcpy(&b->hya.io, hy, sizeof b->hya.io);
+            const FieldDesc* tabs[5] = {HYD_SAT_TABLE, HYD_PWT_TABLE, HYD_TWT_TABLE, HYD_PLF_TABLE, HYD_SLF_TABLE};
+            const int ns[5] = {HYD_SAT_TABLE_N, HYD_PWT_TABLE_N, HYD_TWT_TABLE_N, HYD_PLF_TABLE_N, HYD_SLF_TABLE_N};
+            for (int k = 0; k < 5; ++k)
+                if ((rc = add(tabs[k], ns[k], hy, &b->hya.io))) return fail(rc);
+            b->hya.par = current_soilhydrology_params();
+            const double* hc[2] = {in->baseflow_scalar_c, in->fff_c};
+            if (hc[0] || hc[1]) {
+                const size_t cb = (size_t)ncol * 8;
+                if ((e = cudaMalloc(&b->hyd_params, 3 * cb)) != cudaSuccess) return fail(cuda_err(e, "hydrology params"));
+                double* tmp = b->hyd_params + 2 * (size_t)ncol;
+                for (int k = 0; k < 2; ++k) {
+                    if (!hc[k]) continue;
+                    double* dst = b->hyd_params + k * (size_t)ncol;
+                    if ((e = cudaMemcpy(tmp, hc[k], cb, cudaMemcpyHostToDevice)) != cudaSuccess)
+                        return fail(cuda_err(e, "hydrology params"));
+                    if ((e = launch_permute(dst, tmp, b->d_perm, ncol, 1, 8, 0, b->stream)) != cudaSuccess ||
+                        (e = cudaStreamSynchronize(b->stream)) != cudaSuccess)
+                        return fail(cuda_err(e, "hydrology params"));
+                    if (k == 0) b->hya.baseflow_scalar_c = dst;
+                    else b->hya.fff_c = dst;
+                }
+            }
+        }
     }
     if (cfg->with_canopy) {
         std::memcpy(&b->cargs.io, cio, sizeof b->cargs.io);
@@ -377,7 +411,9 @@ extern "C" int32_t ctsmg_batch_create3(ctsmg_batch* out, const ctsmg_batch_confi
                                        const ctsmg_canopy_params* cpar, const ctsmg_pftcon* pft) {
     if (cfg && cfg->rootmoist) return set_error(CTSMG_E_ARG, "rootmoist needs ctsmg_batch_open", 0, 0);
     if (cfg && cfg->soilresis) return set_error(CTSMG_E_ARG, "soilresis needs ctsmg_batch_open", 0, 0);
-    const ctsmg_batch_inputs in = {sw, st, cio, sf, nullptr, rootr, medlynslope_p, medlynintercept_p, cpar, pft, nullptr};
+    if (cfg && cfg->hydrology) return set_error(CTSMG_E_ARG, "hydrology needs ctsmg_batch_open", 0, 0);
+    const ctsmg_batch_inputs in = {sw, st, cio, sf, nullptr, rootr, medlynslope_p, medlynintercept_p, cpar, pft,
+                                   nullptr, nullptr, nullptr, nullptr};
     return ctsmg_batch_open(out, cfg, &in);
 }
 
@@ -399,6 +435,7 @@ extern "C" int32_t ctsmg_batch_create(ctsmg_batch* out, const ctsmg_soilwater_io
     cfg.stomatalcond_method = 1; cfg.itmax_canopy_fluxes = 40;
     cfg.order = 0; cfg.with_canopy = 0; cfg.bucket = 1;
     cfg.balance = 0; cfg.skip_steps = 0; cfg.soilfluxes = 0; cfg.soilresis = 0; cfg.rootmoist = 0;
+    cfg.hydrology = 0;
     return ctsmg_batch_create2(out, &cfg, sw, st, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
 }
 
@@ -470,6 +507,12 @@ extern "C" int32_t ctsmg_batch_fetch(ctsmg_batch bh, const ctsmg_batch_inputs* i
     if (in->sr && bh->b->cfg.soilresis &&
         (rc = download_table(bh->b, SOILRESIS_SL14_TABLE, SOILRESIS_SL14_NFIELDS, in->sr)))
         return rc;
+    if (in->hy && bh->b->cfg.hydrology) {
+        const FieldDesc* tabs[5] = {HYD_SAT_TABLE, HYD_PWT_TABLE, HYD_TWT_TABLE, HYD_PLF_TABLE, HYD_SLF_TABLE};
+        const int ns[5] = {HYD_SAT_TABLE_N, HYD_PWT_TABLE_N, HYD_TWT_TABLE_N, HYD_PLF_TABLE_N, HYD_SLF_TABLE_N};
+        for (int k = 0; k < 5; ++k)
+            if ((rc = download_table(bh->b, tabs[k], ns[k], in->hy))) return rc;
+    }
     return 0;
 }
 

@@ -19,6 +19,7 @@
 #include "soil_math.cuh"
 #include "moisture_form_kernels.cuh"
 #include "moisture_form_device.cuh"
+#include "hydrology_device.cuh"
 
 namespace ctsmg {
 
@@ -285,24 +286,41 @@ flexcn_kernel(ctsmg_soilwater_io io, int begc, int nfilt, const int32_t* __restr
 // form: SetSoilWaterFractions, SoilWater (moisture form), the flexibleCN fix
 // and, if refresh, the between-step h2osoi_vol refresh
 // (HydrologyNoDrainageMod.F90:302, 346, 580, 590).
+template <bool HYDRO>
 __global__ void __launch_bounds__(128)
 mf_step_kernel(ctsmg_soilwater_io io, int ncol, MoistureFormArgs P, int flexcn, int refresh, DevError* err,
-               const int32_t* __restrict__ filt) {
+               const int32_t* __restrict__ filt, HydroStepArgs hy) {
     const int fc = blockIdx.x * blockDim.x + threadIdx.x;
     if (fc >= ncol) return;
     const int c = filt ? filt[fc] - 1 : fc;
+    ctsmg_soilhydrology_params hp = hy.par;
+    if (HYDRO) {
+        if (hy.baseflow_scalar_c) hp.baseflow_scalar = hy.baseflow_scalar_c[c];
+        if (hy.fff_c) hp.fff = hy.fff_c[c];
+    }
     set_soil_water_fractions(io, c);
+    if (HYDRO) hydro::saturated_excess_runoff(hy.io, c, hp.fff);
     const int info = mf_column(io, c, P);
     if (info > 0) report_error(err, c + 1, info, CTSMG_E_SINGULAR);
     else if (info < 0) report_error(err, c + 1, 0, CTSMG_E_TIMEOUT);
     if (flexcn) flexcn_column(io, c);
+    if (HYDRO) {
+        hydro::perched_water_table(hy.io, c);
+        hydro::theta_based_water_table(hy.io, c);
+        hydro::perched_lateral_flow(hy.io, c, hp, P.dtime);
+        hydro::subsurface_lateral_flow(hy.io, c, hp, P.dtime);
+    }
     if (refresh) refresh_h2osoi_vol(io, c);
 }
 
 cudaError_t launch_mf_step(const ctsmg_soilwater_io& io, int ncol, const MoistureFormArgs& P, int flexcn, int refresh,
-                           DevError* err, const int32_t* d_filt, cudaStream_t s) {
+                           DevError* err, const int32_t* d_filt, cudaStream_t s, const HydroStepArgs* hy) {
     if (ncol <= 0) return cudaSuccess;
-    mf_step_kernel<<<(ncol + 127) / 128, 128, 0, s>>>(io, ncol, P, flexcn, refresh, err, d_filt);
+    if (hy)
+        mf_step_kernel<true><<<(ncol + 127) / 128, 128, 0, s>>>(io, ncol, P, flexcn, refresh, err, d_filt, *hy);
+    else
+        mf_step_kernel<false><<<(ncol + 127) / 128, 128, 0, s>>>(io, ncol, P, flexcn, refresh, err, d_filt,
+                                                                HydroStepArgs{});
     return cudaGetLastError();
 }
 

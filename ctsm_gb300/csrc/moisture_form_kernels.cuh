@@ -29,9 +29,19 @@ __device__ int mf_column(const ctsmg_soilwater_io& io, int c, const MoistureForm
 // d_filt: device copy of the 1-based column filter, or NULL for begc .. begc+nfilt-1.
 cudaError_t launch_moisture_form(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt,
                                  const MoistureFormArgs& P, DevError* err, cudaStream_t s);
-// Resident-step form over positions 0..ncol-1 (or the 1-based position filter).
+// The default hydrology around SoilWater in the resident step: per-column
+// baseflow_scalar / fff override the parameters where given.
+struct HydroStepArgs {
+    ctsmg_hydrology_io io;
+    ctsmg_soilhydrology_params par;
+    const double* baseflow_scalar_c;
+    const double* fff_c;
+};
+
+// Resident-step form over positions 0..ncol-1 (or the 1-based position
+// filter); hy = NULL leaves the hydrology out.
 cudaError_t launch_mf_step(const ctsmg_soilwater_io& io, int ncol, const MoistureFormArgs& P, int flexcn, int refresh,
-                           DevError* err, const int32_t* d_filt, cudaStream_t s);
+                           DevError* err, const int32_t* d_filt, cudaStream_t s, const HydroStepArgs* hy = nullptr);
 cudaError_t launch_flexcn(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt, cudaStream_t s);
 
 } // namespace ctsmg

@@ -45,7 +45,7 @@ class BatchConfig(C.Structure):
                 ("e_ice", C.c_double), ("snow_thermal_cond_method", C.c_int32), ("stomatalcond_method", C.c_int32),
                 ("itmax_canopy_fluxes", C.c_int32), ("order", C.c_int32), ("with_canopy", C.c_int32),
                 ("bucket", C.c_int32), ("balance", C.c_int32), ("skip_steps", C.c_int32), ("soilfluxes", C.c_int32),
-                ("soilresis", C.c_int32), ("rootmoist", C.c_int32)]
+                ("soilresis", C.c_int32), ("rootmoist", C.c_int32), ("hydrology", C.c_int32)]
 
 
 class BatchInputs(C.Structure):
@@ -54,7 +54,8 @@ class BatchInputs(C.Structure):
                 ("rm", C.POINTER(abi.RootMoistIO)), ("rootr", C.POINTER(C.c_double)),
                 ("medlynslope_p", C.POINTER(C.c_double)), ("medlynintercept_p", C.POINTER(C.c_double)),
                 ("cpar", C.POINTER(abi.CanopyParams)), ("pft", C.POINTER(abi.Pftcon)),
-                ("sr", C.POINTER(abi.SoilResisIO))]
+                ("sr", C.POINTER(abi.SoilResisIO)), ("hy", C.POINTER(abi.HydrologyIO)),
+                ("baseflow_scalar_c", C.POINTER(C.c_double)), ("fff_c", C.POINTER(C.c_double))]
 
 
 def _pt(x):
@@ -71,7 +72,7 @@ class SoilBatch:
     def __init__(self, state, npatch, dtime=1800.0, e_ice=6.0, snow_thermal_cond_method=0, canopy=False,
                  ngrid=None, rootr=None, order=None, bucket=True, stomatalcond_method=1, itmax=40,
                  params=None, pftcon=None, per_patch_medlyn=False, balance=False, skip_steps=None,
-                 soilfluxes=False, rootmoist=False, soilresis=False):
+                 soilfluxes=False, rootmoist=False, soilresis=False, hydrology=False, per_column_hydrology=False):
         from . import canopy_inputs
         self.L = load()
         _bind(self.L)
@@ -93,8 +94,9 @@ class SoilBatch:
                           itmax, (1 if canopy else 0) if order is None else order, 1 if canopy else 0,
                           1 if bucket else 0, 1 if balance else 0,
                           _skip(dtime) if skip_steps is None else skip_steps, 1 if soilfluxes else 0,
-                          1 if soilresis else 0, 1 if rootmoist else 0)
+                          1 if soilresis else 0, 1 if rootmoist else 0, 1 if hydrology else 0)
         self.soilresis = soilresis
+        self.hydrology = hydrology
         self.soilfluxes = soilfluxes
         self.rootmoist = rootmoist
         self.h = C.c_void_p()
@@ -111,13 +113,25 @@ class SoilBatch:
             self._rm = abi.make_io(abi.RootMoistIO, abi.ROOTMOIST_FIELDS, state, self.ncol, npatch) \
                 if rootmoist else None
             self._sr = abi.make_io(abi.SoilResisIO, abi.SOILRESIS_FIELDS, state, self.ncol) if soilresis else None
-            self._in = BatchInputs(_pt(self._sw), _pt(self._st), C.pointer(self._ci), _pt(self._sf), _pt(self._rm),
-                                   None if self._rootr is None else self._rootr.ctypes.data_as(dp), ms, mi,
-                                   C.pointer(self._par), C.pointer(self._pft), _pt(self._sr))
-            check(self.L.ctsmg_batch_open(C.byref(self.h), C.byref(cfg), C.byref(self._in)))
+            self._open(cfg, dp, ms, mi, C.pointer(self._ci), C.pointer(self._par), C.pointer(self._pft),
+                       per_column_hydrology)
+        elif hydrology:
+            self._sf = self._rm = self._sr = self._rootr = None
+            self._open(cfg, C.POINTER(C.c_double), None, None, None, None, None, per_column_hydrology)
         else:
             check(self.L.ctsmg_batch_create2(C.byref(self.h), C.byref(cfg), C.byref(self._sw), C.byref(self._st),
                                              None, None, None, None, None, None))
+
+    def _open(self, cfg, dp, ms, mi, ci, par, pft, per_column_hydrology):
+        st = self.state
+        self._hy = abi.make_io(abi.HydrologyIO, abi.HYDROLOGY_FIELDS, st, self.ncol) if self.hydrology else None
+        pc = self.hydrology and per_column_hydrology
+        self._in = BatchInputs(_pt(self._sw), _pt(self._st), ci, _pt(self._sf), _pt(self._rm),
+                               None if self._rootr is None else self._rootr.ctypes.data_as(dp), ms, mi, par, pft,
+                               _pt(self._sr), _pt(self._hy),
+                               st["baseflow_scalar_c"].ctypes.data_as(dp) if pc else None,
+                               st["fff_c"].ctypes.data_as(dp) if pc else None)
+        check(self.L.ctsmg_batch_open(C.byref(self.h), C.byref(cfg), C.byref(self._in)))
 
     def run(self, nsteps, timed=False):
         if timed:
@@ -138,16 +152,21 @@ class SoilBatch:
             sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS +
                              [x for x in abi.SOILWATER_EXTRA if x[0] in st], st, self.ncol)
             tt = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, st, self.ncol, self.npatch)
-        if self.canopy:
+        if self.hydrology and not self.canopy:
+            hy = abi.make_io(abi.HydrologyIO, abi.HYDROLOGY_FIELDS, st, self.ncol)
+            check(self.L.ctsmg_batch_fetch(self.h, C.byref(BatchInputs(_pt(sw), _pt(tt), None, None, None, None, None,
+                                                                       None, None, None, None, _pt(hy)))))
+        elif self.canopy:
             ci = abi.make_io(abi.CanopyIO, abi.CANOPY_FIELDS, st, self.ncol, self.npatch, self.ngrid, 1)
             sf = abi.make_io(abi.SoilFluxesIO, abi.SOILFLUXES_FIELDS, st, self.ncol, self.npatch) \
                 if self.soilfluxes else None
             rm = abi.make_io(abi.RootMoistIO, abi.ROOTMOIST_FIELDS, st, self.ncol, self.npatch) \
                 if self.rootmoist else None
             sr = abi.make_io(abi.SoilResisIO, abi.SOILRESIS_FIELDS, st, self.ncol) if self.soilresis else None
+            hy = abi.make_io(abi.HydrologyIO, abi.HYDROLOGY_FIELDS, st, self.ncol) if self.hydrology else None
             check(self.L.ctsmg_batch_fetch(self.h, C.byref(BatchInputs(_pt(sw), _pt(tt), C.pointer(ci), _pt(sf),
                                                                        _pt(rm), None, None, None, None, None,
-                                                                       _pt(sr)))))
+                                                                       _pt(sr), _pt(hy)))))
         else:
             check(self.L.ctsmg_batch_download(self.h, C.byref(sw), C.byref(tt)))
         return st

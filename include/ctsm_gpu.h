@@ -688,6 +688,14 @@ typedef struct {
      * iteration (src/biogeophys/CanopyFluxesMod.F90:833-895); the root sink
      * then uses that rootr.  The inputs' rm carries the components.       */
     int32_t rootmoist;
+    /* hydrology = 1 (with the moisture form) runs the default hydrology's
+     * water tables and lateral flows around SoilWater in every step:
+     * SaturatedExcessRunoff before it, PerchedWaterTable,
+     * ThetaBasedWaterTable, PerchedLateralFlow and SubsurfaceLateralFlow after
+     * it (HydrologyNoDrainageMod.F90:308-368, HydrologyDrainageMod.F90:139-143),
+     * with the parameters of ctsmg_set_soilhydrology_params, or per column
+     * baseflow_scalar / fff from the inputs (ensemble members).          */
+    int32_t hydrology;
 } ctsmg_batch_config;
 
 /* Everything a batch can hold, in one struct (NULL = not used).           */
@@ -703,6 +711,9 @@ typedef struct {
     const ctsmg_canopy_params* cpar;
     const ctsmg_pftcon* pft;
     const ctsmg_soilresis_io* sr;
+    const ctsmg_hydrology_io* hy;
+    const double* baseflow_scalar_c;     /* (c) or NULL */
+    const double* fff_c;                 /* (c) or NULL */
 } ctsmg_batch_inputs;
 
 /* Create a batch from `in` (the arrays are copied); ctsmg_batch_create*

@@ -70,9 +70,23 @@ def full_steps(A, npatch, ngrid, rootr, nsteps, medlyn_per_patch=False, method=1
             L.oracle_set_patch_medlyn(None, None)
 
 
-def soilwater(L, A, b, filt_c, swm=None, e_ice=6.0):
+def hydrology(L, A, b, filt_c, routines, hydro):
+    """The default-hydrology routines `routines` (indices of oracle_hydrology)
+    with hydro = [(column filter, abi.SoilHydrologyParams), ...] (one entry per
+    parameter set, e.g. per ensemble member)."""
+    ncol = A["zwt"].shape[0]
+    io = abi.make_io(abi.HydrologyIO, abi.HYDROLOGY_FIELDS, A, ncol)
+    for which in routines:
+        for f, par in hydro:
+            f = np.ascontiguousarray(f, dtype=np.int32)
+            assert L.oracle_hydrology(C.byref(b), len(f), _p(f, C.c_int32), C.byref(io), which, C.byref(par), DT) == 0
+
+
+def soilwater(L, A, b, filt_c, swm=None, e_ice=6.0, hydro=None):
     """HydrologyNoDrainage's SetSoilWaterFractions and SoilWater
-    (HydrologyNoDrainageMod.F90:302, 346) in the form swm selects."""
+    (HydrologyNoDrainageMod.F90:302, 346) in the form swm selects; with hydro
+    (see `hydrology`) SaturatedExcessRunoff before SoilWater and the water
+    tables and lateral flows after it (:308-368, HydrologyDrainageMod.F90:139-143)."""
     ncol = A["zwt"].shape[0]
     n = len(filt_c)
     fp = _p(filt_c, C.c_int32)
@@ -83,22 +97,26 @@ def soilwater(L, A, b, filt_c, swm=None, e_ice=6.0):
     else:
         sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS + abi.SOILWATER_EXTRA, A, ncol)
         L.oracle_set_soil_water_fractions(C.byref(b), n, fp, C.byref(sw))
+        if hydro:
+            hydrology(L, A, b, filt_c, [0], hydro)
         e = C.c_int(0)
         assert L.oracle_soilwater_mf(C.byref(b), n, fp, C.byref(sw), e_ice, DT, C.byref(swm), C.byref(e)) == 0, e.value
     if swm is not None and swm.use_flexibleCN:
         L.oracle_flexcn_fix(C.byref(b), n, fp, C.byref(sw))
+    if hydro:
+        hydrology(L, A, b, filt_c, [1, 2, 3, 4], hydro)
 
 
-def soil_steps(A, npatch, nsteps, swm=None, snow_method=0):
-    """nsteps x (SoilWater, SoilTemperature, h2osoi_vol refresh): the batched
-    engine's order 0."""
+def soil_steps(A, npatch, nsteps, swm=None, snow_method=0, hydro=None):
+    """nsteps x (SoilWater [with the default hydrology around it], SoilTemperature,
+    h2osoi_vol refresh): the batched engine's order 0."""
     L = orc.lib()
     ncol = A["zwt"].shape[0]
     b = abi.Bounds(1, ncol, 1, npatch)
     filt = np.arange(1, ncol + 1, dtype=np.int32)
     st = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, A, ncol, npatch)
     for _ in range(nsteps):
-        soilwater(L, A, b, filt, swm)
+        soilwater(L, A, b, filt, swm, hydro=hydro)
         assert L.oracle_soiltemperature(C.byref(b), ncol, _p(filt, C.c_int32), C.byref(st), DT, snow_method) == 0
         inputs.refresh_h2osoi_vol(A)
 

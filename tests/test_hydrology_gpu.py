@@ -23,7 +23,7 @@ WHICH = {"SaturatedExcessRunoff": 0, "PerchedWaterTable": 1, "ThetaBasedWaterTab
 OUT = [n for (n, k, t, u) in abi.HYDROLOGY_FIELDS if u != "in"]
 
 
-def state(ncol, seed):
+def state(ncol, seed, dry=True):
     A, _ = inputs.soil_columns(ncol, seed=seed, snow=True, nbedrock=(3, 20), zwt=(0.1, 9.5))
     r = np.random.Generator(np.random.Philox(seed + 1))
     fi.add_hydrology_fields(A, r)
@@ -31,9 +31,10 @@ def state(ncol, seed):
     sat = r.choice(ncol, ncol // 8, replace=False)          # saturated columns
     A["h2osoi_liq"][soil, sat] = 0.97 * A["watsat"][:abi.NLEVSOI, sat] * A["dz"][soil, sat] * 1000.0
     A["h2osoi_ice"][soil, sat] = 0.0
-    dry = r.choice(ncol, ncol // 8, replace=False)          # nearly dry layers
-    j = r.integers(1, abi.NLEVSOI + 1, size=len(dry))
-    A["h2osoi_liq"][j - LS, dry] = 0.001
+    dry_cols = r.choice(ncol, ncol // 8, replace=False)     # nearly dry layers
+    j = r.integers(1, abi.NLEVSOI + 1, size=len(dry_cols))
+    if dry:    # (the moisture form cannot take them: s at its 0.01 floor makes smp ~ 1e25 mm)
+        A["h2osoi_liq"][j - LS, dry_cols] = 0.001
     full = r.choice(ncol, ncol // 8, replace=False)         # over-full top layer
     A["h2osoi_liq"][1 - LS, full] = 2.0 * A["watsat"][0, full] * A["dz"][1 - LS, full] * 1000.0
     from ctsm_gb300.inputs import set_soil_water_fractions
@@ -92,3 +93,41 @@ def test_driver_sequence_with_filter(gpu_lib):
     assert (R["qflx_latflow_out"][c] == 0).any()          # water table below the bedrock
     assert (R["qflx_ice_runoff_xs"][c] >= 0).all() and (R["qflx_rsub_sat"][c] <= 0).all()
     assert (R["h2osfc"][c] > A["h2osfc"][c]).any()        # top-layer excess went to the surface
+
+
+def test_resident_steps_with_hydrology(gpu_lib):
+    """The moisture form with the default hydrology around it in the batched
+    engine, 4 steps, per-column baseflow_scalar and fff (two parameter sets
+    standing for ensemble members), against the oracle stepped the same way."""
+    from ctsm_gb300.engine import SoilBatch
+    from oracle.steps import soil_steps
+    from tests.parity import noise_spread
+    A = state(4000, seed=84, dry=False)
+    nml = abi.soilwater_movement_nml(1)
+    gpu_lib.set_soilwater_movement(nml)
+    gpu_lib.set_soilhydrology_params(**PAR)
+    try:
+        member = np.arange(4000) % 2
+        sets = [dict(PAR, baseflow_scalar=5.0e-3, fff=0.3), dict(PAR, baseflow_scalar=2.0e-2, fff=0.8)]
+        A["baseflow_scalar_c"] = np.array([sets[m]["baseflow_scalar"] for m in member])
+        A["fff_c"] = np.array([sets[m]["fff"] for m in member])
+        hydro = [(np.nonzero(member == m)[0].astype(np.int32) + 1, abi.SoilHydrologyParams(*sets[m].values()))
+                 for m in (0, 1)]
+        npatch = A["wtcol"].shape[0]
+        R = copy.deepcopy(A)
+        soil_steps(R, npatch, 4, swm=nml, hydro=hydro)
+        G = copy.deepcopy(A)
+        b = SoilBatch(G, npatch, dtime=DT, hydrology=True, per_column_hydrology=True)
+        b.run(4)
+        b.sync()
+        b.download()
+        b.close()
+        keys = ["h2osoi_liq", "h2osoi_ice", "t_soisno", "zwt", "zwt_perched", "frost_table", "h2osfc", "fsat",
+                "qflx_drain", "qflx_drain_perched", "qflx_latflow_out", "num_substeps", "h2osoi_vol"]
+        spread = noise_spread(lambda B: soil_steps(B, npatch, 4, swm=nml, hydro=hydro), A, R,
+                              fields=("qflx_drain", "qflx_drain_perched", "xmf"))
+        errs, bad = compare(G, R, keys, 1e-9, spread)
+        assert not bad, {k: errs[k] for k in bad}
+        assert (R["zwt"] != A["zwt"]).mean() > 0.5          # the water table is prognostic
+    finally:
+        gpu_lib.set_soilwater_movement(abi.soilwater_movement_nml(0, use_bedrock=0))
