@@ -179,7 +179,13 @@ HYDROLOGY_FIELDS = [
     ("qflx_drain_perched", "C", F64, "out"), ("qflx_latflow_out", "C", F64, "out"),
     ("qflx_latflow_in", "C", F64, "out"), ("qflx_rsub_sat", "C", F64, "out"), ("qflx_drain", "C", F64, "out"),
     ("qflx_qrgwl", "C", F64, "out"), ("qflx_ice_runoff_xs", "C", F64, "out"),
-]
+    ("snl", "C", I32, "in"),
+] + [(n, "C", F64, "in") for n in ("frac_sno_eff", "frac_h2osfc", "frac_h2osfc_nosnow", "h2osfc_thresh",
+                                    "qflx_snow_h2osfc", "qflx_floodc", "qflx_ev_soil_col",
+                                    "qflx_liqevap_from_top_layer_col", "qflx_ev_h2osfc_col")] + \
+    [(n, "C", F64, "out") for n in ("qflx_top_soil", "qflx_in_soil", "qflx_top_soil_to_h2osfc", "qinmax",
+                                     "qflx_infl_excess", "qflx_in_soil_limited", "qflx_in_h2osfc",
+                                     "qflx_infl_excess_surf", "qflx_h2osfc_surf", "qflx_h2osfc_drain", "qflx_infl")]
 
 # calc_soilevap_resis (sl_14 uses dsl/soilresis, leepielke_1992 soilbeta)
 SOILRESIS_FIELDS = [
@@ -223,7 +229,8 @@ class HydrologyIO(C.Structure):
 
 class SoilHydrologyParams(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("aq_sp_yield_min", "n_baseflow", "baseflow_scalar",
-                                           "perched_baseflow_scalar", "e_ice", "fff")]
+                                           "perched_baseflow_scalar", "e_ice", "fff", "pc", "mu")] + \
+               [("h2osfcflag", C.c_int32)]
 
 
 class SoilResisIO(C.Structure):

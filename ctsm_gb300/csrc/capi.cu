@@ -35,7 +35,7 @@ static ctsmg_soilwater_params g_swp = {6.0};
 static ctsmg_soil_resistance_params g_sres = {1, 15.0, 0.8};
 // SoilHydrologyMod / SaturatedExcessRunoffMod parameter-file values (absent
 // here; these stand in until ctsmg_set_soilhydrology_params)
-static ctsmg_soilhydrology_params g_shp = {0.01, 1.0, 1.0e-2, 1.0e-5, 6.0, 0.5};
+static ctsmg_soilhydrology_params g_shp = {0.01, 1.0, 1.0e-2, 1.0e-5, 6.0, 0.5, 0.4, 0.13, 1};
 // soilwater_movement_inparm; defaults of the Zeng-Decker form until ctsmg_init
 static ctsmg_soilwater_movement_nml g_swm = {0, 1, 4, 1, 0, 0, 60.0, 1.e-8, 1.e-1, 1.e-2};
 static ctsmg_canopy_params g_cpar;
@@ -370,6 +370,37 @@ const FieldDesc HYD_SLF_TABLE[] = {
     FW(ctsmg_hydrology_io, qflx_ice_runoff_xs, K_C, 8, U_OUT),
 };
 const int HYD_SLF_TABLE_N = sizeof(HYD_SLF_TABLE) / sizeof(HYD_SLF_TABLE[0]);
+const FieldDesc HYD_INF_TABLE[] = {
+    FW(ctsmg_hydrology_io, snl, K_C, 4, U_IN),
+    FW(ctsmg_hydrology_io, qflx_rain_plus_snomelt, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, qflx_snow_h2osfc, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, qflx_floodc, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, qflx_liqevap_from_top_layer_col, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, qflx_ev_soil_col, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, qflx_ev_h2osfc_col, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, qflx_sat_excess_surf, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, frac_sno_eff, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, frac_h2osfc, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, frac_h2osfc_nosnow, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, h2osfc_thresh, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, topo_slope, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, fsat, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, icefrac, K_G, 8, U_IN),
+    FW(ctsmg_hydrology_io, hksat, K_G, 8, U_IN),
+    FW(ctsmg_hydrology_io, h2osfc, K_C, 8, U_INOUT),
+    FW(ctsmg_hydrology_io, qflx_top_soil, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_in_soil, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_top_soil_to_h2osfc, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qinmax, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_infl_excess, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_in_soil_limited, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_in_h2osfc, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_infl_excess_surf, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_h2osfc_surf, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_h2osfc_drain, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_infl, K_C, 8, U_OUT),
+};
+const int HYD_INF_TABLE_N = sizeof(HYD_INF_TABLE) / sizeof(HYD_INF_TABLE[0]);
 const FieldDesc BAREGRND_SOILRESIS[] = {FW(ctsmg_baregrnd_io, soilresis, K_C, 8, U_IN)};
 const FieldDesc BAREGRND_SOILBETA[] = {FW(ctsmg_baregrnd_io, soilbeta, K_C, 8, U_IN)};
 
@@ -1336,7 +1367,7 @@ static int hydrology_call(const ctsmg_bounds* bounds, int32_t n, const int32_t* 
     if ((rc = check_filter(bounds, n, filt))) return rc;
     const int ncol = bounds->endc - bounds->begc + 1;
     if (io->ldc < ncol) return set_error(CTSMG_E_ARG, "ldc smaller than endc-begc+1", 0, 0);
-    if ((which == HYD_PERCHED_LAT || which == HYD_SUBSURFACE_LAT) && !(dtime > 0.0))
+    if ((which == HYD_PERCHED_LAT || which == HYD_SUBSURFACE_LAT || which == HYD_INFIL) && !(dtime > 0.0))
         return set_error(CTSMG_E_ARG, "dtime must be positive", 0, 0);
     for (int i = 0; i < NT; ++i)
         if (T[i].offset == offsetof(ctsmg_hydrology_io, nbedrock)) {
@@ -1380,5 +1411,9 @@ extern "C" int32_t ctsmg_perched_lateral_flow(const ctsmg_bounds* b, int32_t n, 
 extern "C" int32_t ctsmg_subsurface_lateral_flow(const ctsmg_bounds* b, int32_t n, const int32_t* f,
                                                  const ctsmg_hydrology_io* io, double dtime) {
     return hydrology_call(b, n, f, io, dtime, HYD_SUBSURFACE_LAT, HYD_SLF_TABLE, HYD_SLF_TABLE_N);
+}
+extern "C" int32_t ctsmg_infiltration_chain(const ctsmg_bounds* b, int32_t n, const int32_t* f,
+                                            const ctsmg_hydrology_io* io, double dtime) {
+    return hydrology_call(b, n, f, io, dtime, HYD_INFIL, HYD_INF_TABLE, HYD_INF_TABLE_N);
 }
 

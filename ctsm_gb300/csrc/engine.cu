@@ -289,6 +289,9 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
                 b->index[f.name] = (int)b->fields.size();
                 b->fields.push_back(u);
                 it = b->index.find(f.name);
+            } else if (b->fields[it->second].kind != f.kind || b->fields[it->second].esize != f.esize) {
+                return set_error(CTSMG_E_ARG, (std::string("component ") + f.name +
+                                               " is given with two layouts by the tables of the step").c_str(), 0, 0);
             } else if (b->fields[it->second].use == U_IN && f.use != U_IN) {
                 b->fields[it->second].use = f.use;      // written by some call of the step
             }
@@ -310,9 +313,11 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
             return fail(rc);
         if (cfg->hydrology) {
             std::memcpy(&b->hya.io, hy, sizeof b->hya.io);
-            const FieldDesc* tabs[5] = {HYD_SAT_TABLE, HYD_PWT_TABLE, HYD_TWT_TABLE, HYD_PLF_TABLE, HYD_SLF_TABLE};
-            const int ns[5] = {HYD_SAT_TABLE_N, HYD_PWT_TABLE_N, HYD_TWT_TABLE_N, HYD_PLF_TABLE_N, HYD_SLF_TABLE_N};
-            for (int k = 0; k < 5; ++k)
+            const FieldDesc* tabs[6] = {HYD_SAT_TABLE, HYD_INF_TABLE, HYD_PWT_TABLE, HYD_TWT_TABLE, HYD_PLF_TABLE,
+                                        HYD_SLF_TABLE};
+            const int ns[6] = {HYD_SAT_TABLE_N, HYD_INF_TABLE_N, HYD_PWT_TABLE_N, HYD_TWT_TABLE_N, HYD_PLF_TABLE_N,
+                               HYD_SLF_TABLE_N};
+            for (int k = 0; k < 6; ++k)
                 if ((rc = add(tabs[k], ns[k], hy, &b->hya.io))) return fail(rc);
             b->hya.par = current_soilhydrology_params();
             const double* hc[2] = {in->baseflow_scalar_c, in->fff_c};
@@ -508,9 +513,11 @@ extern "C" int32_t ctsmg_batch_fetch(ctsmg_batch bh, const ctsmg_batch_inputs* i
         (rc = download_table(bh->b, SOILRESIS_SL14_TABLE, SOILRESIS_SL14_NFIELDS, in->sr)))
         return rc;
     if (in->hy && bh->b->cfg.hydrology) {
-        const FieldDesc* tabs[5] = {HYD_SAT_TABLE, HYD_PWT_TABLE, HYD_TWT_TABLE, HYD_PLF_TABLE, HYD_SLF_TABLE};
-        const int ns[5] = {HYD_SAT_TABLE_N, HYD_PWT_TABLE_N, HYD_TWT_TABLE_N, HYD_PLF_TABLE_N, HYD_SLF_TABLE_N};
-        for (int k = 0; k < 5; ++k)
+        const FieldDesc* tabs[6] = {HYD_SAT_TABLE, HYD_INF_TABLE, HYD_PWT_TABLE, HYD_TWT_TABLE, HYD_PLF_TABLE,
+                                    HYD_SLF_TABLE};
+        const int ns[6] = {HYD_SAT_TABLE_N, HYD_INF_TABLE_N, HYD_PWT_TABLE_N, HYD_TWT_TABLE_N, HYD_PLF_TABLE_N,
+                           HYD_SLF_TABLE_N};
+        for (int k = 0; k < 6; ++k)
             if ((rc = download_table(bh->b, tabs[k], ns[k], in->hy))) return rc;
     }
     return 0;

@@ -42,6 +42,81 @@ __device__ __forceinline__ void saturated_excess_runoff(const ctsmg_hydrology_io
     io.fcov[c] = fsat;
 }
 
+// SetQflxInputs (SoilHydrologyMod.F90:298-366), InfiltrationExcessRunoff with
+// the hksat qinmax (InfiltrationExcessRunoffMod.F90:196-304),
+// RouteInfiltrationExcess (:369-423, soil columns), UpdateH2osfc with
+// QflxH2osfcSurf / QflxH2osfcDrain and truncate_small_values
+// (SurfaceWaterMod.F90:345-556, NumericsMod.F90:50-99) and Infiltration
+// (:426-457): the infiltration SoilWater takes as input.
+__device__ __forceinline__ void infiltration_chain(const ctsmg_hydrology_io& io, int c,
+                                                   const ctsmg_soilhydrology_params& P, double dtime) {
+    const View v{io, c, io.ldc};
+    const double fh = io.frac_h2osfc[c];
+    // SetQflxInputs
+    const double top = io.qflx_rain_plus_snomelt[c] + io.qflx_snow_h2osfc[c] + io.qflx_floodc[c];
+    double fsno, qflx_evap;
+    if (io.snl[c] >= 0) { fsno = 0.0; qflx_evap = io.qflx_liqevap_from_top_layer_col[c]; }
+    else { fsno = io.frac_sno_eff[c]; qflx_evap = io.qflx_ev_soil_col[c]; }
+    double in_soil = (1.0 - fh) * (top - io.qflx_sat_excess_surf[c]);
+    double to_h2osfc = fh * (top - io.qflx_sat_excess_surf[c]);
+    in_soil = in_soil - (1.0 - fsno - fh) * qflx_evap;
+    to_h2osfc = to_h2osfc - fh * io.qflx_ev_h2osfc_col[c];
+    io.qflx_top_soil[c] = top;
+    io.qflx_in_soil[c] = in_soil;
+    io.qflx_top_soil_to_h2osfc[c] = to_h2osfc;
+    // InfiltrationExcessRunoff (minval over levels 1..3 of 10^(-e_ice icefrac) hksat)
+    double qmu = pow10_dd(-P.e_ice * (io.icefrac[v.g(1)])) * io.hksat[v.g(1)];
+#pragma unroll
+    for (int j = 2; j <= 3; ++j) {
+        const double q = pow10_dd(-P.e_ice * (io.icefrac[v.g(j)])) * io.hksat[v.g(j)];
+        qmu = (q < qmu) ? q : qmu;
+    }
+    const double qinmax = (1.0 - io.fsat[c]) * qmu;
+    const double infl_excess = mx(0.0, (in_soil - (1.0 - fh) * qinmax));
+    io.qinmax[c] = qinmax;
+    io.qflx_infl_excess[c] = infl_excess;
+    // RouteInfiltrationExcess
+    const double limited = in_soil - infl_excess;
+    double in_h2osfc, excess_surf;
+    if (P.h2osfcflag != 0) { in_h2osfc = to_h2osfc + infl_excess; excess_surf = 0.0; }
+    else { in_h2osfc = to_h2osfc; excess_surf = infl_excess; }
+    io.qflx_in_soil_limited[c] = limited;
+    io.qflx_in_h2osfc[c] = in_h2osfc;
+    io.qflx_infl_excess_surf[c] = excess_surf;
+    // UpdateH2osfc
+    const double h0 = io.h2osfc[c], thr = io.h2osfc_thresh[c];
+    double frac_infclust = 0.0;
+    if (P.h2osfcflag == 1) {
+        const double fn = io.frac_h2osfc_nosnow[c];
+        frac_infclust = (fn <= P.pc) ? 0.0 : pow(fn - P.pc, P.mu);
+    }
+    double surf;
+    if (h0 > thr && P.h2osfcflag != 0) {
+        const double k_wet = 1.0e-4 * sin((RPI / 180.0) * io.topo_slope[c]);
+        surf = k_wet * frac_infclust * (h0 - thr);
+        surf = mn(surf, (h0 - thr) / dtime);
+    } else {
+        surf = 0.0;
+    }
+    if (surf < (double)1.0e-8f) surf = 0.0;
+    io.qflx_h2osfc_surf[c] = surf;
+    double hp = h0 + (in_h2osfc - surf) * dtime;
+    if (fabs(hp) < 1.e-13 * fabs(h0)) hp = 0.0;
+    double drain;
+    if (hp < 0.0) {
+        drain = hp / dtime;
+    } else {
+        drain = mn(fh * qinmax, hp / dtime);
+        if (P.h2osfcflag == 0) drain = mx(0.0, hp / dtime);
+    }
+    io.qflx_h2osfc_drain[c] = drain;
+    double h1 = hp - drain * dtime;
+    if (fabs(h1) < 1.e-13 * fabs(hp)) h1 = 0.0;
+    io.h2osfc[c] = h1;
+    // Infiltration
+    io.qflx_infl[c] = limited + drain;
+}
+
 // PerchedWaterTable (SoilHydrologyMod.F90:1525-1641)
 __device__ __forceinline__ void perched_water_table(const ctsmg_hydrology_io& io, int c) {
     const View v{io, c, io.ldc};

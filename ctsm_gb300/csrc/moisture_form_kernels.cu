@@ -299,7 +299,10 @@ mf_step_kernel(ctsmg_soilwater_io io, int ncol, MoistureFormArgs P, int flexcn, 
         if (hy.fff_c) hp.fff = hy.fff_c[c];
     }
     set_soil_water_fractions(io, c);
-    if (HYDRO) hydro::saturated_excess_runoff(hy.io, c, hp.fff);
+    if (HYDRO) {
+        hydro::saturated_excess_runoff(hy.io, c, hp.fff);
+        hydro::infiltration_chain(hy.io, c, hp, P.dtime);    // qflx_infl for SoilWater
+    }
     const int info = mf_column(io, c, P);
     if (info > 0) report_error(err, c + 1, info, CTSMG_E_SINGULAR);
     else if (info < 0) report_error(err, c + 1, 0, CTSMG_E_TIMEOUT);

@@ -218,16 +218,25 @@ def add_baregrnd_fields(A, npatch, ngrid):
 
 
 def add_hydrology_fields(A, rng=None):
-    """The water-table / drainage components a soil state lacks: topographic
-    slope U(0.1, 10) degrees, wtfact U(0.2, 0.6), rain plus snowmelt U(0, 1e-4)
-    mm/s, snow capping U(0, 1e-6) mm/s (builder's choices); zwt_perched and
-    frost_table start at the water table; zero-filled outputs."""
+    """The water-table / drainage / infiltration components a soil state
+    lacks: topographic slope U(0.1, 10) degrees, wtfact U(0.2, 0.6), rain plus
+    snowmelt U(0, 1e-4) mm/s, snow capping U(0, 1e-6) mm/s, the top-layer and
+    surface-water evaporation, h2osfc_thresh U(5, 30) mm (builder's choices);
+    zwt_perched and frost_table start at the water table; zero-filled
+    outputs."""
     r = rng if rng is not None else np.random.Generator(np.random.Philox(7))
     ncol = A["zwt"].shape[0]
     A["topo_slope"] = r.uniform(0.1, 10.0, ncol)
     A["wtfact"] = r.uniform(0.2, 0.6, ncol)
     A["qflx_rain_plus_snomelt"] = r.uniform(0.0, 1e-4, ncol)
     A["qflx_snwcp_liq"] = r.uniform(0.0, 1e-6, ncol)
+    A["qflx_snow_h2osfc"] = r.uniform(0.0, 1e-6, ncol)
+    A["qflx_floodc"] = np.zeros(ncol)
+    A["qflx_liqevap_from_top_layer_col"] = r.uniform(0.0, 2e-5, ncol)
+    A["qflx_ev_soil_col"] = r.uniform(-1e-6, 2e-5, ncol)
+    A["qflx_ev_h2osfc_col"] = r.uniform(0.0, 2e-5, ncol)
+    A["frac_h2osfc_nosnow"] = np.clip(A["frac_h2osfc"] * 1.2, 0.0, 1.0) if "frac_h2osfc" in A else np.zeros(ncol)
+    A["h2osfc_thresh"] = r.uniform(5.0, 30.0, ncol)
     A["zwt_perched"] = A["zwt"].copy()
     A["frost_table"] = A["zwt"].copy()
     if "h2osfc" not in A:

@@ -94,9 +94,10 @@ def calc_soilevap_resis(bounds, num_nolakec, filter_nolakec, state):
     check(L.ctsmg_soilevap_resis(C.byref(bounds), int(num_nolakec), fp, C.byref(io)))
 
 
-HYDROLOGY_ROUTINES = ("SaturatedExcessRunoff", "PerchedWaterTable", "ThetaBasedWaterTable", "PerchedLateralFlow",
+HYDROLOGY_ROUTINES = ("SaturatedExcessRunoff", "InfiltrationChain", "PerchedWaterTable", "ThetaBasedWaterTable", "PerchedLateralFlow",
                       "SubsurfaceLateralFlow")
 _HYD_ENTRY = {"SaturatedExcessRunoff": "ctsmg_saturated_excess_runoff",
+              "InfiltrationChain": "ctsmg_infiltration_chain",
               "PerchedWaterTable": "ctsmg_perched_water_table",
               "ThetaBasedWaterTable": "ctsmg_theta_based_water_table",
               "PerchedLateralFlow": "ctsmg_perched_lateral_flow",
@@ -104,12 +105,15 @@ _HYD_ENTRY = {"SaturatedExcessRunoff": "ctsmg_saturated_excess_runoff",
 
 
 def set_soilhydrology_params(aq_sp_yield_min=0.01, n_baseflow=1.0, baseflow_scalar=1.0e-2,
-                             perched_baseflow_scalar=1.0e-5, e_ice=6.0, fff=0.5):
+                             perched_baseflow_scalar=1.0e-5, e_ice=6.0, fff=0.5, pc=0.4, mu=0.13, h2osfcflag=1):
     """ctsmg_set_soilhydrology_params: readParams of SoilHydrologyMod
-    (SoilHydrologyMod.F90:174-199) and SaturatedExcessRunoffMod (fff)."""
+    (SoilHydrologyMod.F90:174-199), SaturatedExcessRunoffMod (fff) and
+    SurfaceWaterMod (pc, mu), and h2osfcflag.  The parameter-file values are
+    builder's choices (the file is absent)."""
     L = load()
     L.ctsmg_set_soilhydrology_params.argtypes = [C.POINTER(abi.SoilHydrologyParams)]
-    p = abi.SoilHydrologyParams(aq_sp_yield_min, n_baseflow, baseflow_scalar, perched_baseflow_scalar, e_ice, fff)
+    p = abi.SoilHydrologyParams(aq_sp_yield_min, n_baseflow, baseflow_scalar, perched_baseflow_scalar, e_ice, fff,
+                                pc, mu, h2osfcflag)
     check(L.ctsmg_set_soilhydrology_params(C.byref(p)))
 
 
@@ -120,7 +124,7 @@ def hydrology(routine, bounds, num_hydrologyc, filter_hydrologyc, state, dtime=N
     name = _HYD_ENTRY[routine]
     fn = getattr(L, name)
     args = [C.POINTER(abi.Bounds), C.c_int32, C.POINTER(C.c_int32), C.POINTER(abi.HydrologyIO)]
-    lateral = routine in ("PerchedLateralFlow", "SubsurfaceLateralFlow")
+    lateral = routine in ("PerchedLateralFlow", "SubsurfaceLateralFlow", "InfiltrationChain")
     fn.argtypes = args + ([C.c_double] if lateral else [])
     f, fp = _filter(filter_hydrologyc)
     ncol = bounds.endc - bounds.begc + 1

@@ -419,6 +419,9 @@ int32_t ctsmg_root_moist_stress(const ctsmg_bounds* bounds, int32_t num_exposedv
  * urban columns and the volumetric discharge diagnostics are not built.   */
 typedef struct {
     double aq_sp_yield_min, n_baseflow, baseflow_scalar, perched_baseflow_scalar, e_ice, fff;
+    /* surface water (SurfaceWaterMod.F90:42-43, 68-70) and soilhydrology_inst%h2osfcflag (1) */
+    double pc, mu;
+    int32_t h2osfcflag;
 } ctsmg_soilhydrology_params;
 
 typedef struct {
@@ -455,11 +458,44 @@ typedef struct {
     double* qflx_drain;               /* (c)  out (mm/s)                            */
     double* qflx_qrgwl;               /* (c)  out (mm/s)                            */
     double* qflx_ice_runoff_xs;       /* (c)  out (mm/s)                            */
+    /* the infiltration chain before SoilWater (SetQflxInputs,
+     * InfiltrationExcessRunoff with the hksat qinmax, RouteInfiltrationExcess,
+     * UpdateH2osfc, Infiltration)                                          */
+    const int32_t* snl;               /* (c)                                        */
+    const double* frac_sno_eff;       /* (c)                                        */
+    const double* frac_h2osfc;        /* (c)                                        */
+    const double* frac_h2osfc_nosnow; /* (c)                                        */
+    const double* h2osfc_thresh;      /* (c)  (mm)                                  */
+    const double* qflx_snow_h2osfc;   /* (c)  (mm/s)                                */
+    const double* qflx_floodc;        /* (c)  (mm/s)                                */
+    /* the column averages (qflx_*_col), distinct from the patch fluxes of
+     * SoilTemperature / SoilFluxes with the same base name                  */
+    const double* qflx_ev_soil_col;   /* (c)  (mm/s)                                */
+    const double* qflx_liqevap_from_top_layer_col; /* (c) (mm/s)                    */
+    const double* qflx_ev_h2osfc_col; /* (c)  (mm/s)                                */
+    double* qflx_top_soil;            /* (c)  out                                   */
+    double* qflx_in_soil;             /* (c)  out                                   */
+    double* qflx_top_soil_to_h2osfc;  /* (c)  out                                   */
+    double* qinmax;                   /* (c)  out                                   */
+    double* qflx_infl_excess;         /* (c)  out                                   */
+    double* qflx_in_soil_limited;     /* (c)  out                                   */
+    double* qflx_in_h2osfc;           /* (c)  out                                   */
+    double* qflx_infl_excess_surf;    /* (c)  out                                   */
+    double* qflx_h2osfc_surf;         /* (c)  out                                   */
+    double* qflx_h2osfc_drain;        /* (c)  out                                   */
+    double* qflx_infl;                /* (c)  out: infiltration, SoilWater's input  */
 } ctsmg_hydrology_io;
 
 /* readParams of SoilHydrologyMod and SaturatedExcessRunoffMod. */
 int32_t ctsmg_set_soilhydrology_params(const ctsmg_soilhydrology_params* p);
 /* One entry per reference routine, over filter_hydrologyc (1-based). */
+/* SetQflxInputs (SoilHydrologyMod.F90:298-366), InfiltrationExcessRunoff
+ * (InfiltrationExcessRunoffMod.F90:196-304), RouteInfiltrationExcess
+ * (SoilHydrologyMod.F90:369-423), UpdateH2osfc (SurfaceWaterMod.F90:345-556)
+ * and Infiltration (SoilHydrologyMod.F90:426-457), in this order, after
+ * SaturatedExcessRunoff.                                                  */
+int32_t ctsmg_infiltration_chain(const ctsmg_bounds* bounds, int32_t num_hydrologyc,
+                                 const int32_t* filter_hydrologyc, const ctsmg_hydrology_io* io, double dtime);
 int32_t ctsmg_saturated_excess_runoff(const ctsmg_bounds* bounds, int32_t num_hydrologyc,
                                       const int32_t* filter_hydrologyc, const ctsmg_hydrology_io* io);
 int32_t ctsmg_perched_water_table(const ctsmg_bounds* bounds, int32_t num_hydrologyc,

@@ -2,6 +2,10 @@
 // water-table and drainage routines of the default hydrology, for natural
 // soil columns outside hillslopes, statement by statement:
 //   SaturatedExcessRunoff / ComputeFsatTopmodel  SaturatedExcessRunoffMod.F90:200-360
+//   SetQflxInputs, RouteInfiltrationExcess, Infiltration  SoilHydrologyMod.F90:298-457
+//   InfiltrationExcessRunoff (hksat qinmax)  InfiltrationExcessRunoffMod.F90:196-304
+//   UpdateH2osfc, QflxH2osfcSurf, QflxH2osfcDrain  SurfaceWaterMod.F90:345-556
+//   truncate_small_values   src/utils/NumericsMod.F90:50-99 (rel_epsilon 1e-13)
 //   PerchedWaterTable       SoilHydrologyMod.F90:1525-1641
 //   ThetaBasedWaterTable    SoilHydrologyMod.F90:1933-2025
 //   PerchedLateralFlow      SoilHydrologyMod.F90:1645-1929
@@ -56,6 +60,61 @@ extern "C" int oracle_hydrology(const ctsmg_bounds* b, int n, const int32_t* fil
             io->fsat[c] = fsat;
             io->qflx_sat_excess_surf[c] = fsat * io->qflx_rain_plus_snomelt[c];
             io->fcov[c] = fsat;
+        } else if (which == 5) {               // SetQflxInputs .. Infiltration
+            const double fh = io->frac_h2osfc[c];
+            // SetQflxInputs (SoilHydrologyMod.F90:298-366)
+            io->qflx_top_soil[c] = io->qflx_rain_plus_snomelt[c] + io->qflx_snow_h2osfc[c] + io->qflx_floodc[c];
+            double fsno, qflx_evap;
+            if (io->snl[c] >= 0) { fsno = 0.0; qflx_evap = io->qflx_liqevap_from_top_layer_col[c]; }
+            else { fsno = io->frac_sno_eff[c]; qflx_evap = io->qflx_ev_soil_col[c]; }
+            io->qflx_in_soil[c] = (1.0 - fh) * (io->qflx_top_soil[c] - io->qflx_sat_excess_surf[c]);
+            io->qflx_top_soil_to_h2osfc[c] = fh * (io->qflx_top_soil[c] - io->qflx_sat_excess_surf[c]);
+            io->qflx_in_soil[c] = io->qflx_in_soil[c] - (1.0 - fsno - fh) * qflx_evap;
+            io->qflx_top_soil_to_h2osfc[c] = io->qflx_top_soil_to_h2osfc[c] - fh * io->qflx_ev_h2osfc_col[c];
+            // InfiltrationExcessRunoff, hksat qinmax (InfiltrationExcessRunoffMod.F90:196-304)
+            double qmu = 0.0;
+            for (int j = 1; j <= 3; ++j) {
+                const double q = o_pow(10.0, -P->e_ice * (io->icefrac[c + (size_t)(j - 1) * k.ld])) *
+                                 io->hksat[c + (size_t)(j - 1) * k.ld];
+                qmu = (j == 1) ? q : std::min(qmu, q);
+            }
+            io->qinmax[c] = (1.0 - io->fsat[c]) * qmu;
+            io->qflx_infl_excess[c] = std::max(0.0, (io->qflx_in_soil[c] - (1.0 - fh) * io->qinmax[c]));
+            // RouteInfiltrationExcess (:369-423)
+            io->qflx_in_soil_limited[c] = io->qflx_in_soil[c] - io->qflx_infl_excess[c];
+            if (P->h2osfcflag != 0) {
+                io->qflx_in_h2osfc[c] = io->qflx_top_soil_to_h2osfc[c] + io->qflx_infl_excess[c];
+                io->qflx_infl_excess_surf[c] = 0.0;
+            } else {
+                io->qflx_in_h2osfc[c] = io->qflx_top_soil_to_h2osfc[c];
+                io->qflx_infl_excess_surf[c] = io->qflx_infl_excess[c];
+            }
+            // UpdateH2osfc (SurfaceWaterMod.F90:345-556)
+            double frac_infclust = 0.0;
+            if (P->h2osfcflag == 1) {
+                if (io->frac_h2osfc_nosnow[c] <= P->pc) frac_infclust = 0.0;
+                else frac_infclust = o_pow(io->frac_h2osfc_nosnow[c] - P->pc, P->mu);
+            }
+            if (io->h2osfc[c] > io->h2osfc_thresh[c] && P->h2osfcflag != 0) {
+                const double k_wet = 1.0e-4 * std::sin((RPI / 180.0) * io->topo_slope[c]);
+                io->qflx_h2osfc_surf[c] = k_wet * frac_infclust * (io->h2osfc[c] - io->h2osfc_thresh[c]);
+                io->qflx_h2osfc_surf[c] = std::min(io->qflx_h2osfc_surf[c], (io->h2osfc[c] - io->h2osfc_thresh[c]) / dtime);
+            } else {
+                io->qflx_h2osfc_surf[c] = 0.0;
+            }
+            if (io->qflx_h2osfc_surf[c] < (double)1.0e-8f) io->qflx_h2osfc_surf[c] = 0.0;
+            double h2osfc_partial = io->h2osfc[c] + (io->qflx_in_h2osfc[c] - io->qflx_h2osfc_surf[c]) * dtime;
+            if (std::fabs(h2osfc_partial) < 1.e-13 * std::fabs(io->h2osfc[c])) h2osfc_partial = 0.0;
+            if (h2osfc_partial < 0.0) {
+                io->qflx_h2osfc_drain[c] = h2osfc_partial / dtime;
+            } else {
+                io->qflx_h2osfc_drain[c] = std::min(fh * io->qinmax[c], h2osfc_partial / dtime);
+                if (P->h2osfcflag == 0) io->qflx_h2osfc_drain[c] = std::max(0.0, h2osfc_partial / dtime);
+            }
+            io->h2osfc[c] = h2osfc_partial - io->qflx_h2osfc_drain[c] * dtime;
+            if (std::fabs(io->h2osfc[c]) < 1.e-13 * std::fabs(h2osfc_partial)) io->h2osfc[c] = 0.0;
+            // Infiltration (:426-457)
+            io->qflx_infl[c] = io->qflx_in_soil_limited[c] + io->qflx_h2osfc_drain[c];
         } else if (which == 1) {               // PerchedWaterTable
             int k_frz = (k.t(1) > TFRZ) ? NLEVSOI : 1;
             for (int kk = 2; kk <= NLEVSOI; ++kk)

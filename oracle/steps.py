@@ -85,8 +85,8 @@ def hydrology(L, A, b, filt_c, routines, hydro):
 def soilwater(L, A, b, filt_c, swm=None, e_ice=6.0, hydro=None):
     """HydrologyNoDrainage's SetSoilWaterFractions and SoilWater
     (HydrologyNoDrainageMod.F90:302, 346) in the form swm selects; with hydro
-    (see `hydrology`) SaturatedExcessRunoff before SoilWater and the water
-    tables and lateral flows after it (:308-368, HydrologyDrainageMod.F90:139-143)."""
+    (see `hydrology`) SaturatedExcessRunoff and the infiltration chain before
+    SoilWater and the water tables and lateral flows after it (:308-368, HydrologyDrainageMod.F90:139-143)."""
     ncol = A["zwt"].shape[0]
     n = len(filt_c)
     fp = _p(filt_c, C.c_int32)
@@ -98,7 +98,7 @@ def soilwater(L, A, b, filt_c, swm=None, e_ice=6.0, hydro=None):
         sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS + abi.SOILWATER_EXTRA, A, ncol)
         L.oracle_set_soil_water_fractions(C.byref(b), n, fp, C.byref(sw))
         if hydro:
-            hydrology(L, A, b, filt_c, [0], hydro)
+            hydrology(L, A, b, filt_c, [0, 5], hydro)
         e = C.c_int(0)
         assert L.oracle_soilwater_mf(C.byref(b), n, fp, C.byref(sw), e_ice, DT, C.byref(swm), C.byref(e)) == 0, e.value
     if swm is not None and swm.use_flexibleCN:

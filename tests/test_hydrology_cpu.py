@@ -27,7 +27,7 @@ def _run(A, which):
     ncol = A["zwt"].shape[0]
     io = abi.make_io(abi.HydrologyIO, abi.HYDROLOGY_FIELDS, A, ncol)
     f = np.arange(1, ncol + 1, dtype=np.int32)
-    P = abi.SoilHydrologyParams(0.01, 1.0, 1.0e-2, 1.0e-5, 6.0, 0.5)
+    P = abi.SoilHydrologyParams(0.01, 1.0, 1.0e-2, 1.0e-5, 6.0, 0.5, 0.4, 0.13, 1)
     assert orc.lib().oracle_hydrology(C.byref(abi.Bounds(1, ncol, 1, 1)), ncol, _p(f, C.c_int32), C.byref(io),
                                       which, C.byref(P), DT) == 0
 

@@ -17,14 +17,14 @@ pytestmark = pytest.mark.gpu
 LS = -abi.NLEVSNO + 1
 DT = 1800.0
 PAR = dict(aq_sp_yield_min=0.01, n_baseflow=1.0, baseflow_scalar=1.0e-2, perched_baseflow_scalar=1.0e-5, e_ice=6.0,
-           fff=0.5)
+           fff=0.5, pc=0.4, mu=0.13, h2osfcflag=1)
 WHICH = {"SaturatedExcessRunoff": 0, "PerchedWaterTable": 1, "ThetaBasedWaterTable": 2, "PerchedLateralFlow": 3,
-         "SubsurfaceLateralFlow": 4}
+         "SubsurfaceLateralFlow": 4, "InfiltrationChain": 5}
 OUT = [n for (n, k, t, u) in abi.HYDROLOGY_FIELDS if u != "in"]
 
 
 def state(ncol, seed, dry=True):
-    A, _ = inputs.soil_columns(ncol, seed=seed, snow=True, nbedrock=(3, 20), zwt=(0.1, 9.5))
+    A, _ = inputs.soil_columns(ncol, seed=seed, snow=True, nbedrock=(3, 20), zwt=(0.1, 9.5), h2osfc=True)
     r = np.random.Generator(np.random.Philox(seed + 1))
     fi.add_hydrology_fields(A, r)
     soil = slice(1 - LS, abi.NLEVSOI + 1 - LS)
@@ -79,8 +79,8 @@ def test_driver_sequence_with_filter(gpu_lib):
     over a filter with gaps and an offset column range; the branches acted."""
     gpu_lib.set_soilhydrology_params(**PAR)
     A = state(6000, seed=82)
-    seq = ["SaturatedExcessRunoff", "PerchedWaterTable", "ThetaBasedWaterTable", "PerchedLateralFlow",
-           "SubsurfaceLateralFlow"]
+    seq = ["SaturatedExcessRunoff", "InfiltrationChain", "PerchedWaterTable", "ThetaBasedWaterTable",
+           "PerchedLateralFlow", "SubsurfaceLateralFlow"]
     r = np.random.Generator(np.random.Philox(83))
     filt = np.sort(r.choice(np.arange(11, 6011, dtype=np.int32), 5000, replace=False))
     G, R = copy.deepcopy(A), copy.deepcopy(A)
@@ -93,10 +93,13 @@ def test_driver_sequence_with_filter(gpu_lib):
     assert (R["qflx_latflow_out"][c] == 0).any()          # water table below the bedrock
     assert (R["qflx_ice_runoff_xs"][c] >= 0).all() and (R["qflx_rsub_sat"][c] <= 0).all()
     assert (R["h2osfc"][c] > A["h2osfc"][c]).any()        # top-layer excess went to the surface
+    assert (R["qflx_infl_excess"][c] > 0).any() and (R["qflx_h2osfc_drain"][c] > 0).any()
+    assert (R["qflx_infl"][c] != 0).all()
 
 
 def test_resident_steps_with_hydrology(gpu_lib):
-    """The moisture form with the default hydrology around it in the batched
+    """The moisture form with the default hydrology around it (fsat and the
+    infiltration chain feeding SoilWater's qflx_infl before it) in the batched
     engine, 4 steps, per-column baseflow_scalar and fff (two parameter sets
     standing for ensemble members), against the oracle stepped the same way."""
     from ctsm_gb300.engine import SoilBatch
@@ -122,7 +125,7 @@ def test_resident_steps_with_hydrology(gpu_lib):
         b.sync()
         b.download()
         b.close()
-        keys = ["h2osoi_liq", "h2osoi_ice", "t_soisno", "zwt", "zwt_perched", "frost_table", "h2osfc", "fsat",
+        keys = ["h2osoi_liq", "h2osoi_ice", "t_soisno", "zwt", "zwt_perched", "frost_table", "h2osfc", "fsat", "qflx_infl",
                 "qflx_drain", "qflx_drain_perched", "qflx_latflow_out", "num_substeps", "h2osoi_vol"]
         spread = noise_spread(lambda B: soil_steps(B, npatch, 4, swm=nml, hydro=hydro), A, R,
                               fields=("qflx_drain", "qflx_drain_perched", "xmf"))
