@@ -185,7 +185,8 @@ HYDROLOGY_FIELDS = [
                                     "qflx_liqevap_from_top_layer_col", "qflx_ev_h2osfc_col")] + \
     [(n, "C", F64, "out") for n in ("qflx_top_soil", "qflx_in_soil", "qflx_top_soil_to_h2osfc", "qinmax",
                                      "qflx_infl_excess", "qflx_in_soil_limited", "qflx_in_h2osfc",
-                                     "qflx_infl_excess_surf", "qflx_h2osfc_surf", "qflx_h2osfc_drain", "qflx_infl")]
+                                     "qflx_infl_excess_surf", "qflx_h2osfc_surf", "qflx_h2osfc_drain", "qflx_infl")] + \
+    [("wa", "C", F64, "inout"), ("qcharge", "C", F64, "in"), ("hkdepth", "C", F64, "in")]
 
 # calc_soilevap_resis (sl_14 uses dsl/soilresis, leepielke_1992 soilbeta)
 SOILRESIS_FIELDS = [

@@ -401,6 +401,55 @@ const FieldDesc HYD_INF_TABLE[] = {
     FW(ctsmg_hydrology_io, qflx_infl, K_C, 8, U_OUT),
 };
 const int HYD_INF_TABLE_N = sizeof(HYD_INF_TABLE) / sizeof(HYD_INF_TABLE[0]);
+const FieldDesc HYD_WT_TABLE[] = {
+    FW(ctsmg_hydrology_io, z, K_SS, 8, U_IN),
+    FW(ctsmg_hydrology_io, zi, K_ZI, 8, U_IN),
+    FW(ctsmg_hydrology_io, dz, K_SS, 8, U_IN),
+    FW(ctsmg_hydrology_io, t_soisno, K_SS, 8, U_IN),
+    FW(ctsmg_hydrology_io, h2osoi_liq, K_SS, 8, U_IN),
+    FW(ctsmg_hydrology_io, h2osoi_ice, K_SS, 8, U_IN),
+    FW(ctsmg_hydrology_io, h2osoi_vol, K_G, 8, U_INOUT),
+    FW(ctsmg_hydrology_io, zwt, K_C, 8, U_INOUT),
+    FW(ctsmg_hydrology_io, zwt_perched, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, frost_table, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, watsat, K_G, 8, U_IN),
+    FW(ctsmg_hydrology_io, bsw, K_G, 8, U_IN),
+    FW(ctsmg_hydrology_io, sucsat, K_G, 8, U_IN),
+    FW(ctsmg_hydrology_io, wa, K_C, 8, U_INOUT),
+    FW(ctsmg_hydrology_io, qcharge, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, qflx_drain, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_rsub_sat, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_drain_perched, K_C, 8, U_OUT),
+};
+const int HYD_WT_TABLE_N = sizeof(HYD_WT_TABLE) / sizeof(HYD_WT_TABLE[0]);
+const FieldDesc HYD_DR_TABLE[] = {
+    FW(ctsmg_hydrology_io, z, K_SS, 8, U_IN),
+    FW(ctsmg_hydrology_io, zi, K_ZI, 8, U_IN),
+    FW(ctsmg_hydrology_io, dz, K_SS, 8, U_IN),
+    FW(ctsmg_hydrology_io, t_soisno, K_SS, 8, U_IN),
+    FW(ctsmg_hydrology_io, h2osoi_liq, K_SS, 8, U_INOUT),
+    FW(ctsmg_hydrology_io, h2osoi_ice, K_SS, 8, U_INOUT),
+    FW(ctsmg_hydrology_io, h2osfc, K_C, 8, U_INOUT),
+    FW(ctsmg_hydrology_io, zwt, K_C, 8, U_INOUT),
+    FW(ctsmg_hydrology_io, zwt_perched, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, frost_table, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, icefrac, K_G, 8, U_OUT),
+    FW(ctsmg_hydrology_io, watsat, K_G, 8, U_IN),
+    FW(ctsmg_hydrology_io, hksat, K_G, 8, U_IN),
+    FW(ctsmg_hydrology_io, bsw, K_G, 8, U_IN),
+    FW(ctsmg_hydrology_io, sucsat, K_G, 8, U_IN),
+    FW(ctsmg_hydrology_io, eff_porosity, K_G, 8, U_IN),
+    FW(ctsmg_hydrology_io, topo_slope, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, hkdepth, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, wa, K_C, 8, U_INOUT),
+    FW(ctsmg_hydrology_io, qflx_snwcp_liq, K_C, 8, U_IN),
+    FW(ctsmg_hydrology_io, qflx_drain, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_rsub_sat, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_drain_perched, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_qrgwl, K_C, 8, U_OUT),
+    FW(ctsmg_hydrology_io, qflx_ice_runoff_xs, K_C, 8, U_OUT),
+};
+const int HYD_DR_TABLE_N = sizeof(HYD_DR_TABLE) / sizeof(HYD_DR_TABLE[0]);
 const FieldDesc BAREGRND_SOILRESIS[] = {FW(ctsmg_baregrnd_io, soilresis, K_C, 8, U_IN)};
 const FieldDesc BAREGRND_SOILBETA[] = {FW(ctsmg_baregrnd_io, soilbeta, K_C, 8, U_IN)};
 
@@ -1367,7 +1416,7 @@ static int hydrology_call(const ctsmg_bounds* bounds, int32_t n, const int32_t* 
     if ((rc = check_filter(bounds, n, filt))) return rc;
     const int ncol = bounds->endc - bounds->begc + 1;
     if (io->ldc < ncol) return set_error(CTSMG_E_ARG, "ldc smaller than endc-begc+1", 0, 0);
-    if ((which == HYD_PERCHED_LAT || which == HYD_SUBSURFACE_LAT || which == HYD_INFIL) && !(dtime > 0.0))
+    if (which != HYD_SAT_EXCESS && which != HYD_PERCHED_WT && which != HYD_THETA_WT && !(dtime > 0.0))
         return set_error(CTSMG_E_ARG, "dtime must be positive", 0, 0);
     for (int i = 0; i < NT; ++i)
         if (T[i].offset == offsetof(ctsmg_hydrology_io, nbedrock)) {
@@ -1415,5 +1464,13 @@ extern "C" int32_t ctsmg_subsurface_lateral_flow(const ctsmg_bounds* b, int32_t 
 extern "C" int32_t ctsmg_infiltration_chain(const ctsmg_bounds* b, int32_t n, const int32_t* f,
                                             const ctsmg_hydrology_io* io, double dtime) {
     return hydrology_call(b, n, f, io, dtime, HYD_INFIL, HYD_INF_TABLE, HYD_INF_TABLE_N);
+}
+extern "C" int32_t ctsmg_water_table(const ctsmg_bounds* b, int32_t n, const int32_t* f, const ctsmg_hydrology_io* io,
+                                     double dtime) {
+    return hydrology_call(b, n, f, io, dtime, HYD_WATER_TABLE, HYD_WT_TABLE, HYD_WT_TABLE_N);
+}
+extern "C" int32_t ctsmg_drainage(const ctsmg_bounds* b, int32_t n, const int32_t* f, const ctsmg_hydrology_io* io,
+                                  double dtime) {
+    return hydrology_call(b, n, f, io, dtime, HYD_DRAINAGE, HYD_DR_TABLE, HYD_DR_TABLE_N);
 }
 

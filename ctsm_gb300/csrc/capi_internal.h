@@ -18,8 +18,9 @@ extern const int SOILWATER_FLEXCN_NFIELDS;
 extern const FieldDesc SOILRESIS_SL14_TABLE[];
 extern const int SOILRESIS_SL14_NFIELDS;
 extern const FieldDesc HYD_SAT_TABLE[], HYD_PWT_TABLE[], HYD_TWT_TABLE[], HYD_PLF_TABLE[], HYD_SLF_TABLE[],
-    HYD_INF_TABLE[];
-extern const int HYD_SAT_TABLE_N, HYD_PWT_TABLE_N, HYD_TWT_TABLE_N, HYD_PLF_TABLE_N, HYD_SLF_TABLE_N, HYD_INF_TABLE_N;
+    HYD_INF_TABLE[], HYD_WT_TABLE[], HYD_DR_TABLE[];
+extern const int HYD_SAT_TABLE_N, HYD_PWT_TABLE_N, HYD_TWT_TABLE_N, HYD_PLF_TABLE_N, HYD_SLF_TABLE_N, HYD_INF_TABLE_N,
+    HYD_WT_TABLE_N, HYD_DR_TABLE_N;
 extern const FieldDesc SOILTEMP_TABLE[];
 extern const int SOILTEMP_NFIELDS;
 extern const FieldDesc CANOPY_TABLE[];

@@ -101,19 +101,25 @@ static cudaError_t enqueue_step(Batch* b) {
     // order 0 (SoilWater first), after it (and SoilFluxes) otherwise
     const int ord = b->cfg.soilfluxes ? 2 : b->cfg.order;
     const bool mf = b->swm.soilwater_movement_method == 1;
+    // with the hydrology, the Zeng-Decker form also leaves the fused kernel
     const HydroStepArgs* hy = b->cfg.hydrology ? &b->hya : nullptr;
-    if (mf && ord == 0) {
-        e = launch_mf_step(b->dsw, ncol, b->mfa, b->swm.use_flexibleCN, 0, b->err, nullptr, b->stream, hy);
+    const bool own = mf || hy;
+    auto water_step = [&](int refresh) {
+        if (mf) return launch_mf_step(b->dsw, ncol, b->mfa, b->swm.use_flexibleCN, refresh, b->err, nullptr, b->stream, hy);
+        return launch_zd09_step(b->dsw, ncol, b->cfg.e_ice, b->cfg.dtime, b->swm.use_flexibleCN, refresh, nullptr,
+                                b->stream, hy);
+    };
+    if (own && ord == 0) {
+        e = water_step(0);
         if (e != cudaSuccess) return e;
     }
     SoilStepFlags fl;
-    fl.water = mf ? 0 : 1;
+    fl.water = own ? 0 : 1;
     fl.flexcn = b->swm.use_flexibleCN;
-    fl.refresh = (mf && ord >= 1) ? 0 : 1;
+    fl.refresh = (own && ord >= 1) ? 0 : 1;
     e = launch_soilstep(b->dsw, b->dst, ncol, b->cfg.e_ice, b->cfg.dtime, b->cfg.snow_thermal_cond_method, b->ws,
                         ncol, b->err, b->stream, b->block, ord, nullptr, b->cfg.soilfluxes ? &b->dsf : nullptr, fl);
-    if (e == cudaSuccess && mf && ord >= 1)
-        e = launch_mf_step(b->dsw, ncol, b->mfa, b->swm.use_flexibleCN, 1, b->err, nullptr, b->stream, hy);
+    if (e == cudaSuccess && own && ord >= 1) e = water_step(1);
     if (e != cudaSuccess || !b->cfg.balance) return e;
     return launch_balance(b->dsw, b->dst, ncol, b->cfg.dtime, b->bal, b->stream);
 }
@@ -144,6 +150,15 @@ static void batch_free(Batch* b) {
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
+}
+
+// A device io struct starts as the caller's leading dimensions with every
+// component pointer NULL; the tables of the step then fill in the device
+// copies of exactly the components the step's kernels use.
+template <class T>
+static void dev_io(T& d, const T* h, size_t header_bytes) {
+    std::memset(&d, 0, sizeof d);
+    std::memcpy(&d, h, header_bytes);
 }
 
 static bool is_column_kind(int k) { return !(k == K_P || k == K_PL || k == K_PS || k == K_PG || k == K_GR); }
@@ -220,8 +235,8 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
         }
     }
     if (!canopy_only && swm.use_flexibleCN && !sw->wa) return set_error(CTSMG_E_ARG, "use_flexibleCN needs wa", 0, 0);
-    if (cfg->hydrology && (canopy_only || swm.soilwater_movement_method != 1 || !hy || hy->ldc != ncol))
-        return set_error(CTSMG_E_ARG, "hydrology needs the moisture form, the soil step and dense hydrology arrays", 0, 0);
+    if (cfg->hydrology && (canopy_only || !hy || hy->ldc != ncol))
+        return set_error(CTSMG_E_ARG, "hydrology needs the soil step and dense hydrology arrays", 0, 0);
     if (cfg->hydrology && cfg->balance)
         return set_error(CTSMG_E_UNSUPPORTED, "the balance check does not count the lateral and surface fluxes of the "
                          "hydrology routines", 0, 0);
@@ -301,8 +316,8 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
     };
     int rc;
     if (!canopy_only) {
-        std::memcpy(&b->dsw, sw, sizeof b->dsw);
-        std::memcpy(&b->dst, st, sizeof b->dst);
+        dev_io(b->dsw, sw, sizeof(int32_t));
+        dev_io(b->dst, st, 2 * sizeof(int32_t));
         if ((rc = add(SOILWATER_TABLE, SOILWATER_NFIELDS, sw, &b->dsw))) return fail(rc);
         if ((rc = add(SOILTEMP_TABLE, SOILTEMP_NFIELDS, st, &b->dst))) return fail(rc);
         if (swm.soilwater_movement_method == 1) {
@@ -312,13 +327,19 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
         if (swm.use_flexibleCN && (rc = add(SOILWATER_FLEXCN_TABLE, SOILWATER_FLEXCN_NFIELDS, sw, &b->dsw)))
             return fail(rc);
         if (cfg->hydrology) {
-            std::memcpy(&b->hya.io, hy, sizeof b->hya.io);
-            const FieldDesc* tabs[6] = {HYD_SAT_TABLE, HYD_INF_TABLE, HYD_PWT_TABLE, HYD_TWT_TABLE, HYD_PLF_TABLE,
-                                        HYD_SLF_TABLE};
-            const int ns[6] = {HYD_SAT_TABLE_N, HYD_INF_TABLE_N, HYD_PWT_TABLE_N, HYD_TWT_TABLE_N, HYD_PLF_TABLE_N,
-                               HYD_SLF_TABLE_N};
-            for (int k = 0; k < 6; ++k)
+            dev_io(b->hya.io, hy, sizeof(int32_t));
+            const bool aq = swm.soilwater_movement_method == 0;     // aquifer-layer path
+            const FieldDesc* tabs[6] = {HYD_SAT_TABLE, HYD_INF_TABLE, aq ? HYD_WT_TABLE : HYD_PWT_TABLE,
+                                        aq ? HYD_DR_TABLE : HYD_TWT_TABLE, HYD_PLF_TABLE, HYD_SLF_TABLE};
+            const int ns[6] = {HYD_SAT_TABLE_N, HYD_INF_TABLE_N, aq ? HYD_WT_TABLE_N : HYD_PWT_TABLE_N,
+                               aq ? HYD_DR_TABLE_N : HYD_TWT_TABLE_N, HYD_PLF_TABLE_N, HYD_SLF_TABLE_N};
+            for (int k = 0; k < (aq ? 4 : 6); ++k)
                 if ((rc = add(tabs[k], ns[k], hy, &b->hya.io))) return fail(rc);
+            if (aq) {       // SetSoilWaterFractions runs in the step and writes eff_porosity
+                static const FieldDesc EFFPOR[] = {
+                    {offsetof(ctsmg_soilwater_io, eff_porosity), K_G, 8, U_OUT, "eff_porosity"}};
+                if ((rc = add(EFFPOR, 1, sw, &b->dsw))) return fail(rc);
+            }
             b->hya.par = current_soilhydrology_params();
             const double* hc[2] = {in->baseflow_scalar_c, in->fff_c};
             if (hc[0] || hc[1]) {
@@ -340,7 +361,7 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
         }
     }
     if (cfg->with_canopy) {
-        std::memcpy(&b->cargs.io, cio, sizeof b->cargs.io);
+        dev_io(b->cargs.io, cio, 4 * sizeof(int32_t));
         if ((rc = add(CANOPY_TABLE, CANOPY_NFIELDS, cio, &b->cargs.io))) return fail(rc);
         b->cargs.par = *cpar;
         b->cargs.pft = *pft;
@@ -351,12 +372,12 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
         b->cargs.engine = 1;
         const size_t pb = (size_t)npatch * 8;
         if (cfg->soilresis) {
-            std::memcpy(&b->dsr, sr, sizeof b->dsr);
+            dev_io(b->dsr, sr, sizeof(int32_t));
             if ((rc = add(SOILRESIS_SL14_TABLE, SOILRESIS_SL14_NFIELDS, sr, &b->dsr))) return fail(rc);
             b->sra = SoilResisArgs{1, sres.d_max, sres.frac_sat_soil_dsl_init};
         }
         if (cfg->rootmoist) {
-            std::memcpy(&b->drm, rm, sizeof b->drm);
+            dev_io(b->drm, rm, 2 * sizeof(int32_t));
             if ((rc = add(ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, rm, &b->drm))) return fail(rc);
         } else if (!canopy_only) {
             if ((e = cudaMalloc(&b->rootr, pb * NLEVSOI)) != cudaSuccess) return fail(cuda_err(e, "rootr"));
@@ -374,7 +395,7 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
         b->cargs.medlynslope_p = b->mslope;
         b->cargs.medlynintercept_p = b->mint;
         if (cfg->soilfluxes) {
-            std::memcpy(&b->dsf, sf, sizeof b->dsf);
+            dev_io(b->dsf, sf, 2 * sizeof(int32_t));
             if ((rc = add(SOILFLUXES_TABLE, SOILFLUXES_NFIELDS, sf, &b->dsf))) return fail(rc);
         }
         if ((e = cudaMalloc(&b->counter, 256)) != cudaSuccess) return fail(cuda_err(e, "counter"));
@@ -513,11 +534,12 @@ extern "C" int32_t ctsmg_batch_fetch(ctsmg_batch bh, const ctsmg_batch_inputs* i
         (rc = download_table(bh->b, SOILRESIS_SL14_TABLE, SOILRESIS_SL14_NFIELDS, in->sr)))
         return rc;
     if (in->hy && bh->b->cfg.hydrology) {
-        const FieldDesc* tabs[6] = {HYD_SAT_TABLE, HYD_INF_TABLE, HYD_PWT_TABLE, HYD_TWT_TABLE, HYD_PLF_TABLE,
-                                    HYD_SLF_TABLE};
-        const int ns[6] = {HYD_SAT_TABLE_N, HYD_INF_TABLE_N, HYD_PWT_TABLE_N, HYD_TWT_TABLE_N, HYD_PLF_TABLE_N,
-                           HYD_SLF_TABLE_N};
-        for (int k = 0; k < 6; ++k)
+        const bool aq = bh->b->swm.soilwater_movement_method == 0;
+        const FieldDesc* tabs[6] = {HYD_SAT_TABLE, HYD_INF_TABLE, aq ? HYD_WT_TABLE : HYD_PWT_TABLE,
+                                    aq ? HYD_DR_TABLE : HYD_TWT_TABLE, HYD_PLF_TABLE, HYD_SLF_TABLE};
+        const int ns[6] = {HYD_SAT_TABLE_N, HYD_INF_TABLE_N, aq ? HYD_WT_TABLE_N : HYD_PWT_TABLE_N,
+                           aq ? HYD_DR_TABLE_N : HYD_TWT_TABLE_N, HYD_PLF_TABLE_N, HYD_SLF_TABLE_N};
+        for (int k = 0; k < (aq ? 4 : 6); ++k)
             if ((rc = download_table(bh->b, tabs[k], ns[k], in->hy))) return rc;
     }
     return 0;

@@ -16,6 +16,7 @@ namespace hydro {
 constexpr double WATMIN = 0.01;          // clm_varcon.F90:81
 constexpr double PONDMX = 0.0;           // clm_varcon.F90:116
 constexpr double RPI = 3.14159265358979323846;
+constexpr double AQUIFER_WATER_BASELINE = 5000.0;   // clm_varcon.F90:124
 
 struct View {
     const ctsmg_hydrology_io& io;
@@ -347,6 +348,255 @@ __device__ __forceinline__ void subsurface_lateral_flow(const ctsmg_hydrology_io
     io.zwt[c] = zwt;
     io.qflx_rsub_sat[c] = rsub_sat;
     io.qflx_drain[c] = rsub_sat + drainage;
+    io.qflx_qrgwl[c] = io.qflx_snwcp_liq[c];
+}
+
+__device__ __forceinline__ int water_table_index(const View& v, double zwt) {
+    int jwt = NLEVSOI;
+#pragma unroll 1
+    for (int j = 1; j <= NLEVSOI; ++j)
+        if (zwt <= v.zi(j)) { jwt = j - 1; break; }
+    return jwt;
+}
+
+// The perched water table of the aquifer-layer path (frost table at the
+// node depth z(k_frz), SoilHydrologyMod.F90:782-856 and 932-995); returns
+// k_frz and k_perch, and whether the water table is above the frost table.
+struct Perch { int k_frz, k_perch; bool wt_above; };
+__device__ __forceinline__ Perch aquifer_perched(const ctsmg_hydrology_io& io, const View& v, int c, bool write_vol) {
+    const double sat_lev = (double)0.9f;
+    Perch r{};
+    r.k_frz = (io.t_soisno[v.ss(1)] > TFRZ) ? NLEVSOI : 1;
+#pragma unroll 1
+    for (int k = 2; k <= NLEVSOI; ++k)
+        if (io.t_soisno[v.ss(k - 1)] > TFRZ && io.t_soisno[v.ss(k)] <= TFRZ) { r.k_frz = k; break; }
+    const double ft = io.z[v.ss(r.k_frz)];
+    io.frost_table[c] = ft;
+    io.zwt_perched[c] = ft;
+    r.wt_above = io.zwt[c] < ft && io.t_soisno[v.ss(r.k_frz)] <= TFRZ;
+    r.k_perch = 1;
+    if (r.wt_above) return r;
+#pragma unroll 1
+    for (int k = r.k_frz; k >= 1; --k) {
+        const double hv = v.vol(k);
+        if (write_vol) io.h2osoi_vol[v.g(k)] = hv;
+        if (hv / io.watsat[v.g(k)] <= sat_lev) { r.k_perch = k; break; }
+    }
+    if (io.t_soisno[v.ss(r.k_frz)] > TFRZ) r.k_perch = r.k_frz;
+    if (r.k_frz > r.k_perch) {
+        const double s1 = v.vol(r.k_perch) / io.watsat[v.g(r.k_perch)];
+        const double s2 = v.vol(r.k_perch + 1) / io.watsat[v.g(r.k_perch + 1)];
+        const double m = (io.z[v.ss(r.k_perch + 1)] - io.z[v.ss(r.k_perch)]) / (s2 - s1);
+        const double b = io.z[v.ss(r.k_perch + 1)] - m * s2;
+        io.zwt_perched[c] = mx(0.0, m * sat_lev + b);
+    }
+    return r;
+}
+
+// WaterTable (SoilHydrologyMod.F90:607-861)
+__device__ __forceinline__ void water_table(const ctsmg_hydrology_io& io, int c, const ctsmg_soilhydrology_params& P,
+                                            double dtime) {
+    const View v{io, c, io.ldc};
+    io.qflx_drain[c] = 0.0;
+    io.qflx_rsub_sat[c] = 0.0;
+    io.qflx_drain_perched[c] = 0.0;
+    double zwt = io.zwt[c];
+    const int jwt = water_table_index(v, zwt);
+    double rous = specific_yield(io, v, NLEVSOI, zwt, P.aq_sp_yield_min);
+    const double qcharge = io.qcharge[c];
+    if (jwt == NLEVSOI) {
+        io.wa[c] = io.wa[c] + qcharge * dtime;
+        zwt = zwt - (qcharge * dtime) / 1000.0 / rous;
+    } else {
+        double tot = qcharge * dtime;
+        if (tot > 0.0) {                                  // rising water table
+#pragma unroll 1
+            for (int j = jwt + 1; j >= 1; --j) {
+                const double s_y = specific_yield(io, v, j, zwt, P.aq_sp_yield_min);
+                double layer = mn(tot, (s_y * (zwt - v.zi(j - 1)) * 1.e3));
+                layer = mx(layer, 0.0);
+                if (s_y > 0.0) zwt = zwt - layer / s_y / 1000.0;
+                tot = tot - layer;
+                if (tot <= 0.0) break;
+            }
+        } else {                                          // deepening water table
+#pragma unroll 1
+            for (int j = jwt + 1; j <= NLEVSOI; ++j) {
+                const double s_y = specific_yield(io, v, j, zwt, P.aq_sp_yield_min);
+                double layer = mx(tot, -(s_y * (v.zi(j) - zwt) * 1.e3));
+                layer = mn(layer, 0.0);
+                tot = tot - layer;
+                if (tot >= 0.0) { zwt = zwt - layer / s_y / 1000.0; break; }
+                zwt = v.zi(j);
+            }
+            if (tot > 0.0) zwt = zwt - tot / 1000.0 / rous;
+        }
+    }
+    io.zwt[c] = zwt;
+    aquifer_perched(io, v, c, true);
+}
+
+// Drainage (SoilHydrologyMod.F90:864-1410), non-VIC natural soil columns
+__device__ __forceinline__ void drainage(const ctsmg_hydrology_io& io, int c, const ctsmg_soilhydrology_params& P,
+                                         double dtime) {
+    const View v{io, c, io.ldc};
+    double* liq = io.h2osoi_liq;
+    double* ice = io.h2osoi_ice;
+#pragma unroll 1
+    for (int j = 1; j <= NLEVSOI; ++j) {
+        const double ws = io.watsat[v.g(j)];
+        const double vol_ice = mn(ws, ice[v.ss(j)] / (io.dz[v.ss(j)] * DENICE));
+        io.icefrac[v.g(j)] = mn(1.0, vol_ice / ws);
+    }
+    double rsub_sat = 0.0, rsub_top = 0.0;
+    double zwt = io.zwt[c];
+    int jwt = water_table_index(v, zwt);
+    const double q_perch_max = P.perched_baseflow_scalar * sin(io.topo_slope[c] * (RPI / 180.0));
+    const Perch pr = aquifer_perched(io, v, c, false);
+    const double ft = io.frost_table[c];
+    double drain_perched = 0.0;
+    auto imped_k = [&](int k) {
+        const int k1 = (NLEVSOI < k + 1) ? NLEVSOI : k + 1;
+        return pow10_dd(-P.e_ice * (0.5 * (io.icefrac[v.g(k)] + io.icefrac[v.g(k1)])));
+    };
+    if (pr.wt_above) {
+        double wtsub = 0.0, q_perch = 0.0;
+#pragma unroll 1
+        for (int k = jwt + 1; k <= pr.k_frz; ++k) {
+            const double dzmm = io.dz[v.ss(k)] * 1.e3;
+            q_perch = q_perch + imped_k(k) * io.hksat[v.g(k)] * dzmm;
+            wtsub = wtsub + dzmm;
+        }
+        if (wtsub > 0.0) q_perch = q_perch / wtsub;
+        drain_perched = q_perch_max * q_perch * (ft - zwt);
+        double tot = -drain_perched * dtime;
+#pragma unroll 1
+        for (int k = jwt + 1; k <= pr.k_frz; ++k) {
+            double layer = mx(tot, -(liq[v.ss(k)] - WATMIN));
+            layer = mn(layer, 0.0);
+            tot = tot - layer;
+            liq[v.ss(k)] = liq[v.ss(k)] + layer;
+            if (tot >= 0.0) { zwt = zwt - layer / io.eff_porosity[v.g(k)] / 1000.0; break; }
+            zwt = v.zi(k);
+        }
+        drain_perched = drain_perched + tot / dtime;
+        jwt = water_table_index(v, zwt);
+    } else {
+        if (pr.k_frz > pr.k_perch) {
+            double wtsub = 0.0, q_perch = 0.0;
+#pragma unroll 1
+            for (int k = pr.k_perch; k <= pr.k_frz; ++k) {
+                const double dzmm = io.dz[v.ss(k)] * 1.e3;
+                q_perch = q_perch + imped_k(k) * io.hksat[v.g(k)] * dzmm;
+                wtsub = wtsub + dzmm;
+            }
+            if (wtsub > 0.0) q_perch = q_perch / wtsub;
+            double zp = io.zwt_perched[c];
+            drain_perched = q_perch_max * q_perch * (ft - zp);
+            double tot = -drain_perched * dtime;
+#pragma unroll 1
+            for (int k = pr.k_perch + 1; k <= pr.k_frz; ++k) {
+                double layer = mx(tot, -(liq[v.ss(k)] - WATMIN));
+                layer = mn(layer, 0.0);
+                tot = tot - layer;
+                liq[v.ss(k)] = liq[v.ss(k)] + layer;
+                if (tot >= 0.0) { zp = zp - layer / io.eff_porosity[v.g(k)] / 1000.0; break; }
+                zp = v.zi(k);
+            }
+            io.zwt_perched[c] = zp;
+            drain_perched = drain_perched + tot / dtime;
+        } else {
+            drain_perched = 0.0;
+        }
+        const double fff = 1.0 / io.hkdepth[c];
+        double dzsum = 0.0, icefracsum = 0.0;
+#pragma unroll 1
+        for (int j = (jwt > 1 ? jwt : 1); j <= NLEVSOI; ++j) {
+            const double dzmm = io.dz[v.ss(j)] * 1.e3;
+            dzsum = dzsum + dzmm;
+            icefracsum = icefracsum + io.icefrac[v.g(j)] * dzmm;
+        }
+        const double imped = pow10_dd(-P.e_ice * (icefracsum / dzsum));
+        const double rsub_top_max = 10.0 * sin((RPI / 180.0) * io.topo_slope[c]);
+        rsub_top = imped * rsub_top_max * exp(-fff * zwt);
+        const double rous = specific_yield(io, v, NLEVSOI, zwt, P.aq_sp_yield_min);
+        if (jwt == NLEVSOI) {
+            double wa = io.wa[c] - rsub_top * dtime;
+            zwt = zwt + (rsub_top * dtime) / 1000.0 / rous;
+            liq[v.ss(NLEVSOI)] = liq[v.ss(NLEVSOI)] + mx(0.0, (wa - AQUIFER_WATER_BASELINE));
+            io.wa[c] = mn(wa, AQUIFER_WATER_BASELINE);
+        } else {
+            double tot = -rsub_top * dtime;
+            // tot > 0 cannot happen here (rsub_top >= 0); the reference stops the run on it
+#pragma unroll 1
+            for (int j = jwt + 1; j <= NLEVSOI; ++j) {
+                const double s_y = specific_yield(io, v, j, zwt, P.aq_sp_yield_min);
+                double layer = mx(tot, -(s_y * (v.zi(j) - zwt) * 1.e3));
+                layer = mn(layer, 0.0);
+                liq[v.ss(j)] = liq[v.ss(j)] + layer;
+                tot = tot - layer;
+                if (tot >= 0.0) { zwt = zwt - layer / s_y / 1000.0; break; }
+                zwt = v.zi(j);
+            }
+            zwt = zwt - tot / 1000.0 / rous;
+            io.wa[c] = io.wa[c] + tot;
+            jwt = water_table_index(v, zwt);
+        }
+        zwt = mx(0.0, zwt);
+        zwt = mn(80.0, zwt);
+    }
+    io.qflx_drain_perched[c] = drain_perched;
+    // excess above saturation moves up; the top layer's goes to h2osfc
+#pragma unroll 1
+    for (int j = NLEVSOI; j >= 2; --j) {
+        const double cap = io.eff_porosity[v.g(j)] * (io.dz[v.ss(j)] * 1.e3);
+        const double xsi = mx(liq[v.ss(j)] - cap, 0.0);
+        liq[v.ss(j)] = mn(cap, liq[v.ss(j)]);
+        liq[v.ss(j - 1)] = liq[v.ss(j - 1)] + xsi;
+    }
+    const double dz1mm = io.dz[v.ss(1)] * 1.e3, ws1 = io.watsat[v.g(1)];
+    double xs1 = mx(mx(liq[v.ss(1)] - WATMIN, 0.0) - mx(0.0, (PONDMX + ws1 * dz1mm - ice[v.ss(1)] - WATMIN)), 0.0);
+    liq[v.ss(1)] = liq[v.ss(1)] - xs1;
+    if (P.h2osfcflag == 1) { io.h2osfc[c] = io.h2osfc[c] + xs1; rsub_sat = 0.0; }
+    else rsub_sat = xs1 / dtime;
+    xs1 = mx(mx(ice[v.ss(1)], 0.0) - mx(0.0, (PONDMX + ws1 * dz1mm - liq[v.ss(1)])), 0.0);
+    ice[v.ss(1)] = mn(mx(0.0, PONDMX + ws1 * dz1mm - liq[v.ss(1)]), ice[v.ss(1)]);
+    io.qflx_ice_runoff_xs[c] = xs1 / dtime;
+#pragma unroll 1
+    for (int j = 1; j <= NLEVSOI - 1; ++j) {
+        double xs = 0.0;
+        if (liq[v.ss(j)] < WATMIN) {
+            xs = WATMIN - liq[v.ss(j)];
+            if (j == jwt) zwt = zwt + xs / io.eff_porosity[v.g(j)] / 1000.0;
+        }
+        liq[v.ss(j)] = liq[v.ss(j)] + xs;
+        liq[v.ss(j + 1)] = liq[v.ss(j + 1)] - xs;
+    }
+    {
+        const int j = NLEVSOI;
+        double xs = 0.0;
+        if (liq[v.ss(j)] < WATMIN) {
+            xs = WATMIN - liq[v.ss(j)];
+#pragma unroll 1
+            for (int i = NLEVSOI - 1; i >= 1; --i) {
+                const double avail = mx(liq[v.ss(i)] - WATMIN - xs, 0.0);
+                if (avail >= xs) {
+                    liq[v.ss(j)] = liq[v.ss(j)] + xs;
+                    liq[v.ss(i)] = liq[v.ss(i)] - xs;
+                    xs = 0.0;
+                    break;
+                }
+                liq[v.ss(j)] = liq[v.ss(j)] + avail;
+                liq[v.ss(i)] = liq[v.ss(i)] - avail;
+                xs = xs - avail;
+            }
+        }
+        liq[v.ss(j)] = liq[v.ss(j)] + xs;
+        rsub_top = rsub_top - xs / dtime;
+    }
+    io.zwt[c] = zwt;
+    io.qflx_rsub_sat[c] = rsub_sat;
+    io.qflx_drain[c] = rsub_sat + rsub_top;
     io.qflx_qrgwl[c] = io.qflx_snwcp_liq[c];
 }
 

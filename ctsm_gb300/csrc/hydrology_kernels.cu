@@ -20,6 +20,8 @@ hydrology_kernel(ctsmg_hydrology_io io, int begc, int n, const int32_t* __restri
         case HYD_THETA_WT: hydro::theta_based_water_table(io, c); break;
         case HYD_PERCHED_LAT: hydro::perched_lateral_flow(io, c, P, dtime); break;
         case HYD_INFIL: hydro::infiltration_chain(io, c, P, dtime); break;
+        case HYD_WATER_TABLE: hydro::water_table(io, c, P, dtime); break;
+        case HYD_DRAINAGE: hydro::drainage(io, c, P, dtime); break;
         default: hydro::subsurface_lateral_flow(io, c, P, dtime); break;
     }
 }

@@ -19,6 +19,8 @@
 #include "soil_kernels.cuh"
 #include "soil_math.cuh"
 #include "moisture_form_device.cuh"
+#include "moisture_form_kernels.cuh"
+#include "hydrology_device.cuh"
 #include "soilfluxes_device.cuh"
 #include "capi_internal.h"
 
@@ -865,6 +867,47 @@ soilstep_kernel(ctsmg_soilwater_io wio, ctsmg_soiltemp_io tio, ctsmg_soilfluxes_
         if (fl.flexcn) flexcn_column(wio, c);
     }
     if (fl.refresh) refresh_h2osoi_vol(wio, c);
+}
+
+// The Zeng-Decker SoilWater of a resident step in its own kernel, with the
+// aquifer-layer hydrology around it when HYDRO: SetSoilWaterFractions,
+// SaturatedExcessRunoff and the infiltration chain before SoilWater,
+// WaterTable and Drainage after it (HydrologyNoDrainageMod.F90:302-359,
+// HydrologyDrainageMod.F90:132-137), the flexibleCN fix and, if refresh, the
+// h2osoi_vol refresh.
+template <bool HYDRO>
+__global__ void __launch_bounds__(128)
+zd09_step_kernel(ctsmg_soilwater_io io, int ncol, double e_ice, double dtime, int flexcn, int refresh,
+                 const int32_t* __restrict__ filt, HydroStepArgs hy) {
+    const int fc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fc >= ncol) return;
+    const int c = filt ? filt[fc] - 1 : fc;
+    ctsmg_soilhydrology_params hp = hy.par;
+    if (HYDRO) {
+        if (hy.baseflow_scalar_c) hp.baseflow_scalar = hy.baseflow_scalar_c[c];
+        if (hy.fff_c) hp.fff = hy.fff_c[c];
+        set_soil_water_fractions(io, c);
+        hydro::saturated_excess_runoff(hy.io, c, hp.fff);
+        hydro::infiltration_chain(hy.io, c, hp, dtime);
+    }
+    zd09_column(io, c, e_ice, dtime);
+    if (flexcn) flexcn_column(io, c);
+    if (HYDRO) {
+        hydro::water_table(hy.io, c, hp, dtime);
+        hydro::drainage(hy.io, c, hp, dtime);
+    }
+    if (refresh) refresh_h2osoi_vol(io, c);
+}
+
+cudaError_t launch_zd09_step(const ctsmg_soilwater_io& io, int ncol, double e_ice, double dtime, int flexcn,
+                             int refresh, const int32_t* d_filt, cudaStream_t s, const HydroStepArgs* hy) {
+    if (ncol <= 0) return cudaSuccess;
+    if (hy)
+        zd09_step_kernel<true><<<(ncol + 127) / 128, 128, 0, s>>>(io, ncol, e_ice, dtime, flexcn, refresh, d_filt, *hy);
+    else
+        zd09_step_kernel<false><<<(ncol + 127) / 128, 128, 0, s>>>(io, ncol, e_ice, dtime, flexcn, refresh, d_filt,
+                                                                  HydroStepArgs{});
+    return cudaGetLastError();
 }
 
 // Compute_EffecRootFrac_And_VertTranSink_Default

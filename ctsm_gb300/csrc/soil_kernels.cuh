@@ -23,6 +23,11 @@ cudaError_t launch_soilstep(const ctsmg_soilwater_io& wio, const ctsmg_soiltemp_
                             DevError* err, cudaStream_t s, int block, int order = 0,
                             const int32_t* filt = nullptr, const ctsmg_soilfluxes_io* sf = nullptr,
                             SoilStepFlags fl = SoilStepFlags());
+struct HydroStepArgs;
+// The Zeng-Decker SoilWater of a resident step in its own kernel (with the
+// aquifer-layer hydrology when hy is given).
+cudaError_t launch_zd09_step(const ctsmg_soilwater_io& io, int ncol, double e_ice, double dtime, int flexcn,
+                             int refresh, const int32_t* d_filt, cudaStream_t s, const HydroStepArgs* hy);
 cudaError_t launch_rootsink(const int32_t* col_patchi, const int32_t* col_npatches, const double* wtcol,
                             const double* qflx_tran_veg, const double* rootr, int ldp, double* qflx_rootsoi,
                             int ncol, cudaStream_t s, int ldc = 0, const int32_t* filt = nullptr);

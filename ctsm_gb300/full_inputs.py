@@ -237,6 +237,9 @@ def add_hydrology_fields(A, rng=None):
     A["qflx_ev_h2osfc_col"] = r.uniform(0.0, 2e-5, ncol)
     A["frac_h2osfc_nosnow"] = np.clip(A["frac_h2osfc"] * 1.2, 0.0, 1.0) if "frac_h2osfc" in A else np.zeros(ncol)
     A["h2osfc_thresh"] = r.uniform(5.0, 30.0, ncol)
+    A["hkdepth"] = 1.0 / r.uniform(1.0, 5.0, ncol)         # 1/fff of the aquifer path (m)
+    if "wa" not in A:
+        A["wa"] = np.full(ncol, 5000.0)
     A["zwt_perched"] = A["zwt"].copy()
     A["frost_table"] = A["zwt"].copy()
     if "h2osfc" not in A:

@@ -94,10 +94,12 @@ def calc_soilevap_resis(bounds, num_nolakec, filter_nolakec, state):
     check(L.ctsmg_soilevap_resis(C.byref(bounds), int(num_nolakec), fp, C.byref(io)))
 
 
-HYDROLOGY_ROUTINES = ("SaturatedExcessRunoff", "InfiltrationChain", "PerchedWaterTable", "ThetaBasedWaterTable", "PerchedLateralFlow",
+HYDROLOGY_ROUTINES = ("WaterTable", "Drainage", "SaturatedExcessRunoff", "InfiltrationChain", "PerchedWaterTable", "ThetaBasedWaterTable", "PerchedLateralFlow",
                       "SubsurfaceLateralFlow")
 _HYD_ENTRY = {"SaturatedExcessRunoff": "ctsmg_saturated_excess_runoff",
               "InfiltrationChain": "ctsmg_infiltration_chain",
+              "WaterTable": "ctsmg_water_table",
+              "Drainage": "ctsmg_drainage",
               "PerchedWaterTable": "ctsmg_perched_water_table",
               "ThetaBasedWaterTable": "ctsmg_theta_based_water_table",
               "PerchedLateralFlow": "ctsmg_perched_lateral_flow",
@@ -124,7 +126,7 @@ def hydrology(routine, bounds, num_hydrologyc, filter_hydrologyc, state, dtime=N
     name = _HYD_ENTRY[routine]
     fn = getattr(L, name)
     args = [C.POINTER(abi.Bounds), C.c_int32, C.POINTER(C.c_int32), C.POINTER(abi.HydrologyIO)]
-    lateral = routine in ("PerchedLateralFlow", "SubsurfaceLateralFlow", "InfiltrationChain")
+    lateral = routine not in ("SaturatedExcessRunoff", "PerchedWaterTable", "ThetaBasedWaterTable")
     fn.argtypes = args + ([C.c_double] if lateral else [])
     f, fp = _filter(filter_hydrologyc)
     ncol = bounds.endc - bounds.begc + 1

@@ -484,6 +484,10 @@ typedef struct {
     double* qflx_h2osfc_surf;         /* (c)  out                                   */
     double* qflx_h2osfc_drain;        /* (c)  out                                   */
     double* qflx_infl;                /* (c)  out: infiltration, SoilWater's input  */
+    /* the aquifer-layer path (WaterTable, Drainage; SoilWater's ZD09 form)  */
+    double* wa;                       /* (c)  inout: aquifer water (mm)             */
+    const double* qcharge;            /* (c)  aquifer recharge from SoilWater (mm/s)*/
+    const double* hkdepth;            /* (c)  decay factor depth (m)                */
 } ctsmg_hydrology_io;
 
 /* readParams of SoilHydrologyMod and SaturatedExcessRunoffMod. */
@@ -496,6 +500,14 @@ int32_t ctsmg_set_soilhydrology_params(const ctsmg_soilhydrology_params* p);
  * SaturatedExcessRunoff.                                                  */
 int32_t ctsmg_infiltration_chain(const ctsmg_bounds* bounds, int32_t num_hydrologyc,
                                  const int32_t* filter_hydrologyc, const ctsmg_hydrology_io* io, double dtime);
+/* The aquifer-layer path that follows the Zeng-Decker SoilWater
+ * (use_aquifer_layer, HydrologyNoDrainageMod.F90:356-359,
+ * HydrologyDrainageMod.F90:132-137): WaterTable (SoilHydrologyMod.F90:607-861)
+ * and Drainage (:864-1410, the non-VIC branch).                          */
+int32_t ctsmg_water_table(const ctsmg_bounds* bounds, int32_t num_hydrologyc, const int32_t* filter_hydrologyc,
+                          const ctsmg_hydrology_io* io, double dtime);
+int32_t ctsmg_drainage(const ctsmg_bounds* bounds, int32_t num_hydrologyc, const int32_t* filter_hydrologyc,
+                       const ctsmg_hydrology_io* io, double dtime);
 int32_t ctsmg_saturated_excess_runoff(const ctsmg_bounds* bounds, int32_t num_hydrologyc,
                                       const int32_t* filter_hydrologyc, const ctsmg_hydrology_io* io);
 int32_t ctsmg_perched_water_table(const ctsmg_bounds* bounds, int32_t num_hydrologyc,

@@ -10,6 +10,7 @@
 //   ThetaBasedWaterTable    SoilHydrologyMod.F90:1933-2025
 //   PerchedLateralFlow      SoilHydrologyMod.F90:1645-1929
 //   SubsurfaceLateralFlow   SoilHydrologyMod.F90:2029-2565
+//   WaterTable, Drainage    SoilHydrologyMod.F90:607-1410 (aquifer layer, non-VIC)
 // sat_lev = 0.9 is a default-real literal in the reference, reproduced as
 // (double)0.9f.  Parity unpinned: the reference ships no test of these.
 #include <cmath>
@@ -21,7 +22,7 @@
 
 namespace {
 const double TFRZ = 273.15, DENH2O = 1.000e3, DENICE = 0.917e3;
-const double WATMIN = 0.01, PONDMX = 0.0, RPI = 3.14159265358979323846;
+const double WATMIN = 0.01, PONDMX = 0.0, RPI = 3.14159265358979323846, AQUIFER_WATER_BASELINE = 5000.0;
 const int NLEVSNO = CTSMG_NLEVSNO, NLEVSOI = CTSMG_NLEVSOI, LS = -NLEVSNO + 1;
 using oracle_libm::o_pow;
 using oracle_libm::o_exp;
@@ -43,6 +44,262 @@ struct K {
     double& vol(int j) const { return io->h2osoi_vol[c + (size_t)(j - 1) * ld]; }
     double& icefrac(int j) const { return io->icefrac[c + (size_t)(j - 1) * ld]; }
 };
+int jwt_of(const K& k, double zwt) {
+    int jwt = NLEVSOI;
+    for (int j = 1; j <= NLEVSOI; ++j)
+        if (zwt <= k.zi(j)) { jwt = j - 1; break; }
+    return jwt;
+}
+
+double syield(const K& k, int j, double depth, double aq_min) {
+    double s_y = k.watsat(j) * (1. - o_pow(1. + 1.e3 * depth / k.sucsat(j), -1. / k.bsw(j)));
+    return std::max(s_y, aq_min);
+}
+
+// WaterTable (SoilHydrologyMod.F90:607-861)
+void water_table(const K& k, const ctsmg_hydrology_io* io, const ctsmg_soilhydrology_params* P, double dtime) {
+    const int c = k.c;
+    const double sat_lev_r8 = (double)0.9f;
+    io->qflx_drain[c] = 0.0;
+    io->qflx_rsub_sat[c] = 0.0;
+    io->qflx_drain_perched[c] = 0.0;
+    int jwt = jwt_of(k, io->zwt[c]);
+    const double rous = syield(k, NLEVSOI, io->zwt[c], P->aq_sp_yield_min);
+    if (jwt == NLEVSOI) {
+        io->wa[c] = io->wa[c] + io->qcharge[c] * dtime;
+        io->zwt[c] = io->zwt[c] - (io->qcharge[c] * dtime) / 1000.0 / rous;
+    } else {
+        double qcharge_tot = io->qcharge[c] * dtime;
+        if (qcharge_tot > 0.) {
+            for (int j = jwt + 1; j >= 1; --j) {
+                const double s_y = syield(k, j, io->zwt[c], P->aq_sp_yield_min);
+                double layer = std::min(qcharge_tot, (s_y * (io->zwt[c] - k.zi(j - 1)) * 1.e3));
+                layer = std::max(layer, 0.0);
+                if (s_y > 0.0) io->zwt[c] = io->zwt[c] - layer / s_y / 1000.0;
+                qcharge_tot = qcharge_tot - layer;
+                if (qcharge_tot <= 0.) break;
+            }
+        } else {
+            for (int j = jwt + 1; j <= NLEVSOI; ++j) {
+                const double s_y = syield(k, j, io->zwt[c], P->aq_sp_yield_min);
+                double layer = std::max(qcharge_tot, -(s_y * (k.zi(j) - io->zwt[c]) * 1.e3));
+                layer = std::min(layer, 0.0);
+                qcharge_tot = qcharge_tot - layer;
+                if (qcharge_tot >= 0.) {
+                    io->zwt[c] = io->zwt[c] - layer / s_y / 1000.0;
+                    break;
+                } else {
+                    io->zwt[c] = k.zi(j);
+                }
+            }
+            if (qcharge_tot > 0.) io->zwt[c] = io->zwt[c] - qcharge_tot / 1000.0 / rous;
+        }
+        jwt = jwt_of(k, io->zwt[c]);
+    }
+    int k_frz = (k.t(1) > TFRZ) ? NLEVSOI : 1;
+    for (int kk = 2; kk <= NLEVSOI; ++kk)
+        if (k.t(kk - 1) > TFRZ && k.t(kk) <= TFRZ) { k_frz = kk; break; }
+    io->frost_table[c] = k.z(k_frz);
+    io->zwt_perched[c] = io->frost_table[c];
+    if (io->zwt[c] < io->frost_table[c] && k.t(k_frz) <= TFRZ) {
+    } else {
+        int k_perch = 1;
+        for (int kk = k_frz; kk >= 1; --kk) {
+            k.vol(kk) = k.liq(kk) / (k.dz(kk) * DENH2O) + k.ice(kk) / (k.dz(kk) * DENICE);
+            if (k.vol(kk) / k.watsat(kk) <= sat_lev_r8) { k_perch = kk; break; }
+        }
+        if (k.t(k_frz) > TFRZ) k_perch = k_frz;
+        if (k_frz > k_perch) {
+            const double s1 = (k.liq(k_perch) / (k.dz(k_perch) * DENH2O) + k.ice(k_perch) / (k.dz(k_perch) * DENICE)) /
+                              k.watsat(k_perch);
+            const double s2 = (k.liq(k_perch + 1) / (k.dz(k_perch + 1) * DENH2O) +
+                               k.ice(k_perch + 1) / (k.dz(k_perch + 1) * DENICE)) / k.watsat(k_perch + 1);
+            const double m = (k.z(k_perch + 1) - k.z(k_perch)) / (s2 - s1);
+            const double bb = k.z(k_perch + 1) - m * s2;
+            io->zwt_perched[c] = std::max(0.0, m * sat_lev_r8 + bb);
+        }
+    }
+}
+
+// Drainage (SoilHydrologyMod.F90:864-1410), non-VIC
+void drainage(const K& k, const ctsmg_hydrology_io* io, const ctsmg_soilhydrology_params* P, double dtime) {
+    const int c = k.c;
+    double dzmm[NLEVSOI + 1];
+    for (int j = 1; j <= NLEVSOI; ++j) {
+        dzmm[j] = k.dz(j) * 1.e3;
+        const double vol_ice = std::min(k.watsat(j), k.ice(j) / (k.dz(j) * DENICE));
+        k.icefrac(j) = std::min(1.0, vol_ice / k.watsat(j));
+    }
+    io->qflx_drain[c] = 0.0;
+    io->qflx_rsub_sat[c] = 0.0;
+    double rsub_top = 0.0;
+    int jwt = jwt_of(k, io->zwt[c]);
+    const double q_perch_max = P->perched_baseflow_scalar * std::sin(io->topo_slope[c] * (RPI / 180.0));
+    int k_frz = (k.t(1) > TFRZ) ? NLEVSOI : 1;
+    for (int kk = 2; kk <= NLEVSOI; ++kk)
+        if (k.t(kk - 1) > TFRZ && k.t(kk) <= TFRZ) { k_frz = kk; break; }
+    io->frost_table[c] = k.z(k_frz);
+    io->zwt_perched[c] = io->frost_table[c];
+    io->qflx_drain_perched[c] = 0.0;
+    auto imped_k = [&](int kk) {
+        return o_pow(10.0, -P->e_ice * (0.5 * (k.icefrac(kk) + k.icefrac(std::min(NLEVSOI, kk + 1)))));
+    };
+    if (io->zwt[c] < io->frost_table[c] && k.t(k_frz) <= TFRZ) {
+        double wtsub = 0.0, q_perch = 0.0;
+        for (int kk = jwt + 1; kk <= k_frz; ++kk) {
+            q_perch = q_perch + imped_k(kk) * k.hksat(kk) * dzmm[kk];
+            wtsub = wtsub + dzmm[kk];
+        }
+        if (wtsub > 0.0) q_perch = q_perch / wtsub;
+        io->qflx_drain_perched[c] = q_perch_max * q_perch * (io->frost_table[c] - io->zwt[c]);
+        double tot = -io->qflx_drain_perched[c] * dtime;
+        for (int kk = jwt + 1; kk <= k_frz; ++kk) {
+            double layer = std::max(tot, -(k.liq(kk) - WATMIN));
+            layer = std::min(layer, 0.0);
+            tot = tot - layer;
+            k.liq(kk) = k.liq(kk) + layer;
+            if (tot >= 0.) {
+                io->zwt[c] = io->zwt[c] - layer / k.eff(kk) / 1000.0;
+                break;
+            } else {
+                io->zwt[c] = k.zi(kk);
+            }
+        }
+        io->qflx_drain_perched[c] = io->qflx_drain_perched[c] + tot / dtime;
+        jwt = jwt_of(k, io->zwt[c]);
+    } else {
+        const double sat_lev = (double)0.9f;
+        int k_perch = 1;
+        for (int kk = k_frz; kk >= 1; --kk) {
+            const double h2osoi_vol = k.liq(kk) / (k.dz(kk) * DENH2O) + k.ice(kk) / (k.dz(kk) * DENICE);
+            if (h2osoi_vol / k.watsat(kk) <= sat_lev) { k_perch = kk; break; }
+        }
+        if (k.t(k_frz) > TFRZ) k_perch = k_frz;
+        if (k_frz > k_perch) {
+            const double s1 = (k.liq(k_perch) / (k.dz(k_perch) * DENH2O) + k.ice(k_perch) / (k.dz(k_perch) * DENICE)) /
+                              k.watsat(k_perch);
+            const double s2 = (k.liq(k_perch + 1) / (k.dz(k_perch + 1) * DENH2O) +
+                               k.ice(k_perch + 1) / (k.dz(k_perch + 1) * DENICE)) / k.watsat(k_perch + 1);
+            const double m = (k.z(k_perch + 1) - k.z(k_perch)) / (s2 - s1);
+            const double bb = k.z(k_perch + 1) - m * s2;
+            io->zwt_perched[c] = std::max(0.0, m * sat_lev + bb);
+            double wtsub = 0.0, q_perch = 0.0;
+            for (int kk = k_perch; kk <= k_frz; ++kk) {
+                q_perch = q_perch + imped_k(kk) * k.hksat(kk) * dzmm[kk];
+                wtsub = wtsub + dzmm[kk];
+            }
+            if (wtsub > 0.0) q_perch = q_perch / wtsub;
+            io->qflx_drain_perched[c] = q_perch_max * q_perch * (io->frost_table[c] - io->zwt_perched[c]);
+            double tot = -io->qflx_drain_perched[c] * dtime;
+            for (int kk = k_perch + 1; kk <= k_frz; ++kk) {
+                double layer = std::max(tot, -(k.liq(kk) - WATMIN));
+                layer = std::min(layer, 0.0);
+                tot = tot - layer;
+                k.liq(kk) = k.liq(kk) + layer;
+                if (tot >= 0.) {
+                    io->zwt_perched[c] = io->zwt_perched[c] - layer / k.eff(kk) / 1000.0;
+                    break;
+                } else {
+                    io->zwt_perched[c] = k.zi(kk);
+                }
+            }
+            io->qflx_drain_perched[c] = io->qflx_drain_perched[c] + tot / dtime;
+        } else {
+            io->qflx_drain_perched[c] = 0.0;
+        }
+        const double fff = 1.0 / io->hkdepth[c];
+        double dzsum = 0.0, icefracsum = 0.0;
+        for (int j = std::max(jwt, 1); j <= NLEVSOI; ++j) {
+            dzsum = dzsum + dzmm[j];
+            icefracsum = icefracsum + k.icefrac(j) * dzmm[j];
+        }
+        const double imped = o_pow(10.0, -P->e_ice * (icefracsum / dzsum));
+        const double rsub_top_max = 10.0 * std::sin((RPI / (double)180.f) * io->topo_slope[c]);
+        rsub_top = imped * rsub_top_max * o_exp(-fff * io->zwt[c]);
+        const double rous = syield(k, NLEVSOI, io->zwt[c], P->aq_sp_yield_min);
+        if (jwt == NLEVSOI) {
+            io->wa[c] = io->wa[c] - rsub_top * dtime;
+            io->zwt[c] = io->zwt[c] + (rsub_top * dtime) / 1000.0 / rous;
+            k.liq(NLEVSOI) = k.liq(NLEVSOI) + std::max(0.0, (io->wa[c] - AQUIFER_WATER_BASELINE));
+            io->wa[c] = std::min(io->wa[c], AQUIFER_WATER_BASELINE);
+        } else {
+            double tot = -rsub_top * dtime;
+            for (int j = jwt + 1; j <= NLEVSOI; ++j) {
+                const double s_y = syield(k, j, io->zwt[c], P->aq_sp_yield_min);
+                double layer = std::max(tot, -(s_y * (k.zi(j) - io->zwt[c]) * 1.e3));
+                layer = std::min(layer, 0.0);
+                k.liq(j) = k.liq(j) + layer;
+                tot = tot - layer;
+                if (tot >= 0.) {
+                    io->zwt[c] = io->zwt[c] - layer / s_y / 1000.0;
+                    break;
+                } else {
+                    io->zwt[c] = k.zi(j);
+                }
+            }
+            io->zwt[c] = io->zwt[c] - tot / 1000.0 / rous;
+            io->wa[c] = io->wa[c] + tot;
+            jwt = jwt_of(k, io->zwt[c]);
+        }
+        io->zwt[c] = std::max(0.0, io->zwt[c]);
+        io->zwt[c] = std::min(80.0, io->zwt[c]);
+    }
+    for (int j = NLEVSOI; j >= 2; --j) {
+        const double xsi = std::max(k.liq(j) - k.eff(j) * dzmm[j], 0.0);
+        k.liq(j) = std::min(k.eff(j) * dzmm[j], k.liq(j));
+        k.liq(j - 1) = k.liq(j - 1) + xsi;
+    }
+    double xs1 = std::max(std::max(k.liq(1) - WATMIN, 0.0) -
+                          std::max(0.0, (PONDMX + k.watsat(1) * dzmm[1] - k.ice(1) - WATMIN)), 0.0);
+    k.liq(1) = k.liq(1) - xs1;
+    if (P->h2osfcflag == 1) {
+        io->h2osfc[c] = io->h2osfc[c] + xs1;
+        io->qflx_rsub_sat[c] = 0.0;
+    } else {
+        io->qflx_rsub_sat[c] = xs1 / dtime;
+    }
+    xs1 = std::max(std::max(k.ice(1), 0.0) - std::max(0.0, (PONDMX + k.watsat(1) * dzmm[1] - k.liq(1))), 0.0);
+    k.ice(1) = std::min(std::max(0.0, PONDMX + k.watsat(1) * dzmm[1] - k.liq(1)), k.ice(1));
+    io->qflx_ice_runoff_xs[c] = xs1 / dtime;
+    for (int j = 1; j <= NLEVSOI - 1; ++j) {
+        double xs;
+        if (k.liq(j) < WATMIN) {
+            xs = WATMIN - k.liq(j);
+            if (j == jwt) io->zwt[c] = io->zwt[c] + xs / k.eff(j) / 1000.0;
+        } else {
+            xs = 0.0;
+        }
+        k.liq(j) = k.liq(j) + xs;
+        k.liq(j + 1) = k.liq(j + 1) - xs;
+    }
+    {
+        const int j = NLEVSOI;
+        double xs;
+        if (k.liq(j) < WATMIN) {
+            xs = WATMIN - k.liq(j);
+            for (int i = NLEVSOI - 1; i >= 1; --i) {
+                const double avail = std::max(k.liq(i) - WATMIN - xs, 0.0);
+                if (avail >= xs) {
+                    k.liq(j) = k.liq(j) + xs;
+                    k.liq(i) = k.liq(i) - xs;
+                    xs = 0.0;
+                    break;
+                } else {
+                    k.liq(j) = k.liq(j) + avail;
+                    k.liq(i) = k.liq(i) - avail;
+                    xs = xs - avail;
+                }
+            }
+        } else {
+            xs = 0.0;
+        }
+        k.liq(j) = k.liq(j) + xs;
+        rsub_top = rsub_top - xs / dtime;
+    }
+    io->qflx_drain[c] = io->qflx_rsub_sat[c] + rsub_top;
+    io->qflx_qrgwl[c] = io->qflx_snwcp_liq[c];
+}
+
 } // namespace
 
 extern "C" int oracle_hydrology(const ctsmg_bounds* b, int n, const int32_t* filt, const ctsmg_hydrology_io* io,
@@ -115,6 +372,10 @@ extern "C" int oracle_hydrology(const ctsmg_bounds* b, int n, const int32_t* fil
             if (std::fabs(io->h2osfc[c]) < 1.e-13 * std::fabs(h2osfc_partial)) io->h2osfc[c] = 0.0;
             // Infiltration (:426-457)
             io->qflx_infl[c] = io->qflx_in_soil_limited[c] + io->qflx_h2osfc_drain[c];
+        } else if (which == 6) {
+            water_table(k, io, P, dtime);
+        } else if (which == 7) {
+            drainage(k, io, P, dtime);
         } else if (which == 1) {               // PerchedWaterTable
             int k_frz = (k.t(1) > TFRZ) ? NLEVSOI : 1;
             for (int kk = 2; kk <= NLEVSOI; ++kk)

@@ -90,9 +90,14 @@ def soilwater(L, A, b, filt_c, swm=None, e_ice=6.0, hydro=None):
     ncol = A["zwt"].shape[0]
     n = len(filt_c)
     fp = _p(filt_c, C.c_int32)
-    if swm is None or swm.soilwater_movement_method == 0:
-        fields = abi.SOILWATER_FIELDS + ([x for x in abi.SOILWATER_EXTRA if x[0] in A] if swm is not None else [])
+    aquifer = swm is None or swm.soilwater_movement_method == 0
+    if aquifer:
+        fields = abi.SOILWATER_FIELDS + ([x for x in abi.SOILWATER_EXTRA if x[0] in A] if swm is not None or hydro
+                                         else [])
         sw = abi.make_io(abi.SoilWaterIO, fields, A, ncol)
+        if hydro:
+            L.oracle_set_soil_water_fractions(C.byref(b), n, fp, C.byref(sw))
+            hydrology(L, A, b, filt_c, [0, 5], hydro)
         assert L.oracle_soilwater(C.byref(b), n, fp, C.byref(sw), e_ice, DT) == 0
     else:
         sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS + abi.SOILWATER_EXTRA, A, ncol)
@@ -103,8 +108,8 @@ def soilwater(L, A, b, filt_c, swm=None, e_ice=6.0, hydro=None):
         assert L.oracle_soilwater_mf(C.byref(b), n, fp, C.byref(sw), e_ice, DT, C.byref(swm), C.byref(e)) == 0, e.value
     if swm is not None and swm.use_flexibleCN:
         L.oracle_flexcn_fix(C.byref(b), n, fp, C.byref(sw))
-    if hydro:
-        hydrology(L, A, b, filt_c, [1, 2, 3, 4], hydro)
+    if hydro:       # WaterTable + Drainage after the Zeng-Decker form, the default hydrology after the moisture form
+        hydrology(L, A, b, filt_c, [6, 7] if aquifer else [1, 2, 3, 4], hydro)
 
 
 def soil_steps(A, npatch, nsteps, swm=None, snow_method=0, hydro=None):
