@@ -67,6 +67,9 @@ def parse():
     p.add_argument("--serve-rate", type=float, default=8.0)
     p.add_argument("--serve-seconds", type=float, default=60.0)
     p.add_argument("--serve-budget-gb", type=float, default=150.0)
+    p.add_argument("--no-clm5", action="store_true")
+    p.add_argument("--clm5-cols", type=int, default=262144)
+    p.add_argument("--clm5-steps", type=int, default=8)
     return p.parse_args()
 
 
@@ -339,6 +342,47 @@ def ensemble_leg(args, barrier):
             "batched_over_plain": batched / plain}
 
 
+def clm5_leg(args, barrier):
+    """The CLM5-default configuration of the whole scoped step in the resident
+    engine: soil evaporative resistance and root moisture stress, CanopyFluxes,
+    the root sink, SoilTemperature, SoilFluxes, the moisture-form SoilWater
+    with the default hydrology around it (saturated excess, infiltration,
+    perched / theta-based water tables, lateral flows)."""
+    from ctsm_gb300 import abi, full_inputs as fi, soil
+    from ctsm_gb300.engine import SoilBatch
+    r = np.random.Generator(np.random.Philox(args.seed + 7))
+    A, npatch, ngrid, rootr = fi.full_state(args.clm5_cols, seed=args.seed + 7)
+    fi.add_soilfluxes_fields(A, npatch, ngrid)
+    fi.add_rootmoist_fields(A, npatch, rootr, rng=r)
+    fi.add_soilresis_fields(A)
+    fi.add_hydrology_fields(A, r)
+    nml = abi.soilwater_movement_nml(1)
+    soil.set_soilwater_movement(nml)
+    soil.set_soilhydrology_params()
+    soil.set_soil_resistance()
+    try:
+        b = SoilBatch(A, npatch, canopy=True, ngrid=ngrid, soilfluxes=True, rootmoist=True, soilresis=True,
+                      hydrology=True)
+        b.run(args.warmup)
+        b.sync()
+        barrier()
+        ms = b.run(args.clm5_steps, timed=True)
+        b.sync()
+        b.download()
+        b.close()
+    finally:
+        soil.set_soilwater_movement(abi.soilwater_movement_nml(0, use_bedrock=0))
+    ncol = A["zwt"].shape[0]
+    mean_ms = float(ms.mean())
+    return {"workload": "CLM5 default step (soilresis, root moisture stress, CanopyFluxes, root sink, "
+                        "SoilTemperature, SoilFluxes, moisture-form SoilWater + default hydrology), %d columns, "
+                        "%d patches" % (ncol, npatch),
+            "columns": ncol, "patches": npatch, "steps": args.clm5_steps, "ms_per_step": mean_ms,
+            "column_steps_per_s": ncol / (mean_ms * 1e-3),
+            "mean_substeps": float(A["num_substeps"].mean()), "max_substeps": float(A["num_substeps"].max()),
+            "mean_canopy_passes": float(A["num_iter"].mean()), "gpu_launches_per_step": 8}
+
+
 def serving_leg(args):
     """A Poisson stream of run requests through the device pool, bounded in
     wall time: requests still running at the limit are stopped (their steps
@@ -473,6 +517,7 @@ def ours_arm(args, ws, rank, local):
     if rank == 0 and ws == 1:
         for name, flag, fn in (("canopy", args.no_canopy, lambda: canopy_leg(args, barrier)),
                                ("ensemble", args.no_ensemble, lambda: ensemble_leg(args, barrier)),
+                               ("clm5_default", args.no_clm5, lambda: clm5_leg(args, barrier)),
                                ("serving", args.no_serving, lambda: serving_leg(args))):
             if not flag:
                 try:

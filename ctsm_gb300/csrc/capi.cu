@@ -954,7 +954,7 @@ static std::vector<FieldDesc> soilwater_fields(const ctsmg_soilwater_movement_nm
 
 static cudaError_t launch_soilwater_call(const ctsmg_soilwater_io& dio, int begc, int n, const int32_t* dfilt,
                                          const ctsmg_soilwater_movement_nml& nml, double e_ice, double dtime,
-                                         DevError* err, cudaStream_t s) {
+                                         DevError* err, cudaStream_t s, int* d_counter) {
     cudaError_t e;
     if (nml.soilwater_movement_method == 0) {
         e = launch_soilwater(dio, begc, n, dfilt, e_ice, dtime, s);
@@ -962,7 +962,7 @@ static cudaError_t launch_soilwater_call(const ctsmg_soilwater_io& dio, int begc
         MoistureFormArgs P{e_ice, dtime, nml.dtmin, nml.verySmall, nml.xTolerUpper, nml.xTolerLower,
                            nml.lower_boundary_condition, nml.flux_calculation == 42 ? 1 : 0,
                            moisture_form_max_trials(dtime, nml.dtmin)};
-        e = launch_moisture_form(dio, begc, n, dfilt, P, err, s);
+        e = launch_moisture_form(dio, begc, n, dfilt, P, err, s, d_counter);
     }
     if (e == cudaSuccess && nml.use_flexibleCN) e = launch_flexcn(dio, begc, n, dfilt, s);
     return e;
@@ -1012,8 +1012,9 @@ extern "C" int32_t ctsmg_soilwater(const ctsmg_bounds* bounds, int32_t num_hydro
     }
     if (num_hydrologyc == 0) return 0;
     const int ldc = io->ldc;
-    size_t need = table_bytes(T, NT, ldc, 0) + (size_t)num_hydrologyc * 4 + 4096;
+    size_t need = table_bytes(T, NT, ldc, 0) + (size_t)num_hydrologyc * 4 + 4096 + 256;
     if ((rc = arena_reserve(c, need))) return rc;
+    int* dcounter = (int*)arena_take(c, 256);
     cudaError_t e = cudaMemsetAsync(c->err, 0xff, sizeof(DevError), c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(err)");
     std::vector<Chunk> chunks;
@@ -1029,7 +1030,7 @@ extern "C" int32_t ctsmg_soilwater(const ctsmg_bounds* bounds, int32_t num_hydro
             const Chunk& ch = chunks[k];
             if ((e = cudaStreamWaitEvent(c->stream, c->ev_in[k], 0)) != cudaSuccess) return cuda_fail(e, "wait");
             e = launch_soilwater_call(dio, bounds->begc, ch.f1 - ch.f0, dfilt + ch.f0, nml, e_ice, dtime, c->err,
-                                      c->stream);
+                                      c->stream, dcounter);
             if (e != cudaSuccess) return cuda_fail(e, "soilwater kernel launch");
             if ((e = cudaEventRecord(c->ev_done[k], c->stream)) != cudaSuccess) return cuda_fail(e, "record");
             if (k + 1 < K && (rc = chunk_in(c, chunks[k + 1], k + 1, io, &dio, T, NT, ldc, 0))) return rc;
@@ -1043,7 +1044,8 @@ extern "C" int32_t ctsmg_soilwater(const ctsmg_bounds* bounds, int32_t num_hydro
         int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_hydrologyc * 4);
         e = cudaMemcpyAsync(dfilt, filter_hydrologyc, (size_t)num_hydrologyc * 4, cudaMemcpyHostToDevice, c->stream);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
-        e = launch_soilwater_call(dio, bounds->begc, num_hydrologyc, dfilt, nml, e_ice, dtime, c->err, c->stream);
+        e = launch_soilwater_call(dio, bounds->begc, num_hydrologyc, dfilt, nml, e_ice, dtime, c->err, c->stream,
+                                  dcounter);
         if (e != cudaSuccess) return cuda_fail(e, "soilwater kernel launch");
         if ((rc = stage_out(c, io, &dio, T, NT, ldc, 0))) return rc;
         e = cudaStreamSynchronize(c->stream);

@@ -49,6 +49,7 @@ struct Batch {
     double* mslope = nullptr;
     double* mint = nullptr;
     int* counter = nullptr;
+    int* mf_counter = nullptr;     // work counter of the persistent moisture-form kernel
     double* cws = nullptr;         // CanopyFluxes iteration records
     int32_t* d_perm = nullptr;     // sorted position -> original column index (0-based)
     double* ws = nullptr;
@@ -105,7 +106,9 @@ static cudaError_t enqueue_step(Batch* b) {
     const HydroStepArgs* hy = b->cfg.hydrology ? &b->hya : nullptr;
     const bool own = mf || hy;
     auto water_step = [&](int refresh) {
-        if (mf) return launch_mf_step(b->dsw, ncol, b->mfa, b->swm.use_flexibleCN, refresh, b->err, nullptr, b->stream, hy);
+        if (mf)
+            return launch_mf_step(b->dsw, ncol, b->mfa, b->swm.use_flexibleCN, refresh, b->err, nullptr, b->stream,
+                                  b->mf_counter, hy);
         return launch_zd09_step(b->dsw, ncol, b->cfg.e_ice, b->cfg.dtime, b->swm.use_flexibleCN, refresh, nullptr,
                                 b->stream, hy);
     };
@@ -144,7 +147,8 @@ static void batch_free(Batch* b) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
     for (auto& f : b->fields) if (f.dptr) cudaFree(f.dptr);
     for (void* p : {(void*)b->d_perm, (void*)b->ws, (void*)b->err, b->snapshot, (void*)b->rootr, (void*)b->mslope,
-                    (void*)b->mint, (void*)b->counter, (void*)b->cws, b->bal_mem, (void*)b->hyd_params})
+                    (void*)b->mint, (void*)b->counter, (void*)b->cws, b->bal_mem, (void*)b->hyd_params,
+                    (void*)b->mf_counter})
         if (p) cudaFree(p);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
@@ -421,6 +425,8 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
             b->bal.th2osfc_bef = const_cast<double*>(b->dsf.t_h2osfc_bef);
         }
     }
+    if (swm.soilwater_movement_method == 1 && (e = cudaMalloc(&b->mf_counter, 256)) != cudaSuccess)
+        return fail(cuda_err(e, "moisture-form counter"));
     for (auto& f : b->fields) b->state_bytes += f.bytes;
     if ((e = cudaMalloc(&b->ws, (size_t)SOILTEMP_WS_DOUBLES_PER_COL * ncol * 8)) != cudaSuccess) return fail(cuda_err(e, "ws"));
     if ((e = cudaMalloc(&b->err, sizeof(DevError))) != cudaSuccess) return fail(cuda_err(e, "err"));

@@ -3,7 +3,9 @@
 // and the use_flexibleCN negative-liquid fix SoilWater applies after either
 // form (:331-368), in FP64 on sm_103a.
 //
-// One thread owns one column for the whole adaptive sub-step loop.  A trial
+// The kernels are persistent: a lane owns one column for its whole adaptive
+// sub-step loop and, when the column completes, takes the next column of the
+// filter, so columns that need many sub-steps do not hold their warp.  A trial
 // sub-step streams down the column once: the hydraulic properties of level
 // j+1 (compute_hydraulic_properties, :1444-1556, Clapp-Hornberger curve) are
 // formed while the flux, its derivatives (compute_moisture_fluxes_and_derivs,
@@ -15,6 +17,7 @@
 // element is dgtsv's.
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <cooperative_groups.h>
 #include "ctsm_device.cuh"
 #include "soil_math.cuh"
 #include "moisture_form_kernels.cuh"
@@ -57,203 +60,241 @@ __device__ __forceinline__ double rel_sat(const ColView& k, int j, double liq) {
 }
 } // namespace
 
-// Returns 0, dgtsv's info (1-based level of the zero pivot), or -1 when the
-// sub-step loop has not completed the step within P.max_trials trials (the
-// host sets a bound the reference's halving/doubling rule cannot reach).
-__device__ int mf_column(const ctsmg_soilwater_io& io, int c, const MoistureFormArgs& P) {
+// Per-lane state of one column's adaptive sub-step loop: the persistent
+// kernels below run one trial sub-step per loop pass and let a lane whose
+// column has completed take the next column, so a column that needs many
+// sub-steps does not hold the other lanes of its warp.
+// smp_l, hk_l and qout of each trial go straight to the column's arrays (the
+// last trial, the one that completes the step, leaves them as the reference
+// does), so the lane keeps only its liquid water; the expensive error
+// estimate also keeps the flux derivatives.
+template <bool EXPENSIVE>
+struct MFLane {
+    int c, nl, jwt, nsub;
+    bool wt;
+    double zwt, qinfl, dtsub, dtdone, qcharge, vwc_q, imped_q;
+    double liq[N1];
+    double dqodw1[EXPENSIVE ? N1 : 1], dqodw2[EXPENSIVE ? N1 : 1];
+};
+
+enum { MF_MORE = 0, MF_DONE = 1, MF_SINGULAR = 2, MF_NOT_DONE = 3 };
+
+template <bool EXPENSIVE>
+__device__ __forceinline__ void mf_begin(MFLane<EXPENSIVE>& L, const ctsmg_soilwater_io& io, int c, const MoistureFormArgs& P) {
     const ColView k{io, c, io.ldc};
-    const int nl = io.nbedrock[c];
-    const double qinfl = io.qflx_infl[c];
-    const double zwt = io.zwt[c];
-    const bool wt = P.lower_bc == 3;
-    int jwt = NLEVSOI;
-    if (wt) {
+    L.c = c;
+    L.nl = io.nbedrock[c];
+    L.qinfl = io.qflx_infl[c];
+    L.zwt = io.zwt[c];
+    L.wt = P.lower_bc == 3;
+    L.jwt = NLEVSOI;
+    if (L.wt) {
 #pragma unroll 1
         for (int j = 1; j <= NLEVSOI; ++j)
-            if (zwt <= k.zi(j)) { jwt = j - 1; break; }
+            if (L.zwt <= k.zi(j)) { L.jwt = j - 1; break; }
     }
+#pragma unroll 1
+    for (int j = 1; j <= L.nl; ++j) L.liq[j] = k.ss(io.h2osoi_liq, j);
+    L.nsub = 0;
+    L.dtsub = P.dtime;
+    L.dtdone = 0.0;
+    L.qcharge = 0.0;
+    L.vwc_q = 0.0;
+    L.imped_q = 1.0;
+}
 
-    double liq[N1], smp[N1], hk[N1], qout[N1], dqodw1[N1], dqodw2[N1], fn1[N1];
+// One trial sub-step (SoilWaterMovementMod.F90:1197-1399).  Returns MF_MORE,
+// MF_DONE, MF_SINGULAR (with *info = dgtsv's info) or MF_NOT_DONE when the
+// loop has run P.max_trials trials (a bound the reference's halving /
+// doubling rule cannot reach).
+template <bool EXPENSIVE>
+__device__ int mf_trial(MFLane<EXPENSIVE>& L, const ctsmg_soilwater_io& io, const MoistureFormArgs& P, int* info) {
+    const ColView k{io, L.c, io.ldc};
+    const int nl = L.nl, jwt = L.jwt;
+    const bool wt = L.wt;
+    const size_t ld = io.ldc;
+    double* const qout_c = io.qout + L.c;     // level j at qout_c[(j-1) ld]
     double d[N1], du[N1], dl2[N1], b[N1];
+    L.nsub = L.nsub + 1;
+    const double dtsub = L.dtsub;
+    // ---- level 1 suction, then stream the levels
+    double s2c = rel_sat(k, 1, L.liq[1]);
+    double smp_c, dsmpdw_c;
+    suction(k, 1, s2c, smp_c, dsmpdw_c);
+    double qin = L.qinfl, dqidw0 = 0.0, dqidw1 = 0.0;
+    double hk_nl = 0.0, dhkdw_nl = 0.0, qo_nl = 0.0, dq1_nl = 0.0;
+    // pending dgtsv row: d_p, du_p, b_p; its sub-diagonal arrives with the next row
+    double d_p = 0.0, du_p = 0.0, b_p = 0.0;
 #pragma unroll 1
-    for (int j = 1; j <= nl; ++j) liq[j] = k.ss(io.h2osoi_liq, j);
-
-    int nsub = 0;
-    bool done = false;
-    double dtsub = P.dtime, dtdone = 0.0, qcharge = 0.0;
-    double vwc_q = 0.0, imped_q = 1.0;          // compute_qcharge's level jwt+1 of the last trial
-#pragma unroll 1
-    for (int guard = 0; guard < P.max_trials; ++guard) {
-        nsub = nsub + 1;
-        // ---- level 1 suction, then stream the levels
-        double s2c = rel_sat(k, 1, liq[1]);
-        double smp_c, dsmpdw_c;
-        suction(k, 1, s2c, smp_c, dsmpdw_c);
-        double qin = qinfl, dqidw0 = 0.0, dqidw1 = 0.0;
-        double hk_nl = 0.0, dhkdw_nl = 0.0;
-        // pending dgtsv row: d_p, du_p, b_p; its sub-diagonal arrives with the next row
-        double d_p = 0.0, du_p = 0.0, b_p = 0.0;
-#pragma unroll 1
-        for (int j = 1; j <= nl; ++j) {
-            double s2n = 0.0, smp_n = 0.0, dsmpdw_n = 0.0;
-            if (j < nl) {
-                s2n = rel_sat(k, j + 1, liq[j + 1]);
-                suction(k, j + 1, s2n, smp_n, dsmpdw_n);
-            }
-            double s1, imped;
-            if (j == nl) {
-                s1 = s2c;
-                imped = pow10_dd(-P.e_ice * k.g(io.icefrac, j));
+    for (int j = 1; j <= nl; ++j) {
+        double s2n = 0.0, smp_n = 0.0, dsmpdw_n = 0.0;
+        if (j < nl) {
+            s2n = rel_sat(k, j + 1, L.liq[j + 1]);
+            suction(k, j + 1, s2n, smp_n, dsmpdw_n);
+        }
+        double s1, imped;
+        if (j == nl) {
+            s1 = s2c;
+            imped = pow10_dd(-P.e_ice * k.g(io.icefrac, j));
+        } else {
+            s1 = 0.5 * (s2c + s2n);
+            imped = pow10_dd(-P.e_ice * (0.5 * (k.g(io.icefrac, j) + k.g(io.icefrac, j + 1))));
+        }
+        s1 = fmn(s1, 1.0);
+        s1 = fmx(0.01, s1);
+        const double ws = k.g(io.watsat, j), bsw = k.g(io.bsw, j);
+        const double hkj = imped * k.g(io.hksat, j) * pow(s1, 2.0 * bsw + 3.0);
+        const double dhkdw = (2.0 * bsw + 3.0) * hkj / s1;
+        io.smp_l[L.c + (j - 1) * ld] = smp_c;
+        io.hk_l[L.c + (j - 1) * ld] = hkj;
+        if (wt && j == jwt + 1) {
+            L.vwc_q = fmx(L.liq[j], 1.0e-6) / (k.ss(io.dz, j) * DENH2O);
+            L.imped_q = imped;
+        }
+        // flux out of the bottom of level j and its derivatives
+        double qo, dq1, dq2;
+        if (j < nl) {
+            const double dhkds1 = 0.5 * dhkdw / ws;
+            const double dhkds2 = 0.5 * dhkdw / k.g(io.watsat, j + 1);
+            const double num = smp_n - smp_c;
+            const double den = M_TO_MM * (k.ss(io.z, j + 1) - k.ss(io.z, j));
+            qo = -hkj * num / den + hkj;
+            dq1 = (hkj * dsmpdw_c - dhkds1 * num) / den + dhkds1;
+            dq2 = (-hkj * dsmpdw_n - dhkds2 * num) / den + dhkds2;
+        } else if (P.lower_bc == 3) {            // bc_waterTable (nl == nlevsoi)
+            if (NLEVSOI > jwt) {
+                qo = 0.0; dq1 = 0.0; dq2 = 0.0;
             } else {
-                s1 = 0.5 * (s2c + s2n);
-                imped = pow10_dd(-P.e_ice * (0.5 * (k.g(io.icefrac, j) + k.g(io.icefrac, j + 1))));
-            }
-            s1 = fmn(s1, 1.0);
-            s1 = fmx(0.01, s1);
-            const double ws = k.g(io.watsat, j), bsw = k.g(io.bsw, j);
-            const double hkj = imped * k.g(io.hksat, j) * pow(s1, 2.0 * bsw + 3.0);
-            const double dhkdw = (2.0 * bsw + 3.0) * hkj / s1;
-            smp[j] = smp_c;
-            hk[j] = hkj;
-            if (wt && j == jwt + 1) {
-                vwc_q = fmx(liq[j], 1.0e-6) / (k.ss(io.dz, j) * DENH2O);
-                imped_q = imped;
-            }
-            // flux out of the bottom of level j and its derivatives
-            double qo, dq1, dq2;
-            if (j < nl) {
-                const double dhkds1 = 0.5 * dhkdw / ws;
-                const double dhkds2 = 0.5 * dhkdw / k.g(io.watsat, j + 1);
-                const double num = smp_n - smp_c;
-                const double den = M_TO_MM * (k.ss(io.z, j + 1) - k.ss(io.z, j));
+                const double dhkds1 = dhkdw / ws;
+                const double num = -smp_c;
+                const double den = M_TO_MM * (L.zwt - k.ss(io.z, j));
                 qo = -hkj * num / den + hkj;
                 dq1 = (hkj * dsmpdw_c - dhkds1 * num) / den + dhkds1;
-                dq2 = (-hkj * dsmpdw_n - dhkds2 * num) / den + dhkds2;
-            } else if (P.lower_bc == 3) {            // bc_waterTable (nl == nlevsoi)
-                if (NLEVSOI > jwt) {
-                    qo = 0.0; dq1 = 0.0; dq2 = 0.0;
-                } else {
-                    const double dhkds1 = dhkdw / ws;
-                    const double num = -smp_c;
-                    const double den = M_TO_MM * (zwt - k.ss(io.z, j));
-                    qo = -hkj * num / den + hkj;
-                    dq1 = (hkj * dsmpdw_c - dhkds1 * num) / den + dhkds1;
-                    dq2 = 0.0;
-                }
-            } else if (P.lower_bc == 1) {            // bc_flux: free drainage
-                qo = hkj; dq1 = dhkdw / ws; dq2 = 0.0;
-            } else {                                 // bc_zero_flux
-                qo = 0.0; dq1 = 0.0; dq2 = 0.0;
+                dq2 = 0.0;
             }
-            qout[j] = qo; dqodw1[j] = dq1; dqodw2[j] = dq2;
-            if (j == nl) { hk_nl = hkj; dhkdw_nl = dhkdw; }
-            // tridiagonal row j
-            const double dt_dz = dtsub / (M_TO_MM * k.ss(io.dz, j));
-            const double amx = (j == 1) ? 0.0 : dqidw0 * dt_dz;
-            const double bmx = -1.0 - (-dqidw1 + dq1) * dt_dz;
-            const double cmx = (j == nl) ? 0.0 : -dq2 * dt_dz;
-            const double fluxNet = qin - qo - k.g(io.qflx_rootsoi, j);
-            fn1[j] = fluxNet;
-            const double rmx = -fluxNet * dt_dz;
-            if (j == 1) {
-                d_p = bmx; du_p = cmx; b_p = rmx;
+        } else if (P.lower_bc == 1) {            // bc_flux: free drainage
+            qo = hkj; dq1 = dhkdw / ws; dq2 = 0.0;
+        } else {                                 // bc_zero_flux
+            qo = 0.0; dq1 = 0.0; dq2 = 0.0;
+        }
+        qout_c[(j - 1) * ld] = qo;
+        if (EXPENSIVE) { L.dqodw1[j] = dq1; L.dqodw2[j] = dq2; }
+        if (j == nl) { hk_nl = hkj; dhkdw_nl = dhkdw; qo_nl = qo; dq1_nl = dq1; }
+        // tridiagonal row j
+        const double dt_dz = dtsub / (M_TO_MM * k.ss(io.dz, j));
+        const double amx = (j == 1) ? 0.0 : dqidw0 * dt_dz;
+        const double bmx = -1.0 - (-dqidw1 + dq1) * dt_dz;
+        const double cmx = (j == nl) ? 0.0 : -dq2 * dt_dz;
+        const double fluxNet = qin - qo - k.g(io.qflx_rootsoi, j);
+        const double rmx = -fluxNet * dt_dz;
+        if (j == 1) {
+            d_p = bmx; du_p = cmx; b_p = rmx;
+        } else {
+            // dgtsv elimination step i = j-2 (0-based) on rows j-1 (pending) and j
+            double dl = amx, dn = bmx, dun = cmx, bn = rmx;
+            if (fabs(d_p) >= fabs(dl)) {
+                if (d_p == 0.0) { *info = j - 1; return MF_SINGULAR; }
+                const double fact = dl / d_p;
+                dn = dn - fact * du_p;
+                bn = bn - fact * b_p;
+                dl2[j - 1] = 0.0;
             } else {
-                // dgtsv elimination step i = j-2 (0-based) on rows j-1 (pending) and j
-                double dl = amx, dn = bmx, dun = cmx, bn = rmx;
-                if (fabs(d_p) >= fabs(dl)) {
-                    if (d_p == 0.0) return j - 1;
-                    const double fact = dl / d_p;
-                    dn = dn - fact * du_p;
-                    bn = bn - fact * b_p;
-                    dl2[j - 1] = 0.0;
-                } else {
-                    const double fact = d_p / dl;
-                    d_p = dl;
-                    const double temp = dn;
-                    dn = du_p - fact * temp;
-                    dl2[j - 1] = dun;                 // second super-diagonal fill of row j-1
-                    dun = -fact * dun;
-                    du_p = temp;
-                    const double tb = b_p;
-                    b_p = bn;
-                    bn = tb - fact * bn;
-                }
-                d[j - 1] = d_p; du[j - 1] = du_p; b[j - 1] = b_p;
-                d_p = dn; du_p = dun; b_p = bn;
+                const double fact = d_p / dl;
+                d_p = dl;
+                const double temp = dn;
+                dn = du_p - fact * temp;
+                dl2[j - 1] = dun;                 // second super-diagonal fill of row j-1
+                dun = -fact * dun;
+                du_p = temp;
+                const double tb = b_p;
+                b_p = bn;
+                bn = tb - fact * bn;
             }
-            // next level
-            qin = qo; dqidw0 = dq1; dqidw1 = dq2;
-            s2c = s2n; smp_c = smp_n; dsmpdw_c = dsmpdw_n;
+            d[j - 1] = d_p; du[j - 1] = du_p; b[j - 1] = b_p;
+            d_p = dn; du_p = dun; b_p = bn;
         }
-        if (d_p == 0.0) return nl;
-        d[nl] = d_p; du[nl] = du_p; b[nl] = b_p;
-        // back substitution (1-based rows here)
-        b[nl] = b[nl] / d[nl];
-        if (nl > 1) b[nl - 1] = (b[nl - 1] - du[nl - 1] * b[nl]) / d[nl - 1];
-#pragma unroll 1
-        for (int i = nl - 2; i >= 1; --i) b[i] = (b[i] - du[i] * b[i + 1] - dl2[i] * b[i + 2]) / d[i];
-        // ---- error estimate (:1306-1348)
-        double errorMax = 0.0;
-#pragma unroll 1
-        for (int j = 1; j <= nl; ++j) {
-            const double dt_dz = dtsub / (M_TO_MM * k.ss(io.dz, j));
-            double fluxNet0;
-            if (P.expensive) {
-                const double qi = (j == 1) ? qinfl : qout[j - 1];
-                const double qin_test = (j == 1) ? qi + 0.0 * b[j]
-                                                 : qi + dqodw1[j - 1] * b[j - 1] + dqodw2[j - 1] * b[j];
-                const double qout_test = (j == nl) ? qout[j] + dqodw1[j] * b[j]
-                                                   : qout[j] + dqodw1[j] * b[j] + dqodw2[j] * b[j + 1];
-                fluxNet0 = qin_test - qout_test - k.g(io.qflx_rootsoi, j);
-            } else {
-                fluxNet0 = b[j] / dt_dz;
-            }
-            const double e = fabs(fn1[j] - fluxNet0) * dtsub * 0.5;
-            errorMax = (j == 1) ? e : ((errorMax < e) ? e : errorMax);
-        }
-        if (errorMax > P.xTolerUpper && dtsub > P.dtmin) {
-            dtsub = fmx(dtsub / 2.0, P.dtmin);
-            continue;
-        }
-#pragma unroll 1
-        for (int j = 1; j <= nl; ++j) liq[j] = liq[j] + b[j] * (M_TO_MM * k.ss(io.dz, j));
-        double qcTemp;
-        if (P.lower_bc == 1) qcTemp = hk_nl + dhkdw_nl * b[nl];
-        else if (P.lower_bc == 2) qcTemp = 0.0;
-        else qcTemp = qout[nl] + dqodw1[nl] * b[nl];
-        qcharge = qcharge + qcTemp * (dtsub / P.dtime);
-        dtdone = dtdone + dtsub;
-        if (fabs(P.dtime - dtdone) < P.verySmall) { done = true; break; }
-        if (errorMax < P.xTolerLower) dtsub = dtsub * 2.0;
-        dtsub = fmn(dtsub, P.dtime - dtdone);
+        // next level
+        qin = qo; dqidw0 = dq1; dqidw1 = dq2;
+        s2c = s2n; smp_c = smp_n; dsmpdw_c = dsmpdw_n;
     }
-    if (!done) return -1;
-    io.num_substeps[c] = (double)nsub;
+    if (d_p == 0.0) { *info = nl; return MF_SINGULAR; }
+    d[nl] = d_p; du[nl] = du_p; b[nl] = b_p;
+    // back substitution (1-based rows here)
+    b[nl] = b[nl] / d[nl];
+    if (nl > 1) b[nl - 1] = (b[nl - 1] - du[nl - 1] * b[nl]) / d[nl - 1];
+#pragma unroll 1
+    for (int i = nl - 2; i >= 1; --i) b[i] = (b[i] - du[i] * b[i + 1] - dl2[i] * b[i + 2]) / d[i];
+    // ---- error estimate (:1306-1348)
+    double errorMax = 0.0;
+#pragma unroll 1
+    for (int j = 1; j <= nl; ++j) {
+        const double dt_dz = dtsub / (M_TO_MM * k.ss(io.dz, j));
+        const double qi = (j == 1) ? L.qinfl : qout_c[(j - 2) * ld];
+        const double qo = qout_c[(j - 1) * ld];
+        double fluxNet0;
+        if (EXPENSIVE) {
+            const double qin_test = (j == 1) ? qi + 0.0 * b[j]
+                                             : qi + L.dqodw1[j - 1] * b[j - 1] + L.dqodw2[j - 1] * b[j];
+            const double qout_test = (j == nl) ? qo + L.dqodw1[j] * b[j]
+                                               : qo + L.dqodw1[j] * b[j] + L.dqodw2[j] * b[j + 1];
+            fluxNet0 = qin_test - qout_test - k.g(io.qflx_rootsoi, j);
+        } else {
+            fluxNet0 = b[j] / dt_dz;
+        }
+        // fluxNet1, the net flux at the start of the sub-step, as the row's rmx had it
+        const double fn1 = qi - qo - k.g(io.qflx_rootsoi, j);
+        const double e = fabs(fn1 - fluxNet0) * dtsub * 0.5;
+        errorMax = (j == 1) ? e : ((errorMax < e) ? e : errorMax);
+    }
+    if (errorMax > P.xTolerUpper && dtsub > P.dtmin) {
+        L.dtsub = fmx(dtsub / 2.0, P.dtmin);
+        return (L.nsub >= P.max_trials) ? MF_NOT_DONE : MF_MORE;
+    }
+#pragma unroll 1
+    for (int j = 1; j <= nl; ++j) L.liq[j] = L.liq[j] + b[j] * (M_TO_MM * k.ss(io.dz, j));
+    double qcTemp;
+    if (P.lower_bc == 1) qcTemp = hk_nl + dhkdw_nl * b[nl];
+    else if (P.lower_bc == 2) qcTemp = 0.0;
+    else qcTemp = qo_nl + dq1_nl * b[nl];
+    L.qcharge = L.qcharge + qcTemp * (dtsub / P.dtime);
+    L.dtdone = L.dtdone + dtsub;
+    if (fabs(P.dtime - L.dtdone) < P.verySmall) return MF_DONE;
+    double nd = dtsub;
+    if (errorMax < P.xTolerLower) nd = nd * 2.0;
+    L.dtsub = fmn(nd, P.dtime - L.dtdone);
+    return (L.nsub >= P.max_trials) ? MF_NOT_DONE : MF_MORE;
+}
+
+// The end of soilwater_moisture_form for a completed column (:1401-1436).
+template <bool EXPENSIVE>
+__device__ void mf_finish(MFLane<EXPENSIVE>& L, const ctsmg_soilwater_io& io, const MoistureFormArgs& P) {
+    const ColView k{io, L.c, io.ldc};
+    const int c = L.c, nl = L.nl, jwt = L.jwt;
+    io.num_substeps[c] = (double)L.nsub;
     // over-saturated layers pass their excess upward (:1405-1409)
 #pragma unroll 1
     for (int j = nl; j >= 2; --j) {
         const double cap = k.g(io.eff_porosity, j) * M_TO_MM * k.ss(io.dz, j);
-        const double over = fmx(liq[j] - cap, 0.0);
-        liq[j] = fmn(cap, liq[j]);
-        liq[j - 1] = liq[j - 1] + over;
+        const double over = fmx(L.liq[j] - cap, 0.0);
+        L.liq[j] = fmn(cap, L.liq[j]);
+        L.liq[j - 1] = L.liq[j - 1] + over;
     }
     double* h2osoi_liq = io.h2osoi_liq;
 #pragma unroll 1
     for (int j = 1; j <= nl; ++j) {
-        h2osoi_liq[c + (size_t)(j - LS) * k.ld] = liq[j];
-        io.smp_l[c + (size_t)(j - 1) * k.ld] = smp[j];
-        io.hk_l[c + (size_t)(j - 1) * k.ld] = hk[j];
-        io.qin[c + (size_t)(j - 1) * k.ld] = (j == 1) ? qinfl : qout[j - 1];
-        io.qout[c + (size_t)(j - 1) * k.ld] = qout[j];
+        h2osoi_liq[c + (size_t)(j - LS) * k.ld] = L.liq[j];
+        io.qin[c + (size_t)(j - 1) * k.ld] = (j == 1) ? L.qinfl : io.qout[c + (size_t)(j - 2) * k.ld];
     }
+    double qcharge = L.qcharge;
     // compute_qcharge for the water-table boundary (:2016-2135)
-    if (wt && jwt < NLEVSOI) {
+    if (L.wt && jwt < NLEVSOI) {
+        const double zwt = L.zwt;
         const double wh_zwt = -k.g(io.sucsat, jwt + 1) - zwt * M_TO_MM;
-        double s1 = fmx(vwc_q / k.g(io.watsat, jwt + 1), 0.01);
+        double s1 = fmx(L.vwc_q / k.g(io.watsat, jwt + 1), 0.01);
         s1 = fmn(1.0, s1);
-        const double ka = imped_q * k.g(io.hksat, jwt + 1) * pow(s1, 2.0 * k.g(io.bsw, jwt + 1) + 3.0);
+        const double ka = L.imped_q * k.g(io.hksat, jwt + 1) * pow(s1, 2.0 * k.g(io.bsw, jwt + 1) + 3.0);
         const int jm = jwt > 1 ? jwt : 1;
-        const double smp1 = fmx(io.smpmin[c], smp[jm]);
+        const double smp1 = fmx(io.smpmin[c], io.smp_l[c + (size_t)(jm - 1) * k.ld]);
         const double wh = smp1 - k.ss(io.z, jm) * M_TO_MM;
         if (jwt == 0) qcharge = -ka * (wh_zwt - wh) / ((zwt + (double)1.e-3f) * M_TO_MM);
         else qcharge = -ka * (wh_zwt - wh) / ((zwt - k.ss(io.z, jwt)) * M_TO_MM * 2.0);
@@ -261,18 +302,52 @@ __device__ int mf_column(const ctsmg_soilwater_io& io, int c, const MoistureForm
         qcharge = fmn(10.0 / P.dtime, qcharge);
     }
     io.qcharge[c] = qcharge;
-    return 0;
 }
 
+// The next filter position for the calling lane: the lanes that ask at the
+// same time take consecutive positions with one atomic, so a warp's first
+// columns (and most refills) are neighbours in memory.
+__device__ __forceinline__ int mf_grab(int* counter) {
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    int base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(counter, (int)g.size());
+    base = g.shfl(base, 0);
+    return base + (int)g.thread_rank();
+}
+
+// The persistent loop: begin(fc) prepares filter position fc and returns its
+// column; end(fc, status, info) finishes it.
+template <bool EXPENSIVE, class Begin, class End>
+__device__ __forceinline__ void mf_persistent(const ctsmg_soilwater_io& io, int n, int* counter,
+                                              const MoistureFormArgs& P, Begin begin, End end) {
+    MFLane<EXPENSIVE> L;
+    int fc = mf_grab(counter);
+    if (fc >= n) return;
+    mf_begin(L, io, begin(fc), P);
+#pragma unroll 1
+    for (;;) {
+        int info = 0;
+        const int st = mf_trial(L, io, P, &info);
+        if (st == MF_MORE) continue;
+        if (st == MF_DONE) mf_finish(L, io, P);
+        end(fc, L.c, st, info);
+        fc = mf_grab(counter);
+        if (fc >= n) break;
+        mf_begin(L, io, begin(fc), P);
+    }
+}
+
+template <bool EXPENSIVE>
 __global__ void __launch_bounds__(128)
 moisture_form_kernel(ctsmg_soilwater_io io, int begc, int nfilt, const int32_t* __restrict__ filt,
-                     MoistureFormArgs P, DevError* err) {
-    const int fc = blockIdx.x * blockDim.x + threadIdx.x;
-    if (fc >= nfilt) return;
-    const int cg = filt ? filt[fc] : fc + begc;
-    const int info = mf_column(io, cg - begc, P);
-    if (info > 0) report_error(err, cg, info, CTSMG_E_SINGULAR);
-    else if (info < 0) report_error(err, cg, 0, CTSMG_E_TIMEOUT);
+                     MoistureFormArgs P, DevError* err, int* counter) {
+    mf_persistent<EXPENSIVE>(io, nfilt, counter, P,
+                  [&](int fc) { return (filt ? filt[fc] : fc + begc) - begc; },
+                  [&](int fc, int c, int st, int info) {
+                      if (st == MF_SINGULAR) report_error(err, c + begc, info, CTSMG_E_SINGULAR);
+                      else if (st == MF_NOT_DONE) report_error(err, c + begc, 0, CTSMG_E_TIMEOUT);
+                  });
 }
 
 __global__ void __launch_bounds__(128)
@@ -286,51 +361,106 @@ flexcn_kernel(ctsmg_soilwater_io io, int begc, int nfilt, const int32_t* __restr
 // form: SetSoilWaterFractions, SoilWater (moisture form), the flexibleCN fix
 // and, if refresh, the between-step h2osoi_vol refresh
 // (HydrologyNoDrainageMod.F90:302, 346, 580, 590).
+// The resident step's moisture-form SoilWater in three launches, so that the
+// persistent sub-step kernel holds nothing but the sub-step loop and its
+// lanes stay converged outside it: before it, one thread per column runs
+// SetSoilWaterFractions (and with HYDRO SaturatedExcessRunoff and the
+// infiltration chain that yields qflx_infl); after it, the flexibleCN fix,
+// with HYDRO the water tables and lateral flows, and the h2osoi_vol refresh.
+__device__ __forceinline__ ctsmg_soilhydrology_params column_params(const HydroStepArgs& hy, int c) {
+    ctsmg_soilhydrology_params hp = hy.par;
+    if (hy.baseflow_scalar_c) hp.baseflow_scalar = hy.baseflow_scalar_c[c];
+    if (hy.fff_c) hp.fff = hy.fff_c[c];
+    return hp;
+}
+
 template <bool HYDRO>
 __global__ void __launch_bounds__(128)
-mf_step_kernel(ctsmg_soilwater_io io, int ncol, MoistureFormArgs P, int flexcn, int refresh, DevError* err,
+mf_pre_kernel(ctsmg_soilwater_io io, int ncol, double dtime, const int32_t* __restrict__ filt, HydroStepArgs hy) {
+    const int fc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fc >= ncol) return;
+    const int c = filt ? filt[fc] - 1 : fc;
+    set_soil_water_fractions(io, c);
+    if (HYDRO) {
+        const ctsmg_soilhydrology_params hp = column_params(hy, c);
+        hydro::saturated_excess_runoff(hy.io, c, hp.fff);
+        hydro::infiltration_chain(hy.io, c, hp, dtime);
+    }
+}
+
+template <bool EXPENSIVE>
+__global__ void __launch_bounds__(128)
+mf_core_kernel(ctsmg_soilwater_io io, int ncol, MoistureFormArgs P, DevError* err, const int32_t* __restrict__ filt,
+               int* counter) {
+    mf_persistent<EXPENSIVE>(io, ncol, counter, P, [&](int fc) { return filt ? filt[fc] - 1 : fc; },
+                  [&](int fc, int c, int st, int info) {
+                      if (st == MF_SINGULAR) report_error(err, c + 1, info, CTSMG_E_SINGULAR);
+                      else if (st == MF_NOT_DONE) report_error(err, c + 1, 0, CTSMG_E_TIMEOUT);
+                  });
+}
+
+template <bool HYDRO>
+__global__ void __launch_bounds__(128)
+mf_post_kernel(ctsmg_soilwater_io io, int ncol, double dtime, int flexcn, int refresh,
                const int32_t* __restrict__ filt, HydroStepArgs hy) {
     const int fc = blockIdx.x * blockDim.x + threadIdx.x;
     if (fc >= ncol) return;
     const int c = filt ? filt[fc] - 1 : fc;
-    ctsmg_soilhydrology_params hp = hy.par;
-    if (HYDRO) {
-        if (hy.baseflow_scalar_c) hp.baseflow_scalar = hy.baseflow_scalar_c[c];
-        if (hy.fff_c) hp.fff = hy.fff_c[c];
-    }
-    set_soil_water_fractions(io, c);
-    if (HYDRO) {
-        hydro::saturated_excess_runoff(hy.io, c, hp.fff);
-        hydro::infiltration_chain(hy.io, c, hp, P.dtime);    // qflx_infl for SoilWater
-    }
-    const int info = mf_column(io, c, P);
-    if (info > 0) report_error(err, c + 1, info, CTSMG_E_SINGULAR);
-    else if (info < 0) report_error(err, c + 1, 0, CTSMG_E_TIMEOUT);
     if (flexcn) flexcn_column(io, c);
     if (HYDRO) {
+        const ctsmg_soilhydrology_params hp = column_params(hy, c);
         hydro::perched_water_table(hy.io, c);
         hydro::theta_based_water_table(hy.io, c);
-        hydro::perched_lateral_flow(hy.io, c, hp, P.dtime);
-        hydro::subsurface_lateral_flow(hy.io, c, hp, P.dtime);
+        hydro::perched_lateral_flow(hy.io, c, hp, dtime);
+        hydro::subsurface_lateral_flow(hy.io, c, hp, dtime);
     }
     if (refresh) refresh_h2osoi_vol(io, c);
 }
 
+// Blocks of a persistent launch: every SM filled to the kernel's occupancy.
+template <class K>
+static int persistent_blocks(K kernel, int n) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0);
+    const int full = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1);
+    const int need = (n + 127) / 128;
+    return need < full ? need : full;
+}
+
 cudaError_t launch_mf_step(const ctsmg_soilwater_io& io, int ncol, const MoistureFormArgs& P, int flexcn, int refresh,
-                           DevError* err, const int32_t* d_filt, cudaStream_t s, const HydroStepArgs* hy) {
+                           DevError* err, const int32_t* d_filt, cudaStream_t s, int* d_counter,
+                           const HydroStepArgs* hy) {
     if (ncol <= 0) return cudaSuccess;
-    if (hy)
-        mf_step_kernel<true><<<(ncol + 127) / 128, 128, 0, s>>>(io, ncol, P, flexcn, refresh, err, d_filt, *hy);
+    const int nb = (ncol + 127) / 128;
+    const HydroStepArgs none{};
+    if (hy) mf_pre_kernel<true><<<nb, 128, 0, s>>>(io, ncol, P.dtime, d_filt, *hy);
+    else mf_pre_kernel<false><<<nb, 128, 0, s>>>(io, ncol, P.dtime, d_filt, none);
+    cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    if (P.expensive)
+        mf_core_kernel<true><<<persistent_blocks(mf_core_kernel<true>, ncol), 128, 0, s>>>(io, ncol, P, err, d_filt,
+                                                                                          d_counter);
     else
-        mf_step_kernel<false><<<(ncol + 127) / 128, 128, 0, s>>>(io, ncol, P, flexcn, refresh, err, d_filt,
-                                                                HydroStepArgs{});
+        mf_core_kernel<false><<<persistent_blocks(mf_core_kernel<false>, ncol), 128, 0, s>>>(io, ncol, P, err, d_filt,
+                                                                                            d_counter);
+    if (hy) mf_post_kernel<true><<<nb, 128, 0, s>>>(io, ncol, P.dtime, flexcn, refresh, d_filt, *hy);
+    else if (flexcn || refresh) mf_post_kernel<false><<<nb, 128, 0, s>>>(io, ncol, P.dtime, flexcn, refresh, d_filt, none);
     return cudaGetLastError();
 }
 
 cudaError_t launch_moisture_form(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt,
-                                 const MoistureFormArgs& P, DevError* err, cudaStream_t s) {
+                                 const MoistureFormArgs& P, DevError* err, cudaStream_t s, int* d_counter) {
     if (nfilt <= 0) return cudaSuccess;
-    moisture_form_kernel<<<(nfilt + 127) / 128, 128, 0, s>>>(io, begc, nfilt, d_filt, P, err);
+    cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    if (P.expensive)
+        moisture_form_kernel<true><<<persistent_blocks(moisture_form_kernel<true>, nfilt), 128, 0, s>>>(
+            io, begc, nfilt, d_filt, P, err, d_counter);
+    else
+        moisture_form_kernel<false><<<persistent_blocks(moisture_form_kernel<false>, nfilt), 128, 0, s>>>(
+            io, begc, nfilt, d_filt, P, err, d_counter);
     return cudaGetLastError();
 }
 

@@ -24,11 +24,10 @@ inline int moisture_form_max_trials(double dtime, double dtmin) {
     return 2 * (int)n + 128;
 }
 
-__device__ int mf_column(const ctsmg_soilwater_io& io, int c, const MoistureFormArgs& P);
 
 // d_filt: device copy of the 1-based column filter, or NULL for begc .. begc+nfilt-1.
 cudaError_t launch_moisture_form(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt,
-                                 const MoistureFormArgs& P, DevError* err, cudaStream_t s);
+                                 const MoistureFormArgs& P, DevError* err, cudaStream_t s, int* d_counter);
 // The default hydrology around SoilWater in the resident step: per-column
 // baseflow_scalar / fff override the parameters where given.
 struct HydroStepArgs {
@@ -40,8 +39,10 @@ struct HydroStepArgs {
 
 // Resident-step form over positions 0..ncol-1 (or the 1-based position
 // filter); hy = NULL leaves the hydrology out.
+// d_counter: one int of device scratch (the persistent kernel's work counter).
 cudaError_t launch_mf_step(const ctsmg_soilwater_io& io, int ncol, const MoistureFormArgs& P, int flexcn, int refresh,
-                           DevError* err, const int32_t* d_filt, cudaStream_t s, const HydroStepArgs* hy = nullptr);
+                           DevError* err, const int32_t* d_filt, cudaStream_t s, int* d_counter,
+                           const HydroStepArgs* hy = nullptr);
 cudaError_t launch_flexcn(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt, cudaStream_t s);
 
 } // namespace ctsmg
