@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <numeric>
@@ -655,6 +656,107 @@ extern "C" int32_t ctsmg_batch_set_block(ctsmg_batch bh, int32_t block) {
         return set_error(CTSMG_E_ARG, "block must be 64, 128 or 256", 0, 0);
     bh->b->block = block;
     return build_graph(bh->b);
+}
+
+// Host copy of one component in the caller's column order.
+static int field_to_host(Batch* b, const UField& u, std::vector<char>& out) {
+    out.resize(u.bytes);
+    cudaError_t e;
+    if (!is_column_kind(u.kind)) {
+        e = cudaMemcpy(out.data(), u.dptr, u.bytes, cudaMemcpyDeviceToHost);
+    } else {
+        void* tmp = nullptr;
+        e = cudaMalloc(&tmp, u.bytes);
+        if (e == cudaSuccess) e = launch_permute(tmp, u.dptr, b->d_perm, b->cfg.ncol, kind_levels(u.kind), u.esize, 1, b->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+        if (e == cudaSuccess) e = cudaMemcpy(out.data(), tmp, u.bytes, cudaMemcpyDeviceToHost);
+        if (tmp) cudaFree(tmp);
+    }
+    return e == cudaSuccess ? 0 : cuda_err(e, "checkpoint D2H");
+}
+
+static int field_from_host(Batch* b, const UField& u, const std::vector<char>& in) {
+    cudaError_t e;
+    if (!is_column_kind(u.kind)) {
+        e = cudaMemcpy(u.dptr, in.data(), u.bytes, cudaMemcpyHostToDevice);
+    } else {
+        void* tmp = nullptr;
+        e = cudaMalloc(&tmp, u.bytes);
+        if (e == cudaSuccess) e = cudaMemcpy(tmp, in.data(), u.bytes, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = launch_permute(u.dptr, tmp, b->d_perm, b->cfg.ncol, kind_levels(u.kind), u.esize, 0, b->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+        if (tmp) cudaFree(tmp);
+    }
+    return e == cudaSuccess ? 0 : cuda_err(e, "restart H2D");
+}
+
+static const char CK_MAGIC[8] = {'C', 'T', 'S', 'M', 'G', 'C', 'K', '1'};
+
+extern "C" int32_t ctsmg_batch_save(ctsmg_batch bh, const char* path) {
+    if (!bh || !path) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
+    Batch* b = bh->b;
+    CK(cudaStreamSynchronize(b->stream), "sync");
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return set_error(CTSMG_E_ARG, "cannot open the checkpoint file for writing", 0, 0);
+    int rc = 0;
+    const int32_t head[4] = {b->cfg.ncol, b->cfg.npatch, b->cfg.ngrid, (int32_t)b->fields.size()};
+    bool ok = std::fwrite(CK_MAGIC, 1, 8, f) == 8 && std::fwrite(head, 4, 4, f) == 4;
+    std::vector<char> buf;
+    for (size_t i = 0; ok && i < b->fields.size(); ++i) {
+        const UField& u = b->fields[i];
+        if ((rc = field_to_host(b, u, buf))) break;
+        const uint16_t nl = (uint16_t)u.name.size();
+        const int32_t ke[2] = {u.kind, u.esize};
+        const int64_t nb = (int64_t)u.bytes;
+        ok = std::fwrite(&nl, 2, 1, f) == 1 && std::fwrite(u.name.data(), 1, nl, f) == nl &&
+             std::fwrite(ke, 4, 2, f) == 2 && std::fwrite(&nb, 8, 1, f) == 1 &&
+             std::fwrite(buf.data(), 1, u.bytes, f) == u.bytes;
+    }
+    if (std::fclose(f) != 0) ok = false;
+    if (rc) return rc;
+    return ok ? 0 : set_error(CTSMG_E_ARG, "writing the checkpoint file failed", 0, 0);
+}
+
+extern "C" int32_t ctsmg_batch_load(ctsmg_batch bh, const char* path) {
+    if (!bh || !path) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
+    Batch* b = bh->b;
+    CK(cudaStreamSynchronize(b->stream), "sync");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return set_error(CTSMG_E_ARG, "cannot open the checkpoint file", 0, 0);
+    auto bad = [&](const char* m) { std::fclose(f); return set_error(CTSMG_E_ARG, m, 0, 0); };
+    char magic[8];
+    int32_t head[4];
+    if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, CK_MAGIC, 8) != 0) return bad("not a checkpoint file");
+    if (std::fread(head, 4, 4, f) != 4) return bad("truncated checkpoint header");
+    if (head[0] != b->cfg.ncol || head[1] != b->cfg.npatch || head[2] != b->cfg.ngrid)
+        return bad("checkpoint sizes differ from the batch's (ncol, npatch, ngrid)");
+    std::vector<char> seen(b->fields.size(), 0), buf;
+    for (int32_t r = 0; r < head[3]; ++r) {
+        uint16_t nl;
+        int32_t ke[2];
+        int64_t nb;
+        if (std::fread(&nl, 2, 1, f) != 1) return bad("truncated checkpoint record");
+        std::string name(nl, '\0');
+        if (std::fread(&name[0], 1, nl, f) != nl || std::fread(ke, 4, 2, f) != 2 || std::fread(&nb, 8, 1, f) != 1)
+            return bad("truncated checkpoint record");
+        auto it = b->index.find(name);
+        if (it == b->index.end()) {               // a component this batch does not hold
+            if (std::fseek(f, (long)nb, SEEK_CUR) != 0) return bad("truncated checkpoint record");
+            continue;
+        }
+        const UField& u = b->fields[it->second];
+        if (ke[0] != u.kind || ke[1] != u.esize || (size_t)nb != u.bytes)
+            return bad("checkpoint component has another layout than the batch's");
+        buf.resize(u.bytes);
+        if (std::fread(buf.data(), 1, u.bytes, f) != u.bytes) return bad("truncated checkpoint data");
+        int rc = field_from_host(b, u, buf);
+        if (rc) { std::fclose(f); return rc; }
+        seen[it->second] = 1;
+    }
+    std::fclose(f);
+    for (size_t i = 0; i < seen.size(); ++i)
+        if (!seen[i]) return set_error(CTSMG_E_ARG, (std::string("checkpoint lacks component ") + b->fields[i].name).c_str(), 0, 0);
+    return 0;
 }
 
 extern "C" int64_t ctsmg_batch_state_bytes(ctsmg_batch bh) { return bh ? (int64_t)bh->b->state_bytes : 0; }

@@ -186,6 +186,16 @@ class SoilBatch:
     def set_block(self, block):
         check(self.L.ctsmg_batch_set_block(self.h, block))
 
+    def save(self, path):
+        """ctsmg_batch_save: write the resident state to a checkpoint file."""
+        self.L.ctsmg_batch_save.argtypes = [C.c_void_p, C.c_char_p]
+        check(self.L.ctsmg_batch_save(self.h, str(path).encode()))
+
+    def load(self, path):
+        """ctsmg_batch_load: restore the resident state from a checkpoint file."""
+        self.L.ctsmg_batch_load.argtypes = [C.c_void_p, C.c_char_p]
+        check(self.L.ctsmg_batch_load(self.h, str(path).encode()))
+
     def state_bytes(self):
         return int(self.L.ctsmg_batch_state_bytes(self.h))
 

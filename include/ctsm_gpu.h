@@ -810,6 +810,15 @@ int32_t ctsmg_batch_balance(ctsmg_batch b, double* errh2o_max, double* errsoi_ma
 int32_t ctsmg_batch_autotune(ctsmg_batch b, int32_t trial_steps, int32_t* block_out);
 int32_t ctsmg_batch_set_block(ctsmg_batch b, int32_t block);
 int64_t ctsmg_batch_state_bytes(ctsmg_batch b);
+/* Checkpoint / restart of a batch's resident state (the restart role of
+ * src/main/restFileMod.F90; NetCDF/PIO are absent here, so the file is a
+ * self-describing binary: the magic "CTSMGCK1", the batch sizes, then one
+ * record per component -- name, kind, element size, byte count and the
+ * array in the caller's column order and the reference's level layout).
+ * ctsmg_batch_load restores a file into a batch created with the same sizes
+ * and components; every component the batch holds must be in the file.    */
+int32_t ctsmg_batch_save(ctsmg_batch b, const char* path);
+int32_t ctsmg_batch_load(ctsmg_batch b, const char* path);
 int32_t ctsmg_batch_destroy(ctsmg_batch b);
 
 /* ---------------------------------------------------------------- serving pool */
