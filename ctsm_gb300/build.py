@@ -12,6 +12,8 @@ LIB = os.path.join(HERE, "libctsm_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
            "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
+# extra nvcc flags for tuning builds (e.g. -DCTSMG_PIPE_CHUNKS=8)
+NVFLAGS += os.environ.get("CTSMG_NVCC_EXTRA", "").split()
 
 
 def nvcc():

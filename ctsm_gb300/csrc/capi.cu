@@ -151,19 +151,31 @@ int kind_levels(int kind) {
     return 0;
 }
 
+// rows of a component the drop-in calls copy (FieldDesc::lev0 / nlev)
+static int copy_rows(const FieldDesc& f) { return f.nlev ? f.nlev : kind_levels(f.kind); }
+static size_t copy_row0(const FieldDesc& f) { return f.nlev ? (size_t)f.lev0 : 0; }
+
 #define FW(S, name, kind, esz, use) {offsetof(S, name), kind, esz, use, #name}
+// Rows of SoilWater's (Zeng-Decker) components: levels 1..nlevsoi of the
+// snow/soil and ground arrays, 1..nlevgrnd of t_soisno and zi (the frozen
+// water-table search), the snow rows not at all; the fluxes and diagnostics
+// it writes over levels 1..nlevsoi are not copied in.
+#define FWR(S, name, kind, esz, use, lev0, nlev, no_in) {offsetof(S, name), kind, esz, use, #name, lev0, nlev, no_in}
+#define SWR(name, kind, use, lev0, nlev, no_in) FWR(ctsmg_soilwater_io, name, kind, 8, use, lev0, nlev, no_in)
+constexpr int SS1 = 1 - (-NLEVSNO + 1);    // row of level 1 in a [SS] array
+constexpr int ZI1 = 1 + NLEVSNO;           // row of level 1 in a [ZI] array
 const FieldDesc SOILWATER_TABLE[] = {
-    FW(ctsmg_soilwater_io, z, K_SS, 8, U_IN), FW(ctsmg_soilwater_io, zi, K_ZI, 8, U_IN),
-    FW(ctsmg_soilwater_io, dz, K_SS, 8, U_IN), FW(ctsmg_soilwater_io, zwt, K_C, 8, U_IN),
-    FW(ctsmg_soilwater_io, qcharge, K_C, 8, U_OUT), FW(ctsmg_soilwater_io, icefrac, K_G, 8, U_OUT),
-    FW(ctsmg_soilwater_io, qin, K_S, 8, U_OUT), FW(ctsmg_soilwater_io, qout, K_S, 8, U_OUT),
-    FW(ctsmg_soilwater_io, smpmin, K_C, 8, U_IN), FW(ctsmg_soilwater_io, watsat, K_G, 8, U_IN),
-    FW(ctsmg_soilwater_io, hksat, K_G, 8, U_IN), FW(ctsmg_soilwater_io, bsw, K_G, 8, U_IN),
-    FW(ctsmg_soilwater_io, sucsat, K_G, 8, U_IN), FW(ctsmg_soilwater_io, smp_l, K_G, 8, U_OUT),
-    FW(ctsmg_soilwater_io, hk_l, K_G, 8, U_OUT), FW(ctsmg_soilwater_io, h2osoi_ice, K_SS, 8, U_IN),
-    FW(ctsmg_soilwater_io, h2osoi_liq, K_SS, 8, U_INOUT), FW(ctsmg_soilwater_io, h2osoi_vol, K_G, 8, U_IN),
-    FW(ctsmg_soilwater_io, qflx_deficit, K_C, 8, U_OUT), FW(ctsmg_soilwater_io, qflx_infl, K_C, 8, U_IN),
-    FW(ctsmg_soilwater_io, qflx_rootsoi, K_S, 8, U_IN), FW(ctsmg_soilwater_io, t_soisno, K_SS, 8, U_IN),
+    SWR(z, K_SS, U_IN, SS1, NLEVSOI, 0), SWR(zi, K_ZI, U_IN, ZI1, NLEVGRND, 0),
+    SWR(dz, K_SS, U_IN, SS1, NLEVSOI, 0), SWR(zwt, K_C, U_IN, 0, 0, 0),
+    SWR(qcharge, K_C, U_OUT, 0, 0, 1), SWR(icefrac, K_G, U_OUT, 0, NLEVSOI, 1),
+    SWR(qin, K_S, U_OUT, 0, 0, 1), SWR(qout, K_S, U_OUT, 0, 0, 1),
+    SWR(smpmin, K_C, U_IN, 0, 0, 0), SWR(watsat, K_G, U_IN, 0, NLEVSOI, 0),
+    SWR(hksat, K_G, U_IN, 0, NLEVSOI, 0), SWR(bsw, K_G, U_IN, 0, NLEVSOI, 0),
+    SWR(sucsat, K_G, U_IN, 0, NLEVSOI, 0), SWR(smp_l, K_G, U_OUT, 0, NLEVSOI, 1),
+    SWR(hk_l, K_G, U_OUT, 0, NLEVSOI, 1), SWR(h2osoi_ice, K_SS, U_IN, SS1, NLEVSOI, 0),
+    SWR(h2osoi_liq, K_SS, U_INOUT, SS1, NLEVSOI, 0), SWR(h2osoi_vol, K_G, U_IN, 0, NLEVSOI, 0),
+    SWR(qflx_deficit, K_C, U_OUT, 0, 0, 1), SWR(qflx_infl, K_C, U_IN, 0, 0, 0),
+    SWR(qflx_rootsoi, K_S, U_IN, 0, 0, 0), SWR(t_soisno, K_SS, U_IN, SS1, NLEVGRND, 0),
 };
 const int SOILWATER_NFIELDS = sizeof(SOILWATER_TABLE) / sizeof(SOILWATER_TABLE[0]);
 
@@ -703,8 +715,12 @@ static int stage_in(ThreadCtx* c, const void* hio, void* dio, size_t io_size, co
         }
         size_t nb = field_bytes(tab[i], ldc, ldp, ldg);
         void* dp = arena_take(c, nb);
-        cudaError_t e = cudaMemcpyAsync(dp, hp, nb, cudaMemcpyHostToDevice, c->stream);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync H2D");
+        if (!tab[i].no_in) {
+            const size_t row = nb / kind_levels(tab[i].kind), off = copy_row0(tab[i]) * row;
+            cudaError_t e = cudaMemcpyAsync(static_cast<char*>(dp) + off, static_cast<const char*>(hp) + off,
+                                            copy_rows(tab[i]) * row, cudaMemcpyHostToDevice, c->stream);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync H2D");
+        }
         field_ptr(dio, tab[i]) = dp;
     }
     return 0;
@@ -716,7 +732,10 @@ static int stage_out(ThreadCtx* c, const void* hio, const void* dio, const Field
         if (tab[i].use == U_IN) continue;
         void* hp = field_ptr(const_cast<void*>(hio), tab[i]);
         const void* dp = field_ptr(const_cast<void*>(dio), tab[i]);
-        cudaError_t e = cudaMemcpyAsync(hp, dp, field_bytes(tab[i], ldc, ldp, ldg), cudaMemcpyDeviceToHost, c->stream);
+        const size_t nb = field_bytes(tab[i], ldc, ldp, ldg), row = nb / kind_levels(tab[i].kind),
+                     off = copy_row0(tab[i]) * row;
+        cudaError_t e = cudaMemcpyAsync(static_cast<char*>(hp) + off, static_cast<const char*>(dp) + off,
+                                        copy_rows(tab[i]) * row, cudaMemcpyDeviceToHost, c->stream);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync D2H");
     }
     return 0;
@@ -783,8 +802,9 @@ static cudaError_t copy_slice(const FieldDesc& f, void* dst, const void* src, in
                               cudaMemcpyKind kind, cudaStream_t s) {
     if (hi <= lo) return cudaSuccess;
     const size_t es = f.esize, pitch = (size_t)ld * es, w = (size_t)(hi - lo) * es;
-    return cudaMemcpy2DAsync(static_cast<char*>(dst) + lo * es, pitch, static_cast<const char*>(src) + lo * es, pitch,
-                             w, kind_levels(f.kind), kind, s);
+    const size_t off = copy_row0(f) * pitch + lo * es;
+    return cudaMemcpy2DAsync(static_cast<char*>(dst) + off, pitch, static_cast<const char*>(src) + off, pitch,
+                             w, copy_rows(f), kind, s);
 }
 
 static bool patch_field(const FieldDesc& f) { return f.kind == K_P || f.kind == K_PL || f.kind == K_PS || f.kind == K_PG; }
@@ -801,6 +821,7 @@ static int chunk_in(ThreadCtx* c, const Chunk& ch, int k, const void* hio, const
                     int nf, int ldc, int ldp) {
     for (int i = 0; i < nf; ++i) {
         const FieldDesc& f = tab[i];
+        if (f.no_in) continue;
         const bool pf = patch_field(f);
         cudaError_t e = copy_slice(f, field_ptr(const_cast<void*>(dio), f), field_ptr(const_cast<void*>(hio), f),
                                    pf ? ldp : ldc, pf ? ch.p0 : ch.c0, pf ? ch.p1 : ch.c1, cudaMemcpyHostToDevice,
@@ -992,7 +1013,13 @@ extern "C" int32_t ctsmg_soilwater(const ctsmg_bounds* bounds, int32_t num_hydro
         nml = g_swm;
         e_ice = g_swp.e_ice;
     }
-    const std::vector<FieldDesc> tab = soilwater_fields(nml);
+    std::vector<FieldDesc> tab = soilwater_fields(nml);
+    // outputs are left uncopied on the way in only when the filter covers
+    // every column of the bounds (columns outside it keep their values)
+    bool dense = num_hydrologyc == ncol;
+    for (int i = 0; dense && i < num_hydrologyc; ++i) dense = filter_hydrologyc[i] == bounds->begc + i;
+    if (!dense)
+        for (auto& f : tab) f.no_in = 0;
     const FieldDesc* T = tab.data();
     const int NT = (int)tab.size();
     for (const FieldDesc& f : tab)

@@ -7,7 +7,13 @@
 namespace ctsmg {
 enum Kind { K_C, K_P, K_SS, K_ZI, K_G, K_S, K_SN, K_PL, K_GR, K_PS, K_PG };
 enum Use { U_IN, U_OUT, U_INOUT };
-struct FieldDesc { size_t offset; int kind; int esize; int use; const char* name; };
+// A component of an io struct.  The drop-in calls copy rows [lev0, lev0 +
+// nlev) of its storage (nlev = 0: every row), and skip the copy-in when
+// no_in is set (an output the call writes over that whole range).
+struct FieldDesc {
+    size_t offset; int kind; int esize; int use; const char* name;
+    int lev0 = 0, nlev = 0, no_in = 0;
+};
 
 extern const FieldDesc SOILWATER_TABLE[];
 extern const int SOILWATER_NFIELDS;
