@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include "ctsm_device.cuh"
+#include "fastmath.cuh"
 #include "canopy_kernels.cuh"
 #include "rootfind.cuh"
 #include "qsat.cuh"
@@ -73,9 +74,9 @@ __device__ __forceinline__ bool quadratic(double a, double b, double c, double& 
 // sites (FrictionVelocity, the stability functions, Photosynthesis): the
 // iterating kernel holds one copy of each instead of an inline expansion per
 // call site.  The functions are CUDA's own; only where their code sits changes.
-__device__ __noinline__ double xlog(double x) { return log(x); }
-__device__ __noinline__ double xexp(double x) { return exp(x); }
-__device__ __noinline__ double xpow(double x, double y) { return pow(x, y); }
+__device__ __noinline__ double xlog(double x) { return fm::log(x); }
+__device__ __noinline__ double xexp(double x) { return fm::exp(x); }
+__device__ __noinline__ double xpow(double x, double y) { return fm::pow(x, y); }
 __device__ __noinline__ double xatan(double x) { return atan(x); }
 
 // FrictionVelocityMod.F90:1120-1155

@@ -37,7 +37,7 @@ __device__ __forceinline__ double mn(double a, double b) { return (b < a) ? b : 
 __device__ __forceinline__ void saturated_excess_runoff(const ctsmg_hydrology_io& io, int c, double fff) {
     const double zt = (io.frost_table[c] > io.zwt_perched[c] && io.frost_table[c] <= io.zwt[c]) ? io.zwt_perched[c]
                                                                                                  : io.zwt[c];
-    const double fsat = io.wtfact[c] * exp(-0.5 * fff * zt);
+    const double fsat = io.wtfact[c] * fm::exp(-0.5 * fff * zt);
     io.fsat[c] = fsat;
     io.qflx_sat_excess_surf[c] = fsat * io.qflx_rain_plus_snomelt[c];
     io.fcov[c] = fsat;
@@ -89,7 +89,7 @@ __device__ __forceinline__ void infiltration_chain(const ctsmg_hydrology_io& io,
     double frac_infclust = 0.0;
     if (P.h2osfcflag == 1) {
         const double fn = io.frac_h2osfc_nosnow[c];
-        frac_infclust = (fn <= P.pc) ? 0.0 : pow(fn - P.pc, P.mu);
+        frac_infclust = (fn <= P.pc) ? 0.0 : fm::pow(fn - P.pc, P.mu);
     }
     double surf;
     if (h0 > thr && P.h2osfcflag != 0) {
@@ -186,7 +186,7 @@ __device__ __forceinline__ void theta_based_water_table(const ctsmg_hydrology_io
 __device__ __forceinline__ double specific_yield(const ctsmg_hydrology_io& io, const View& v, int k, double depth,
                                                  double aq_sp_yield_min) {
     const double s_y = io.watsat[v.g(k)] *
-                       (1.0 - pow(1.0 + 1.e3 * depth / io.sucsat[v.g(k)], -1.0 / io.bsw[v.g(k)]));
+                       (1.0 - fm::pow(1.0 + 1.e3 * depth / io.sucsat[v.g(k)], -1.0 / io.bsw[v.g(k)]));
     return mx(s_y, aq_sp_yield_min);
 }
 
@@ -260,7 +260,7 @@ __device__ __forceinline__ void subsurface_lateral_flow(const ctsmg_hydrology_io
     double latflow_out = 0.0;
     const double zib = v.zi(nb);
     if (zwt <= zib)
-        latflow_out = ice_imped_col * P.baseflow_scalar * tan(RPI / 180.0 * io.topo_slope[c]) * pow(zib - zwt, P.n_baseflow);
+        latflow_out = ice_imped_col * P.baseflow_scalar * tan(RPI / 180.0 * io.topo_slope[c]) * fm::pow(zib - zwt, P.n_baseflow);
     io.qflx_latflow_out[c] = latflow_out;
     io.qflx_latflow_in[c] = 0.0;
     const double net = latflow_out - 0.0;
@@ -518,7 +518,7 @@ __device__ __forceinline__ void drainage(const ctsmg_hydrology_io& io, int c, co
         }
         const double imped = pow10_dd(-P.e_ice * (icefracsum / dzsum));
         const double rsub_top_max = 10.0 * sin((RPI / 180.0) * io.topo_slope[c]);
-        rsub_top = imped * rsub_top_max * exp(-fff * zwt);
+        rsub_top = imped * rsub_top_max * fm::exp(-fff * zwt);
         const double rous = specific_yield(io, v, NLEVSOI, zwt, P.aq_sp_yield_min);
         if (jwt == NLEVSOI) {
             double wa = io.wa[c] - rsub_top * dtime;

@@ -47,7 +47,7 @@ struct ColView {
 // division by watsat is compute_hydraulic_properties' :1540)
 __device__ __forceinline__ void suction(const ColView& k, int j, double s2, double& smp, double& dsmpdw) {
     const double bsw = k.g(k.io.bsw, j);
-    smp = -k.g(k.io.sucsat, j) * pow(s2, -bsw);
+    smp = -k.g(k.io.sucsat, j) * fm::pow(s2, -bsw);
     const double dsmpds = -bsw * smp / s2;
     dsmpdw = dsmpds / k.g(k.io.watsat, j);
 }
@@ -143,7 +143,7 @@ __device__ int mf_trial(MFLane<EXPENSIVE>& L, const ctsmg_soilwater_io& io, cons
         s1 = fmn(s1, 1.0);
         s1 = fmx(0.01, s1);
         const double ws = k.g(io.watsat, j), bsw = k.g(io.bsw, j);
-        const double hkj = imped * k.g(io.hksat, j) * pow(s1, 2.0 * bsw + 3.0);
+        const double hkj = imped * k.g(io.hksat, j) * fm::pow(s1, 2.0 * bsw + 3.0);
         const double dhkdw = (2.0 * bsw + 3.0) * hkj / s1;
         io.smp_l[L.c + (j - 1) * ld] = smp_c;
         io.hk_l[L.c + (j - 1) * ld] = hkj;
@@ -292,7 +292,7 @@ __device__ void mf_finish(MFLane<EXPENSIVE>& L, const ctsmg_soilwater_io& io, co
         const double wh_zwt = -k.g(io.sucsat, jwt + 1) - zwt * M_TO_MM;
         double s1 = fmx(L.vwc_q / k.g(io.watsat, jwt + 1), 0.01);
         s1 = fmn(1.0, s1);
-        const double ka = L.imped_q * k.g(io.hksat, jwt + 1) * pow(s1, 2.0 * k.g(io.bsw, jwt + 1) + 3.0);
+        const double ka = L.imped_q * k.g(io.hksat, jwt + 1) * fm::pow(s1, 2.0 * k.g(io.bsw, jwt + 1) + 3.0);
         const int jm = jwt > 1 ? jwt : 1;
         const double smp1 = fmx(io.smpmin[c], io.smp_l[c + (size_t)(jm - 1) * k.ld]);
         const double wh = smp1 - k.ss(io.z, jm) * M_TO_MM;

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include "ctsm_device.cuh"
+#include "fastmath.cuh"
 #include "rootmoist_kernels.cuh"
 
 namespace ctsmg {
@@ -34,7 +35,7 @@ __global__ void rootmoist_kernel(ctsmg_rootmoist_io io, ctsmg_pftcon pft, int be
             io.rootr[pg] = 0.0;
         } else {
             const double s_node = fmax(liqvol / eff, 0.01);
-            double smp = -io.sucsat[g] * pow(s_node, -io.bsw[g]);
+            double smp = -io.sucsat[g] * fm::pow(s_node, -io.bsw[g]);
             smp = fmax(smpsc, smp);
             const double rr = fmin((eff / ws) * (smp - smpsc) / (smpso - smpsc), 1.0);
             io.rresis[pg] = rr;

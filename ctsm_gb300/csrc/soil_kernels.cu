@@ -71,7 +71,7 @@ __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, d
                 const double t = SS(io.t_soisno, j);
                 double smp1 = HFUS * (TFRZ - t) / (GRAV * t) * 1000.0;
                 smp1 = fmax(G(io.sucsat, NLEVSOI), smp1);
-                vwc_zwt = G(io.watsat, NLEVSOI) * pow(smp1 / G(io.sucsat, NLEVSOI), -1.0 / G(io.bsw, NLEVSOI));
+                vwc_zwt = G(io.watsat, NLEVSOI) * fm::pow(smp1 / G(io.sucsat, NLEVSOI), -1.0 / G(io.bsw, NLEVSOI));
                 vwc_zwt = fmin(vwc_zwt, sp(0.5f) * (G(io.watsat, NLEVSOI) + G(io.h2osoi_vol, NLEVSOI)));
                 break;
             }
@@ -87,8 +87,8 @@ __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, d
         const bool above = zwtmm <= zimm[j - 1];
         const bool inside = !above && (zwtmm < zimm[j]) && (zwtmm > zimm[j - 1]);
         double temp0 = 0.0, tempi = 1.0;
-        if (!above) temp0 = pow(((ss + zwtmm - zimm[j - 1]) / ss), 1.0 - 1.0 / bb);
-        if (!above && !inside) tempi = pow(((ss + zwtmm - zimm[j]) / ss), 1.0 - 1.0 / bb);
+        if (!above) temp0 = fm::pow(((ss + zwtmm - zimm[j - 1]) / ss), 1.0 - 1.0 / bb);
+        if (!above && !inside) tempi = fm::pow(((ss + zwtmm - zimm[j]) / ss), 1.0 - 1.0 / bb);
         double veq;
         if (above) {
             veq = ws;
@@ -102,18 +102,18 @@ __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, d
             veq = fmax(veq, 0.0);
             veq = fmin(ws, veq);
         }
-        double q = -ss * pow(fmax(veq / ws, 0.01), -bb);
+        double q = -ss * fm::pow(fmax(veq / ws, 0.01), -bb);
         zq[j] = fmax(smpmin, q);
     }
     if (jwt == NLEVSOI) {
         const int j = NLEVSOI;
         const double ss = G(io.sucsat, j), ws = G(io.watsat, j), bb = G(io.bsw, j);
         double tempi = 1.0;
-        double temp0 = pow(((ss + zwtmm - zimm[j]) / ss), 1.0 - 1.0 / bb);
+        double temp0 = fm::pow(((ss + zwtmm - zimm[j]) / ss), 1.0 - 1.0 / bb);
         double veq = -ss * ws / (1.0 - 1.0 / bb) / (zwtmm - zimm[j]) * (tempi - temp0);
         veq = fmax(veq, 0.0);
         veq = fmin(ws, veq);
-        double q = -ss * pow(fmax(veq / ws, 0.01), -bb);
+        double q = -ss * fm::pow(fmax(veq / ws, 0.01), -bb);
         zq[j + 1] = fmax(smpmin, q);
     }
 #pragma unroll 1
@@ -122,13 +122,13 @@ __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, d
         const double wsj = G(io.watsat, j), wsp = G(io.watsat, jp), bb = G(io.bsw, j);
         double s1 = 0.5 * (vwc_liq[j] + vwc_liq[jp]) / (0.5 * (wsj + wsp));
         s1 = fmin(1.0, s1);
-        double s2 = G(io.hksat, j) * pow(s1, 2.0 * bb + 2.0);
+        double s2 = G(io.hksat, j) * fm::pow(s1, 2.0 * bb + 2.0);
         imped[j] = pow10_dd(-e_ice * (0.5 * (icef[j] + icef[jp])));
         hk[j] = imped[j] * s1 * s2;
         dhkdw[j] = imped[j] * (2.0 * bb + 3.0) * s2 * (1.0 / (wsj + wsp));
         double s_node = fmax(vwc_liq[j] / wsj, 0.01);
         s_node = fmin(1.0, s_node);
-        double sm = -G(io.sucsat, j) * pow(s_node, -bb);
+        double sm = -G(io.sucsat, j) * fm::pow(s_node, -bb);
         sm = fmax(smpmin, sm);
         smp[j] = sm;
         dsmpdw[j] = -bb * sm / vwc_liq[j];
@@ -200,7 +200,7 @@ __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, d
             const double ws = G(io.watsat, j), bb = G(io.bsw, j);
             double s_node = fmax(sp(0.5f) * ((vwc_zwt + vwc_liq[j]) / ws), 0.01);
             s_node = fmin(1.0, s_node);
-            double smp1 = -G(io.sucsat, j) * pow(s_node, -bb);
+            double smp1 = -G(io.sucsat, j) * fm::pow(s_node, -bb);
             smp1 = fmax(smpmin, smp1);
             double dsmpdw1 = -bb * smp1 / (s_node * ws);
             den = (zmm[j + 1] - zmm[j]);
@@ -251,7 +251,7 @@ __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, d
         const int jq = jwt + 1;
         double s_node = fmax(G(io.h2osoi_vol, jq) / G(io.watsat, jq), 0.01);
         double s1 = fmin(1.0, s_node);
-        double ka = imped[jq] * G(io.hksat, jq) * pow(s1, 2.0 * G(io.bsw, jq) + 3.0);
+        double ka = imped[jq] * G(io.hksat, jq) * fm::pow(s1, 2.0 * G(io.bsw, jq) + 3.0);
         const int jm = max(1, jwt);
         double smp1 = fmax(smpmin, smp[jm]);
         double wh = smp1 - zq[jm];
@@ -316,7 +316,7 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
                 double satw = (liq / DENH2O + ice / DENICE + 0.0 / DENICE) / (dzj * ws);
                 satw = fmin(1.0, satw);
                 if (satw > .1e-6) {
-                    double dke = (T[ssi(j)] >= TFRZ) ? fmax(0.0, log10(satw) + 1.0) : satw;
+                    double dke = (T[ssi(j)] >= TFRZ) ? fmax(0.0, fm::log10(satw) + 1.0) : satw;
                     double fl = (liq / (DENH2O * dzj)) / (liq / (DENH2O * dzj) + ice / (DENICE * dzj) + 0.0 / (DENICE * dzj));
                     double dksat = io.tkmg[gi(j)] * tkwat_tkice_pow(fl * ws, (1.0 - fl) * ws);
                     t = dke * dksat + (1.0 - dke) * io.tkdry[gi(j)];
@@ -705,7 +705,7 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
             if (wice0 > 0. && tj > TFRZ) { imelt = 1; tinc = TFRZ - tj; tj = TFRZ; }
             if (tj < TFRZ) {
                 double smp = HFUS * (TFRZ - tj) / (GRAV * tj) * 1000.0;
-                supercool = io.watsat[gi(j)] * pow(smp / io.sucsat[gi(j)], -1.0 / io.bsw[gi(j)]);
+                supercool = io.watsat[gi(j)] * fm::pow(smp / io.sucsat[gi(j)], -1.0 / io.bsw[gi(j)]);
                 supercool = supercool * DZ(j) * 1000.0;
             }
             if (wliq0 > supercool && tj < TFRZ) { imelt = 2; tinc = TFRZ - tj; tj = TFRZ; }
@@ -1144,7 +1144,39 @@ __global__ void diag_powers_kernel(int n, const double* __restrict__ a, const do
     out[2 * (size_t)n + i] = pow(TKWAT, a[i]) * pow(TKICE, b[i]);
     out[3 * (size_t)n + i] = tkwat_tkice_pow(a[i], b[i]);
 }
+__global__ void diag_fastmath_kernel(int n, const double* __restrict__ x, const double* __restrict__ y,
+                                     double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t N = (size_t)n;
+    out[i] = fm::log(x[i]);
+    out[N + i] = fm::log10(x[i]);
+    out[2 * N + i] = fm::exp(y[i]);
+    out[3 * N + i] = fm::pow(x[i], y[i]);
+    out[4 * N + i] = log(x[i]);
+    out[5 * N + i] = log10(x[i]);
+    out[6 * N + i] = exp(y[i]);
+    out[7 * N + i] = pow(x[i], y[i]);
+}
 } // namespace ctsmg
+
+extern "C" int32_t ctsmg_diag_fastmath(int32_t n, const double* x, const double* y, double* out) {
+    using namespace ctsmg;
+    if (n <= 0 || !x || !y || !out) return set_error(CTSMG_E_ARG, "bad arguments", 0, 0);
+    double* d = nullptr;
+    const size_t nb = (size_t)n * 8;
+    cudaError_t e = cudaMalloc(&d, 10 * nb);
+    if (e == cudaSuccess) e = cudaMemcpy(d, x, nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d + n, y, nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        diag_fastmath_kernel<<<(n + 127) / 128, 128>>>(n, d, d + n, d + 2 * (size_t)n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * (size_t)n, 8 * nb, cudaMemcpyDeviceToHost);
+    if (d) cudaFree(d);
+    if (e != cudaSuccess) return set_error(CTSMG_E_CUDA, cudaGetErrorString(e), 0, 0);
+    return 0;
+}
 
 extern "C" int32_t ctsmg_diag_powers(int32_t n, const double* a, const double* b, double* out) {
     using namespace ctsmg;

@@ -1,23 +1,21 @@
 // soil_math.cuh -- constant-base powers shared by the soil-water and heat kernels.
 #pragma once
 #include <cuda_runtime.h>
+#include "fastmath.cuh"
 
 namespace ctsmg {
 
 // Powers with a constant base, as exp of a double-double exponent: the
 // product x*ln(base) is formed exactly as hi + lo (FMA error term, Dekker's
 // product; ln(base) split into its nearest double and the remainder), and
-// exp(hi + lo) = exp(hi) (1 + lo) + O(lo^2).  The result carries exp's
-// rounding only, within about 1 ulp of the exact power -- as close as pow
-// itself, for one exp instead of one pow per factor.
+// exp(hi + lo) is the table-driven exponential with the low part carried into
+// its reduced argument.  The result is within about half an ulp of the exact
+// power, for one exponential instead of one pow per factor.
 constexpr double LN10_HI = 2.302585092994046, LN10_LO = -2.1707562233822494e-16;
 constexpr double LN_TKWAT_HI = -0.5621189181535413, LN_TKWAT_LO = 1.1409357209435452e-17;   // ln(0.57)
 constexpr double LN_TKICE_HI = 0.8285518175661483, LN_TKICE_LO = 3.2758189660989295e-17;    // ln(2.290)
 
-__device__ __forceinline__ double exp_dd(double hi, double lo) {
-    const double r = exp(hi);
-    return fma(r, lo, r);
-}
+__device__ __forceinline__ double exp_dd(double hi, double lo) { return fm::exp_dd(hi, lo); }
 
 // 10^x (IceImpedance, SoilWaterMovementMod.F90:2139-2160)
 __device__ __forceinline__ double pow10_dd(double x) {

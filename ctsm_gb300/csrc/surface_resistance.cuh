@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include "ctsm_gpu.h"
 #include "ctsm_device.cuh"
+#include "fastmath.cuh"
 
 namespace ctsmg {
 
@@ -25,10 +26,10 @@ __device__ __forceinline__ void soilevap_resis_column(const ctsmg_soilresis_io& 
         const double vi = io.h2osoi_ice[s1] / (dz * DENICE);
         const double eff_por_top = fmax(0.01, ws - ((vi < ws) ? vi : ws));
         const double bsw = io.bsw[g1];
-        const double aird = ws * pow(io.sucsat[g1] / 1.e7, 1.0 / bsw);
-        const double d0 = (double)2.12e-5f * pow(io.t_soisno[s1] / (double)273.15f, 1.75);
+        const double aird = ws * fm::pow(io.sucsat[g1] / 1.e7, 1.0 / bsw);
+        const double d0 = (double)2.12e-5f * fm::pow(io.t_soisno[s1] / (double)273.15f, 1.75);
         const double eps = ws - aird;
-        const double dg = eps * d0 * pow(eps / ws, 3.0 / fmax(3.0, bsw));
+        const double dg = eps * d0 * fm::pow(eps / ws, 3.0 / fmax(3.0, bsw));
         double dsl = a.d_max * fmax(0.001, (a.frac_sat_soil_dsl_init * eff_por_top - vwc_liq)) /
                      fmax(0.001, (a.frac_sat_soil_dsl_init * ws - aird));
         dsl = fmax(dsl, 0.0);

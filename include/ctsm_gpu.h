@@ -894,6 +894,13 @@ int32_t ctsmg_measure_fp64_tflops(double* tflops);
  * pow(tkwat, a[i]) * pow(tkice, b[i]) and out[3n+i] = the exp form of that
  * product.  Host arrays; out holds 4n doubles. */
 int32_t ctsmg_diag_powers(int32_t n, const double* a, const double* b, double* out);
+/* Diagnostic for the tests (no reference counterpart): the table-driven
+ * logarithm, exponential and power of the column kernels beside CUDA's.  For
+ * each i: out[i] = log(x[i]), out[n+i] = log10(x[i]), out[2n+i] = exp(y[i]),
+ * out[3n+i] = pow(x[i], y[i]) by the kernels' forms, and out[4n+i] ..
+ * out[7n+i] the same four by the CUDA math library.  Host arrays; out holds
+ * 8n doubles. */
+int32_t ctsmg_diag_fastmath(int32_t n, const double* x, const double* y, double* out);
 
 #ifdef __cplusplus
 }
