@@ -11,16 +11,16 @@ NLEVSNO, NLEVSOI, NLEVGRND = abi.NLEVSNO, abi.NLEVSOI, abi.NLEVGRND
 # from the ncu capture of 65,536 columns of the same workload, and DRAM bytes
 # per column-step from the 1-pass capture of the full 524,288-column launch;
 # both summarised in profiles/soilstep_kernel_uneven_columns.md.
-FLOPS_PER_COLUMN_STEP = (302494944 + 180903465 + 2 * 779430043) / 65536.0
-TRAFFIC_PER_COLUMN_STEP = (6585233152 + 4161359616) / 524288.0
+FLOPS_PER_COLUMN_STEP = (148978105 + 162750456 + 2 * 608026028) / 65536.0
+TRAFFIC_PER_COLUMN_STEP = (6665794560 + 4179119872) / 524288.0
 
 # FP64 floating-point operations per CanopyFluxes pass of one patch
 # (canopy_iterate_kernel: DADD + DMUL + 2 x DFMA executed over 262,144 patches
-# of the canopy workload, 6.266 passes per patch on average), and DRAM bytes
+# of the canopy workload, 5.508 passes per patch on average), and DRAM bytes
 # per patch-step of that kernel from the 1-pass capture of the full
 # 2,097,152-patch launch (profiles/canopy_iterate_kernel_canopy_workload.md).
-CANOPY_FLOPS_PER_PASS = (739121234 + 1058410707 + 2 * 3057904378) / (262144 * 6.266)
-CANOPY_TRAFFIC_PER_PATCH_STEP = (41889384704 + 15773437184) / 2097152.0
+CANOPY_FLOPS_PER_PASS = (489099825 + 889105990 + 2 * 2293152799) / (262144 * 5.507728576660156)
+CANOPY_TRAFFIC_PER_PATCH_STEP = (39389850624 + 15903046144) / 2097152.0
 
 
 def _active_levels(kind, nsnow):
