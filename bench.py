@@ -205,6 +205,18 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def copied_bytes(reset=False):
+    """Host<->device bytes the drop-in entry points copied since the last
+    reset, as counted by the library at each copy."""
+    import ctypes as C
+    from ctsm_gb300 import _lib
+    L = _lib.load()
+    L.ctsmg_copy_bytes.argtypes = [C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_int32]
+    h2d, d2h = C.c_int64(0), C.c_int64(0)
+    _lib.check(L.ctsmg_copy_bytes(C.byref(h2d), C.byref(d2h), 1 if reset else 0))
+    return h2d.value, d2h.value
+
+
 # ---------------------------------------------------------------- arms
 def reference_arm(args, ws, rank):
     if rank != 0:
@@ -273,15 +285,15 @@ def canopy_leg(args, barrier):
         canopy.CanopyFluxes(bnd, npatch, filt, H, DT, ngrid)
         barrier()
         k = 3
+        copied_bytes(reset=True)
         t0 = time.perf_counter()
         for _ in range(k):
             canopy.CanopyFluxes(bnd, npatch, filt, H, DT, ngrid)
         barrier()
         te = (time.perf_counter() - t0) / k
-        h2d = sum(H[n].nbytes for (n, kk, t, u) in abi.CANOPY_FIELDS)
-        d2h = sum(H[n].nbytes for (n, kk, t, u) in abi.CANOPY_FIELDS if u != "in")
+        h2d, d2h = copied_bytes()
         out["e2e"] = {"value": npatch / te, "unit": "patch-steps/s", "ms_per_call": 1e3 * te,
-                      "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                      "h2d_bytes_per_step": h2d // k, "d2h_bytes_per_step": d2h // k,
                       "path": "ctsmg_canopyfluxes (plain drop-in, pinned host arrays)"}
     return out
 
@@ -494,15 +506,16 @@ def ours_arm(args, ws, rank, local):
             soil.SoilWater(bnd, ncol, filt, H, DT)
             soil.SoilTemperature(bnd, ncol, filt, H, DT)
         barrier()
+        copied_bytes(reset=True)
         t0 = time.perf_counter()
         for _ in range(ke):
             soil.SoilWater(bnd, ncol, filt, H, DT)
             soil.SoilTemperature(bnd, ncol, filt, H, DT)
         barrier()
         te = max_over_ranks(time.perf_counter() - t0, ws, "cuda")
-        h2d, d2h = roofline.dropin_copy_bytes_per_column(1.0)
-        e2e = {"value": job_value(ws, ncol, ke, te), "unit": UNIT, "h2d_bytes_per_step": int(h2d * ncol),
-               "d2h_bytes_per_step": int(d2h * ncol), "steps": ke, "ms_per_step": 1e3 * te / ke,
+        h2d, d2h = copied_bytes()
+        e2e = {"value": job_value(ws, ncol, ke, te), "unit": UNIT, "h2d_bytes_per_step": h2d // ke,
+               "d2h_bytes_per_step": d2h // ke, "steps": ke, "ms_per_step": 1e3 * te / ke,
                "path": "ctsmg_soilwater + ctsmg_soiltemperature (plain drop-in, pinned host arrays)"}
 
     # ---------------- CPU baseline (rank 0 only, N = 1 only)

@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <atomic>
 #include <algorithm>
 #include <string>
 #include <vector>
@@ -24,6 +25,28 @@
 #include "capi_internal.h"
 
 namespace ctsmg {
+
+// ------------------------------------------------------------ copy accounting
+// Host<->device bytes moved by the entry points of this file, for
+// ctsmg_copy_bytes (every copy below goes through these three).
+static std::atomic<int64_t> g_h2d_bytes{0}, g_d2h_bytes{0};
+static void count_copy(cudaMemcpyKind k, size_t n) {
+    if (k == cudaMemcpyHostToDevice) g_h2d_bytes += (int64_t)n;
+    else if (k == cudaMemcpyDeviceToHost) g_d2h_bytes += (int64_t)n;
+}
+static cudaError_t copy_async(void* dst, const void* src, size_t n, cudaMemcpyKind k, cudaStream_t s) {
+    count_copy(k, n);
+    return cudaMemcpyAsync(dst, src, n, k, s);
+}
+static cudaError_t copy_2d_async(void* dst, size_t dpitch, const void* src, size_t spitch, size_t w, size_t h,
+                                 cudaMemcpyKind k, cudaStream_t s) {
+    count_copy(k, w * h);
+    return cudaMemcpy2DAsync(dst, dpitch, src, spitch, w, h, k, s);
+}
+static cudaError_t copy_sync(void* dst, const void* src, size_t n, cudaMemcpyKind k) {
+    count_copy(k, n);
+    return cudaMemcpy(dst, src, n, k);
+}
 
 // ------------------------------------------------------------ global state
 static std::mutex g_mu;
@@ -717,7 +740,7 @@ static int stage_in(ThreadCtx* c, const void* hio, void* dio, size_t io_size, co
         void* dp = arena_take(c, nb);
         if (!tab[i].no_in) {
             const size_t row = nb / kind_levels(tab[i].kind), off = copy_row0(tab[i]) * row;
-            cudaError_t e = cudaMemcpyAsync(static_cast<char*>(dp) + off, static_cast<const char*>(hp) + off,
+            cudaError_t e = copy_async(static_cast<char*>(dp) + off, static_cast<const char*>(hp) + off,
                                             copy_rows(tab[i]) * row, cudaMemcpyHostToDevice, c->stream);
             if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync H2D");
         }
@@ -734,7 +757,7 @@ static int stage_out(ThreadCtx* c, const void* hio, const void* dio, const Field
         const void* dp = field_ptr(const_cast<void*>(dio), tab[i]);
         const size_t nb = field_bytes(tab[i], ldc, ldp, ldg), row = nb / kind_levels(tab[i].kind),
                      off = copy_row0(tab[i]) * row;
-        cudaError_t e = cudaMemcpyAsync(static_cast<char*>(hp) + off, static_cast<const char*>(dp) + off,
+        cudaError_t e = copy_async(static_cast<char*>(hp) + off, static_cast<const char*>(dp) + off,
                                         copy_rows(tab[i]) * row, cudaMemcpyDeviceToHost, c->stream);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync D2H");
     }
@@ -803,7 +826,7 @@ static cudaError_t copy_slice(const FieldDesc& f, void* dst, const void* src, in
     if (hi <= lo) return cudaSuccess;
     const size_t es = f.esize, pitch = (size_t)ld * es, w = (size_t)(hi - lo) * es;
     const size_t off = copy_row0(f) * pitch + lo * es;
-    return cudaMemcpy2DAsync(static_cast<char*>(dst) + off, pitch, static_cast<const char*>(src) + off, pitch,
+    return copy_2d_async(static_cast<char*>(dst) + off, pitch, static_cast<const char*>(src) + off, pitch,
                              w, copy_rows(f), kind, s);
 }
 
@@ -850,7 +873,7 @@ static int chunk_out(ThreadCtx* c, const Chunk& ch, int k, const void* hio, cons
 
 static int read_error(ThreadCtx* c, int* code, int* index, int* level) {
     DevError h;
-    cudaError_t e = cudaMemcpy(&h, c->err, sizeof h, cudaMemcpyDeviceToHost);
+    cudaError_t e = copy_sync(&h, c->err, sizeof h, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(err)");
     if (h.key == ~0ull) { *code = 0; return 0; }
     *code = (int)(h.key & 0xff);
@@ -1049,7 +1072,7 @@ extern "C" int32_t ctsmg_soilwater(const ctsmg_bounds* bounds, int32_t num_hydro
         ctsmg_soilwater_io dio;
         stage_alloc(c, io, &dio, sizeof dio, T, NT, ldc, 0);
         int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_hydrologyc * 4);
-        e = cudaMemcpyAsync(dfilt, filter_hydrologyc, (size_t)num_hydrologyc * 4, cudaMemcpyHostToDevice, c->h2d);
+        e = copy_async(dfilt, filter_hydrologyc, (size_t)num_hydrologyc * 4, cudaMemcpyHostToDevice, c->h2d);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
         const int K = (int)chunks.size();
         if ((rc = chunk_in(c, chunks[0], 0, io, &dio, T, NT, ldc, 0))) return rc;
@@ -1069,7 +1092,7 @@ extern "C" int32_t ctsmg_soilwater(const ctsmg_bounds* bounds, int32_t num_hydro
         ctsmg_soilwater_io dio;
         if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, 0))) return rc;
         int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_hydrologyc * 4);
-        e = cudaMemcpyAsync(dfilt, filter_hydrologyc, (size_t)num_hydrologyc * 4, cudaMemcpyHostToDevice, c->stream);
+        e = copy_async(dfilt, filter_hydrologyc, (size_t)num_hydrologyc * 4, cudaMemcpyHostToDevice, c->stream);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
         e = launch_soilwater_call(dio, bounds->begc, num_hydrologyc, dfilt, nml, e_ice, dtime, c->err, c->stream,
                                   dcounter);
@@ -1115,7 +1138,7 @@ extern "C" int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds, int32_t num
         stage_alloc(c, io, &dio, sizeof dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp);
         int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_nolakec * 4);
         double* ws = (double*)arena_take(c, ws_bytes);
-        cudaError_t e = cudaMemcpyAsync(dfilt, filter_nolakec, (size_t)num_nolakec * 4, cudaMemcpyHostToDevice, c->h2d);
+        cudaError_t e = copy_async(dfilt, filter_nolakec, (size_t)num_nolakec * 4, cudaMemcpyHostToDevice, c->h2d);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
         if ((e = cudaMemsetAsync(c->err, 0xff, sizeof(DevError), c->stream)) != cudaSuccess)
             return cuda_fail(e, "cudaMemsetAsync(err)");
@@ -1145,7 +1168,7 @@ extern "C" int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds, int32_t num
     if ((rc = stage_in(c, io, &dio, sizeof dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp))) return rc;
     int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_nolakec * 4);
     double* ws = (double*)arena_take(c, ws_bytes);
-    cudaError_t e = cudaMemcpyAsync(dfilt, filter_nolakec, (size_t)num_nolakec * 4, cudaMemcpyHostToDevice, c->stream);
+    cudaError_t e = copy_async(dfilt, filter_nolakec, (size_t)num_nolakec * 4, cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
     e = cudaMemsetAsync(c->err, 0xff, sizeof(DevError), c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(err)");
@@ -1210,7 +1233,7 @@ extern "C" int32_t ctsmg_canopyfluxes(const ctsmg_bounds* bounds, int32_t num_ex
     int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_exposedvegp * 4);
     int* counter = (int*)arena_take(c, 256);
     double* cws = (double*)arena_take(c, canopy_ws_bytes(num_exposedvegp));
-    cudaError_t e = cudaMemcpyAsync(dfilt, filter_exposedvegp, (size_t)num_exposedvegp * 4, cudaMemcpyHostToDevice, c->stream);
+    cudaError_t e = copy_async(dfilt, filter_exposedvegp, (size_t)num_exposedvegp * 4, cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
     e = cudaMemsetAsync(c->err, 0xff, sizeof(DevError), c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(err)");
@@ -1282,9 +1305,9 @@ extern "C" int32_t ctsmg_soilfluxes(const ctsmg_bounds* bounds, int32_t num_nola
     int32_t* dfp = (int32_t*)arena_take(c, (size_t)num_nolakep * 4 + 4);
     cudaError_t e = cudaSuccess;
     if (num_nolakec > 0)
-        e = cudaMemcpyAsync(dfc, filter_nolakec, (size_t)num_nolakec * 4, cudaMemcpyHostToDevice, c->stream);
+        e = copy_async(dfc, filter_nolakec, (size_t)num_nolakec * 4, cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess && num_nolakep > 0)
-        e = cudaMemcpyAsync(dfp, filter_nolakep, (size_t)num_nolakep * 4, cudaMemcpyHostToDevice, c->stream);
+        e = copy_async(dfp, filter_nolakep, (size_t)num_nolakep * 4, cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
     e = launch_soilfluxes(dio, bounds->begc, bounds->begp, num_nolakec, dfc, num_nolakep, dfp, dtime, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "soilfluxes kernel launch");
@@ -1324,7 +1347,7 @@ extern "C" int32_t ctsmg_root_moist_stress(const ctsmg_bounds* bounds, int32_t n
     ctsmg_rootmoist_io dio;
     if ((rc = stage_in(c, io, &dio, sizeof dio, ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, ldc, ldp))) return rc;
     int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_exposedvegp * 4);
-    cudaError_t e = cudaMemcpyAsync(dfilt, filter_exposedvegp, (size_t)num_exposedvegp * 4, cudaMemcpyHostToDevice,
+    cudaError_t e = copy_async(dfilt, filter_exposedvegp, (size_t)num_exposedvegp * 4, cudaMemcpyHostToDevice,
                                     c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
     e = launch_rootmoist(dio, pft, bounds->begc, bounds->begp, num_exposedvegp, dfilt, c->stream);
@@ -1362,7 +1385,7 @@ extern "C" int32_t ctsmg_soilevap_resis(const ctsmg_bounds* bounds, int32_t num_
     ctsmg_soilresis_io dio;
     if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, 0))) return rc;
     int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_nolakec * 4);
-    cudaError_t e = cudaMemcpyAsync(dfilt, filter_nolakec, (size_t)num_nolakec * 4, cudaMemcpyHostToDevice, c->stream);
+    cudaError_t e = copy_async(dfilt, filter_nolakec, (size_t)num_nolakec * 4, cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
     const SoilResisArgs a{par.soil_resis_method, par.d_max, par.frac_sat_soil_dsl_init};
     e = launch_soilevap_resis(dio, bounds->begc, num_nolakec, dfilt, a, c->stream);
@@ -1410,7 +1433,7 @@ extern "C" int32_t ctsmg_baregroundfluxes(const ctsmg_bounds* bounds, int32_t nu
     if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, ldp, ldg))) return rc;
     int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_noexposedvegp * 4);
     int* dlast = (int*)arena_take(c, (size_t)ldc * 4);
-    cudaError_t e = cudaMemcpyAsync(dfilt, filter_noexposedvegp, (size_t)num_noexposedvegp * 4, cudaMemcpyHostToDevice,
+    cudaError_t e = copy_async(dfilt, filter_noexposedvegp, (size_t)num_noexposedvegp * 4, cudaMemcpyHostToDevice,
                                     c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
     const BareArgs a{cp.a_coef, cp.a_exp, cp.wind_min, cp.zetamaxstable, sres.soil_resis_method};
@@ -1460,7 +1483,7 @@ static int hydrology_call(const ctsmg_bounds* bounds, int32_t n, const int32_t* 
     ctsmg_hydrology_io dio;
     if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, 0))) return rc;
     int32_t* dfilt = (int32_t*)arena_take(c, (size_t)n * 4);
-    cudaError_t e = cudaMemcpyAsync(dfilt, filt, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream);
+    cudaError_t e = copy_async(dfilt, filt, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
     e = launch_hydrology(dio, bounds->begc, n, dfilt, which, current_soilhydrology_params(), dtime, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "hydrology kernel launch");
@@ -1503,3 +1526,10 @@ extern "C" int32_t ctsmg_drainage(const ctsmg_bounds* b, int32_t n, const int32_
     return hydrology_call(b, n, f, io, dtime, HYD_DRAINAGE, HYD_DR_TABLE, HYD_DR_TABLE_N);
 }
 
+extern "C" int32_t ctsmg_copy_bytes(int64_t* h2d, int64_t* d2h, int32_t reset) {
+    using namespace ctsmg;
+    if (h2d) *h2d = g_h2d_bytes.load();
+    if (d2h) *d2h = g_d2h_bytes.load();
+    if (reset) { g_h2d_bytes = 0; g_d2h_bytes = 0; }
+    return 0;
+}

@@ -48,18 +48,3 @@ def step_bytes_per_column(mean_snow_layers, patches_per_column=1.0):
         if w:
             wr += lev * size * mult
     return rd, wr
-
-
-def dropin_copy_bytes_per_column(patches_per_column=1.0):
-    """(H2D, D2H) bytes per column of one plain SoilWater + SoilTemperature call
-    pair: the C-ABI copies every component's full level extent in and the
-    written components back."""
-    h2d = d2h = 0.0
-    for table in (abi.SOILWATER_FIELDS, abi.SOILTEMP_FIELDS):
-        for (n, k, t, u) in table:
-            size = 8 if t == "f8" else 4
-            b = abi.LEVELS[k][1] * size * (patches_per_column if k in ("P", "PL") else 1.0)
-            h2d += b
-            if u != "in":
-                d2h += b
-    return h2d, d2h

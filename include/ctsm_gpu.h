@@ -886,6 +886,11 @@ int32_t ctsmg_pool_free(ctsmg_pool p, int32_t* cols_largest, int32_t* patches_la
 int32_t ctsmg_pool_destroy(ctsmg_pool p);
 
 /* ---------------------------------------------------------------- measurement */
+/* Host<->device bytes copied by the drop-in entry points of this process
+ * (host arrays in, written components back, filters and status reads) since
+ * the last reset; reset != 0 zeroes the counters after reading them.  No
+ * reference counterpart. */
+int32_t ctsmg_copy_bytes(int64_t* h2d, int64_t* d2h, int32_t reset);
 /* FP64 FMA throughput of the current GPU in TFLOP/s (a DFMA loop over every
  * SM); the denominator of the FP64 roofline fraction.  No reference counterpart. */
 int32_t ctsmg_measure_fp64_tflops(double* tflops);

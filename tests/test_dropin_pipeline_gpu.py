@@ -33,3 +33,35 @@ def test_pipelined_equals_single_shot(gpu_lib):
     for k in ("t_soisno", "h2osoi_liq", "qin", "xmf", "eflx_fgr"):
         np.testing.assert_array_equal(P[k][..., skipped], A[k][..., skipped], err_msg=k)
     assert not np.array_equal(P["t_soisno"], A["t_soisno"])
+
+
+def _copied(reset=False):
+    import ctypes as C
+    from ctsm_gb300 import _lib
+    L = _lib.load()
+    L.ctsmg_copy_bytes.argtypes = [C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_int32]
+    h, d = C.c_int64(0), C.c_int64(0)
+    _lib.check(L.ctsmg_copy_bytes(C.byref(h), C.byref(d), 1 if reset else 0))
+    return h.value, d.value
+
+
+def test_copy_accounting(gpu_lib):
+    """The library counts the bytes each drop-in call moves: the pipelined and
+    the one-piece forms move the same bytes, a dense filter skips the copy-in
+    of the components SoilWater overwrites, and a reset zeroes the counters."""
+    A, npatch = inputs.soil_columns(40000, seed=72, snow=True, nbedrock=(3, 20))
+    ncol = A["zwt"].shape[0]
+    b = abi.Bounds(1, ncol, 1, npatch)
+    dense = np.arange(1, ncol + 1, dtype=np.int32)
+    runs = {}
+    for name, f in (("asc", dense), ("desc", np.ascontiguousarray(dense[::-1])),
+                    ("gaps", np.ascontiguousarray(dense[(dense % 7) != 3]))):
+        S = copy.deepcopy(A)
+        _copied(reset=True)
+        soil.SoilWater(b, len(f), f, S, DT)
+        runs[name] = _copied(reset=True)
+    assert _copied() == (0, 0)
+    full = sum(A[n].nbytes for (n, k, t, u) in abi.SOILWATER_FIELDS if n in A)
+    assert runs["asc"] == runs["desc"]
+    assert 0 < runs["asc"][0] < runs["gaps"][0] <= full + 4 * ncol + 64
+    assert 0 < runs["asc"][1] == runs["gaps"][1]
