@@ -71,10 +71,15 @@ static bool g_cpar_set = false;
 #endif
 constexpr int PIPE_CHUNKS = CTSMG_PIPE_CHUNKS;   // chunks of a pipelined drop-in call
 constexpr int PIPE_MIN_COLUMNS = 32768;  // smaller calls run in one piece
+#ifndef CTSMG_PIPE_STREAMS
+#define CTSMG_PIPE_STREAMS 4
+#endif
+constexpr int PIPE_STREAMS = CTSMG_PIPE_STREAMS; // compute streams of a pipelined call
 
 struct ThreadCtx {
     cudaStream_t stream = nullptr;
     cudaStream_t h2d = nullptr, d2h = nullptr;      // copy streams of the pipelined calls
+    cudaStream_t xs[PIPE_STREAMS - 1] = {};         // further compute streams of a pipelined call
     cudaEvent_t ev_in[PIPE_CHUNKS] = {}, ev_done[PIPE_CHUNKS] = {};
     char* arena = nullptr;
     size_t arena_cap = 0, arena_top = 0;
@@ -90,6 +95,8 @@ struct ThreadCtx {
         }
         if (h2d) cudaStreamDestroy(h2d);
         if (d2h) cudaStreamDestroy(d2h);
+        for (cudaStream_t x : xs)
+            if (x) cudaStreamDestroy(x);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -129,6 +136,11 @@ static int ctx_get(ThreadCtx** out) {
             delete c;
             return cuda_fail(e, "cudaStreamCreate");
         }
+        for (cudaStream_t& x : c->xs)
+            if ((e = cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking)) != cudaSuccess) {
+                delete c;
+                return cuda_fail(e, "cudaStreamCreate");
+            }
         for (int k = 0; k < PIPE_CHUNKS && e == cudaSuccess; ++k) {
             e = cudaEventCreateWithFlags(&c->ev_in[k], cudaEventDisableTiming);
             if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_done[k], cudaEventDisableTiming);
@@ -871,6 +883,32 @@ static int chunk_out(ThreadCtx* c, const Chunk& ch, int k, const void* hio, cons
     return 0;
 }
 
+// Compute stream of chunk k.  A chunk of a pipelined call is a fraction of a
+// wave of the GPU; consecutive chunks run on PIPE_STREAMS streams in turn so
+// that the kernels of chunks whose data have arrived run side by side (their
+// columns are disjoint).
+static cudaStream_t chunk_stream(ThreadCtx* c, int k) {
+    const int i = k % PIPE_STREAMS;
+    return i ? c->xs[i - 1] : c->stream;
+}
+
+// Order the further compute streams after the work already queued on
+// c->stream (the status reset).
+static int fork_streams(ThreadCtx* c) {
+    cudaError_t e = cudaEventRecord(c->ev_done[0], c->stream);
+    for (cudaStream_t x : c->xs)
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(x, c->ev_done[0], 0);
+    return e == cudaSuccess ? 0 : cuda_fail(e, "fork streams");
+}
+
+static cudaError_t join_streams(ThreadCtx* c) {
+    cudaError_t e = cudaStreamSynchronize(c->d2h);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    for (cudaStream_t x : c->xs)
+        if (e == cudaSuccess) e = cudaStreamSynchronize(x);
+    return e;
+}
+
 static int read_error(ThreadCtx* c, int* code, int* index, int* level) {
     DevError h;
     cudaError_t e = copy_sync(&h, c->err, sizeof h, cudaMemcpyDeviceToHost);
@@ -1062,9 +1100,9 @@ extern "C" int32_t ctsmg_soilwater(const ctsmg_bounds* bounds, int32_t num_hydro
     }
     if (num_hydrologyc == 0) return 0;
     const int ldc = io->ldc;
-    size_t need = table_bytes(T, NT, ldc, 0) + (size_t)num_hydrologyc * 4 + 4096 + 256;
+    size_t need = table_bytes(T, NT, ldc, 0) + (size_t)num_hydrologyc * 4 + 4096 + 128 * PIPE_STREAMS;
     if ((rc = arena_reserve(c, need))) return rc;
-    int* dcounter = (int*)arena_take(c, 256);
+    int* dcounter = (int*)arena_take(c, 128 * PIPE_STREAMS);   // one 128-byte slot per compute stream
     cudaError_t e = cudaMemsetAsync(c->err, 0xff, sizeof(DevError), c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(err)");
     std::vector<Chunk> chunks;
@@ -1075,19 +1113,21 @@ extern "C" int32_t ctsmg_soilwater(const ctsmg_bounds* bounds, int32_t num_hydro
         e = copy_async(dfilt, filter_hydrologyc, (size_t)num_hydrologyc * 4, cudaMemcpyHostToDevice, c->h2d);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
         const int K = (int)chunks.size();
+        if ((rc = fork_streams(c))) return rc;
         if ((rc = chunk_in(c, chunks[0], 0, io, &dio, T, NT, ldc, 0))) return rc;
         for (int k = 0; k < K; ++k) {
             const Chunk& ch = chunks[k];
-            if ((e = cudaStreamWaitEvent(c->stream, c->ev_in[k], 0)) != cudaSuccess) return cuda_fail(e, "wait");
+            cudaStream_t ks = chunk_stream(c, k);
+            if ((e = cudaStreamWaitEvent(ks, c->ev_in[k], 0)) != cudaSuccess) return cuda_fail(e, "wait");
+            // one lane-refill counter per compute stream (chunks on one stream run in order)
             e = launch_soilwater_call(dio, bounds->begc, ch.f1 - ch.f0, dfilt + ch.f0, nml, e_ice, dtime, c->err,
-                                      c->stream, dcounter);
+                                      ks, dcounter + 32 * (k % PIPE_STREAMS));
             if (e != cudaSuccess) return cuda_fail(e, "soilwater kernel launch");
-            if ((e = cudaEventRecord(c->ev_done[k], c->stream)) != cudaSuccess) return cuda_fail(e, "record");
+            if ((e = cudaEventRecord(c->ev_done[k], ks)) != cudaSuccess) return cuda_fail(e, "record");
             if (k + 1 < K && (rc = chunk_in(c, chunks[k + 1], k + 1, io, &dio, T, NT, ldc, 0))) return rc;
             if ((rc = chunk_out(c, ch, k, io, &dio, T, NT, ldc, 0))) return rc;
         }
-        if ((e = cudaStreamSynchronize(c->d2h)) != cudaSuccess) return cuda_fail(e, "soilwater");
-        if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return cuda_fail(e, "soilwater");
+        if ((e = join_streams(c)) != cudaSuccess) return cuda_fail(e, "soilwater");
     } else {
         ctsmg_soilwater_io dio;
         if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, 0))) return rc;
@@ -1145,20 +1185,21 @@ extern "C" int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds, int32_t num
         int snow_method;
         { std::lock_guard<std::mutex> lk(g_mu); snow_method = g_opt.snow_thermal_cond_method; }
         const int K = (int)chunks.size();
+        if ((rc = fork_streams(c))) return rc;
         if ((rc = chunk_in(c, chunks[0], 0, io, &dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp))) return rc;
         for (int k = 0; k < K; ++k) {
             const Chunk& ch = chunks[k];
-            if ((e = cudaStreamWaitEvent(c->stream, c->ev_in[k], 0)) != cudaSuccess) return cuda_fail(e, "wait");
+            cudaStream_t ks = chunk_stream(c, k);
+            if ((e = cudaStreamWaitEvent(ks, c->ev_in[k], 0)) != cudaSuccess) return cuda_fail(e, "wait");
             e = launch_soiltemp(dio, bounds->begc, bounds->begp, ch.f1 - ch.f0, dfilt + ch.f0, dtime, snow_method,
-                                ws + ch.f0, num_nolakec, c->err, c->stream);
+                                ws + ch.f0, num_nolakec, c->err, ks);
             if (e != cudaSuccess) return cuda_fail(e, "soiltemperature kernel launch");
-            if ((e = cudaEventRecord(c->ev_done[k], c->stream)) != cudaSuccess) return cuda_fail(e, "record");
+            if ((e = cudaEventRecord(c->ev_done[k], ks)) != cudaSuccess) return cuda_fail(e, "record");
             if (k + 1 < K && (rc = chunk_in(c, chunks[k + 1], k + 1, io, &dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp)))
                 return rc;
             if ((rc = chunk_out(c, ch, k, io, &dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp))) return rc;
         }
-        if ((e = cudaStreamSynchronize(c->d2h)) != cudaSuccess) return cuda_fail(e, "soiltemperature");
-        if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) return cuda_fail(e, "soiltemperature");
+        if ((e = join_streams(c)) != cudaSuccess) return cuda_fail(e, "soiltemperature");
         int code = 0, idx = 0, lev = 0;
         if ((rc = read_error(c, &code, &idx, &lev))) return rc;
         if (code) return set_error(code, "BandDiagonal ERROR: dgbsv returned error code", idx, lev);

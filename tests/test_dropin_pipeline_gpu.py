@@ -47,8 +47,10 @@ def _copied(reset=False):
 
 def test_copy_accounting(gpu_lib):
     """The library counts the bytes each drop-in call moves: the pipelined and
-    the one-piece forms move the same bytes, a dense filter skips the copy-in
-    of the components SoilWater overwrites, and a reset zeroes the counters."""
+    the one-piece forms move the same bytes for the same work, an ascending
+    filter over every column skips the copy-in of the components SoilWater
+    overwrites (a filter in another order or with gaps copies them in), and
+    a reset zeroes the counters."""
     A, npatch = inputs.soil_columns(40000, seed=72, snow=True, nbedrock=(3, 20))
     ncol = A["zwt"].shape[0]
     b = abi.Bounds(1, ncol, 1, npatch)
@@ -62,6 +64,11 @@ def test_copy_accounting(gpu_lib):
         runs[name] = _copied(reset=True)
     assert _copied() == (0, 0)
     full = sum(A[n].nbytes for (n, k, t, u) in abi.SOILWATER_FIELDS if n in A)
-    assert runs["asc"] == runs["desc"]
-    assert 0 < runs["asc"][0] < runs["gaps"][0] <= full + 4 * ncol + 64
-    assert 0 < runs["asc"][1] == runs["gaps"][1]
+    ngaps = int(np.count_nonzero((dense % 7) != 3))
+    # one piece vs pipelined: the same component bytes, except the unfiltered
+    # columns between two chunks, which the pipelined form does not move
+    per_col = (runs["desc"][0] - 4 * ncol) / ncol
+    assert 0 <= (runs["desc"][0] - 4 * ncol) - (runs["gaps"][0] - 4 * ngaps) <= 16 * per_col
+    assert 0 < runs["asc"][0] < runs["gaps"][0] <= full + 4 * ncol
+    assert 0 < runs["asc"][1] == runs["desc"][1]
+    assert 0 <= runs["asc"][1] - runs["gaps"][1] <= 16 * runs["asc"][1] / ncol
