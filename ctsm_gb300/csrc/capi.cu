@@ -802,16 +802,32 @@ int check_filter(const ctsmg_bounds* b, int nf, const int32_t* filt) {
 // patch order that does not follow the columns) run the call in one piece.
 struct Chunk { int f0, f1, c0, c1, p0, p1; };
 
+// Filter entries per chunk for a kernel whose full-GPU wave is `wave`
+// columns: chunks of about one wave (a chunk's kernel seldom overlaps the
+// next one, whose data is still arriving, so a fraction of a wave leaves SMs
+// idle and a wave and a bit costs two), at least 4 and at most PIPE_CHUNKS of
+// them, rounded up to whole waves when larger than one.  wave = 0: PIPE_CHUNKS
+// equal chunks.
+static int chunk_columns(int num, int wave) {
+    if (wave <= 0) return (num + PIPE_CHUNKS - 1) / PIPE_CHUNKS;
+    long long k = ((long long)num + wave / 2) / wave;
+    k = std::min<long long>(std::max<long long>(k, 4), PIPE_CHUNKS);
+    long long cc = (num + k - 1) / k;
+    if (cc > wave) cc = (cc + wave - 1) / wave * wave;
+    return (int)cc;
+}
+
 static bool plan_chunks(const ctsmg_bounds* b, int num, const int32_t* filt, const int32_t* col_patchi,
-                        const int32_t* col_npatches, std::vector<Chunk>& out) {
+                        const int32_t* col_npatches, int wave, std::vector<Chunk>& out) {
     if (num < PIPE_MIN_COLUMNS || !filt) return false;
     for (int i = 1; i < num; ++i)
         if (filt[i] <= filt[i - 1]) return false;
     out.clear();
+    const int cc = chunk_columns(num, wave);
     for (int k = 0; k < PIPE_CHUNKS; ++k) {
         Chunk ch;
-        ch.f0 = (int)((long long)num * k / PIPE_CHUNKS);
-        ch.f1 = (int)((long long)num * (k + 1) / PIPE_CHUNKS);
+        ch.f0 = (int)std::min<long long>((long long)cc * k, num);
+        ch.f1 = (int)std::min<long long>((long long)cc * (k + 1), num);
         if (ch.f1 <= ch.f0) continue;
         ch.c0 = filt[ch.f0] - b->begc;
         ch.c1 = filt[ch.f1 - 1] - b->begc + 1;
@@ -1106,7 +1122,9 @@ extern "C" int32_t ctsmg_soilwater(const ctsmg_bounds* bounds, int32_t num_hydro
     cudaError_t e = cudaMemsetAsync(c->err, 0xff, sizeof(DevError), c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(err)");
     std::vector<Chunk> chunks;
-    if (plan_chunks(bounds, num_hydrologyc, filter_hydrologyc, nullptr, nullptr, chunks)) {
+    // SoilWater's call is bound by its copies: PIPE_CHUNKS chunks keep the
+    // pipeline's fill and drain short (wave-sized chunks measured slower)
+    if (plan_chunks(bounds, num_hydrologyc, filter_hydrologyc, nullptr, nullptr, 0, chunks)) {
         ctsmg_soilwater_io dio;
         stage_alloc(c, io, &dio, sizeof dio, T, NT, ldc, 0);
         int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_hydrologyc * 4);
@@ -1173,7 +1191,8 @@ extern "C" int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds, int32_t num
     size_t need = table_bytes(SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp) + ws_bytes + (size_t)num_nolakec * 4 + 8192;
     if ((rc = arena_reserve(c, need))) return rc;
     std::vector<Chunk> chunks;
-    if (plan_chunks(bounds, num_nolakec, filter_nolakec, io->col_patchi, io->col_npatches, chunks)) {
+    if (plan_chunks(bounds, num_nolakec, filter_nolakec, io->col_patchi, io->col_npatches, soiltemp_wave_columns(),
+                    chunks)) {
         ctsmg_soiltemp_io dio;
         stage_alloc(c, io, &dio, sizeof dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp);
         int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_nolakec * 4);

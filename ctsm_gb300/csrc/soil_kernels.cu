@@ -949,6 +949,19 @@ cudaError_t launch_soiltemp(const ctsmg_soiltemp_io& io, int begc, int begp, int
     return cudaGetLastError();
 }
 
+static int wave_columns(const void* kernel, int block) {
+    int dev = 0, sms = 0, bpsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bpsm, kernel, block, 0) != cudaSuccess)
+        return 0;
+    return sms * bpsm * block;
+}
+
+int soiltemp_wave_columns() {
+    static const int w = wave_columns((const void*)soiltemp_kernel, 128);
+    return w;
+}
+
 template <int ORDER>
 static void launch_soilstep_order(const ctsmg_soilwater_io& wio, const ctsmg_soiltemp_io& tio,
                                   const ctsmg_soilfluxes_io& sf, int ncol, double e_ice, double dtime,

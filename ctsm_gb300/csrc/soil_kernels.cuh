@@ -11,6 +11,10 @@ cudaError_t launch_soilwater(const ctsmg_soilwater_io& io, int begc, int nfilt, 
                              double e_ice, double dtime, cudaStream_t s);
 cudaError_t launch_soiltemp(const ctsmg_soiltemp_io& io, int begc, int begp, int nfilt, const int32_t* d_filt,
                             double dtime, int snow_method, double* ws, int ws_ld, DevError* err, cudaStream_t s);
+// Columns one launch of the drop-in kernel keeps resident on the whole GPU
+// at once (SMs x resident blocks x block size): the size of a chunk of a
+// pipelined drop-in call that fills the GPU without a partial second wave.
+int soiltemp_wave_columns();
 // What the fused soil step does beside the heat solve: water = 1 runs the
 // Zeng-Decker SoilWater inside (0: the caller runs the moisture form in its
 // own kernel), flexcn = 1 applies the use_flexibleCN fix after it, refresh = 1
