@@ -32,6 +32,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -165,8 +166,8 @@ class Clocks:
     def __init__(self, gpu):
         self.gpu = gpu
         self.p = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv") if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else "/tmp/clocks_bench.csv"
+        # raw samples, kept for inspection (CTSMG_CLOCKS_CSV names the file)
+        self.path = os.environ.get("CTSMG_CLOCKS_CSV", os.path.join(tempfile.gettempdir(), "clocks_bench.csv"))
 
     def start(self):
         try:

@@ -6,7 +6,7 @@ checkout, so the values below are the CLM5 technical note's
 Photosynthesis/CLM50_Tech_Note_Photosynthesis.rst:149-260) and the
 reference's module constants; parity is oracle vs kernel on the same values.
 
-Configuration of the path (the benchmark spec / the canopy workload): z0param_method
+Configuration of the canopy workload: z0param_method
 = ZengWang2007, use_biomass_heat_storage = .false., satellite phenology (no
 CN, no LUNA), no hydraulic stress, Medlyn 2011 stomatal conductance,
 light_inhibit = .true., soil resistance sl14 (soilresis given), nlevcan = 1,
