@@ -71,6 +71,9 @@ static bool g_cpar_set = false;
 #endif
 constexpr int PIPE_CHUNKS = CTSMG_PIPE_CHUNKS;   // chunks of a pipelined drop-in call
 constexpr int PIPE_MIN_COLUMNS = 32768;  // smaller calls run in one piece
+#ifndef CTSMG_GROUP_COLUMNS
+#define CTSMG_GROUP_COLUMNS 1     // heat-solve work order grouped by snow / bedrock layers
+#endif
 #ifndef CTSMG_PIPE_STREAMS
 #define CTSMG_PIPE_STREAMS 4
 #endif
@@ -83,11 +86,14 @@ struct ThreadCtx {
     cudaEvent_t ev_in[PIPE_CHUNKS] = {}, ev_done[PIPE_CHUNKS] = {};
     char* arena = nullptr;
     size_t arena_cap = 0, arena_top = 0;
+    int32_t* order = nullptr;                       // page-locked work order of a call
+    size_t order_cap = 0;
     DevError* err = nullptr;
     std::string msg;
     int err_index = 0, err_level = 0;
     ~ThreadCtx() {
         if (arena) cudaFree(arena);
+        if (order) cudaFreeHost(order);
         if (err) cudaFree(err);
         for (int k = 0; k < PIPE_CHUNKS; ++k) {
             if (ev_in[k]) cudaEventDestroy(ev_in[k]);
@@ -925,6 +931,46 @@ static cudaError_t join_streams(ThreadCtx* c) {
     return e;
 }
 
+// Page-locked host buffer of n filter entries (grown on demand).
+static int32_t* order_buffer(ThreadCtx* c, size_t n) {
+    if (n <= c->order_cap) return c->order;
+    if (c->order) cudaFreeHost(c->order);
+    c->order = nullptr;
+    c->order_cap = 0;
+    const size_t cap = n + n / 4 + 1024;
+    if (cudaMallocHost(&c->order, cap * sizeof(int32_t)) != cudaSuccess) {
+        c->order = nullptr;
+        return nullptr;
+    }
+    c->order_cap = cap;
+    return c->order;
+}
+
+// Filter entries [f0, f1) grouped by snow layers, then bedrock depth (deepest
+// first; a stable counting sort) into out[f0..f1): a warp of the heat-solve
+// kernel then takes columns whose level loops have the same lengths, as the
+// resident step's column order does.  Each column's result does not depend
+// on the order, and the set of columns of [f0, f1) is unchanged.
+static void group_by_layers(const int32_t* filt, int f0, int f1, const int32_t* snl, const int32_t* nbedrock,
+                            int begc, int32_t* out) {
+    if (!CTSMG_GROUP_COLUMNS) {
+        std::memcpy(out + f0, filt + f0, (size_t)(f1 - f0) * sizeof(int32_t));
+        return;
+    }
+    constexpr int NB = NLEVGRND + 2, NK = (NLEVSNO + 1) * NB;
+    int count[NK + 1];
+    std::memset(count, 0, sizeof count);
+    auto key = [&](int32_t col) {
+        const int cc = col - begc;
+        const int sn = std::min(std::max(-snl[cc], 0), NLEVSNO);
+        const int nb = nbedrock ? std::min(std::max(nbedrock[cc], 0), NB - 1) : 0;
+        return (NLEVSNO - sn) * NB + (NB - 1 - nb);
+    };
+    for (int i = f0; i < f1; ++i) ++count[key(filt[i]) + 1];
+    for (int k = 0; k < NK; ++k) count[k + 1] += count[k];
+    for (int i = f0; i < f1; ++i) out[f0 + count[key(filt[i])]++] = filt[i];
+}
+
 static int read_error(ThreadCtx* c, int* code, int* index, int* level) {
     DevError h;
     cudaError_t e = copy_sync(&h, c->err, sizeof h, cudaMemcpyDeviceToHost);
@@ -1197,7 +1243,11 @@ extern "C" int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds, int32_t num
         stage_alloc(c, io, &dio, sizeof dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp);
         int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_nolakec * 4);
         double* ws = (double*)arena_take(c, ws_bytes);
-        cudaError_t e = copy_async(dfilt, filter_nolakec, (size_t)num_nolakec * 4, cudaMemcpyHostToDevice, c->h2d);
+        int32_t* hord = order_buffer(c, (size_t)num_nolakec);
+        if (!hord) return set_error(CTSMG_E_CUDA, "cudaMallocHost(work order)", 0, 0);
+        for (const Chunk& ch : chunks)
+            group_by_layers(filter_nolakec, ch.f0, ch.f1, io->snl, io->nbedrock, bounds->begc, hord);
+        cudaError_t e = copy_async(dfilt, hord, (size_t)num_nolakec * 4, cudaMemcpyHostToDevice, c->h2d);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
         if ((e = cudaMemsetAsync(c->err, 0xff, sizeof(DevError), c->stream)) != cudaSuccess)
             return cuda_fail(e, "cudaMemsetAsync(err)");
@@ -1228,7 +1278,10 @@ extern "C" int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds, int32_t num
     if ((rc = stage_in(c, io, &dio, sizeof dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp))) return rc;
     int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_nolakec * 4);
     double* ws = (double*)arena_take(c, ws_bytes);
-    cudaError_t e = copy_async(dfilt, filter_nolakec, (size_t)num_nolakec * 4, cudaMemcpyHostToDevice, c->stream);
+    int32_t* hord = order_buffer(c, (size_t)num_nolakec);
+    if (!hord) return set_error(CTSMG_E_CUDA, "cudaMallocHost(work order)", 0, 0);
+    group_by_layers(filter_nolakec, 0, num_nolakec, io->snl, io->nbedrock, bounds->begc, hord);
+    cudaError_t e = copy_async(dfilt, hord, (size_t)num_nolakec * 4, cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
     e = cudaMemsetAsync(c->err, 0xff, sizeof(DevError), c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(err)");
