@@ -1,5 +1,5 @@
 """Large drop-in calls over an ascending filter run pipelined (chunks of the
-filter copy in, compute and copy out on three streams); other filters run in
+filter copy in, compute and copy out on separate streams); other filters run in
 one piece.  Both forms must give bit-identical results, including columns
 that are not in the filter (left as they were)."""
 import copy
