@@ -143,6 +143,11 @@ __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, d
         io.qin[c + (size_t)(j - 1) * ld] = qi;
         io.qout[c + (size_t)(j - 1) * ld] = qo;
     };
+    // The inflow of level j and its derivatives (qin, dqidw0, dqidw1) are the
+    // outflow of level j-1 and its derivatives (qout, dqodw1, dqodw2): the
+    // reference evaluates the same expressions on the same operands twice;
+    // here each interface is evaluated once and carried down.
+    double q_up, dq_up0, dq_up1;
     {   // top node
         const int j = 1;
         double qin = io.qflx_infl[c];
@@ -157,18 +162,14 @@ __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, d
         bmx[j] = dzmm[j] * (0.0 + 1.0 / dtime) + dqodw1;
         cmx[j] = dqodw2;
         setq(j, qin, qout);
+        q_up = qout; dq_up0 = dqodw1; dq_up1 = dqodw2;
     }
 #pragma unroll 1
     for (int j = 2; j <= NLEVSOI - 1; ++j) {
-        double den = (zmm[j] - zmm[j - 1]);
-        double dzq = (zq[j] - zq[j - 1]);
-        double num = (smp[j] - smp[j - 1]) - dzq;
-        double qin = -hk[j - 1] * num / den;
-        double dqidw0 = -(-hk[j - 1] * dsmpdw[j - 1] + num * dhkdw[j - 1]) / den;
-        double dqidw1 = -(hk[j - 1] * dsmpdw[j] + num * dhkdw[j - 1]) / den;
-        den = (zmm[j + 1] - zmm[j]);
-        dzq = (zq[j + 1] - zq[j]);
-        num = (smp[j + 1] - smp[j]) - dzq;
+        const double qin = q_up, dqidw0 = dq_up0, dqidw1 = dq_up1;
+        double den = (zmm[j + 1] - zmm[j]);
+        double dzq = (zq[j + 1] - zq[j]);
+        double num = (smp[j + 1] - smp[j]) - dzq;
         double qout = -hk[j] * num / den;
         double dqodw1 = -(-hk[j] * dsmpdw[j] + num * dhkdw[j]) / den;
         double dqodw2 = -(hk[j] * dsmpdw[j + 1] + num * dhkdw[j]) / den;
@@ -177,15 +178,11 @@ __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, d
         bmx[j] = dzmm[j] / dtime - dqidw1 + dqodw1;
         cmx[j] = dqodw2;
         setq(j, qin, qout);
+        q_up = qout; dq_up0 = dqodw1; dq_up1 = dqodw2;
     }
     {   // bottom node and aquifer layer
         const int j = NLEVSOI;
-        double den = (zmm[j] - zmm[j - 1]);
-        double dzq = (zq[j] - zq[j - 1]);
-        double num = (smp[j] - smp[j - 1]) - dzq;
-        double qin = -hk[j - 1] * num / den;
-        double dqidw0 = -(-hk[j - 1] * dsmpdw[j - 1] + num * dhkdw[j - 1]) / den;
-        double dqidw1 = -(hk[j - 1] * dsmpdw[j] + num * dhkdw[j - 1]) / den;
+        const double qin = q_up, dqidw0 = dq_up0, dqidw1 = dq_up1;
         if (j > jwt) {
             rmx[j] = qin - 0.0 - ROOT(j);
             amx[j] = -dqidw0;
@@ -203,9 +200,9 @@ __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, d
             double smp1 = -G(io.sucsat, j) * fm::pow(s_node, -bb);
             smp1 = fmax(smpmin, smp1);
             double dsmpdw1 = -bb * smp1 / (s_node * ws);
-            den = (zmm[j + 1] - zmm[j]);
-            dzq = (zq[j + 1] - zq[j]);
-            num = (smp1 - smp[j]) - dzq;
+            const double den = (zmm[j + 1] - zmm[j]);
+            const double dzq = (zq[j + 1] - zq[j]);
+            const double num = (smp1 - smp[j]) - dzq;
             double qout = -hk[j] * num / den;
             double dqodw1 = -(-hk[j] * dsmpdw[j] + num * dhkdw[j]) / den;
             double dqodw2 = -(hk[j] * dsmpdw1 + num * dhkdw[j]) / den;
@@ -213,8 +210,10 @@ __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, d
             amx[j] = -dqidw0;
             bmx[j] = dzmm[j] / dtime - dqidw1 + dqodw1;
             cmx[j] = dqodw2;
-            double dqidw0a = -(-hk[j] * dsmpdw[j] + num * dhkdw[j]) / den;
-            double dqidw1a = -(hk[j] * dsmpdw1 + num * dhkdw[j]) / den;
+            // the aquifer layer's inflow derivatives: the same expressions as
+            // dqodw1 / dqodw2 (SoilWaterMovementMod.F90 evaluates them again)
+            const double dqidw0a = dqodw1;
+            const double dqidw1a = dqodw2;
             rmx[j + 1] = qout - 0.0;
             amx[j + 1] = -dqidw0a;
             bmx[j + 1] = dzmm[j + 1] / dtime - dqidw1a + 0.0;

@@ -10,7 +10,11 @@ NLEVSNO, NLEVSOI, NLEVGRND = abi.NLEVSNO, abi.NLEVSOI, abi.NLEVGRND
 # uneven-column workload (DADD + DMUL + 2 x DFMA executed, libm included),
 # from the ncu capture of 65,536 columns of the same workload, and DRAM bytes
 # per column-step from the 1-pass capture of the full 524,288-column launch;
-# both summarised in profiles/soilstep_kernel_uneven_columns.md.
+# both summarised in profiles/soilstep_kernel_uneven_columns.md.  The capture
+# predates the Zeng-Decker solve's carrying of each interface's flux and
+# derivatives from one level to the next (3 divisions and 9 other FP64
+# operations fewer per level), so this count is a few per cent above the
+# kernel's current one and the FP64 rate derived from it is as much high.
 FLOPS_PER_COLUMN_STEP = (148978105 + 162750456 + 2 * 608026028) / 65536.0
 TRAFFIC_PER_COLUMN_STEP = (6665794560 + 4179119872) / 524288.0
 
