@@ -57,3 +57,23 @@ def test_reference_arm_other_ranks_do_nothing(capsys):
         ncol, seed, warmup, steps, gpus = 1024, 1, 3, 4, 2
     assert bench.reference_arm(Args(), 2, 1) is None
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_json_line(capsys):
+    """Rank 0 of the reference arm times the CPU oracle and prints one JSON
+    line with the contract's keys (a small workload: ~10 s of oracle work)."""
+    import json
+    sys.path.insert(0, ROOT)
+    import bench
+
+    class Args:
+        ncol, seed, warmup, steps, gpus = 2048, 2026, 1, 16, 1
+    bench.reference_arm(Args(), 1, 0)
+    lines = [l for l in capsys.readouterr().out.splitlines() if l.startswith("{")]
+    line = json.loads(lines[-1])
+    assert line["impl"] == "reference" and line["metric"] == bench.METRIC and line["unit"] == bench.UNIT
+    assert line["value"] > 0 and line["higher_is_better"] is True and line["n_gpus"] == 1
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
+    assert line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"] == {"value": line["value"], "unit": bench.UNIT, "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
