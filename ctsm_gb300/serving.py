@@ -330,3 +330,48 @@ def serve(pool, requests, time_limit=None, tick_clock=False, clock=time.perf_cou
                 never_admitted=len(queue) - nq, max_running_columns=max_running_cols,
                 p50_s_per_day=percentile(per_day, 50), p99_s_per_day=percentile(per_day, 99),
                 p50_wait_s=percentile(wait, 50), p99_wait_s=percentile(wait, 99))
+
+
+def main(argv=None):
+    """Command line: run a Poisson request stream through a pool and print its
+    statistics as one JSON line; --out also writes every request's record
+    (arrival, admission, completion, time per simulated day, whether its
+    final state is finite, its share of patches at itmax)."""
+    import argparse
+    import json
+    p = argparse.ArgumentParser(prog="python -m ctsm_gb300.serving",
+                                description="Poisson request stream through the serving pool")
+    p.add_argument("--requests", type=int, default=64)
+    p.add_argument("--rate", type=float, default=2.0, help="arrivals per second")
+    p.add_argument("--seed", type=int, default=2026)
+    p.add_argument("--budget-gb", type=float, default=150.0, help="device memory budget of the pool")
+    p.add_argument("--time-limit", type=float, default=None, help="seconds; default: run to completion")
+    p.add_argument("--out", default=None, help="JSON file for the statistics and per-request records")
+    a = p.parse_args(argv)
+    from . import soil
+    soil.init()
+    t0 = time.time()
+    reqs = request_stream(a.requests, a.rate, seed=a.seed)
+    gen_s = time.time() - t0
+    pool = Pool(budget_bytes=a.budget_gb * 1e9)
+    try:
+        st = serve(pool, reqs, time_limit=a.time_limit)
+    finally:
+        pool.close()
+    st["gen_s"] = gen_s
+    st["offered_column_steps"] = int(sum(q.column_steps() for q in reqs))
+    if a.out:
+        recs = []
+        for q in reqs:
+            A = q.state
+            recs.append(dict(rid=q.rid, ncol=q.ncol, nsteps=q.nsteps, days=q.days, arrival=q.arrival,
+                             admit=q.t_admit, done=q.t_done, s_per_day=(q.t_done - q.arrival) / q.days,
+                             finite=bool(np.isfinite(A["t_soisno"]).all() and np.isfinite(A["t_veg"]).all()),
+                             itmax_frac=float((A["num_iter"] >= 40).mean())))
+        with open(a.out, "w") as f:
+            json.dump({"stats": st, "requests": recs}, f)
+    print(json.dumps(st), flush=True)
+
+
+if __name__ == "__main__":
+    main()

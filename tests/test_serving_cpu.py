@@ -124,3 +124,10 @@ def test_serve_time_limit_stops_running():
 def test_percentile():
     assert serving.percentile([1, 2, 3, 4], 50) == 2.5
     assert math.isnan(serving.percentile([], 99))
+
+
+def test_command_line_parses(capsys):
+    from ctsm_gb300 import serving
+    with pytest.raises(SystemExit) as e:
+        serving.main(["--help"])
+    assert e.value.code == 0 and "--requests" in capsys.readouterr().out
