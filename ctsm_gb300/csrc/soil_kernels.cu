@@ -436,6 +436,13 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
     // ---------------- matrix row + RHS generator (SetRHSVec* :1913-2353,
     // SetMatrix* :2356-2926).  Row r: -nlevsno..nlevgrnd; returns the five
     // bands B(1..5, r) (band k couples row r to row r + 3 - k) and rhs(r).
+    // Rows are generated once each, in ascending order.  A row's quotient
+    // tk(j)/dzp is the next row's tk(j-1)/dzm (the same operands: dzm of row
+    // j+1 is Z(j+1)-Z(j)), so it is carried from one row to the next (q_dn of
+    // row q_row); and -(1-cnfac) fj tk / dz is the exact negation of
+    // (1-cnfac) fj tk / dz.  Both leave every value as the reference computes it.
+    double q_dn = 0.0;
+    int q_row = -1000;
     auto make_row = [&](int r, double* bnd, double& rhs) {
         bnd[0] = bnd[1] = bnd[2] = bnd[3] = bnd[4] = 0.0;
         if (r < 0) {                                   // snow layer j = r + 1
@@ -443,17 +450,24 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
             const double dzp = Z(j + 1) - Z(j);
             const double fj = fact[L(j)], tj = T[ssi(j)];
             if (j == snl + 1) {
-                bnd[2] = 1.0 + (1.0 - CNFAC) * fj * tk[L(j)] / dzp - fj * dhsdT;
+                const double x = (1.0 - CNFAC) * fj * tk[L(j)] / dzp;
+                bnd[2] = 1.0 + x - fj * dhsdT;
                 rhs = tj + fj * (hs_top_snow - dhsdT * tj + CNFAC * fn[L(j)]);
+                if (j != 0) bnd[1] = -x;
+                else bnd[0] = -x;
             } else {
                 const double dzm = (Z(j) - Z(j - 1));
                 bnd[3] = -(1.0 - CNFAC) * fj * tk[L(j - 1)] / dzm;
-                bnd[2] = 1.0 + (1.0 - CNFAC) * fj * (tk[L(j)] / dzp + tk[L(j - 1)] / dzm);
+                const double qp = tk[L(j)] / dzp;
+                const double qm = (q_row == j - 1) ? q_dn : tk[L(j - 1)] / dzm;
+                bnd[2] = 1.0 + (1.0 - CNFAC) * fj * (qp + qm);
+                q_dn = qp;
+                q_row = j;
                 double rr = tj + CNFAC * fj * (fn[L(j)] - fn[L(j - 1)]);
                 rhs = rr + fj * sabg_lyr_col(j);
+                if (j != 0) bnd[1] = -(1.0 - CNFAC) * fj * tk[L(j)] / dzp;
+                else bnd[0] = -(1.0 - CNFAC) * fj * tk[L(j)] / dzp;
             }
-            if (j != 0) bnd[1] = -(1.0 - CNFAC) * fj * tk[L(j)] / dzp;
-            else bnd[0] = -(1.0 - CNFAC) * fj * tk[L(j)] / dzp;
         } else if (r == 0) {                           // standing surface water
             bnd[2] = 1.0 + (1.0 - CNFAC) * (dtime / c_h2osfc) * tk_h2osfc / dzm_ssw - (dtime / c_h2osfc) * dhsdT;
             bnd[1] = -(1.0 - CNFAC) * (dtime / c_h2osfc) * tk_h2osfc / dzm_ssw;
@@ -463,15 +477,19 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
             const double fj = fact[L(j)], tj = T[ssi(j)];
             if (j == snl + 1) {
                 const double dzp = Z(j + 1) - Z(j);
-                bnd[2] = 1.0 + (1.0 - CNFAC) * fj * tk[L(j)] / dzp - fj * dhsdT;
-                bnd[1] = -(1.0 - CNFAC) * fj * tk[L(j)] / dzp;
+                const double x = (1.0 - CNFAC) * fj * tk[L(j)] / dzp;
+                bnd[2] = 1.0 + x - fj * dhsdT;
+                bnd[1] = -x;
                 rhs = tj + fj * (hs_top_snow - dhsdT * tj + CNFAC * fn[L(j)]);
             } else if (j == 1) {
                 const double dzm = (Z(j) - Z(j - 1));
                 const double dzp = (Z(j + 1) - Z(j));
                 bnd[1] = -(1.0 - CNFAC) * fj * tk[L(j)] / dzp;
-                bnd[2] = 1.0 + (1.0 - CNFAC) * fj * (tk[L(j)] / dzp + frac_sno * tk[L(j - 1)] / dzm) -
+                const double qp = tk[L(j)] / dzp;
+                bnd[2] = 1.0 + (1.0 - CNFAC) * fj * (qp + frac_sno * tk[L(j - 1)] / dzm) -
                          (1.0 - frac_sno) * fj * dhsdT;
+                q_dn = qp;
+                q_row = j;
                 bnd[4] = -frac_sno * (1.0 - CNFAC) * fj * tk[L(j - 1)] / dzm;
                 double rr = tj + fj * ((1.0 - frac_sno) * (hs_soil - dhsdT * tj) + CNFAC * (fn[L(j)] - frac_sno * fn[L(j - 1)]));
                 rhs = rr + frac_sno * fj * sabg_lyr_col(j);
@@ -479,13 +497,18 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
                 const double dzm = (Z(j) - Z(j - 1));
                 const double dzp = (Z(j + 1) - Z(j));
                 bnd[1] = -(1.0 - CNFAC) * fj * tk[L(j)] / dzp;
-                bnd[2] = 1.0 + (1.0 - CNFAC) * fj * (tk[L(j)] / dzp + tk[L(j - 1)] / dzm);
+                const double qp = tk[L(j)] / dzp;
+                const double qm = (q_row == j - 1) ? q_dn : tk[L(j - 1)] / dzm;
+                bnd[2] = 1.0 + (1.0 - CNFAC) * fj * (qp + qm);
+                q_dn = qp;
+                q_row = j;
                 bnd[3] = -(1.0 - CNFAC) * fj * tk[L(j - 1)] / dzm;
                 rhs = tj + CNFAC * fj * (fn[L(j)] - fn[L(j - 1)]);
             } else {
                 const double dzm = (Z(j) - Z(j - 1));
-                bnd[2] = 1.0 + (1.0 - CNFAC) * fj * tk[L(j - 1)] / dzm;
-                bnd[3] = -(1.0 - CNFAC) * fj * tk[L(j - 1)] / dzm;
+                const double x = (1.0 - CNFAC) * fj * tk[L(j - 1)] / dzm;
+                bnd[2] = 1.0 + x;
+                bnd[3] = -x;
                 rhs = tj - CNFAC * fj * fn[L(j - 1)] + fj * fn[L(j)];
             }
             if (j == 1 && frac_h2osfc != 0.0) {

@@ -13,8 +13,10 @@ NLEVSNO, NLEVSOI, NLEVGRND = abi.NLEVSNO, abi.NLEVSOI, abi.NLEVGRND
 # both summarised in profiles/soilstep_kernel_uneven_columns.md.  The capture
 # predates the Zeng-Decker solve's carrying of each interface's flux and
 # derivatives from one level to the next (3 divisions and 9 other FP64
-# operations fewer per level), so this count is a few per cent above the
-# kernel's current one and the FP64 rate derived from it is as much high.
+# operations fewer per level) and the heat system's carrying of each row's
+# tk/dz quotient (one division fewer per row), so this count is a few per
+# cent above the kernel's current one and the FP64 rate derived from it is as
+# much high.
 FLOPS_PER_COLUMN_STEP = (148978105 + 162750456 + 2 * 608026028) / 65536.0
 TRAFFIC_PER_COLUMN_STEP = (6665794560 + 4179119872) / 524288.0
 
