@@ -873,9 +873,9 @@ static void stage_alloc(ThreadCtx* c, const void* hio, void* dio, size_t io_size
     for (int i = 0; i < nf; ++i) field_ptr(dio, tab[i]) = arena_take(c, field_bytes(tab[i], ldc, ldp, 0));
 }
 
-// Enqueue the copy-in of chunk k (h2d stream) and record ev_in[k].
-static int chunk_in(ThreadCtx* c, const Chunk& ch, int k, const void* hio, const void* dio, const FieldDesc* tab,
-                    int nf, int ldc, int ldp) {
+// Enqueue the copy-in of chunk k's components (h2d stream).
+static int chunk_copies_in(ThreadCtx* c, const Chunk& ch, const void* hio, const void* dio, const FieldDesc* tab,
+                           int nf, int ldc, int ldp) {
     for (int i = 0; i < nf; ++i) {
         const FieldDesc& f = tab[i];
         if (f.no_in) continue;
@@ -885,6 +885,14 @@ static int chunk_in(ThreadCtx* c, const Chunk& ch, int k, const void* hio, const
                                    c->h2d);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy2DAsync H2D");
     }
+    return 0;
+}
+
+// Enqueue the copy-in of chunk k (h2d stream) and record ev_in[k].
+static int chunk_in(ThreadCtx* c, const Chunk& ch, int k, const void* hio, const void* dio, const FieldDesc* tab,
+                    int nf, int ldc, int ldp) {
+    int rc = chunk_copies_in(c, ch, hio, dio, tab, nf, ldc, ldp);
+    if (rc) return rc;
     cudaError_t e = cudaEventRecord(c->ev_in[k], c->h2d);
     return e == cudaSuccess ? 0 : cuda_fail(e, "cudaEventRecord");
 }
@@ -1245,17 +1253,27 @@ extern "C" int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds, int32_t num
         double* ws = (double*)arena_take(c, ws_bytes);
         int32_t* hord = order_buffer(c, (size_t)num_nolakec);
         if (!hord) return set_error(CTSMG_E_CUDA, "cudaMallocHost(work order)", 0, 0);
-        for (const Chunk& ch : chunks)
+        // chunk k's components, then its work order (sorted on the host while
+        // those copies run), then ev_in[k]
+        auto stage_chunk = [&](int k) -> int {
+            const Chunk& ch = chunks[k];
+            int r = chunk_copies_in(c, ch, io, &dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp);
+            if (r) return r;
             group_by_layers(filter_nolakec, ch.f0, ch.f1, io->snl, io->nbedrock, bounds->begc, hord);
-        cudaError_t e = copy_async(dfilt, hord, (size_t)num_nolakec * 4, cudaMemcpyHostToDevice, c->h2d);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
+            cudaError_t ce = copy_async(dfilt + ch.f0, hord + ch.f0, (size_t)(ch.f1 - ch.f0) * 4,
+                                        cudaMemcpyHostToDevice, c->h2d);
+            if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemcpyAsync(filter)");
+            ce = cudaEventRecord(c->ev_in[k], c->h2d);
+            return ce == cudaSuccess ? 0 : cuda_fail(ce, "cudaEventRecord");
+        };
+        cudaError_t e;
         if ((e = cudaMemsetAsync(c->err, 0xff, sizeof(DevError), c->stream)) != cudaSuccess)
             return cuda_fail(e, "cudaMemsetAsync(err)");
         int snow_method;
         { std::lock_guard<std::mutex> lk(g_mu); snow_method = g_opt.snow_thermal_cond_method; }
         const int K = (int)chunks.size();
         if ((rc = fork_streams(c))) return rc;
-        if ((rc = chunk_in(c, chunks[0], 0, io, &dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp))) return rc;
+        if ((rc = stage_chunk(0))) return rc;
         for (int k = 0; k < K; ++k) {
             const Chunk& ch = chunks[k];
             cudaStream_t ks = chunk_stream(c, k);
@@ -1264,8 +1282,7 @@ extern "C" int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds, int32_t num
                                 ws + ch.f0, num_nolakec, c->err, ks);
             if (e != cudaSuccess) return cuda_fail(e, "soiltemperature kernel launch");
             if ((e = cudaEventRecord(c->ev_done[k], ks)) != cudaSuccess) return cuda_fail(e, "record");
-            if (k + 1 < K && (rc = chunk_in(c, chunks[k + 1], k + 1, io, &dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp)))
-                return rc;
+            if (k + 1 < K && (rc = stage_chunk(k + 1))) return rc;
             if ((rc = chunk_out(c, ch, k, io, &dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp))) return rc;
         }
         if ((e = join_streams(c)) != cudaSuccess) return cuda_fail(e, "soiltemperature");
