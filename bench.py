@@ -56,6 +56,7 @@ def parse():
     p.add_argument("--ncol", type=int, default=524288)
     p.add_argument("--seed", type=int, default=2026)
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-gate", action="store_true", help="skip the oracle parity and balance check of the run")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-canopy", action="store_true")
     p.add_argument("--no-ensemble", action="store_true")
@@ -111,39 +112,123 @@ def make_inputs(ncol, seed):
 
 
 # ---------------------------------------------------------------- CPU oracle
+def bench_config(A, ncol):
+    """The workload's `config` dict: identical on both arms (it describes the
+    inputs only; how the GPU arm ran them goes under "tuning")."""
+    state_gb = sum(v.nbytes for v in A.values()) / 1e9 * ncol / A["zwt"].shape[0]
+    return {"workload": WORKLOAD, "ncol_per_gpu": ncol, "mean_snow_layers": float(-A["snl"].mean()),
+            "dtime_s": DT, "l2": "inputs larger than L2 (state %.2f GB vs 129 MB L2)" % state_gb}
+
+
+class OracleSoilStepper:
+    """The CPU oracle (C++ restatement, OpenMP over clumps of columns) stepping
+    a private copy of the first `ncol` columns of A through the benched step:
+    SoilWater (Zeng-Decker), SoilTemperature, the h2osoi_vol refresh."""
+
+    def __init__(self, A, ncol=None):
+        from ctsm_gb300 import abi
+        from oracle import oracle as orc
+        self.L = orc.lib()
+        n = A["zwt"].shape[0] if ncol is None else min(ncol, A["zwt"].shape[0])
+        self.n = n
+        # one patch per column in this workload, so patch arrays slice like column arrays
+        self.S = {k: np.array(v[..., :n], order="C", copy=True) for k, v in A.items()}
+        self.b = abi.Bounds(1, n, 1, n)
+        self.filt = np.arange(1, n + 1, dtype=np.int32)
+        self.fp = self.filt.ctypes.data_as(C.POINTER(C.c_int32))
+        self.sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS, self.S, n)
+        self.st = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, self.S, n, n)
+
+    def step(self, k=1):
+        from ctsm_gb300 import inputs
+        for _ in range(k):
+            rc = self.L.oracle_soilwater(C.byref(self.b), self.n, self.fp, C.byref(self.sw), 6.0, DT)
+            rc = rc or self.L.oracle_soiltemperature(C.byref(self.b), self.n, self.fp, C.byref(self.st), DT, 0)
+            if rc:
+                raise RuntimeError("oracle step failed (rc %d)" % rc)
+            inputs.refresh_h2osoi_vol(self.S)
+
+
+def host_threads():
+    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+
 def oracle_rate(A, npatch, target_s=10.0, max_cols=131072):
     """Column-steps/s of the CPU oracle on a bounded sample of the workload
     (the first `max_cols` columns, as many 1800 s steps as fit in ~target_s)."""
-    from ctsm_gb300 import abi, inputs
-    from oracle import oracle as orc
-    L = orc.lib()
-    n = min(max_cols, A["zwt"].shape[0])
-    S = {}
-    for k, v in A.items():
-        # one patch per column in this workload, so patch arrays slice like column arrays
-        S[k] = np.ascontiguousarray(v[:n]) if v.ndim == 1 else np.ascontiguousarray(v[:, :n])
-    np_s = n  # one patch per column in this workload
-    b = abi.Bounds(1, n, 1, np_s)
-    filt = np.arange(1, n + 1, dtype=np.int32)
-    fp = filt.ctypes.data_as(C.POINTER(C.c_int32))
-    sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS, S, n)
-    st = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, S, n, np_s)
-
-    def one():
-        L.oracle_soilwater(C.byref(b), n, fp, C.byref(sw), 6.0, DT)
-        L.oracle_soiltemperature(C.byref(b), n, fp, C.byref(st), DT, 0)
-        inputs.refresh_h2osoi_vol(S)
-
+    o = OracleSoilStepper(A, max_cols)
     t0 = time.perf_counter()
-    one()
+    o.step()
     t1 = time.perf_counter() - t0
     steps = max(1, min(64, int(target_s / max(t1, 1e-6))))
     t0 = time.perf_counter()
-    for _ in range(steps):
-        one()
+    o.step(steps)
     dt = time.perf_counter() - t0
-    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return n * steps / dt, n, steps, dt, threads
+    return o.n * steps / dt, o.n, steps, dt, host_threads()
+
+
+# ---------------------------------------------------------------- correctness gate
+# The benched run is checked against the oracle on the same inputs
+# (BalanceCheckMod.F90:592-658 water, :1103-1113 errsoi for the thresholds).
+GATE_TOL = 1e-9
+GATE_STATE = ("h2osoi_liq", "h2osoi_ice", "t_soisno")
+GATE_FLUXES = ("qcharge", "qflx_deficit", "t_grnd", "eflx_fgr12", "xmf", "qflx_snomelt", "t_h2osfc")
+
+
+def _rel_err_cols(g, r):
+    """Per-column max relative error |g-r| / (|r| + 1e-12 max|r|) over the
+    levels of one field (level-major arrays: columns on the last axis)."""
+    g = np.asarray(g, dtype=np.float64)
+    r = np.asarray(r, dtype=np.float64)
+    scale = float(np.nanmax(np.abs(r))) if r.size else 0.0
+    d = np.abs(g - r) / (np.abs(r) + 1e-12 * scale + 1e-300)
+    d = np.where(np.isnan(g) & np.isnan(r), 0.0, d)
+    d = np.where(np.isnan(g) ^ np.isnan(r), np.inf, d)
+    return d if d.ndim == 1 else d.max(axis=0)
+
+
+def compare_states(G, R, fields, tol=GATE_TOL):
+    """{field: max rel err}, and the number of columns with any field above tol."""
+    errs, worst = {}, None
+    for k in fields:
+        e = _rel_err_cols(G[k], R[k])
+        errs[k] = float(e.max()) if e.size else 0.0
+        worst = e if worst is None else np.maximum(worst, e)
+    return errs, int(np.count_nonzero(worst > tol))
+
+
+def soil_gate(A0, npatch, G, nsteps, G1, balance, identical):
+    """Parity of the benched run: (1) the GPU state after `nsteps` steps (G)
+    against the oracle stepped `nsteps` from the same initial state (A0), every
+    column; (2) one further step from the GPU's evolved state, GPU (G1) against
+    the oracle; (3) the reference's balance thresholds over every column and
+    every step after skip_steps, from a replica batch with the balance check
+    on whose final state is bit-identical to the benched one (`identical`)."""
+    from ctsm_gb300 import balance as bal
+    fields = GATE_STATE + GATE_FLUXES
+    o = OracleSoilStepper(A0)
+    t0 = time.perf_counter()
+    o.step(nsteps)
+    t_oracle = time.perf_counter() - t0
+    traj, traj_cols = compare_states(G, o.S, fields)
+    o1 = OracleSoilStepper(G)
+    o1.step(1)
+    one, one_cols = compare_states(G1, o1.S, fields)
+    h2o_max, soi_max = balance
+    finite = int(np.count_nonzero(~np.isfinite(G["t_soisno"]).all(axis=0) | ~np.isfinite(G["h2osoi_liq"]).all(axis=0)))
+    gate = {"columns": int(o.n), "steps": int(nsteps), "tol": GATE_TOL,
+            "trajectory": {"max_rel_err": traj, "columns_above_tol": traj_cols},
+            "one_step_from_evolved_state": {"max_rel_err": one, "columns_above_tol": one_cols},
+            "nonfinite_columns": finite,
+            "balance": {"errh2o_max_mm": float(np.max(h2o_max)), "errsoi_max_w_m2": float(np.max(soi_max)),
+                        "h2o_warning": bal.H2O_WARNING_THRESH, "h2o_stop": bal.ERROR_THRESH,
+                        "errsoi_warning": bal.ERRSOI_WARNING, "errsoi_stop": bal.ERRSOI_STOP,
+                        "columns_above_stop": int(np.count_nonzero((h2o_max >= bal.ERROR_THRESH) |
+                                                                   (soi_max >= bal.ERRSOI_STOP))),
+                        "replica_bit_identical": bool(identical)}}
+    gate["pass"] = bool(one_cols == 0 and finite == 0 and identical and gate["balance"]["columns_above_stop"] == 0
+                        and np.all(np.isfinite(h2o_max)) and np.all(np.isfinite(soi_max)))
+    return gate, o.n * nsteps / t_oracle, t_oracle
 
 
 def cpu_model():
@@ -220,26 +305,31 @@ def copied_bytes(reset=False):
 
 # ---------------------------------------------------------------- arms
 def reference_arm(args, ws, rank):
+    """The reference's CPU implementation of the path (the oracle port: the
+    Fortran cannot be built on either machine) on the same workload and config
+    as the GPU arm: every one of the `ncol` columns, W untimed and K timed
+    steps, all host threads."""
     if rank != 0:
         return
-    A, npatch = make_inputs(min(args.ncol, 131072), args.seed)
-    rates = []
-    for _ in range(max(1, args.warmup)):
-        oracle_rate(A, npatch, target_s=2.0, max_cols=32768)
-    sample = None
-    for _ in range(max(1, args.steps // 16)):
-        r, n, steps, dt, threads = oracle_rate(A, npatch, target_s=8.0)
-        rates.append(r)
-        sample = "first %d columns of the workload x %d steps (%.1f s)" % (n, steps, dt)
-    v = statistics.median(rates)
+    A, npatch = make_inputs(args.ncol, rank_seed(args.seed, 0))
+    cfg = bench_config(A, args.ncol)
+    o = OracleSoilStepper(A)
+    o.step(max(0, args.warmup))
+    t0 = time.perf_counter()
+    o.step(args.steps)
+    dt = time.perf_counter() - t0
+    v = o.n * args.steps / dt
+    threads = host_threads()
+    sample = "all %d columns of the workload x %d steps (%.1f s) after %d untimed steps" % (
+        o.n, args.steps, dt, args.warmup)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.ncol / v,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded Philox draws; no dataset)",
-            "config": {"workload": WORKLOAD, "ncol": args.ncol, "l2": "state > L2 (129 MB)"},
+            "data": "synthetic (seeded Philox draws; no dataset)", "config": cfg,
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
                              "cpu": cpu_model(),
-                             "note": "C++ restatement of the reference Fortran (no Fortran compiler on the build image)"},
+                             "note": "C++ restatement of the reference Fortran (no Fortran compiler on the build "
+                                     "image or the GPU box)"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -440,9 +530,11 @@ def ours_arm(args, ws, rank, local):
     A, npatch = make_inputs(args.ncol, rank_seed(args.seed, rank))
     ncol = args.ncol
     mean_snow = float(-A["snl"].mean())
+    cfg = bench_config(A, ncol)
 
     # ---------------- batched resident engine
-    batch = SoilBatch(copy.deepcopy(A), npatch, dtime=DT)
+    G = copy.deepcopy(A)
+    batch = SoilBatch(G, npatch, dtime=DT)
     block = batch.autotune(trial_steps=2)
     batch.run(args.warmup)
     batch.sync()
@@ -487,9 +579,38 @@ def ours_arm(args, ws, rank, local):
             "peak_source": peak_src, "algorithmic_bytes_per_column_step": rd + wr,
             "kernel": "soilstep_kernel", "fp64": fp64_line,
             "note": "the step is FP64-pipe bound on GB300; the HBM fraction is reported as required"}
-    state_gb = batch.state_bytes() / 1e9
-    batch.close()
-    del batch
+
+    # ---------------- correctness gate of the benched run (after the timed region)
+    gate = None
+    cpu = None
+    nsteps_run = args.warmup + args.steps
+    if not args.no_gate:
+        batch.download()                      # G: the state the timed steps left
+        G1 = copy.deepcopy(G)
+        batch.run(1)
+        batch.sync()
+        batch.download(G1)                    # one further step from that state
+        batch.close()
+        del batch
+        R = copy.deepcopy(A)
+        rb = SoilBatch(R, npatch, dtime=DT, balance=True)
+        rb.set_block(block)
+        rb.run(nsteps_run)
+        rb.sync()
+        rb.download()
+        h2o_max, soi_max, _, _ = rb.balance()
+        rb.close()
+        identical = all(np.array_equal(R[k], G[k], equal_nan=True) for k in GATE_STATE + GATE_FLUXES)
+        del R
+        gate, oracle_cs, t_oracle = soil_gate(A, npatch, G, nsteps_run, G1, (h2o_max, soi_max), identical)
+        if rank == 0 and ws == 1 and not args.no_cpu:
+            cpu = {"value": oracle_cs, "unit": UNIT, "cores": host_threads(), "kind": "port",
+                   "sample": "all %d columns x %d steps (%.1f s): the oracle run of the correctness gate"
+                             % (ncol, nsteps_run, t_oracle), "cpu": cpu_model()}
+        del G1
+    else:
+        batch.close()
+        del batch
 
     # ---------------- plain drop-in e2e (host buffers, copies in the timed region)
     e2e = None
@@ -525,9 +646,8 @@ def ours_arm(args, ws, rank, local):
                "ms_per_call": {"SoilWater": 1e3 * t_sw / ke, "SoilTemperature": 1e3 * t_st / ke},
                "path": "ctsmg_soilwater + ctsmg_soiltemperature (plain drop-in, pinned host arrays)"}
 
-    # ---------------- CPU baseline (rank 0 only, N = 1 only)
-    cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu:
+    # ---------------- CPU baseline (rank 0 only, N = 1 only) when the gate did not time the oracle
+    if cpu is None and rank == 0 and ws == 1 and not args.no_cpu:
         r, n, steps, dt, threads = oracle_rate(A, npatch)
         cpu = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": "first %d columns of the workload x %d steps (%.1f s)" % (n, steps, dt),
@@ -549,10 +669,9 @@ def ours_arm(args, ws, rank, local):
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * t_rank / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic (seeded Philox draws; no dataset)",
-                "config": {"workload": WORKLOAD, "ncol_per_gpu": ncol, "mean_snow_layers": mean_snow,
-                           "block": block, "graph": "one CUDA graph per step",
-                           "l2": "inputs larger than L2 (resident state %.2f GB vs 129 MB L2)" % state_gb},
+                "data": "synthetic (seeded Philox draws; no dataset)", "config": cfg,
+                "tuning": {"block": block, "graph": "one CUDA graph per step", "mean_snow_layers": mean_snow},
+                "parity": gate,
                 "gpu_launches": int(args.steps), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clk, "wall_s_timed": wall, "fp64_peak_tflops": fp64.value}
         line.update(extra)

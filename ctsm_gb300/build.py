@@ -1,6 +1,8 @@
 """In-tree build of libctsm_gpu.so for sm_103a (nvcc, one -gencode, parallel TUs)."""
 import concurrent.futures as cf
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 
@@ -27,13 +29,29 @@ def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
-def _stale():
-    if not os.path.exists(LIB):
-        return True
-    t = os.path.getmtime(LIB)
-    deps = sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+STAMP = os.path.join(BUILD, "stamp")
+
+
+def _digest():
+    """Hash of every source and header, the flags and the host architecture:
+    the library is rebuilt whenever any of them differs from the last build."""
+    h = hashlib.sha256()
+    deps = sources() + sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h")))
     deps.append(os.path.join(ROOT, "include", "ctsm_gpu.h"))
-    return any(os.path.getmtime(d) > t for d in deps)
+    for d in deps:
+        h.update(os.path.basename(d).encode())
+        with open(d, "rb") as f:
+            h.update(f.read())
+    h.update(" ".join(ARCH + NVFLAGS).encode())
+    h.update(platform.machine().encode())
+    return h.hexdigest()
+
+
+def _stale():
+    if not os.path.exists(LIB) or not os.path.exists(STAMP):
+        return True
+    with open(STAMP) as f:
+        return f.read().strip() != _digest()
 
 
 def build(force=False, verbose=False):
@@ -60,6 +78,12 @@ def build(force=False, verbose=False):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stderr)
     os.replace(tmp, LIB)
+    with open(STAMP, "w") as f:
+        f.write(_digest() + "\n")
+    with open(os.path.join(BUILD, "build.log"), "w") as f:
+        f.write(" ".join([nv] + ARCH + NVFLAGS) + "\n")
+        for src, (_, log) in zip(sources(), results):
+            f.write("%s\n%s" % (os.path.basename(src), log))
     if verbose:
         for _, log in results:
             print(log)

@@ -1005,6 +1005,13 @@ int current_snow_method() {
     return g_init ? g_opt.snow_thermal_cond_method : 0;
 }
 
+bool snow_method_if_init(int* method) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_init) return false;
+    *method = g_opt.snow_thermal_cond_method;
+    return true;
+}
+
 } // namespace ctsmg
 
 using namespace ctsmg;
@@ -1073,6 +1080,7 @@ extern "C" int32_t ctsmg_finalize(void) {
     t_ctx = nullptr;
     ++g_gen;
     g_init = false;
+    noalloc_forget_devices();
     return 0;
 }
 

@@ -41,6 +41,12 @@ size_t field_bytes(const FieldDesc& f, int ldc, int ldp, int ldg = 0);
 int set_error(int code, const char* what, int index, int level);
 int check_filter(const ctsmg_bounds* b, int nf, const int32_t* filt);
 int current_snow_method();
+// false when ctsmg_init has not been called (or ctsmg_finalize came after it);
+// otherwise the snow thermal conductivity method in force goes to *method
+bool snow_method_if_init(int* method);
+// drops the per-device addresses the allocation-free SoilTemperature looked up
+// (ctsmg_finalize; the next call after ctsmg_init looks them up again)
+void noalloc_forget_devices();
 // the soilwater_movement_inparm namelist in force (ctsmg_init / ctsmg_set_soilwater_movement)
 ctsmg_soilwater_movement_nml current_soilwater_nml();
 ctsmg_soil_resistance_params current_soil_resistance();

@@ -1077,10 +1077,18 @@ static std::mutex g_noalloc_mu;
 static double* g_noalloc_ws_addr[NOALLOC_MAX_DEVICES];
 static DevError* g_noalloc_err_addr[NOALLOC_MAX_DEVICES];
 
-// Same work as soiltemp_kernel, with the filter and patch indices checked on
-// the device (the caller's filter is in device memory, so the host cannot
-// check it without a staging copy): a bad index is recorded as CTSMG_E_ARG and
-// that column is skipped.
+// Error levels of the allocation-free call's device checks (every record
+// carries the filter position, 1-based, so records rank by position).
+constexpr int NOALLOC_BAD_FILTER = -1;     // filter entry outside begc..endc
+constexpr int NOALLOC_BAD_SNL = -2;        // snl outside -nlevsno..0
+constexpr int NOALLOC_BAD_NBEDROCK = -3;   // nbedrock outside 1..nlevgrnd
+constexpr int NOALLOC_BAD_PATCHES = -4;    // the column's patches outside begp..endp
+
+// Same work as soiltemp_kernel, with the filter entry and the column's snl,
+// nbedrock and patch range checked on the device (the caller's filter and
+// arrays are in device memory, so the host cannot check them without a
+// staging copy): a bad entry is recorded as CTSMG_E_ARG with its filter
+// position and a level code naming the check, and that column is skipped.
 __global__ void __launch_bounds__(128)
 soiltemp_noalloc_kernel(ctsmg_soiltemp_io io, int begc, int endc, int begp, int endp, int nfilt,
                         const int32_t* __restrict__ filt, double dtime, int snow_method, double* ws,
@@ -1088,20 +1096,23 @@ soiltemp_noalloc_kernel(ctsmg_soiltemp_io io, int begc, int endc, int begp, int 
     const int fc = blockIdx.x * blockDim.x + threadIdx.x;
     if (fc >= nfilt) return;
     const int cg = filt ? filt[fc] : begc + fc;
-    if (cg < begc || cg > endc) { report_error(err, fc + 1, 0, CTSMG_E_ARG); return; }
+    if (cg < begc || cg > endc) { report_error(err, fc + 1, NOALLOC_BAD_FILTER, CTSMG_E_ARG); return; }
     const int c = cg - begc;
-    const int snl = io.snl[c], pi = io.col_patchi[c], np = io.col_npatches[c];
-    if (snl > 0 || snl < -NLEVSNO || np < 0 || pi < begp || pi + np - 1 > endp) {
-        report_error(err, cg, 0, CTSMG_E_ARG);
-        return;
-    }
+    const int snl = io.snl[c], nbr = io.nbedrock[c], pi = io.col_patchi[c], np = io.col_npatches[c];
+    int bad = 0;
+    if (snl > 0 || snl < -NLEVSNO) bad = NOALLOC_BAD_SNL;
+    else if (nbr < 1 || nbr > NLEVGRND) bad = NOALLOC_BAD_NBEDROCK;
+    else if (np < 0 || pi < begp || pi + np - 1 > endp) bad = NOALLOC_BAD_PATCHES;
+    if (bad) { report_error(err, fc + 1, bad, CTSMG_E_ARG); return; }
     Scratch S{ws, NOALLOC_MAX_COLUMNS, fc};
     int info = soiltemp_column(io, c, begp, dtime, snow_method, S);
-    if (info != 0) report_error(err, cg, info, CTSMG_E_SINGULAR);
+    if (info != 0) report_error(err, fc + 1, info, CTSMG_E_SINGULAR);
 }
 
 // Looks up the device addresses of the scratch array and the error record
-// once per device, with that device current.
+// once per device, with that device current.  ctsmg_finalize clears the table
+// (noalloc_forget_devices), so after a device reset the caller runs
+// ctsmg_finalize and ctsmg_init and the next call looks the addresses up anew.
 static int noalloc_setup(int dev, double** ws, DevError** err) {
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
         return set_error(CTSMG_E_UNSUPPORTED, "device ordinal beyond the allocation-free table", dev, 0);
@@ -1120,12 +1131,23 @@ static int noalloc_setup(int dev, double** ws, DevError** err) {
     *err = g_noalloc_err_addr[dev];
     return 0;
 }
+
+void noalloc_forget_devices() {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    for (int d = 0; d < NOALLOC_MAX_DEVICES; ++d) {
+        g_noalloc_ws_addr[d] = nullptr;
+        g_noalloc_err_addr[d] = nullptr;
+    }
+}
 } // namespace ctsmg
 
 extern "C" int32_t ctsmg_soiltemperature_noalloc(const ctsmg_bounds* bounds, int32_t num_nolakec,
                                                  const int32_t* filter_nolakec_dev,
                                                  const ctsmg_soiltemp_io* io_dev, double dtime, void* stream) {
     using namespace ctsmg;
+    int snow_method = 0;
+    if (!snow_method_if_init(&snow_method))
+        return set_error(CTSMG_E_NOT_INIT, "ctsmg_init has not been called", 0, 0);
     if (!bounds || !io_dev) return set_error(CTSMG_E_ARG, "null bounds or io", 0, 0);
     if (bounds->endc < bounds->begc || bounds->endp < bounds->begp - 1)
         return set_error(CTSMG_E_ARG, "empty or inverted bounds", 0, 0);
@@ -1152,81 +1174,29 @@ extern "C" int32_t ctsmg_soiltemperature_noalloc(const ctsmg_bounds* bounds, int
     if (e != cudaSuccess) return set_error(CTSMG_E_CUDA, cudaGetErrorString(e), 0, 0);
     soiltemp_noalloc_kernel<<<(num_nolakec + 127) / 128, 128, 0, s>>>(
         *io_dev, bounds->begc, bounds->endc, bounds->begp, bounds->endp, num_nolakec, filter_nolakec_dev, dtime,
-        current_snow_method(), ws, err);
+        snow_method, ws, err);
     e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(CTSMG_E_CUDA, cudaGetErrorString(e), 0, 0);
     DevError h;
     e = cudaMemcpyAsync(&h, err, sizeof h, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return set_error(CTSMG_E_CUDA, cudaGetErrorString(e), 0, 0);
-    if (h.key != ~0ull) {
-        const int code = (int)(h.key & 0xff);
-        const int idx = (int)(h.key >> 32), lev = (int)((h.key >> 8) & 0xffffff) - 1024;
-        return set_error(code, code == CTSMG_E_SINGULAR ? "BandDiagonal ERROR: dgbsv returned error code"
-                                                        : "filter or patch index outside the bounds", idx, lev);
+    if (h.key == ~0ull) return 0;
+    const int code = (int)(h.key & 0xff);
+    const int pos = (int)(h.key >> 32), lev = (int)((h.key >> 8) & 0xffffff) - 1024;
+    if (code == CTSMG_E_SINGULAR) {
+        // the reference's endrun names the column: read that filter entry back
+        int32_t col = bounds->begc + pos - 1;
+        if (filter_nolakec_dev) {
+            e = cudaMemcpyAsync(&col, filter_nolakec_dev + (pos - 1), sizeof col, cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) return set_error(CTSMG_E_CUDA, cudaGetErrorString(e), 0, 0);
+        }
+        return set_error(code, "BandDiagonal ERROR: dgbsv returned error code", col, lev);
     }
-    return 0;
-}
-
-// ---------------------------------------------------------------- diagnostic
-namespace ctsmg {
-__global__ void diag_powers_kernel(int n, const double* __restrict__ a, const double* __restrict__ b,
-                                   double* __restrict__ out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    out[i] = pow(10.0, a[i]);
-    out[n + i] = pow10_dd(a[i]);
-    out[2 * (size_t)n + i] = pow(TKWAT, a[i]) * pow(TKICE, b[i]);
-    out[3 * (size_t)n + i] = tkwat_tkice_pow(a[i], b[i]);
-}
-__global__ void diag_fastmath_kernel(int n, const double* __restrict__ x, const double* __restrict__ y,
-                                     double* __restrict__ out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const size_t N = (size_t)n;
-    out[i] = fm::log(x[i]);
-    out[N + i] = fm::log10(x[i]);
-    out[2 * N + i] = fm::exp(y[i]);
-    out[3 * N + i] = fm::pow(x[i], y[i]);
-    out[4 * N + i] = log(x[i]);
-    out[5 * N + i] = log10(x[i]);
-    out[6 * N + i] = exp(y[i]);
-    out[7 * N + i] = pow(x[i], y[i]);
-}
-} // namespace ctsmg
-
-extern "C" int32_t ctsmg_diag_fastmath(int32_t n, const double* x, const double* y, double* out) {
-    using namespace ctsmg;
-    if (n <= 0 || !x || !y || !out) return set_error(CTSMG_E_ARG, "bad arguments", 0, 0);
-    double* d = nullptr;
-    const size_t nb = (size_t)n * 8;
-    cudaError_t e = cudaMalloc(&d, 10 * nb);
-    if (e == cudaSuccess) e = cudaMemcpy(d, x, nb, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(d + n, y, nb, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) {
-        diag_fastmath_kernel<<<(n + 127) / 128, 128>>>(n, d, d + n, d + 2 * (size_t)n);
-        e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * (size_t)n, 8 * nb, cudaMemcpyDeviceToHost);
-    if (d) cudaFree(d);
-    if (e != cudaSuccess) return set_error(CTSMG_E_CUDA, cudaGetErrorString(e), 0, 0);
-    return 0;
-}
-
-extern "C" int32_t ctsmg_diag_powers(int32_t n, const double* a, const double* b, double* out) {
-    using namespace ctsmg;
-    if (n <= 0 || !a || !b || !out) return set_error(CTSMG_E_ARG, "bad arguments", 0, 0);
-    double* d = nullptr;
-    const size_t nb = (size_t)n * 8;
-    cudaError_t e = cudaMalloc(&d, 6 * nb);
-    if (e == cudaSuccess) e = cudaMemcpy(d, a, nb, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(d + n, b, nb, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) {
-        diag_powers_kernel<<<(n + 127) / 128, 128>>>(n, d, d + n, d + 2 * (size_t)n);
-        e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * (size_t)n, 4 * nb, cudaMemcpyDeviceToHost);
-    if (d) cudaFree(d);
-    if (e != cudaSuccess) return set_error(CTSMG_E_CUDA, cudaGetErrorString(e), 0, 0);
-    return 0;
+    const char* what = lev == NOALLOC_BAD_FILTER ? "filter entry outside begc..endc (index = filter position)"
+                     : lev == NOALLOC_BAD_SNL ? "snl outside -nlevsno..0 (index = filter position)"
+                     : lev == NOALLOC_BAD_NBEDROCK ? "nbedrock outside 1..nlevgrnd (index = filter position)"
+                     : "column patches outside begp..endp (index = filter position)";
+    return set_error(code, what, pos, lev);
 }

@@ -9,8 +9,8 @@ NLEVSNO, NLEVSOI, NLEVGRND = abi.NLEVSNO, abi.NLEVSOI, abi.NLEVGRND
 # FP64 floating-point operations per column-step of soilstep_kernel on the
 # uneven-column workload (DADD + DMUL + 2 x DFMA executed, libm included),
 # from the ncu capture of 65,536 columns of the same workload, and DRAM bytes
-# per column-step from the 1-pass capture of the full 524,288-column launch;
-# both summarised in profiles/soilstep_kernel_uneven_columns.md.  The capture
+# per column-step from the 1-pass capture of the full 524,288-column launch.
+# The capture
 # predates the Zeng-Decker solve's carrying of each interface's flux and
 # derivatives from one level to the next (3 divisions and 9 other FP64
 # operations fewer per level) and the heat system's carrying of each row's
@@ -24,7 +24,7 @@ TRAFFIC_PER_COLUMN_STEP = (6665794560 + 4179119872) / 524288.0
 # (canopy_iterate_kernel: DADD + DMUL + 2 x DFMA executed over 262,144 patches
 # of the canopy workload, 5.508 passes per patch on average), and DRAM bytes
 # per patch-step of that kernel from the 1-pass capture of the full
-# 2,097,152-patch launch (profiles/canopy_iterate_kernel_canopy_workload.md).
+# 2,097,152-patch launch.
 CANOPY_FLOPS_PER_PASS = (489099825 + 889105990 + 2 * 2293152799) / (262144 * 5.507728576660156)
 CANOPY_TRAFFIC_PER_PATCH_STEP = (39389850624 + 15903046144) / 2097152.0
 

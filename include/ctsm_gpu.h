@@ -682,10 +682,16 @@ int32_t ctsmg_soilfluxes(const ctsmg_bounds* bounds, int32_t num_nolakec, const 
  * caller (filter NULL = begc..begc+num_nolakec-1); the call allocates nothing:
  * the band-solve scratch is a fixed array inside the library, sized for at
  * most 16384 columns per call (larger filters return CTSMG_E_ARG).  The first
- * call on a device looks up that array's address (make it before any stream
- * capture).  All calls share the one array, so calls that overlap on the GPU
- * (other streams, other host threads) race: serialise them.  stream is a
- * cudaStream_t (NULL = default stream); the call waits for it to finish. */
+ * call on a device after ctsmg_init looks up that array's address (make it
+ * before any stream capture); ctsmg_finalize forgets the addresses, so after a
+ * device reset the caller runs ctsmg_finalize and ctsmg_init again.  Without
+ * ctsmg_init the call returns CTSMG_E_NOT_INIT.  A filter entry outside
+ * begc..endc, or a column whose snl, nbedrock or patch range is out of bounds,
+ * is skipped and returns CTSMG_E_ARG with its filter position as the index;
+ * the other columns are computed.  All calls share the one array, so calls
+ * that overlap on the GPU (other streams, other host threads) race: serialise
+ * them.  stream is a cudaStream_t (NULL = default stream); the call waits for
+ * it to finish. */
 int32_t ctsmg_soiltemperature_noalloc(const ctsmg_bounds* bounds, int32_t num_nolakec,
                                       const int32_t* filter_nolakec_dev, const ctsmg_soiltemp_io* io_dev,
                                       double dtime, void* stream);
@@ -894,19 +900,6 @@ int32_t ctsmg_copy_bytes(int64_t* h2d, int64_t* d2h, int32_t reset);
 /* FP64 FMA throughput of the current GPU in TFLOP/s (a DFMA loop over every
  * SM); the denominator of the FP64 roofline fraction.  No reference counterpart. */
 int32_t ctsmg_measure_fp64_tflops(double* tflops);
-/* Diagnostic for the tests (no reference counterpart): for each i, out[i] =
- * pow(10, a[i]) and out[n+i] = the soil step's exp form of it; out[2n+i] =
- * pow(tkwat, a[i]) * pow(tkice, b[i]) and out[3n+i] = the exp form of that
- * product.  Host arrays; out holds 4n doubles. */
-int32_t ctsmg_diag_powers(int32_t n, const double* a, const double* b, double* out);
-/* Diagnostic for the tests (no reference counterpart): the table-driven
- * logarithm, exponential and power of the column kernels beside CUDA's.  For
- * each i: out[i] = log(x[i]), out[n+i] = log10(x[i]), out[2n+i] = exp(y[i]),
- * out[3n+i] = pow(x[i], y[i]) by the kernels' forms, and out[4n+i] ..
- * out[7n+i] the same four by the CUDA math library.  Host arrays; out holds
- * 8n doubles. */
-int32_t ctsmg_diag_fastmath(int32_t n, const double* x, const double* y, double* out);
-
 #ifdef __cplusplus
 }
 #endif

@@ -1,20 +1,22 @@
 """Regenerates the golden fixtures in this directory from the reference's own
-tests and technical-note tables (read as text; run in the build container,
-where the reference checkout is mounted at /root/reference):
+tests and technical-note tables, read as text from a checkout of the
+reference whose path is the one required argument:
 
   layer_table_20sl.json  doc/source/tech_note/Ecosystem/CLM50_Tech_Note_Ecosystem.rst:164-219
   skip_steps.json        src/biogeophys/test/Balance_test/test_Balance.pf:40-105
   quadratic_kat.json     src/utils/test/quadratic_test/test_quadratic.pf
   qsat_coeffs.json       src/biogeophys/QSatMod.F90:16-54
 
-    python tests/golden/make_golden.py [/root/reference]
+    python tests/golden/make_golden.py <path of the reference checkout>
 """
 import json
 import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: make_golden.py <path of the reference checkout>")
+REF = sys.argv[1]
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 

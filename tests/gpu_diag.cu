@@ -1,0 +1,75 @@
+// gpu_diag.cu -- test-only library (not part of libctsm_gpu.so): the column
+// kernels' device math beside CUDA's functions, for the GPU tests.
+//   ctsmg_diag_powers(n, a, b, out): out[i] = pow(10, a[i]), out[n+i] = the
+//     soil step's exp form of it, out[2n+i] = pow(tkwat, a[i]) * pow(tkice,
+//     b[i]), out[3n+i] = the exp form of that product (4n doubles).
+//   ctsmg_diag_fastmath(n, x, y, out): the table-driven log, log10, exp, pow
+//     (rows 0-3) and CUDA's log, log10, exp, pow (rows 4-7) (8n doubles).
+// Host arrays in and out.  Built by tests/gpu_diag.py with nvcc for sm_103a.
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "ctsm_gpu.h"
+#include "ctsm_device.cuh"
+#include "soil_math.cuh"
+
+static int32_t diag_fail(cudaError_t e) { return e == cudaSuccess ? 0 : CTSMG_E_CUDA; }
+
+namespace ctsmg {
+__global__ void diag_powers_kernel(int n, const double* __restrict__ a, const double* __restrict__ b,
+                                   double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = pow(10.0, a[i]);
+    out[n + i] = pow10_dd(a[i]);
+    out[2 * (size_t)n + i] = pow(TKWAT, a[i]) * pow(TKICE, b[i]);
+    out[3 * (size_t)n + i] = tkwat_tkice_pow(a[i], b[i]);
+}
+__global__ void diag_fastmath_kernel(int n, const double* __restrict__ x, const double* __restrict__ y,
+                                     double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t N = (size_t)n;
+    out[i] = fm::log(x[i]);
+    out[N + i] = fm::log10(x[i]);
+    out[2 * N + i] = fm::exp(y[i]);
+    out[3 * N + i] = fm::pow(x[i], y[i]);
+    out[4 * N + i] = log(x[i]);
+    out[5 * N + i] = log10(x[i]);
+    out[6 * N + i] = exp(y[i]);
+    out[7 * N + i] = pow(x[i], y[i]);
+}
+} // namespace ctsmg
+
+extern "C" int32_t ctsmg_diag_fastmath(int32_t n, const double* x, const double* y, double* out) {
+    using namespace ctsmg;
+    if (n <= 0 || !x || !y || !out) return CTSMG_E_ARG;
+    double* d = nullptr;
+    const size_t nb = (size_t)n * 8;
+    cudaError_t e = cudaMalloc(&d, 10 * nb);
+    if (e == cudaSuccess) e = cudaMemcpy(d, x, nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d + n, y, nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        diag_fastmath_kernel<<<(n + 127) / 128, 128>>>(n, d, d + n, d + 2 * (size_t)n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * (size_t)n, 8 * nb, cudaMemcpyDeviceToHost);
+    if (d) cudaFree(d);
+    return diag_fail(e);
+}
+
+extern "C" int32_t ctsmg_diag_powers(int32_t n, const double* a, const double* b, double* out) {
+    using namespace ctsmg;
+    if (n <= 0 || !a || !b || !out) return CTSMG_E_ARG;
+    double* d = nullptr;
+    const size_t nb = (size_t)n * 8;
+    cudaError_t e = cudaMalloc(&d, 6 * nb);
+    if (e == cudaSuccess) e = cudaMemcpy(d, a, nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d + n, b, nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        diag_powers_kernel<<<(n + 127) / 128, 128>>>(n, d, d + n, d + 2 * (size_t)n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * (size_t)n, 4 * nb, cudaMemcpyDeviceToHost);
+    if (d) cudaFree(d);
+    return diag_fail(e);
+}

@@ -77,3 +77,36 @@ def test_reference_arm_json_line(capsys):
     assert line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"] == {"value": line["value"], "unit": bench.UNIT, "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
+    # the same workload config dict as the GPU arm builds from the same inputs
+    A, _ = bench.make_inputs(Args.ncol, bench.rank_seed(Args.seed, 0))
+    assert line["config"] == json.loads(json.dumps(bench.bench_config(A, Args.ncol)))
+    assert "all 2048 columns" in line["cpu_baseline"]["sample"]
+
+
+def test_soil_gate_passes_on_oracle_states_and_flags_a_planted_error():
+    """The bench's correctness gate, fed oracle states in place of the GPU's:
+    identical states pass; a planted 1e-7 relative error in one column of the
+    one-step state is caught and counted."""
+    import copy
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    import bench
+    A, npatch = bench.make_inputs(512, 7)
+    o = bench.OracleSoilStepper(A)
+    o.step(3)
+    G = copy.deepcopy(o.S)
+    o.step(1)
+    G1 = copy.deepcopy(o.S)
+    zero = (np.zeros(512), np.zeros(512))
+    gate, rate, _ = bench.soil_gate(A, npatch, G, 3, G1, zero, True)
+    assert gate["pass"] and rate > 0
+    assert gate["trajectory"]["columns_above_tol"] == 0 and gate["one_step_from_evolved_state"]["columns_above_tol"] == 0
+    assert all(v == 0.0 for v in gate["trajectory"]["max_rel_err"].values())
+    bad = copy.deepcopy(G1)
+    bad["t_soisno"][-1, 100] *= 1.0 + 1e-7
+    gate, _, _ = bench.soil_gate(A, npatch, G, 3, bad, zero, True)
+    assert not gate["pass"] and gate["one_step_from_evolved_state"]["columns_above_tol"] == 1
+    assert gate["one_step_from_evolved_state"]["max_rel_err"]["t_soisno"] > 5e-8
+    over = (np.full(512, 2e-5), np.zeros(512))
+    gate, _, _ = bench.soil_gate(A, npatch, G, 3, G1, over, True)
+    assert not gate["pass"] and gate["balance"]["columns_above_stop"] == 512

@@ -19,10 +19,9 @@ def _ulps(x, ref):
 
 
 def test_device_matches_host_and_cuda(gpu_lib, tmp_path):
-    from ctsm_gb300._lib import load, check
+    from gpu_diag import load, check
     L = load()
     P = C.POINTER(C.c_double)
-    L.ctsmg_diag_fastmath.argtypes = [C.c_int32, P, P, P]
     r = np.random.Generator(np.random.Philox(5))
     n = 1 << 20
     q = n // 4

@@ -18,10 +18,9 @@ def _ulps(x, ref):
 
 
 def test_constant_base_powers(gpu_lib):
-    from ctsm_gb300._lib import load, check
+    from gpu_diag import load, check
     L = load()
     P = C.POINTER(C.c_double)
-    L.ctsmg_diag_powers.argtypes = [C.c_int32, P, P, P]
     r = np.random.Generator(np.random.Philox(3))
     n = 200000
     x = np.concatenate([-6.0 * r.uniform(0, 1, n - 4), [0.0, -0.0, -6.0, -1e-300]])
