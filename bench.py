@@ -123,9 +123,13 @@ def bench_config(A, ncol):
 class OracleSoilStepper:
     """The CPU oracle (C++ restatement, OpenMP over clumps of columns) stepping
     a private copy of the first `ncol` columns of A through the benched step:
-    SoilWater (Zeng-Decker), SoilTemperature, the h2osoi_vol refresh."""
+    SoilWater (Zeng-Decker), SoilTemperature, the h2osoi_vol refresh.  With
+    noise = (ulps, seed) every libm result of the oracle is perturbed by up to
+    `ulps` ulp (a deterministic hash of its arguments); with track_water the
+    column water budget error of every step (BalanceCheckMod.F90:592-658 over
+    the scoped fluxes) is kept as water_err_max."""
 
-    def __init__(self, A, ncol=None):
+    def __init__(self, A, ncol=None, noise=None, track_water=False):
         from ctsm_gb300 import abi
         from oracle import oracle as orc
         self.L = orc.lib()
@@ -138,15 +142,39 @@ class OracleSoilStepper:
         self.fp = self.filt.ctypes.data_as(C.POINTER(C.c_int32))
         self.sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS, self.S, n)
         self.st = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, self.S, n, n)
+        self.noise = noise
+        self.water_err_max = np.zeros(n) if track_water else None
+
+    def _water(self):
+        from ctsm_gb300.abi import NLEVSNO, NLEVSOI
+        S = self.S
+        LS = -NLEVSNO + 1
+        w = S["h2osfc"] + S["h2osno_no_layers"]
+        for j in range(LS, NLEVSOI + 1):
+            w = w + np.where(j >= S["snl"] + 1, S["h2osoi_liq"][j - LS] + S["h2osoi_ice"][j - LS], 0.0)
+        return w
 
     def step(self, k=1):
         from ctsm_gb300 import inputs
-        for _ in range(k):
-            rc = self.L.oracle_soilwater(C.byref(self.b), self.n, self.fp, C.byref(self.sw), 6.0, DT)
-            rc = rc or self.L.oracle_soiltemperature(C.byref(self.b), self.n, self.fp, C.byref(self.st), DT, 0)
-            if rc:
-                raise RuntimeError("oracle step failed (rc %d)" % rc)
-            inputs.refresh_h2osoi_vol(self.S)
+        from ctsm_gb300.abi import NLEVSNO, NLEVSOI
+        if self.noise:
+            self.L.oracle_set_libm_noise(int(self.noise[0]), int(self.noise[1]))
+        try:
+            for _ in range(k):
+                w0 = self._water() if self.water_err_max is not None else None
+                rc = self.L.oracle_soilwater(C.byref(self.b), self.n, self.fp, C.byref(self.sw), 6.0, DT)
+                rc = rc or self.L.oracle_soiltemperature(C.byref(self.b), self.n, self.fp, C.byref(self.st), DT, 0)
+                if rc:
+                    raise RuntimeError("oracle step failed (rc %d)" % rc)
+                if w0 is not None:
+                    S = self.S
+                    deep = S["zwt"] > S["zi"][NLEVSOI + NLEVSNO]
+                    net = (S["qflx_infl"] - S["qflx_rootsoi"].sum(axis=0) - np.where(deep, S["qcharge"], 0.0)) * DT
+                    np.maximum(self.water_err_max, np.abs((self._water() - w0) - net), out=self.water_err_max)
+                inputs.refresh_h2osoi_vol(self.S)
+        finally:
+            if self.noise:
+                self.L.oracle_set_libm_noise(0, 0)
 
 
 def host_threads():
@@ -168,65 +196,129 @@ def oracle_rate(A, npatch, target_s=10.0, max_cols=131072):
 
 
 # ---------------------------------------------------------------- correctness gate
-# The benched run is checked against the oracle on the same inputs
-# (BalanceCheckMod.F90:592-658 water, :1103-1113 errsoi for the thresholds).
+# The benched run is checked against the oracle on the same inputs.  State
+# variables and well-conditioned outputs are held to 1e-9 relative; the two
+# outputs that difference nearly equal terms -- eflx_fgr12 (heat flux between
+# levels 1 and 2 from the new temperatures, SoilTemperatureMod.F90:572-595)
+# and xmf (latent heat of phase change summed over levels, :1492-1502) -- to
+# 1e-9 relative plus the oracle's own spread under 4-ulp libm noise (and, for
+# eflx_fgr12, the rounding bound of the two temperatures it differences), the
+# test the parity suite applies.  Thresholds of BalanceCheckMod.F90:592-658
+# (water) and :1103-1113 (errsoi).
 GATE_TOL = 1e-9
 GATE_STATE = ("h2osoi_liq", "h2osoi_ice", "t_soisno")
-GATE_FLUXES = ("qcharge", "qflx_deficit", "t_grnd", "eflx_fgr12", "xmf", "qflx_snomelt", "t_h2osfc")
+GATE_FLUXES = ("qcharge", "qflx_deficit", "t_grnd", "qflx_snomelt", "t_h2osfc")
+GATE_CANCEL = ("eflx_fgr12", "xmf")
+GATE_NOISE_ULPS = 4
+GATE_NOISE_RUNS = 4
 
 
-def _rel_err_cols(g, r):
+def _rel_err_cols(g, r, band=None):
     """Per-column max relative error |g-r| / (|r| + 1e-12 max|r|) over the
-    levels of one field (level-major arrays: columns on the last axis)."""
+    levels of one field (level-major arrays: columns on the last axis); with a
+    band, (|g-r| - band) clipped at 0 over 1e-9 |r| scaled to the same units."""
     g = np.asarray(g, dtype=np.float64)
     r = np.asarray(r, dtype=np.float64)
     scale = float(np.nanmax(np.abs(r))) if r.size else 0.0
-    d = np.abs(g - r) / (np.abs(r) + 1e-12 * scale + 1e-300)
+    d = np.abs(g - r)
+    if band is not None:
+        d = np.maximum(d - band, 0.0)
+    d = d / (np.abs(r) + 1e-12 * scale + 1e-300)
     d = np.where(np.isnan(g) & np.isnan(r), 0.0, d)
     d = np.where(np.isnan(g) ^ np.isnan(r), np.inf, d)
     return d if d.ndim == 1 else d.max(axis=0)
 
 
-def compare_states(G, R, fields, tol=GATE_TOL):
-    """{field: max rel err}, and the number of columns with any field above tol."""
+def compare_states(G, R, fields, tol=GATE_TOL, bands=None):
+    """{field: max rel err}, and the per-column bool of any field above tol."""
     errs, worst = {}, None
     for k in fields:
-        e = _rel_err_cols(G[k], R[k])
+        e = _rel_err_cols(G[k], R[k], None if bands is None else bands.get(k))
         errs[k] = float(e.max()) if e.size else 0.0
         worst = e if worst is None else np.maximum(worst, e)
-    return errs, int(np.count_nonzero(worst > tol))
+    return errs, worst > tol
 
 
-def soil_gate(A0, npatch, G, nsteps, G1, balance, identical):
-    """Parity of the benched run: (1) the GPU state after `nsteps` steps (G)
-    against the oracle stepped `nsteps` from the same initial state (A0), every
-    column; (2) one further step from the GPU's evolved state, GPU (G1) against
-    the oracle; (3) the reference's balance thresholds over every column and
-    every step after skip_steps, from a replica batch with the balance check
-    on whose final state is bit-identical to the benched one (`identical`)."""
+def fgr12_rounding_bound(R, ulps=8):
+    """(1-cnfac) tk_1 ulps eps (|T_1| + |T_2|) / (z_2 - z_1): the error of
+    eflx_fgr12 that the rounding of the two new temperatures alone allows,
+    with tk_1 the interface conductivity of SoilTemperatureMod.F90:822-828."""
+    from ctsm_gb300.abi import NLEVSNO
+    eps = np.finfo(np.float64).eps
+    r1, r2 = 1 + NLEVSNO - 1, 2 + NLEVSNO - 1
+    t1, t2 = R["thk"][r1], R["thk"][r2]
+    z1, z2, zi = R["z"][r1], R["z"][r2], R["zi"][1 + NLEVSNO]
+    tk = t1 * t2 * (z2 - z1) / (t1 * (z2 - zi) + t2 * (zi - z1))
+    return 0.5 * np.abs(tk) * ulps * eps * (np.abs(R["t_soisno"][r1]) + np.abs(R["t_soisno"][r2])) / (z2 - z1)
+
+
+def soil_gate(A0, npatch, G, nsteps, G1, balance, identical, sensitivity_runs=4):
+    """Parity of the benched run.
+    (1) One step from the GPU's evolved state: the GPU's next step (G1)
+        against the oracle's step from the same state (G), every column.
+    (2) The trajectory: the GPU state after `nsteps` steps (G) against the
+        oracle stepped `nsteps` from the same initial state (A0), every
+        column.  Phase change switches on and off at the freezing point on an
+        ulp of temperature, so trajectories of an FP64 code part where a level
+        sits at the threshold; columns that do are counted, together with the
+        columns where the oracle itself parts from its own trajectory when
+        every libm result it uses is perturbed by 2 ulp (`sensitivity_runs`
+        realisations): the reference's own sensitivity.
+    (3) The reference's balance thresholds over every column and every step
+        after skip_steps, from a replica batch with the balance check on whose
+        final state is bit-identical to the benched one (`identical`), beside
+        the oracle's own water budget error over the same steps."""
     from ctsm_gb300 import balance as bal
-    fields = GATE_STATE + GATE_FLUXES
-    o = OracleSoilStepper(A0)
+    state = GATE_STATE + GATE_FLUXES
+    # (1)
+    o1 = OracleSoilStepper(G)
+    o1.step(1)
+    bands = {k: np.zeros_like(o1.S[k]) for k in GATE_CANCEL}
+    for seed in range(1, GATE_NOISE_RUNS + 1):
+        on = OracleSoilStepper(G, noise=(GATE_NOISE_ULPS, seed))
+        on.step(1)
+        for k in GATE_CANCEL:
+            np.maximum(bands[k], np.abs(on.S[k] - o1.S[k]), out=bands[k])
+        del on
+    bands["eflx_fgr12"] = bands["eflx_fgr12"] + fgr12_rounding_bound(o1.S)
+    one, one_bad = compare_states(G1, o1.S, state)
+    one_c, one_c_bad = compare_states(G1, o1.S, GATE_CANCEL, bands=bands)
+    one.update({k + " (conditioned)": v for k, v in one_c.items()})
+    one_bad = one_bad | one_c_bad
+    del o1
+    # (2)
+    o = OracleSoilStepper(A0, track_water=True)
     t0 = time.perf_counter()
     o.step(nsteps)
     t_oracle = time.perf_counter() - t0
-    traj, traj_cols = compare_states(G, o.S, fields)
-    o1 = OracleSoilStepper(G)
-    o1.step(1)
-    one, one_cols = compare_states(G1, o1.S, fields)
+    traj, traj_bad = compare_states(G, o.S, GATE_STATE)
+    sens = np.zeros(o.n, dtype=bool)
+    for seed in range(1, sensitivity_runs + 1):
+        on = OracleSoilStepper(A0, noise=(2, 100 + seed))
+        on.step(nsteps)
+        sens |= compare_states(on.S, o.S, GATE_STATE)[1]
+        del on
     h2o_max, soi_max = balance
     finite = int(np.count_nonzero(~np.isfinite(G["t_soisno"]).all(axis=0) | ~np.isfinite(G["h2osoi_liq"]).all(axis=0)))
     gate = {"columns": int(o.n), "steps": int(nsteps), "tol": GATE_TOL,
-            "trajectory": {"max_rel_err": traj, "columns_above_tol": traj_cols},
-            "one_step_from_evolved_state": {"max_rel_err": one, "columns_above_tol": one_cols},
+            "one_step_from_evolved_state": {"max_rel_err": one, "columns_above_tol": int(one_bad.sum()),
+                                            "conditioned": list(GATE_CANCEL)},
+            "trajectory": {"max_rel_err": traj, "columns_above_tol": int(traj_bad.sum()),
+                           "oracle_self_sensitive_columns": int(sens.sum()),
+                           "above_tol_and_sensitive": int((traj_bad & sens).sum()),
+                           "sensitivity": "oracle vs itself with every libm result perturbed by up to 2 ulp, "
+                                          "%d realisations" % sensitivity_runs},
             "nonfinite_columns": finite,
             "balance": {"errh2o_max_mm": float(np.max(h2o_max)), "errsoi_max_w_m2": float(np.max(soi_max)),
+                        "oracle_errh2o_max_mm": float(o.water_err_max.max()),
                         "h2o_warning": bal.H2O_WARNING_THRESH, "h2o_stop": bal.ERROR_THRESH,
                         "errsoi_warning": bal.ERRSOI_WARNING, "errsoi_stop": bal.ERRSOI_STOP,
+                        "columns_above_warning": int(np.count_nonzero((h2o_max >= bal.H2O_WARNING_THRESH) |
+                                                                      (soi_max >= bal.ERRSOI_WARNING))),
                         "columns_above_stop": int(np.count_nonzero((h2o_max >= bal.ERROR_THRESH) |
                                                                    (soi_max >= bal.ERRSOI_STOP))),
                         "replica_bit_identical": bool(identical)}}
-    gate["pass"] = bool(one_cols == 0 and finite == 0 and identical and gate["balance"]["columns_above_stop"] == 0
+    gate["pass"] = bool(not one_bad.any() and finite == 0 and identical and gate["balance"]["columns_above_stop"] == 0
                         and np.all(np.isfinite(h2o_max)) and np.all(np.isfinite(soi_max)))
     return gate, o.n * nsteps / t_oracle, t_oracle
 

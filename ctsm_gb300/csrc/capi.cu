@@ -50,7 +50,7 @@ static cudaError_t copy_sync(void* dst, const void* src, size_t n, cudaMemcpyKin
 
 // ------------------------------------------------------------ global state
 static std::mutex g_mu;
-static bool g_init = false;
+static std::atomic<bool> g_init{false};   // read without g_mu by every entry point
 static ctsmg_options g_opt;
 static ctsmg_soilwater_params g_swp = {6.0};
 // soil_resis_inparm and the two parameter-file values (the parameter file is
@@ -108,7 +108,7 @@ struct ThreadCtx {
 };
 static thread_local ThreadCtx* t_ctx = nullptr;
 static thread_local unsigned t_gen = 0;
-static unsigned g_gen = 1;               // bumped by ctsmg_finalize
+static std::atomic<unsigned> g_gen{1};   // bumped by ctsmg_finalize
 static std::vector<ThreadCtx*> g_ctxs;
 
 static thread_local std::string t_msg;

@@ -5,12 +5,16 @@
 //     b[i]), out[3n+i] = the exp form of that product (4n doubles).
 //   ctsmg_diag_fastmath(n, x, y, out): the table-driven log, log10, exp, pow
 //     (rows 0-3) and CUDA's log, log10, exp, pow (rows 4-7) (8n doubles).
+//   ctsmg_diag_crdiv(n, a, b, out): out[i] = a[i] / b[i] (CUDA), out[n+i] =
+//     the shared-reciprocal quotient of cr_div.cuh, out[2n+i] = its
+//     reciprocal RN(1/b[i]) (3n doubles).
 // Host arrays in and out.  Built by tests/gpu_diag.py with nvcc for sm_103a.
 #include <cuda_runtime.h>
 #include <cstdint>
 #include "ctsm_gpu.h"
 #include "ctsm_device.cuh"
 #include "soil_math.cuh"
+#include "cr_div.cuh"
 
 static int32_t diag_fail(cudaError_t e) { return e == cudaSuccess ? 0 : CTSMG_E_CUDA; }
 
@@ -70,6 +74,35 @@ extern "C" int32_t ctsmg_diag_powers(int32_t n, const double* a, const double* b
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * (size_t)n, 4 * nb, cudaMemcpyDeviceToHost);
+    if (d) cudaFree(d);
+    return diag_fail(e);
+}
+
+namespace ctsmg {
+__global__ void diag_crdiv_kernel(int n, const double* __restrict__ a, const double* __restrict__ b,
+                                  double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Recip R = recip(b[i]);
+    out[i] = a[i] / b[i];
+    out[n + i] = divr(a[i], R);
+    out[2 * (size_t)n + i] = R.y;
+}
+} // namespace ctsmg
+
+extern "C" int32_t ctsmg_diag_crdiv(int32_t n, const double* a, const double* b, double* out) {
+    using namespace ctsmg;
+    if (n <= 0 || !a || !b || !out) return CTSMG_E_ARG;
+    double* d = nullptr;
+    const size_t nb = (size_t)n * 8;
+    cudaError_t e = cudaMalloc(&d, 5 * nb);
+    if (e == cudaSuccess) e = cudaMemcpy(d, a, nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d + n, b, nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        diag_crdiv_kernel<<<(n + 127) / 128, 128>>>(n, d, d + n, d + 2 * (size_t)n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * (size_t)n, 3 * nb, cudaMemcpyDeviceToHost);
     if (d) cudaFree(d);
     return diag_fail(e);
 }

@@ -33,6 +33,7 @@ def load():
         P = C.POINTER(C.c_double)
         _LIB.ctsmg_diag_fastmath.argtypes = [C.c_int32, P, P, P]
         _LIB.ctsmg_diag_powers.argtypes = [C.c_int32, P, P, P]
+        _LIB.ctsmg_diag_crdiv.argtypes = [C.c_int32, P, P, P]
     return _LIB
 
 

@@ -89,3 +89,31 @@ def test_canopy_ragged(canopy_lib, npatch):
     spread = _band(A, R, npatch, ncol, ngrid, filt)
     errs, bad = compare(G, R, [k for k in OUT if k != "err_canopy"], 1e-9, spread)
     assert not bad, {k: errs[k] for k in bad}
+
+
+def test_canopy_ball_berry_matches_oracle(canopy_lib, gpu_lib):
+    """Ball-Berry 1987 stomatal conductance (stomatalcond_method = 0,
+    PhotosynthesisMod.F90:2684-2690 in ci_func, :1962-1974 for rs): the same
+    parity bar as the Medlyn default, with identical pass counts."""
+    gpu_lib.init(stomatalcond_method=0)
+    try:
+        A, npatch, ncol, ngrid = ci.canopy_patches(20000, seed=5)
+        filt = np.arange(1, npatch + 1, dtype=np.int32)
+        G, R = copy.deepcopy(A), copy.deepcopy(A)
+        run_oracle(R, npatch, ncol, ngrid, filt, method=0)
+        canopy_lib.CanopyFluxes(abi.Bounds(1, ncol, 1, npatch), npatch, filt, G, DT, ngrid)
+        # the Medlyn default gives other conductances: the method did switch
+        M = copy.deepcopy(A)
+        run_oracle(M, npatch, ncol, ngrid, filt, method=1)
+        assert np.abs(M["rssun"] - R["rssun"]).max() > 1.0
+        np.testing.assert_array_equal(G["num_iter"], R["num_iter"])
+        sp = noise_spread(lambda B: run_oracle(B, npatch, ncol, ngrid, filt, method=0), A, R,
+                          fields=CANOPY_CANCELLATION, input_ulps=4)
+        operand = np.abs(A["liqcan"]) + np.abs(A["snocan"])
+        sp["liqcan"] = sp["liqcan"] + 1e-9 * operand
+        sp["snocan"] = sp["snocan"] + 1e-9 * operand
+        errs, bad = compare(G, R, [k for k in OUT if k != "err_canopy"], 1e-9, sp)
+        assert not bad, {k: errs[k] for k in bad}
+        assert np.abs(G["err_canopy"] - R["err_canopy"]).max() < 1e-9
+    finally:
+        gpu_lib.init()
