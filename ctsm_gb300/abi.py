@@ -258,6 +258,18 @@ def soilwater_movement_nml(method=1, upper=1, lower=None, flux_calculation=1, us
                                 verySmall, xTolerUpper, xTolerLower)
 
 
+ROOTSINK_FIELDS = [
+    ("col_patchi", "C", I32, "in"), ("col_npatches", "C", I32, "in"), ("wtcol", "P", F64, "in"),
+    ("qflx_tran_veg", "P", F64, "in"), ("qflx_tran_veg_col", "C", F64, "in"), ("rootr", "PG", F64, "in"),
+    ("rootr_col", "G", F64, "out"), ("qflx_rootsoi", "S", F64, "out"),
+]
+
+
+class RootSinkIO(C.Structure):
+    _fields_ = [("ldc", C.c_int32), ("ldp", C.c_int32)] + \
+               [(n, _ptr_type(t)) for (n, _, t, _) in ROOTSINK_FIELDS]
+
+
 class RootMoistIO(C.Structure):
     _fields_ = [("ldc", C.c_int32), ("ldp", C.c_int32)] + \
                [(n, _ptr_type(t)) for (n, _, t, _) in ROOTMOIST_FIELDS]

@@ -244,6 +244,13 @@ const FieldDesc SOILWATER_FLEXCN_TABLE[] = {
     FW(ctsmg_soilwater_io, wa, K_C, 8, U_INOUT),
 };
 const int SOILWATER_FLEXCN_NFIELDS = sizeof(SOILWATER_FLEXCN_TABLE) / sizeof(SOILWATER_FLEXCN_TABLE[0]);
+// SetSoilWaterFractions: levels 1..nlevsoi of the soil components
+const FieldDesc SOILWATER_FRACTIONS_TABLE[] = {
+    SWR(dz, K_SS, U_IN, SS1, NLEVSOI, 0), SWR(h2osoi_ice, K_SS, U_IN, SS1, NLEVSOI, 0),
+    SWR(watsat, K_G, U_IN, 0, NLEVSOI, 0), SWR(eff_porosity, K_G, U_INOUT, 0, NLEVSOI, 0),
+    SWR(icefrac, K_G, U_INOUT, 0, NLEVSOI, 0),
+};
+const int SOILWATER_FRACTIONS_NFIELDS = sizeof(SOILWATER_FRACTIONS_TABLE) / sizeof(SOILWATER_FRACTIONS_TABLE[0]);
 
 // calc_soilevap_resis: sl_14 (dsl, soilresis) and leepielke_1992 (soilbeta)
 const FieldDesc SOILRESIS_SL14_TABLE[] = {
@@ -534,6 +541,18 @@ const FieldDesc SOILTEMP_TABLE[] = {
 const int SOILTEMP_NFIELDS = sizeof(SOILTEMP_TABLE) / sizeof(SOILTEMP_TABLE[0]);
 
 #define FC(name, kind, esz, use) FW(ctsmg_canopy_io, name, kind, esz, use)
+// Compute_EffecRootFrac_And_VertTranSink_Default: levels 1..nlevsoi of rootr
+// (patches) and of the two column outputs
+const FieldDesc ROOTSINK_TABLE[] = {
+    FW(ctsmg_rootsink_io, col_patchi, K_C, 4, U_IN), FW(ctsmg_rootsink_io, col_npatches, K_C, 4, U_IN),
+    FW(ctsmg_rootsink_io, wtcol, K_P, 8, U_IN), FW(ctsmg_rootsink_io, qflx_tran_veg, K_P, 8, U_IN),
+    FWR(ctsmg_rootsink_io, rootr, K_PG, 8, U_IN, 0, NLEVSOI, 0),
+    FWR(ctsmg_rootsink_io, rootr_col, K_G, 8, U_INOUT, 0, NLEVSOI, 0),
+    FW(ctsmg_rootsink_io, qflx_rootsoi, K_S, 8, U_INOUT),
+};
+const int ROOTSINK_NFIELDS = sizeof(ROOTSINK_TABLE) / sizeof(ROOTSINK_TABLE[0]);
+const FieldDesc ROOTSINK_TRANCOL_TABLE[] = {FW(ctsmg_rootsink_io, qflx_tran_veg_col, K_C, 8, U_IN)};
+
 #define FR(name, kind, esz, use) FW(ctsmg_rootmoist_io, name, kind, esz, use)
 const FieldDesc ROOTMOIST_TABLE[] = {
     FR(h2osoi_liq, K_SS, 8, U_IN),
@@ -744,9 +763,32 @@ size_t field_bytes(const FieldDesc& f, int ldc, int ldp, int ldg) {
     return (size_t)ld * kind_levels(f.kind) * f.esize;
 }
 
+// One field's levels between the caller's array and its device copy (both
+// with leading dimension ld): only the n columns (patches) the call's bounds
+// span of each level move, so a clump that passes a view into arrays shared
+// with other clumps (c_loc(field(begc, lb)) with the processor-wide leading
+// dimension) reads and writes its own columns alone.
+static cudaError_t copy_field(void* dst, const void* src, const FieldDesc& f, int ld, int n, cudaMemcpyKind k,
+                              cudaStream_t s) {
+    const size_t es = f.esize, pitch = (size_t)ld * es, off = copy_row0(f) * pitch;
+    const size_t rows = copy_rows(f);
+    if (n >= ld) return copy_async(static_cast<char*>(dst) + off, static_cast<const char*>(src) + off, rows * pitch, k, s);
+    if (n <= 0) return cudaSuccess;
+    return copy_2d_async(static_cast<char*>(dst) + off, pitch, static_cast<const char*>(src) + off, pitch,
+                         (size_t)n * es, rows, k, s);
+}
+
+// Leading dimension and bounds extent of a field's kind (gridcell arrays move whole).
+static void field_extent(const FieldDesc& f, int ldc, int ldp, int ldg, int nc, int np, int* ld, int* n) {
+    const bool pf = f.kind == K_P || f.kind == K_PL || f.kind == K_PS || f.kind == K_PG;
+    *ld = pf ? ldp : (f.kind == K_GR ? ldg : ldc);
+    *n = pf ? (np < 0 ? ldp : np) : (f.kind == K_GR ? ldg : (nc < 0 ? ldc : nc));
+}
+
 // Copy the host struct's arrays into the arena; fill dio with device pointers.
+// nc / np: columns / patches of the call's bounds (-1: the whole leading dimension).
 static int stage_in(ThreadCtx* c, const void* hio, void* dio, size_t io_size, const FieldDesc* tab, int nf,
-                    int ldc, int ldp, int ldg = 0) {
+                    int ldc, int ldp, int ldg, int nc, int np) {
     std::memcpy(dio, hio, io_size);
     for (int i = 0; i < nf; ++i) {
         const void* hp = field_ptr(const_cast<void*>(hio), tab[i]);
@@ -757,9 +799,9 @@ static int stage_in(ThreadCtx* c, const void* hio, void* dio, size_t io_size, co
         size_t nb = field_bytes(tab[i], ldc, ldp, ldg);
         void* dp = arena_take(c, nb);
         if (!tab[i].no_in) {
-            const size_t row = nb / kind_levels(tab[i].kind), off = copy_row0(tab[i]) * row;
-            cudaError_t e = copy_async(static_cast<char*>(dp) + off, static_cast<const char*>(hp) + off,
-                                            copy_rows(tab[i]) * row, cudaMemcpyHostToDevice, c->stream);
+            int ld, n;
+            field_extent(tab[i], ldc, ldp, ldg, nc, np, &ld, &n);
+            cudaError_t e = copy_field(dp, hp, tab[i], ld, n, cudaMemcpyHostToDevice, c->stream);
             if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync H2D");
         }
         field_ptr(dio, tab[i]) = dp;
@@ -768,15 +810,14 @@ static int stage_in(ThreadCtx* c, const void* hio, void* dio, size_t io_size, co
 }
 
 static int stage_out(ThreadCtx* c, const void* hio, const void* dio, const FieldDesc* tab, int nf,
-                     int ldc, int ldp, int ldg = 0) {
+                     int ldc, int ldp, int ldg, int nc, int np) {
     for (int i = 0; i < nf; ++i) {
         if (tab[i].use == U_IN) continue;
         void* hp = field_ptr(const_cast<void*>(hio), tab[i]);
         const void* dp = field_ptr(const_cast<void*>(dio), tab[i]);
-        const size_t nb = field_bytes(tab[i], ldc, ldp, ldg), row = nb / kind_levels(tab[i].kind),
-                     off = copy_row0(tab[i]) * row;
-        cudaError_t e = copy_async(static_cast<char*>(hp) + off, static_cast<const char*>(dp) + off,
-                                        copy_rows(tab[i]) * row, cudaMemcpyDeviceToHost, c->stream);
+        int ld, n;
+        field_extent(tab[i], ldc, ldp, ldg, nc, np, &ld, &n);
+        cudaError_t e = copy_field(hp, dp, tab[i], ld, n, cudaMemcpyDeviceToHost, c->stream);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync D2H");
     }
     return 0;
@@ -1210,14 +1251,14 @@ extern "C" int32_t ctsmg_soilwater(const ctsmg_bounds* bounds, int32_t num_hydro
         if ((e = join_streams(c)) != cudaSuccess) return cuda_fail(e, "soilwater");
     } else {
         ctsmg_soilwater_io dio;
-        if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, 0))) return rc;
+        if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, 0, 0, bounds->endc - bounds->begc + 1, -1))) return rc;
         int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_hydrologyc * 4);
         e = copy_async(dfilt, filter_hydrologyc, (size_t)num_hydrologyc * 4, cudaMemcpyHostToDevice, c->stream);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
         e = launch_soilwater_call(dio, bounds->begc, num_hydrologyc, dfilt, nml, e_ice, dtime, c->err, c->stream,
                                   dcounter);
         if (e != cudaSuccess) return cuda_fail(e, "soilwater kernel launch");
-        if ((rc = stage_out(c, io, &dio, T, NT, ldc, 0))) return rc;
+        if ((rc = stage_out(c, io, &dio, T, NT, ldc, 0, 0, bounds->endc - bounds->begc + 1, -1))) return rc;
         e = cudaStreamSynchronize(c->stream);
         if (e != cudaSuccess) return cuda_fail(e, "soilwater");
     }
@@ -1300,7 +1341,7 @@ extern "C" int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds, int32_t num
         return 0;
     }
     ctsmg_soiltemp_io dio;
-    if ((rc = stage_in(c, io, &dio, sizeof dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp))) return rc;
+    if ((rc = stage_in(c, io, &dio, sizeof dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp, 0, bounds->endc - bounds->begc + 1, bounds->endp - bounds->begp + 1))) return rc;
     int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_nolakec * 4);
     double* ws = (double*)arena_take(c, ws_bytes);
     int32_t* hord = order_buffer(c, (size_t)num_nolakec);
@@ -1315,7 +1356,7 @@ extern "C" int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds, int32_t num
     e = launch_soiltemp(dio, bounds->begc, bounds->begp, num_nolakec, dfilt, dtime, snow_method, ws,
                         num_nolakec, c->err, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "soiltemperature kernel launch");
-    if ((rc = stage_out(c, io, &dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp))) return rc;
+    if ((rc = stage_out(c, io, &dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp, 0, bounds->endc - bounds->begc + 1, bounds->endp - bounds->begp + 1))) return rc;
     e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "soiltemperature");
     int code = 0, idx = 0, lev = 0;
@@ -1367,7 +1408,7 @@ extern "C" int32_t ctsmg_canopyfluxes(const ctsmg_bounds* bounds, int32_t num_ex
                   canopy_ws_bytes(num_exposedvegp) + 8192;
     if ((rc = arena_reserve(c, need))) return rc;
     CanopyArgs a;
-    if ((rc = stage_in(c, io, &a.io, sizeof a.io, CANOPY_TABLE, CANOPY_NFIELDS, ldc, ldp, ldg))) return rc;
+    if ((rc = stage_in(c, io, &a.io, sizeof a.io, CANOPY_TABLE, CANOPY_NFIELDS, ldc, ldp, ldg, bounds->endc - bounds->begc + 1, bounds->endp - bounds->begp + 1))) return rc;
     int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_exposedvegp * 4);
     int* counter = (int*)arena_take(c, 256);
     double* cws = (double*)arena_take(c, canopy_ws_bytes(num_exposedvegp));
@@ -1389,7 +1430,7 @@ extern "C" int32_t ctsmg_canopyfluxes(const ctsmg_bounds* bounds, int32_t num_ex
     a.medlynintercept_p = nullptr;
     e = launch_canopy(a, num_exposedvegp, dfilt, dtime, counter, c->err, cws, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "canopy kernel launch");
-    if ((rc = stage_out(c, io, &a.io, CANOPY_TABLE, CANOPY_NFIELDS, ldc, ldp, ldg))) return rc;
+    if ((rc = stage_out(c, io, &a.io, CANOPY_TABLE, CANOPY_NFIELDS, ldc, ldp, ldg, bounds->endc - bounds->begc + 1, bounds->endp - bounds->begp + 1))) return rc;
     e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "canopyfluxes");
     int code = 0, idx = 0, lev = 0;
@@ -1438,7 +1479,7 @@ extern "C" int32_t ctsmg_soilfluxes(const ctsmg_bounds* bounds, int32_t num_nola
                   ((size_t)num_nolakec + (size_t)num_nolakep) * 4 + 8192;
     if ((rc = arena_reserve(c, need))) return rc;
     ctsmg_soilfluxes_io dio;
-    if ((rc = stage_in(c, io, &dio, sizeof dio, SOILFLUXES_TABLE, SOILFLUXES_NFIELDS, ldc, ldp))) return rc;
+    if ((rc = stage_in(c, io, &dio, sizeof dio, SOILFLUXES_TABLE, SOILFLUXES_NFIELDS, ldc, ldp, 0, bounds->endc - bounds->begc + 1, bounds->endp - bounds->begp + 1))) return rc;
     int32_t* dfc = (int32_t*)arena_take(c, (size_t)num_nolakec * 4 + 4);
     int32_t* dfp = (int32_t*)arena_take(c, (size_t)num_nolakep * 4 + 4);
     cudaError_t e = cudaSuccess;
@@ -1449,7 +1490,7 @@ extern "C" int32_t ctsmg_soilfluxes(const ctsmg_bounds* bounds, int32_t num_nola
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
     e = launch_soilfluxes(dio, bounds->begc, bounds->begp, num_nolakec, dfc, num_nolakep, dfp, dtime, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "soilfluxes kernel launch");
-    if ((rc = stage_out(c, io, &dio, SOILFLUXES_TABLE, SOILFLUXES_NFIELDS, ldc, ldp))) return rc;
+    if ((rc = stage_out(c, io, &dio, SOILFLUXES_TABLE, SOILFLUXES_NFIELDS, ldc, ldp, 0, bounds->endc - bounds->begc + 1, bounds->endp - bounds->begp + 1))) return rc;
     e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "soilfluxes");
     return 0;
@@ -1483,14 +1524,14 @@ extern "C" int32_t ctsmg_root_moist_stress(const ctsmg_bounds* bounds, int32_t n
     size_t need = table_bytes(ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, ldc, ldp) + (size_t)num_exposedvegp * 4 + 4096;
     if ((rc = arena_reserve(c, need))) return rc;
     ctsmg_rootmoist_io dio;
-    if ((rc = stage_in(c, io, &dio, sizeof dio, ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, ldc, ldp))) return rc;
+    if ((rc = stage_in(c, io, &dio, sizeof dio, ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, ldc, ldp, 0, bounds->endc - bounds->begc + 1, bounds->endp - bounds->begp + 1))) return rc;
     int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_exposedvegp * 4);
     cudaError_t e = copy_async(dfilt, filter_exposedvegp, (size_t)num_exposedvegp * 4, cudaMemcpyHostToDevice,
                                     c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
     e = launch_rootmoist(dio, pft, bounds->begc, bounds->begp, num_exposedvegp, dfilt, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "root moisture stress kernel launch");
-    if ((rc = stage_out(c, io, &dio, ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, ldc, ldp))) return rc;
+    if ((rc = stage_out(c, io, &dio, ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, ldc, ldp, 0, bounds->endc - bounds->begc + 1, bounds->endp - bounds->begp + 1))) return rc;
     e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "root moisture stress");
     return 0;
@@ -1502,6 +1543,74 @@ extern "C" int32_t ctsmg_set_soil_resistance(const ctsmg_soil_resistance_params*
         return set_error(CTSMG_E_ARG, "calc_soilevap_resis:: a soilevap resis function must be specified!", 0, 0);
     std::lock_guard<std::mutex> lk(g_mu);
     g_sres = *p;
+    return 0;
+}
+
+extern "C" int32_t ctsmg_set_soil_water_fractions(const ctsmg_bounds* bounds, int32_t num_hydrologyc,
+                                                  const int32_t* filter_hydrologyc, const ctsmg_soilwater_io* io) {
+    ThreadCtx* c;
+    int rc = ctx_get(&c);
+    if (rc) return rc;
+    if (!io) return set_error(CTSMG_E_ARG, "null io", 0, 0);
+    if ((rc = check_filter(bounds, num_hydrologyc, filter_hydrologyc))) return rc;
+    const int ncol = bounds->endc - bounds->begc + 1;
+    if (io->ldc < ncol) return set_error(CTSMG_E_ARG, "ldc smaller than endc-begc+1", 0, 0);
+    if (num_hydrologyc == 0) return 0;
+    const int ldc = io->ldc;
+    const FieldDesc* T = SOILWATER_FRACTIONS_TABLE;
+    const int NT = SOILWATER_FRACTIONS_NFIELDS;
+    if ((rc = arena_reserve(c, table_bytes(T, NT, ldc, 0) + (size_t)num_hydrologyc * 4 + 4096))) return rc;
+    ctsmg_soilwater_io dio;
+    if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, 0, 0, bounds->endc - bounds->begc + 1, -1))) return rc;
+    int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_hydrologyc * 4);
+    cudaError_t e = copy_async(dfilt, filter_hydrologyc, (size_t)num_hydrologyc * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
+    e = launch_set_soil_water_fractions(dio, bounds->begc, num_hydrologyc, dfilt, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "soil water fractions kernel launch");
+    if ((rc = stage_out(c, io, &dio, T, NT, ldc, 0, 0, bounds->endc - bounds->begc + 1, -1))) return rc;
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "soil water fractions");
+    return 0;
+}
+
+extern "C" int32_t ctsmg_root_sink(const ctsmg_bounds* bounds, int32_t num_filterc, const int32_t* filterc,
+                                   const ctsmg_rootsink_io* io) {
+    ThreadCtx* c;
+    int rc = ctx_get(&c);
+    if (rc) return rc;
+    if (!io) return set_error(CTSMG_E_ARG, "null io", 0, 0);
+    if ((rc = check_filter(bounds, num_filterc, filterc))) return rc;
+    if (bounds->endp < bounds->begp - 1) return set_error(CTSMG_E_ARG, "bad patch bounds", 0, 0);
+    const int ncol = bounds->endc - bounds->begc + 1, npat = bounds->endp - bounds->begp + 1;
+    if (io->ldc < ncol || io->ldp < npat) return set_error(CTSMG_E_ARG, "ldc/ldp smaller than the bounds", 0, 0);
+    if (!io->col_patchi || !io->col_npatches) return set_error(CTSMG_E_ARG, "null col_patchi / col_npatches", 0, 0);
+    for (int i = 0; i < num_filterc; ++i) {
+        const int cc = filterc[i] - bounds->begc;
+        const int pi = io->col_patchi[cc], np = io->col_npatches[cc];
+        if (np < 0 || (np > 0 && (pi < bounds->begp || pi + np - 1 > bounds->endp)))
+            return set_error(CTSMG_E_ARG, "column patches outside begp..endp", filterc[i], 0);
+    }
+    if (num_filterc == 0) return 0;
+    const int ldc = io->ldc, ldp = io->ldp;
+    const bool tc = io->qflx_tran_veg_col != nullptr;
+    size_t need = table_bytes(ROOTSINK_TABLE, ROOTSINK_NFIELDS, ldc, ldp) + (size_t)num_filterc * 4 + 4096 +
+                  (tc ? table_bytes(ROOTSINK_TRANCOL_TABLE, 1, ldc, ldp) : 0);
+    if ((rc = arena_reserve(c, need))) return rc;
+    ctsmg_rootsink_io dio;
+    if ((rc = stage_in(c, io, &dio, sizeof dio, ROOTSINK_TABLE, ROOTSINK_NFIELDS, ldc, ldp, 0, bounds->endc - bounds->begc + 1, bounds->endp - bounds->begp + 1))) return rc;
+    if (tc) {
+        ctsmg_rootsink_io tmp;
+        if ((rc = stage_in(c, io, &tmp, sizeof tmp, ROOTSINK_TRANCOL_TABLE, 1, ldc, ldp, 0, bounds->endc - bounds->begc + 1, bounds->endp - bounds->begp + 1))) return rc;
+        dio.qflx_tran_veg_col = tmp.qflx_tran_veg_col;
+    }
+    int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_filterc * 4);
+    cudaError_t e = copy_async(dfilt, filterc, (size_t)num_filterc * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
+    e = launch_rootsink_dropin(dio, bounds->begc, bounds->begp, num_filterc, dfilt, c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "root sink kernel launch");
+    if ((rc = stage_out(c, io, &dio, ROOTSINK_TABLE, ROOTSINK_NFIELDS, ldc, ldp, 0, bounds->endc - bounds->begc + 1, bounds->endp - bounds->begp + 1))) return rc;
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "root sink");
     return 0;
 }
 
@@ -1521,14 +1630,14 @@ extern "C" int32_t ctsmg_soilevap_resis(const ctsmg_bounds* bounds, int32_t num_
     const int ldc = io->ldc;
     if ((rc = arena_reserve(c, table_bytes(T, NT, ldc, 0) + (size_t)num_nolakec * 4 + 4096))) return rc;
     ctsmg_soilresis_io dio;
-    if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, 0))) return rc;
+    if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, 0, 0, bounds->endc - bounds->begc + 1, -1))) return rc;
     int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_nolakec * 4);
     cudaError_t e = copy_async(dfilt, filter_nolakec, (size_t)num_nolakec * 4, cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
     const SoilResisArgs a{par.soil_resis_method, par.d_max, par.frac_sat_soil_dsl_init};
     e = launch_soilevap_resis(dio, bounds->begc, num_nolakec, dfilt, a, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "soil resistance kernel launch");
-    if ((rc = stage_out(c, io, &dio, T, NT, ldc, 0))) return rc;
+    if ((rc = stage_out(c, io, &dio, T, NT, ldc, 0, 0, bounds->endc - bounds->begc + 1, -1))) return rc;
     e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "soil resistance");
     return 0;
@@ -1568,7 +1677,7 @@ extern "C" int32_t ctsmg_baregroundfluxes(const ctsmg_bounds* bounds, int32_t nu
     size_t need = table_bytes(T, NT, ldc, ldp, ldg) + (size_t)num_noexposedvegp * 4 + (size_t)ldc * 4 + 8192;
     if ((rc = arena_reserve(c, need))) return rc;
     ctsmg_baregrnd_io dio;
-    if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, ldp, ldg))) return rc;
+    if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, ldp, ldg, bounds->endc - bounds->begc + 1, bounds->endp - bounds->begp + 1))) return rc;
     int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_noexposedvegp * 4);
     int* dlast = (int*)arena_take(c, (size_t)ldc * 4);
     cudaError_t e = copy_async(dfilt, filter_noexposedvegp, (size_t)num_noexposedvegp * 4, cudaMemcpyHostToDevice,
@@ -1577,7 +1686,7 @@ extern "C" int32_t ctsmg_baregroundfluxes(const ctsmg_bounds* bounds, int32_t nu
     const BareArgs a{cp.a_coef, cp.a_exp, cp.wind_min, cp.zetamaxstable, sres.soil_resis_method};
     e = launch_baregrnd(dio, bounds->begc, bounds->begp, num_noexposedvegp, dfilt, a, dlast, ldc, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "bare ground kernel launch");
-    if ((rc = stage_out(c, io, &dio, T, NT, ldc, ldp, ldg))) return rc;
+    if ((rc = stage_out(c, io, &dio, T, NT, ldc, ldp, ldg, bounds->endc - bounds->begc + 1, bounds->endp - bounds->begp + 1))) return rc;
     e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "bare ground fluxes");
     return 0;
@@ -1619,13 +1728,13 @@ static int hydrology_call(const ctsmg_bounds* bounds, int32_t n, const int32_t* 
     const int ldc = io->ldc;
     if ((rc = arena_reserve(c, table_bytes(T, NT, ldc, 0) + (size_t)n * 4 + 4096))) return rc;
     ctsmg_hydrology_io dio;
-    if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, 0))) return rc;
+    if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, 0, 0, bounds->endc - bounds->begc + 1, -1))) return rc;
     int32_t* dfilt = (int32_t*)arena_take(c, (size_t)n * 4);
     cudaError_t e = copy_async(dfilt, filt, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
     e = launch_hydrology(dio, bounds->begc, n, dfilt, which, current_soilhydrology_params(), dtime, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "hydrology kernel launch");
-    if ((rc = stage_out(c, io, &dio, T, NT, ldc, 0))) return rc;
+    if ((rc = stage_out(c, io, &dio, T, NT, ldc, 0, 0, bounds->endc - bounds->begc + 1, -1))) return rc;
     e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "hydrology");
     return 0;

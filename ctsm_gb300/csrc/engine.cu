@@ -44,6 +44,7 @@ struct Batch {
     SoilResisArgs sra{};
     HydroStepArgs hya{};
     double* hyd_params = nullptr;         // per-column baseflow_scalar / fff (positions order)
+    double* dmax_c = nullptr;             // per-column d_max of the soil resistance (positions order)
     MoistureFormArgs mfa{};
     CanopyArgs cargs{};
     double* rootr = nullptr;
@@ -148,7 +149,7 @@ static void batch_free(Batch* b) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
     for (auto& f : b->fields) if (f.dptr) cudaFree(f.dptr);
     for (void* p : {(void*)b->d_perm, (void*)b->ws, (void*)b->err, b->snapshot, (void*)b->rootr, (void*)b->mslope,
-                    (void*)b->mint, (void*)b->counter, (void*)b->cws, b->bal_mem, (void*)b->hyd_params,
+                    (void*)b->mint, (void*)b->counter, (void*)b->cws, b->bal_mem, (void*)b->hyd_params, (void*)b->dmax_c,
                     (void*)b->mf_counter})
         if (p) cudaFree(p);
     if (b->ev0) cudaEventDestroy(b->ev0);
@@ -380,6 +381,15 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
             dev_io(b->dsr, sr, sizeof(int32_t));
             if ((rc = add(SOILRESIS_SL14_TABLE, SOILRESIS_SL14_NFIELDS, sr, &b->dsr))) return fail(rc);
             b->sra = SoilResisArgs{1, sres.d_max, sres.frac_sat_soil_dsl_init};
+            if (in->d_max_c) {      // per-column d_max, in the batch's position order
+                const size_t cb = (size_t)ncol * 8;
+                if ((e = cudaMalloc(&b->dmax_c, 2 * cb)) != cudaSuccess) return fail(cuda_err(e, "d_max"));
+                if ((e = cudaMemcpy(b->dmax_c + ncol, in->d_max_c, cb, cudaMemcpyHostToDevice)) != cudaSuccess ||
+                    (e = launch_permute(b->dmax_c, b->dmax_c + ncol, b->d_perm, ncol, 1, 8, 0, b->stream)) != cudaSuccess ||
+                    (e = cudaStreamSynchronize(b->stream)) != cudaSuccess)
+                    return fail(cuda_err(e, "d_max"));
+                b->sra.d_max_c = b->dmax_c;
+            }
         }
         if (cfg->rootmoist) {
             dev_io(b->drm, rm, 2 * sizeof(int32_t));

@@ -464,6 +464,22 @@ cudaError_t launch_moisture_form(const ctsmg_soilwater_io& io, int begc, int nfi
     return cudaGetLastError();
 }
 
+// SetSoilWaterFractions (src/biogeophys/SoilHydrologyMod.F90:236-249) as a
+// drop-in over a column filter.
+__global__ void __launch_bounds__(128)
+swfrac_kernel(ctsmg_soilwater_io io, int begc, int nfilt, const int32_t* __restrict__ filt) {
+    const int fc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fc >= nfilt) return;
+    set_soil_water_fractions(io, (filt ? filt[fc] : fc + begc) - begc);
+}
+
+cudaError_t launch_set_soil_water_fractions(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt,
+                                            cudaStream_t s) {
+    if (nfilt <= 0) return cudaSuccess;
+    swfrac_kernel<<<(nfilt + 127) / 128, 128, 0, s>>>(io, begc, nfilt, d_filt);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_flexcn(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt, cudaStream_t s) {
     if (nfilt <= 0) return cudaSuccess;
     flexcn_kernel<<<(nfilt + 127) / 128, 128, 0, s>>>(io, begc, nfilt, d_filt);

@@ -43,6 +43,8 @@ struct HydroStepArgs {
 cudaError_t launch_mf_step(const ctsmg_soilwater_io& io, int ncol, const MoistureFormArgs& P, int flexcn, int refresh,
                            DevError* err, const int32_t* d_filt, cudaStream_t s, int* d_counter,
                            const HydroStepArgs* hy = nullptr);
+cudaError_t launch_set_soil_water_fractions(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt,
+                                            cudaStream_t s);
 cudaError_t launch_flexcn(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt, cudaStream_t s);
 
 } // namespace ctsmg

@@ -18,6 +18,7 @@
 #include <mutex>
 #include "soil_kernels.cuh"
 #include "soil_math.cuh"
+#include "cr_div.cuh"
 #include "moisture_form_device.cuh"
 #include "moisture_form_kernels.cuh"
 #include "hydrology_device.cuh"
@@ -30,41 +31,100 @@ __device__ __forceinline__ double ipow4(double x) { double x2 = x * x; return x2
 __device__ __forceinline__ double ipow3(double x) { double x2 = x * x; return x2 * x; }
 
 // ============================================================ SoilWater (ZD09)
-// src/biogeophys/SoilWaterMovementMod.F90:414-972 for one column.
+// src/biogeophys/SoilWaterMovementMod.F90:414-972 for one column, as one
+// downward sweep.  Level j+1's water content, ice fraction, equilibrium
+// matric potential and node potential are formed one level ahead, so row j
+// of the tridiagonal system (:775-894) is complete as soon as the sweep
+// reaches it and is eliminated at once (the forward pass of
+// TridiagonalMod.F90:67-80); only the elimination's gam and r vectors are
+// kept for the back substitution (:82-89).  Every value is the reference's
+// expression on the reference's operands; quotients that share a divisor
+// (the porosity, the suction, the node spacing, dtime, the pivot bet) are
+// formed from one correctly rounded reciprocal (cr_div.cuh), which gives the
+// same bits as the division.
+struct ZdLevel {
+    double zmm, dzmm, zimm, ws, bb, vwc, icef, zq, smp, dsmpdw, hks;
+};
+
+__device__ __forceinline__ ZdLevel zd09_level(const ctsmg_soilwater_io& io, int c, int j, double zimm_prev,
+                                              double zwtmm, double smpmin) {
+    const int ld = io.ldc;
+    const size_t ss_ix = c + (size_t)(j - LS) * ld, g_ix = c + (size_t)(j - 1) * ld;
+    ZdLevel L;
+    const double dzj = io.dz[ss_ix], ws = io.watsat[g_ix], ss = io.sucsat[g_ix], bb = io.bsw[g_ix];
+    L.ws = ws;
+    L.bb = bb;
+    L.hks = io.hksat[g_ix];
+    L.zmm = io.z[ss_ix] * 1.e3;
+    L.dzmm = dzj * 1.e3;
+    L.zimm = io.zi[c + (size_t)(j + NLEVSNO) * ld] * 1.e3;
+    const Recip rws = recip(ws);
+    // :649-665 ice fraction and liquid content
+    const double vol_ice = fmin(ws, io.h2osoi_ice[ss_ix] / (dzj * DENICE));
+    L.icef = fmin(1.0, divr(vol_ice, rws));
+    io.icefrac[g_ix] = L.icef;
+    L.vwc = fmax(io.h2osoi_liq[ss_ix], 1.0e-6) / (dzj * DENH2O);
+    // :670-712 equilibrium volumetric water and matric potential: water table
+    // above the layer, inside it, below it.  temp0 is the same expression in
+    // the last two cases and tempi is only needed in the last, so each power
+    // has one call site.
+    const bool above = zwtmm <= zimm_prev;
+    const bool inside = !above && (zwtmm < L.zimm) && (zwtmm > zimm_prev);
+    double temp0 = 0.0, tempi = 1.0, veq;
+    if (!above) {
+        const Recip rss = recip(ss);
+        const double e = 1.0 - 1.0 / bb;
+        temp0 = fm::pow(divr(ss + zwtmm - zimm_prev, rss), e);
+        if (!inside) tempi = fm::pow(divr(ss + zwtmm - L.zimm, rss), e);
+    }
+    if (above) {
+        veq = ws;
+    } else if (inside) {
+        double voleq1 = -ss * ws / (1.0 - 1.0 / bb) / (zwtmm - zimm_prev) * (tempi - temp0);
+        veq = (voleq1 * (zwtmm - zimm_prev) + ws * (L.zimm - zwtmm)) / (L.zimm - zimm_prev);
+        veq = fmin(ws, veq);
+        veq = fmax(veq, 0.0);
+    } else {
+        veq = -ss * ws / (1.0 - 1.0 / bb) / (L.zimm - zimm_prev) * (tempi - temp0);
+        veq = fmax(veq, 0.0);
+        veq = fmin(ws, veq);
+    }
+    L.zq = fmax(smpmin, -ss * fm::pow(fmax(divr(veq, rws), 0.01), -bb));
+    // :740-760 node matric potential and its derivative
+    double s_node = fmax(divr(L.vwc, rws), 0.01);
+    s_node = fmin(1.0, s_node);
+    const double sm = fmax(smpmin, -ss * fm::pow(s_node, -bb));
+    L.smp = sm;
+    L.dsmpdw = -bb * sm / L.vwc;
+    io.smp_l[g_ix] = sm;
+    return L;
+}
+
 __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, double dtime) {
     const int ld = io.ldc;
     auto SS = [&](const double* p, int j) { return p[c + (size_t)(j - LS) * ld]; };
     auto G = [&](const double* p, int j) { return p[c + (size_t)(j - 1) * ld]; };
     auto ZI = [&](int j) { return io.zi[c + (size_t)(j + NLEVSNO) * ld]; };
-
-    constexpr int N1 = NLEVSOI + 2;
-    double zmm[N1], dzmm[N1], zimm[N1], vwc_liq[N1], zq[N1];
-    double hk[N1], dhkdw[N1], smp[N1], dsmpdw[N1], imped[N1], icef[N1];
-    double amx[N1], bmx[N1], cmx[N1], rmx[N1];
+    auto ROOT = [&](int j) { return io.qflx_rootsoi[c + (size_t)(j - 1) * ld]; };
+    auto setq = [&](int j, double qi, double qo) {
+        io.qin[c + (size_t)(j - 1) * ld] = qi;
+        io.qout[c + (size_t)(j - 1) * ld] = qo;
+    };
 
     const double zwt = io.zwt[c], smpmin = io.smpmin[c];
-#pragma unroll 1
-    for (int j = 1; j <= NLEVSOI; ++j) {
-        const double dzj = SS(io.dz, j), ws = G(io.watsat, j);
-        zmm[j] = SS(io.z, j) * 1.e3;
-        dzmm[j] = dzj * 1.e3;
-        zimm[j] = ZI(j) * 1.e3;
-        double vol_ice = fmin(ws, SS(io.h2osoi_ice, j) / (dzj * DENICE));
-        icef[j] = fmin(1.0, vol_ice / ws);
-        io.icefrac[c + (size_t)(j - 1) * ld] = icef[j];
-        vwc_liq[j] = fmax(SS(io.h2osoi_liq, j), 1.0e-6) / (dzj * DENH2O);
-    }
-    zimm[0] = 0.0;
     const double zwtmm = zwt * 1.e3;
+    const Recip rdt = recip(dtime);
 
+    // :638-647 index of the layer right above the water table
     int jwt = NLEVSOI;
 #pragma unroll 1
     for (int j = 1; j <= NLEVSOI; ++j) {
         if (zwt <= ZI(j)) { jwt = j - 1; break; }
     }
+    // :649-665 water content at the water table (frozen case)
     double vwc_zwt = G(io.watsat, NLEVSOI);
     if (SS(io.t_soisno, jwt + 1) < TFRZ) {
-        vwc_zwt = vwc_liq[NLEVSOI];
+        vwc_zwt = fmax(SS(io.h2osoi_liq, NLEVSOI), 1.0e-6) / (SS(io.dz, NLEVSOI) * DENH2O);
 #pragma unroll 1
         for (int j = NLEVSOI; j <= NLEVGRND; ++j) {
             if (zwt <= ZI(j)) {
@@ -77,195 +137,143 @@ __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, d
             }
         }
     }
-#pragma unroll 1
-    for (int j = 1; j <= NLEVSOI; ++j) {
-        const double ss = G(io.sucsat, j), ws = G(io.watsat, j), bb = G(io.bsw, j);
-        // three cases (:674-706): water table above the layer, inside it, below
-        // it.  temp0 is the same expression in the last two and tempi is only
-        // needed in the last, so each power has one call site and a warp whose
-        // lanes are in different cases evaluates it once.
-        const bool above = zwtmm <= zimm[j - 1];
-        const bool inside = !above && (zwtmm < zimm[j]) && (zwtmm > zimm[j - 1]);
-        double temp0 = 0.0, tempi = 1.0;
-        if (!above) temp0 = fm::pow(((ss + zwtmm - zimm[j - 1]) / ss), 1.0 - 1.0 / bb);
-        if (!above && !inside) tempi = fm::pow(((ss + zwtmm - zimm[j]) / ss), 1.0 - 1.0 / bb);
-        double veq;
-        if (above) {
-            veq = ws;
-        } else if (inside) {
-            double voleq1 = -ss * ws / (1.0 - 1.0 / bb) / (zwtmm - zimm[j - 1]) * (tempi - temp0);
-            veq = (voleq1 * (zwtmm - zimm[j - 1]) + ws * (zimm[j] - zwtmm)) / (zimm[j] - zimm[j - 1]);
-            veq = fmin(ws, veq);
-            veq = fmax(veq, 0.0);
-        } else {
-            veq = -ss * ws / (1.0 - 1.0 / bb) / (zimm[j] - zimm[j - 1]) * (tempi - temp0);
-            veq = fmax(veq, 0.0);
-            veq = fmin(ws, veq);
-        }
-        double q = -ss * fm::pow(fmax(veq / ws, 0.01), -bb);
-        zq[j] = fmax(smpmin, q);
-    }
-    if (jwt == NLEVSOI) {
-        const int j = NLEVSOI;
-        const double ss = G(io.sucsat, j), ws = G(io.watsat, j), bb = G(io.bsw, j);
-        double tempi = 1.0;
-        double temp0 = fm::pow(((ss + zwtmm - zimm[j]) / ss), 1.0 - 1.0 / bb);
-        double veq = -ss * ws / (1.0 - 1.0 / bb) / (zwtmm - zimm[j]) * (tempi - temp0);
-        veq = fmax(veq, 0.0);
-        veq = fmin(ws, veq);
-        double q = -ss * fm::pow(fmax(veq / ws, 0.01), -bb);
-        zq[j + 1] = fmax(smpmin, q);
-    }
-#pragma unroll 1
-    for (int j = 1; j <= NLEVSOI; ++j) {
-        const int jp = min(NLEVSOI, j + 1);
-        const double wsj = G(io.watsat, j), wsp = G(io.watsat, jp), bb = G(io.bsw, j);
-        double s1 = 0.5 * (vwc_liq[j] + vwc_liq[jp]) / (0.5 * (wsj + wsp));
-        s1 = fmin(1.0, s1);
-        double s2 = G(io.hksat, j) * fm::pow(s1, 2.0 * bb + 2.0);
-        imped[j] = pow10_dd(-e_ice * (0.5 * (icef[j] + icef[jp])));
-        hk[j] = imped[j] * s1 * s2;
-        dhkdw[j] = imped[j] * (2.0 * bb + 3.0) * s2 * (1.0 / (wsj + wsp));
-        double s_node = fmax(vwc_liq[j] / wsj, 0.01);
-        s_node = fmin(1.0, s_node);
-        double sm = -G(io.sucsat, j) * fm::pow(s_node, -bb);
-        sm = fmax(smpmin, sm);
-        smp[j] = sm;
-        dsmpdw[j] = -bb * sm / vwc_liq[j];
-        io.smp_l[c + (size_t)(j - 1) * ld] = sm;
-        io.hk_l[c + (size_t)(j - 1) * ld] = hk[j];
-    }
-    zmm[NLEVSOI + 1] = sp(0.5f) * (1.e3 * zwt + zmm[NLEVSOI]);
-    dzmm[NLEVSOI + 1] = (jwt < NLEVSOI) ? dzmm[NLEVSOI] : (1.e3 * zwt - zmm[NLEVSOI]);
 
-    auto ROOT = [&](int j) { return io.qflx_rootsoi[c + (size_t)(j - 1) * ld]; };
-    auto setq = [&](int j, double qi, double qo) {
-        io.qin[c + (size_t)(j - 1) * ld] = qi;
-        io.qout[c + (size_t)(j - 1) * ld] = qo;
-    };
-    // The inflow of level j and its derivatives (qin, dqidw0, dqidw1) are the
-    // outflow of level j-1 and its derivatives (qout, dqodw1, dqodw2): the
-    // reference evaluates the same expressions on the same operands twice;
-    // here each interface is evaluated once and carried down.
-    double q_up, dq_up0, dq_up1;
-    {   // top node
-        const int j = 1;
-        double qin = io.qflx_infl[c];
-        double den = (zmm[j + 1] - zmm[j]);
-        double dzq = (zq[j + 1] - zq[j]);
-        double num = (smp[j + 1] - smp[j]) - dzq;
-        double qout = -hk[j] * num / den;
-        double dqodw1 = -(-hk[j] * dsmpdw[j] + num * dhkdw[j]) / den;
-        double dqodw2 = -(hk[j] * dsmpdw[j + 1] + num * dhkdw[j]) / den;
-        rmx[j] = qin - qout - ROOT(j);
-        amx[j] = 0.0;
-        bmx[j] = dzmm[j] * (0.0 + 1.0 / dtime) + dqodw1;
-        cmx[j] = dqodw2;
-        setq(j, qin, qout);
-        q_up = qout; dq_up0 = dqodw1; dq_up1 = dqodw2;
-    }
-#pragma unroll 1
-    for (int j = 2; j <= NLEVSOI - 1; ++j) {
-        const double qin = q_up, dqidw0 = dq_up0, dqidw1 = dq_up1;
-        double den = (zmm[j + 1] - zmm[j]);
-        double dzq = (zq[j + 1] - zq[j]);
-        double num = (smp[j + 1] - smp[j]) - dzq;
-        double qout = -hk[j] * num / den;
-        double dqodw1 = -(-hk[j] * dsmpdw[j] + num * dhkdw[j]) / den;
-        double dqodw2 = -(hk[j] * dsmpdw[j + 1] + num * dhkdw[j]) / den;
-        rmx[j] = qin - qout - ROOT(j);
-        amx[j] = -dqidw0;
-        bmx[j] = dzmm[j] / dtime - dqidw1 + dqodw1;
-        cmx[j] = dqodw2;
-        setq(j, qin, qout);
-        q_up = qout; dq_up0 = dqodw1; dq_up1 = dqodw2;
-    }
-    {   // bottom node and aquifer layer
-        const int j = NLEVSOI;
-        const double qin = q_up, dqidw0 = dq_up0, dqidw1 = dq_up1;
-        if (j > jwt) {
-            rmx[j] = qin - 0.0 - ROOT(j);
-            amx[j] = -dqidw0;
-            bmx[j] = dzmm[j] / dtime - dqidw1 + 0.0;
-            cmx[j] = 0.0;
-            setq(j, qin, 0.0);
-            rmx[j + 1] = 0.0;
-            amx[j + 1] = 0.0;
-            bmx[j + 1] = dzmm[j + 1] / dtime;
-            cmx[j + 1] = 0.0;
+    // forward elimination state: gam(j) and the eliminated right-hand side
+    // r(j) per row, bet of the last row and its reciprocal, c of the last row
+    constexpr int N1 = NLEVSOI + 2;
+    double gam[N1], rr[N1];
+    Recip rbet{};
+    double c_prev = 0.0;
+    auto eliminate = [&](int j, double a, double b, double cc, double r) {
+        if (j == 1) {
+            rbet = recip(b);
+            rr[1] = divr(r, rbet);
         } else {
-            const double ws = G(io.watsat, j), bb = G(io.bsw, j);
-            double s_node = fmax(sp(0.5f) * ((vwc_zwt + vwc_liq[j]) / ws), 0.01);
-            s_node = fmin(1.0, s_node);
-            double smp1 = -G(io.sucsat, j) * fm::pow(s_node, -bb);
-            smp1 = fmax(smpmin, smp1);
-            double dsmpdw1 = -bb * smp1 / (s_node * ws);
-            const double den = (zmm[j + 1] - zmm[j]);
-            const double dzq = (zq[j + 1] - zq[j]);
-            const double num = (smp1 - smp[j]) - dzq;
-            double qout = -hk[j] * num / den;
-            double dqodw1 = -(-hk[j] * dsmpdw[j] + num * dhkdw[j]) / den;
-            double dqodw2 = -(hk[j] * dsmpdw1 + num * dhkdw[j]) / den;
-            rmx[j] = qin - qout - ROOT(j);
-            amx[j] = -dqidw0;
-            bmx[j] = dzmm[j] / dtime - dqidw1 + dqodw1;
-            cmx[j] = dqodw2;
-            // the aquifer layer's inflow derivatives: the same expressions as
-            // dqodw1 / dqodw2 (SoilWaterMovementMod.F90 evaluates them again)
-            const double dqidw0a = dqodw1;
-            const double dqidw1a = dqodw2;
-            rmx[j + 1] = qout - 0.0;
-            amx[j + 1] = -dqidw0a;
-            bmx[j + 1] = dzmm[j + 1] / dtime - dqidw1a + 0.0;
-            cmx[j + 1] = 0.0;
-            setq(j, qin, qout);
+            const double g = divr(c_prev, rbet);
+            const double bet = b - a * g;
+            rbet = recip(bet);
+            rr[j] = divr(r - a * rr[j - 1], rbet);
+            gam[j] = g;
         }
-    }
-    // Tridiagonal (TridiagonalMod.F90:60-89), jtop = 1, levels 1..nlevsoi+1;
-    // gam overwrites amx, the solution overwrites rmx
-    {
-        double bet = bmx[1];
-        rmx[1] = rmx[1] / bet;
+        c_prev = cc;
+    };
+
+    // values the recharge needs (:919-955): imped at jwt+1, smp and zq at max(1, jwt)
+    const int jq = jwt + 1, jm = max(1, jwt);
+    double imped_q = 0.0, smp_m = 0.0, zq_m = 0.0;
+
+    ZdLevel cur = zd09_level(io, c, 1, 0.0, zwtmm, smpmin);
+    double q_up = 0.0, dq_up0 = 0.0, dq_up1 = 0.0;
 #pragma unroll 1
-        for (int j = 2; j <= NLEVSOI + 1; ++j) {
-            double gam = cmx[j - 1] / bet;
-            bet = bmx[j] - amx[j] * gam;
-            rmx[j] = (rmx[j] - amx[j] * rmx[j - 1]) / bet;
-            amx[j] = gam;
+    for (int j = 1; j <= NLEVSOI; ++j) {
+        const bool bottom = j == NLEVSOI;
+        ZdLevel nx = bottom ? cur : zd09_level(io, c, j + 1, cur.zimm, zwtmm, smpmin);
+        // :716-737 interface conductivity and its derivative (jp = min(nlevsoi, j+1))
+        const Recip rB = recip(cur.ws + nx.ws);
+        const double s1 = fmin(1.0, divr(cur.vwc + nx.vwc, rB));
+        const double s2 = cur.hks * fm::pow(s1, 2.0 * cur.bb + 2.0);
+        const double imped = pow10_dd(-e_ice * (0.5 * (cur.icef + nx.icef)));
+        const double hk = imped * s1 * s2;
+        const double dhkdw = imped * (2.0 * cur.bb + 3.0) * s2 * rB.y;
+        io.hk_l[c + (size_t)(j - 1) * ld] = hk;
+        if (j == jq) imped_q = imped;
+        if (j == jm) { smp_m = cur.smp; zq_m = cur.zq; }
+        if (!bottom) {
+            // :775-846 top and interior rows; the inflow of level j and its
+            // derivatives are the outflow of level j-1 and its derivatives
+            const Recip rden = recip(nx.zmm - cur.zmm);
+            const double num = (nx.smp - cur.smp) - (nx.zq - cur.zq);
+            const double qout = divr(-hk * num, rden);
+            const double dqodw1 = divr(-(-hk * cur.dsmpdw + num * dhkdw), rden);
+            const double dqodw2 = divr(-(hk * nx.dsmpdw + num * dhkdw), rden);
+            if (j == 1) {
+                const double qin = io.qflx_infl[c];
+                eliminate(1, 0.0, cur.dzmm * (0.0 + rdt.y) + dqodw1, dqodw2, qin - qout - ROOT(1));
+                setq(1, qin, qout);
+            } else {
+                eliminate(j, -dq_up0, divr(cur.dzmm, rdt) - dq_up1 + dqodw1, dqodw2, q_up - qout - ROOT(j));
+                setq(j, q_up, qout);
+            }
+            q_up = qout; dq_up0 = dqodw1; dq_up1 = dqodw2;
+        } else {
+            // :847-894 bottom node and the aquifer layer below it
+            const double zmm_a = sp(0.5f) * (1.e3 * zwt + cur.zmm);
+            const double dzmm_a = (jwt < NLEVSOI) ? cur.dzmm : (1.e3 * zwt - cur.zmm);
+            if (j > jwt) {
+                eliminate(j, -dq_up0, divr(cur.dzmm, rdt) - dq_up1 + 0.0, 0.0, q_up - 0.0 - ROOT(j));
+                setq(j, q_up, 0.0);
+                eliminate(j + 1, 0.0, divr(dzmm_a, rdt), 0.0, 0.0);
+            } else {
+                // zq of the aquifer node (:701-712)
+                const double ss = G(io.sucsat, j), ws = cur.ws, bb = cur.bb;
+                const double tempi = 1.0;
+                const double temp0 = fm::pow(((ss + zwtmm - cur.zimm) / ss), 1.0 - 1.0 / bb);
+                double veq = -ss * ws / (1.0 - 1.0 / bb) / (zwtmm - cur.zimm) * (tempi - temp0);
+                veq = fmax(veq, 0.0);
+                veq = fmin(ws, veq);
+                const double zq_a = fmax(smpmin, -ss * fm::pow(fmax(veq / ws, 0.01), -bb));
+                double s_node = fmax(sp(0.5f) * ((vwc_zwt + cur.vwc) / ws), 0.01);
+                s_node = fmin(1.0, s_node);
+                double smp1 = -ss * fm::pow(s_node, -bb);
+                smp1 = fmax(smpmin, smp1);
+                const double dsmpdw1 = -bb * smp1 / (s_node * ws);
+                const Recip rden = recip(zmm_a - cur.zmm);
+                const double num = (smp1 - cur.smp) - (zq_a - cur.zq);
+                const double qout = divr(-hk * num, rden);
+                const double dqodw1 = divr(-(-hk * cur.dsmpdw + num * dhkdw), rden);
+                const double dqodw2 = divr(-(hk * dsmpdw1 + num * dhkdw), rden);
+                eliminate(j, -dq_up0, divr(cur.dzmm, rdt) - dq_up1 + dqodw1, dqodw2, q_up - qout - ROOT(j));
+                // the aquifer layer's inflow derivatives are dqodw1 / dqodw2
+                eliminate(j + 1, -dqodw1, divr(dzmm_a, rdt) - dqodw2 + 0.0, 0.0, qout - 0.0);
+                setq(j, q_up, qout);
+            }
+            rr[0] = dzmm_a;   // the aquifer layer's thickness, kept for the recharge
         }
-#pragma unroll 1
-        for (int j = NLEVSOI; j >= 1; --j) rmx[j] = rmx[j] - amx[j + 1] * rmx[j + 1];
+        cur = nx;
     }
-    const double* dwat2 = rmx;
+    // :82-89 back substitution; the solution (dwat2) overwrites r
+    const double dzmm_a = rr[0];
+#pragma unroll 1
+    for (int j = NLEVSOI; j >= 1; --j) rr[j] = rr[j] - gam[j + 1] * rr[j + 1];
+    // :912-917 update and deficit
     double deficit = 0.0;
 #pragma unroll 1
     for (int j = 1; j <= NLEVSOI; ++j) {
         double& liq = io.h2osoi_liq[c + (size_t)(j - LS) * ld];
-        double v = liq + dwat2[j] * dzmm[j];
+        double v = liq + rr[j] * (SS(io.dz, j) * 1.e3);
         liq = v;
         if (v < 0.0) deficit = deficit - v;
     }
     double qcharge;
     if (jwt < NLEVSOI) {
-        const int jq = jwt + 1;
         double s_node = fmax(G(io.h2osoi_vol, jq) / G(io.watsat, jq), 0.01);
         double s1 = fmin(1.0, s_node);
-        double ka = imped[jq] * G(io.hksat, jq) * fm::pow(s1, 2.0 * G(io.bsw, jq) + 3.0);
-        const int jm = max(1, jwt);
-        double smp1 = fmax(smpmin, smp[jm]);
-        double wh = smp1 - zq[jm];
+        double ka = imped_q * G(io.hksat, jq) * fm::pow(s1, 2.0 * G(io.bsw, jq) + 3.0);
+        double smp1 = fmax(smpmin, smp_m);
+        double wh = smp1 - zq_m;
         if (jwt == 0) qcharge = -ka * (0.0 - wh) / ((zwt + sp(1.e-3f)) * 1000.0);
         else qcharge = -ka * (0.0 - wh) / ((zwt - SS(io.z, jwt)) * 1000.0 * sp(2.0f));
-        qcharge = fmax(-10.0 / dtime, qcharge);
-        qcharge = fmin(10.0 / dtime, qcharge);
+        qcharge = fmax(-divr(10.0, rdt), qcharge);
+        qcharge = fmin(divr(10.0, rdt), qcharge);
     } else {
-        qcharge = dwat2[NLEVSOI + 1] * dzmm[NLEVSOI + 1] / dtime;
+        qcharge = divr(rr[NLEVSOI + 1] * dzmm_a, rdt);
     }
     io.qcharge[c] = qcharge;
     io.qflx_deficit[c] = deficit;
 }
 
 // ============================================================ SoilTemperature
+// The band LU's tests on the integer pipe (FP64 instructions are the step's
+// limit on GB300): x != 0.0 (NaN counts as nonzero, as in IEEE), and |a| > |b|
+// with a NaN a or b false, as the IEEE comparison of fabs values.
+__device__ __forceinline__ bool nonzero(double x) { return (__double_as_longlong(x) << 1) != 0; }
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+    return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+__device__ __forceinline__ bool abs_gt(unsigned long long ua, unsigned long long ub) {
+    return ua <= 0x7ff0000000000000ull && ub <= 0x7ff0000000000000ull && ua > ub;
+}
+
 // Scratch slot of one column: row i (1-based, i = 1..n) occupies 6 doubles
 // U(i,i..i+4), y(i) at ws[((i-1)*6 + k) * ws_ld + slot].
 struct Scratch {
@@ -297,14 +305,24 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
 
     constexpr int NL = NLEVSNO + NLEVGRND + 2;
     auto L = [](int j) { return j + NLEVSNO; };
-    double tk[NL], fact[NL], fn[NL];
+    // per level: interface conductivity tk(j), diffusion factor fact(j),
+    // heat flux fn(j) and the reciprocal of the node spacing z(j+1) - z(j)
+    // (shared by fn, the matrix rows of levels j and j+1 and the flux from
+    // the new temperatures)
+    double tk[NL], fact[NL], fn[NL], rdz[NL];
+    const Recip R_DENH2O = CTSMG_CONST_RECIP(DENH2O), R_DENICE = CTSMG_CONST_RECIP(DENICE);
+    const Recip R_HFUS = CTSMG_CONST_RECIP(HFUS);
+    const Recip rdt = recip(dtime);
+    const Recip rfsno = recip(frac_sno);
+    auto RDZ = [&](int j) { return Recip{Z(j + 1) - Z(j), rdz[L(j)], crdiv_in_range(Z(j + 1) - Z(j))}; };
 
-    // ---------------- SoilThermProp (:664-896): thk, tk, cv -> fact
+    // ---------------- SoilThermProp (:664-896) -> thk, tk, cv, and
+    // ComputeHeatDiffFluxAndFactor (:1876-1906) -> fact, fn, one level behind
+    // the conductivity (fn(j) needs tk(j), which needs thk(j+1))
     double thk_prev = 0.0;
-    double cvv[NL];
 #pragma unroll 1
     for (int j = snl + 1; j <= NLEVGRND; ++j) {
-        double t;
+        double t, cv;
         if (j >= 1) {
             const double liq = LIQ[ssi(j)], ice = ICE[ssi(j)], dzj = DZ(j), ws = io.watsat[gi(j)];
             if (j > nbedrock) {
@@ -312,21 +330,21 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
                 // overwrites it with thk_bedrock (:710-725); the value is unused
                 t = THK_BEDROCK;
             } else {
-                double satw = (liq / DENH2O + ice / DENICE + 0.0 / DENICE) / (dzj * ws);
+                double satw = (divr(liq, R_DENH2O) + divr(ice, R_DENICE) + 0.0 / DENICE) / (dzj * ws);
                 satw = fmin(1.0, satw);
                 if (satw > .1e-6) {
                     double dke = (T[ssi(j)] >= TFRZ) ? fmax(0.0, fm::log10(satw) + 1.0) : satw;
-                    double fl = (liq / (DENH2O * dzj)) / (liq / (DENH2O * dzj) + ice / (DENICE * dzj) + 0.0 / (DENICE * dzj));
+                    const double xl = liq / (DENH2O * dzj);
+                    double fl = xl / (xl + ice / (DENICE * dzj) + zero_over(DENICE * dzj));
                     double dksat = io.tkmg[gi(j)] * tkwat_tkice_pow(fl * ws, (1.0 - fl) * ws);
                     t = dke * dksat + (1.0 - dke) * io.tkdry[gi(j)];
                 } else {
                     t = io.tkdry[gi(j)];
                 }
             }
-            double cv = io.csol[gi(j)] * (1.0 - ws) * dzj + (ice * CPICE + liq * CPLIQ) + 0.0 * CPICE;
+            cv = io.csol[gi(j)] * (1.0 - ws) * dzj + (ice * CPICE + liq * CPLIQ) + 0.0 * CPICE;
             if (j > nbedrock) cv = CSOL_BEDROCK * dzj;
             if (j == 1 && io.h2osno_no_layers[c] > 0.0) cv = cv + CPICE * io.h2osno_no_layers[c];
-            cvv[L(j)] = cv;
         } else {
             const double liq = LIQ[ssi(j)], ice = ICE[ssi(j)];
             double b = (ice + liq) / (frac_sno * DZ(j));
@@ -337,16 +355,26 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
                 if (b <= 156) t = sp(0.023f) + sp(0.234f) * (b / 1000);
                 else t = sp(0.138f) - sp(1.01f) * (b / 1000) + (sp(3.233f) * ((b / 1000) * (b / 1000)));
             }
-            cvv[L(j)] = (frac_sno > 0.0) ? fmax(THIN_SFCLAYER, (CPLIQ * liq + CPICE * ice) / frac_sno) : THIN_SFCLAYER;
+            cv = (frac_sno > 0.0) ? fmax(THIN_SFCLAYER, divr(CPLIQ * liq + CPICE * ice, rfsno)) : THIN_SFCLAYER;
         }
         io.thk[ssi(j)] = t;
+        double f;
+        if (j == snl + 1) f = dtime / cv * DZ(j) / (0.5 * (Z(j) - ZI(j - 1) + CAPR * (Z(j + 1) - ZI(j - 1))));
+        else f = dtime / cv;
+        fact[L(j)] = f;
+        io.fact[ssi(j)] = f;
         if (j > snl + 1) {
             const int jm = j - 1;
-            tk[L(jm)] = thk_prev * t * (Z(j) - Z(jm)) / (thk_prev * (Z(j) - ZI(jm)) + t * (ZI(jm) - Z(jm)));
+            const double tkm = thk_prev * t * (Z(j) - Z(jm)) / (thk_prev * (Z(j) - ZI(jm)) + t * (ZI(jm) - Z(jm)));
+            tk[L(jm)] = tkm;
+            const Recip r = recip(Z(j) - Z(jm));
+            rdz[L(jm)] = r.y;
+            fn[L(jm)] = divr(tkm * (T[ssi(j)] - T[ssi(jm)]), r);
         }
         thk_prev = t;
     }
     tk[L(NLEVGRND)] = 0.0;
+    fn[L(NLEVGRND)] = io.eflx_bot[c];
     const double thk1 = io.thk[ssi(1)];
     const double z1 = Z(1);
     double tk_h2osfc;
@@ -403,24 +431,6 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
         return s;
     };
 
-    // ---------------- ComputeHeatDiffFluxAndFactor (:1876-1906)
-#pragma unroll 1
-    for (int j = snl + 1; j <= NLEVGRND; ++j) {
-        double f, flux;
-        if (j == snl + 1) {
-            f = dtime / cvv[L(j)] * DZ(j) / (0.5 * (Z(j) - ZI(j - 1) + CAPR * (Z(j + 1) - ZI(j - 1))));
-            flux = tk[L(j)] * (T[ssi(j + 1)] - T[ssi(j)]) / (Z(j + 1) - Z(j));
-        } else if (j <= NLEVGRND - 1) {
-            f = dtime / cvv[L(j)];
-            flux = tk[L(j)] * (T[ssi(j + 1)] - T[ssi(j)]) / (Z(j + 1) - Z(j));
-        } else {
-            f = dtime / cvv[L(j)];
-            flux = io.eflx_bot[c];
-        }
-        fact[L(j)] = f;
-        fn[L(j)] = flux;
-        io.fact[ssi(j)] = f;
-    }
     double c_h2osfc, dz_h2osfc;
     if ((io.h2osfc[c] > THIN_SFCLAYER) && (frac_h2osfc > THIN_SFCLAYER)) {
         c_h2osfc = fmax(THIN_SFCLAYER, CPLIQ * io.h2osfc[c] / frac_h2osfc);
@@ -440,33 +450,32 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
     // tk(j)/dzp is the next row's tk(j-1)/dzm (the same operands: dzm of row
     // j+1 is Z(j+1)-Z(j)), so it is carried from one row to the next (q_dn of
     // row q_row); and -(1-cnfac) fj tk / dz is the exact negation of
-    // (1-cnfac) fj tk / dz.  Both leave every value as the reference computes it.
+    // (1-cnfac) fj tk / dz.  The quotients by the node spacings use the
+    // reciprocals formed with the fluxes (rdz).
     double q_dn = 0.0;
     int q_row = -1000;
     auto make_row = [&](int r, double* bnd, double& rhs) {
         bnd[0] = bnd[1] = bnd[2] = bnd[3] = bnd[4] = 0.0;
         if (r < 0) {                                   // snow layer j = r + 1
             const int j = r + 1;
-            const double dzp = Z(j + 1) - Z(j);
             const double fj = fact[L(j)], tj = T[ssi(j)];
             if (j == snl + 1) {
-                const double x = (1.0 - CNFAC) * fj * tk[L(j)] / dzp;
+                const double x = divr((1.0 - CNFAC) * fj * tk[L(j)], RDZ(j));
                 bnd[2] = 1.0 + x - fj * dhsdT;
                 rhs = tj + fj * (hs_top_snow - dhsdT * tj + CNFAC * fn[L(j)]);
                 if (j != 0) bnd[1] = -x;
                 else bnd[0] = -x;
             } else {
-                const double dzm = (Z(j) - Z(j - 1));
-                bnd[3] = -(1.0 - CNFAC) * fj * tk[L(j - 1)] / dzm;
-                const double qp = tk[L(j)] / dzp;
-                const double qm = (q_row == j - 1) ? q_dn : tk[L(j - 1)] / dzm;
+                bnd[3] = divr(-(1.0 - CNFAC) * fj * tk[L(j - 1)], RDZ(j - 1));
+                const double qp = divr(tk[L(j)], RDZ(j));
+                const double qm = (q_row == j - 1) ? q_dn : divr(tk[L(j - 1)], RDZ(j - 1));
                 bnd[2] = 1.0 + (1.0 - CNFAC) * fj * (qp + qm);
                 q_dn = qp;
                 q_row = j;
                 double rr = tj + CNFAC * fj * (fn[L(j)] - fn[L(j - 1)]);
                 rhs = rr + fj * sabg_lyr_col(j);
-                if (j != 0) bnd[1] = -(1.0 - CNFAC) * fj * tk[L(j)] / dzp;
-                else bnd[0] = -(1.0 - CNFAC) * fj * tk[L(j)] / dzp;
+                if (j != 0) bnd[1] = divr(-(1.0 - CNFAC) * fj * tk[L(j)], RDZ(j));
+                else bnd[0] = divr(-(1.0 - CNFAC) * fj * tk[L(j)], RDZ(j));
             }
         } else if (r == 0) {                           // standing surface water
             bnd[2] = 1.0 + (1.0 - CNFAC) * (dtime / c_h2osfc) * tk_h2osfc / dzm_ssw - (dtime / c_h2osfc) * dhsdT;
@@ -476,37 +485,31 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
             const int j = r;
             const double fj = fact[L(j)], tj = T[ssi(j)];
             if (j == snl + 1) {
-                const double dzp = Z(j + 1) - Z(j);
-                const double x = (1.0 - CNFAC) * fj * tk[L(j)] / dzp;
+                const double x = divr((1.0 - CNFAC) * fj * tk[L(j)], RDZ(j));
                 bnd[2] = 1.0 + x - fj * dhsdT;
                 bnd[1] = -x;
                 rhs = tj + fj * (hs_top_snow - dhsdT * tj + CNFAC * fn[L(j)]);
             } else if (j == 1) {
-                const double dzm = (Z(j) - Z(j - 1));
-                const double dzp = (Z(j + 1) - Z(j));
-                bnd[1] = -(1.0 - CNFAC) * fj * tk[L(j)] / dzp;
-                const double qp = tk[L(j)] / dzp;
-                bnd[2] = 1.0 + (1.0 - CNFAC) * fj * (qp + frac_sno * tk[L(j - 1)] / dzm) -
+                bnd[1] = divr(-(1.0 - CNFAC) * fj * tk[L(j)], RDZ(j));
+                const double qp = divr(tk[L(j)], RDZ(j));
+                bnd[2] = 1.0 + (1.0 - CNFAC) * fj * (qp + divr(frac_sno * tk[L(j - 1)], RDZ(j - 1))) -
                          (1.0 - frac_sno) * fj * dhsdT;
                 q_dn = qp;
                 q_row = j;
-                bnd[4] = -frac_sno * (1.0 - CNFAC) * fj * tk[L(j - 1)] / dzm;
+                bnd[4] = divr(-frac_sno * (1.0 - CNFAC) * fj * tk[L(j - 1)], RDZ(j - 1));
                 double rr = tj + fj * ((1.0 - frac_sno) * (hs_soil - dhsdT * tj) + CNFAC * (fn[L(j)] - frac_sno * fn[L(j - 1)]));
                 rhs = rr + frac_sno * fj * sabg_lyr_col(j);
             } else if (j <= NLEVGRND - 1) {
-                const double dzm = (Z(j) - Z(j - 1));
-                const double dzp = (Z(j + 1) - Z(j));
-                bnd[1] = -(1.0 - CNFAC) * fj * tk[L(j)] / dzp;
-                const double qp = tk[L(j)] / dzp;
-                const double qm = (q_row == j - 1) ? q_dn : tk[L(j - 1)] / dzm;
+                bnd[1] = divr(-(1.0 - CNFAC) * fj * tk[L(j)], RDZ(j));
+                const double qp = divr(tk[L(j)], RDZ(j));
+                const double qm = (q_row == j - 1) ? q_dn : divr(tk[L(j - 1)], RDZ(j - 1));
                 bnd[2] = 1.0 + (1.0 - CNFAC) * fj * (qp + qm);
                 q_dn = qp;
                 q_row = j;
-                bnd[3] = -(1.0 - CNFAC) * fj * tk[L(j - 1)] / dzm;
+                bnd[3] = divr(-(1.0 - CNFAC) * fj * tk[L(j - 1)], RDZ(j - 1));
                 rhs = tj + CNFAC * fj * (fn[L(j)] - fn[L(j - 1)]);
             } else {
-                const double dzm = (Z(j) - Z(j - 1));
-                const double x = (1.0 - CNFAC) * fj * tk[L(j - 1)] / dzm;
+                const double x = divr((1.0 - CNFAC) * fj * tk[L(j - 1)], RDZ(j - 1));
                 bnd[2] = 1.0 + x;
                 bnd[3] = -x;
                 rhs = tj - CNFAC * fj * fn[L(j - 1)] + fj * fn[L(j)];
@@ -542,9 +545,9 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
     for (int j = 1; j <= n; ++j) {
         const int km = min(2, n - j);
         int jp = 0;
-        double dmax = fabs(W[0][0]);
-        if (km >= 1 && fabs(W[1][0]) > dmax) { jp = 1; dmax = fabs(W[1][0]); }
-        if (km >= 2 && fabs(W[2][0]) > dmax) { jp = 2; }
+        unsigned long long dmax = abs_bits(W[0][0]);
+        if (km >= 1 && abs_gt(abs_bits(W[1][0]), dmax)) { jp = 1; dmax = abs_bits(W[1][0]); }
+        if (km >= 2 && abs_gt(abs_bits(W[2][0]), dmax)) { jp = 2; }
         if (jp == 1) {
 #pragma unroll
             for (int b = 0; b < 5; ++b) { double t = W[0][b]; W[0][b] = W[1][b]; W[1][b] = t; }
@@ -554,7 +557,7 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
             for (int b = 0; b < 5; ++b) { double t = W[0][b]; W[0][b] = W[2][b]; W[2][b] = t; }
             double t = y[0]; y[0] = y[2]; y[2] = t;
         }
-        if (W[0][0] != 0.0) {
+        if (nonzero(W[0][0])) {
             if (km > 0) {
                 const double rp = 1.0 / W[0][0];
                 W[1][0] = W[1][0] * rp;
@@ -562,7 +565,7 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
 #pragma unroll
                 for (int b = 1; b < 5; ++b) {
                     const double yk = W[0][b];
-                    if (yk != 0.0) {
+                    if (nonzero(yk)) {
                         const double temp = -1.0 * yk;
                         W[1][b] = W[1][b] + W[1][0] * temp;
                         if (km > 1) W[2][b] = W[2][b] + W[2][0] * temp;
@@ -573,7 +576,7 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
             info = j;
         }
         // dgbtrs forward step j (no-op for j = n)
-        if (j < n && y[0] != 0.0) {
+        if (j < n && nonzero(y[0])) {
             const double temp = -1.0 * y[0];
             y[1] = y[1] + W[1][0] * temp;
             if (km > 1) y[2] = y[2] + W[2][0] * temp;
@@ -610,7 +613,7 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
     for (int k = 0; k < 5; ++k) x[k] = (n - k >= 1) ? S.at(n - k, 5) : 0.0;
 #pragma unroll 1
     for (int j = n; j >= 1; --j) {
-        if (x[0] != 0.0) {
+        if (nonzero(x[0])) {
             x[0] = x[0] / S.at(j, 0);
             const double temp = x[0];
 #pragma unroll
@@ -629,13 +632,13 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
     for (int j = snl + 1; j <= NLEVGRND; ++j) T[ssi(j)] = TV(j <= 0 ? j - 1 : j);
     double t_h2osfc = (frac_h2osfc == 0.0) ? T[ssi(1)] : TV(0);
     io.t_h2osfc[c] = t_h2osfc;
-    const double fn1_1 = tk[L(1)] * (T[ssi(2)] - T[ssi(1)]) / (Z(2) - Z(1));
+    const double fn1_1 = divr(tk[L(1)] * (T[ssi(2)] - T[ssi(1)]), RDZ(1));
     io.eflx_fgr12[c] = -CNFAC * fn[L(1)] - (1.0 - CNFAC) * fn1_1;
 #pragma unroll 1
     for (int j = 1; j <= NLEVGRND; ++j) {
         double v;
         if (j < NLEVGRND) {
-            double fn1 = tk[L(j)] * (T[ssi(j + 1)] - T[ssi(j)]) / (Z(j + 1) - Z(j));
+            double fn1 = divr(tk[L(j)] * (T[ssi(j + 1)] - T[ssi(j)]), RDZ(j));
             v = -CNFAC * fn[L(j)] - (1.0 - CNFAC) * fn1;
         } else {
             v = 0.0;
@@ -653,8 +656,8 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
         double h2osfc = io.h2osfc[c];
         double tinc = TFRZ - t_h2osfc;
         t_h2osfc = TFRZ;
-        double hm = frac_h2osfc * (dhsdT * tinc - tinc * c_h2osfc / dtime);
-        double xm = hm * dtime / HFUS;
+        double hm = frac_h2osfc * (dhsdT * tinc - divr(tinc * c_h2osfc, rdt));
+        double xm = divr(hm * dtime, R_HFUS);
         double temp1 = h2osfc + xm;
         double z_avg = frac_sno * io.snow_depth[c];
         double rho_avg = (z_avg > 0.0) ? fmin(800.0, h2osno_total / z_avg) : 200.0;
@@ -666,7 +669,7 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
             h2osno_total = h2osno_total - xm;
             io.h2osfc[c] = h2osfc + xm;
             io.xmf_h2osfc[c] = hm;
-            io.qflx_h2osfc_to_ice[c] = -xm / dtime;
+            io.qflx_h2osfc_to_ice[c] = divr(-xm, rdt);
             if (frac_sno > 0 && snl < 0) io.snow_depth[c] = h2osno_total / (rho_avg * frac_sno);
             else io.snow_depth[c] = h2osno_total / DENICE;
             if (snl == 0) {
@@ -677,7 +680,7 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
                 double c2 = (frac_h2osfc != 0.0) ? (-CPLIQ * xm - frac_h2osfc * dhsdT * dtime) : 0.0;
                 double t0 = (c1 * T[ssi(0)] + c2 * t_h2osfc) / (c1 + c2);
                 T[ssi(0)] = t0;
-                io.eflx_h2osfc_to_snow[c] = (t_h2osfc - t0) * c2 / dtime;
+                io.eflx_h2osfc_to_snow[c] = divr((t_h2osfc - t0) * c2, rdt);
             }
         } else {
             rho_avg = (h2osno_total * rho_avg + h2osfc * DENICE) / (h2osno_total + h2osfc);
@@ -685,9 +688,9 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
             if (snl == 0) io.h2osno_no_layers[c] = io.h2osno_no_layers[c] + h2osfc;
             else ICE[ssi(0)] = ICE[ssi(0)] + h2osfc;
             h2osno_total = h2osno_total + h2osfc;
-            io.qflx_h2osfc_to_ice[c] = h2osfc / dtime;
+            io.qflx_h2osfc_to_ice[c] = divr(h2osfc, rdt);
             t_h2osfc = t_h2osfc - temp1 * HFUS / (dtime * dhsdT - c_h2osfc);
-            io.xmf_h2osfc[c] = (hm - frac_h2osfc * temp1 * HFUS / dtime);
+            io.xmf_h2osfc[c] = (hm - divr(frac_h2osfc * temp1 * HFUS, rdt));
             if (snl == 0) {
                 T[ssi(0)] = t_h2osfc;
             } else {
@@ -753,7 +756,7 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
         if (imelt == 2 && hm > 0.0) { hm = 0.0; imelt = 0; }
         double ice = wice0, liq = wliq0;
         if (imelt > 0 && fabs(hm) > 0.0) {
-            double xm = hm * dtime / HFUS;
+            double xm = divr(hm * dtime, R_HFUS);
             if (j == 1) {
                 if (io.h2osno_no_layers[c] > 0.0 && xm > 0.0) {
                     double temp1 = io.h2osno_no_layers[c];
@@ -761,10 +764,10 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
                     io.h2osno_no_layers[c] = nl;
                     double propor = nl / temp1;
                     io.snow_depth[c] = propor * io.snow_depth[c];
-                    double heatr = hm - HFUS * (temp1 - nl) / dtime;
-                    if (heatr > 0.0) { xm = heatr * dtime / HFUS; hm = heatr; }
+                    double heatr = hm - divr(HFUS * (temp1 - nl), rdt);
+                    if (heatr > 0.0) { xm = divr(heatr * dtime, R_HFUS); hm = heatr; }
                     else { xm = 0.0; hm = 0.0; }
-                    qflx_snomelt = fmax(0.0, (temp1 - nl)) / dtime;
+                    qflx_snomelt = divr(fmax(0.0, (temp1 - nl)), rdt);
                     xmf = HFUS * qflx_snomelt;
                     qflx_snow_drain = qflx_snomelt;
                 }
@@ -772,38 +775,38 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
             double heatr = 0.0;
             if (xm > 0.0) {
                 ice = fmax(0.0, wice0 - xm);
-                if (j >= 1) heatr = hm - HFUS * (0.0 - 0.0 + wice0 - ice) / dtime;
-                else heatr = hm - HFUS * (wice0 - ice) / dtime;
+                if (j >= 1) heatr = hm - divr(HFUS * (0.0 - 0.0 + wice0 - ice), rdt);
+                else heatr = hm - divr(HFUS * (wice0 - ice), rdt);
             } else if (xm < 0.0) {
                 if (j <= 0) ice = fmin(wmass0, wice0 - xm);
                 else ice = (wmass0 - 0.0 < supercool) ? 0.0 : fmin(wmass0 - 0.0 - supercool, wice0 - xm);
-                heatr = hm - HFUS * (wice0 - ice) / dtime;
+                heatr = hm - divr(HFUS * (wice0 - ice), rdt);
             }
             liq = fmax(0.0, wmass0 - ice - 0.0);
             if (fabs(heatr) > 0.0) {
                 if (j == snl + 1) {
                     if (j == 1) tj = tj + fj * heatr / (1.0 - (1.0 - frac_h2osfc) * fj * dhsdT);
-                    else tj = tj + (fj / frac_sno) * heatr / (1.0 - fj * dhsdT);
+                    else tj = tj + divr(fj, rfsno) * heatr / (1.0 - fj * dhsdT);
                 } else if (j == 1) {
                     tj = tj + fj * heatr / (1.0 - (1.0 - frac_sno - frac_h2osfc) * fj * dhsdT);
                 } else {
                     if (j > 0) tj = tj + fj * heatr;
-                    else if (frac_sno > 0.0) tj = tj + (fj / frac_sno) * heatr;
+                    else if (frac_sno > 0.0) tj = tj + divr(fj, rfsno) * heatr;
                 }
                 if (j <= 0) {
                     if (liq * ice > 0.0) tj = TFRZ;
                 }
             }
-            if (j >= 1) xmf = xmf + HFUS * (wice0 - ice) / dtime + HFUS * (0.0 - 0.0) / dtime;
-            else xmf = xmf + HFUS * (wice0 - ice) / dtime;
+            if (j >= 1) xmf = xmf + divr(HFUS * (wice0 - ice), rdt) + zero_over(dtime);
+            else xmf = xmf + divr(HFUS * (wice0 - ice), rdt);
             if (imelt == 1 && j < 1) {
-                double m = fmax(0.0, (wice0 - ice)) / dtime;
+                double m = divr(fmax(0.0, (wice0 - ice)), rdt);
                 io.qflx_snomelt_lyr[ix] = m;
                 qflx_snomelt = qflx_snomelt + m;
                 io.snomelt_accum[c] = io.snomelt_accum[c] + m * dtime * 1.e-3;
             }
             if (imelt == 2 && j < 1) {
-                double f = fmax(0.0, (ice - wice0)) / dtime;
+                double f = divr(fmax(0.0, (ice - wice0)), rdt);
                 io.qflx_snofrz_lyr[ix] = f;
                 qflx_snofrz = qflx_snofrz + f;
             }
@@ -953,6 +956,43 @@ __global__ void rootsink_kernel(const int32_t* __restrict__ col_patchi, const in
         if (temp != 0.0) rc = rc / temp;
         qflx_rootsoi[c + (size_t)(j - 1) * ldc] = rc * tran_col;
     }
+}
+
+// Compute_EffecRootFrac_And_VertTranSink_Default
+// (src/biogeophys/SoilWaterPlantSinkMod.F90:332-420) as the drop-in: the
+// column effective root fraction and the soil water sink over a column
+// filter, the column transpiration from qflx_tran_veg_col or, if that is
+// NULL, the wtcol-weighted patch sum.  The per-level quotient by the
+// patches' weighted transpiration shares one reciprocal.
+__global__ void __launch_bounds__(128)
+rootsink_dropin_kernel(ctsmg_rootsink_io io, int begc, int begp, int nfilt, const int32_t* __restrict__ filt) {
+    const int fc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fc >= nfilt) return;
+    const int c = filt[fc] - begc;
+    const int p0 = io.col_patchi[c] - begp, np = io.col_npatches[c];
+    const int ldc = io.ldc, ldp = io.ldp;
+    double temp = 0.0;
+#pragma unroll 1
+    for (int p = p0; p < p0 + np; ++p) temp = temp + io.qflx_tran_veg[p] * io.wtcol[p];
+    const double tcol = io.qflx_tran_veg_col ? io.qflx_tran_veg_col[c] : temp;
+    const bool scale = temp != 0.0;
+    const Recip rt = recip(temp);
+#pragma unroll 1
+    for (int j = 1; j <= NLEVSOI; ++j) {
+        double rc = 0.0;
+        for (int p = p0; p < p0 + np; ++p)
+            rc = rc + io.rootr[p + (size_t)(j - 1) * ldp] * io.qflx_tran_veg[p] * io.wtcol[p];
+        if (scale) rc = divr(rc, rt);
+        io.rootr_col[c + (size_t)(j - 1) * ldc] = rc;
+        io.qflx_rootsoi[c + (size_t)(j - 1) * ldc] = rc * tcol;
+    }
+}
+
+cudaError_t launch_rootsink_dropin(const ctsmg_rootsink_io& io, int begc, int begp, int nfilt, const int32_t* d_filt,
+                                   cudaStream_t s) {
+    if (nfilt <= 0) return cudaSuccess;
+    rootsink_dropin_kernel<<<(nfilt + 127) / 128, 128, 0, s>>>(io, begc, begp, nfilt, d_filt);
+    return cudaGetLastError();
 }
 
 // ------------------------------------------------------------ launchers

@@ -32,6 +32,8 @@ struct HydroStepArgs;
 // aquifer-layer hydrology when hy is given).
 cudaError_t launch_zd09_step(const ctsmg_soilwater_io& io, int ncol, double e_ice, double dtime, int flexcn,
                              int refresh, const int32_t* d_filt, cudaStream_t s, const HydroStepArgs* hy);
+cudaError_t launch_rootsink_dropin(const ctsmg_rootsink_io& io, int begc, int begp, int nfilt, const int32_t* d_filt,
+                                   cudaStream_t s);
 cudaError_t launch_rootsink(const int32_t* col_patchi, const int32_t* col_npatches, const double* wtcol,
                             const double* qflx_tran_veg, const double* rootr, int ldp, double* qflx_rootsoi,
                             int ncol, cudaStream_t s, int ldc = 0, const int32_t* filt = nullptr);

@@ -13,6 +13,7 @@ namespace ctsmg {
 struct SoilResisArgs {
     int method;                      // 1 sl_14, 0 leepielke_1992
     double d_max, frac_sat_soil_dsl_init;
+    const double* d_max_c = nullptr; // per-column d_max (resident ensembles) or NULL
 };
 
 // Default-real literals of the reference (2.12e-5, 273.15) as the single
@@ -30,7 +31,7 @@ __device__ __forceinline__ void soilevap_resis_column(const ctsmg_soilresis_io& 
         const double d0 = (double)2.12e-5f * fm::pow(io.t_soisno[s1] / (double)273.15f, 1.75);
         const double eps = ws - aird;
         const double dg = eps * d0 * fm::pow(eps / ws, 3.0 / fmax(3.0, bsw));
-        double dsl = a.d_max * fmax(0.001, (a.frac_sat_soil_dsl_init * eff_por_top - vwc_liq)) /
+        double dsl = (a.d_max_c ? a.d_max_c[c] : a.d_max) * fmax(0.001, (a.frac_sat_soil_dsl_init * eff_por_top - vwc_liq)) /
                      fmax(0.001, (a.frac_sat_soil_dsl_init * ws - aird));
         dsl = fmax(dsl, 0.0);
         dsl = fmin(dsl, 200.0);

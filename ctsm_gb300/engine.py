@@ -55,7 +55,8 @@ class BatchInputs(C.Structure):
                 ("medlynslope_p", C.POINTER(C.c_double)), ("medlynintercept_p", C.POINTER(C.c_double)),
                 ("cpar", C.POINTER(abi.CanopyParams)), ("pft", C.POINTER(abi.Pftcon)),
                 ("sr", C.POINTER(abi.SoilResisIO)), ("hy", C.POINTER(abi.HydrologyIO)),
-                ("baseflow_scalar_c", C.POINTER(C.c_double)), ("fff_c", C.POINTER(C.c_double))]
+                ("baseflow_scalar_c", C.POINTER(C.c_double)), ("fff_c", C.POINTER(C.c_double)),
+                ("d_max_c", C.POINTER(C.c_double))]
 
 
 def _pt(x):
@@ -130,7 +131,8 @@ class SoilBatch:
                                None if self._rootr is None else self._rootr.ctypes.data_as(dp), ms, mi, par, pft,
                                _pt(self._sr), _pt(self._hy),
                                st["baseflow_scalar_c"].ctypes.data_as(dp) if pc else None,
-                               st["fff_c"].ctypes.data_as(dp) if pc else None)
+                               st["fff_c"].ctypes.data_as(dp) if pc else None,
+                               st["d_max_c"].ctypes.data_as(dp) if (self.soilresis and "d_max_c" in st) else None)
         check(self.L.ctsmg_batch_open(C.byref(self.h), C.byref(cfg), C.byref(self._in)))
 
     def run(self, nsteps, timed=False):

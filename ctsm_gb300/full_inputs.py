@@ -13,10 +13,15 @@ dz_j exp(-3 z_j) (normalised) that the plain workloads use for the sink.
 
 Ensemble members perturb 8 parameters by a factor drawn log-uniformly in
 [0.5, 1.5] (baseflow_scalar, fff, medlynslope, medlynintercept, jmaxb1, kmax,
-om_frac_sf, d_max).  On the scoped path medlynslope and medlynintercept enter
-Photosynthesis (per patch) and om_frac_sf the soil-property preparation; the
-other five act only in routines outside the path (drainage, runoff, LUNA,
-hydraulic stress, soil resistance) and are stored per member without effect.
+om_frac_sf, d_max).  medlynslope and medlynintercept enter Photosynthesis (per
+patch) and om_frac_sf the soil-property preparation.  With clm5=True the
+members run the CLM5-default step, where three more act per column:
+baseflow_scalar in SubsurfaceLateralFlow (SoilHydrologyMod.F90:2336), fff in
+SaturatedExcessRunoff (SaturatedExcessRunoffMod.F90:352) and d_max in the
+sl_14 soil resistance (SurfaceResistanceMod.F90:404).  jmaxb1 belongs to LUNA
+(LunaMod.F90:419) and kmax to the plant-hydraulic-stress photosynthesis
+(PhotosynthesisMod.F90:846), both outside the path: they are stored per
+member without effect.
 """
 import numpy as np
 
@@ -24,6 +29,10 @@ from . import abi, inputs, canopy_inputs
 
 ENSEMBLE_PARAMS = ("baseflow_scalar", "fff", "medlynslope", "medlynintercept", "jmaxb1", "kmax", "om_frac_sf",
                    "d_max")
+# defaults the member factors scale (the parameter-file values, absent here,
+# are builder's choices: ctsm_gb300.soil.set_soilhydrology_params /
+# set_soil_resistance use the same)
+BASEFLOW_SCALAR, FFF, D_MAX = 1.0e-2, 0.5, 15.0
 
 
 def full_state(ncol, seed=0, npatch_max=4, om_frac_sf=1.0, rng=None):
@@ -106,10 +115,13 @@ def _reprep_soil(A, r, om_frac_sf):
         A[k][:] = props[k]
 
 
-def ensemble(nmembers, seed=0, cols=(512, 8192), npatch_max=4):
+def ensemble(nmembers, seed=0, cols=(512, 8192), npatch_max=4, clm5=False):
     """Pack `nmembers` members (column counts U{cols}) into one state.
     Returns (A, npatch, ngrid, rootr, member_of_column, params) with params a
-    dict name -> (nmembers,) factors and per-patch Medlyn arrays in A."""
+    dict name -> (nmembers,) factors and per-patch Medlyn arrays in A.  With
+    clm5=True A also holds the components of the CLM5-default step (SoilFluxes,
+    root moisture stress, soil resistance, the default hydrology) and the
+    members' per-column baseflow_scalar_c, fff_c and d_max_c."""
     r = np.random.Generator(np.random.Philox(seed))
     factors = {k: np.exp(r.uniform(np.log(0.5), np.log(1.5), nmembers)) for k in ENSEMBLE_PARAMS}
     ncols = r.integers(cols[0], cols[1] + 1, nmembers)
@@ -127,6 +139,15 @@ def ensemble(nmembers, seed=0, cols=(512, 8192), npatch_max=4):
     base_int = np.array([row[7] for row in pft])[it]
     A["medlynslope_p"] = np.ascontiguousarray(base_slope * factors["medlynslope"][member_patch])
     A["medlynintercept_p"] = np.ascontiguousarray(base_int * factors["medlynintercept"][member_patch])
+    if clm5:
+        rc = np.random.Generator(np.random.Philox(seed * 1000003 + nmembers + 7))
+        add_soilfluxes_fields(A, npatch, ngrid)
+        add_rootmoist_fields(A, npatch, rootr, rng=rc)
+        add_soilresis_fields(A)
+        add_hydrology_fields(A, rc)
+        A["baseflow_scalar_c"] = np.ascontiguousarray(BASEFLOW_SCALAR * factors["baseflow_scalar"][member_col])
+        A["fff_c"] = np.ascontiguousarray(FFF * factors["fff"][member_col])
+        A["d_max_c"] = np.ascontiguousarray(D_MAX * factors["d_max"][member_col])
     return A, npatch, ngrid, rootr, member_col, factors
 
 

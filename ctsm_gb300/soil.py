@@ -62,6 +62,22 @@ def SoilTemperature(bounds, num_nolakec, filter_nolakec, state, dtime):
     check(L.ctsmg_soiltemperature(C.byref(bounds), int(num_nolakec), fp, C.byref(io), float(dtime)))
 
 
+def RootSink(bounds, num_filterc, filterc, state, tran_col=True):
+    """Compute_EffecRootFrac_And_VertTranSink_Default
+    (SoilWaterPlantSinkMod.F90:332) over the column filter; tran_col=False
+    passes no qflx_tran_veg_col (the library then uses the wtcol-weighted sum
+    of the patches' transpiration)."""
+    L = load()
+    L.ctsmg_root_sink.argtypes = [C.POINTER(abi.Bounds), C.c_int32, C.POINTER(C.c_int32),
+                                  C.POINTER(abi.RootSinkIO)]
+    f, fp = _filter(filterc)
+    ncol = bounds.endc - bounds.begc + 1
+    npat = bounds.endp - bounds.begp + 1
+    fields = [x for x in abi.ROOTSINK_FIELDS if tran_col or x[0] != "qflx_tran_veg_col"]
+    io = abi.make_io(abi.RootSinkIO, fields, state, ncol, npat)
+    check(L.ctsmg_root_sink(C.byref(bounds), int(num_filterc), fp, C.byref(io)))
+
+
 def SoilFluxes(bounds, num_nolakec, filter_nolakec, num_nolakep, filter_nolakep, state, dtime):
     """SoilFluxes (SoilFluxesMod.F90:36) after SoilTemperature; `state` also
     holds tssbef / t_h2osfc_bef, the temperatures saved before SoilTemperature."""

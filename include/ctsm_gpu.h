@@ -403,6 +403,37 @@ typedef struct {
 int32_t ctsmg_root_moist_stress(const ctsmg_bounds* bounds, int32_t num_exposedvegp,
                                 const int32_t* filter_exposedvegp, const ctsmg_rootmoist_io* io);
 
+/* SetSoilWaterFractions (src/biogeophys/SoilHydrologyMod.F90:236-249, called
+ * at src/biogeophys/HydrologyNoDrainageMod.F90:302 before SoilWater), without
+ * excess ice: eff_porosity and icefrac on levels 1..nlevsoi from dz,
+ * h2osoi_ice and watsat of the SoilWater io struct.                      */
+int32_t ctsmg_set_soil_water_fractions(const ctsmg_bounds* bounds, int32_t num_hydrologyc,
+                                       const int32_t* filter_hydrologyc, const ctsmg_soilwater_io* io);
+
+/* ---------------------------------------------------------------- root water sink */
+/* Components of Compute_EffecRootFrac_And_VertTranSink_Default
+ * (src/biogeophys/SoilWaterPlantSinkMod.F90:332-420), the transpiration sink
+ * SoilWater's Zeng-Decker and moisture forms take (called from
+ * src/biogeophys/SoilWaterPlantSinkMod.F90:55-120 before SoilWater).  Every
+ * patch of a filtered column is active (patch%active).                    */
+typedef struct {
+    int32_t ldc, ldp;
+    const int32_t* col_patchi;        /* (c)  first patch of the column (global)     */
+    const int32_t* col_npatches;      /* (c)                                        */
+    const double*  wtcol;             /* (p)  patch weight on the column             */
+    const double*  qflx_tran_veg;     /* (p)  patch transpiration (mm/s)             */
+    const double*  qflx_tran_veg_col; /* (c)  column transpiration (mm/s); NULL = the
+                                         wtcol-weighted sum of the patches'          */
+    const double*  rootr;             /* [PG] patch effective root fraction (levels
+                                         1..nlevsoi read)                           */
+    double*        rootr_col;         /* [G]  out: column effective root fraction,
+                                         levels 1..nlevsoi                          */
+    double*        qflx_rootsoi;      /* [S]  out: soil water sink (mm/s)            */
+} ctsmg_rootsink_io;
+
+int32_t ctsmg_root_sink(const ctsmg_bounds* bounds, int32_t num_filterc, const int32_t* filterc,
+                        const ctsmg_rootsink_io* io);
+
 /* ------------------------------------------------------- hydrology neighbours of SoilWater */
 /* The water-table and drainage routines of the default (no aquifer layer)
  * hydrology around SoilWater, for natural soil columns outside hillslopes
@@ -768,6 +799,8 @@ typedef struct {
     const ctsmg_hydrology_io* hy;
     const double* baseflow_scalar_c;     /* (c) or NULL */
     const double* fff_c;                 /* (c) or NULL */
+    const double* d_max_c;               /* (c) or NULL: per-column d_max of the sl_14
+                                            soil resistance (ensemble members)     */
 } ctsmg_batch_inputs;
 
 /* Create a batch from `in` (the arrays are copied); ctsmg_batch_create*

@@ -1023,3 +1023,37 @@ extern "C" void oracle_rootsink(int ncol, int ldp, const int32_t* col_patchi, co
         }
     }
 }
+
+// Compute_EffecRootFrac_And_VertTranSink_Default
+// (src/biogeophys/SoilWaterPlantSinkMod.F90:332-420) over a column filter with
+// the drop-in's io struct: rootr_col zeroed (:376-381), accumulated level by
+// level over the column's patches (:383-393), temp summed (:394-401), then
+// the quotient and qflx_rootsoi = rootr_col * qflx_tran_veg_col (:403-412);
+// a NULL qflx_tran_veg_col stands for the wtcol-weighted patch sum.
+extern "C" int oracle_root_sink(const ctsmg_bounds* b, int nf, const int32_t* filt, const ctsmg_rootsink_io* io) {
+    const int ldc = io->ldc, ldp = io->ldp;
+    std::vector<double> temp(b->endc - b->begc + 1, 0.0);
+    for (int j = 1; j <= NLEVSOI; ++j)
+        for (int fc = 0; fc < nf; ++fc) io->rootr_col[(filt[fc] - b->begc) + (size_t)(j - 1) * ldc] = 0.0;
+    for (int j = 1; j <= NLEVSOI; ++j)
+        for (int fc = 0; fc < nf; ++fc) {
+            const int c = filt[fc] - b->begc;
+            const int p0 = io->col_patchi[c] - b->begp, np = io->col_npatches[c];
+            double& r = io->rootr_col[c + (size_t)(j - 1) * ldc];
+            for (int p = p0; p < p0 + np; ++p) r = r + io->rootr[p + (size_t)(j - 1) * ldp] * io->qflx_tran_veg[p] * io->wtcol[p];
+        }
+    for (int fc = 0; fc < nf; ++fc) {
+        const int c = filt[fc] - b->begc;
+        const int p0 = io->col_patchi[c] - b->begp, np = io->col_npatches[c];
+        for (int p = p0; p < p0 + np; ++p) temp[c] = temp[c] + io->qflx_tran_veg[p] * io->wtcol[p];
+    }
+    for (int j = 1; j <= NLEVSOI; ++j)
+        for (int fc = 0; fc < nf; ++fc) {
+            const int c = filt[fc] - b->begc;
+            double& r = io->rootr_col[c + (size_t)(j - 1) * ldc];
+            if (temp[c] != 0.0) r = r / temp[c];
+            const double tcol = io->qflx_tran_veg_col ? io->qflx_tran_veg_col[c] : temp[c];
+            io->qflx_rootsoi[c + (size_t)(j - 1) * ldc] = r * tcol;
+        }
+    return 0;
+}

@@ -39,6 +39,7 @@ def lib():
         _LIB.oracle_set_patch_medlyn.restype = None
         _LIB.oracle_rootsink.argtypes = [I, I, P(C.c_int32), P(C.c_int32)] + [P(C.c_double)] * 4
         _LIB.oracle_rootsink.restype = None
+        _LIB.oracle_root_sink.argtypes = [P(abi.Bounds), I, P(C.c_int32), P(abi.RootSinkIO)]
         _LIB.oracle_canopyfluxes.argtypes = [P(abi.Bounds), I, P(C.c_int32), P(abi.CanopyIO), C.c_double, P(C.c_int)]
         _LIB.oracle_hydrology.argtypes = [P(abi.Bounds), I, P(C.c_int32), P(abi.HydrologyIO), I,
                                           P(abi.SoilHydrologyParams), C.c_double]

@@ -15,7 +15,7 @@ def _p(a, t=C.c_double):
 
 
 def full_steps(A, npatch, ngrid, rootr, nsteps, medlyn_per_patch=False, method=1, itmax=40, snow_method=0,
-               soilfluxes=False, rootmoist=False, swm=None):
+               soilfluxes=False, rootmoist=False, swm=None, soilresis=None, hydro=None):
     """nsteps x (CanopyFluxes, root sink, SoilTemperature, [SoilFluxes,]
     SoilWater, h2osoi_vol refresh) in place on A.  displa / z0mv keep their
     SatellitePhenology values and cgrnds / cgrndl restart from zero every
@@ -24,7 +24,10 @@ def full_steps(A, npatch, ngrid, rootr, nsteps, medlyn_per_patch=False, method=1
     moisture stress of the current soil state at the start of every step
     (A then holds the ROOTMOIST components; `rootr` is not used).  swm (an
     abi.SoilWaterMovementNml) selects the SoilWater form and the flexibleCN
-    fix; None is the Zeng-Decker form."""
+    fix; None is the Zeng-Decker form.  soilresis = [(column filter,
+    abi.SoilResistanceParams), ...] runs calc_soilevap_resis first in every
+    step (one entry per parameter set, e.g. per ensemble member); hydro (see
+    `hydrology`) runs the default hydrology around SoilWater."""
     L = orc.lib()
     ncol = A["zwt"].shape[0]
     L.oracle_set_canopy_params(C.byref(canopy_inputs.make_params()), C.byref(canopy_inputs.make_pftcon()), method,
@@ -42,6 +45,11 @@ def full_steps(A, npatch, ngrid, rootr, nsteps, medlyn_per_patch=False, method=1
             A["z0mv"][:] = z0mv0
             A["cgrnds"][:] = 0.0
             A["cgrndl"][:] = 0.0
+            if soilresis:
+                sr = abi.make_io(abi.SoilResisIO, abi.SOILRESIS_FIELDS, A, ncol)
+                for f, par in soilresis:
+                    f = np.ascontiguousarray(f, dtype=np.int32)
+                    assert L.oracle_soilevap_resis(C.byref(b), len(f), _p(f, C.c_int32), C.byref(sr), C.byref(par)) == 0
             if rootmoist:
                 rm = abi.make_io(abi.RootMoistIO, abi.ROOTMOIST_FIELDS, A, ncol, npatch)
                 assert L.oracle_root_moist_stress(C.byref(b), npatch, _p(filt_p, C.c_int32), C.byref(rm)) == 0
@@ -61,7 +69,7 @@ def full_steps(A, npatch, ngrid, rootr, nsteps, medlyn_per_patch=False, method=1
                 sf = abi.make_io(abi.SoilFluxesIO, abi.SOILFLUXES_FIELDS, A, ncol, npatch)
                 assert L.oracle_soilfluxes(C.byref(b), ncol, _p(filt_c, C.c_int32), npatch, _p(filt_p, C.c_int32),
                                            C.byref(sf), DT) == 0
-            soilwater(L, A, b, filt_c, swm)
+            soilwater(L, A, b, filt_c, swm, hydro=hydro)
             inputs.refresh_h2osoi_vol(A)
     finally:
         A["displa"][:] = displa0

@@ -143,3 +143,93 @@ def test_full_step_with_root_moisture_stress_matches_oracle(gpu_lib):
     errs, bad = compare(G, R, STATE + SF_OUT + ["btran", "rootr", "rresis", "eff_porosity", "h2osoi_liqvol"], 1e-9,
                         spread)
     assert not bad, {k: errs[k] for k in bad}
+
+
+def test_clm5_ensemble_members_match_oracle(gpu_lib):
+    """The perturbed-parameter ensemble on the CLM5-default step (soil
+    resistance, root moisture stress, CanopyFluxes, root sink,
+    SoilTemperature, SoilFluxes, the moisture form with the default hydrology)
+    with six of the eight parameters acting: medlynslope / medlynintercept per
+    patch, om_frac_sf in the soil properties, baseflow_scalar, fff and d_max
+    per column.  Every member's result equals the oracle stepped with that
+    member's parameters."""
+    from ctsm_gb300 import abi, canopy
+    from ctsm_gb300.engine import SoilBatch
+    nm = 4
+    A, npatch, ngrid, rootr, member_col, f = fi.ensemble(nm, seed=12, cols=(200, 500), clm5=True)
+    nml = abi.soilwater_movement_nml(1)
+    gpu_lib.set_soilwater_movement(nml)
+    gpu_lib.set_soilhydrology_params()
+    gpu_lib.set_soil_resistance()
+    canopy.set_params()
+    try:
+        hydro, sres = [], []
+        for m in range(nm):
+            cols = np.nonzero(member_col == m)[0].astype(np.int32) + 1
+            hydro.append((cols, abi.SoilHydrologyParams(0.01, 1.0, fi.BASEFLOW_SCALAR * f["baseflow_scalar"][m], 1.0e-5,
+                                                        6.0, fi.FFF * f["fff"][m], 0.4, 0.13, 1)))
+            sres.append((cols, abi.SoilResistanceParams(1, fi.D_MAX * f["d_max"][m], 0.8)))
+        kw = dict(medlyn_per_patch=True, soilfluxes=True, rootmoist=True, swm=nml, soilresis=sres, hydro=hydro)
+        R = copy.deepcopy(A)
+        full_steps(R, npatch, ngrid, rootr, 2, **kw)
+        G = copy.deepcopy(A)
+        b = SoilBatch(G, npatch, canopy=True, ngrid=ngrid, per_patch_medlyn=True, soilfluxes=True, rootmoist=True,
+                      soilresis=True, hydrology=True, per_column_hydrology=True)
+        b.run(2)
+        b.sync()
+        b.download()
+        b.close()
+        keys = STATE + ["soilresis", "dsl", "btran", "zwt", "zwt_perched", "fsat", "qflx_infl", "qflx_drain",
+                        "qflx_latflow_out", "num_substeps", "eflx_soil_grnd"]
+        cancel = CANCEL + ("qflx_drain", "qflx_drain_perched", "eflx_soil_grnd")
+        spread = noise_spread(lambda B: full_steps(B, npatch, ngrid, rootr, 2, **kw), A, R, fields=cancel,
+                              input_ulps=4)
+        for k in ("liqcan", "snocan"):
+            spread[k] = spread[k] + 1e-9 * (np.abs(A["liqcan"]) + np.abs(A["snocan"]))
+        errs, bad = compare(G, R, keys, 1e-9, spread)
+        assert not bad, {k: errs[k] for k in bad}
+        # the three per-column parameters act: members differ where only they differ
+        assert len(np.unique(np.round(A["d_max_c"], 12))) == nm
+        assert np.ptp(R["soilresis"]) > 0 and (R["zwt"] != A["zwt"]).mean() > 0.5
+    finally:
+        gpu_lib.set_soilwater_movement(abi.soilwater_movement_nml(0, use_bedrock=0))
+
+
+def test_plain_clm5_step_matches_oracle(gpu_lib):
+    """The CLM5-default step made of drop-in calls alone (ctsm_gb300.plain_step,
+    the plain arm of the ensemble benchmark: soil resistance, root moisture
+    stress, CanopyFluxes, the root-sink drop-in, SoilTemperature, SoilFluxes,
+    SetSoilWaterFractions, the default hydrology around the moisture-form
+    SoilWater) against the oracle stepped the same way, one member's
+    parameters, 2 steps."""
+    from ctsm_gb300 import abi, canopy
+    from ctsm_gb300.plain_step import PlainCLM5Step
+    A, npatch, ngrid, rootr, member_col, f = fi.ensemble(1, seed=21, cols=(900, 900), clm5=True)
+    nml = abi.soilwater_movement_nml(1)
+    gpu_lib.set_soilwater_movement(nml)
+    try:
+        med = (float(f["medlynslope"][0]), float(f["medlynintercept"][0]))
+        dmax, bs, fff = (fi.D_MAX * f["d_max"][0], fi.BASEFLOW_SCALAR * f["baseflow_scalar"][0], fi.FFF * f["fff"][0])
+        cols = np.arange(1, A["zwt"].shape[0] + 1, dtype=np.int32)
+        kw = dict(medlyn_per_patch=True, soilfluxes=True, rootmoist=True, swm=nml,
+                  soilresis=[(cols, abi.SoilResistanceParams(1, dmax, 0.8))],
+                  hydro=[(cols, abi.SoilHydrologyParams(0.01, 1.0, bs, 1.0e-5, 6.0, fff, 0.4, 0.13, 1))])
+        R = copy.deepcopy(A)
+        full_steps(R, npatch, ngrid, rootr, 2, **kw)
+        G = copy.deepcopy(A)
+        st = PlainCLM5Step(G, npatch, ngrid, medlyn=med, d_max=dmax, baseflow_scalar=bs, fff=fff)
+        st.step()
+        st.step()
+        keys = STATE + ["soilresis", "btran", "zwt", "qflx_infl", "qflx_drain", "num_substeps", "eflx_soil_grnd"]
+        cancel = CANCEL + ("qflx_drain", "eflx_soil_grnd")
+        spread = noise_spread(lambda B: full_steps(B, npatch, ngrid, rootr, 2, **kw), A, R, fields=cancel,
+                              input_ulps=4)
+        for k in ("liqcan", "snocan"):
+            spread[k] = spread[k] + 1e-9 * (np.abs(A["liqcan"]) + np.abs(A["snocan"]))
+        errs, bad = compare(G, R, keys, 1e-9, spread)
+        assert not bad, {k: errs[k] for k in bad}
+    finally:
+        gpu_lib.set_soilwater_movement(abi.soilwater_movement_nml(0, use_bedrock=0))
+        gpu_lib.set_soil_resistance()
+        gpu_lib.set_soilhydrology_params()
+        canopy.set_params()
