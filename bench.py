@@ -481,59 +481,88 @@ def canopy_leg(args, barrier):
     return out
 
 
+def member_state(A, member_col, m):
+    """Member m of a packed ensemble state as a state of its own (its columns,
+    patches and gridcells, index maps rebased)."""
+    ncol, npatch = A["zwt"].shape[0], A["wtcol"].shape[0]
+    cols = np.nonzero(member_col == m)[0]
+    pidx = np.nonzero(np.isin(A["patch_column"] - 1, cols))[0]
+    S = {}
+    for k, v in A.items():
+        if v.shape[-1] == ncol:
+            S[k] = np.ascontiguousarray(v[..., cols])
+        elif v.shape[-1] == npatch:
+            S[k] = np.ascontiguousarray(v[..., pidx])
+    S["col_patchi"] = (A["col_patchi"][cols] - pidx[0]).astype(np.int32)
+    S["patch_column"] = (A["patch_column"][pidx] - cols[0]).astype(np.int32)
+    S["patch_gridcell"] = S["patch_column"].copy()
+    return S, len(pidx), len(cols)
+
+
 def ensemble_leg(args, barrier):
-    """The perturbed-parameter ensemble through the full step: all members in
+    """The perturbed-parameter ensemble on the CLM5-default step (soil
+    resistance, root moisture stress, CanopyFluxes, root sink,
+    SoilTemperature, SoilFluxes, the moisture-form SoilWater with the default
+    hydrology), six of the eight parameters acting (medlynslope,
+    medlynintercept, om_frac_sf, baseflow_scalar, fff, d_max): every member in
     one resident batch (one CUDA graph per step) against the plain form, one
-    set of drop-in calls per member (timed on a sample of members)."""
-    from ctsm_gb300 import full_inputs as fi, plain_step, canopy
+    set of drop-in C-ABI calls per member, timed over every member."""
+    from ctsm_gb300 import abi, canopy, full_inputs as fi, soil
     from ctsm_gb300.engine import SoilBatch
-    A, npatch, ngrid, rootr, member_col, factors = fi.ensemble(args.ens_members, seed=args.seed)
+    from ctsm_gb300.plain_step import PlainCLM5Step
+    A, npatch, ngrid, rootr, member_col, f = fi.ensemble(args.ens_members, seed=args.seed, clm5=True)
     ncol = A["zwt"].shape[0]
-    b = SoilBatch(copy.deepcopy(A), npatch, canopy=True, ngrid=ngrid, rootr=rootr, per_patch_medlyn=True)
-    block = b.autotune(trial_steps=1)
-    b.run(args.warmup)
-    b.sync()
-    barrier()
-    ms = b.run(args.ens_steps, timed=True)
-    b.sync()
-    b.close()
-    batched = ncol * args.ens_steps / (float(ms.sum()) * 1e-3)
-    # plain form on the first members, two steps each
-    nm = min(8, args.ens_members)
-    cols_done = 0
-    t_plain = 0.0
-    for m in range(nm):
-        cols = np.nonzero(member_col == m)[0]
-        pmask = np.isin(A["patch_column"] - 1, cols)
-        pidx = np.nonzero(pmask)[0]
-        S = {}
-        for k, v in A.items():
-            if v.shape[-1] == ncol:
-                S[k] = np.ascontiguousarray(v[..., cols])
-            elif v.shape[-1] == npatch:
-                S[k] = np.ascontiguousarray(v[..., pidx])
-        S["col_patchi"] = (A["col_patchi"][cols] - pidx[0]).astype(np.int32)
-        S["patch_column"] = (A["patch_column"][pidx] - cols[0]).astype(np.int32)
-        S["patch_gridcell"] = S["patch_column"].copy()
-        rr = np.ascontiguousarray(rootr[:, pidx])
-        d0, z0 = S["displa"].copy(), S["z0mv"].copy()
-        med = (float(factors["medlynslope"][m]), float(factors["medlynintercept"][m]))
-        plain_step.full_step(S, len(pidx), len(cols), rr, d0, z0, med)          # warm-up
+    nml = abi.soilwater_movement_nml(1)
+    soil.set_soilwater_movement(nml)
+    soil.set_soilhydrology_params()
+    soil.set_soil_resistance()
+    canopy.set_params()
+    try:
+        b = SoilBatch(copy.deepcopy(A), npatch, canopy=True, ngrid=ngrid, per_patch_medlyn=True, soilfluxes=True,
+                      rootmoist=True, soilresis=True, hydrology=True, per_column_hydrology=True)
+        block = b.autotune(trial_steps=1)
+        b.run(args.warmup)
+        b.sync()
+        barrier()
+        ms = b.run(args.ens_steps, timed=True)
+        b.sync()
+        b.close()
+        batched = ncol * args.ens_steps / (float(ms.sum()) * 1e-3)
+        # the plain form: every member, one set of drop-in calls per member and step
+        steppers = []
+        for m in range(args.ens_members):
+            S, npm, ncm = member_state(A, member_col, m)
+            steppers.append(PlainCLM5Step(S, npm, ncm, medlyn=(float(f["medlynslope"][m]),
+                                                               float(f["medlynintercept"][m])),
+                                          d_max=fi.D_MAX * float(f["d_max"][m]),
+                                          baseflow_scalar=fi.BASEFLOW_SCALAR * float(f["baseflow_scalar"][m]),
+                                          fff=fi.FFF * float(f["fff"][m])))
+        for st in steppers[:4]:
+            st.step()                                             # warm-up
+        kp = 2
         barrier()
         t0 = time.perf_counter()
-        for _ in range(2):
-            plain_step.full_step(S, len(pidx), len(cols), rr, d0, z0, med)
+        for _ in range(kp):
+            for st in steppers:
+                st.step()
         barrier()
-        t_plain += time.perf_counter() - t0
-        cols_done += 2 * len(cols)
-    canopy.set_params()
-    plain = cols_done / t_plain
-    return {"workload": "%d members, columns U{512..8192} each (%d columns, %d patches), full soil+canopy step, "
-                        "8 parameters log-uniform x[0.5,1.5]" % (args.ens_members, ncol, npatch),
+        t_plain = time.perf_counter() - t0
+        plain = ncol * kp / t_plain
+    finally:
+        soil.set_soilwater_movement(abi.soilwater_movement_nml(0, use_bedrock=0))
+        soil.set_soilhydrology_params()
+        soil.set_soil_resistance()
+        canopy.set_params()
+    return {"workload": "%d members, columns U{512..8192} each (%d columns, %d patches), CLM5-default step "
+                        "(soil resistance, root moisture stress, CanopyFluxes, root sink, SoilTemperature, "
+                        "SoilFluxes, moisture-form SoilWater + default hydrology), 8 parameters log-uniform "
+                        "x[0.5,1.5], 6 acting (jmaxb1: LUNA, kmax: plant hydraulics, outside the path)"
+                        % (args.ens_members, ncol, npatch),
             "columns": ncol, "patches": npatch, "steps": args.ens_steps, "ms_per_step": float(ms.mean()),
             "batched_column_steps_per_s": batched, "block": block,
             "plain_column_steps_per_s": plain,
-            "plain_sample": "%d members x 2 steps, one set of drop-in calls per member" % nm,
+            "plain_sample": "all %d members x %d steps, one set of %d drop-in C-ABI calls (and 3 parameter setters) per member and step "
+                            "(%.2f s)" % (args.ens_members, kp, 14, t_plain),
             "batched_over_plain": batched / plain}
 
 
@@ -589,18 +618,15 @@ def serving_leg(args):
     cap = pool.capacity
     st = serving.serve(pool, reqs, time_limit=args.serve_seconds)
     pool.close()
-    pace = []
-    for q in reqs:
-        if q.steps_done > 0:
-            end = q.t_done if q.t_done == q.t_done else st["wall_s"]
-            pace.append((end - q.arrival) / (q.steps_done / serving.STEPS_PER_DAY))
     st.update({"workload": "Poisson arrivals at %.2f/s, %d requests, columns log-uniform 1..50000, "
                            "lengths U{48..17520} steps, full soil+canopy step" % (args.serve_rate, args.serve_requests),
                "budget_gb": args.serve_budget_gb, "capacity_columns": cap[0], "time_limit_s": args.serve_seconds,
                "offered_column_steps": int(sum(q.column_steps() for q in reqs)),
-               "p50_pace_s_per_day": serving.percentile(pace, 50), "p99_pace_s_per_day": serving.percentile(pace, 99),
-               "latency_note": "p50/p99_s_per_day: completed requests, (completion - arrival) / simulated days; "
-                               "pace: every request, (end or limit - arrival) / simulated days run"})
+               "latency_note": "headline p50/p99_pace_s_per_day: every request that ran, (completion or time "
+                               "limit - arrival) / simulated days it advanced; p50/p99_s_per_day: completed "
+                               "requests only, (completion - arrival) / simulated days; nonfinite_*: final "
+                               "states with a non-finite temperature or liquid water (melted snow layers stay "
+                               "layers without SnowHydrology and heat without bound, in the oracle alike)"})
     return st
 
 

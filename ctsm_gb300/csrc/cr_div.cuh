@@ -2,25 +2,29 @@
 //
 // The soil kernels divide many numerators by the same denominator (the layer
 // spacing z(j+1)-z(j) in the heat flux, the matrix rows and the post-solve
-// flux; dtime; the porosity; the band-LU pivot in the back substitution).  On
-// GB300 an FP64 division is 8 FP64-pipe instructions and the correctly rounded
-// reciprocal RN(1/b) 5 (measured), so a quotient is formed here from y =
-// RN(1/b), computed once per divisor, by one Newton-Markstein correction
-// (P. Markstein, "Computation of elementary functions on the IBM RISC
-// System/6000 processor", IBM J. Res. Dev. 34(1), 1990; J.-M. Muller et al.,
-// Handbook of Floating-Point Arithmetic, 2nd ed., 2018, sec. 4.7):
+// flux; dtime; the porosity; the pivot of each elimination step), and every
+// FP64 instruction counts on GB300: an IEEE division is 8 FP64-pipe
+// instructions (measured).  Here a quotient is formed from an approximate
+// reciprocal y of b, computed once per divisor, and one Newton-Markstein
+// correction (P. Markstein, "Computation of elementary functions on the IBM
+// RISC System/6000 processor", IBM J. Res. Dev. 34(1), 1990; J.-M. Muller et
+// al., Handbook of Floating-Point Arithmetic, 2nd ed., 2018, sec. 4.7):
 //
 //   q0 = RN(a y),  r = RN(a - b q0) (one FMA),  q = RN(q0 + r y) (one FMA).
 //
-// With y = (1/b)(1 + e1), q0 = (a/b)(1 + e1)(1 + e2) and r = RN(a - b q0),
-// |e_i| <= u = 2^-53, the exact value before the last rounding is
-// (a/b)(1 + d) with |d| <= (2u + u^2)^2 (1 + u) < 2^-103.9, so q is RN(a/b)
-// -- the same bits as the division -- unless a/b lies within 2^-103.9 |a/b|
-// of the midpoint between two doubles, where it may be the other neighbour
-// (one ulp).  Three FP64 instructions per quotient.  Zero, subnormal, huge,
-// infinite and NaN operands (biased exponent of a or b outside [0x201,
-// 0x5fe], checked with integer instructions) take the ordinary division, so
-// special values behave exactly as a / b.
+// On the device y is the special-function unit's reciprocal seed
+// (rcp.approx.ftz.f64, relative error below 2^-19.9, measured) refined by one
+// Newton step y1 = y0 + y0 (1 - b y0): relative error e1 below 2^-39.8.  Then
+// q0 = (a/b)(1 + e1)(1 + e2), |e2| <= 2^-53, and the exact value before the
+// last rounding is (a/b)(1 - h (e1 + e3 + e1 e3)) with h = e1 + e2 + e1 e2 and
+// |e3| <= 2^-53: within 2^-79 |a/b| of a/b, so q is RN(a/b) -- the same bits
+// as the division -- unless a/b lies within 2^-79 |a/b| of the midpoint
+// between two doubles, where it may be the other neighbour (one ulp).  A
+// reciprocal costs 2 FP64 instructions and a quotient 3 (a division 8).  The
+// host build (the tests' reference for this header) uses y = RN(1/b).  Zero,
+// subnormal, huge, infinite and NaN operands (biased exponent of a or b
+// outside [0x201, 0x5fe], checked with integer instructions) take the
+// ordinary division, so special values behave exactly as a / b.
 #pragma once
 #include <cstring>
 
@@ -33,7 +37,7 @@
 namespace ctsmg {
 
 struct Recip {
-    double b, y;   // divisor and RN(1/b)
+    double b, y;   // divisor and its reciprocal (RN(1/b) on the host, within 2^-39.8 on the device)
     int ok;        // b inside the exponent range of the fast path
 };
 
@@ -52,7 +56,9 @@ CTSMG_CRD_HD Recip recip(double b) {
     Recip r;
     r.b = b;
 #ifdef __CUDA_ARCH__
-    r.y = __drcp_rn(b);
+    double y0;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y0) : "d"(b));
+    r.y = __fma_rn(y0, __fma_rn(-b, y0, 1.0), y0);
 #else
     r.y = 1.0 / b;
 #endif
@@ -60,7 +66,7 @@ CTSMG_CRD_HD Recip recip(double b) {
     return r;
 }
 
-// a / R.b: RN(a/b) except within 2^-103.9 |a/b| of a rounding midpoint.
+// a / R.b: RN(a/b) except within 2^-79 |a/b| of a rounding midpoint.
 CTSMG_CRD_HD double divr(double a, const Recip& R) {
     if (!(R.ok & crdiv_in_range(a))) return a / R.b;
 #ifdef __CUDA_ARCH__
@@ -82,6 +88,9 @@ CTSMG_CRD_HD double zero_over(double b) {
     return (b < 0.0) ? -0.0 : 0.0;
 #endif
 }
+
+// a / b through a reciprocal of its own: 5 FP64 instructions against 8.
+CTSMG_CRD_HD double divf(double a, double b) { return divr(a, recip(b)); }
 
 // A constant divisor with its reciprocal RN(1/b) formed by the compiler.
 #define CTSMG_CONST_RECIP(b) (::ctsmg::Recip{(b), 1.0 / (b), 1})

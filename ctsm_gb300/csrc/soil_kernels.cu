@@ -60,32 +60,32 @@ __device__ __forceinline__ ZdLevel zd09_level(const ctsmg_soilwater_io& io, int 
     L.zimm = io.zi[c + (size_t)(j + NLEVSNO) * ld] * 1.e3;
     const Recip rws = recip(ws);
     // :649-665 ice fraction and liquid content
-    const double vol_ice = fmin(ws, io.h2osoi_ice[ss_ix] / (dzj * DENICE));
+    const double vol_ice = fmin(ws, divf(io.h2osoi_ice[ss_ix], dzj * DENICE));
     L.icef = fmin(1.0, divr(vol_ice, rws));
     io.icefrac[g_ix] = L.icef;
-    L.vwc = fmax(io.h2osoi_liq[ss_ix], 1.0e-6) / (dzj * DENH2O);
+    L.vwc = divf(fmax(io.h2osoi_liq[ss_ix], 1.0e-6), dzj * DENH2O);
     // :670-712 equilibrium volumetric water and matric potential: water table
     // above the layer, inside it, below it.  temp0 is the same expression in
     // the last two cases and tempi is only needed in the last, so each power
     // has one call site.
     const bool above = zwtmm <= zimm_prev;
     const bool inside = !above && (zwtmm < L.zimm) && (zwtmm > zimm_prev);
-    double temp0 = 0.0, tempi = 1.0, veq;
+    double temp0 = 0.0, tempi = 1.0, veq, omb = 0.0;
     if (!above) {
         const Recip rss = recip(ss);
-        const double e = 1.0 - 1.0 / bb;
-        temp0 = fm::pow(divr(ss + zwtmm - zimm_prev, rss), e);
-        if (!inside) tempi = fm::pow(divr(ss + zwtmm - L.zimm, rss), e);
+        omb = 1.0 - divf(1.0, bb);                // 1 - 1/b
+        temp0 = fm::pow(divr(ss + zwtmm - zimm_prev, rss), omb);
+        if (!inside) tempi = fm::pow(divr(ss + zwtmm - L.zimm, rss), omb);
     }
     if (above) {
         veq = ws;
     } else if (inside) {
-        double voleq1 = -ss * ws / (1.0 - 1.0 / bb) / (zwtmm - zimm_prev) * (tempi - temp0);
-        veq = (voleq1 * (zwtmm - zimm_prev) + ws * (L.zimm - zwtmm)) / (L.zimm - zimm_prev);
+        double voleq1 = divf(divf(-ss * ws, omb), zwtmm - zimm_prev) * (tempi - temp0);
+        veq = divf(voleq1 * (zwtmm - zimm_prev) + ws * (L.zimm - zwtmm), L.zimm - zimm_prev);
         veq = fmin(ws, veq);
         veq = fmax(veq, 0.0);
     } else {
-        veq = -ss * ws / (1.0 - 1.0 / bb) / (L.zimm - zimm_prev) * (tempi - temp0);
+        veq = divf(divf(-ss * ws, omb), L.zimm - zimm_prev) * (tempi - temp0);
         veq = fmax(veq, 0.0);
         veq = fmin(ws, veq);
     }
@@ -95,7 +95,7 @@ __device__ __forceinline__ ZdLevel zd09_level(const ctsmg_soilwater_io& io, int 
     s_node = fmin(1.0, s_node);
     const double sm = fmax(smpmin, -ss * fm::pow(s_node, -bb));
     L.smp = sm;
-    L.dsmpdw = -bb * sm / L.vwc;
+    L.dsmpdw = divf(-bb * sm, L.vwc);
     io.smp_l[g_ix] = sm;
     return L;
 }
@@ -174,7 +174,7 @@ __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, d
         const double s2 = cur.hks * fm::pow(s1, 2.0 * cur.bb + 2.0);
         const double imped = pow10_dd(-e_ice * (0.5 * (cur.icef + nx.icef)));
         const double hk = imped * s1 * s2;
-        const double dhkdw = imped * (2.0 * cur.bb + 3.0) * s2 * rB.y;
+        const double dhkdw = imped * (2.0 * cur.bb + 3.0) * s2 * divr(1.0, rB);
         io.hk_l[c + (size_t)(j - 1) * ld] = hk;
         if (j == jq) imped_q = imped;
         if (j == jm) { smp_m = cur.smp; zq_m = cur.zq; }
@@ -188,7 +188,7 @@ __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, d
             const double dqodw2 = divr(-(hk * nx.dsmpdw + num * dhkdw), rden);
             if (j == 1) {
                 const double qin = io.qflx_infl[c];
-                eliminate(1, 0.0, cur.dzmm * (0.0 + rdt.y) + dqodw1, dqodw2, qin - qout - ROOT(1));
+                eliminate(1, 0.0, cur.dzmm * (0.0 + divr(1.0, rdt)) + dqodw1, dqodw2, qin - qout - ROOT(1));
                 setq(1, qin, qout);
             } else {
                 eliminate(j, -dq_up0, divr(cur.dzmm, rdt) - dq_up1 + dqodw1, dqodw2, q_up - qout - ROOT(j));
@@ -330,12 +330,12 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
                 // overwrites it with thk_bedrock (:710-725); the value is unused
                 t = THK_BEDROCK;
             } else {
-                double satw = (divr(liq, R_DENH2O) + divr(ice, R_DENICE) + 0.0 / DENICE) / (dzj * ws);
+                double satw = divf(divr(liq, R_DENH2O) + divr(ice, R_DENICE) + 0.0 / DENICE, dzj * ws);
                 satw = fmin(1.0, satw);
                 if (satw > .1e-6) {
                     double dke = (T[ssi(j)] >= TFRZ) ? fmax(0.0, fm::log10(satw) + 1.0) : satw;
-                    const double xl = liq / (DENH2O * dzj);
-                    double fl = xl / (xl + ice / (DENICE * dzj) + zero_over(DENICE * dzj));
+                    const double xl = divf(liq, DENH2O * dzj);
+                    double fl = divf(xl, xl + divf(ice, DENICE * dzj) + zero_over(DENICE * dzj));
                     double dksat = io.tkmg[gi(j)] * tkwat_tkice_pow(fl * ws, (1.0 - fl) * ws);
                     t = dke * dksat + (1.0 - dke) * io.tkdry[gi(j)];
                 } else {
@@ -347,7 +347,7 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
             if (j == 1 && io.h2osno_no_layers[c] > 0.0) cv = cv + CPICE * io.h2osno_no_layers[c];
         } else {
             const double liq = LIQ[ssi(j)], ice = ICE[ssi(j)];
-            double b = (ice + liq) / (frac_sno * DZ(j));
+            double b = divf(ice + liq, frac_sno * DZ(j));
             io.bw[ssi(j)] = b;
             if (snow_method == 0) {
                 t = TKAIR + (7.75e-5 * b + 1.105e-6 * b * b) * (TKICE - TKAIR);
@@ -359,13 +359,13 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
         }
         io.thk[ssi(j)] = t;
         double f;
-        if (j == snl + 1) f = dtime / cv * DZ(j) / (0.5 * (Z(j) - ZI(j - 1) + CAPR * (Z(j + 1) - ZI(j - 1))));
-        else f = dtime / cv;
+        if (j == snl + 1) f = divf(divf(dtime, cv) * DZ(j), 0.5 * (Z(j) - ZI(j - 1) + CAPR * (Z(j + 1) - ZI(j - 1))));
+        else f = divf(dtime, cv);
         fact[L(j)] = f;
         io.fact[ssi(j)] = f;
         if (j > snl + 1) {
             const int jm = j - 1;
-            const double tkm = thk_prev * t * (Z(j) - Z(jm)) / (thk_prev * (Z(j) - ZI(jm)) + t * (ZI(jm) - Z(jm)));
+            const double tkm = divf(thk_prev * t * (Z(j) - Z(jm)), thk_prev * (Z(j) - ZI(jm)) + t * (ZI(jm) - Z(jm)));
             tk[L(jm)] = tkm;
             const Recip r = recip(Z(j) - Z(jm));
             rdz[L(jm)] = r.y;
@@ -559,7 +559,7 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
         }
         if (nonzero(W[0][0])) {
             if (km > 0) {
-                const double rp = 1.0 / W[0][0];
+                const double rp = divf(1.0, W[0][0]);
                 W[1][0] = W[1][0] * rp;
                 if (km > 1) W[2][0] = W[2][0] * rp;
 #pragma unroll
@@ -614,7 +614,7 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
 #pragma unroll 1
     for (int j = n; j >= 1; --j) {
         if (nonzero(x[0])) {
-            x[0] = x[0] / S.at(j, 0);
+            x[0] = divf(x[0], S.at(j, 0));
             const double temp = x[0];
 #pragma unroll
             for (int k = 1; k <= 4; ++k)
@@ -729,8 +729,8 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
         } else {
             if (wice0 > 0. && tj > TFRZ) { imelt = 1; tinc = TFRZ - tj; tj = TFRZ; }
             if (tj < TFRZ) {
-                double smp = HFUS * (TFRZ - tj) / (GRAV * tj) * 1000.0;
-                supercool = io.watsat[gi(j)] * fm::pow(smp / io.sucsat[gi(j)], -1.0 / io.bsw[gi(j)]);
+                double smp = divf(HFUS * (TFRZ - tj), GRAV * tj) * 1000.0;
+                supercool = io.watsat[gi(j)] * fm::pow(divf(smp, io.sucsat[gi(j)]), divf(-1.0, io.bsw[gi(j)]));
                 supercool = supercool * DZ(j) * 1000.0;
             }
             if (wliq0 > supercool && tj < TFRZ) { imelt = 2; tinc = TFRZ - tj; tj = TFRZ; }
@@ -742,14 +742,14 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
         double hm = 0.0;
         if (imelt > 0) {
             if (j == snl + 1) {
-                if (j > 0) hm = dhsdT * tinc - tinc / fj;
-                else hm = frac_sno * (dhsdT * tinc - tinc / fj);
+                if (j > 0) hm = dhsdT * tinc - divf(tinc, fj);
+                else hm = frac_sno * (dhsdT * tinc - divf(tinc, fj));
                 if (j == 1 && frac_h2osfc != 0.0) hm = hm - frac_h2osfc * (dhsdT * tinc);
             } else if (j == 1) {
-                hm = (1.0 - frac_sno - frac_h2osfc) * dhsdT * tinc - tinc / fj;
+                hm = (1.0 - frac_sno - frac_h2osfc) * dhsdT * tinc - divf(tinc, fj);
             } else {
-                if (j < 1) hm = -frac_sno * (tinc / fj);
-                else hm = -tinc / fj;
+                if (j < 1) hm = -frac_sno * divf(tinc, fj);
+                else hm = divf(-tinc, fj);
             }
         }
         if (imelt == 1 && hm < 0.0) { hm = 0.0; imelt = 0; }

@@ -148,6 +148,7 @@ def ensemble(nmembers, seed=0, cols=(512, 8192), npatch_max=4, clm5=False):
         A["baseflow_scalar_c"] = np.ascontiguousarray(BASEFLOW_SCALAR * factors["baseflow_scalar"][member_col])
         A["fff_c"] = np.ascontiguousarray(FFF * factors["fff"][member_col])
         A["d_max_c"] = np.ascontiguousarray(D_MAX * factors["d_max"][member_col])
+        A["rootr_col"] = np.zeros((abi.NLEVGRND, A["zwt"].shape[0]))     # written by the root sink
     return A, npatch, ngrid, rootr, member_col, factors
 
 

@@ -286,6 +286,12 @@ def serve(pool, requests, time_limit=None, tick_clock=False, clock=time.perf_cou
         q = running.pop(slot)
         pool.evict(q)
         q.t_done = now()
+        A = q.state
+        if A is not None and "t_soisno" in A:
+            bad = ~(np.isfinite(A["t_soisno"]).all(axis=0) & np.isfinite(A["h2osoi_liq"]).all(axis=0))
+            if "t_veg" in A:
+                bad |= np.bincount(A["patch_column"] - 1, weights=~np.isfinite(A["t_veg"]), minlength=q.ncol) > 0
+            q.extra["nonfinite_columns"] = int(bad.sum())
 
     while nq < len(queue) or running:
         t = now()
@@ -320,6 +326,10 @@ def serve(pool, requests, time_limit=None, tick_clock=False, clock=time.perf_cou
     wall = clock() - t0
     done = [q for q in requests if q.steps_done == q.nsteps]
     per_day = [(q.t_done - q.arrival) / q.days for q in done]
+    # pace of every request that ran: seconds from arrival to its end (or the
+    # time limit) per simulated day it advanced
+    pace = [(q.t_done - q.arrival) / (q.steps_done / STEPS_PER_DAY) for q in requests if q.steps_done > 0]
+    nonfinite = [q.extra.get("nonfinite_columns", 0) for q in requests if q.steps_done > 0]
     wait = [q.t_admit - q.arrival for q in requests if not math.isnan(q.t_admit)]
     steady = None
     if t_all is not None and wall - t_all > 1.0:
@@ -329,7 +339,9 @@ def serve(pool, requests, time_limit=None, tick_clock=False, clock=time.perf_cou
                 requests=len(requests), completed=len(done), stopped=len(requests) - len(done) - (len(queue) - nq),
                 never_admitted=len(queue) - nq, max_running_columns=max_running_cols,
                 p50_s_per_day=percentile(per_day, 50), p99_s_per_day=percentile(per_day, 99),
-                p50_wait_s=percentile(wait, 50), p99_wait_s=percentile(wait, 99))
+                p50_pace_s_per_day=percentile(pace, 50), p99_pace_s_per_day=percentile(pace, 99),
+                p50_wait_s=percentile(wait, 50), p99_wait_s=percentile(wait, 99),
+                nonfinite_requests=int(sum(1 for n in nonfinite if n > 0)), nonfinite_columns=int(sum(nonfinite)))
 
 
 def main(argv=None):

@@ -6,6 +6,9 @@ reference whose path is the one required argument:
   skip_steps.json        src/biogeophys/test/Balance_test/test_Balance.pf:40-105
   quadratic_kat.json     src/utils/test/quadratic_test/test_quadratic.pf
   qsat_coeffs.json       src/biogeophys/QSatMod.F90:16-54
+  pedotransfer.json      src/main/FuncPedotransferMod.F90:28,83-103 (the default
+                         Cosby 1984 table 5) and the organic-soil mixing of
+                         src/biogeophys/SoilStateInitTimeConstMod.F90:200-210,543-602
 
     python tests/golden/make_golden.py <path of the reference checkout>
 """
@@ -88,9 +91,43 @@ def qsat():
     return {"source": "QSatMod.F90 (Flatau et al. 1992 coefficients)", "coeffs": out}
 
 
+def _rhs(line):
+    """Right-hand side of a Fortran assignment, comment stripped, blanks squeezed."""
+    return " ".join(line.split("!")[0].split("=", 1)[1].split())
+
+
+def pedotransfer():
+    """The expressions of the default pedotransfer function and of the
+    organic-soil mixing, as the reference's source lines state them."""
+    ft = read("src/main/FuncPedotransferMod.F90")
+    assert re.search(r"ipedof0\s*=\s*cosby_1984_table5", ft)
+    body = ft[ft.index("subroutine pedotransf_cosby1984_table5"):]
+    body = body[:body.index("end subroutine pedotransf_cosby1984_table5")]
+    t5 = {name: _rhs(next(l for l in body.splitlines() if re.match(r"\s*%s\s*=" % name, l)))
+          for name in ("watsat", "bsw", "sucsat", "xksat")}
+    st = read("src/biogeophys/SoilStateInitTimeConstMod.F90").splitlines()
+    consts = {name: _rhs(next(l for l in st if re.search(r"::\s*%s\s*=" % name, l)).split("::", 1)[1])
+              for name in ("zsapric", "pcalpha", "pcbeta")}
+    org = {name: _rhs(next(l for l in st if re.match(r"\s*%s\s+=\s*m" % name, l)))
+           for name in ("om_watsat", "om_b", "om_sucsat", "om_hksat")}
+
+    def stmt(key, first):
+        i = next(k for k, l in enumerate(st) if key in l and first in l)
+        text = st[i]
+        while text.split("!")[0].rstrip().endswith("&"):
+            i += 1
+            text = text.split("!")[0].rstrip()[:-1] + " " + st[i].strip().lstrip("&")
+        return _rhs(text)
+    return {"source": "FuncPedotransferMod.F90 pedotransf_cosby1984_table5; SoilStateInitTimeConstMod.F90",
+            "table5": t5, "constants": consts, "organic": org,
+            "tkdry": stmt("tkdry_col(c,lev)", "0.135_r8"), "tksatu": stmt("tksatu_col(c,lev)", "0.57_r8"),
+            "bsw": stmt("bsw_col(c,lev)", "bsw_sf"), "watsat": stmt("watsat_col(c,lev)    =", "watsat_sf")}
+
+
 def main():
     for fname, fn in (("layer_table_20sl.json", layer_table), ("skip_steps.json", skip_steps),
-                      ("quadratic_kat.json", quadratic), ("qsat_coeffs.json", qsat)):
+                      ("quadratic_kat.json", quadratic), ("qsat_coeffs.json", qsat),
+                      ("pedotransfer.json", pedotransfer)):
         with open(os.path.join(OUT, fname), "w") as f:
             json.dump(fn(), f, indent=1)
         print("wrote", fname)

@@ -111,3 +111,17 @@ def compare(gpu, ref, fields, tol=1e-9, spread=None):
             errs[k] = max_rel_err(g, r)
     bad = [k for k, v in errs.items() if v > tol]
     return errs, bad
+
+
+def evap_veg_rounding_bound(R, ulps=8):
+    """Absolute error of qflx_evap_veg = rpp * efpot that the rounding of
+    efpot's operands allows: efpot = forc_rho (elai + esai) / rb
+    (wtgaq (qsatl + qsatldT dt_veg) - wtgq0 qg - wtaq0 forc_q)
+    (CanopyFluxesMod.F90:1335-1339) is a difference of humidities the size of
+    the canopy-air humidity qaf, so near saturation its sign is set by
+    rounding: ulps * eps * forc_rho (elai + esai) / rb1 * (|qaf| + |forc_q|),
+    per patch, from the oracle's state R."""
+    eps = np.finfo(np.float64).eps
+    c = R["patch_column"] - 1
+    return ulps * eps * R["forc_rho"][c] * (R["elai"] + R["esai"]) / R["rb1"] * (np.abs(R["qaf"]) +
+                                                                                  np.abs(R["forc_q"][c]))

@@ -1,9 +1,12 @@
-"""The shared-reciprocal quotient of ctsm_gb300/csrc/cr_div.cuh on the device:
-the bits of the device's IEEE division a / b over random and edge-case pairs
-(whole double range, physical magnitudes, all-ones significands, zeros,
-subnormals, infinities, NaN) -- it can differ by one ulp only where a/b lies
-within 2^-103.9 |a/b| of a rounding midpoint -- and __drcp_rn equal to the
-host's correctly rounded 1/b."""
+"""The shared-reciprocal quotient of ctsm_gb300/csrc/cr_div.cuh on the device
+(the special-function unit's reciprocal seed, one Newton step, one
+Newton-Markstein correction) against the device's IEEE division a / b over
+random and edge-case pairs (whole double range, physical magnitudes, all-ones
+significands, zeros, subnormals, infinities, NaN): the same bits except where
+a/b lies within 2^-79 |a/b| of a rounding midpoint, where it may be the other
+neighbour -- so every quotient is within one ulp and almost none differ -- and
+special values exactly as the division.  The reciprocal itself is within
+2^-39.8 of 1/b in the fast range."""
 import numpy as np
 import pytest
 
@@ -39,7 +42,15 @@ def test_device_crdiv_equals_division(gpu_lib):
     check(L.ctsmg_diag_crdiv(n, a.ctypes.data_as(P), b.ctypes.data_as(P), out.ctypes.data_as(P)))
     ieee, crd, rcp = out.reshape(3, n)
     same = (ieee.view(np.uint64) == crd.view(np.uint64)) | (np.isnan(ieee) & np.isnan(crd))
-    assert same.all(), (a[~same][:5], b[~same][:5])
+    ulp = np.abs(ieee.view(np.int64) - crd.view(np.int64))
+    assert (same | (ulp <= 1)).all(), (a[~same][:5], b[~same][:5])
+    assert (~same).sum() <= 4, (~same).sum()
+    ea = (a.view(np.uint64) >> np.uint64(52)) & np.uint64(0x7ff)
+    eb = (b.view(np.uint64) >> np.uint64(52)) & np.uint64(0x7ff)
+    fast = (ea >= 0x201) & (ea <= 0x5fe) & (eb >= 0x201) & (eb <= 0x5fe)
+    special = ~fast
+    assert same[special].all()                                   # outside the fast range: the division itself
     with np.errstate(all="ignore"):
-        host_rcp = 1.0 / b
-    np.testing.assert_array_equal(rcp, host_rcp)
+        exact = 1.0 / b
+    rel = np.abs(rcp[fast] - exact[fast]) / np.abs(exact[fast])
+    assert rel.max() < 2.0 ** -39.8, rel.max()
