@@ -690,8 +690,15 @@ def ours_arm(args, ws, rank, local):
     fp64_line = None
     if flops_cs:
         ach_tf = flops_cs * ncol / mean_launch_s / 1e12
+        # issue slots of the FP64 pipe: the measured DFMA loop issues
+        # peak / 2 FLOP / 32 lanes warp instructions per second
+        ach_wi = roofline.FP64_WARP_INST_PER_COLUMN_STEP * ncol / mean_launch_s
+        peak_wi = fp64.value * 1e12 / 64.0
         fp64_line = {"achieved": ach_tf, "peak": fp64.value, "unit": "TFLOP/s", "frac": ach_tf / fp64.value,
-                     "flops_per_column_step": flops_cs, "peak_source": "measured live (DFMA loop)"}
+                     "flops_per_column_step": flops_cs, "peak_source": "measured live (DFMA loop)",
+                     "issue": {"achieved_warp_inst_per_s": ach_wi, "peak_warp_inst_per_s": peak_wi,
+                               "frac": ach_wi / peak_wi,
+                               "warp_inst_per_column_step": roofline.FP64_WARP_INST_PER_COLUMN_STEP}}
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
             "traffic": roofline.TRAFFIC_PER_COLUMN_STEP * ncol if roofline.TRAFFIC_PER_COLUMN_STEP else None,
             "peak_source": peak_src, "algorithmic_bytes_per_column_step": rd + wr,

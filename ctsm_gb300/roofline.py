@@ -6,19 +6,15 @@ from . import abi
 
 NLEVSNO, NLEVSOI, NLEVGRND = abi.NLEVSNO, abi.NLEVSOI, abi.NLEVGRND
 
-# FP64 floating-point operations per column-step of soilstep_kernel on the
-# uneven-column workload (DADD + DMUL + 2 x DFMA executed, libm included),
-# from the ncu capture of 65,536 columns of the same workload, and DRAM bytes
-# per column-step from the 1-pass capture of the full 524,288-column launch.
-# The capture
-# predates the Zeng-Decker solve's carrying of each interface's flux and
-# derivatives from one level to the next (3 divisions and 9 other FP64
-# operations fewer per level) and the heat system's carrying of each row's
-# tk/dz quotient (one division fewer per row), so this count is a few per
-# cent above the kernel's current one and the FP64 rate derived from it is as
-# much high.
-FLOPS_PER_COLUMN_STEP = (148978105 + 162750456 + 2 * 608026028) / 65536.0
-TRAFFIC_PER_COLUMN_STEP = (6665794560 + 4179119872) / 524288.0
+# Per column-step of soilstep_kernel on the uneven-column workload, from an
+# ncu capture of one launch over 65,536 columns of the same workload (state
+# 420 MB, larger than L2): FP64 FLOPs (DADD + DMUL + 2 x DFMA executed, libm
+# included), FP64-pipe warp instructions (every FP64 instruction one issue
+# slot of the pipe, whatever its lanes) and DRAM bytes read + written.  The
+# full 524,288-column launch is scaled from it by columns.
+FLOPS_PER_COLUMN_STEP = (143180655 + 157036799 + 2 * 399076403) / 65536.0
+FP64_WARP_INST_PER_COLUMN_STEP = 29425746 / 65536.0
+TRAFFIC_PER_COLUMN_STEP = (571910656 + 339028736) / 65536.0
 
 # FP64 floating-point operations per CanopyFluxes pass of one patch
 # (canopy_iterate_kernel: DADD + DMUL + 2 x DFMA executed over 262,144 patches
