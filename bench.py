@@ -395,6 +395,47 @@ def copied_bytes(reset=False):
     return h2d.value, d2h.value
 
 
+def pipe_trace(enable):
+    """Turns the drop-in calls' per-chunk timeline on or off for this thread
+    and returns the last recorded call's marks: one (copy-in start, copy-in
+    end, kernel start, kernel end, copy-out end, host copy-in enqueued, host
+    copy-out enqueued) tuple per chunk, in ms."""
+    import ctypes as C
+    from ctsm_gb300 import _lib
+    L = _lib.load()
+    L.ctsmg_pipe_trace.argtypes = [C.c_int32, C.POINTER(C.c_float), C.c_int32, C.POINTER(C.c_int32)]
+    buf = (C.c_float * (7 * 64))()
+    n = C.c_int32(0)
+    _lib.check(L.ctsmg_pipe_trace(1 if enable else 0, buf, 64, C.byref(n)))
+    return [tuple(buf[7 * k:7 * k + 7]) for k in range(n.value)]
+
+
+def pipeline_summary(marks):
+    """Busy time of the copy-in stream, the kernels and the copy-out stream of
+    one pipelined call, and its span, from its per-chunk marks (ms)."""
+    if not marks:
+        return {"chunks": 0}
+
+    def union(iv):
+        tot, end = 0.0, -1e30
+        for a, b in sorted(iv):
+            if b > end:
+                tot += b - max(a, end)
+                end = b
+        return tot
+    out_iv, prev = [], 0.0
+    for m in marks:                       # a chunk's copy-out starts after its kernel and the previous copy-out
+        a = max(m[3], prev)
+        out_iv.append((a, m[4]))
+        prev = m[4]
+    return {"chunks": len(marks), "span_ms": round(max(m[4] for m in marks), 3),
+            "h2d_busy_ms": round(union([(m[0], m[1]) for m in marks]), 3),
+            "kernel_busy_ms": round(union([(m[2], m[3]) for m in marks]), 3),
+            "d2h_busy_ms": round(union(out_iv), 3),
+            "first_kernel_start_ms": round(marks[0][2], 3), "last_copy_in_end_ms": round(marks[-1][1], 3),
+            "marks_ms": [[round(x, 3) for x in m] for m in marks]}
+
+
 # ---------------------------------------------------------------- arms
 def reference_arm(args, ws, rank):
     """The reference's CPU implementation of the path (the oracle port: the
@@ -587,6 +628,10 @@ def clm5_leg(args, barrier):
     try:
         b = SoilBatch(A, npatch, canopy=True, ngrid=ngrid, soilfluxes=True, rootmoist=True, soilresis=True,
                       hydrology=True)
+        # two steps first, so the tuner's bucketed order sees sub-step counts
+        # of this run rather than the inputs' zeros
+        b.run(2)
+        tuned = b.tune(trial_steps=2)
         b.run(args.warmup)
         b.sync()
         barrier()
@@ -604,7 +649,10 @@ def clm5_leg(args, barrier):
             "columns": ncol, "patches": npatch, "steps": args.clm5_steps, "ms_per_step": mean_ms,
             "column_steps_per_s": ncol / (mean_ms * 1e-3),
             "mean_substeps": float(A["num_substeps"].mean()), "max_substeps": float(A["num_substeps"].max()),
-            "mean_canopy_passes": float(A["num_iter"].mean()), "gpu_launches_per_step": 8}
+            "mean_canopy_passes": float(A["num_iter"].mean()), "gpu_launches_per_step": 8,
+            "tuning": {"block": tuned["block"], "mf_order": tuned["mf_order"],
+                       "ms_per_step": {k: {str(blk): round(v, 3) for blk, v in t.items()}
+                                       for k, t in tuned["ms_per_step"].items()}}}
 
 
 def serving_leg(args):
@@ -653,7 +701,8 @@ def ours_arm(args, ws, rank, local):
     # ---------------- batched resident engine
     G = copy.deepcopy(A)
     batch = SoilBatch(G, npatch, dtime=DT)
-    block = batch.autotune(trial_steps=2)
+    tuned = batch.tune(trial_steps=2)
+    block = tuned["block"]
     batch.run(args.warmup)
     batch.sync()
 
@@ -766,9 +815,20 @@ def ours_arm(args, ws, rank, local):
         barrier()
         te = max_over_ranks(time.perf_counter() - t0, ws, "cuda")
         h2d, d2h = copied_bytes()
+        # one more pair outside the timed region: bytes and the per-chunk
+        # timeline of each call
+        per_call = {}
+        for name, call in (("SoilWater", soil.SoilWater), ("SoilTemperature", soil.SoilTemperature)):
+            copied_bytes(reset=True)
+            pipe_trace(True)
+            call(bnd, ncol, filt, H, DT)
+            marks = pipe_trace(False)
+            bi, bo = copied_bytes()
+            per_call[name] = dict(h2d_bytes=bi, d2h_bytes=bo, **pipeline_summary(marks))
         e2e = {"value": job_value(ws, ncol, ke, te), "unit": UNIT, "h2d_bytes_per_step": h2d // ke,
                "d2h_bytes_per_step": d2h // ke, "steps": ke, "ms_per_step": 1e3 * te / ke,
                "ms_per_call": {"SoilWater": 1e3 * t_sw / ke, "SoilTemperature": 1e3 * t_st / ke},
+               "calls": per_call,
                "path": "ctsmg_soilwater + ctsmg_soiltemperature (plain drop-in, pinned host arrays)"}
 
     # ---------------- CPU baseline (rank 0 only, N = 1 only) when the gate did not time the oracle
@@ -795,7 +855,8 @@ def ours_arm(args, ws, rank, local):
                 "warmup": args.warmup, "ms_per_step": 1e3 * t_rank / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic (seeded Philox draws; no dataset)", "config": cfg,
-                "tuning": {"block": block, "graph": "one CUDA graph per step", "mean_snow_layers": mean_snow},
+                "tuning": {"block": block, "column_order": tuned["order"], "graph": "one CUDA graph per step",
+                           "autotune_ms_per_step": tuned["ms_per_step"], "mean_snow_layers": mean_snow},
                 "parity": gate,
                 "gpu_launches": int(args.steps), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                 "clocks": clk, "wall_s_timed": wall, "fp64_peak_tflops": fp64.value}

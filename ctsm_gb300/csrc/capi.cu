@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <chrono>
 #include <mutex>
 #include <atomic>
 #include <algorithm>
@@ -84,6 +85,15 @@ struct ThreadCtx {
     cudaStream_t h2d = nullptr, d2h = nullptr;      // copy streams of the pipelined calls
     cudaStream_t xs[PIPE_STREAMS - 1] = {};         // further compute streams of a pipelined call
     cudaEvent_t ev_in[PIPE_CHUNKS] = {}, ev_done[PIPE_CHUNKS] = {};
+    // per-chunk timeline of the last pipelined call (ctsmg_pipe_trace):
+    // copy-in start / end, kernel start / end, copy-out end
+    bool trace = false;
+    int trace_n = 0;
+    cudaEvent_t tr[PIPE_CHUNKS][5] = {};
+    // host clock: when the calling thread finished enqueuing each chunk's
+    // copy-in and copy-out, from the first mark
+    std::chrono::steady_clock::time_point tr_t0{};
+    float trh[PIPE_CHUNKS][2] = {};
     char* arena = nullptr;
     size_t arena_cap = 0, arena_top = 0;
     int32_t* order = nullptr;                       // page-locked work order of a call
@@ -98,6 +108,8 @@ struct ThreadCtx {
         for (int k = 0; k < PIPE_CHUNKS; ++k) {
             if (ev_in[k]) cudaEventDestroy(ev_in[k]);
             if (ev_done[k]) cudaEventDestroy(ev_done[k]);
+            for (cudaEvent_t t : tr[k])
+                if (t) cudaEventDestroy(t);
         }
         if (h2d) cudaStreamDestroy(h2d);
         if (d2h) cudaStreamDestroy(d2h);
@@ -195,6 +207,9 @@ int kind_levels(int kind) {
 // rows of a component the drop-in calls copy (FieldDesc::lev0 / nlev)
 static int copy_rows(const FieldDesc& f) { return f.nlev ? f.nlev : kind_levels(f.kind); }
 static size_t copy_row0(const FieldDesc& f) { return f.nlev ? (size_t)f.lev0 : 0; }
+// rows of the copy-in (host to device)
+static int copy_in_rows(const FieldDesc& f) { return f.in_nlev ? f.in_nlev : copy_rows(f); }
+static size_t copy_in_row0(const FieldDesc& f) { return f.in_nlev ? (size_t)f.in_lev0 : copy_row0(f); }
 
 #define FW(S, name, kind, esz, use) {offsetof(S, name), kind, esz, use, #name}
 // Rows of SoilWater's (Zeng-Decker) components: levels 1..nlevsoi of the
@@ -540,6 +555,21 @@ const FieldDesc SOILTEMP_TABLE[] = {
 };
 const int SOILTEMP_NFIELDS = sizeof(SOILTEMP_TABLE) / sizeof(SOILTEMP_TABLE[0]);
 
+// The SoilTemperature table for a filter that covers every column of the
+// bounds: what the heat solve writes on every filtered column is not copied
+// in -- eflx_fgr (levels 1..nlevgrnd), the per-layer melt and freeze fluxes
+// (every snow level), the column outputs -- and of fact, thk and
+// imelt (written on levels snl+1..nlevgrnd) only the snow rows go in.
+static std::vector<FieldDesc> soiltemp_dense_table() {
+    std::vector<FieldDesc> t(SOILTEMP_TABLE, SOILTEMP_TABLE + SOILTEMP_NFIELDS);
+    for (FieldDesc& f : t) {
+        const std::string n = f.name;
+        if (n == "fact" || n == "thk" || n == "imelt") { f.in_lev0 = 0; f.in_nlev = NLEVSNO; }
+        else if (f.use == U_OUT && n != "bw" && f.kind != K_P) f.no_in = 1;
+    }
+    return t;
+}
+
 #define FC(name, kind, esz, use) FW(ctsmg_canopy_io, name, kind, esz, use)
 // Compute_EffecRootFrac_And_VertTranSink_Default: levels 1..nlevsoi of rootr
 // (patches) and of the two column outputs
@@ -770,8 +800,9 @@ size_t field_bytes(const FieldDesc& f, int ldc, int ldp, int ldg) {
 // dimension) reads and writes its own columns alone.
 static cudaError_t copy_field(void* dst, const void* src, const FieldDesc& f, int ld, int n, cudaMemcpyKind k,
                               cudaStream_t s) {
-    const size_t es = f.esize, pitch = (size_t)ld * es, off = copy_row0(f) * pitch;
-    const size_t rows = copy_rows(f);
+    const bool in = k == cudaMemcpyHostToDevice;
+    const size_t es = f.esize, pitch = (size_t)ld * es, off = (in ? copy_in_row0(f) : copy_row0(f)) * pitch;
+    const size_t rows = in ? copy_in_rows(f) : copy_rows(f);
     if (n >= ld) return copy_async(static_cast<char*>(dst) + off, static_cast<const char*>(src) + off, rows * pitch, k, s);
     if (n <= 0) return cudaSuccess;
     return copy_2d_async(static_cast<char*>(dst) + off, pitch, static_cast<const char*>(src) + off, pitch,
@@ -899,10 +930,11 @@ static bool plan_chunks(const ctsmg_bounds* b, int num, const int32_t* filt, con
 static cudaError_t copy_slice(const FieldDesc& f, void* dst, const void* src, int ld, int lo, int hi,
                               cudaMemcpyKind kind, cudaStream_t s) {
     if (hi <= lo) return cudaSuccess;
+    const bool in = kind == cudaMemcpyHostToDevice;
     const size_t es = f.esize, pitch = (size_t)ld * es, w = (size_t)(hi - lo) * es;
-    const size_t off = copy_row0(f) * pitch + lo * es;
+    const size_t off = (in ? copy_in_row0(f) : copy_row0(f)) * pitch + lo * es;
     return copy_2d_async(static_cast<char*>(dst) + off, pitch, static_cast<const char*>(src) + off, pitch,
-                             w, copy_rows(f), kind, s);
+                             w, in ? copy_in_rows(f) : copy_rows(f), kind, s);
 }
 
 static bool patch_field(const FieldDesc& f) { return f.kind == K_P || f.kind == K_PL || f.kind == K_PS || f.kind == K_PG; }
@@ -912,6 +944,19 @@ static void stage_alloc(ThreadCtx* c, const void* hio, void* dio, size_t io_size
                         int ldc, int ldp) {
     std::memcpy(dio, hio, io_size);
     for (int i = 0; i < nf; ++i) field_ptr(dio, tab[i]) = arena_take(c, field_bytes(tab[i], ldc, ldp, 0));
+}
+
+// Timeline mark `slot` of chunk k on stream s when the calling thread traces
+// its pipelined calls (0 copy-in start, 1 copy-in end, 2 kernel start,
+// 3 kernel end, 4 copy-out end).
+static void trace_mark(ThreadCtx* c, int k, int slot, cudaStream_t s) {
+    if (!c->trace || !c->tr[k][slot]) return;
+    cudaEventRecord(c->tr[k][slot], s);
+    const auto now = std::chrono::steady_clock::now();
+    if (k == 0 && slot == 0) c->tr_t0 = now;
+    const float ms = std::chrono::duration<float, std::milli>(now - c->tr_t0).count();
+    if (slot == 1) c->trh[k][0] = ms;
+    if (slot == 4) c->trh[k][1] = ms;
 }
 
 // Enqueue the copy-in of chunk k's components (h2d stream).
@@ -932,8 +977,10 @@ static int chunk_copies_in(ThreadCtx* c, const Chunk& ch, const void* hio, const
 // Enqueue the copy-in of chunk k (h2d stream) and record ev_in[k].
 static int chunk_in(ThreadCtx* c, const Chunk& ch, int k, const void* hio, const void* dio, const FieldDesc* tab,
                     int nf, int ldc, int ldp) {
+    trace_mark(c, k, 0, c->h2d);
     int rc = chunk_copies_in(c, ch, hio, dio, tab, nf, ldc, ldp);
     if (rc) return rc;
+    trace_mark(c, k, 1, c->h2d);
     cudaError_t e = cudaEventRecord(c->ev_in[k], c->h2d);
     return e == cudaSuccess ? 0 : cuda_fail(e, "cudaEventRecord");
 }
@@ -951,6 +998,7 @@ static int chunk_out(ThreadCtx* c, const Chunk& ch, int k, const void* hio, cons
                        pf ? ch.p0 : ch.c0, pf ? ch.p1 : ch.c1, cudaMemcpyDeviceToHost, c->d2h);
         if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy2DAsync D2H");
     }
+    trace_mark(c, k, 4, c->d2h);
     return 0;
 }
 
@@ -1240,15 +1288,18 @@ extern "C" int32_t ctsmg_soilwater(const ctsmg_bounds* bounds, int32_t num_hydro
             const Chunk& ch = chunks[k];
             cudaStream_t ks = chunk_stream(c, k);
             if ((e = cudaStreamWaitEvent(ks, c->ev_in[k], 0)) != cudaSuccess) return cuda_fail(e, "wait");
+            trace_mark(c, k, 2, ks);
             // one lane-refill counter per compute stream (chunks on one stream run in order)
             e = launch_soilwater_call(dio, bounds->begc, ch.f1 - ch.f0, dfilt + ch.f0, nml, e_ice, dtime, c->err,
                                       ks, dcounter + 32 * (k % PIPE_STREAMS));
             if (e != cudaSuccess) return cuda_fail(e, "soilwater kernel launch");
+            trace_mark(c, k, 3, ks);
             if ((e = cudaEventRecord(c->ev_done[k], ks)) != cudaSuccess) return cuda_fail(e, "record");
             if (k + 1 < K && (rc = chunk_in(c, chunks[k + 1], k + 1, io, &dio, T, NT, ldc, 0))) return rc;
             if ((rc = chunk_out(c, ch, k, io, &dio, T, NT, ldc, 0))) return rc;
         }
         if ((e = join_streams(c)) != cudaSuccess) return cuda_fail(e, "soilwater");
+        c->trace_n = c->trace ? K : 0;
     } else {
         ctsmg_soilwater_io dio;
         if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, 0, 0, bounds->endc - bounds->begc + 1, -1))) return rc;
@@ -1290,14 +1341,20 @@ extern "C" int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds, int32_t num
     }
     if (num_nolakec == 0) return 0;
     const int ldc = io->ldc, ldp = io->ldp;
+    // outputs the heat solve writes on every filtered column are not copied
+    // in when the filter is every column of the bounds in order
+    static const std::vector<FieldDesc> dense_tab = soiltemp_dense_table();
+    bool dense = num_nolakec == ncol;
+    for (int i = 0; dense && i < num_nolakec; ++i) dense = filter_nolakec[i] == bounds->begc + i;
+    const FieldDesc* TT = dense ? dense_tab.data() : SOILTEMP_TABLE;
     const size_t ws_bytes = (size_t)SOILTEMP_WS_DOUBLES_PER_COL * num_nolakec * 8;
-    size_t need = table_bytes(SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp) + ws_bytes + (size_t)num_nolakec * 4 + 8192;
+    size_t need = table_bytes(TT, SOILTEMP_NFIELDS, ldc, ldp) + ws_bytes + (size_t)num_nolakec * 4 + 8192;
     if ((rc = arena_reserve(c, need))) return rc;
     std::vector<Chunk> chunks;
     if (plan_chunks(bounds, num_nolakec, filter_nolakec, io->col_patchi, io->col_npatches, soiltemp_wave_columns(),
                     chunks)) {
         ctsmg_soiltemp_io dio;
-        stage_alloc(c, io, &dio, sizeof dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp);
+        stage_alloc(c, io, &dio, sizeof dio, TT, SOILTEMP_NFIELDS, ldc, ldp);
         int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_nolakec * 4);
         double* ws = (double*)arena_take(c, ws_bytes);
         int32_t* hord = order_buffer(c, (size_t)num_nolakec);
@@ -1306,12 +1363,14 @@ extern "C" int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds, int32_t num
         // those copies run), then ev_in[k]
         auto stage_chunk = [&](int k) -> int {
             const Chunk& ch = chunks[k];
-            int r = chunk_copies_in(c, ch, io, &dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp);
+            trace_mark(c, k, 0, c->h2d);
+            int r = chunk_copies_in(c, ch, io, &dio, TT, SOILTEMP_NFIELDS, ldc, ldp);
             if (r) return r;
             group_by_layers(filter_nolakec, ch.f0, ch.f1, io->snl, io->nbedrock, bounds->begc, hord);
             cudaError_t ce = copy_async(dfilt + ch.f0, hord + ch.f0, (size_t)(ch.f1 - ch.f0) * 4,
                                         cudaMemcpyHostToDevice, c->h2d);
             if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemcpyAsync(filter)");
+            trace_mark(c, k, 1, c->h2d);
             ce = cudaEventRecord(c->ev_in[k], c->h2d);
             return ce == cudaSuccess ? 0 : cuda_fail(ce, "cudaEventRecord");
         };
@@ -1327,21 +1386,24 @@ extern "C" int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds, int32_t num
             const Chunk& ch = chunks[k];
             cudaStream_t ks = chunk_stream(c, k);
             if ((e = cudaStreamWaitEvent(ks, c->ev_in[k], 0)) != cudaSuccess) return cuda_fail(e, "wait");
+            trace_mark(c, k, 2, ks);
             e = launch_soiltemp(dio, bounds->begc, bounds->begp, ch.f1 - ch.f0, dfilt + ch.f0, dtime, snow_method,
                                 ws + ch.f0, num_nolakec, c->err, ks);
             if (e != cudaSuccess) return cuda_fail(e, "soiltemperature kernel launch");
+            trace_mark(c, k, 3, ks);
             if ((e = cudaEventRecord(c->ev_done[k], ks)) != cudaSuccess) return cuda_fail(e, "record");
             if (k + 1 < K && (rc = stage_chunk(k + 1))) return rc;
-            if ((rc = chunk_out(c, ch, k, io, &dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp))) return rc;
+            if ((rc = chunk_out(c, ch, k, io, &dio, TT, SOILTEMP_NFIELDS, ldc, ldp))) return rc;
         }
         if ((e = join_streams(c)) != cudaSuccess) return cuda_fail(e, "soiltemperature");
+        c->trace_n = c->trace ? K : 0;
         int code = 0, idx = 0, lev = 0;
         if ((rc = read_error(c, &code, &idx, &lev))) return rc;
         if (code) return set_error(code, "BandDiagonal ERROR: dgbsv returned error code", idx, lev);
         return 0;
     }
     ctsmg_soiltemp_io dio;
-    if ((rc = stage_in(c, io, &dio, sizeof dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp, 0, bounds->endc - bounds->begc + 1, bounds->endp - bounds->begp + 1))) return rc;
+    if ((rc = stage_in(c, io, &dio, sizeof dio, TT, SOILTEMP_NFIELDS, ldc, ldp, 0, bounds->endc - bounds->begc + 1, bounds->endp - bounds->begp + 1))) return rc;
     int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_nolakec * 4);
     double* ws = (double*)arena_take(c, ws_bytes);
     int32_t* hord = order_buffer(c, (size_t)num_nolakec);
@@ -1356,7 +1418,7 @@ extern "C" int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds, int32_t num
     e = launch_soiltemp(dio, bounds->begc, bounds->begp, num_nolakec, dfilt, dtime, snow_method, ws,
                         num_nolakec, c->err, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "soiltemperature kernel launch");
-    if ((rc = stage_out(c, io, &dio, SOILTEMP_TABLE, SOILTEMP_NFIELDS, ldc, ldp, 0, bounds->endc - bounds->begc + 1, bounds->endp - bounds->begp + 1))) return rc;
+    if ((rc = stage_out(c, io, &dio, TT, SOILTEMP_NFIELDS, ldc, ldp, 0, bounds->endc - bounds->begc + 1, bounds->endp - bounds->begp + 1))) return rc;
     e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "soiltemperature");
     int code = 0, idx = 0, lev = 0;
@@ -1771,6 +1833,40 @@ extern "C" int32_t ctsmg_water_table(const ctsmg_bounds* b, int32_t n, const int
 extern "C" int32_t ctsmg_drainage(const ctsmg_bounds* b, int32_t n, const int32_t* f, const ctsmg_hydrology_io* io,
                                   double dtime) {
     return hydrology_call(b, n, f, io, dtime, HYD_DRAINAGE, HYD_DR_TABLE, HYD_DR_TABLE_N);
+}
+
+// Per-chunk timeline of the calling thread's pipelined drop-in calls.
+extern "C" int32_t ctsmg_pipe_trace(int32_t enable, float* ms_out, int32_t max_chunks, int32_t* nchunks_out) {
+    ThreadCtx* c;
+    int rc = ctx_get(&c);
+    if (rc) return rc;
+    if (ms_out && nchunks_out) {
+        const int n = std::min(c->trace_n, (int)std::max(max_chunks, 0));
+        for (int k = 0; k < n; ++k) {
+            for (int j = 0; j < 5; ++j) {
+                float ms = 0.f;
+                cudaError_t e = cudaEventElapsedTime(&ms, c->tr[0][0], c->tr[k][j]);
+                if (e != cudaSuccess) return cuda_fail(e, "cudaEventElapsedTime(trace)");
+                ms_out[k * 7 + j] = ms;
+            }
+            ms_out[k * 7 + 5] = c->trh[k][0];
+            ms_out[k * 7 + 6] = c->trh[k][1];
+        }
+        *nchunks_out = n;
+    } else if (nchunks_out) {
+        *nchunks_out = c->trace_n;
+    }
+    if (enable >= 0) {
+        if (enable && !c->tr[0][0])
+            for (int k = 0; k < PIPE_CHUNKS; ++k)
+                for (cudaEvent_t& t : c->tr[k]) {
+                    cudaError_t e = cudaEventCreate(&t);
+                    if (e != cudaSuccess) return cuda_fail(e, "cudaEventCreate(trace)");
+                }
+        c->trace = enable != 0;
+        c->trace_n = 0;
+    }
+    return 0;
 }
 
 extern "C" int32_t ctsmg_copy_bytes(int64_t* h2d, int64_t* d2h, int32_t reset) {

@@ -13,6 +13,9 @@ enum Use { U_IN, U_OUT, U_INOUT };
 struct FieldDesc {
     size_t offset; int kind; int esize; int use; const char* name;
     int lev0 = 0, nlev = 0, no_in = 0;
+    // rows copied in when they differ from the rows copied out (in_nlev > 0):
+    // an output the call writes on some rows only needs the others copied in
+    int in_lev0 = 0, in_nlev = 0;
 };
 
 extern const FieldDesc SOILWATER_TABLE[];

@@ -51,9 +51,15 @@ struct Batch {
     double* mslope = nullptr;
     double* mint = nullptr;
     int* counter = nullptr;
-    int* mf_counter = nullptr;     // work counter of the persistent moisture-form kernel
+    int* mf_work = nullptr;        // work counter and work order of the persistent moisture-form kernel
+    bool mf_sort = false;          // its columns bucketed by previous sub-steps and bedrock depth
     double* cws = nullptr;         // CanopyFluxes iteration records
     int32_t* d_perm = nullptr;     // sorted position -> original column index (0-based)
+    std::vector<int32_t> h_perm;   // host copy of d_perm
+    // the keys the column orders sort by, in the caller's column order
+    std::vector<int32_t> key_snl, key_nbedrock;
+    std::vector<double> key_zwt;
+    int order_key = 0;             // the column order in force (COLUMN_ORDERS)
     double* ws = nullptr;
     DevError* err = nullptr;
     void* snapshot = nullptr;
@@ -110,7 +116,7 @@ static cudaError_t enqueue_step(Batch* b) {
     auto water_step = [&](int refresh) {
         if (mf)
             return launch_mf_step(b->dsw, ncol, b->mfa, b->swm.use_flexibleCN, refresh, b->err, nullptr, b->stream,
-                                  b->mf_counter, hy);
+                                  b->mf_work, hy, b->mf_sort);
         return launch_zd09_step(b->dsw, ncol, b->cfg.e_ice, b->cfg.dtime, b->swm.use_flexibleCN, refresh, nullptr,
                                 b->stream, hy);
     };
@@ -150,7 +156,7 @@ static void batch_free(Batch* b) {
     for (auto& f : b->fields) if (f.dptr) cudaFree(f.dptr);
     for (void* p : {(void*)b->d_perm, (void*)b->ws, (void*)b->err, b->snapshot, (void*)b->rootr, (void*)b->mslope,
                     (void*)b->mint, (void*)b->counter, (void*)b->cws, b->bal_mem, (void*)b->hyd_params, (void*)b->dmax_c,
-                    (void*)b->mf_counter})
+                    (void*)b->mf_work})
         if (p) cudaFree(p);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
@@ -174,6 +180,40 @@ static bool is_column_kind(int k) { return !(k == K_P || k == K_PL || k == K_PS 
 using namespace ctsmg;
 
 struct ctsmg_batch_s { Batch* b; };
+
+namespace ctsmg {
+// Column orders the batch can hold its columns in (position -> caller's
+// column): sorted by snow layers, bedrock depth and water-table depth in the
+// three priorities below, or the caller's own order.  A warp's lanes hold 32
+// consecutive positions, so the order decides how uniform their level loops
+// and branches are.
+constexpr int N_COLUMN_ORDERS = 4;
+static const char* const COLUMN_ORDER_NAMES[N_COLUMN_ORDERS] = {
+    "snl,nbedrock,zwt", "snl,zwt,nbedrock", "nbedrock,snl,zwt", "caller"};
+
+static std::vector<int32_t> column_order(int key, const std::vector<int32_t>& snl, const std::vector<int32_t>& nb,
+                                         const std::vector<double>& zwt) {
+    const int n = (int)snl.size();
+    std::vector<int32_t> perm(n);
+    std::iota(perm.begin(), perm.end(), 0);
+    auto by = [&](auto first, auto second, auto third) {
+        std::stable_sort(perm.begin(), perm.end(), [&](int a, int c) {
+            if (first(a) != first(c)) return first(a) < first(c);
+            if (second(a) != second(c)) return second(a) < second(c);
+            return third(a) < third(c);
+        });
+    };
+    auto S = [&](int i) { return (double)snl[i]; };
+    auto N = [&](int i) { return (double)nb[i]; };
+    auto Z = [&](int i) { return zwt[i]; };
+    if (key == 0) by(S, N, Z);
+    else if (key == 1) by(S, Z, N);
+    else if (key == 2) by(N, S, Z);
+    return perm;
+}
+} // namespace ctsmg
+
+
 
 extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* cfg, const ctsmg_batch_inputs* in) {
     if (!in) return set_error(CTSMG_E_ARG, "null inputs", 0, 0);
@@ -267,12 +307,14 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
     // in which threads take columns changes
     std::vector<int32_t> perm(ncol), inv(ncol);
     std::iota(perm.begin(), perm.end(), 0);
-    if (cfg->bucket && !canopy_only)
-        std::stable_sort(perm.begin(), perm.end(), [&](int a, int c) {
-            if (st->snl[a] != st->snl[c]) return st->snl[a] < st->snl[c];
-            if (st->nbedrock[a] != st->nbedrock[c]) return st->nbedrock[a] < st->nbedrock[c];
-            return sw->zwt[a] < sw->zwt[c];
-        });
+    if (!canopy_only) {
+        b->key_snl.assign(st->snl, st->snl + ncol);
+        b->key_nbedrock.assign(st->nbedrock, st->nbedrock + ncol);
+        b->key_zwt.assign(sw->zwt, sw->zwt + ncol);
+        b->order_key = cfg->bucket ? 0 : 3;
+        perm = column_order(b->order_key, b->key_snl, b->key_nbedrock, b->key_zwt);
+    }
+    b->h_perm = perm;
     for (int i = 0; i < ncol; ++i) inv[perm[i]] = i;
     if ((e = cudaMalloc(&b->d_perm, (size_t)ncol * 4)) != cudaSuccess) return fail(cuda_err(e, "perm"));
     if ((e = cudaMemcpy(b->d_perm, perm.data(), (size_t)ncol * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
@@ -436,8 +478,8 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
             b->bal.th2osfc_bef = const_cast<double*>(b->dsf.t_h2osfc_bef);
         }
     }
-    if (swm.soilwater_movement_method == 1 && (e = cudaMalloc(&b->mf_counter, 256)) != cudaSuccess)
-        return fail(cuda_err(e, "moisture-form counter"));
+    if (swm.soilwater_movement_method == 1 && (e = cudaMalloc(&b->mf_work, mf_work_bytes(ncol))) != cudaSuccess)
+        return fail(cuda_err(e, "moisture-form work order"));
     for (auto& f : b->fields) b->state_bytes += f.bytes;
     if ((e = cudaMalloc(&b->ws, (size_t)SOILTEMP_WS_DOUBLES_PER_COL * ncol * 8)) != cudaSuccess) return fail(cuda_err(e, "ws"));
     if ((e = cudaMalloc(&b->err, sizeof(DevError))) != cudaSuccess) return fail(cuda_err(e, "err"));
@@ -659,6 +701,135 @@ extern "C" int32_t ctsmg_batch_autotune(ctsmg_batch bh, int32_t trial_steps, int
     if (rc) return rc;
     if (block_out) *block_out = best;
     return 0;
+}
+
+// Moves every resident column component (and the per-column parameter
+// buffers) to the column order `key`: a gather on the device from the order
+// in force.  Only for batches without patches of their own in the step
+// (no CanopyFluxes): patch arrays are indexed through col_patchi, which moves
+// with its column.
+static int reorder_columns(Batch* b, int key) {
+    if (key == b->order_key) return 0;
+    const int ncol = b->cfg.ncol;
+    const std::vector<int32_t> np = column_order(key, b->key_snl, b->key_nbedrock, b->key_zwt);
+    std::vector<int32_t> inv(ncol), g(ncol);
+    for (int i = 0; i < ncol; ++i) inv[b->h_perm[i]] = i;
+    for (int i = 0; i < ncol; ++i) g[i] = inv[np[i]];        // new position i <- current position g[i]
+    size_t maxb = 8 * (size_t)ncol;
+    for (auto& f : b->fields) maxb = std::max(maxb, f.bytes);
+    int32_t* dg = nullptr;
+    void* tmp = nullptr;
+    cudaError_t e = cudaMalloc(&dg, (size_t)ncol * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&tmp, maxb);
+    if (e == cudaSuccess) e = cudaMemcpy(dg, g.data(), (size_t)ncol * 4, cudaMemcpyHostToDevice);
+    auto move = [&](void* p, int nlev, int esize, size_t bytes) {
+        if (e == cudaSuccess) e = launch_permute(tmp, p, dg, ncol, nlev, esize, 0, b->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(p, tmp, bytes, cudaMemcpyDeviceToDevice, b->stream);
+    };
+    for (auto& f : b->fields)
+        if (is_column_kind(f.kind)) move(f.dptr, kind_levels(f.kind), f.esize, f.bytes);
+    if (b->hyd_params) {
+        if (b->hya.baseflow_scalar_c) move(b->hyd_params, 1, 8, (size_t)ncol * 8);
+        if (b->hya.fff_c) move(b->hyd_params + ncol, 1, 8, (size_t)ncol * 8);
+    }
+    if (b->dmax_c) move(b->dmax_c, 1, 8, (size_t)ncol * 8);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_perm, np.data(), (size_t)ncol * 4, cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (dg) cudaFree(dg);
+    if (tmp) cudaFree(tmp);
+    if (e != cudaSuccess) return cuda_err(e, "column reorder");
+    b->h_perm = np;
+    b->order_key = key;
+    return 0;
+}
+
+// Times trial_steps steps for every (column order, moisture-form work order,
+// threads per block) candidate on the batch's own data and keeps the fastest;
+// the state is restored (in the chosen column order) afterwards.  Column
+// orders are tuned for batches without CanopyFluxes; the moisture-form work
+// order (bucketed or filter order) for batches with the moisture form.
+extern "C" int32_t ctsmg_batch_autotune2(ctsmg_batch bh, int32_t trial_steps, int32_t* block_out,
+                                         int32_t* order_out, int32_t* mf_sort_out, float* ms_out,
+                                         int32_t* ncand_out) {
+    if (!bh) return set_error(CTSMG_E_ARG, "null batch", 0, 0);
+    Batch* b = bh->b;
+    if (trial_steps < 1) trial_steps = 1;
+    const bool orders = !b->cfg.with_canopy && !b->key_snl.empty();
+    const int norders = orders ? N_COLUMN_ORDERS : 1;
+    const bool mf = b->mf_work != nullptr;
+    const int nmf = mf ? 2 : 1;
+    const int cands[3] = {64, 128, 256};
+    const int key0 = b->order_key;
+    const bool sort0 = b->mf_sort;
+    if (!b->snapshot) CK(cudaMalloc(&b->snapshot, b->state_bytes), "snapshot");
+    auto copy_state = [&](bool save) -> int {
+        size_t off = 0;
+        for (auto& f : b->fields) {
+            void* snap = (char*)b->snapshot + off;
+            CK(cudaMemcpyAsync(save ? snap : f.dptr, save ? f.dptr : snap, f.bytes, cudaMemcpyDeviceToDevice,
+                               b->stream), "snapshot");
+            off += f.bytes;
+        }
+        return 0;
+    };
+    int rc = 0;
+    int best_block = b->block, best_key = key0;
+    bool best_sort = sort0;
+    float best_ms = 1e30f;
+    for (int o = 0; o < norders; ++o) {
+        const int key = orders ? o : key0;
+        // the snapshot is taken in the candidate's column order, restored
+        // after each timing, and the columns go back to the order in force
+        if ((rc = reorder_columns(b, key)) || (rc = copy_state(true))) return rc;
+        for (int m = 0; m < nmf; ++m) {
+            b->mf_sort = mf ? (m == 0) : sort0;
+            for (int k = 0; k < 3; ++k) {
+                b->block = cands[k];
+                if ((rc = build_graph(b))) return rc;
+                CK(cudaGraphLaunch(b->graph, b->stream), "warm");
+                CK(cudaEventRecord(b->ev0, b->stream), "ev");
+                for (int st = 0; st < trial_steps; ++st) CK(cudaGraphLaunch(b->graph, b->stream), "trial");
+                CK(cudaEventRecord(b->ev1, b->stream), "ev");
+                CK(cudaEventSynchronize(b->ev1), "ev sync");
+                float ms;
+                CK(cudaEventElapsedTime(&ms, b->ev0, b->ev1), "elapsed");
+                ms /= trial_steps;
+                if (ms_out) ms_out[(o * nmf + m) * 3 + k] = ms;
+                if (ms < best_ms) { best_ms = ms; best_block = cands[k]; best_key = key; best_sort = b->mf_sort; }
+            }
+            if ((rc = copy_state(false))) return rc;
+        }
+        if ((rc = reorder_columns(b, key0))) return rc;
+    }
+    CK(cudaMemsetAsync(b->err, 0xff, sizeof(DevError), b->stream), "err reset");
+    if (b->cfg.balance) {
+        const int ncol = b->cfg.ncol;
+        const size_t ssb = (size_t)ncol * (NLEVSNO + NLEVGRND) * 8, cb = (size_t)ncol * 8;
+        CK(cudaMemsetAsync(b->bal_mem, 0, ssb + 6 * cb + 256, b->stream), "balance reset");
+    }
+    CK(cudaStreamSynchronize(b->stream), "sync");
+    cudaFree(b->snapshot);
+    b->snapshot = nullptr;
+    if ((rc = reorder_columns(b, best_key))) return rc;
+    b->block = best_block;
+    b->mf_sort = best_sort;
+    if ((rc = build_graph(b))) return rc;
+    if (block_out) *block_out = best_block;
+    if (order_out) *order_out = best_key;
+    if (mf_sort_out) *mf_sort_out = mf ? (best_sort ? 1 : 0) : -1;
+    if (ncand_out) *ncand_out = norders * nmf * 3;
+    return 0;
+}
+
+extern "C" const char* ctsmg_batch_order_name(int32_t key) {
+    return (key >= 0 && key < N_COLUMN_ORDERS) ? COLUMN_ORDER_NAMES[key] : "";
+}
+
+extern "C" int32_t ctsmg_batch_set_mf_order(ctsmg_batch bh, int32_t sorted) {
+    if (!bh || (sorted != 0 && sorted != 1)) return set_error(CTSMG_E_ARG, "sorted must be 0 or 1", 0, 0);
+    if (!bh->b->mf_work) return set_error(CTSMG_E_ARG, "the batch has no moisture form", 0, 0);
+    bh->b->mf_sort = sorted == 1;
+    return build_graph(bh->b);
 }
 
 extern "C" int32_t ctsmg_batch_set_block(ctsmg_batch bh, int32_t block) {

@@ -374,25 +374,118 @@ __device__ __forceinline__ ctsmg_soilhydrology_params column_params(const HydroS
     return hp;
 }
 
-template <bool HYDRO>
+struct MfOrder {
+    int* hist;      // [MF_NKEY] positions per bucket
+    int* fill;      // [MF_NKEY] positions handed out per bucket
+    int* key;       // [ncol] bucket of each position
+    int* order;     // [ncol] positions in bucket order
+};
+
+__host__ __device__ __forceinline__ MfOrder mf_order_of(int* w, int ncol) {
+    return MfOrder{w + 32, w + 32 + MF_NKEY, w + MF_WORK_HEAD, w + MF_WORK_HEAD + ncol};
+}
+
+// Bucket of a column: sub-step class of the previous step (a count that is
+// not a number, or 0 before the first step, counts as 1), then bedrock depth,
+// both descending.
+__device__ __forceinline__ int mf_key(double nsub_prev, int nl) {
+    int cls = 0;
+    if (nsub_prev > 1.5) cls = 1;
+    if (nsub_prev > 2.5) cls = 2;
+    if (nsub_prev > 4.5) cls = 3;
+    if (nsub_prev > 8.5) cls = 4;
+    if (nsub_prev > 16.5) cls = 5;
+    nl = nl < 1 ? 1 : (nl > NLEVSOI ? NLEVSOI : nl);
+    return (MF_NCLS - 1 - cls) * NLEVSOI + (NLEVSOI - nl);
+}
+
+template <bool HYDRO, bool SORT>
 __global__ void __launch_bounds__(128)
-mf_pre_kernel(ctsmg_soilwater_io io, int ncol, double dtime, const int32_t* __restrict__ filt, HydroStepArgs hy) {
-    const int fc = blockIdx.x * blockDim.x + threadIdx.x;
-    if (fc >= ncol) return;
-    const int c = filt ? filt[fc] - 1 : fc;
-    set_soil_water_fractions(io, c);
-    if (HYDRO) {
-        const ctsmg_soilhydrology_params hp = column_params(hy, c);
-        hydro::saturated_excess_runoff(hy.io, c, hp.fff);
-        hydro::infiltration_chain(hy.io, c, hp, dtime);
+mf_pre_kernel(ctsmg_soilwater_io io, int ncol, double dtime, const int32_t* __restrict__ filt, HydroStepArgs hy,
+              int* work) {
+    __shared__ int bh[SORT ? MF_NKEY : 1];
+    if (SORT) {
+        for (int i = threadIdx.x; i < MF_NKEY; i += blockDim.x) bh[i] = 0;
+        __syncthreads();
     }
+    const int fc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fc < ncol) {
+        const int c = filt ? filt[fc] - 1 : fc;
+        set_soil_water_fractions(io, c);
+        if (HYDRO) {
+            const ctsmg_soilhydrology_params hp = column_params(hy, c);
+            hydro::saturated_excess_runoff(hy.io, c, hp.fff);
+            hydro::infiltration_chain(hy.io, c, hp, dtime);
+        }
+        if (SORT) {
+            const int k = mf_key(io.num_substeps[c], io.nbedrock[c]);
+            mf_order_of(work, ncol).key[fc] = k;
+            atomicAdd(&bh[k], 1);
+        }
+    }
+    if (SORT) {
+        __syncthreads();
+        int* hist = mf_order_of(work, ncol).hist;
+        for (int i = threadIdx.x; i < MF_NKEY; i += blockDim.x)
+            if (bh[i]) atomicAdd(&hist[i], bh[i]);
+    }
+}
+
+// Scatter of the filter positions into bucket order: a block ranks its own
+// positions within each bucket in shared memory and takes one run of slots
+// per bucket from the bucket's fill counter.  (The order within a bucket
+// depends on block timing; every column's result is independent of it.)
+__global__ void __launch_bounds__(128) mf_order_kernel(int ncol, int* work) {
+    __shared__ int bh[MF_NKEY], start[MF_NKEY];
+    const MfOrder O = mf_order_of(work, ncol);
+    for (int i = threadIdx.x; i < MF_NKEY; i += blockDim.x) bh[i] = 0;
+    if (threadIdx.x < 32) {             // exclusive prefix sum of the histogram by warp 0
+        constexpr int PER = (MF_NKEY + 31) / 32;
+        const int lane = threadIdx.x;
+        int v[PER], sum = 0;
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int i = lane * PER + q;
+            v[q] = i < MF_NKEY ? O.hist[i] : 0;
+            sum += v[q];
+        }
+        int inc = sum;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, inc, off);
+            if (lane >= off) inc += t;
+        }
+        int run = inc - sum;
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int i = lane * PER + q;
+            if (i < MF_NKEY) start[i] = run;
+            run += v[q];
+        }
+    }
+    __syncthreads();
+    const int fc = blockIdx.x * blockDim.x + threadIdx.x;
+    int k = 0, r = 0;
+    if (fc < ncol) {
+        k = O.key[fc];
+        r = atomicAdd(&bh[k], 1);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < MF_NKEY; i += blockDim.x)
+        if (bh[i]) start[i] += atomicAdd(&O.fill[i], bh[i]);
+    __syncthreads();
+    if (fc < ncol) O.order[start[k] + r] = fc;
 }
 
 template <bool EXPENSIVE>
 __global__ void __launch_bounds__(128)
 mf_core_kernel(ctsmg_soilwater_io io, int ncol, MoistureFormArgs P, DevError* err, const int32_t* __restrict__ filt,
-               int* counter) {
-    mf_persistent<EXPENSIVE>(io, ncol, counter, P, [&](int fc) { return filt ? filt[fc] - 1 : fc; },
+               int* counter, const int* __restrict__ order) {
+    mf_persistent<EXPENSIVE>(io, ncol, counter, P,
+                  [&](int fc) {
+                      const int p = order ? order[fc] : fc;
+                      return filt ? filt[p] - 1 : p;
+                  },
                   [&](int fc, int c, int st, int info) {
                       if (st == MF_SINGULAR) report_error(err, c + 1, info, CTSMG_E_SINGULAR);
                       else if (st == MF_NOT_DONE) report_error(err, c + 1, 0, CTSMG_E_TIMEOUT);
@@ -430,21 +523,29 @@ static int persistent_blocks(K kernel, int n) {
 }
 
 cudaError_t launch_mf_step(const ctsmg_soilwater_io& io, int ncol, const MoistureFormArgs& P, int flexcn, int refresh,
-                           DevError* err, const int32_t* d_filt, cudaStream_t s, int* d_counter,
-                           const HydroStepArgs* hy) {
+                           DevError* err, const int32_t* d_filt, cudaStream_t s, int* d_work,
+                           const HydroStepArgs* hy, bool sorted) {
     if (ncol <= 0) return cudaSuccess;
     const int nb = (ncol + 127) / 128;
     const HydroStepArgs none{};
-    if (hy) mf_pre_kernel<true><<<nb, 128, 0, s>>>(io, ncol, P.dtime, d_filt, *hy);
-    else mf_pre_kernel<false><<<nb, 128, 0, s>>>(io, ncol, P.dtime, d_filt, none);
-    cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(int), s);
+    cudaError_t e = cudaMemsetAsync(d_work, 0, (sorted ? MF_WORK_HEAD : 1) * sizeof(int), s);
     if (e != cudaSuccess) return e;
+    const HydroStepArgs& ha = hy ? *hy : none;
+    if (hy && sorted) mf_pre_kernel<true, true><<<nb, 128, 0, s>>>(io, ncol, P.dtime, d_filt, ha, d_work);
+    else if (hy) mf_pre_kernel<true, false><<<nb, 128, 0, s>>>(io, ncol, P.dtime, d_filt, ha, d_work);
+    else if (sorted) mf_pre_kernel<false, true><<<nb, 128, 0, s>>>(io, ncol, P.dtime, d_filt, ha, d_work);
+    else mf_pre_kernel<false, false><<<nb, 128, 0, s>>>(io, ncol, P.dtime, d_filt, ha, d_work);
+    const int* order = nullptr;
+    if (sorted) {
+        mf_order_kernel<<<nb, 128, 0, s>>>(ncol, d_work);
+        order = mf_order_of(d_work, ncol).order;
+    }
     if (P.expensive)
         mf_core_kernel<true><<<persistent_blocks(mf_core_kernel<true>, ncol), 128, 0, s>>>(io, ncol, P, err, d_filt,
-                                                                                          d_counter);
+                                                                                          d_work, order);
     else
         mf_core_kernel<false><<<persistent_blocks(mf_core_kernel<false>, ncol), 128, 0, s>>>(io, ncol, P, err, d_filt,
-                                                                                            d_counter);
+                                                                                            d_work, order);
     if (hy) mf_post_kernel<true><<<nb, 128, 0, s>>>(io, ncol, P.dtime, flexcn, refresh, d_filt, *hy);
     else if (flexcn || refresh) mf_post_kernel<false><<<nb, 128, 0, s>>>(io, ncol, P.dtime, flexcn, refresh, d_filt, none);
     return cudaGetLastError();

@@ -37,12 +37,26 @@ struct HydroStepArgs {
     const double* fff_c;
 };
 
+// The resident step's work order for the persistent sub-step kernel: every
+// step the filter positions are bucketed by the sub-step count their column
+// took the step before (1, 2, 3-4, 5-8, 9-16, more) and by its bedrock depth
+// (the length of each trial's level loops), both descending, so the lanes of
+// a warp run level loops of one length, finish their sub-step loops together
+// and the longest columns start first.  The scratch holds the work counter,
+// the bucket histogram and fill counters, each position's bucket and the
+// order itself.
+constexpr int MF_NCLS = 6;
+constexpr int MF_NKEY = MF_NCLS * NLEVSOI;
+constexpr int MF_WORK_HEAD = 32 + 2 * MF_NKEY;       // ints before the per-position arrays
+inline size_t mf_work_bytes(int ncol) { return ((size_t)MF_WORK_HEAD + 2 * (size_t)(ncol > 0 ? ncol : 0)) * sizeof(int); }
+
 // Resident-step form over positions 0..ncol-1 (or the 1-based position
 // filter); hy = NULL leaves the hydrology out.
-// d_counter: one int of device scratch (the persistent kernel's work counter).
+// d_work: device scratch, one int (the persistent kernel's work counter) or,
+// with sorted, mf_work_bytes(ncol) for the bucketed work order.
 cudaError_t launch_mf_step(const ctsmg_soilwater_io& io, int ncol, const MoistureFormArgs& P, int flexcn, int refresh,
-                           DevError* err, const int32_t* d_filt, cudaStream_t s, int* d_counter,
-                           const HydroStepArgs* hy = nullptr);
+                           DevError* err, const int32_t* d_filt, cudaStream_t s, int* d_work,
+                           const HydroStepArgs* hy = nullptr, bool sorted = false);
 cudaError_t launch_set_soil_water_fractions(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt,
                                             cudaStream_t s);
 cudaError_t launch_flexcn(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt, cudaStream_t s);

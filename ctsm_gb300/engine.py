@@ -185,8 +185,41 @@ class SoilBatch:
         check(self.L.ctsmg_batch_autotune(self.h, trial_steps, C.byref(b)))
         return b.value
 
+    def tune(self, trial_steps=2):
+        """ctsmg_batch_autotune2: the fastest (column order, moisture-form
+        work order, threads per block) on the batch's own data.  Returns
+        {"block", "order", "mf_order", "ms_per_step": {candidate name:
+        {block: ms}}}; mf_order is "sub-steps,bedrock", "positions" or None
+        (no moisture form), and a candidate name is the column order's, with
+        the work order after a slash for a moisture-form batch."""
+        L = self.L
+        L.ctsmg_batch_autotune2.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                            C.POINTER(C.c_int32), C.POINTER(C.c_float), C.POINTER(C.c_int32)]
+        L.ctsmg_batch_order_name.restype = C.c_char_p
+        b, o, m, n = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+        ms = (C.c_float * 24)()
+        check(L.ctsmg_batch_autotune2(self.h, trial_steps, C.byref(b), C.byref(o), C.byref(m), ms, C.byref(n)))
+        mf_names = ("sub-steps,bedrock", "positions")
+        nmf = 2 if m.value >= 0 else 1
+        norders = n.value // (3 * nmf)
+        table = {}
+        for i in range(norders):
+            oname = L.ctsmg_batch_order_name(i if norders > 1 else o.value).decode()
+            for j in range(nmf):
+                name = oname + ("/" + mf_names[j] if nmf == 2 else "")
+                table[name] = {blk: float(ms[(i * nmf + j) * 3 + k]) for k, blk in enumerate((64, 128, 256))}
+        return {"block": b.value, "order": L.ctsmg_batch_order_name(o.value).decode(),
+                "mf_order": (mf_names[0] if m.value == 1 else mf_names[1]) if m.value >= 0 else None,
+                "ms_per_step": table}
+
     def set_block(self, block):
         check(self.L.ctsmg_batch_set_block(self.h, block))
+
+    def set_mf_order(self, sorted_):
+        """ctsmg_batch_set_mf_order: True buckets the moisture-form columns by
+        the previous step's sub-step count and bedrock depth, False takes
+        them in position order."""
+        check(self.L.ctsmg_batch_set_mf_order(self.h, 1 if sorted_ else 0))
 
     def save(self, path):
         """ctsmg_batch_save: write the resident state to a checkpoint file."""

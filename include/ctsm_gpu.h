@@ -847,6 +847,32 @@ int32_t ctsmg_batch_balance(ctsmg_batch b, double* errh2o_max, double* errsoi_ma
 /* Time trial_steps steps for each candidate threads-per-block (64, 128, 256)
  * on the batch's own data, keep the fastest, restore the state. */
 int32_t ctsmg_batch_autotune(ctsmg_batch b, int32_t trial_steps, int32_t* block_out);
+/* Autotuner over (column order, moisture-form work order, threads per
+ * block).  The batch holds its columns in one of four orders -- sorted by
+ * (snl, nbedrock, zwt), by (snl, zwt, nbedrock), by (nbedrock, snl, zwt), or
+ * the caller's order -- which decides how uniform the level loops and
+ * branches of a warp's 32 lanes are.  With the moisture form, its persistent
+ * sub-step kernel takes the columns either bucketed by the sub-step count of
+ * the previous step and the bedrock depth (rebuilt on the device every step)
+ * or in position order.  Every candidate is timed at 64, 128 and 256 threads
+ * per block over trial_steps steps of the batch's own data, the fastest is
+ * kept (the resident columns are moved into its order on the device) and the
+ * state restored.  Column orders are tuned for batches without CanopyFluxes
+ * (with it, the column order in force is kept).  ms_out (NULL or 24 floats)
+ * receives the milliseconds per step of every candidate, indexed
+ * (order * n_mf + mf) * 3 + block, n_mf = 2 with the moisture form (mf 0 the
+ * bucketed work order) else 1; order_out the chosen column order (0..3,
+ * ctsmg_batch_order_name names it), mf_sort_out 1 / 0 for the chosen work
+ * order (-1 without the moisture form), ncand_out the candidates timed.
+ * No reference counterpart: the reference runs its clump loop in one fixed
+ * order (src/main/clm_driver.F90:525).                                    */
+int32_t ctsmg_batch_autotune2(ctsmg_batch b, int32_t trial_steps, int32_t* block_out, int32_t* order_out,
+                              int32_t* mf_sort_out, float* ms_out, int32_t* ncand_out);
+const char* ctsmg_batch_order_name(int32_t order);
+/* The moisture-form work order of a batch with the moisture form: 1 buckets
+ * the columns by the previous step's sub-step count and bedrock depth, 0
+ * takes them in position order (the default).  Results do not depend on it. */
+int32_t ctsmg_batch_set_mf_order(ctsmg_batch b, int32_t sorted);
 int32_t ctsmg_batch_set_block(ctsmg_batch b, int32_t block);
 int64_t ctsmg_batch_state_bytes(ctsmg_batch b);
 /* Checkpoint / restart of a batch's resident state (the restart role of
@@ -930,6 +956,16 @@ int32_t ctsmg_pool_destroy(ctsmg_pool p);
  * the last reset; reset != 0 zeroes the counters after reading them.  No
  * reference counterpart. */
 int32_t ctsmg_copy_bytes(int64_t* h2d, int64_t* d2h, int32_t reset);
+/* Per-chunk timeline of the calling thread's pipelined drop-in calls
+ * (ctsmg_soilwater, ctsmg_soiltemperature over an ascending filter of at
+ * least 32,768 columns).  enable = 1 / 0 turns the recording on / off for
+ * later calls, -1 leaves it.  With ms_out (7 floats per chunk, at most
+ * max_chunks chunks) the last recorded call's marks are read first, in ms
+ * from its first copy-in: on the GPU copy-in start, copy-in end, kernel
+ * start, kernel end, copy-out end; on the host clock the moments the calling
+ * thread finished enqueuing the chunk's copy-in and its copy-out;
+ * *nchunks_out = its chunks.  No reference counterpart. */
+int32_t ctsmg_pipe_trace(int32_t enable, float* ms_out, int32_t max_chunks, int32_t* nchunks_out);
 /* FP64 FMA throughput of the current GPU in TFLOP/s (a DFMA loop over every
  * SM); the denominator of the FP64 roofline fraction.  No reference counterpart. */
 int32_t ctsmg_measure_fp64_tflops(double* tflops);

@@ -97,3 +97,36 @@ def test_batch_order_invariance(gpu_lib):
     b.close()
     for k in ("h2osoi_liq", "t_soisno", "qcharge"):
         np.testing.assert_array_equal(S[k], G[k][..., sub][..., ::-1])
+
+
+def test_autotune_orders_and_blocks_leave_results_unchanged(gpu_lib):
+    """ctsmg_batch_autotune2 times every (column order, threads per block)
+    candidate and moves the resident columns into the chosen order; a tuned
+    batch then steps to the same bits as an untuned one (results are returned
+    in the caller's column order either way), and each forced order gives the
+    same bits too.  The caller's order is the slowest of the four: sorting by
+    layer counts is what lets a warp's lanes run level loops of equal length."""
+    from ctsm_gb300.engine import SoilBatch
+    A, npatch = inputs.soil_columns(20000, seed=78, snow=True, nbedrock=(3, 20), forcing="full", npatch_max=3,
+                                    h2osfc=True)
+    U = copy.deepcopy(A)
+    b = SoilBatch(U, npatch)
+    b.run(3)
+    b.sync()
+    b.download()
+    b.close()
+    T = copy.deepcopy(A)
+    b = SoilBatch(T, npatch, balance=True)
+    tuned = b.tune(trial_steps=1)
+    assert tuned["block"] in (64, 128, 256) and len(tuned["ms_per_step"]) == 4
+    assert all(len(v) == 3 and min(v.values()) > 0 for v in tuned["ms_per_step"].values())
+    b.run(3)
+    b.sync()
+    b.download()
+    h2o, soi, _, _ = b.balance()
+    b.close()
+    for k in STATE + ["t_soisno", "qin", "qout", "fact"]:
+        assert np.array_equal(T[k], U[k], equal_nan=True), k
+    assert np.isfinite(h2o).all() and np.isfinite(soi).all()
+    t = tuned["ms_per_step"]
+    assert min(t["caller"].values()) > min(t["snl,nbedrock,zwt"].values())

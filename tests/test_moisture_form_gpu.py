@@ -193,3 +193,40 @@ def test_full_step_with_moisture_form(soil_mf):
     errs, bad = compare(G, R, ["h2osoi_liq", "h2osoi_ice", "t_soisno", "t_grnd", "h2osoi_vol", "t_veg",
                                "qflx_tran_veg", "num_substeps", "eflx_soil_grnd"] + list(cancel), 1e-9, spread)
     assert not bad, {k: errs[k] for k in bad}
+
+
+def test_mf_work_orders_give_identical_bits(soil_mf):
+    """The persistent sub-step kernel's bucketed work order (previous step's
+    sub-step count, bedrock depth) changes which lane takes which column and
+    when, never a column's arithmetic: 4 steps in the bucketed order, in
+    position order and after the autotuner (which times both) give the same
+    bits, and the tuner reports both work orders."""
+    from ctsm_gb300.engine import SoilBatch
+    A, npatch = inputs.soil_columns(9000, seed=41, snow=True, nbedrock=(3, 20), forcing="full", npatch_max=3,
+                                    zwt=(0.5, 9.5))
+    r = np.random.Generator(np.random.Philox(42))
+    A["qflx_rootsoi"][:] = r.uniform(0.0, 2e-5, A["qflx_rootsoi"].shape)
+    A["qflx_infl"][:] = r.uniform(0.0, 5e-4, A["zwt"].shape[0])
+    soil_mf.set_soilwater_movement(abi.soilwater_movement_nml(1))
+    out = []
+    for mode in ("sorted", "positions", "tuned"):
+        G = copy.deepcopy(A)
+        b = SoilBatch(G, npatch, dtime=DT)
+        if mode == "positions":
+            b.set_mf_order(False)
+        b.run(2)
+        if mode == "tuned":
+            t = b.tune(trial_steps=1)
+            assert t["mf_order"] in ("sub-steps,bedrock", "positions")
+            # a soil-only batch tunes its column order too: 4 orders x 2 work orders
+            assert len(t["ms_per_step"]) == 8 and all(len(v) == 3 for v in t["ms_per_step"].values())
+            assert sum(k.endswith("/positions") for k in t["ms_per_step"]) == 4
+        b.run(2)
+        b.sync()
+        b.download()
+        b.close()
+        out.append(G)
+    assert (out[0]["num_substeps"] >= 1).all() and out[0]["num_substeps"].max() > 1
+    for G in out[1:]:
+        for k in STATE + ["qin", "qout", "smp_l", "hk_l"]:
+            assert np.array_equal(G[k], out[0][k], equal_nan=True), k
