@@ -169,24 +169,33 @@ struct PsnPatch {
 // 1722-1817).
 struct PsnTemp { double kc, ko, cp, lmr1, lmr2, vc1, vc2, j1, j2, tpu1, tpu2, q10; };
 
-// everything one patch carries from setup to the passes and on to finalize
+// What a patch carries from setup to the passes and on to finalize, in two
+// parts.  PatchK holds the quantities setup fixes for the whole iteration:
+// the displaced heights and roughness, the wind, the longwave factors, the
+// logarithms of the fixed heights over z0m in FrictionVelocity, (zetam)^0.333
+// and (zetat)^-0.333, exp(-(elai+esai)), sqrt(dleaf), 1 - exp(-elai_dl), the
+// ground's emitted longwave factor lw_grnd and the photosynthesis constants.
+// The iterating kernel keeps it in shared memory, so that the registers hold
+// only what the passes change.
+struct PatchK {
+    double displa, z0mv, hgt_u, hgt_t, hgt_q, zldis, ur, tl_ini, air, bir, cir, dayl_factor, liqcan, snocan;
+    double lg_u, lg_u10, lg_t, lg_q, lg_2m, lg_u10m, pz_m, pz_t, s1_zetam, s2_zetat, w_sai, sqrt_dleaf, one_m_edl,
+        lw_grnd;
+    PsnPatch q;
+};
+
+// Patch holds what the passes change: the state carried from pass to pass and
+// the last pass's values that finalize uses.
 struct Patch {
     int p, c, g, ivt, itlef, nmozsgn, num_iter, c3, err_code, err_idx;
-    double displa, z0mv, hgt_u, hgt_t, hgt_q, zldis, ur, um, obu, obuold, fm;
-    double t_veg, tl_ini, qsatl, el, qsatldT, taf, qaf, dth, dqh, delq;
-    double del, efeb, air, bir, cir, dayl_factor, liqcan, snocan;
+    double um, obu, obuold, fm;
+    double t_veg, qsatl, el, qsatldT, taf, qaf, dth, dqh, delq;
+    double del, efeb;
     // last-pass values used after the iteration
     double tlbef, dt_veg, err, eflx_sh_veg, qflx_evap_veg, qflx_tran_veg, lw_leaf, zeta;
     double ustar, temp1, temp2, temp12m, temp22m, ram1, rah_a, raw_a, rah_b, uaf, rb;
     double wtl0, wta0, wtg, wtal, wtgq, wtlq0, wtaq0, wtalq, efe;
     double u10_clm, u10, vds, vpd_can, rh_leaf, rhaf_last, vpd_last;
-    // quantities of the pass that do not change between passes: logarithms of
-    // the fixed heights over z0m in FrictionVelocity, (zetam)^0.333 and
-    // (zetat)^-0.333, exp(-(elai+esai)), sqrt(dleaf), 1 - exp(-elai_dl) and
-    // the ground's emitted longwave factor lw_grnd
-    double lg_u, lg_u10, lg_t, lg_q, lg_2m, lg_u10m, pz_m, pz_t, s1_zetam, s2_zetat, w_sai, sqrt_dleaf, one_m_edl,
-        lw_grnd;
-    PsnPatch q;
     PhaseOut sun, sha;
     PsnState st;
 };
@@ -195,25 +204,30 @@ struct Patch {
 // patch's filter position (level-major like the model arrays).
 #define PATCH_INTS(X) X(p) X(c) X(g) X(ivt) X(itlef) X(nmozsgn) X(num_iter) X(c3) X(err_code) X(err_idx)
 #define PATCH_DOUBLES(X)                                                                                              \
-    X(displa) X(z0mv) X(hgt_u) X(hgt_t) X(hgt_q) X(zldis) X(ur) X(um) X(obu) X(obuold) X(fm)                          \
-    X(t_veg) X(tl_ini) X(qsatl) X(el) X(qsatldT) X(taf) X(qaf) X(dth) X(dqh) X(delq)                                  \
-    X(del) X(efeb) X(air) X(bir) X(cir) X(dayl_factor) X(liqcan) X(snocan)                                            \
+    X(um) X(obu) X(obuold) X(fm)                                                                                      \
+    X(t_veg) X(qsatl) X(el) X(qsatldT) X(taf) X(qaf) X(dth) X(dqh) X(delq)                                             \
+    X(del) X(efeb)                                                                                                    \
     X(tlbef) X(dt_veg) X(err) X(eflx_sh_veg) X(qflx_evap_veg) X(qflx_tran_veg) X(lw_leaf) X(zeta)                     \
     X(ustar) X(temp1) X(temp2) X(temp12m) X(temp22m) X(ram1) X(rah_a) X(raw_a) X(rah_b) X(uaf) X(rb)                  \
     X(wtl0) X(wta0) X(wtg) X(wtal) X(wtgq) X(wtlq0) X(wtaq0) X(wtalq) X(efe)                                          \
     X(u10_clm) X(u10) X(vds) X(vpd_can) X(rh_leaf) X(rhaf_last) X(vpd_last)                                           \
-    X(lg_u) X(lg_u10) X(lg_t) X(lg_q) X(lg_2m) X(lg_u10m) X(pz_m) X(pz_t) X(s1_zetam) X(s2_zetat) X(w_sai)         \
-    X(sqrt_dleaf) X(one_m_edl)                                                                                        \
-    X(lw_grnd)                                                                                                        \
-    X(q.vcmax25top) X(q.jmax25top) X(q.vcmaxse) X(q.jmaxse) X(q.tpuse) X(q.f25_lmr) X(q.f25_vc) X(q.f25_j)            \
-    X(q.f25_tpu) X(q.cf) X(q.mslope) X(q.mint) X(q.mbb)                                                               \
     X(sun.rs) X(sun.psn) X(sun.lmr) X(sun.ci) X(sun.gs_mol_phase)                                                     \
     X(sha.rs) X(sha.psn) X(sha.lmr) X(sha.ci) X(sha.gs_mol_phase)                                                     \
     X(st.ac) X(st.aj) X(st.ap) X(st.ag) X(st.an) X(st.gs_mol)
+#define PATCHK_DOUBLES(X)                                                                                             \
+    X(displa) X(z0mv) X(hgt_u) X(hgt_t) X(hgt_q) X(zldis) X(ur) X(tl_ini) X(air) X(bir) X(cir) X(dayl_factor)          \
+    X(liqcan) X(snocan)                                                                                               \
+    X(lg_u) X(lg_u10) X(lg_t) X(lg_q) X(lg_2m) X(lg_u10m) X(pz_m) X(pz_t) X(s1_zetam) X(s2_zetat) X(w_sai)         \
+    X(sqrt_dleaf) X(one_m_edl) X(lw_grnd)                                                                             \
+    X(q.vcmax25top) X(q.jmax25top) X(q.vcmaxse) X(q.jmaxse) X(q.tpuse) X(q.f25_lmr) X(q.f25_vc) X(q.f25_j)            \
+    X(q.f25_tpu) X(q.cf) X(q.mslope) X(q.mint) X(q.mbb)
 #define PATCH_COUNT(m) +1
 constexpr int NPI = 0 PATCH_INTS(PATCH_COUNT);
-constexpr int NPD = 0 PATCH_DOUBLES(PATCH_COUNT);
-static_assert(sizeof(Patch) == NPI * 4 + NPD * 8, "every Patch component must be listed in PATCH_INTS / PATCH_DOUBLES");
+constexpr int NPV = 0 PATCH_DOUBLES(PATCH_COUNT);
+constexpr int NPK = 0 PATCHK_DOUBLES(PATCH_COUNT);
+constexpr int NPD = NPV + NPK;                // double planes of the record: Patch's, then PatchK's
+static_assert(sizeof(Patch) == NPI * 4 + NPV * 8, "every Patch component must be listed in PATCH_INTS / PATCH_DOUBLES");
+static_assert(sizeof(PatchK) == NPK * 8, "every PatchK component must be listed in PATCHK_DOUBLES");
 
 __device__ __forceinline__ void store_patch(double* ws, int ld, int f, const Patch& s) {
     int* wi = reinterpret_cast<int*>(ws + (size_t)NPD * ld);
@@ -225,6 +239,20 @@ __device__ __forceinline__ void store_patch(double* ws, int ld, int f, const Pat
 #define ST_I(m) wi[(size_t)(k++) * ld + f] = s.m;
     PATCH_INTS(ST_I)
 #undef ST_I
+}
+
+__device__ __forceinline__ void store_patchk(double* ws, int ld, int f, const PatchK& s) {
+    int k = NPV;
+#define ST_K(m) ws[(size_t)(k++) * ld + f] = s.m;
+    PATCHK_DOUBLES(ST_K)
+#undef ST_K
+}
+
+__device__ __forceinline__ void load_patchk(const double* __restrict__ ws, int ld, int f, PatchK& s) {
+    int k = NPV;
+#define LD_K(m) s.m = ws[(size_t)(k++) * ld + f];
+    PATCHK_DOUBLES(LD_K)
+#undef LD_K
 }
 
 __device__ __forceinline__ void load_patch(const double* __restrict__ ws, int ld, int f, Patch& s) {
@@ -241,12 +269,12 @@ __device__ __forceinline__ void load_patch(const double* __restrict__ ws, int ld
 
 // PhotosynthesisMod.F90:1555-1830: the factors of the pass's t_veg.  The
 // day-time ones (kc, ko, cp, vcmax, jmax, tpu) only when a phase has light.
-__device__ void psn_temp(const CanopyArgs& A, const Patch& s, double forc_pbot, double oair, bool day, PsnTemp& T) {
+__device__ void psn_temp(const CanopyArgs& A, const Patch& s, const PatchK& K, double forc_pbot, double oair, bool day, PsnTemp& T) {
     const ctsmg_canopy_params& P = A.par;
     const double t_veg = s.t_veg;
     if (s.c3) {
         T.lmr1 = ft(t_veg, P.lmrha);
-        T.lmr2 = fth(t_veg, P.lmrhd, P.lmrse, s.q.f25_lmr);
+        T.lmr2 = fth(t_veg, P.lmrhd, P.lmrse, K.q.f25_lmr);
     } else {
         T.q10 = xpow(2.0, (t_veg - (TFRZ + 25.0)) / 10.0);
         T.lmr2 = 1.0 + xexp(1.3 * (t_veg - (TFRZ + 55.0)));
@@ -259,26 +287,26 @@ __device__ void psn_temp(const CanopyArgs& A, const Patch& s, double forc_pbot, 
     T.cp = 0.5 * oair / sco * ft(t_veg, P.cpha);
     if (s.c3) {
         T.vc1 = ft(t_veg, P.vcmaxha);
-        T.vc2 = fth(t_veg, P.vcmaxhd, s.q.vcmaxse, s.q.f25_vc);
+        T.vc2 = fth(t_veg, P.vcmaxhd, K.q.vcmaxse, K.q.f25_vc);
     } else {
         T.vc1 = 1.0 + xexp(0.2 * ((TFRZ + 15.0) - t_veg));
         T.vc2 = 1.0 + xexp(0.3 * (t_veg - (TFRZ + 40.0)));
     }
     T.j1 = ft(t_veg, P.jmaxha);
-    T.j2 = fth(t_veg, P.jmaxhd, s.q.jmaxse, s.q.f25_j);
+    T.j2 = fth(t_veg, P.jmaxhd, K.q.jmaxse, K.q.f25_j);
     T.tpu1 = ft(t_veg, P.tpuha);
-    T.tpu2 = fth(t_veg, P.tpuhd, s.q.tpuse, s.q.f25_tpu);
+    T.tpu2 = fth(t_veg, P.tpuhd, K.q.tpuse, K.q.f25_tpu);
 }
 
 // PhotosynthesisMod.F90:1243-2062, one phase, nlevcan = nrad = 1
-__device__ PhaseOut photosynthesis(const CanopyArgs& A, const Patch& s, const PsnTemp& T, int pidx, double forc_pbot,
+__device__ PhaseOut photosynthesis(const CanopyArgs& A, const Patch& s, const PatchK& K, const PsnTemp& T, int pidx, double forc_pbot,
                                    double esat_tv, double eair, double oair, double cair, double rb, double btran,
                                    double par_z, double lai_z, double vcmaxcint, PsnState& st, double& vpd_can,
                                    double& rh_leaf, Err& err) {
     const ctsmg_canopy_params& P = A.par;
     const int method = A.method;
     LANE_PROBE(3);
-    const PsnPatch& q = s.q;
+    const PsnPatch& q = K.q;
     const double medlyn_int = q.mint;
     const bool c3 = s.c3 != 0;
     const double qe = c3 ? 0.0 : 0.05;
@@ -369,11 +397,11 @@ __device__ PhaseOut photosynthesis(const CanopyArgs& A, const Patch& s, const Ps
 
 // FrictionVelocityMod.F90:754-1117 for one patch (z0h = z0q = z0m), with the
 // logarithms of the fixed heights taken from the patch record.
-__device__ void friction_velocity(const Patch& s, int iter, double& fm, double& ustar, double& temp1, double& temp2,
+__device__ void friction_velocity(const Patch& s, const PatchK& K, int iter, double& fm, double& ustar, double& temp1, double& temp2,
                                   double& temp12m, double& temp22m, double& u10_clm, double& u10, double& vds) {
     const double zetam = 1.574, zetat = 0.465;
-    const double obu = s.obu, z0m = s.z0mv, um = s.um;
-    double zldis = s.hgt_u - s.displa;
+    const double obu = s.obu, z0m = K.z0mv, um = s.um;
+    double zldis = K.hgt_u - K.displa;
     double zeta = zldis / obu;
     // values several branches share, evaluated once: stab1(-zetam) and
     // stab2(-zetat) (constants, kept in the record), (-zeta)^0.333, and
@@ -383,13 +411,13 @@ __device__ void friction_velocity(const Patch& s, int iter, double& fm, double& 
     const double s2z0 = (obu < 0.0) ? stab2(z0m / obu) : 0.0;
     if (zeta < -zetam) {
         LANE_PROBE(8);
-        ustar = VKC * um / (xlog(-zetam * obu / z0m) - s.s1_zetam + stab1(z0m / obu) + 1.14 * (pz - s.pz_m));
+        ustar = VKC * um / (xlog(-zetam * obu / z0m) - K.s1_zetam + stab1(z0m / obu) + 1.14 * (pz - K.pz_m));
     } else if (zeta < 0.0) {
         LANE_PROBE(9);
-        ustar = VKC * um / (s.lg_u - stab1(zeta) + stab1(z0m / obu));
+        ustar = VKC * um / (K.lg_u - stab1(zeta) + stab1(z0m / obu));
     } else if (zeta <= 1.0) {
         LANE_PROBE(10);
-        ustar = VKC * um / (s.lg_u + 5.0 * zeta - 5.0 * z0m / obu);
+        ustar = VKC * um / (K.lg_u + 5.0 * zeta - 5.0 * z0m / obu);
     } else
         ustar = VKC * um / (xlog(obu / z0m) + 5.0 - 5.0 * z0m / obu + (5.0 * xlog(zeta) + zeta - 1.0));
     vds = (zeta < 0.0) ? 2.e-3 * ustar * (1.0 + xpow(300.0 / (-obu), 0.666)) : 2.e-3 * ustar;
@@ -398,27 +426,27 @@ __device__ void friction_velocity(const Patch& s, int iter, double& fm, double& 
     } else {
         const double z10 = 10.0 + z0m;
         if (zeta < -zetam)
-            u10_clm = um - (ustar / VKC * (xlog(-zetam * obu / z10) - s.s1_zetam + stab1(z10 / obu) + 1.14 * (pz - s.pz_m)));
+            u10_clm = um - (ustar / VKC * (xlog(-zetam * obu / z10) - K.s1_zetam + stab1(z10 / obu) + 1.14 * (pz - K.pz_m)));
         else if (zeta < 0.0)
-            u10_clm = um - (ustar / VKC * (s.lg_u10 - stab1(zeta) + stab1(z10 / obu)));
+            u10_clm = um - (ustar / VKC * (K.lg_u10 - stab1(zeta) + stab1(z10 / obu)));
         else if (zeta <= 1.0)
-            u10_clm = um - (ustar / VKC * (s.lg_u10 + 5.0 * zeta - 5.0 * z10 / obu));
+            u10_clm = um - (ustar / VKC * (K.lg_u10 + 5.0 * zeta - 5.0 * z10 / obu));
         else
             u10_clm = um - (ustar / VKC * (xlog(obu / z10) + 5.0 - 5.0 * z10 / obu + (5.0 * xlog(zeta) + zeta - 1.0)));
     }
     auto tprof = [&](double zl, double z0, double lgz) {   // z0 = z0m in every call
         const double zt = zl / obu;
         if (zt < -zetat)
-            return VKC / (xlog(-zetat * obu / z0) - s.s2_zetat + s2z0 + 0.8 * (s.pz_t - xpow(-zt, -0.333)));
+            return VKC / (xlog(-zetat * obu / z0) - K.s2_zetat + s2z0 + 0.8 * (K.pz_t - xpow(-zt, -0.333)));
         else if (zt < 0.0)
             return VKC / (lgz - stab2(zt) + s2z0);
         else if (zt <= 1.0)
             return VKC / (lgz + 5.0 * zt - 5.0 * z0 / obu);
         return VKC / (xlog(obu / z0) + 5.0 - 5.0 * z0 / obu + (5.0 * xlog(zt) + zt - 1.0));
     };
-    temp1 = tprof(s.hgt_t - s.displa, s.z0mv, s.lg_t);
-    temp2 = (s.hgt_q == s.hgt_t) ? temp1 : tprof(s.hgt_q - s.displa, s.z0mv, s.lg_q);   // z0qv == z0hv here
-    temp12m = tprof(2.0 + s.z0mv, s.z0mv, s.lg_2m);
+    temp1 = tprof(K.hgt_t - K.displa, K.z0mv, K.lg_t);
+    temp2 = (K.hgt_q == K.hgt_t) ? temp1 : tprof(K.hgt_q - K.displa, K.z0mv, K.lg_q);   // z0qv == z0hv here
+    temp12m = tprof(2.0 + K.z0mv, K.z0mv, K.lg_2m);
     temp22m = temp12m;
     double fmnew;
     LANE_PROBE(2);
@@ -439,10 +467,10 @@ __device__ void friction_velocity(const Patch& s, int iter, double& fm, double& 
     } else {
         fm10 = -5.0 * zeta10;
     }
-    u10 = s.ur - ustar / VKC * (s.lg_u10m - fm + fm10);
+    u10 = K.ur - ustar / VKC * (K.lg_u10m - fm + fm10);
 }
 
-__device__ void setup(const CanopyArgs& A, Patch& s, int p, Err& err) {
+__device__ void setup(const CanopyArgs& A, Patch& s, PatchK& K, int p, Err& err) {
     const ctsmg_canopy_io& io = A.io;
     s.p = p;
     s.c = io.patch_column[p] - A.begc;
@@ -452,64 +480,64 @@ __device__ void setup(const CanopyArgs& A, Patch& s, int p, Err& err) {
     const double elai = io.elai[p], esai = io.esai[p], emv = io.emv[p], emg = io.emg[c];
     s.del = 0.0; s.efeb = 0.0; s.obuold = 0.0;
     s.wtgq = 0.0; s.wtlq0 = 0.0; s.wtaq0 = 0.0; s.wtalq = 0.0;
-    s.dayl_factor = fmin(1.0, fmax(0.01, (io.dayl[g] * io.dayl[g]) / (io.max_dayl[g] * io.max_dayl[g])));
+    K.dayl_factor = fmin(1.0, fmax(0.01, (io.dayl[g] * io.dayl[g]) / (io.max_dayl[g] * io.max_dayl[g])));
     io.rb1[p] = 0.0;
     const double lt = fmin(elai + esai, TLSAI_CRIT);
     const double egvf = (1.0 - xexp(-lt)) / (1.0 - xexp(-TLSAI_CRIT));
-    s.displa = egvf * io.displa[p];
-    s.z0mv = xexp(egvf * xlog(io.z0mv[p]) + (1.0 - egvf) * xlog(io.z0mg[c]));
-    s.hgt_u = io.forc_hgt_u[g] + s.z0mv + s.displa;
-    s.hgt_t = io.forc_hgt_t[g] + s.z0mv + s.displa;
-    s.hgt_q = io.forc_hgt_q[g] + s.z0mv + s.displa;
-    s.air = emv * (1.0 + (1.0 - emv) * (1.0 - emg)) * io.forc_lwrad[c];
-    s.bir = -(2.0 - emv * (1.0 - emg)) * emv * SB;
-    s.cir = emv * emg * SB;
+    K.displa = egvf * io.displa[p];
+    K.z0mv = xexp(egvf * xlog(io.z0mv[p]) + (1.0 - egvf) * xlog(io.z0mg[c]));
+    K.hgt_u = io.forc_hgt_u[g] + K.z0mv + K.displa;
+    K.hgt_t = io.forc_hgt_t[g] + K.z0mv + K.displa;
+    K.hgt_q = io.forc_hgt_q[g] + K.z0mv + K.displa;
+    K.air = emv * (1.0 + (1.0 - emv) * (1.0 - emg)) * io.forc_lwrad[c];
+    K.bir = -(2.0 - emv * (1.0 - emg)) * emv * SB;
+    K.cir = emv * emg * SB;
     s.t_veg = io.t_veg[p];
     qsat(s.t_veg, io.forc_pbot[c], s.qsatl, s.el, &s.qsatldT);
     s.nmozsgn = 0;
     const double thm = io.thm[p], forc_q = io.forc_q[c], qg = io.qg[c];
     s.taf = (io.t_grnd[c] + thm) / 2.0;
     s.qaf = (forc_q + qg) / 2.0;
-    s.ur = fmax(A.par.wind_min, sqrt(io.forc_u[g] * io.forc_u[g] + io.forc_v[g] * io.forc_v[g]));
+    K.ur = fmax(A.par.wind_min, sqrt(io.forc_u[g] * io.forc_u[g] + io.forc_v[g] * io.forc_v[g]));
     s.dth = thm - s.taf;
     s.dqh = forc_q - s.qaf;
     s.delq = qg - s.qaf;
     const double dthv = s.dth * (1.0 + 0.61 * forc_q) + 0.61 * io.forc_th[c] * s.dqh;
-    s.zldis = s.hgt_u - s.displa;
-    if (s.zldis < 0.0) flag(err, CTSMG_E_FORCING_HEIGHT, p + A.begp);
+    K.zldis = K.hgt_u - K.displa;
+    if (K.zldis < 0.0) flag(err, CTSMG_E_FORCING_HEIGHT, p + A.begp);
     const double thv = io.thv[c];
-    s.um = (dthv >= 0.0) ? fmax(s.ur, 0.1) : sqrt(s.ur * s.ur + 0.5 * 0.5);
-    const double rib = GRAV * s.zldis * dthv / (thv * s.um * s.um);
+    s.um = (dthv >= 0.0) ? fmax(K.ur, 0.1) : sqrt(K.ur * K.ur + 0.5 * 0.5);
+    const double rib = GRAV * K.zldis * dthv / (thv * s.um * s.um);
     double zeta;
     if (rib >= 0.0) {
-        zeta = rib * xlog(s.zldis / s.z0mv) / (1.0 - 5.0 * fmin(rib, 0.19));
+        zeta = rib * xlog(K.zldis / K.z0mv) / (1.0 - 5.0 * fmin(rib, 0.19));
         zeta = fmin(A.par.zetamaxstable, fmax(zeta, 0.01));
     } else {
-        zeta = rib * xlog(s.zldis / s.z0mv);
+        zeta = rib * xlog(K.zldis / K.z0mv);
         zeta = fmax(-100.0, fmin(zeta, -0.01));
     }
-    s.obu = s.zldis / zeta;
+    s.obu = K.zldis / zeta;
     // fixed during the iteration: FrictionVelocity's logarithms of the
     // heights over z0m, the pass's vegetation / snow factors, lw_grnd
-    s.lg_u = xlog(s.zldis / s.z0mv);
-    s.lg_u10 = xlog(s.zldis / (10.0 + s.z0mv));
-    s.lg_t = xlog((s.hgt_t - s.displa) / s.z0mv);
-    s.lg_q = xlog((s.hgt_q - s.displa) / s.z0mv);
-    s.lg_2m = xlog((2.0 + s.z0mv) / s.z0mv);
-    s.lg_u10m = xlog(fmax(1.0, s.hgt_u / 10.0));
-    s.pz_m = xpow(1.574, 0.333);
-    s.pz_t = xpow(0.465, -0.333);
-    s.s1_zetam = stab1(-1.574);
-    s.s2_zetat = stab2(-0.465);
-    s.w_sai = xexp(-(elai + esai));
-    s.sqrt_dleaf = sqrt(A.pft.dleaf[s.ivt]);
+    K.lg_u = xlog(K.zldis / K.z0mv);
+    K.lg_u10 = xlog(K.zldis / (10.0 + K.z0mv));
+    K.lg_t = xlog((K.hgt_t - K.displa) / K.z0mv);
+    K.lg_q = xlog((K.hgt_q - K.displa) / K.z0mv);
+    K.lg_2m = xlog((2.0 + K.z0mv) / K.z0mv);
+    K.lg_u10m = xlog(fmax(1.0, K.hgt_u / 10.0));
+    K.pz_m = xpow(1.574, 0.333);
+    K.pz_t = xpow(0.465, -0.333);
+    K.s1_zetam = stab1(-1.574);
+    K.s2_zetat = stab2(-0.465);
+    K.w_sai = xexp(-(elai + esai));
+    K.sqrt_dleaf = sqrt(A.pft.dleaf[s.ivt]);
     {
         const double fsno_dl = io.snow_depth[c] / A.par.z_dl;
         const double elai_dl = A.par.lai_dl * (1.0 - fmin(fsno_dl, 1.0));
-        s.one_m_edl = 1.0 - xexp(-elai_dl);
+        K.one_m_edl = 1.0 - xexp(-elai_dl);
         const int ldc = io.ldc, snl = io.snl[c];
         const double frac_sno = io.frac_sno_eff[c], frac_h2osfc = io.frac_h2osfc[c];
-        s.lw_grnd = (frac_sno * ipow4(io.t_soisno[c + (size_t)(snl + NLEVSNO) * ldc]) +
+        K.lw_grnd = (frac_sno * ipow4(io.t_soisno[c + (size_t)(snl + NLEVSNO) * ldc]) +
                      (1.0 - frac_sno - frac_h2osfc) * ipow4(io.t_soisno[c + (size_t)NLEVSNO * ldc]) +
                      frac_h2osfc * ipow4(io.t_h2osfc[c]));
     }
@@ -520,27 +548,27 @@ __device__ void setup(const CanopyArgs& A, Patch& s, int p, Err& err) {
         const int ivt = s.ivt;
         s.c3 = (llround(F.c3psn[ivt]) == 1) ? 1 : 0;
         const double lnc = 1.0 / (F.slatop[ivt] * F.leafcn[ivt]);
-        double vcmax25top = lnc * F.flnr[ivt] * P.fnr * P.act25 * s.dayl_factor;
+        double vcmax25top = lnc * F.flnr[ivt] * P.fnr * P.act25 * K.dayl_factor;
         vcmax25top = vcmax25top * F.fnitr[ivt];
         const double t10c = fmin(fmax((io.t_a10[p] - TFRZ), 11.0), 35.0);
-        s.q.vcmax25top = vcmax25top;
-        s.q.jmax25top = ((2.59 - 0.035 * t10c) * vcmax25top) * P.jmax25top_sf;
-        s.q.vcmaxse = (668.39 - 1.07 * t10c) * P.vcmaxse_sf;
-        s.q.jmaxse = (659.70 - 0.75 * t10c) * P.jmaxse_sf;
-        s.q.tpuse = (668.39 - 1.07 * t10c) * P.tpuse_sf;
-        s.q.f25_lmr = fth25(P.lmrhd, P.lmrse);
-        s.q.f25_vc = fth25(P.vcmaxhd, s.q.vcmaxse);
-        s.q.f25_j = fth25(P.jmaxhd, s.q.jmaxse);
-        s.q.f25_tpu = fth25(P.tpuhd, s.q.tpuse);
-        s.q.cf = io.forc_pbot[c] / (RGAS * 1.e-3 * thm) * 1.e06;
-        s.q.mslope = A.medlynslope_p ? A.medlynslope_p[p] : F.medlynslope[ivt];
-        s.q.mint = A.medlynintercept_p ? A.medlynintercept_p[p] : F.medlynintercept[ivt];
-        s.q.mbb = F.mbbopt[ivt];
+        K.q.vcmax25top = vcmax25top;
+        K.q.jmax25top = ((2.59 - 0.035 * t10c) * vcmax25top) * P.jmax25top_sf;
+        K.q.vcmaxse = (668.39 - 1.07 * t10c) * P.vcmaxse_sf;
+        K.q.jmaxse = (659.70 - 0.75 * t10c) * P.jmaxse_sf;
+        K.q.tpuse = (668.39 - 1.07 * t10c) * P.tpuse_sf;
+        K.q.f25_lmr = fth25(P.lmrhd, P.lmrse);
+        K.q.f25_vc = fth25(P.vcmaxhd, K.q.vcmaxse);
+        K.q.f25_j = fth25(P.jmaxhd, K.q.jmaxse);
+        K.q.f25_tpu = fth25(P.tpuhd, K.q.tpuse);
+        K.q.cf = io.forc_pbot[c] / (RGAS * 1.e-3 * thm) * 1.e06;
+        K.q.mslope = A.medlynslope_p ? A.medlynslope_p[p] : F.medlynslope[ivt];
+        K.q.mint = A.medlynintercept_p ? A.medlynintercept_p[p] : F.medlynintercept[ivt];
+        K.q.mbb = F.mbbopt[ivt];
     }
     s.num_iter = 0;
-    s.tl_ini = s.t_veg;
-    s.liqcan = io.liqcan[p];
-    s.snocan = io.snocan[p];
+    K.tl_ini = s.t_veg;
+    K.liqcan = io.liqcan[p];
+    K.snocan = io.snocan[p];
     s.fm = 0.0;
     s.itlef = 0;
     s.st = PsnState{0, 0, 0, 0, 0, 0};
@@ -550,13 +578,13 @@ __device__ void setup(const CanopyArgs& A, Patch& s, int p, Err& err) {
 
 // one pass of the stability iteration (CanopyFluxesMod.F90:1028-1456);
 // returns true when the patch leaves the iteration
-__device__ bool pass(const CanopyArgs& A, Patch& s, Err& err, double dtime) {
+__device__ bool pass(const CanopyArgs& A, Patch& s, const PatchK& K, Err& err, double dtime) {
     const ctsmg_canopy_io& io = A.io;
     const ctsmg_canopy_params& P = A.par;
     const int p = s.p, c = s.c, g = s.g;
     const int pg = p + A.begp;
     LANE_PROBE(0);
-    friction_velocity(s, s.itlef + 1, s.fm, s.ustar, s.temp1, s.temp2, s.temp12m, s.temp22m, s.u10_clm, s.u10, s.vds);
+    friction_velocity(s, K, s.itlef + 1, s.fm, s.ustar, s.temp1, s.temp2, s.temp12m, s.temp22m, s.u10_clm, s.u10, s.vds);
     const double ustar = s.ustar;
     s.tlbef = s.t_veg;
     const double del2 = s.del;
@@ -565,10 +593,10 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, Err& err, double dtime) {
     s.raw_a = 1.0 / (s.temp2 * ustar);
     s.uaf = s.um * sqrt(1.0 / (s.ram1 * s.um));
     const double elai = io.elai[p], esai = io.esai[p];
-    const double cfl = P.cv / (sqrt(s.uaf) * s.sqrt_dleaf);
+    const double cfl = P.cv / (sqrt(s.uaf) * K.sqrt_dleaf);
     s.rb = 1.0 / (cfl * s.uaf);
     const double rb = s.rb;
-    const double w = s.w_sai;
+    const double w = K.w_sai;
     const double csoilb = VKC / (P.a_coef * xpow(io.z0mg[c] * s.uaf / NU_PARAM, P.a_exp));
     const double csoilcn = csoilb * w + P.csoilc * (1.0 - w);
     s.rah_b = 1.0 / (csoilcn * s.uaf);
@@ -583,13 +611,13 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, Err& err, double dtime) {
     const double oair = io.forc_po2[g], cair = io.forc_pco2[g];
     const double parsun = io.parsun_z[p], parsha = io.parsha_z[p];
     PsnTemp T;
-    psn_temp(A, s, forc_pbot, oair, parsun > 0.0 || parsha > 0.0, T);
+    psn_temp(A, s, K, forc_pbot, oair, parsun > 0.0 || parsha > 0.0, T);
     // sunlit then shaded phase (PhotosynthesisMod called with phase='sun' and
     // 'sha', CanopyFluxesMod.F90:1143-1169); a loop, so the phase body and
     // its root finder are compiled once
 #pragma unroll 1
     for (int ph = 0; ph < 2; ++ph) {
-        const PhaseOut o = photosynthesis(A, s, T, pg, forc_pbot, svpts, eah, oair, cair, rb, btran,
+        const PhaseOut o = photosynthesis(A, s, K, T, pg, forc_pbot, svpts, eah, oair, cair, rb, btran,
                                           ph ? parsha : parsun, ph ? laisha : laisun,
                                           ph ? io.vcmaxcintsha[p] : io.vcmaxcintsun[p], s.st, s.vpd_can, s.rh_leaf,
                                           err);
@@ -611,7 +639,7 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, Err& err, double dtime) {
     const double rppdry = (fdry > 0.0) ? fdry * rb * (laisun / (rb + s.sun.rs) + laisha / (rb + s.sha.rs)) / elai : 0.0;
     const double forc_rho = io.forc_rho[c], forc_q = io.forc_q[c], qg = io.qg[c], t_grnd = io.t_grnd[c];
     double efpot = forc_rho * ((elai + esai) / rb) * (s.qsatl - s.qaf);
-    const double h2ocan = s.liqcan + s.snocan;
+    const double h2ocan = K.liqcan + K.snocan;
     double rpp;
     if (efpot > 0.0) {
         if (btran > 0.0) { s.qflx_tran_veg = efpot * rppdry; rpp = rppdry + fwet; }
@@ -624,7 +652,7 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, Err& err, double dtime) {
     const double fv = (double)io.frac_veg_nosno[p];
     const double wtaq = fv / s.raw_a;
     const double wtlq = fv * (elai + esai) / rb * rpp;
-    const double rdl = s.one_m_edl / (0.004 * s.uaf);
+    const double rdl = K.one_m_edl / (0.004 * s.uaf);
     s.wtgq = (s.delq < 0.0) ? fv / (raw_b + rdl) : fv / (raw_b + io.soilresis[c]);
     const double wtsqi = 1.0 / (wtaq + wtlq + s.wtgq);
     const double wtgq0 = s.wtgq * wtsqi;
@@ -642,12 +670,12 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, Err& err, double dtime) {
         s.efe = 0.1 * efeold;
         erre = s.efe - efeold;
     }
-    const double lw_grnd = s.lw_grnd;
+    const double lw_grnd = K.lw_grnd;
     const double sabv = io.sabv[p];
     const double t_veg = s.t_veg;
-    double dt_veg = ((1.0 - 0.0) * (sabv + s.air + s.bir * ipow4(t_veg) + s.cir * lw_grnd) - efsh - s.efe - 0.0 + 0.0 -
-                     (0.0 / dtime) * (t_veg - s.tl_ini)) /
-                    ((1.0 - 0.0) * (-4.0 * s.bir * ipow3(t_veg)) + 4.0 * 0.0 * io.emv[p] * SB * ipow3(t_veg) + dc1 * wtga +
+    double dt_veg = ((1.0 - 0.0) * (sabv + K.air + K.bir * ipow4(t_veg) + K.cir * lw_grnd) - efsh - s.efe - 0.0 + 0.0 -
+                     (0.0 / dtime) * (t_veg - K.tl_ini)) /
+                    ((1.0 - 0.0) * (-4.0 * K.bir * ipow3(t_veg)) + 4.0 * 0.0 * io.emv[p] * SB * ipow3(t_veg) + dc1 * wtga +
                      dc2 * wtgaq * s.qsatldT + 0.0 / dtime);
     s.t_veg = s.tlbef + dt_veg;
     const double dels = dt_veg;
@@ -657,9 +685,9 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, Err& err, double dtime) {
         dt_veg = 1.0 * dels / s.del;
         s.t_veg = s.tlbef + dt_veg;
         const double tb3 = ipow3(s.tlbef);
-        s.err = (1.0 - 0.0) * (sabv + s.air + s.bir * tb3 * (s.tlbef + 4.0 * dt_veg) + s.cir * lw_grnd) -
+        s.err = (1.0 - 0.0) * (sabv + K.air + K.bir * tb3 * (s.tlbef + 4.0 * dt_veg) + K.cir * lw_grnd) -
                 0.0 * io.emv[p] * SB * tb3 * (s.tlbef + 4.0 * dt_veg) + 0.0 - (efsh + dc1 * wtga * dt_veg) -
-                (s.efe + dc2 * wtgaq * s.qsatldT * dt_veg) - (0.0 / dtime) * (s.t_veg - s.tl_ini);
+                (s.efe + dc2 * wtgaq * s.qsatldT * dt_veg) - (0.0 / dtime) * (s.t_veg - K.tl_ini);
     }
     s.dt_veg = dt_veg;
     efpot = forc_rho * ((elai + esai) / rb) * (wtgaq * (s.qsatl + s.qsatldT * dt_veg) - wtgq0 * qg - s.wtaq0 * forc_q);
@@ -679,19 +707,19 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, Err& err, double dtime) {
     const double qstar = s.temp2 * s.dqh;
     const double forc_th = io.forc_th[c], thv = io.thv[c];
     const double thvstar = tstar * (1.0 + 0.61 * forc_q) + 0.61 * forc_th * qstar;
-    double zeta = s.zldis * VKC * GRAV * thvstar / ((ustar * ustar) * thv);
+    double zeta = K.zldis * VKC * GRAV * thvstar / ((ustar * ustar) * thv);
     if (zeta >= 0.0) {
         zeta = fmin(P.zetamaxstable, fmax(zeta, 0.01));
-        s.um = fmax(s.ur, 0.1);
+        s.um = fmax(K.ur, 0.1);
     } else {
         zeta = fmax(-100.0, fmin(zeta, -0.01));
         const double wc = (ustar * thvstar > 0.0) ? 0.0 : 1.0 * xpow(-GRAV * ustar * thvstar * 1000.0 / thv, 0.333);
-        s.um = sqrt(s.ur * s.ur + wc * wc);
+        s.um = sqrt(K.ur * K.ur + wc * wc);
     }
     s.zeta = zeta;
-    s.obu = s.zldis / zeta;
+    s.obu = K.zldis / zeta;
     if (s.obuold * s.obu < 0.0) s.nmozsgn = s.nmozsgn + 1;
-    if (s.nmozsgn >= 4) s.obu = s.zldis / (-0.01);
+    if (s.nmozsgn >= 4) s.obu = K.zldis / (-0.01);
     s.obuold = s.obu;
     s.itlef = s.itlef + 1;
     if (s.itlef > 2) {
@@ -705,7 +733,7 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, Err& err, double dtime) {
 }
 
 // after the iteration (CanopyFluxesMod.F90:1461-1655)
-__device__ void finalize(const CanopyArgs& A, const Patch& s, double dtime) {
+__device__ void finalize(const CanopyArgs& A, const Patch& s, const PatchK& K, double dtime) {
     const ctsmg_canopy_io& io = A.io;
     const int p = s.p, c = s.c, g = s.g;
     const int ldc = io.ldc;
@@ -717,8 +745,8 @@ __device__ void finalize(const CanopyArgs& A, const Patch& s, double dtime) {
                             frac_h2osfc * ipow4(io.t_h2osfc[c]));
     const double tb3 = ipow3(s.tlbef);
     const double emv = io.emv[p], emg = io.emg[c];
-    io.err_canopy[p] = (1.0 - 0.0) * (io.sabv[p] + s.air + s.bir * tb3 * (s.tlbef + 4.0 * s.dt_veg) + s.cir * lw_grnd) -
-                       s.lw_leaf + 0.0 - s.eflx_sh_veg - HVAP * s.qflx_evap_veg - ((s.t_veg - s.tl_ini) * 0.0 / dtime);
+    io.err_canopy[p] = (1.0 - 0.0) * (io.sabv[p] + K.air + K.bir * tb3 * (s.tlbef + 4.0 * s.dt_veg) + K.cir * lw_grnd) -
+                       s.lw_leaf + 0.0 - s.eflx_sh_veg - HVAP * s.qflx_evap_veg - ((s.t_veg - K.tl_ini) * 0.0 / dtime);
     const double thm = io.thm[p], forc_rho = io.forc_rho[c], forc_q = io.forc_q[c];
     const double t_veg = s.t_veg;
     const double delt = s.wtal * io.t_grnd[c] - s.wtl0 * t_veg - s.wta0 * thm - 0.0;
@@ -754,7 +782,7 @@ __device__ void finalize(const CanopyArgs& A, const Patch& s, double dtime) {
     io.cgrnds[p] = cgrnds;
     io.cgrndl[p] = cgrndl;
     io.cgrnd[p] = cgrnds + cgrndl * io.htvp[c];
-    double liqcan = s.liqcan, snocan = s.snocan;
+    double liqcan = K.liqcan, snocan = K.snocan;
     const double snocan_baseline = snocan;
     const double net = (s.qflx_tran_veg - s.qflx_evap_veg) * dtime;
     if (t_veg > TFRZ) {
@@ -768,14 +796,14 @@ __device__ void finalize(const CanopyArgs& A, const Patch& s, double dtime) {
     io.liqcan[p] = liqcan;
     io.snocan[p] = snocan;
     if (!A.engine) {
-        io.displa[p] = s.displa;
-        io.z0mv[p] = s.z0mv;
+        io.displa[p] = K.displa;
+        io.z0mv[p] = K.z0mv;
     }
-    io.z0hv[p] = s.z0mv;
-    io.z0qv[p] = s.z0mv;
-    io.forc_hgt_u_patch[p] = s.hgt_u;
-    io.forc_hgt_t_patch[p] = s.hgt_t;
-    io.forc_hgt_q_patch[p] = s.hgt_q;
+    io.z0hv[p] = K.z0mv;
+    io.z0qv[p] = K.z0mv;
+    io.forc_hgt_u_patch[p] = K.hgt_u;
+    io.forc_hgt_t_patch[p] = K.hgt_t;
+    io.forc_hgt_q_patch[p] = K.hgt_q;
     io.t_veg[p] = t_veg;
     io.taf[p] = s.taf;
     io.qaf[p] = s.qaf;
@@ -839,12 +867,14 @@ canopy_setup_kernel(CanopyArgs A, int nfilt, const int32_t* __restrict__ filt, d
     const Order O = order_of(ws, nfilt);
     if (f < nfilt) {
         Patch s{};
+        PatchK K{};
         Err err{0, 0};
-        setup(A, s, (filt ? filt[f] : f + A.begp) - A.begp, err);
+        setup(A, s, K, (filt ? filt[f] : f + A.begp) - A.begp, err);
         s.err_code = err.code;
         s.err_idx = err.idx;
         store_patch(ws, nfilt, f, s);
-        const double zeta0 = s.zldis / s.obu;
+        store_patchk(ws, nfilt, f, K);
+        const double zeta0 = K.zldis / s.obu;
         const bool dark = !(A.io.parsun_z[s.p] > 0.0 || A.io.parsha_z[s.p] > 0.0);
         const int regime = zeta0 < -1.574 ? 3 : zeta0 < -0.465 ? 2 : zeta0 < 0.0 ? 1 : 0;
         int heavy = 2;
@@ -886,8 +916,14 @@ __global__ void __launch_bounds__(128) canopy_order_kernel(int nfilt, double* __
 #ifndef CTSMG_CANOPY_MIN_BLOCKS
 #define CTSMG_CANOPY_MIN_BLOCKS 4
 #endif
-__global__ void __launch_bounds__(128, CTSMG_CANOPY_MIN_BLOCKS)
+constexpr int CANOPY_ITERATE_THREADS = 128;
+__global__ void __launch_bounds__(CANOPY_ITERATE_THREADS, CTSMG_CANOPY_MIN_BLOCKS)
 canopy_iterate_kernel(CanopyArgs A, int nfilt, double* __restrict__ ws, double dtime, int* __restrict__ next) {
+    // the lane's PatchK in shared memory (41 doubles a lane: consecutive lanes
+    // 82 words apart, so a half-warp's 8-byte accesses hit distinct banks);
+    // launched with CANOPY_ITERATE_THREADS threads
+    __shared__ PatchK ksh[CANOPY_ITERATE_THREADS];
+    PatchK& K = ksh[threadIdx.x];
     Patch s;
     Err err{0, 0};
     const int* __restrict__ order = order_of(ws, nfilt).order;
@@ -907,11 +943,12 @@ canopy_iterate_kernel(CanopyArgs A, int nfilt, double* __restrict__ ws, double d
                 f = order[i];
                 LANE_PROBE(12);
                 load_patch(ws, nfilt, f, s);
+                load_patchk(ws, nfilt, f, K);
                 err = Err{s.err_code, s.err_idx};
             }
         }
         __syncwarp();
-        if (have && pass(A, s, err, dtime)) {
+        if (have && pass(A, s, K, err, dtime)) {
             s.err_code = err.code;
             s.err_idx = err.idx;
             store_patch(ws, nfilt, f, s);
@@ -926,8 +963,10 @@ canopy_finalize_kernel(CanopyArgs A, int nfilt, const double* __restrict__ ws, d
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= nfilt) return;
     Patch s;
+    PatchK K;
     load_patch(ws, nfilt, f, s);
-    finalize(A, s, dtime);
+    load_patchk(ws, nfilt, f, K);
+    finalize(A, s, K, dtime);
     if (s.err_code) report_error(derr, s.err_idx, 0, s.err_code);
 }
 
@@ -956,11 +995,15 @@ cudaError_t launch_canopy(const CanopyArgs& a, int nfilt, const int32_t* d_filt,
     int dev = 0;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, canopy::canopy_iterate_kernel, 128, 0);
+    // 4 blocks of 41 KB of PatchK per SM: ask for the shared-memory carveout
+    cudaFuncSetAttribute(canopy::canopy_iterate_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         cudaSharedmemCarveoutMaxShared);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, canopy::canopy_iterate_kernel,
+                                                  canopy::CANOPY_ITERATE_THREADS, 0);
     if (per_sm < 1) per_sm = 1;
     const long long want = (long long)nsm * per_sm;
     const int blocks = (int)(want < nb ? want : nb);
-    canopy::canopy_iterate_kernel<<<blocks, 128, 0, s>>>(a, nfilt, ws, dtime, d_counter);
+    canopy::canopy_iterate_kernel<<<blocks, canopy::CANOPY_ITERATE_THREADS, 0, s>>>(a, nfilt, ws, dtime, d_counter);
     canopy::canopy_finalize_kernel<<<nb, 128, 0, s>>>(a, nfilt, ws, dtime, err);
     return cudaGetLastError();
 }
