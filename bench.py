@@ -692,6 +692,12 @@ def ours_arm(args, ws, rank, local):
     L.ctsmg_measure_fp64_tflops.argtypes = [C.POINTER(C.c_double)]
     fp64 = C.c_double(0.0)
     L.ctsmg_measure_fp64_tflops(C.byref(fp64))
+    L.ctsmg_measure_fp64_lane_cost.argtypes = [C.c_int32, C.POINTER(C.c_float)]
+    lane_cost = {}
+    for lanes in (32, 8, 1):
+        t = C.c_float(0.0)
+        L.ctsmg_measure_fp64_lane_cost(lanes, C.byref(t))
+        lane_cost["ms_%d_lanes" % lanes] = round(float(t.value), 3)
 
     A, npatch = make_inputs(args.ncol, rank_seed(args.seed, rank))
     ncol = args.ncol
@@ -859,7 +865,8 @@ def ours_arm(args, ws, rank, local):
                            "autotune_ms_per_step": tuned["ms_per_step"], "mean_snow_layers": mean_snow},
                 "parity": gate,
                 "gpu_launches": int(args.steps), "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
-                "clocks": clk, "wall_s_timed": wall, "fp64_peak_tflops": fp64.value}
+                "clocks": clk, "wall_s_timed": wall, "fp64_peak_tflops": fp64.value,
+                "fp64_lane_cost": lane_cost}
         line.update(extra)
         print(json.dumps(line), flush=True)
     if ws > 1:

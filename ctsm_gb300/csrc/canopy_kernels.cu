@@ -403,50 +403,83 @@ __device__ void friction_velocity(const Patch& s, const PatchK& K, int iter, dou
     const double obu = s.obu, z0m = K.z0mv, um = s.um;
     double zldis = K.hgt_u - K.displa;
     double zeta = zldis / obu;
-    // values several branches share, evaluated once: stab1(-zetam) and
-    // stab2(-zetat) (constants, kept in the record), (-zeta)^0.333, and
-    // stab2(z0m/obu), the same in all three scalar profiles
     LANE_PROBE(1);
-    const double pz = (zeta < -zetam) ? xpow(-zeta, 0.333) : 0.0;
-    const double s2z0 = (obu < 0.0) ? stab2(z0m / obu) : 0.0;
-    if (zeta < -zetam) {
-        LANE_PROBE(8);
-        ustar = VKC * um / (xlog(-zetam * obu / z0m) - K.s1_zetam + stab1(z0m / obu) + 1.14 * (pz - K.pz_m));
-    } else if (zeta < 0.0) {
-        LANE_PROBE(9);
-        ustar = VKC * um / (K.lg_u - stab1(zeta) + stab1(z0m / obu));
-    } else if (zeta <= 1.0) {
-        LANE_PROBE(10);
-        ustar = VKC * um / (K.lg_u + 5.0 * zeta - 5.0 * z0m / obu);
-    } else
-        ustar = VKC * um / (xlog(obu / z0m) + 5.0 - 5.0 * z0m / obu + (5.0 * xlog(zeta) + zeta - 1.0));
-    vds = (zeta < 0.0) ? 2.e-3 * ustar * (1.0 + xpow(300.0 / (-obu), 0.666)) : 2.e-3 * ustar;
-    if (zldis - z0m <= 10.0) {
-        u10_clm = um;
-    } else {
-        const double z10 = 10.0 + z0m;
-        if (zeta < -zetam)
-            u10_clm = um - (ustar / VKC * (xlog(-zetam * obu / z10) - K.s1_zetam + stab1(z10 / obu) + 1.14 * (pz - K.pz_m)));
-        else if (zeta < 0.0)
-            u10_clm = um - (ustar / VKC * (K.lg_u10 - stab1(zeta) + stab1(z10 / obu)));
-        else if (zeta <= 1.0)
-            u10_clm = um - (ustar / VKC * (K.lg_u10 + 5.0 * zeta - 5.0 * z10 / obu));
-        else
-            u10_clm = um - (ustar / VKC * (xlog(obu / z10) + 5.0 - 5.0 * z10 / obu + (5.0 * xlog(zeta) + zeta - 1.0)));
+    // The momentum and scalar profiles each take one of four stability
+    // branches, and a warp's lanes are often in different ones.  Every
+    // logarithm, power and stability function the branches need is formed
+    // once per warp in a "slot" whose argument each lane selects for its own
+    // branch, then the branches combine the slots' values: the arguments and
+    // the arithmetic are the reference's, only the control flow differs.
+    const bool b1 = zeta < -zetam, b2 = !b1 && zeta < 0.0, b3 = !b1 && !b2 && zeta <= 1.0, b4 = !b1 && !b2 && !b3;
+    const bool tall = !(zldis - z0m <= 10.0);
+    const double z10 = 10.0 + z0m;
+    // the scalar profiles' heights and their branches (z0 = z0m in every call)
+    const bool two = !(K.hgt_q == K.hgt_t);
+    const double zl[3] = {K.hgt_t - K.displa, two ? K.hgt_q - K.displa : 0.0, 2.0 + K.z0mv};
+    double zt[3];
+    int tb[3];                      // 1..4: zt < -zetat, zt < 0, zt <= 1, else
+    bool any_t1 = false, any_t4 = false;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        zt[i] = zl[i] / obu;
+        tb[i] = (zt[i] < -zetat) ? 1 : (zt[i] < 0.0) ? 2 : (zt[i] <= 1.0) ? 3 : 4;
+        if (i == 1 && !two) tb[i] = 0;
+        any_t1 |= tb[i] == 1;
+        any_t4 |= tb[i] == 4;
     }
-    auto tprof = [&](double zl, double z0, double lgz) {   // z0 = z0m in every call
-        const double zt = zl / obu;
-        if (zt < -zetat)
-            return VKC / (xlog(-zetat * obu / z0) - K.s2_zetat + s2z0 + 0.8 * (K.pz_t - xpow(-zt, -0.333)));
-        else if (zt < 0.0)
-            return VKC / (lgz - stab2(zt) + s2z0);
-        else if (zt <= 1.0)
-            return VKC / (lgz + 5.0 * zt - 5.0 * z0 / obu);
-        return VKC / (xlog(obu / z0) + 5.0 - 5.0 * z0 / obu + (5.0 * xlog(zt) + zt - 1.0));
-    };
-    temp1 = tprof(K.hgt_t - K.displa, K.z0mv, K.lg_t);
-    temp2 = (K.hgt_q == K.hgt_t) ? temp1 : tprof(K.hgt_q - K.displa, K.z0mv, K.lg_q);   // z0qv == z0hv here
-    temp12m = tprof(2.0 + K.z0mv, K.z0mv, K.lg_2m);
+    // slots shared by the branches
+    double pz = 0.0, s2z0 = 0.0, st_z0 = 0.0, st_zeta = 0.0, st_z10 = 0.0, l_a = 0.0, l_b = 0.0, l_zeta = 0.0;
+    double l_t1 = 0.0, p_vds = 0.0;
+    if (b1) pz = xpow(-zeta, 0.333);
+    if (obu < 0.0) s2z0 = stab2(z0m / obu);
+    if (b1 || b2) st_z0 = stab1(z0m / obu);
+    if (b2) st_zeta = stab1(zeta);
+    if ((b1 || b2) && tall) st_z10 = stab1(z10 / obu);
+    if (b1 || b4 || any_t4) l_a = xlog(b1 ? -zetam * obu / z0m : obu / z0m);     // b1: ustar; else log(obu / z0m)
+    if ((b1 || b4) && tall) l_b = xlog(b1 ? -zetam * obu / z10 : obu / z10);
+    if (b4) l_zeta = xlog(zeta);
+    if (any_t1) l_t1 = xlog(-zetat * obu / z0m);
+    // log(obu / z0m) for a scalar branch 4 of a lane whose momentum branch
+    // took slot l_a for branch 1 (zl and zldis of opposite signs)
+    double l_obu = l_a;
+    if (b1 && any_t4) l_obu = xlog(obu / z0m);
+    if (zeta < 0.0) p_vds = xpow(300.0 / (-obu), 0.666);
+    LANE_PROBE(8);
+    if (b1) ustar = VKC * um / (l_a - K.s1_zetam + st_z0 + 1.14 * (pz - K.pz_m));
+    else if (b2) ustar = VKC * um / (K.lg_u - st_zeta + st_z0);
+    else if (b3) ustar = VKC * um / (K.lg_u + 5.0 * zeta - 5.0 * z0m / obu);
+    else ustar = VKC * um / (l_a + 5.0 - 5.0 * z0m / obu + (5.0 * l_zeta + zeta - 1.0));
+    vds = (zeta < 0.0) ? 2.e-3 * ustar * (1.0 + p_vds) : 2.e-3 * ustar;
+    if (!tall) {
+        u10_clm = um;
+    } else if (b1) {
+        u10_clm = um - (ustar / VKC * (l_b - K.s1_zetam + st_z10 + 1.14 * (pz - K.pz_m)));
+    } else if (b2) {
+        u10_clm = um - (ustar / VKC * (K.lg_u10 - st_zeta + st_z10));
+    } else if (b3) {
+        u10_clm = um - (ustar / VKC * (K.lg_u10 + 5.0 * zeta - 5.0 * z10 / obu));
+    } else {
+        u10_clm = um - (ustar / VKC * (l_b + 5.0 - 5.0 * z10 / obu + (5.0 * l_zeta + zeta - 1.0)));
+    }
+    // scalar profiles: per call one power slot (branch 1) and one logarithm
+    // slot (branch 2: stab2's logarithm; branch 4: log(zt))
+    const double lgz[3] = {K.lg_t, K.lg_q, K.lg_2m};
+    double tp[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const int b = tb[i];
+        const double z = zt[i];
+        double pw = 0.0, lg = 0.0;
+        if (b == 1) pw = xpow(-z, -0.333);
+        if (b == 2 || b == 4) lg = xlog(b == 2 ? (1.0 + sqrt(1.0 - 16.0 * z)) * 0.5 : z);
+        if (b == 1) tp[i] = VKC / (l_t1 - K.s2_zetat + s2z0 + 0.8 * (K.pz_t - pw));
+        else if (b == 2) tp[i] = VKC / (lgz[i] - 2.0 * lg + s2z0);
+        else if (b == 3) tp[i] = VKC / (lgz[i] + 5.0 * z - 5.0 * z0m / obu);
+        else tp[i] = VKC / (l_obu + 5.0 - 5.0 * z0m / obu + (5.0 * lg + z - 1.0));
+    }
+    temp1 = tp[0];
+    temp2 = two ? tp[1] : temp1;                  // z0qv == z0hv here
+    temp12m = tp[2];
     temp22m = temp12m;
     double fmnew;
     LANE_PROBE(2);

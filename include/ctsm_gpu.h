@@ -956,6 +956,14 @@ int32_t ctsmg_pool_destroy(ctsmg_pool p);
  * the last reset; reset != 0 zeroes the counters after reading them.  No
  * reference counterpart. */
 int32_t ctsmg_copy_bytes(int64_t* h2d, int64_t* d2h, int32_t reset);
+/* How the pipelined drop-in calls (ctsmg_soilwater, ctsmg_soiltemperature
+ * over an ascending filter of at least 32,768 columns) copy their inputs in:
+ * mode 0 (the default) with one gather kernel per chunk that reads the
+ * caller's arrays through their device-mapped addresses when every array the
+ * call copies in is page-locked (cudaHostAlloc / cudaHostRegister) and
+ * element-aligned, else with the copy engines; mode 1 with the copy engines
+ * always.  Results do not depend on it.  No reference counterpart. */
+int32_t ctsmg_set_copy_mode(int32_t mode);
 /* Per-chunk timeline of the calling thread's pipelined drop-in calls
  * (ctsmg_soilwater, ctsmg_soiltemperature over an ascending filter of at
  * least 32,768 columns).  enable = 1 / 0 turns the recording on / off for
@@ -969,6 +977,11 @@ int32_t ctsmg_pipe_trace(int32_t enable, float* ms_out, int32_t max_chunks, int3
 /* FP64 FMA throughput of the current GPU in TFLOP/s (a DFMA loop over every
  * SM); the denominator of the FP64 roofline fraction.  No reference counterpart. */
 int32_t ctsmg_measure_fp64_tflops(double* tflops);
+/* Milliseconds of the same DFMA loop (512 x 128 FMAs per thread, 8 blocks of
+ * 256 threads per SM) when only the first active_lanes (1..32) lanes of each
+ * warp run it: equal times for 1 and 32 lanes mean an FP64 warp instruction
+ * costs its issue slot whatever its active lanes.  No reference counterpart. */
+int32_t ctsmg_measure_fp64_lane_cost(int32_t active_lanes, float* ms_out);
 #ifdef __cplusplus
 }
 #endif
