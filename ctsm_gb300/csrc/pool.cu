@@ -4,9 +4,10 @@
 // one model step through one CUDA graph over filters of the active slots,
 // and finished requests are copied out and their ranges freed.
 //
-// The step is the batch engine's (CanopyFluxes, root sink, SoilTemperature,
-// SoilWater, h2osoi_vol refresh in the order of src/main/clm_driver.F90:766,
-// 900, 950; or SoilWater then SoilTemperature without the canopy), run over
+// The step is the batch engine's (optionally the root moisture stress, then
+// CanopyFluxes, root sink, SoilTemperature, SoilWater, h2osoi_vol refresh in
+// the order of src/main/clm_driver.F90:709, 766, 900, 950; or SoilWater then
+// SoilTemperature without the canopy), run over
 // the filter of active positions the way the reference runs each clump over
 // filter_nolakec / filter_exposedvegp.
 #include <cuda_runtime.h>
@@ -20,6 +21,7 @@
 #include "ctsm_device.cuh"
 #include "soil_kernels.cuh"
 #include "canopy_kernels.cuh"
+#include "rootmoist_kernels.cuh"
 #include "capi_internal.h"
 
 namespace ctsmg {
@@ -77,6 +79,7 @@ struct Pool {
     std::map<std::string, int> index;
     ctsmg_soilwater_io dsw{};
     ctsmg_soiltemp_io dst{};
+    ctsmg_rootmoist_io drm{};
     CanopyArgs cargs{};
     double* rootr = nullptr;
     double* mslope = nullptr;
@@ -122,11 +125,13 @@ static int kind_cap(const Pool* P, int k) {
 static int kind_start(const Request& r, int k) { return patch_kind(k) ? r.p0 : (k == K_GR ? r.g0 : r.c0); }
 static int kind_count(const Request& r, int k) { return patch_kind(k) ? r.np : (k == K_GR ? r.ng : r.nc); }
 
-static void for_tables(int with_canopy, void (*fn)(const FieldDesc&, void*), void* ctx) {
+static void for_tables(int with_canopy, int rootmoist, void (*fn)(const FieldDesc&, void*), void* ctx) {
     for (int i = 0; i < SOILWATER_NFIELDS; ++i) fn(SOILWATER_TABLE[i], ctx);
     for (int i = 0; i < SOILTEMP_NFIELDS; ++i) fn(SOILTEMP_TABLE[i], ctx);
     if (with_canopy)
         for (int i = 0; i < CANOPY_NFIELDS; ++i) fn(CANOPY_TABLE[i], ctx);
+    if (with_canopy && rootmoist)
+        for (int i = 0; i < ROOTMOIST_NFIELDS; ++i) fn(ROOTMOIST_TABLE[i], ctx);
 }
 
 struct SlotBytes { int64_t c = 0, p = 0, g = 0; std::map<std::string, int> seen; };
@@ -141,9 +146,9 @@ static void add_slot_bytes(const FieldDesc& f, void* ctx) {
     else s->c += b;
 }
 
-static void slot_bytes(int with_canopy, int64_t* cb, int64_t* pb, int64_t* gb) {
+static void slot_bytes(int with_canopy, int rootmoist, int64_t* cb, int64_t* pb, int64_t* gb) {
     SlotBytes s;
-    for_tables(with_canopy, add_slot_bytes, &s);
+    for_tables(with_canopy, rootmoist, add_slot_bytes, &s);
     s.c += (int64_t)SOILTEMP_WS_DOUBLES_PER_COL * 8 + 4;            // band scratch, filter entry
     if (with_canopy)       // rootr, Medlyn slope/intercept, filter, iteration record
         s.p += (int64_t)NLEVSOI * 8 + 2 * 8 + 4 + (int64_t)canopy_ws_bytes_per_patch();
@@ -155,9 +160,14 @@ static cudaError_t enqueue_tick(Pool* P) {
     cudaError_t e = cudaSuccess;
     const int nc = P->ncol_act;
     if (P->cfg.with_canopy) {
+        if (P->cfg.rootmoist) {
+            e = launch_rootmoist(P->drm, P->cargs.pft, 1, 1, P->npat_act, P->d_pfilt, P->stream);
+            if (e != cudaSuccess) return e;
+        }
         e = launch_canopy(P->cargs, P->npat_act, P->d_pfilt, P->cfg.dtime, P->counter, P->err, P->cws, P->stream);
         if (e != cudaSuccess) return e;
-        e = launch_rootsink(P->dst.col_patchi, P->dst.col_npatches, P->dst.wtcol, P->cargs.io.qflx_tran_veg, P->rootr,
+        e = launch_rootsink(P->dst.col_patchi, P->dst.col_npatches, P->dst.wtcol, P->cargs.io.qflx_tran_veg,
+                            P->cfg.rootmoist ? P->drm.rootr : P->rootr,
                             P->cfg.patch_capacity, (double*)P->dsw.qflx_rootsoi, nc, P->stream, P->cfg.col_capacity,
                             P->d_cfilt);
         if (e != cudaSuccess) return e;
@@ -238,10 +248,20 @@ using namespace ctsmg;
 
 struct ctsmg_pool_s { Pool* P; };
 
+extern "C" int32_t ctsmg_pool_slot_bytes2(int32_t with_canopy, int32_t rootmoist, int64_t* col_bytes,
+                                          int64_t* patch_bytes, int64_t* grid_bytes) {
+    int64_t c, p, g;
+    slot_bytes(with_canopy, rootmoist, &c, &p, &g);
+    if (col_bytes) *col_bytes = c;
+    if (patch_bytes) *patch_bytes = p;
+    if (grid_bytes) *grid_bytes = g;
+    return 0;
+}
+
 extern "C" int32_t ctsmg_pool_slot_bytes(int32_t with_canopy, int64_t* col_bytes, int64_t* patch_bytes,
                                          int64_t* grid_bytes) {
     int64_t c, p, g;
-    slot_bytes(with_canopy, &c, &p, &g);
+    slot_bytes(with_canopy, 0, &c, &p, &g);
     if (col_bytes) *col_bytes = c;
     if (patch_bytes) *patch_bytes = p;
     if (grid_bytes) *grid_bytes = g;
@@ -256,6 +276,8 @@ extern "C" int32_t ctsmg_pool_create(ctsmg_pool* out, const ctsmg_pool_config* c
     if (!(cfg->dtime > 0.0)) return set_error(CTSMG_E_ARG, "dtime must be positive", 0, 0);
     if (cfg->with_canopy && (!cpar || !pft || cfg->patch_capacity <= 0 || cfg->grid_capacity <= 0))
         return set_error(CTSMG_E_ARG, "with_canopy needs params, pftcon, patch and gridcell capacity", 0, 0);
+    if (cfg->rootmoist && !cfg->with_canopy)
+        return set_error(CTSMG_E_ARG, "rootmoist needs with_canopy", 0, 0);
     const ctsmg_soilwater_movement_nml swm = current_soilwater_nml();
     if (swm.soilwater_movement_method != 0 || swm.use_flexibleCN)
         return set_error(CTSMG_E_UNSUPPORTED, "the serving pool steps the Zeng-Decker form without the flexibleCN fix",
@@ -319,6 +341,11 @@ extern "C" int32_t ctsmg_pool_create(ctsmg_pool* out, const ctsmg_pool_config* c
         P->cargs.medlynintercept_p = P->mint;
         if ((e = cudaMalloc(&P->counter, 256)) != cudaSuccess) return fail(pcuda(e, "counter"));
         if ((e = cudaMalloc(&P->cws, canopy_ws_bytes(PC))) != cudaSuccess) return fail(pcuda(e, "canopy ws"));
+        if (cfg->rootmoist) {
+            P->drm.ldc = CC;
+            P->drm.ldp = PC;
+            if ((rc = add(ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, &P->drm))) return fail(rc);
+        }
     }
     if ((e = cudaMalloc(&P->ws, (size_t)SOILTEMP_WS_DOUBLES_PER_COL * CC * 8)) != cudaSuccess) return fail(pcuda(e, "ws"));
     if ((e = cudaMalloc(&P->err, sizeof(DevError))) != cudaSuccess) return fail(pcuda(e, "err"));
@@ -339,14 +366,28 @@ extern "C" int32_t ctsmg_pool_admit(ctsmg_pool ph, int32_t ncol, int32_t npatch,
                                     const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
                                     const ctsmg_canopy_io* cio, const double* rootr, const double* medlynslope_p,
                                     const double* medlynintercept_p, int32_t* slot_out) {
+    return ctsmg_pool_admit2(ph, ncol, npatch, ngrid, nsteps, sw, st, cio, nullptr, rootr, medlynslope_p,
+                             medlynintercept_p, slot_out);
+}
+
+extern "C" int32_t ctsmg_pool_admit2(ctsmg_pool ph, int32_t ncol, int32_t npatch, int32_t ngrid, int32_t nsteps,
+                                     const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
+                                     const ctsmg_canopy_io* cio, const ctsmg_rootmoist_io* rm, const double* rootr,
+                                     const double* medlynslope_p, const double* medlynintercept_p,
+                                     int32_t* slot_out) {
     if (!ph || !sw || !st || !slot_out) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
     Pool* P = ph->P;
     const bool can = P->cfg.with_canopy != 0;
+    const bool rms = can && P->cfg.rootmoist != 0;
     if (ncol <= 0 || npatch < 0 || ngrid < 0 || nsteps < 1) return set_error(CTSMG_E_ARG, "bad request sizes", 0, 0);
     if (sw->ldc != ncol || st->ldc != ncol || st->ldp != npatch)
         return set_error(CTSMG_E_ARG, "request arrays must be dense: ldc = ncol, ldp = npatch", 0, 0);
-    if (can && (!cio || !rootr || cio->ldc != ncol || cio->ldp != npatch || cio->ldg != ngrid || cio->begg != 1))
+    if (can && (!cio || (!rootr && !rms) || cio->ldc != ncol || cio->ldp != npatch || cio->ldg != ngrid ||
+                cio->begg != 1))
         return set_error(CTSMG_E_ARG, "canopy request needs cio (ldg = ngrid, begg = 1) and rootr", 0, 0);
+    if (rms && (!rm || rm->ldc != ncol || rm->ldp != npatch))
+        return set_error(CTSMG_E_ARG, "a rootmoist pool needs the request's root moisture stress components (dense)",
+                         0, 0);
     for (int c = 0; c < ncol; ++c) {
         const int s = st->snl[c], pi = st->col_patchi[c], np = st->col_npatches[c], nb = st->nbedrock[c];
         if (s > 0 || s < -NLEVSNO) return set_error(CTSMG_E_ARG, "snl outside -nlevsno..0", c + 1, 0);
@@ -424,9 +465,11 @@ extern "C" int32_t ctsmg_pool_admit(ctsmg_pool ph, int32_t ncol, int32_t npatch,
     cudaError_t e = upload(SOILWATER_TABLE, SOILWATER_NFIELDS, sw);
     if (e == cudaSuccess) e = upload(SOILTEMP_TABLE, SOILTEMP_NFIELDS, st);
     if (e == cudaSuccess && can) e = upload(CANOPY_TABLE, CANOPY_NFIELDS, cio);
+    if (e == cudaSuccess && rms) e = upload(ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, rm);
     if (e == cudaSuccess && can && npatch > 0) {
-        e = cudaMemcpy2DAsync(P->rootr + r.p0, (size_t)P->cfg.patch_capacity * 8, rootr, (size_t)npatch * 8,
-                              (size_t)npatch * 8, NLEVSOI, cudaMemcpyHostToDevice, P->copy);
+        if (rootr)
+            e = cudaMemcpy2DAsync(P->rootr + r.p0, (size_t)P->cfg.patch_capacity * 8, rootr, (size_t)npatch * 8,
+                                  (size_t)npatch * 8, NLEVSOI, cudaMemcpyHostToDevice, P->copy);
         ms.resize(npatch); mi.resize(npatch);
         for (int p = 0; p < npatch; ++p) {
             ms[p] = medlynslope_p ? medlynslope_p[p] : P->cargs.pft.medlynslope[cio->itype[p]];
@@ -498,6 +541,12 @@ extern "C" int32_t ctsmg_pool_poll(ctsmg_pool ph, int32_t* slots, int32_t cap, i
 
 extern "C" int32_t ctsmg_pool_evict(ctsmg_pool ph, int32_t slot, const ctsmg_soilwater_io* sw,
                                     const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio, int32_t* steps_done) {
+    return ctsmg_pool_evict2(ph, slot, sw, st, cio, nullptr, steps_done);
+}
+
+extern "C" int32_t ctsmg_pool_evict2(ctsmg_pool ph, int32_t slot, const ctsmg_soilwater_io* sw,
+                                     const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio,
+                                     const ctsmg_rootmoist_io* rm, int32_t* steps_done) {
     if (!ph || !sw || !st) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
     Pool* P = ph->P;
     if (slot < 0 || slot >= (int)P->req.size() || P->req[slot].state == R_FREE)
@@ -507,6 +556,9 @@ extern "C" int32_t ctsmg_pool_evict(ctsmg_pool ph, int32_t slot, const ctsmg_soi
         return set_error(CTSMG_E_ARG, "eviction arrays must be dense like the request", slot, 0);
     if (cio && P->cfg.with_canopy && (cio->ldc != r.nc || cio->ldp != r.np || cio->ldg != r.ng))
         return set_error(CTSMG_E_ARG, "eviction canopy arrays must be dense like the request", slot, 0);
+    const bool rms = rm && P->cfg.with_canopy && P->cfg.rootmoist;
+    if (rms && (rm->ldc != r.nc || rm->ldp != r.np))
+        return set_error(CTSMG_E_ARG, "eviction root moisture arrays must be dense like the request", slot, 0);
     if (r.state == R_RUNNING) {                      // stop after the steps already enqueued
         PK(cudaEventRecord(r.done, P->stream), "done event");
         r.state = R_DONE;
@@ -541,6 +593,7 @@ extern "C" int32_t ctsmg_pool_evict(ctsmg_pool ph, int32_t slot, const ctsmg_soi
     cudaError_t e = download(SOILWATER_TABLE, SOILWATER_NFIELDS, sw);
     if (e == cudaSuccess) e = download(SOILTEMP_TABLE, SOILTEMP_NFIELDS, st);
     if (e == cudaSuccess && cio && P->cfg.with_canopy) e = download(CANOPY_TABLE, CANOPY_NFIELDS, cio);
+    if (e == cudaSuccess && rms) e = download(ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, rm);
     cudaError_t se = cudaStreamSynchronize(P->copy);
     if (e == cudaSuccess) e = se;
     if (e != cudaSuccess) return pcuda(e, "evict copy");

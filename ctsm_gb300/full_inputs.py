@@ -185,6 +185,23 @@ def add_soilfluxes_fields(A, npatch, ngrid):
     return A
 
 
+def snow_free(A):
+    """Workload columns with their snow layers taken away (snl = 0): melted
+    snow layers are removed only by SnowHydrology, outside the path, and a
+    layer that has melted but stays a layer heats without bound in the
+    reference's arithmetic (the oracle shows it within days)."""
+    LS = -abi.NLEVSNO + 1
+    A["snl"][:] = 0
+    for j in range(LS, 1):
+        A["h2osoi_liq"][j - LS] = 0.0
+        A["h2osoi_ice"][j - LS] = 0.0
+        A["dz"][j - LS] = 0.0
+    for k in ("frac_sno_eff", "frac_sno", "snow_depth", "h2osno_no_layers"):
+        if k in A:
+            A[k][:] = 0.0
+    return A
+
+
 def add_rootmoist_fields(A, npatch, rootr, rng=None):
     """Root fractions (levels 1..nlevgrnd, zero below nlevsoi as
     RootBiophysMod leaves them) and zero-filled stress outputs.  rootfr is the

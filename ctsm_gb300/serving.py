@@ -34,7 +34,7 @@ class PoolConfig(C.Structure):
     _fields_ = [("col_capacity", C.c_int32), ("patch_capacity", C.c_int32), ("grid_capacity", C.c_int32),
                 ("dtime", C.c_double), ("e_ice", C.c_double), ("snow_thermal_cond_method", C.c_int32),
                 ("stomatalcond_method", C.c_int32), ("itmax_canopy_fluxes", C.c_int32), ("with_canopy", C.c_int32),
-                ("max_inflight", C.c_int32)]
+                ("max_inflight", C.c_int32), ("rootmoist", C.c_int32)]
 
 
 def _bind(L):
@@ -42,6 +42,12 @@ def _bind(L):
         return
     P = C.POINTER
     L.ctsmg_pool_slot_bytes.argtypes = [C.c_int32, P(C.c_int64), P(C.c_int64), P(C.c_int64)]
+    L.ctsmg_pool_slot_bytes2.argtypes = [C.c_int32, C.c_int32, P(C.c_int64), P(C.c_int64), P(C.c_int64)]
+    L.ctsmg_pool_admit2.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P(abi.SoilWaterIO),
+                                    P(abi.SoilTempIO), P(abi.CanopyIO), P(abi.RootMoistIO), P(C.c_double),
+                                    P(C.c_double), P(C.c_double), P(C.c_int32)]
+    L.ctsmg_pool_evict2.argtypes = [C.c_void_p, C.c_int32, P(abi.SoilWaterIO), P(abi.SoilTempIO), P(abi.CanopyIO),
+                                    P(abi.RootMoistIO), P(C.c_int32)]
     L.ctsmg_pool_create.argtypes = [P(C.c_void_p), P(PoolConfig), P(abi.CanopyParams), P(abi.Pftcon)]
     L.ctsmg_pool_admit.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P(abi.SoilWaterIO),
                                    P(abi.SoilTempIO), P(abi.CanopyIO), P(C.c_double), P(C.c_double), P(C.c_double),
@@ -56,20 +62,20 @@ def _bind(L):
     L._pool_bound = True
 
 
-def slot_bytes(canopy=True):
+def slot_bytes(canopy=True, rootmoist=False):
     """(column, patch, gridcell) device bytes per slot."""
     L = load()
     _bind(L)
     c, p, g = C.c_int64(), C.c_int64(), C.c_int64()
-    check(L.ctsmg_pool_slot_bytes(1 if canopy else 0, C.byref(c), C.byref(p), C.byref(g)))
+    check(L.ctsmg_pool_slot_bytes2(1 if canopy else 0, 1 if rootmoist else 0, C.byref(c), C.byref(p), C.byref(g)))
     return c.value, p.value, g.value
 
 
-def capacities(budget_bytes, canopy=True, patches_per_column=4):
+def capacities(budget_bytes, canopy=True, patches_per_column=4, rootmoist=False):
     """Slot capacities that fit `budget_bytes`: one gridcell and up to
     `patches_per_column` patches per column slot, so patches and gridcells
     never run out before columns do."""
-    c, p, g = slot_bytes(canopy)
+    c, p, g = slot_bytes(canopy, rootmoist)
     per_col = c + patches_per_column * p + g
     ncol = int(budget_bytes // per_col)
     if ncol < 1:
@@ -120,15 +126,22 @@ def _pinned_like(a):
     return np.ascontiguousarray(a), None
 
 
-def make_request(rid, seed, ncol, nsteps, arrival=0.0, pinned=True):
+def make_request(rid, seed, ncol, nsteps, arrival=0.0, pinned=True, physical=False):
     """A request's state from its seed: the full-step inputs (snow, uneven
     bedrock, 1-4 patches per column) with the eight perturbed parameters
     drawn log-uniformly in [0.5, 1.5] times their defaults, as for ensemble
     members (medlynslope / medlynintercept per patch, om_frac_sf in the soil
-    properties; the others are inert on this path)."""
+    properties; the others are inert on this path).  physical: for a pool
+    with the root moisture stress -- the columns without snow layers (melted
+    layers are removed only by SnowHydrology, outside the path) and with the
+    root moisture stress components, so that transpiration follows the soil
+    water and a year-long request stays in the physical domain."""
     r = np.random.Generator(np.random.Philox(seed))
     factors = {k: float(np.exp(r.uniform(np.log(0.5), np.log(1.5)))) for k in full_inputs.ENSEMBLE_PARAMS}
     A, npatch, ngrid, rootr = full_inputs.full_state(ncol, om_frac_sf=factors["om_frac_sf"], rng=r)
+    if physical:
+        full_inputs.snow_free(A)
+        full_inputs.add_rootmoist_fields(A, npatch, rootr, rng=r)
     pft = canopy_inputs.DEFAULT_PFT
     it = A["itype"]
     A["medlynslope_p"] = np.array([row[6] for row in pft])[it] * factors["medlynslope"]
@@ -161,10 +174,11 @@ def stream_draws(n, rate, seed=0, cols=(1, 50000), steps=(48, 17520)):
     return arr, ncols, lens, seeds
 
 
-def request_stream(n, rate, seed=0, cols=(1, 50000), steps=(48, 17520), pinned=True):
+def request_stream(n, rate, seed=0, cols=(1, 50000), steps=(48, 17520), pinned=True, physical=False):
     """n requests drawn by stream_draws, each with its state."""
     arr, ncols, lens, seeds = stream_draws(n, rate, seed, cols, steps)
-    return [make_request(i, int(seeds[i]), int(ncols[i]), int(lens[i]), float(arr[i]), pinned) for i in range(n)]
+    return [make_request(i, int(seeds[i]), int(ncols[i]), int(lens[i]), float(arr[i]), pinned, physical)
+            for i in range(n)]
 
 
 class Pool:
@@ -173,17 +187,18 @@ class Pool:
 
     def __init__(self, budget_bytes=None, col_capacity=None, canopy=True, dtime=1800.0, e_ice=6.0,
                  snow_thermal_cond_method=0, stomatalcond_method=1, itmax=40, params=None, pftcon=None,
-                 max_inflight=2, patches_per_column=4):
+                 max_inflight=2, patches_per_column=4, rootmoist=False):
         self.L = load()
         _bind(self.L)
         if col_capacity is None:
-            cc, pc, gc = capacities(budget_bytes, canopy, patches_per_column)
+            cc, pc, gc = capacities(budget_bytes, canopy, patches_per_column, rootmoist)
         else:
             cc, pc, gc = col_capacity, patches_per_column * col_capacity, col_capacity
         self.capacity = (cc, pc, gc)
         self.canopy = canopy
+        self.rootmoist = bool(rootmoist and canopy)
         cfg = PoolConfig(cc, pc, gc, dtime, e_ice, snow_thermal_cond_method, stomatalcond_method, itmax,
-                         1 if canopy else 0, max_inflight)
+                         1 if canopy else 0, max_inflight, 1 if self.rootmoist else 0)
         self._par = params if params is not None else canopy_inputs.make_params()
         self._pft = pftcon if pftcon is not None else canopy_inputs.make_pftcon()
         self.h = C.c_void_p()
@@ -194,18 +209,19 @@ class Pool:
         sw = abi.make_io(abi.SoilWaterIO, abi.SOILWATER_FIELDS, A, n)
         st = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, A, n, npch)
         ci = abi.make_io(abi.CanopyIO, abi.CANOPY_FIELDS, A, n, npch, ng, 1) if self.canopy else None
-        return sw, st, ci
+        rm = abi.make_io(abi.RootMoistIO, abi.ROOTMOIST_FIELDS, A, n, npch) if self.rootmoist else None
+        return sw, st, ci, rm
 
     def admit(self, q):
         """Admits request q; returns its slot, or None when the pool is full."""
-        sw, st, ci = self._ios(q)
+        sw, st, ci, rm = self._ios(q)
         dp = C.POINTER(C.c_double)
         slot = C.c_int32()
         ms = q.state["medlynslope_p"].ctypes.data_as(dp) if "medlynslope_p" in q.state else None
         mi = q.state["medlynintercept_p"].ctypes.data_as(dp) if "medlynintercept_p" in q.state else None
-        rc = self.L.ctsmg_pool_admit(self.h, q.ncol, q.npatch, q.ngrid, q.nsteps, C.byref(sw), C.byref(st),
-                                     C.byref(ci) if ci is not None else None,
-                                     q.rootr.ctypes.data_as(dp) if self.canopy else None, ms, mi, C.byref(slot))
+        rc = self.L.ctsmg_pool_admit2(self.h, q.ncol, q.npatch, q.ngrid, q.nsteps, C.byref(sw), C.byref(st),
+                                      C.byref(ci) if ci is not None else None, C.byref(rm) if rm is not None else None,
+                                      q.rootr.ctypes.data_as(dp) if self.canopy else None, ms, mi, C.byref(slot))
         if rc == E_FULL:
             return None
         check(rc)
@@ -226,10 +242,11 @@ class Pool:
     def evict(self, q):
         """Copies q's final state into q.state and frees its slots; returns
         the number of steps it ran."""
-        sw, st, ci = self._ios(q)
+        sw, st, ci, rm = self._ios(q)
         steps = C.c_int32()
-        check(self.L.ctsmg_pool_evict(self.h, q.slot, C.byref(sw), C.byref(st),
-                                      C.byref(ci) if ci is not None else None, C.byref(steps)))
+        check(self.L.ctsmg_pool_evict2(self.h, q.slot, C.byref(sw), C.byref(st),
+                                       C.byref(ci) if ci is not None else None,
+                                       C.byref(rm) if rm is not None else None, C.byref(steps)))
         q.steps_done = steps.value
         q.slot = -1
         return steps.value
@@ -359,13 +376,16 @@ def main(argv=None):
     p.add_argument("--budget-gb", type=float, default=150.0, help="device memory budget of the pool")
     p.add_argument("--time-limit", type=float, default=None, help="seconds; default: run to completion")
     p.add_argument("--out", default=None, help="JSON file for the statistics and per-request records")
+    p.add_argument("--cols-max", type=int, default=50000, help="largest request (columns)")
+    p.add_argument("--plain", action="store_true",
+                   help="the step without the root moisture stress, on the workload's snowy columns")
     a = p.parse_args(argv)
     from . import soil
     soil.init()
     t0 = time.time()
-    reqs = request_stream(a.requests, a.rate, seed=a.seed)
+    reqs = request_stream(a.requests, a.rate, seed=a.seed, cols=(1, a.cols_max), physical=not a.plain)
     gen_s = time.time() - t0
-    pool = Pool(budget_bytes=a.budget_gb * 1e9)
+    pool = Pool(budget_bytes=a.budget_gb * 1e9, rootmoist=not a.plain)
     try:
         st = serve(pool, reqs, time_limit=a.time_limit)
     finally:
@@ -379,6 +399,8 @@ def main(argv=None):
             recs.append(dict(rid=q.rid, ncol=q.ncol, nsteps=q.nsteps, days=q.days, arrival=q.arrival,
                              admit=q.t_admit, done=q.t_done, s_per_day=(q.t_done - q.arrival) / q.days,
                              finite=bool(np.isfinite(A["t_soisno"]).all() and np.isfinite(A["t_veg"]).all()),
+                             nonfinite_columns=q.extra.get("nonfinite_columns", 0),
+                             liq_min=float(A["h2osoi_liq"][abi.NLEVSNO:abi.NLEVSNO + abi.NLEVSOI].min()),
                              itmax_frac=float((A["num_iter"] >= 40).mean())))
         with open(a.out, "w") as f:
             json.dump({"stats": st, "requests": recs}, f)

@@ -10,7 +10,7 @@ import pytest
 
 from ctsm_gb300 import serving
 from oracle.steps import full_steps
-from tests.parity import compare, noise_spread
+from tests.parity import compare, noise_spread, evap_veg_rounding_bound
 
 pytestmark = pytest.mark.gpu
 OUT = ["h2osoi_liq", "h2osoi_ice", "t_soisno", "t_grnd", "h2osoi_vol", "t_veg", "eflx_sh_veg", "qflx_evap_veg",
@@ -115,3 +115,57 @@ def test_stopped_request_and_refusal(gpu_lib):
     assert pool.largest_free() == before
     pool.close()
     _same(G.state, _batch(q, 4))
+
+
+def test_rootmoist_pool_matches_batch_and_oracle(gpu_lib):
+    """A pool with the root moisture stress (btran and rootr from the soil
+    state at the start of every tick, CanopyFluxesMod.F90:709): a snow-free
+    request alone in the pool equals the resident batch with rootmoist bit
+    for bit, and the oracle stepped the same way within the parity tolerance;
+    the stress outputs come back with the request."""
+    from ctsm_gb300.engine import SoilBatch
+    q = serving.make_request(0, 515, 240, 4, pinned=False, physical=True)
+    assert (q.state["snl"] == 0).all() and "rootfr" in q.state
+    A = {k: np.array(v, copy=True) for k, v in q.state.items()}
+    G = _clone(q)
+    pool = serving.Pool(col_capacity=1024, rootmoist=True)
+    st = serving.serve(pool, [G], tick_clock=True)
+    pool.close()
+    assert st["completed"] == 1 and G.steps_done == 4
+    B = {k: np.array(v, copy=True) for k, v in q.state.items()}
+    b = SoilBatch(B, q.npatch, canopy=True, ngrid=q.ngrid, per_patch_medlyn=True, rootmoist=True)
+    b.run(4)
+    b.sync()
+    b.download()
+    b.close()
+    _same(G.state, B, OUT + ["btran", "rootr", "rresis"])
+    R = copy.deepcopy(A)
+    run = lambda S: full_steps(S, q.npatch, q.ngrid, q.rootr, 4, medlyn_per_patch=True, rootmoist=True)
+    run(R)
+    spread = noise_spread(run, A, R, fields=CANCEL + ("qflx_evap_veg",), input_ulps=4)
+    for k in ("liqcan", "snocan"):
+        spread[k] = spread[k] + 1e-9 * (np.abs(A["liqcan"]) + np.abs(A["snocan"]))
+    # near saturation the sign of efpot is set by rounding (see parity.evap_veg_rounding_bound)
+    spread["qflx_evap_veg"] = spread["qflx_evap_veg"] + evap_veg_rounding_bound(R)
+    errs, bad = compare(G.state, R, OUT[:22] + ["btran"], 1e-9, spread)
+    assert not bad, {k: errs[k] for k in bad}
+
+
+def test_physical_stream_stays_finite(gpu_lib):
+    """Year-long requests through the root-moisture pool stay in the physical
+    domain: 6 requests of 40..400 columns, 17,520 steps (a simulated year)
+    each, every final state finite, no negative soil liquid, temperatures in
+    range."""
+    reqs = serving.request_stream(6, 0.0, seed=99, cols=(40, 400), steps=(17520, 17520), pinned=False,
+                                  physical=True)
+    pool = serving.Pool(col_capacity=4096, rootmoist=True)
+    st = serving.serve(pool, reqs, tick_clock=True)
+    pool.close()
+    assert st["completed"] == 6
+    for q in reqs:
+        A = q.state
+        assert q.extra["nonfinite_columns"] == 0, q.rid
+        soil = A["h2osoi_liq"][serving.abi.NLEVSNO:serving.abi.NLEVSNO + serving.abi.NLEVSOI]
+        assert soil.min() >= -1e-9, (q.rid, float(soil.min()))
+        T = A["t_soisno"][serving.abi.NLEVSNO:]
+        assert 200.0 < T.min() and T.max() < 350.0, (q.rid, float(T.min()), float(T.max()))

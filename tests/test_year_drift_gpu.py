@@ -151,18 +151,8 @@ def test_month_full_step_drift_and_balance(gpu_lib):
 
 
 def snow_free(A):
-    """Workload columns with their snow layers taken away (snl = 0): melted
-    snow layers are removed only by SnowHydrology, outside the path, and a
-    layer that has melted but stays a layer heats without bound in the
-    reference's arithmetic (the oracle shows it within days)."""
-    A["snl"][:] = 0
-    for j in range(LS, 1):
-        A["h2osoi_liq"][j - LS] = 0.0
-        A["h2osoi_ice"][j - LS] = 0.0
-        A["dz"][j - LS] = 0.0
-    for k in ("frac_sno_eff", "frac_sno", "snow_depth", "h2osno_no_layers"):
-        A[k][:] = 0.0
-    return A
+    """The workload columns without snow layers (full_inputs.snow_free)."""
+    return fi.snow_free(A)
 
 
 def test_year_clm5_step_drift(gpu_lib):
