@@ -853,7 +853,8 @@ int32_t ctsmg_batch_autotune(ctsmg_batch b, int32_t trial_steps, int32_t* block_
  * the caller's order -- which decides how uniform the level loops and
  * branches of a warp's 32 lanes are.  With the moisture form, its persistent
  * sub-step kernel takes the columns either bucketed by the sub-step count of
- * the previous step and the bedrock depth (rebuilt on the device every step)
+ * the previous step, heaviest first, each block of positions in order within
+ * a bucket (rebuilt on the device every step)
  * or in position order.  Every candidate is timed at 64, 128 and 256 threads
  * per block over trial_steps steps of the batch's own data, the fastest is
  * kept (the resident columns are moved into its order on the device) and the
@@ -870,7 +871,8 @@ int32_t ctsmg_batch_autotune2(ctsmg_batch b, int32_t trial_steps, int32_t* block
                               int32_t* mf_sort_out, float* ms_out, int32_t* ncand_out);
 const char* ctsmg_batch_order_name(int32_t order);
 /* The moisture-form work order of a batch with the moisture form: 1 buckets
- * the columns by the previous step's sub-step count and bedrock depth, 0
+ * the columns by the previous step's sub-step count (heaviest first, each
+ * block of 128 positions in order within a bucket), 0
  * takes them in position order (the default).  Results do not depend on it. */
 int32_t ctsmg_batch_set_mf_order(ctsmg_batch b, int32_t sorted);
 int32_t ctsmg_batch_set_block(ctsmg_batch b, int32_t block);
@@ -908,6 +910,9 @@ typedef struct {
     int32_t snow_thermal_cond_method, stomatalcond_method, itmax_canopy_fluxes;
     int32_t with_canopy;
     int32_t max_inflight;     /* ticks queued ahead of the device (>= 1)      */
+    int32_t rootmoist;        /* 1: each tick starts with the root moisture
+                                 stress (btran, rootr from the soil state;
+                                 needs with_canopy and ctsmg_pool_admit2)  */
 } ctsmg_pool_config;
 
 #define CTSMG_E_FULL          11   /* pool: no free range large enough (nothing changed) */
@@ -916,6 +921,9 @@ typedef struct {
  * scratch, filters, root fractions, per-patch Medlyn parameters), for sizing
  * the capacities from a memory budget.                                      */
 int32_t ctsmg_pool_slot_bytes(int32_t with_canopy, int64_t* col_bytes, int64_t* patch_bytes, int64_t* grid_bytes);
+/* The same for a pool with the root moisture stress (rootmoist = 1). */
+int32_t ctsmg_pool_slot_bytes2(int32_t with_canopy, int32_t rootmoist, int64_t* col_bytes, int64_t* patch_bytes,
+                               int64_t* grid_bytes);
 /* cpar / pft may be NULL when with_canopy = 0. */
 int32_t ctsmg_pool_create(ctsmg_pool* out, const ctsmg_pool_config* cfg, const ctsmg_canopy_params* cpar,
                           const ctsmg_pftcon* pft);
@@ -930,6 +938,13 @@ int32_t ctsmg_pool_admit(ctsmg_pool p, int32_t ncol, int32_t npatch, int32_t ngr
                          const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio,
                          const double* rootr, const double* medlynslope_p, const double* medlynintercept_p,
                          int32_t* slot_out);
+/* ctsmg_pool_admit for a pool with rootmoist = 1: rm holds the request's
+ * root moisture stress components (dense like the others; rootr may then be
+ * NULL -- the tick computes it). */
+int32_t ctsmg_pool_admit2(ctsmg_pool p, int32_t ncol, int32_t npatch, int32_t ngrid, int32_t nsteps,
+                          const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio,
+                          const ctsmg_rootmoist_io* rm, const double* rootr, const double* medlynslope_p,
+                          const double* medlynintercept_p, int32_t* slot_out);
 /* Enqueue one step of every running request (returns at once unless
  * max_inflight ticks are already queued).  *ncol_stepped (may be NULL) is
  * the number of columns the tick advances. */
@@ -942,6 +957,10 @@ int32_t ctsmg_pool_poll(ctsmg_pool p, int32_t* slots, int32_t cap, int32_t* n);
  * (may be NULL) is the number of steps it ran. */
 int32_t ctsmg_pool_evict(ctsmg_pool p, int32_t slot, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
                          const ctsmg_canopy_io* cio, int32_t* steps_done);
+/* ctsmg_pool_evict that also returns the root moisture stress components
+ * (rm may be NULL). */
+int32_t ctsmg_pool_evict2(ctsmg_pool p, int32_t slot, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
+                          const ctsmg_canopy_io* cio, const ctsmg_rootmoist_io* rm, int32_t* steps_done);
 /* Wait for the device; reports a band-solve or CanopyFluxes failure as its
  * status with the request slot in ctsmg_last_error_index and the column (or
  * patch) within the request in the level slot. */
