@@ -853,8 +853,7 @@ int32_t ctsmg_batch_autotune(ctsmg_batch b, int32_t trial_steps, int32_t* block_
  * the caller's order -- which decides how uniform the level loops and
  * branches of a warp's 32 lanes are.  With the moisture form, its persistent
  * sub-step kernel takes the columns either bucketed by the sub-step count of
- * the previous step, heaviest first, each block of positions in order within
- * a bucket (rebuilt on the device every step)
+ * the previous step and the bedrock depth (rebuilt on the device every step)
  * or in position order.  Every candidate is timed at 64, 128 and 256 threads
  * per block over trial_steps steps of the batch's own data, the fastest is
  * kept (the resident columns are moved into its order on the device) and the
@@ -871,8 +870,7 @@ int32_t ctsmg_batch_autotune2(ctsmg_batch b, int32_t trial_steps, int32_t* block
                               int32_t* mf_sort_out, float* ms_out, int32_t* ncand_out);
 const char* ctsmg_batch_order_name(int32_t order);
 /* The moisture-form work order of a batch with the moisture form: 1 buckets
- * the columns by the previous step's sub-step count (heaviest first, each
- * block of 128 positions in order within a bucket), 0
+ * the columns by the previous step's sub-step count and bedrock depth, 0
  * takes them in position order (the default).  Results do not depend on it. */
 int32_t ctsmg_batch_set_mf_order(ctsmg_batch b, int32_t sorted);
 int32_t ctsmg_batch_set_block(ctsmg_batch b, int32_t block);

@@ -212,8 +212,8 @@ def test_mf_work_orders_give_identical_bits(soil_mf):
     for mode in ("sorted", "positions", "tuned"):
         G = copy.deepcopy(A)
         b = SoilBatch(G, npatch, dtime=DT)
-        if mode == "positions":
-            b.set_mf_order(False)
+        if mode != "tuned":
+            b.set_mf_order(mode == "sorted")
         b.run(2)
         if mode == "tuned":
             t = b.tune(trial_steps=1)
