@@ -1197,6 +1197,27 @@ static int32_t* order_buffer(ThreadCtx* c, size_t n) {
     return c->order;
 }
 
+// Filter entries [f0, f1) grouped by water-table depth in 0.25 m bins (a
+// stable counting sort) into out[f0..f1): the Zeng-Decker solve branches on
+// the level that holds the water table, so a warp whose columns share it
+// runs one branch per level.
+static void group_by_water_table(const int32_t* filt, int f0, int f1, const double* zwt, int begc, int32_t* out) {
+    if (!CTSMG_GROUP_COLUMNS) {
+        std::memcpy(out + f0, filt + f0, (size_t)(f1 - f0) * sizeof(int32_t));
+        return;
+    }
+    constexpr int NK = 64;
+    int count[NK + 1];
+    std::memset(count, 0, sizeof count);
+    auto key = [&](int32_t col) {
+        const double z = zwt[col - begc] * 4.0;
+        return (z >= 0.0 && z < (double)(NK - 1)) ? (int)z : NK - 1;    // deeper, negative or NaN: last bin
+    };
+    for (int i = f0; i < f1; ++i) ++count[key(filt[i]) + 1];
+    for (int k = 0; k < NK; ++k) count[k + 1] += count[k];
+    for (int i = f0; i < f1; ++i) out[f0 + count[key(filt[i])]++] = filt[i];
+}
+
 // Filter entries [f0, f1) grouped by snow layers, then bedrock depth (deepest
 // first; a stable counting sort) into out[f0..f1): a warp of the heat-solve
 // kernel then takes columns whose level loops have the same lengths, as the
@@ -1435,11 +1456,34 @@ extern "C" int32_t ctsmg_soilwater(const ctsmg_bounds* bounds, int32_t num_hydro
         stage_alloc(c, io, &dio, sizeof dio, T, NT, ldc, 0);
         gather_setup(c, io, &dio, T, NT, ldc, 0);
         int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_hydrologyc * 4);
-        e = copy_async(dfilt, filter_hydrologyc, (size_t)num_hydrologyc * 4, cudaMemcpyHostToDevice, in_stream(c));
-        if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
+        // the Zeng-Decker form takes each chunk's columns grouped by
+        // water-table depth (sorted on the host while the chunk's copies run);
+        // the moisture form's persistent kernel takes them in filter order
+        const bool zd = nml.soilwater_movement_method == 0;
+        int32_t* hord = zd ? order_buffer(c, (size_t)num_hydrologyc) : nullptr;
+        if (zd && !hord) return set_error(CTSMG_E_CUDA, "cudaMallocHost(work order)", 0, 0);
+        if (!zd) {
+            e = copy_async(dfilt, filter_hydrologyc, (size_t)num_hydrologyc * 4, cudaMemcpyHostToDevice,
+                           in_stream(c));
+            if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync(filter)");
+        }
+        auto sw_chunk_in = [&](int k) -> int {
+            const Chunk& ch = chunks[k];
+            if (!zd) return chunk_in(c, ch, k, io, &dio, T, NT, ldc, 0);
+            trace_mark(c, k, 0, in_stream(c));
+            int r = chunk_copies_in(c, ch, io, &dio, T, NT, ldc, 0);
+            if (r) return r;
+            group_by_water_table(filter_hydrologyc, ch.f0, ch.f1, io->zwt, bounds->begc, hord);
+            cudaError_t ce = copy_async(dfilt + ch.f0, hord + ch.f0, (size_t)(ch.f1 - ch.f0) * 4,
+                                        cudaMemcpyHostToDevice, in_stream(c));
+            if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemcpyAsync(filter)");
+            trace_mark(c, k, 1, in_stream(c));
+            ce = cudaEventRecord(c->ev_in[k], in_stream(c));
+            return ce == cudaSuccess ? 0 : cuda_fail(ce, "cudaEventRecord");
+        };
         const int K = (int)chunks.size();
         if ((rc = fork_streams(c))) return rc;
-        if ((rc = chunk_in(c, chunks[0], 0, io, &dio, T, NT, ldc, 0))) return rc;
+        if ((rc = sw_chunk_in(0))) return rc;
         for (int k = 0; k < K; ++k) {
             const Chunk& ch = chunks[k];
             cudaStream_t ks = chunk_stream(c, k);
@@ -1451,7 +1495,7 @@ extern "C" int32_t ctsmg_soilwater(const ctsmg_bounds* bounds, int32_t num_hydro
             if (e != cudaSuccess) return cuda_fail(e, "soilwater kernel launch");
             trace_mark(c, k, 3, ks);
             if ((e = cudaEventRecord(c->ev_done[k], ks)) != cudaSuccess) return cuda_fail(e, "record");
-            if (k + 1 < K && (rc = chunk_in(c, chunks[k + 1], k + 1, io, &dio, T, NT, ldc, 0))) return rc;
+            if (k + 1 < K && (rc = sw_chunk_in(k + 1))) return rc;
             if ((rc = chunk_out(c, ch, k, io, &dio, T, NT, ldc, 0))) return rc;
         }
         c->gather = false;
