@@ -52,6 +52,7 @@ struct Batch {
     double* mint = nullptr;
     int* counter = nullptr;
     int* mf_work = nullptr;        // work counter and work order of the persistent moisture-form kernel
+    void* mf_compact = nullptr;    // the moisture form's components moved into the work order
     bool mf_sort = false;          // its columns bucketed by previous sub-steps and bedrock depth
     double* cws = nullptr;         // CanopyFluxes iteration records
     int32_t* d_perm = nullptr;     // sorted position -> original column index (0-based)
@@ -116,7 +117,7 @@ static cudaError_t enqueue_step(Batch* b) {
     auto water_step = [&](int refresh) {
         if (mf)
             return launch_mf_step(b->dsw, ncol, b->mfa, b->swm.use_flexibleCN, refresh, b->err, nullptr, b->stream,
-                                  b->mf_work, hy, b->mf_sort);
+                                  b->mf_work, hy, b->mf_sort, b->mf_compact);
         return launch_zd09_step(b->dsw, ncol, b->cfg.e_ice, b->cfg.dtime, b->swm.use_flexibleCN, refresh, nullptr,
                                 b->stream, hy);
     };
@@ -156,7 +157,7 @@ static void batch_free(Batch* b) {
     for (auto& f : b->fields) if (f.dptr) cudaFree(f.dptr);
     for (void* p : {(void*)b->d_perm, (void*)b->ws, (void*)b->err, b->snapshot, (void*)b->rootr, (void*)b->mslope,
                     (void*)b->mint, (void*)b->counter, (void*)b->cws, b->bal_mem, (void*)b->hyd_params, (void*)b->dmax_c,
-                    (void*)b->mf_work})
+                    (void*)b->mf_work, b->mf_compact})
         if (p) cudaFree(p);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
@@ -478,7 +479,8 @@ extern "C" int32_t ctsmg_batch_open(ctsmg_batch* out, const ctsmg_batch_config* 
             b->bal.th2osfc_bef = const_cast<double*>(b->dsf.t_h2osfc_bef);
         }
     }
-    if (swm.soilwater_movement_method == 1 && (e = cudaMalloc(&b->mf_work, mf_work_bytes(ncol))) != cudaSuccess)
+    if (swm.soilwater_movement_method == 1 && ((e = cudaMalloc(&b->mf_work, mf_work_bytes(ncol))) != cudaSuccess ||
+                                                (e = cudaMalloc(&b->mf_compact, mf_compact_bytes(ncol))) != cudaSuccess))
         return fail(cuda_err(e, "moisture-form work order"));
     for (auto& f : b->fields) b->state_bytes += f.bytes;
     if ((e = cudaMalloc(&b->ws, (size_t)SOILTEMP_WS_DOUBLES_PER_COL * ncol * 8)) != cudaSuccess) return fail(cuda_err(e, "ws"));

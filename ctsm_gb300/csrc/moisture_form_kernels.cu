@@ -17,6 +17,7 @@
 // element is dgtsv's.
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <type_traits>
 #include <cooperative_groups.h>
 #include "ctsm_device.cuh"
 #include "soil_math.cuh"
@@ -480,16 +481,122 @@ __global__ void __launch_bounds__(128) mf_order_kernel(int ncol, int* work) {
 template <bool EXPENSIVE>
 __global__ void __launch_bounds__(128)
 mf_core_kernel(ctsmg_soilwater_io io, int ncol, MoistureFormArgs P, DevError* err, const int32_t* __restrict__ filt,
-               int* counter, const int* __restrict__ order) {
+               int* counter, const int* __restrict__ order, int compact) {
+    // compact: io holds the columns of the work order at positions 0..ncol-1
+    // (order maps a position back to its filter position, for errors)
     mf_persistent<EXPENSIVE>(io, ncol, counter, P,
                   [&](int fc) {
+                      if (compact) return fc;
                       const int p = order ? order[fc] : fc;
                       return filt ? filt[p] - 1 : p;
                   },
                   [&](int fc, int c, int st, int info) {
-                      if (st == MF_SINGULAR) report_error(err, c + 1, info, CTSMG_E_SINGULAR);
-                      else if (st == MF_NOT_DONE) report_error(err, c + 1, 0, CTSMG_E_TIMEOUT);
+                      int col = c;
+                      if (compact) {
+                          const int q = order[c];
+                          col = filt ? filt[q] - 1 : q;
+                      }
+                      if (st == MF_SINGULAR) report_error(err, col + 1, info, CTSMG_E_SINGULAR);
+                      else if (st == MF_NOT_DONE) report_error(err, col + 1, 0, CTSMG_E_TIMEOUT);
                   });
+}
+
+// Compact mode: the components the sub-step kernel reads and writes, moved
+// for the columns of the work order into a workspace in that order (a warp's
+// columns then sit side by side in memory and run level loops of one length),
+// and the written ones moved back afterwards.  Each move copies rows
+// [row0, row0 + rows) of one component; the workspace arrays have the
+// component's own row layout with the work order's length as leading
+// dimension, so the kernel's indexing is unchanged.
+struct MfMove {
+    char* orig;             // the component (the step's leading dimension)
+    char* work;             // its workspace copy (leading dimension ncol)
+    int row0, rows, esize, out;
+};
+struct MfMoves {
+    MfMove m[MF_MOVES];
+    int n;
+};
+
+__global__ void __launch_bounds__(128)
+mf_move_kernel(MfMoves mv, int n, int ld, const int* __restrict__ order, const int32_t* __restrict__ filt, int back) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int q = order[p];
+    const int c = filt ? filt[q] - 1 : q;
+    for (int i = 0; i < mv.n; ++i) {
+        const MfMove& M = mv.m[i];
+        if (back && !M.out) continue;
+        for (int r = M.row0; r < M.row0 + M.rows; ++r) {
+            const size_t o = (size_t)r * ld + c, w = (size_t)r * n + p;
+            if (M.esize == 8) {
+                double* a = reinterpret_cast<double*>(M.orig);
+                double* b = reinterpret_cast<double*>(M.work);
+                if (back) a[o] = b[w];
+                else b[w] = a[o];
+            } else {
+                int32_t* a = reinterpret_cast<int32_t*>(M.orig);
+                int32_t* b = reinterpret_cast<int32_t*>(M.work);
+                if (back) a[o] = b[w];
+                else b[w] = a[o];
+            }
+        }
+    }
+}
+
+namespace {
+// The moves of compact mode and the workspace io (pointers into `ws`, which
+// holds mf_compact_bytes(ncol) bytes): sets cio and mv, returns the bytes used.
+size_t mf_compact_layout(const ctsmg_soilwater_io& io, int ncol, char* ws, ctsmg_soilwater_io* cio, MfMoves* mv) {
+    constexpr int SS = NLEVSNO + NLEVGRND, ZI = NLEVSNO + NLEVGRND + 1;
+    *cio = io;
+    cio->ldc = ncol;
+    mv->n = 0;
+    size_t off = 0;
+    auto add = [&](auto*& dptr, auto* optr, int kind_rows, int row0, int rows, int esize, int out) {
+        char* w = ws ? ws + off : nullptr;
+        off += ((size_t)kind_rows * ncol * esize + 255) / 256 * 256;
+        if (!ws) return;
+        MfMove& M = mv->m[mv->n++];
+        M.orig = reinterpret_cast<char*>(const_cast<void*>(static_cast<const void*>(optr)));
+        M.work = w;
+        M.row0 = row0;
+        M.rows = rows;
+        M.esize = esize;
+        M.out = out;
+        using T = std::remove_reference_t<decltype(dptr)>;
+        dptr = reinterpret_cast<T>(w);
+    };
+    // levels 1..nlevsoi of the snow+soil and interface components
+    add(cio->z, io.z, SS, NLEVSNO, NLEVSOI, 8, 0);
+    add(cio->dz, io.dz, SS, NLEVSNO, NLEVSOI, 8, 0);
+    add(cio->h2osoi_liq, io.h2osoi_liq, SS, NLEVSNO, NLEVSOI, 8, 1);
+    add(cio->zi, io.zi, ZI, NLEVSNO, NLEVSOI + 1, 8, 0);
+    add(cio->watsat, io.watsat, NLEVGRND, 0, NLEVSOI, 8, 0);
+    add(cio->sucsat, io.sucsat, NLEVGRND, 0, NLEVSOI, 8, 0);
+    add(cio->bsw, io.bsw, NLEVGRND, 0, NLEVSOI, 8, 0);
+    add(cio->hksat, io.hksat, NLEVGRND, 0, NLEVSOI, 8, 0);
+    add(cio->eff_porosity, io.eff_porosity, NLEVGRND, 0, NLEVSOI, 8, 0);
+    add(cio->icefrac, io.icefrac, NLEVGRND, 0, NLEVSOI, 8, 0);
+    add(cio->smp_l, io.smp_l, NLEVGRND, 0, NLEVSOI, 8, 1);
+    add(cio->hk_l, io.hk_l, NLEVGRND, 0, NLEVSOI, 8, 1);
+    add(cio->qflx_rootsoi, io.qflx_rootsoi, NLEVSOI, 0, NLEVSOI, 8, 0);
+    add(cio->qin, io.qin, NLEVSOI, 0, NLEVSOI, 8, 1);
+    add(cio->qout, io.qout, NLEVSOI, 0, NLEVSOI, 8, 1);
+    add(cio->zwt, io.zwt, 1, 0, 1, 8, 0);
+    add(cio->smpmin, io.smpmin, 1, 0, 1, 8, 0);
+    add(cio->qflx_infl, io.qflx_infl, 1, 0, 1, 8, 0);
+    add(cio->qcharge, io.qcharge, 1, 0, 1, 8, 1);
+    add(cio->num_substeps, io.num_substeps, 1, 0, 1, 8, 1);
+    add(cio->nbedrock, io.nbedrock, 1, 0, 1, 4, 0);
+    return off;
+}
+} // namespace
+
+size_t mf_compact_bytes(int ncol) {
+    ctsmg_soilwater_io io{}, cio{};
+    MfMoves mv;
+    return mf_compact_layout(io, ncol > 0 ? ncol : 0, nullptr, &cio, &mv);
 }
 
 template <bool HYDRO>
@@ -524,7 +631,7 @@ static int persistent_blocks(K kernel, int n) {
 
 cudaError_t launch_mf_step(const ctsmg_soilwater_io& io, int ncol, const MoistureFormArgs& P, int flexcn, int refresh,
                            DevError* err, const int32_t* d_filt, cudaStream_t s, int* d_work,
-                           const HydroStepArgs* hy, bool sorted) {
+                           const HydroStepArgs* hy, bool sorted, void* d_compact) {
     if (ncol <= 0) return cudaSuccess;
     const int nb = (ncol + 127) / 128;
     const HydroStepArgs none{};
@@ -536,16 +643,25 @@ cudaError_t launch_mf_step(const ctsmg_soilwater_io& io, int ncol, const Moistur
     else if (sorted) mf_pre_kernel<false, true><<<nb, 128, 0, s>>>(io, ncol, P.dtime, d_filt, ha, d_work);
     else mf_pre_kernel<false, false><<<nb, 128, 0, s>>>(io, ncol, P.dtime, d_filt, ha, d_work);
     const int* order = nullptr;
+    const bool compact = sorted && d_compact;
+    ctsmg_soilwater_io cio = io;
+    MfMoves mv;
+    mv.n = 0;
     if (sorted) {
         mf_order_kernel<<<nb, 128, 0, s>>>(ncol, d_work);
         order = mf_order_of(d_work, ncol).order;
     }
+    if (compact) {
+        mf_compact_layout(io, ncol, static_cast<char*>(d_compact), &cio, &mv);
+        mf_move_kernel<<<nb, 128, 0, s>>>(mv, ncol, io.ldc, order, d_filt, 0);
+    }
     if (P.expensive)
-        mf_core_kernel<true><<<persistent_blocks(mf_core_kernel<true>, ncol), 128, 0, s>>>(io, ncol, P, err, d_filt,
-                                                                                          d_work, order);
+        mf_core_kernel<true><<<persistent_blocks(mf_core_kernel<true>, ncol), 128, 0, s>>>(
+            cio, ncol, P, err, d_filt, d_work, order, compact ? 1 : 0);
     else
-        mf_core_kernel<false><<<persistent_blocks(mf_core_kernel<false>, ncol), 128, 0, s>>>(io, ncol, P, err, d_filt,
-                                                                                            d_work, order);
+        mf_core_kernel<false><<<persistent_blocks(mf_core_kernel<false>, ncol), 128, 0, s>>>(
+            cio, ncol, P, err, d_filt, d_work, order, compact ? 1 : 0);
+    if (compact) mf_move_kernel<<<nb, 128, 0, s>>>(mv, ncol, io.ldc, order, d_filt, 1);
     if (hy) mf_post_kernel<true><<<nb, 128, 0, s>>>(io, ncol, P.dtime, flexcn, refresh, d_filt, *hy);
     else if (flexcn || refresh) mf_post_kernel<false><<<nb, 128, 0, s>>>(io, ncol, P.dtime, flexcn, refresh, d_filt, none);
     return cudaGetLastError();

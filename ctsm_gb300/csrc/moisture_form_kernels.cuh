@@ -49,14 +49,21 @@ constexpr int MF_NCLS = 6;
 constexpr int MF_NKEY = MF_NCLS * NLEVSOI;
 constexpr int MF_WORK_HEAD = 32 + 2 * MF_NKEY;       // ints before the per-position arrays
 inline size_t mf_work_bytes(int ncol) { return ((size_t)MF_WORK_HEAD + 2 * (size_t)(ncol > 0 ? ncol : 0)) * sizeof(int); }
+// With the work order, the sub-step kernel runs on a compact copy of the
+// components it uses, moved into the order (and the written ones back): the
+// workspace bytes for ncol columns.
+constexpr int MF_MOVES = 24;
+size_t mf_compact_bytes(int ncol);
 
 // Resident-step form over positions 0..ncol-1 (or the 1-based position
 // filter); hy = NULL leaves the hydrology out.
 // d_work: device scratch, one int (the persistent kernel's work counter) or,
-// with sorted, mf_work_bytes(ncol) for the bucketed work order.
+// with sorted, mf_work_bytes(ncol) for the bucketed work order; d_compact
+// (with sorted; may be NULL) mf_compact_bytes(ncol) of workspace for the
+// compact copy.
 cudaError_t launch_mf_step(const ctsmg_soilwater_io& io, int ncol, const MoistureFormArgs& P, int flexcn, int refresh,
                            DevError* err, const int32_t* d_filt, cudaStream_t s, int* d_work,
-                           const HydroStepArgs* hy = nullptr, bool sorted = false);
+                           const HydroStepArgs* hy = nullptr, bool sorted = false, void* d_compact = nullptr);
 cudaError_t launch_set_soil_water_fractions(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt,
                                             cudaStream_t s);
 cudaError_t launch_flexcn(const ctsmg_soilwater_io& io, int begc, int nfilt, const int32_t* d_filt, cudaStream_t s);

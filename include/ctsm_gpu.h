@@ -870,8 +870,10 @@ int32_t ctsmg_batch_autotune2(ctsmg_batch b, int32_t trial_steps, int32_t* block
                               int32_t* mf_sort_out, float* ms_out, int32_t* ncand_out);
 const char* ctsmg_batch_order_name(int32_t order);
 /* The moisture-form work order of a batch with the moisture form: 1 buckets
- * the columns by the previous step's sub-step count and bedrock depth, 0
- * takes them in position order (the default).  Results do not depend on it. */
+ * the columns by the previous step's sub-step count and bedrock depth and
+ * runs the sub-step kernel on a copy of its components moved into that order
+ * (and the written ones moved back), 0 takes them in position order (the
+ * default).  Results do not depend on it. */
 int32_t ctsmg_batch_set_mf_order(ctsmg_batch b, int32_t sorted);
 int32_t ctsmg_batch_set_block(ctsmg_batch b, int32_t block);
 int64_t ctsmg_batch_state_bytes(ctsmg_batch b);
