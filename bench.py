@@ -711,11 +711,15 @@ def ours_arm(args, ws, rank, local):
     fp64 = C.c_double(0.0)
     L.ctsmg_measure_fp64_tflops(C.byref(fp64))
     L.ctsmg_measure_fp64_lane_cost.argtypes = [C.c_int32, C.POINTER(C.c_float)]
-    lane_cost = {}
+    L.ctsmg_measure_fp64_div_lane_cost.argtypes = [C.c_int32, C.POINTER(C.c_float)]
+    lane_cost = {"dfma": {}, "ddiv": {}}
     for lanes in (32, 8, 1):
         t = C.c_float(0.0)
         L.ctsmg_measure_fp64_lane_cost(lanes, C.byref(t))
-        lane_cost["ms_%d_lanes" % lanes] = round(float(t.value), 3)
+        lane_cost["dfma"]["ms_%d_lanes" % lanes] = round(float(t.value), 3)
+        t = C.c_float(0.0)
+        L.ctsmg_measure_fp64_div_lane_cost(lanes, C.byref(t))
+        lane_cost["ddiv"]["ms_%d_lanes" % lanes] = round(float(t.value), 3)
 
     A, npatch = make_inputs(args.ncol, rank_seed(args.seed, rank))
     ncol = args.ncol

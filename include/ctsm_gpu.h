@@ -1001,6 +1001,9 @@ int32_t ctsmg_measure_fp64_tflops(double* tflops);
  * warp run it: equal times for 1 and 32 lanes mean an FP64 warp instruction
  * costs its issue slot whatever its active lanes.  No reference counterpart. */
 int32_t ctsmg_measure_fp64_lane_cost(int32_t active_lanes, float* ms_out);
+/* The same for a loop of FP64 divisions (256 x 8 per thread): whether a
+ * division's cost follows its active lanes.  No reference counterpart. */
+int32_t ctsmg_measure_fp64_div_lane_cost(int32_t active_lanes, float* ms_out);
 #ifdef __cplusplus
 }
 #endif
