@@ -478,8 +478,11 @@ __global__ void __launch_bounds__(128) mf_order_kernel(int ncol, int* work) {
     if (fc < ncol) O.order[start[k] + r] = fc;
 }
 
+#ifndef CTSMG_MF_MIN_BLOCKS
+#define CTSMG_MF_MIN_BLOCKS 1
+#endif
 template <bool EXPENSIVE>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, CTSMG_MF_MIN_BLOCKS)
 mf_core_kernel(ctsmg_soilwater_io io, int ncol, MoistureFormArgs P, DevError* err, const int32_t* __restrict__ filt,
                int* counter, const int* __restrict__ order, int compact) {
     // compact: io holds the columns of the work order at positions 0..ncol-1
