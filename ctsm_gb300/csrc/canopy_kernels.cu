@@ -947,7 +947,7 @@ __global__ void __launch_bounds__(128) canopy_order_kernel(int nfilt, double* __
 }
 
 #ifndef CTSMG_CANOPY_MIN_BLOCKS
-#define CTSMG_CANOPY_MIN_BLOCKS 4
+#define CTSMG_CANOPY_MIN_BLOCKS 5
 #endif
 constexpr int CANOPY_ITERATE_THREADS = 128;
 __global__ void __launch_bounds__(CANOPY_ITERATE_THREADS, CTSMG_CANOPY_MIN_BLOCKS)
@@ -1028,7 +1028,7 @@ cudaError_t launch_canopy(const CanopyArgs& a, int nfilt, const int32_t* d_filt,
     int dev = 0;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     int per_sm = 0;
-    // 4 blocks of 41 KB of PatchK per SM: ask for the shared-memory carveout
+    // 5 blocks of 41 KB of PatchK per SM: ask for the shared-memory carveout
     cudaFuncSetAttribute(canopy::canopy_iterate_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                          cudaSharedmemCarveoutMaxShared);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, canopy::canopy_iterate_kernel,
