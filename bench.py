@@ -680,13 +680,13 @@ def serving_leg(args):
     since arrival -- is reported beside the completed requests' latency)."""
     from ctsm_gb300 import serving
     reqs = serving.request_stream(args.serve_requests, args.serve_rate, seed=args.seed, physical=True)
-    pool = serving.Pool(budget_bytes=args.serve_budget_gb * 1e9, rootmoist=True)
+    pool = serving.Pool(budget_bytes=args.serve_budget_gb * 1e9, rootmoist=True, hydrology=True)
     cap = pool.capacity
     st = serving.serve(pool, reqs, time_limit=args.serve_seconds)
     pool.close()
     st.update({"workload": "Poisson arrivals at %.2f/s, %d requests, columns log-uniform 1..50000, "
                            "lengths U{48..17520} steps, snow-free columns, full soil+canopy step with the root "
-                           "moisture stress" % (args.serve_rate, args.serve_requests),
+                           "moisture stress and the aquifer-layer hydrology" % (args.serve_rate, args.serve_requests),
                "budget_gb": args.serve_budget_gb, "capacity_columns": cap[0], "time_limit_s": args.serve_seconds,
                "offered_column_steps": int(sum(q.column_steps() for q in reqs)),
                "latency_note": "headline p50/p99_pace_s_per_day: every request that ran, (completion or time "

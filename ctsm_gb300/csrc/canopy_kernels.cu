@@ -963,7 +963,7 @@ canopy_iterate_kernel(CanopyArgs A, int nfilt, double* __restrict__ ws, double d
     int f = -1;                        // filter position of the patch this lane holds
     bool have = true;                  // the work queue was not empty when this lane last looked
     // The loop runs until every lane of the warp is out of work, and the
-    // lanes that took a new patch this round meet the others at __syncwarp()
+    // lanes that took a new patch in this iteration meet the others at __syncwarp()
     // before the pass, so each pass is executed by the whole warp at once.
     // (Block size is a multiple of 32 and no lane leaves the loop early.)
 #pragma unroll 1

@@ -5,8 +5,9 @@
 // and finished requests are copied out and their ranges freed.
 //
 // The step is the batch engine's (optionally the root moisture stress, then
-// CanopyFluxes, root sink, SoilTemperature, SoilWater, h2osoi_vol refresh in
-// the order of src/main/clm_driver.F90:709, 766, 900, 950; or SoilWater then
+// CanopyFluxes, root sink, SoilTemperature, SoilWater -- optionally inside the
+// aquifer-layer hydrology -- and the h2osoi_vol refresh in the order of
+// src/main/clm_driver.F90:709, 766, 900, 950; or SoilWater then
 // SoilTemperature without the canopy), run over
 // the filter of active positions the way the reference runs each clump over
 // filter_nolakec / filter_exposedvegp.
@@ -22,6 +23,7 @@
 #include "soil_kernels.cuh"
 #include "canopy_kernels.cuh"
 #include "rootmoist_kernels.cuh"
+#include "moisture_form_kernels.cuh"
 #include "capi_internal.h"
 
 namespace ctsmg {
@@ -80,6 +82,7 @@ struct Pool {
     ctsmg_soilwater_io dsw{};
     ctsmg_soiltemp_io dst{};
     ctsmg_rootmoist_io drm{};
+    HydroStepArgs hya{};
     CanopyArgs cargs{};
     double* rootr = nullptr;
     double* mslope = nullptr;
@@ -125,13 +128,26 @@ static int kind_cap(const Pool* P, int k) {
 static int kind_start(const Request& r, int k) { return patch_kind(k) ? r.p0 : (k == K_GR ? r.g0 : r.c0); }
 static int kind_count(const Request& r, int k) { return patch_kind(k) ? r.np : (k == K_GR ? r.ng : r.nc); }
 
-static void for_tables(int with_canopy, int rootmoist, void (*fn)(const FieldDesc&, void*), void* ctx) {
+// The aquifer-layer hydrology around the Zeng-Decker form (the batch
+// engine's tables): saturated excess, infiltration, water table, drainage;
+// eff_porosity, which SetSoilWaterFractions writes in the step, is the
+// pool's own (neither copied in nor out).
+static const FieldDesc* const HYD_TABS[4] = {HYD_SAT_TABLE, HYD_INF_TABLE, HYD_WT_TABLE, HYD_DR_TABLE};
+static const int* const HYD_NS[4] = {&HYD_SAT_TABLE_N, &HYD_INF_TABLE_N, &HYD_WT_TABLE_N, &HYD_DR_TABLE_N};
+static const FieldDesc POOL_EFFPOR[] = {{offsetof(ctsmg_soilwater_io, eff_porosity), K_G, 8, U_OUT, "eff_porosity"}};
+
+static void for_tables(const ctsmg_pool_config& c, void (*fn)(const FieldDesc&, void*), void* ctx) {
     for (int i = 0; i < SOILWATER_NFIELDS; ++i) fn(SOILWATER_TABLE[i], ctx);
     for (int i = 0; i < SOILTEMP_NFIELDS; ++i) fn(SOILTEMP_TABLE[i], ctx);
-    if (with_canopy)
+    if (c.with_canopy)
         for (int i = 0; i < CANOPY_NFIELDS; ++i) fn(CANOPY_TABLE[i], ctx);
-    if (with_canopy && rootmoist)
+    if (c.with_canopy && c.rootmoist)
         for (int i = 0; i < ROOTMOIST_NFIELDS; ++i) fn(ROOTMOIST_TABLE[i], ctx);
+    if (c.hydrology) {
+        for (int t = 0; t < 4; ++t)
+            for (int i = 0; i < *HYD_NS[t]; ++i) fn(HYD_TABS[t][i], ctx);
+        fn(POOL_EFFPOR[0], ctx);
+    }
 }
 
 struct SlotBytes { int64_t c = 0, p = 0, g = 0; std::map<std::string, int> seen; };
@@ -146,9 +162,10 @@ static void add_slot_bytes(const FieldDesc& f, void* ctx) {
     else s->c += b;
 }
 
-static void slot_bytes(int with_canopy, int rootmoist, int64_t* cb, int64_t* pb, int64_t* gb) {
+static void slot_bytes(const ctsmg_pool_config& cfg, int64_t* cb, int64_t* pb, int64_t* gb) {
     SlotBytes s;
-    for_tables(with_canopy, rootmoist, add_slot_bytes, &s);
+    const int with_canopy = cfg.with_canopy;
+    for_tables(cfg, add_slot_bytes, &s);
     s.c += (int64_t)SOILTEMP_WS_DOUBLES_PER_COL * 8 + 4;            // band scratch, filter entry
     if (with_canopy)       // rootr, Medlyn slope/intercept, filter, iteration record
         s.p += (int64_t)NLEVSOI * 8 + 2 * 8 + 4 + (int64_t)canopy_ws_bytes_per_patch();
@@ -172,8 +189,24 @@ static cudaError_t enqueue_tick(Pool* P) {
                             P->d_cfilt);
         if (e != cudaSuccess) return e;
     }
-    return launch_soilstep(P->dsw, P->dst, nc, P->cfg.e_ice, P->cfg.dtime, P->cfg.snow_thermal_cond_method, P->ws,
-                           P->cfg.col_capacity, P->err, P->stream, P->block, P->cfg.with_canopy ? 1 : 0, P->d_cfilt);
+    const int ord = P->cfg.with_canopy ? 1 : 0;
+    if (!P->cfg.hydrology)
+        return launch_soilstep(P->dsw, P->dst, nc, P->cfg.e_ice, P->cfg.dtime, P->cfg.snow_thermal_cond_method, P->ws,
+                               P->cfg.col_capacity, P->err, P->stream, P->block, ord, P->d_cfilt);
+    // SoilWater with the hydrology in its own kernel, before the heat solve
+    // without the canopy (order 0) and after it with (order 1)
+    if (ord == 0) {
+        e = launch_zd09_step(P->dsw, nc, P->cfg.e_ice, P->cfg.dtime, 0, 0, P->d_cfilt, P->stream, &P->hya);
+        if (e != cudaSuccess) return e;
+    }
+    SoilStepFlags fl;
+    fl.water = 0;
+    fl.flexcn = 0;
+    fl.refresh = ord == 0 ? 1 : 0;
+    e = launch_soilstep(P->dsw, P->dst, nc, P->cfg.e_ice, P->cfg.dtime, P->cfg.snow_thermal_cond_method, P->ws,
+                        P->cfg.col_capacity, P->err, P->stream, P->block, ord, P->d_cfilt, nullptr, fl);
+    if (e != cudaSuccess || ord == 0) return e;
+    return launch_zd09_step(P->dsw, nc, P->cfg.e_ice, P->cfg.dtime, 0, 1, P->d_cfilt, P->stream, &P->hya);
 }
 
 // Filters of the running requests in pool-position order (each request's
@@ -248,10 +281,11 @@ using namespace ctsmg;
 
 struct ctsmg_pool_s { Pool* P; };
 
-extern "C" int32_t ctsmg_pool_slot_bytes2(int32_t with_canopy, int32_t rootmoist, int64_t* col_bytes,
-                                          int64_t* patch_bytes, int64_t* grid_bytes) {
+extern "C" int32_t ctsmg_pool_slot_bytes_cfg(const ctsmg_pool_config* cfg, int64_t* col_bytes, int64_t* patch_bytes,
+                                             int64_t* grid_bytes) {
+    if (!cfg) return set_error(CTSMG_E_ARG, "null configuration", 0, 0);
     int64_t c, p, g;
-    slot_bytes(with_canopy, rootmoist, &c, &p, &g);
+    slot_bytes(*cfg, &c, &p, &g);
     if (col_bytes) *col_bytes = c;
     if (patch_bytes) *patch_bytes = p;
     if (grid_bytes) *grid_bytes = g;
@@ -261,7 +295,9 @@ extern "C" int32_t ctsmg_pool_slot_bytes2(int32_t with_canopy, int32_t rootmoist
 extern "C" int32_t ctsmg_pool_slot_bytes(int32_t with_canopy, int64_t* col_bytes, int64_t* patch_bytes,
                                          int64_t* grid_bytes) {
     int64_t c, p, g;
-    slot_bytes(with_canopy, 0, &c, &p, &g);
+    ctsmg_pool_config cfg{};
+    cfg.with_canopy = with_canopy;
+    slot_bytes(cfg, &c, &p, &g);
     if (col_bytes) *col_bytes = c;
     if (patch_bytes) *patch_bytes = p;
     if (grid_bytes) *grid_bytes = g;
@@ -347,6 +383,15 @@ extern "C" int32_t ctsmg_pool_create(ctsmg_pool* out, const ctsmg_pool_config* c
             if ((rc = add(ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, &P->drm))) return fail(rc);
         }
     }
+    if (cfg->hydrology) {
+        P->hya.io.ldc = CC;
+        for (int t = 0; t < 4; ++t)
+            if ((rc = add(HYD_TABS[t], *HYD_NS[t], &P->hya.io))) return fail(rc);
+        if ((rc = add(POOL_EFFPOR, 1, &P->dsw))) return fail(rc);
+        P->hya.par = current_soilhydrology_params();
+        P->hya.baseflow_scalar_c = nullptr;
+        P->hya.fff_c = nullptr;
+    }
     if ((e = cudaMalloc(&P->ws, (size_t)SOILTEMP_WS_DOUBLES_PER_COL * CC * 8)) != cudaSuccess) return fail(pcuda(e, "ws"));
     if ((e = cudaMalloc(&P->err, sizeof(DevError))) != cudaSuccess) return fail(pcuda(e, "err"));
     if ((e = cudaMemset(P->err, 0xff, sizeof(DevError))) != cudaSuccess) return fail(pcuda(e, "err"));
@@ -366,19 +411,29 @@ extern "C" int32_t ctsmg_pool_admit(ctsmg_pool ph, int32_t ncol, int32_t npatch,
                                     const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
                                     const ctsmg_canopy_io* cio, const double* rootr, const double* medlynslope_p,
                                     const double* medlynintercept_p, int32_t* slot_out) {
-    return ctsmg_pool_admit2(ph, ncol, npatch, ngrid, nsteps, sw, st, cio, nullptr, rootr, medlynslope_p,
-                             medlynintercept_p, slot_out);
+    ctsmg_pool_request R{ncol, npatch, ngrid, nsteps, sw, st, cio, nullptr, nullptr, rootr, medlynslope_p,
+                         medlynintercept_p};
+    return ctsmg_pool_admit_request(ph, &R, slot_out);
 }
 
-extern "C" int32_t ctsmg_pool_admit2(ctsmg_pool ph, int32_t ncol, int32_t npatch, int32_t ngrid, int32_t nsteps,
-                                     const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
-                                     const ctsmg_canopy_io* cio, const ctsmg_rootmoist_io* rm, const double* rootr,
-                                     const double* medlynslope_p, const double* medlynintercept_p,
-                                     int32_t* slot_out) {
-    if (!ph || !sw || !st || !slot_out) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
+extern "C" int32_t ctsmg_pool_admit_request(ctsmg_pool ph, const ctsmg_pool_request* req, int32_t* slot_out) {
+    if (!ph || !req || !slot_out) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
+    const int32_t ncol = req->ncol, npatch = req->npatch, ngrid = req->ngrid, nsteps = req->nsteps;
+    const ctsmg_soilwater_io* sw = req->sw;
+    const ctsmg_soiltemp_io* st = req->st;
+    const ctsmg_canopy_io* cio = req->cio;
+    const ctsmg_rootmoist_io* rm = req->rm;
+    const ctsmg_hydrology_io* hyio = req->hy;
+    const double* rootr = req->rootr;
+    const double* medlynslope_p = req->medlynslope_p;
+    const double* medlynintercept_p = req->medlynintercept_p;
+    if (!sw || !st) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
     Pool* P = ph->P;
     const bool can = P->cfg.with_canopy != 0;
     const bool rms = can && P->cfg.rootmoist != 0;
+    const bool hyd = P->cfg.hydrology != 0;
+    if (hyd && (!hyio || hyio->ldc != ncol))
+        return set_error(CTSMG_E_ARG, "a hydrology pool needs the request's hydrology components (dense)", 0, 0);
     if (ncol <= 0 || npatch < 0 || ngrid < 0 || nsteps < 1) return set_error(CTSMG_E_ARG, "bad request sizes", 0, 0);
     if (sw->ldc != ncol || st->ldc != ncol || st->ldp != npatch)
         return set_error(CTSMG_E_ARG, "request arrays must be dense: ldc = ncol, ldp = npatch", 0, 0);
@@ -466,6 +521,7 @@ extern "C" int32_t ctsmg_pool_admit2(ctsmg_pool ph, int32_t ncol, int32_t npatch
     if (e == cudaSuccess) e = upload(SOILTEMP_TABLE, SOILTEMP_NFIELDS, st);
     if (e == cudaSuccess && can) e = upload(CANOPY_TABLE, CANOPY_NFIELDS, cio);
     if (e == cudaSuccess && rms) e = upload(ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, rm);
+    for (int t = 0; t < 4 && hyd && e == cudaSuccess; ++t) e = upload(HYD_TABS[t], *HYD_NS[t], hyio);
     if (e == cudaSuccess && can && npatch > 0) {
         if (rootr)
             e = cudaMemcpy2DAsync(P->rootr + r.p0, (size_t)P->cfg.patch_capacity * 8, rootr, (size_t)npatch * 8,
@@ -541,13 +597,19 @@ extern "C" int32_t ctsmg_pool_poll(ctsmg_pool ph, int32_t* slots, int32_t cap, i
 
 extern "C" int32_t ctsmg_pool_evict(ctsmg_pool ph, int32_t slot, const ctsmg_soilwater_io* sw,
                                     const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio, int32_t* steps_done) {
-    return ctsmg_pool_evict2(ph, slot, sw, st, cio, nullptr, steps_done);
+    ctsmg_pool_request R{0, 0, 0, 0, sw, st, cio, nullptr, nullptr, nullptr, nullptr, nullptr};
+    return ctsmg_pool_evict_request(ph, slot, &R, steps_done);
 }
 
-extern "C" int32_t ctsmg_pool_evict2(ctsmg_pool ph, int32_t slot, const ctsmg_soilwater_io* sw,
-                                     const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio,
-                                     const ctsmg_rootmoist_io* rm, int32_t* steps_done) {
-    if (!ph || !sw || !st) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
+extern "C" int32_t ctsmg_pool_evict_request(ctsmg_pool ph, int32_t slot, const ctsmg_pool_request* req,
+                                            int32_t* steps_done) {
+    if (!ph || !req) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
+    const ctsmg_soilwater_io* sw = req->sw;
+    const ctsmg_soiltemp_io* st = req->st;
+    const ctsmg_canopy_io* cio = req->cio;
+    const ctsmg_rootmoist_io* rm = req->rm;
+    const ctsmg_hydrology_io* hyio = req->hy;
+    if (!sw || !st) return set_error(CTSMG_E_ARG, "null argument", 0, 0);
     Pool* P = ph->P;
     if (slot < 0 || slot >= (int)P->req.size() || P->req[slot].state == R_FREE)
         return set_error(CTSMG_E_ARG, "no request in this slot", slot, 0);
@@ -559,6 +621,9 @@ extern "C" int32_t ctsmg_pool_evict2(ctsmg_pool ph, int32_t slot, const ctsmg_so
     const bool rms = rm && P->cfg.with_canopy && P->cfg.rootmoist;
     if (rms && (rm->ldc != r.nc || rm->ldp != r.np))
         return set_error(CTSMG_E_ARG, "eviction root moisture arrays must be dense like the request", slot, 0);
+    const bool hyd = hyio && P->cfg.hydrology;
+    if (hyd && hyio->ldc != r.nc)
+        return set_error(CTSMG_E_ARG, "eviction hydrology arrays must be dense like the request", slot, 0);
     if (r.state == R_RUNNING) {                      // stop after the steps already enqueued
         PK(cudaEventRecord(r.done, P->stream), "done event");
         r.state = R_DONE;
@@ -594,6 +659,7 @@ extern "C" int32_t ctsmg_pool_evict2(ctsmg_pool ph, int32_t slot, const ctsmg_so
     if (e == cudaSuccess) e = download(SOILTEMP_TABLE, SOILTEMP_NFIELDS, st);
     if (e == cudaSuccess && cio && P->cfg.with_canopy) e = download(CANOPY_TABLE, CANOPY_NFIELDS, cio);
     if (e == cudaSuccess && rms) e = download(ROOTMOIST_TABLE, ROOTMOIST_NFIELDS, rm);
+    for (int t = 0; t < 4 && hyd && e == cudaSuccess; ++t) e = download(HYD_TABS[t], *HYD_NS[t], hyio);
     cudaError_t se = cudaStreamSynchronize(P->copy);
     if (e == cudaSuccess) e = se;
     if (e != cudaSuccess) return pcuda(e, "evict copy");

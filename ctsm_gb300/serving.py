@@ -34,7 +34,15 @@ class PoolConfig(C.Structure):
     _fields_ = [("col_capacity", C.c_int32), ("patch_capacity", C.c_int32), ("grid_capacity", C.c_int32),
                 ("dtime", C.c_double), ("e_ice", C.c_double), ("snow_thermal_cond_method", C.c_int32),
                 ("stomatalcond_method", C.c_int32), ("itmax_canopy_fluxes", C.c_int32), ("with_canopy", C.c_int32),
-                ("max_inflight", C.c_int32), ("rootmoist", C.c_int32)]
+                ("max_inflight", C.c_int32), ("rootmoist", C.c_int32), ("hydrology", C.c_int32)]
+
+
+class PoolRequest(C.Structure):
+    _fields_ = [("ncol", C.c_int32), ("npatch", C.c_int32), ("ngrid", C.c_int32), ("nsteps", C.c_int32),
+                ("sw", C.POINTER(abi.SoilWaterIO)), ("st", C.POINTER(abi.SoilTempIO)), ("cio", C.POINTER(abi.CanopyIO)),
+                ("rm", C.POINTER(abi.RootMoistIO)), ("hy", C.POINTER(abi.HydrologyIO)),
+                ("rootr", C.POINTER(C.c_double)), ("medlynslope_p", C.POINTER(C.c_double)),
+                ("medlynintercept_p", C.POINTER(C.c_double))]
 
 
 def _bind(L):
@@ -42,12 +50,9 @@ def _bind(L):
         return
     P = C.POINTER
     L.ctsmg_pool_slot_bytes.argtypes = [C.c_int32, P(C.c_int64), P(C.c_int64), P(C.c_int64)]
-    L.ctsmg_pool_slot_bytes2.argtypes = [C.c_int32, C.c_int32, P(C.c_int64), P(C.c_int64), P(C.c_int64)]
-    L.ctsmg_pool_admit2.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P(abi.SoilWaterIO),
-                                    P(abi.SoilTempIO), P(abi.CanopyIO), P(abi.RootMoistIO), P(C.c_double),
-                                    P(C.c_double), P(C.c_double), P(C.c_int32)]
-    L.ctsmg_pool_evict2.argtypes = [C.c_void_p, C.c_int32, P(abi.SoilWaterIO), P(abi.SoilTempIO), P(abi.CanopyIO),
-                                    P(abi.RootMoistIO), P(C.c_int32)]
+    L.ctsmg_pool_slot_bytes_cfg.argtypes = [P(PoolConfig), P(C.c_int64), P(C.c_int64), P(C.c_int64)]
+    L.ctsmg_pool_admit_request.argtypes = [C.c_void_p, P(PoolRequest), P(C.c_int32)]
+    L.ctsmg_pool_evict_request.argtypes = [C.c_void_p, C.c_int32, P(PoolRequest), P(C.c_int32)]
     L.ctsmg_pool_create.argtypes = [P(C.c_void_p), P(PoolConfig), P(abi.CanopyParams), P(abi.Pftcon)]
     L.ctsmg_pool_admit.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P(abi.SoilWaterIO),
                                    P(abi.SoilTempIO), P(abi.CanopyIO), P(C.c_double), P(C.c_double), P(C.c_double),
@@ -62,20 +67,22 @@ def _bind(L):
     L._pool_bound = True
 
 
-def slot_bytes(canopy=True, rootmoist=False):
+def slot_bytes(canopy=True, rootmoist=False, hydrology=False):
     """(column, patch, gridcell) device bytes per slot."""
     L = load()
     _bind(L)
     c, p, g = C.c_int64(), C.c_int64(), C.c_int64()
-    check(L.ctsmg_pool_slot_bytes2(1 if canopy else 0, 1 if rootmoist else 0, C.byref(c), C.byref(p), C.byref(g)))
+    cfg = PoolConfig(with_canopy=1 if canopy else 0, rootmoist=1 if rootmoist else 0,
+                     hydrology=1 if hydrology else 0)
+    check(L.ctsmg_pool_slot_bytes_cfg(C.byref(cfg), C.byref(c), C.byref(p), C.byref(g)))
     return c.value, p.value, g.value
 
 
-def capacities(budget_bytes, canopy=True, patches_per_column=4, rootmoist=False):
+def capacities(budget_bytes, canopy=True, patches_per_column=4, rootmoist=False, hydrology=False):
     """Slot capacities that fit `budget_bytes`: one gridcell and up to
     `patches_per_column` patches per column slot, so patches and gridcells
     never run out before columns do."""
-    c, p, g = slot_bytes(canopy, rootmoist)
+    c, p, g = slot_bytes(canopy, rootmoist, hydrology)
     per_col = c + patches_per_column * p + g
     ncol = int(budget_bytes // per_col)
     if ncol < 1:
@@ -132,16 +139,19 @@ def make_request(rid, seed, ncol, nsteps, arrival=0.0, pinned=True, physical=Fal
     drawn log-uniformly in [0.5, 1.5] times their defaults, as for ensemble
     members (medlynslope / medlynintercept per patch, om_frac_sf in the soil
     properties; the others are inert on this path).  physical: for a pool
-    with the root moisture stress -- the columns without snow layers (melted
-    layers are removed only by SnowHydrology, outside the path) and with the
-    root moisture stress components, so that transpiration follows the soil
-    water and a year-long request stays in the physical domain."""
+    with the root moisture stress and the hydrology -- the columns without
+    snow layers (melted layers are removed only by SnowHydrology, outside the
+    path), with the root moisture stress components (transpiration follows
+    the soil water) and the hydrology's (drainage takes water out of the
+    column and repairs over-dried layers), so that a year-long request stays
+    in the physical domain."""
     r = np.random.Generator(np.random.Philox(seed))
     factors = {k: float(np.exp(r.uniform(np.log(0.5), np.log(1.5)))) for k in full_inputs.ENSEMBLE_PARAMS}
     A, npatch, ngrid, rootr = full_inputs.full_state(ncol, om_frac_sf=factors["om_frac_sf"], rng=r)
     if physical:
         full_inputs.snow_free(A)
         full_inputs.add_rootmoist_fields(A, npatch, rootr, rng=r)
+        full_inputs.add_hydrology_fields(A, r)
     pft = canopy_inputs.DEFAULT_PFT
     it = A["itype"]
     A["medlynslope_p"] = np.array([row[6] for row in pft])[it] * factors["medlynslope"]
@@ -187,18 +197,19 @@ class Pool:
 
     def __init__(self, budget_bytes=None, col_capacity=None, canopy=True, dtime=1800.0, e_ice=6.0,
                  snow_thermal_cond_method=0, stomatalcond_method=1, itmax=40, params=None, pftcon=None,
-                 max_inflight=2, patches_per_column=4, rootmoist=False):
+                 max_inflight=2, patches_per_column=4, rootmoist=False, hydrology=False):
         self.L = load()
         _bind(self.L)
         if col_capacity is None:
-            cc, pc, gc = capacities(budget_bytes, canopy, patches_per_column, rootmoist)
+            cc, pc, gc = capacities(budget_bytes, canopy, patches_per_column, rootmoist, hydrology)
         else:
             cc, pc, gc = col_capacity, patches_per_column * col_capacity, col_capacity
         self.capacity = (cc, pc, gc)
         self.canopy = canopy
         self.rootmoist = bool(rootmoist and canopy)
+        self.hydrology = bool(hydrology)
         cfg = PoolConfig(cc, pc, gc, dtime, e_ice, snow_thermal_cond_method, stomatalcond_method, itmax,
-                         1 if canopy else 0, max_inflight, 1 if self.rootmoist else 0)
+                         1 if canopy else 0, max_inflight, 1 if self.rootmoist else 0, 1 if self.hydrology else 0)
         self._par = params if params is not None else canopy_inputs.make_params()
         self._pft = pftcon if pftcon is not None else canopy_inputs.make_pftcon()
         self.h = C.c_void_p()
@@ -210,18 +221,25 @@ class Pool:
         st = abi.make_io(abi.SoilTempIO, abi.SOILTEMP_FIELDS, A, n, npch)
         ci = abi.make_io(abi.CanopyIO, abi.CANOPY_FIELDS, A, n, npch, ng, 1) if self.canopy else None
         rm = abi.make_io(abi.RootMoistIO, abi.ROOTMOIST_FIELDS, A, n, npch) if self.rootmoist else None
-        return sw, st, ci, rm
+        hy = abi.make_io(abi.HydrologyIO, abi.HYDROLOGY_FIELDS, A, n) if self.hydrology else None
+        return sw, st, ci, rm, hy
+
+    def _request(self, q, ios):
+        sw, st, ci, rm, hy = ios
+        dp = C.POINTER(C.c_double)
+        ptr = lambda io, T: C.pointer(io) if io is not None else C.POINTER(T)()
+        return PoolRequest(q.ncol, q.npatch, q.ngrid, q.nsteps, C.pointer(sw), C.pointer(st),
+                           ptr(ci, abi.CanopyIO), ptr(rm, abi.RootMoistIO), ptr(hy, abi.HydrologyIO),
+                           q.rootr.ctypes.data_as(dp) if self.canopy else dp(),
+                           q.state["medlynslope_p"].ctypes.data_as(dp) if "medlynslope_p" in q.state else dp(),
+                           q.state["medlynintercept_p"].ctypes.data_as(dp) if "medlynintercept_p" in q.state else dp())
 
     def admit(self, q):
         """Admits request q; returns its slot, or None when the pool is full."""
-        sw, st, ci, rm = self._ios(q)
-        dp = C.POINTER(C.c_double)
+        ios = self._ios(q)
+        req = self._request(q, ios)
         slot = C.c_int32()
-        ms = q.state["medlynslope_p"].ctypes.data_as(dp) if "medlynslope_p" in q.state else None
-        mi = q.state["medlynintercept_p"].ctypes.data_as(dp) if "medlynintercept_p" in q.state else None
-        rc = self.L.ctsmg_pool_admit2(self.h, q.ncol, q.npatch, q.ngrid, q.nsteps, C.byref(sw), C.byref(st),
-                                      C.byref(ci) if ci is not None else None, C.byref(rm) if rm is not None else None,
-                                      q.rootr.ctypes.data_as(dp) if self.canopy else None, ms, mi, C.byref(slot))
+        rc = self.L.ctsmg_pool_admit_request(self.h, C.byref(req), C.byref(slot))
         if rc == E_FULL:
             return None
         check(rc)
@@ -242,11 +260,10 @@ class Pool:
     def evict(self, q):
         """Copies q's final state into q.state and frees its slots; returns
         the number of steps it ran."""
-        sw, st, ci, rm = self._ios(q)
+        ios = self._ios(q)
+        req = self._request(q, ios)
         steps = C.c_int32()
-        check(self.L.ctsmg_pool_evict2(self.h, q.slot, C.byref(sw), C.byref(st),
-                                       C.byref(ci) if ci is not None else None,
-                                       C.byref(rm) if rm is not None else None, C.byref(steps)))
+        check(self.L.ctsmg_pool_evict_request(self.h, q.slot, C.byref(req), C.byref(steps)))
         q.steps_done = steps.value
         q.slot = -1
         return steps.value
@@ -378,14 +395,15 @@ def main(argv=None):
     p.add_argument("--out", default=None, help="JSON file for the statistics and per-request records")
     p.add_argument("--cols-max", type=int, default=50000, help="largest request (columns)")
     p.add_argument("--plain", action="store_true",
-                   help="the step without the root moisture stress, on the workload's snowy columns")
+                   help="the step without the root moisture stress and the hydrology, on the workload's snowy "
+                        "columns")
     a = p.parse_args(argv)
     from . import soil
     soil.init()
     t0 = time.time()
     reqs = request_stream(a.requests, a.rate, seed=a.seed, cols=(1, a.cols_max), physical=not a.plain)
     gen_s = time.time() - t0
-    pool = Pool(budget_bytes=a.budget_gb * 1e9, rootmoist=not a.plain)
+    pool = Pool(budget_bytes=a.budget_gb * 1e9, rootmoist=not a.plain, hydrology=not a.plain)
     try:
         st = serve(pool, reqs, time_limit=a.time_limit)
     finally:

@@ -912,8 +912,30 @@ typedef struct {
     int32_t max_inflight;     /* ticks queued ahead of the device (>= 1)      */
     int32_t rootmoist;        /* 1: each tick starts with the root moisture
                                  stress (btran, rootr from the soil state;
-                                 needs with_canopy and ctsmg_pool_admit2)  */
+                                 needs with_canopy)                        */
+    int32_t hydrology;        /* 1: the aquifer-layer hydrology around the
+                                 Zeng-Decker SoilWater (saturated excess,
+                                 infiltration, water table, drainage) with
+                                 the parameters of ctsmg_set_soilhydrology_params
+                                 at creation                               */
 } ctsmg_pool_config;
+
+/* One request's host arrays for ctsmg_pool_admit_request /
+ * ctsmg_pool_evict_request (dense: begc = begp = begg = 1, ldc = ncol, ldp =
+ * npatch, ldg = ngrid).  cio with with_canopy; rm with rootmoist; hy with
+ * hydrology; rootr (p, 1:nlevsoi) with with_canopy and no rootmoist;
+ * medlynslope_p / medlynintercept_p (p) may be NULL (pftcon values). */
+typedef struct {
+    int32_t ncol, npatch, ngrid, nsteps;
+    const ctsmg_soilwater_io* sw;
+    const ctsmg_soiltemp_io* st;
+    const ctsmg_canopy_io* cio;
+    const ctsmg_rootmoist_io* rm;
+    const ctsmg_hydrology_io* hy;
+    const double* rootr;
+    const double* medlynslope_p;
+    const double* medlynintercept_p;
+} ctsmg_pool_request;
 
 #define CTSMG_E_FULL          11   /* pool: no free range large enough (nothing changed) */
 
@@ -921,9 +943,10 @@ typedef struct {
  * scratch, filters, root fractions, per-patch Medlyn parameters), for sizing
  * the capacities from a memory budget.                                      */
 int32_t ctsmg_pool_slot_bytes(int32_t with_canopy, int64_t* col_bytes, int64_t* patch_bytes, int64_t* grid_bytes);
-/* The same for a pool with the root moisture stress (rootmoist = 1). */
-int32_t ctsmg_pool_slot_bytes2(int32_t with_canopy, int32_t rootmoist, int64_t* col_bytes, int64_t* patch_bytes,
-                               int64_t* grid_bytes);
+/* The same for the configuration cfg (its with_canopy, rootmoist and
+ * hydrology; the capacities are ignored). */
+int32_t ctsmg_pool_slot_bytes_cfg(const ctsmg_pool_config* cfg, int64_t* col_bytes, int64_t* patch_bytes,
+                                  int64_t* grid_bytes);
 /* cpar / pft may be NULL when with_canopy = 0. */
 int32_t ctsmg_pool_create(ctsmg_pool* out, const ctsmg_pool_config* cfg, const ctsmg_canopy_params* cpar,
                           const ctsmg_pftcon* pft);
@@ -938,13 +961,8 @@ int32_t ctsmg_pool_admit(ctsmg_pool p, int32_t ncol, int32_t npatch, int32_t ngr
                          const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio,
                          const double* rootr, const double* medlynslope_p, const double* medlynintercept_p,
                          int32_t* slot_out);
-/* ctsmg_pool_admit for a pool with rootmoist = 1: rm holds the request's
- * root moisture stress components (dense like the others; rootr may then be
- * NULL -- the tick computes it). */
-int32_t ctsmg_pool_admit2(ctsmg_pool p, int32_t ncol, int32_t npatch, int32_t ngrid, int32_t nsteps,
-                          const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st, const ctsmg_canopy_io* cio,
-                          const ctsmg_rootmoist_io* rm, const double* rootr, const double* medlynslope_p,
-                          const double* medlynintercept_p, int32_t* slot_out);
+/* ctsmg_pool_admit with every component a configuration can use. */
+int32_t ctsmg_pool_admit_request(ctsmg_pool p, const ctsmg_pool_request* req, int32_t* slot_out);
 /* Enqueue one step of every running request (returns at once unless
  * max_inflight ticks are already queued).  *ncol_stepped (may be NULL) is
  * the number of columns the tick advances. */
@@ -957,10 +975,10 @@ int32_t ctsmg_pool_poll(ctsmg_pool p, int32_t* slots, int32_t cap, int32_t* n);
  * (may be NULL) is the number of steps it ran. */
 int32_t ctsmg_pool_evict(ctsmg_pool p, int32_t slot, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
                          const ctsmg_canopy_io* cio, int32_t* steps_done);
-/* ctsmg_pool_evict that also returns the root moisture stress components
- * (rm may be NULL). */
-int32_t ctsmg_pool_evict2(ctsmg_pool p, int32_t slot, const ctsmg_soilwater_io* sw, const ctsmg_soiltemp_io* st,
-                          const ctsmg_canopy_io* cio, const ctsmg_rootmoist_io* rm, int32_t* steps_done);
+/* ctsmg_pool_evict that also returns the root moisture stress and
+ * hydrology components (req->rm / req->hy may be NULL; the sizes in req are
+ * not used). */
+int32_t ctsmg_pool_evict_request(ctsmg_pool p, int32_t slot, const ctsmg_pool_request* req, int32_t* steps_done);
 /* Wait for the device; reports a band-solve or CanopyFluxes failure as its
  * status with the request slot in ctsmg_last_error_index and the column (or
  * patch) within the request in the level slot. */

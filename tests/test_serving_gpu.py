@@ -117,48 +117,60 @@ def test_stopped_request_and_refusal(gpu_lib):
     _same(G.state, _batch(q, 4))
 
 
+HYD_DEFAULTS = dict(aq_sp_yield_min=0.01, n_baseflow=1.0, baseflow_scalar=1.0e-2, perched_baseflow_scalar=1.0e-5,
+                    e_ice=6.0, fff=0.5, pc=0.4, mu=0.13, h2osfcflag=1)
+
+
 def test_rootmoist_pool_matches_batch_and_oracle(gpu_lib):
     """A pool with the root moisture stress (btran and rootr from the soil
-    state at the start of every tick, CanopyFluxesMod.F90:709): a snow-free
-    request alone in the pool equals the resident batch with rootmoist bit
-    for bit, and the oracle stepped the same way within the parity tolerance;
-    the stress outputs come back with the request."""
+    state at the start of every tick, CanopyFluxesMod.F90:709) and the
+    aquifer-layer hydrology around the Zeng-Decker SoilWater (saturated
+    excess, infiltration, water table, drainage): a snow-free request alone
+    in the pool equals the resident batch with both bit for bit, and the
+    oracle stepped the same way within the parity tolerance; the stress and
+    hydrology outputs come back with the request."""
+    from ctsm_gb300 import abi
     from ctsm_gb300.engine import SoilBatch
+    gpu_lib.set_soilhydrology_params(**HYD_DEFAULTS)
     q = serving.make_request(0, 515, 240, 4, pinned=False, physical=True)
-    assert (q.state["snl"] == 0).all() and "rootfr" in q.state
+    assert (q.state["snl"] == 0).all() and "rootfr" in q.state and "wa" in q.state
     A = {k: np.array(v, copy=True) for k, v in q.state.items()}
     G = _clone(q)
-    pool = serving.Pool(col_capacity=1024, rootmoist=True)
+    pool = serving.Pool(col_capacity=1024, rootmoist=True, hydrology=True)
     st = serving.serve(pool, [G], tick_clock=True)
     pool.close()
     assert st["completed"] == 1 and G.steps_done == 4
     B = {k: np.array(v, copy=True) for k, v in q.state.items()}
-    b = SoilBatch(B, q.npatch, canopy=True, ngrid=q.ngrid, per_patch_medlyn=True, rootmoist=True)
+    b = SoilBatch(B, q.npatch, canopy=True, ngrid=q.ngrid, per_patch_medlyn=True, rootmoist=True, hydrology=True)
     b.run(4)
     b.sync()
     b.download()
     b.close()
-    _same(G.state, B, OUT + ["btran", "rootr", "rresis"])
+    _same(G.state, B, OUT + ["btran", "rootr", "rresis", "zwt", "wa", "qflx_drain", "qflx_infl"])
     R = copy.deepcopy(A)
-    run = lambda S: full_steps(S, q.npatch, q.ngrid, q.rootr, 4, medlyn_per_patch=True, rootmoist=True)
+    cols = np.arange(1, q.ncol + 1, dtype=np.int32)
+    par = abi.SoilHydrologyParams(*HYD_DEFAULTS.values())
+    run = lambda S: full_steps(S, q.npatch, q.ngrid, q.rootr, 4, medlyn_per_patch=True, rootmoist=True,
+                               hydro=[(cols, par)])
     run(R)
-    spread = noise_spread(run, A, R, fields=CANCEL + ("qflx_evap_veg",), input_ulps=4)
+    spread = noise_spread(run, A, R, fields=CANCEL + ("qflx_evap_veg", "qflx_drain"), input_ulps=4)
     for k in ("liqcan", "snocan"):
         spread[k] = spread[k] + 1e-9 * (np.abs(A["liqcan"]) + np.abs(A["snocan"]))
     # near saturation the sign of efpot is set by rounding (see parity.evap_veg_rounding_bound)
     spread["qflx_evap_veg"] = spread["qflx_evap_veg"] + evap_veg_rounding_bound(R)
-    errs, bad = compare(G.state, R, OUT[:22] + ["btran"], 1e-9, spread)
+    errs, bad = compare(G.state, R, OUT[:22] + ["btran", "zwt", "wa", "qflx_drain"], 1e-9, spread)
     assert not bad, {k: errs[k] for k in bad}
 
 
 def test_physical_stream_stays_finite(gpu_lib):
-    """Year-long requests through the root-moisture pool stay in the physical
-    domain: 6 requests of 40..400 columns, 17,520 steps (a simulated year)
-    each, every final state finite, no negative soil liquid, temperatures in
-    range."""
+    """Year-long requests through the pool with the root moisture stress and
+    the hydrology stay in the physical domain: 6 requests of 40..400
+    columns, 17,520 steps (a simulated year) each, every final state finite,
+    no negative soil liquid, temperatures in range."""
+    gpu_lib.set_soilhydrology_params(**HYD_DEFAULTS)
     reqs = serving.request_stream(6, 0.0, seed=99, cols=(40, 400), steps=(17520, 17520), pinned=False,
                                   physical=True)
-    pool = serving.Pool(col_capacity=4096, rootmoist=True)
+    pool = serving.Pool(col_capacity=4096, rootmoist=True, hydrology=True)
     st = serving.serve(pool, reqs, tick_clock=True)
     pool.close()
     assert st["completed"] == 6
