@@ -57,6 +57,12 @@ static cudaError_t copy_sync(void* dst, const void* src, size_t n, cudaMemcpyKin
 // both directions of ~275 against ~225 GB/s).  A pipelined call whose
 // copied-in arrays are all page-locked therefore copies each chunk in with
 // one gather kernel on the copy-in stream; other arrays take the engines.
+#ifndef CTSMG_GATHER_UNROLL
+#define CTSMG_GATHER_UNROLL 4          // loads in flight per thread of the gather kernel
+#endif
+#ifndef CTSMG_GATHER_BLOCKS_PER_SM
+#define CTSMG_GATHER_BLOCKS_PER_SM 2   // its blocks of 256 threads per SM
+#endif
 constexpr int GATHER_MAX_FIELDS = 72;
 struct GatherField {
     const char* src;        // device-mapped address of the caller's array
@@ -74,7 +80,7 @@ __device__ __forceinline__ void gather_rows(const GatherField& F, long long lo, 
     const long long n = w * F.rows, step = (long long)gridDim.x * blockDim.x;
     const W* __restrict__ src = reinterpret_cast<const W*>(F.src);
     W* __restrict__ dst = reinterpret_cast<W*>(F.dst);
-    constexpr int U = 4;                           // loads in flight per thread
+    constexpr int U = CTSMG_GATHER_UNROLL;         // loads in flight per thread
     for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += U * step) {
         W v[U];
         long long o[U];
@@ -1081,7 +1087,7 @@ static void gather_setup(ThreadCtx* c, const void* hio, const void* dio, const F
         int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        c->gather_grid = 2 * (sms > 0 ? sms : 1);
+        c->gather_grid = CTSMG_GATHER_BLOCKS_PER_SM * (sms > 0 ? sms : 1);
     }
     c->gather = true;
 }
