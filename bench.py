@@ -853,10 +853,35 @@ def ours_arm(args, ws, rank, local):
             marks = pipe_trace(False)
             bi, bo = copied_bytes()
             per_call[name] = dict(h2d_bytes=bi, d2h_bytes=bo, **pipeline_summary(marks))
+        # the same pairs with the time-constant inputs (soil properties, soil
+        # layer geometry) kept on the device between calls, as a host that
+        # sets them once at initialisation would opt in to
+        Lb = _lib.load()
+        Lb.ctsmg_set_time_constant_inputs.argtypes = [C.c_int32]
+        _lib.check(Lb.ctsmg_set_time_constant_inputs(1))
+        try:
+            soil.SoilWater(bnd, ncol, filt, H, DT)
+            soil.SoilTemperature(bnd, ncol, filt, H, DT)
+            barrier()
+            copied_bytes(reset=True)
+            t0 = time.perf_counter()
+            for _ in range(ke):
+                soil.SoilWater(bnd, ncol, filt, H, DT)
+                soil.SoilTemperature(bnd, ncol, filt, H, DT)
+            barrier()
+            tr = max_over_ranks(time.perf_counter() - t0, ws, "cuda")
+            h2d_r, d2h_r = copied_bytes()
+        finally:
+            Lb.ctsmg_set_time_constant_inputs(0)
         e2e = {"value": job_value(ws, ncol, ke, te), "unit": UNIT, "h2d_bytes_per_step": h2d // ke,
                "d2h_bytes_per_step": d2h // ke, "steps": ke, "ms_per_step": 1e3 * te / ke,
                "ms_per_call": {"SoilWater": 1e3 * t_sw / ke, "SoilTemperature": 1e3 * t_st / ke},
                "calls": per_call,
+               "time_constant_inputs_resident": {
+                   "value": job_value(ws, ncol, ke, tr), "unit": UNIT, "ms_per_step": 1e3 * tr / ke,
+                   "h2d_bytes_per_step": h2d_r // ke, "d2h_bytes_per_step": d2h_r // ke,
+                   "note": "ctsmg_set_time_constant_inputs(1): soil properties and soil-layer geometry copied "
+                           "once, every other input and output copied every call"},
                "path": "ctsmg_soilwater + ctsmg_soiltemperature (plain drop-in, pinned host arrays)"}
 
     # ---------------- CPU baseline (rank 0 only, N = 1 only) when the gate did not time the oracle

@@ -152,6 +152,19 @@ struct ThreadCtx {
     cudaEvent_t ev_in[PIPE_CHUNKS] = {}, ev_done[PIPE_CHUNKS] = {};
     // per-chunk timeline of the last pipelined call (ctsmg_pipe_trace):
     // copy-in start / end, kernel start / end, copy-out end
+    // device copies of time-constant inputs kept across calls
+    // (ctsmg_set_time_constant_inputs): one per host array, leading
+    // dimension and size, valid for the columns [lo, hi) of that array
+    struct TcEntry {
+        const void* host;
+        int ld, esize, row0, rows;      // the rows the call copies in
+        size_t bytes;
+        void* dev;
+        int lo, hi;
+        bool valid;
+    };
+    std::vector<TcEntry> tc;
+    unsigned tc_gen = 0;
     // copy-in of the current pipelined call by gather_kernel (page-locked arrays)
     bool gather = false;
     GatherTable gt{};
@@ -171,6 +184,8 @@ struct ThreadCtx {
     std::string msg;
     int err_index = 0, err_level = 0;
     ~ThreadCtx() {
+        for (auto& t : tc)
+            if (t.dev) cudaFree(t.dev);
         if (arena) cudaFree(arena);
         if (order) cudaFreeHost(order);
         if (err) cudaFree(err);
@@ -1095,6 +1110,77 @@ static void gather_setup(ThreadCtx* c, const void* hio, const void* dio, const F
 // The stream that carries a pipelined call's copy-in.
 static cudaStream_t in_stream(ThreadCtx* c) { return c->gather ? c->h2dk : c->h2d; }
 
+// ---------------------------------------------------- time-constant inputs
+// With ctsmg_set_time_constant_inputs(1) a pipelined call keeps the device
+// copy of each input the model never changes after initialisation (soil
+// hydraulic and thermal properties, the soil-layer geometry) per host array
+// and copied rows (SoilWater and SoilTemperature copy different rows of the
+// same arrays, so each keeps its own), and copies it in again only when the
+// call's columns are not yet covered or after
+// ctsmg_invalidate_time_constant_inputs.
+static std::atomic<int> g_tc_on{0};
+static std::atomic<unsigned> g_tc_gen{1};
+
+static bool time_constant(const char* name, const char* const* names) {
+    for (int i = 0; names[i]; ++i)
+        if (std::strcmp(name, names[i]) == 0) return true;
+    return false;
+}
+// SoilWater's Zeng-Decker form copies levels 1..nlevsoi of z / dz and the soil
+// interfaces only: the soil layers, which do not move
+static const char* const TC_SOILWATER[] = {"z", "zi", "dz", "smpmin", "watsat", "hksat", "bsw", "sucsat", nullptr};
+static const char* const TC_SOILTEMP[] = {"watsat", "bsw", "sucsat", "tkmg", "tkdry", "csol", nullptr};
+
+// Points the time-constant components of a pipelined call at their kept
+// device copies (dio), marks the ones already covered for [lo, hi) as not
+// copied in (tab), and returns the entries this call fills.
+static int tc_bind(ThreadCtx* c, const void* hio, void* dio, std::vector<FieldDesc>& tab, const char* const* names,
+                   int ldc, int ldp, int lo, int hi, std::vector<ThreadCtx::TcEntry*>& fill) {
+    fill.clear();
+    if (!g_tc_on.load()) return 0;
+    if (c->tc_gen != g_tc_gen.load()) {
+        for (auto& t : c->tc)
+            if (t.dev) cudaFree(t.dev);
+        c->tc.clear();
+        c->tc_gen = g_tc_gen.load();
+    }
+    c->tc.reserve(c->tc.size() + tab.size());          // the pointers in fill stay valid
+    for (FieldDesc& f : tab) {
+        if (!time_constant(f.name, names) || f.use != U_IN) continue;
+        const void* h = field_ptr(const_cast<void*>(hio), f);
+        const size_t bytes = field_bytes(f, ldc, ldp, 0);
+        const int row0 = (int)copy_in_row0(f), rows = copy_in_rows(f);
+        ThreadCtx::TcEntry* e = nullptr;
+        for (auto& t : c->tc)
+            if (t.host == h && t.ld == ldc && t.esize == f.esize && t.bytes == bytes && t.row0 == row0 &&
+                t.rows == rows) {
+                e = &t;
+                break;
+            }
+        if (!e) {
+            void* d = nullptr;
+            cudaError_t ce = cudaMalloc(&d, bytes);
+            if (ce != cudaSuccess) return cuda_fail(ce, "cudaMalloc(time-constant input)");
+            c->tc.push_back(ThreadCtx::TcEntry{h, ldc, f.esize, row0, rows, bytes, d, 0, 0, false});
+            e = &c->tc.back();
+        }
+        field_ptr(dio, f) = e->dev;
+        if (e->valid && e->lo <= lo && hi <= e->hi) f.no_in = 1;
+        else fill.push_back(e);
+    }
+    return 0;
+}
+
+// After a successful call: the entries it filled now cover [lo, hi).
+static void tc_commit(std::vector<ThreadCtx::TcEntry*>& fill, int lo, int hi) {
+    for (auto* e : fill) {
+        e->valid = true;
+        e->lo = lo;
+        e->hi = hi;
+    }
+    fill.clear();
+}
+
 // Timeline mark `slot` of chunk k on stream s when the calling thread traces
 // its pipelined calls (0 copy-in start, 1 copy-in end, 2 kernel start,
 // 3 kernel end, 4 copy-out end).
@@ -1460,6 +1546,11 @@ extern "C" int32_t ctsmg_soilwater(const ctsmg_bounds* bounds, int32_t num_hydro
     if (plan_chunks(bounds, num_hydrologyc, filter_hydrologyc, nullptr, nullptr, 0, chunks)) {
         ctsmg_soilwater_io dio;
         stage_alloc(c, io, &dio, sizeof dio, T, NT, ldc, 0);
+        std::vector<ThreadCtx::TcEntry*> tc_fill;
+        const int tc_lo = chunks.front().c0, tc_hi = chunks.back().c1;
+        if (nml.soilwater_movement_method == 0 &&
+            (rc = tc_bind(c, io, &dio, tab, TC_SOILWATER, ldc, 0, tc_lo, tc_hi, tc_fill)))
+            return rc;
         gather_setup(c, io, &dio, T, NT, ldc, 0);
         int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_hydrologyc * 4);
         // the Zeng-Decker form takes each chunk's columns grouped by
@@ -1507,6 +1598,7 @@ extern "C" int32_t ctsmg_soilwater(const ctsmg_bounds* bounds, int32_t num_hydro
         c->gather = false;
         if ((e = join_streams(c)) != cudaSuccess) return cuda_fail(e, "soilwater");
         c->trace_n = c->trace ? K : 0;
+        tc_commit(tc_fill, tc_lo, tc_hi);
     } else {
         ctsmg_soilwater_io dio;
         if ((rc = stage_in(c, io, &dio, sizeof dio, T, NT, ldc, 0, 0, bounds->endc - bounds->begc + 1, -1))) return rc;
@@ -1561,7 +1653,16 @@ extern "C" int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds, int32_t num
     if (plan_chunks(bounds, num_nolakec, filter_nolakec, io->col_patchi, io->col_npatches, soiltemp_wave_columns(),
                     chunks)) {
         ctsmg_soiltemp_io dio;
+        std::vector<FieldDesc> ttab;
+        std::vector<ThreadCtx::TcEntry*> tc_fill;
+        const int tc_lo = chunks.front().c0, tc_hi = chunks.back().c1;
+        if (g_tc_on.load()) {           // a copy of the table whose no_in marks the kept components
+            ttab.assign(TT, TT + SOILTEMP_NFIELDS);
+            TT = ttab.data();
+        }
         stage_alloc(c, io, &dio, sizeof dio, TT, SOILTEMP_NFIELDS, ldc, ldp);
+        if (!ttab.empty() && (rc = tc_bind(c, io, &dio, ttab, TC_SOILTEMP, ldc, ldp, tc_lo, tc_hi, tc_fill)))
+            return rc;
         gather_setup(c, io, &dio, TT, SOILTEMP_NFIELDS, ldc, ldp);
         int32_t* dfilt = (int32_t*)arena_take(c, (size_t)num_nolakec * 4);
         double* ws = (double*)arena_take(c, ws_bytes);
@@ -1606,6 +1707,7 @@ extern "C" int32_t ctsmg_soiltemperature(const ctsmg_bounds* bounds, int32_t num
         c->gather = false;
         if ((e = join_streams(c)) != cudaSuccess) return cuda_fail(e, "soiltemperature");
         c->trace_n = c->trace ? K : 0;
+        tc_commit(tc_fill, tc_lo, tc_hi);
         int code = 0, idx = 0, lev = 0;
         if ((rc = read_error(c, &code, &idx, &lev))) return rc;
         if (code) return set_error(code, "BandDiagonal ERROR: dgbsv returned error code", idx, lev);
@@ -2042,6 +2144,21 @@ extern "C" int32_t ctsmg_water_table(const ctsmg_bounds* b, int32_t n, const int
 extern "C" int32_t ctsmg_drainage(const ctsmg_bounds* b, int32_t n, const int32_t* f, const ctsmg_hydrology_io* io,
                                   double dtime) {
     return hydrology_call(b, n, f, io, dtime, HYD_DRAINAGE, HYD_DR_TABLE, HYD_DR_TABLE_N);
+}
+
+// Keep (1) or stop keeping (0) device copies of the time-constant inputs of
+// the pipelined drop-in calls; either way the kept copies are dropped.
+extern "C" int32_t ctsmg_set_time_constant_inputs(int32_t resident) {
+    if (resident != 0 && resident != 1) return set_error(CTSMG_E_ARG, "resident must be 0 or 1", 0, 0);
+    g_tc_on = resident;
+    ++g_tc_gen;
+    return 0;
+}
+
+// Drop the kept copies (a time-constant input changed on the host).
+extern "C" int32_t ctsmg_invalidate_time_constant_inputs(void) {
+    ++g_tc_gen;
+    return 0;
 }
 
 // Copy-in mode of the pipelined drop-in calls: 0 a gather kernel when the

@@ -1001,6 +1001,19 @@ int32_t ctsmg_copy_bytes(int64_t* h2d, int64_t* d2h, int32_t reset);
  * element-aligned, else with the copy engines; mode 1 with the copy engines
  * always.  Results do not depend on it.  No reference counterpart. */
 int32_t ctsmg_set_copy_mode(int32_t mode);
+/* Time-constant inputs of the pipelined drop-in calls.  With resident = 1,
+ * ctsmg_soilwater (Zeng-Decker form: levels 1..nlevsoi of z, dz and zi,
+ * smpmin, watsat, hksat, bsw, sucsat) and ctsmg_soiltemperature (watsat, bsw,
+ * sucsat, tkmg, tkdry, csol) keep their device copy of each such host array
+ * between calls -- keyed by the array's address, leading dimension, size
+ * and the rows the call reads -- and copy it in again only for columns not
+ * yet covered.  These are the
+ * components CTSM sets at initialisation (SoilStateInitTimeConstMod) and the
+ * soil-layer geometry; a caller that changes one on the host calls
+ * ctsmg_invalidate_time_constant_inputs() before its next call.  Default 0:
+ * every input is copied in on every call.  No reference counterpart. */
+int32_t ctsmg_set_time_constant_inputs(int32_t resident);
+int32_t ctsmg_invalidate_time_constant_inputs(void);
 /* Per-chunk timeline of the calling thread's pipelined drop-in calls
  * (ctsmg_soilwater, ctsmg_soiltemperature over an ascending filter of at
  * least 32,768 columns).  enable = 1 / 0 turns the recording on / off for

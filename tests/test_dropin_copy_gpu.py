@@ -77,3 +77,50 @@ def test_copy_mode_rejects_unknown_modes(gpu_lib):
     L.ctsmg_set_copy_mode.argtypes = [C.c_int32]
     assert L.ctsmg_set_copy_mode(2) != 0
     assert L.ctsmg_set_copy_mode(0) == 0
+
+
+def test_time_constant_inputs_kept_between_calls(gpu_lib):
+    """ctsmg_set_time_constant_inputs(1): the pipelined calls keep their device
+    copies of the soil properties and the soil-layer geometry between calls.
+    Two pairs of calls give the same bits as with every input copied, the
+    second pair copies fewer bytes in, and after a soil property changes on
+    the host and ctsmg_invalidate_time_constant_inputs() the next pair sees
+    the new values."""
+    from ctsm_gb300 import _lib
+    L = _lib.load()
+    L.ctsmg_set_time_constant_inputs.argtypes = [C.c_int32]
+    L.ctsmg_copy_bytes.argtypes = [C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.c_int32]
+    A, npatch = inputs.soil_columns(40000, seed=93, snow=True, nbedrock=(3, 20), forcing="full", npatch_max=3)
+    ncol = A["zwt"].shape[0]
+
+    def h2d():
+        bi, bo = C.c_int64(), C.c_int64()
+        _lib.check(L.ctsmg_copy_bytes(C.byref(bi), C.byref(bo), 1))
+        return bi.value
+
+    def run(resident, change=False):
+        _lib.check(L.ctsmg_set_time_constant_inputs(1 if resident else 0))
+        S = copy.deepcopy(A)
+        h2d()
+        _pair(gpu_lib, S, ncol, npatch)
+        first = h2d()
+        _pair(gpu_lib, S, ncol, npatch)
+        second = h2d()
+        if change:
+            S["watsat"][...] = S["watsat"] * 1.01          # a soil property edited on the host
+            L.ctsmg_invalidate_time_constant_inputs()
+            _pair(gpu_lib, S, ncol, npatch)
+        return S, first, second
+
+    try:
+        S0, f0, s0 = run(False)
+        S1, f1, s1 = run(True)
+        C0, _, _ = run(False, change=True)
+        C1, _, _ = run(True, change=True)
+    finally:
+        L.ctsmg_set_time_constant_inputs(0)
+    assert f1 == f0 == s0 and s1 < s0
+    for k in A:
+        assert np.array_equal(S1[k], S0[k], equal_nan=True), k
+        assert np.array_equal(C1[k], C0[k], equal_nan=True), k
+    assert not np.array_equal(C0["h2osoi_liq"], S0["h2osoi_liq"])
