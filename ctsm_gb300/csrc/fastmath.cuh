@@ -72,7 +72,15 @@ CTSMG_FM_HD double add(double a, double b) { return __dadd_rn(a, b); }
 CTSMG_FM_HD double sub(double a, double b) { return __dsub_rn(a, b); }
 CTSMG_FM_HD double mul(double a, double b) { return __dmul_rn(a, b); }
 CTSMG_FM_HD double fma_(double a, double b, double c) { return __fma_rn(a, b, c); }
-CTSMG_FM_HD double i2d(int k) { return __int2double_rn(k); }
+// (double)k for any int, built on the integer pipe (an int-to-FP64
+// conversion is an FP64-pipe instruction): exact, as the conversion
+CTSMG_FM_HD double i2d(int k) {
+    const unsigned a = k < 0 ? 0u - (unsigned)k : (unsigned)k;
+    const int e = 31 - __clz(a | 1u);                            // a in [2^e, 2^(e+1)) for a > 0
+    const uint64_t m = ((uint64_t)a << (52 - e)) & 0x000FFFFFFFFFFFFFULL;
+    const uint64_t b = ((uint64_t)(k < 0) << 63) | ((uint64_t)(1023 + e) << 52) | m;
+    return k == 0 ? 0.0 : __longlong_as_double((long long)b);
+}
 CTSMG_FM_HD double invf(int j) { return __ldg(&LOG_INVF_D[j]); }
 CTSMG_FM_HD HiLo loghl(int j) { const double2 t = __ldg(&LOG_HILO_D[j]); return {t.x, t.y}; }
 CTSMG_FM_HD HiLo exphl(int j) { const double2 t = __ldg(&EXP_HILO_D[j]); return {t.x, t.y}; }

@@ -8,6 +8,11 @@
 //   ctsmg_diag_crdiv(n, a, b, out): out[i] = a[i] / b[i] (CUDA), out[n+i] =
 //     the shared-reciprocal quotient of cr_div.cuh, out[2n+i] = its
 //     reciprocal RN(1/b[i]) (3n doubles).
+//   ctsmg_diag_fcmp(n, a, b, out): the integer-pipe comparisons of fcmp.cuh
+//     beside the FP64 ones -- rows 0-7 a<b, a<=b, a>b, a>=b, a==b, a!=0,
+//     |a|>0 (IEEE; row 7 unused), rows 8-15 the same from fcmp.cuh, rows
+//     16-19 fmin(a,b), fmax(a,b), ic::min, ic::max, row 20 fm::i2d(i - n/2)
+//     (21n doubles).
 // Host arrays in and out.  Built by tests/gpu_diag.py with nvcc for sm_103a.
 #include <cuda_runtime.h>
 #include <cstdint>
@@ -15,6 +20,7 @@
 #include "ctsm_device.cuh"
 #include "soil_math.cuh"
 #include "cr_div.cuh"
+#include "fcmp.cuh"
 
 static int32_t diag_fail(cudaError_t e) { return e == cudaSuccess ? 0 : CTSMG_E_CUDA; }
 
@@ -103,6 +109,39 @@ extern "C" int32_t ctsmg_diag_crdiv(int32_t n, const double* a, const double* b,
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * (size_t)n, 3 * nb, cudaMemcpyDeviceToHost);
+    if (d) cudaFree(d);
+    return diag_fail(e);
+}
+
+namespace ctsmg {
+__global__ void diag_fcmp_kernel(int n, const double* __restrict__ a, const double* __restrict__ b,
+                                 double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double x = a[i], y = b[i];
+    auto put = [&](int row, double v) { out[(size_t)row * n + i] = v; };
+    put(0, x < y); put(1, x <= y); put(2, x > y); put(3, x >= y); put(4, x == y); put(5, x != 0.0);
+    put(6, fabs(x) > 0.0); put(7, 0.0);
+    put(8, ic::lt(x, y)); put(9, ic::le(x, y)); put(10, ic::gt(x, y)); put(11, ic::ge(x, y));
+    put(12, ic::eq(x, y)); put(13, ic::ne0(x)); put(14, ic::abs_gt0(x)); put(15, 0.0);
+    put(16, fmin(x, y)); put(17, fmax(x, y)); put(18, ic::min(x, y)); put(19, ic::max(x, y));
+    put(20, fm::i2d(i - n / 2));
+}
+} // namespace ctsmg
+
+extern "C" int32_t ctsmg_diag_fcmp(int32_t n, const double* a, const double* b, double* out) {
+    using namespace ctsmg;
+    if (n <= 0 || !a || !b || !out) return CTSMG_E_ARG;
+    double* d = nullptr;
+    const size_t nb = (size_t)n * 8;
+    cudaError_t e = cudaMalloc(&d, 23 * nb);
+    if (e == cudaSuccess) e = cudaMemcpy(d, a, nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d + n, b, nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        diag_fcmp_kernel<<<(n + 127) / 128, 128>>>(n, d, d + n, d + 2 * (size_t)n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * (size_t)n, 21 * nb, cudaMemcpyDeviceToHost);
     if (d) cudaFree(d);
     return diag_fail(e);
 }

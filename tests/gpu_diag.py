@@ -34,6 +34,7 @@ def load():
         _LIB.ctsmg_diag_fastmath.argtypes = [C.c_int32, P, P, P]
         _LIB.ctsmg_diag_powers.argtypes = [C.c_int32, P, P, P]
         _LIB.ctsmg_diag_crdiv.argtypes = [C.c_int32, P, P, P]
+        _LIB.ctsmg_diag_fcmp.argtypes = [C.c_int32, P, P, P]
     return _LIB
 
 
