@@ -22,6 +22,7 @@
 #include "canopy_kernels.cuh"
 #include "rootfind.cuh"
 #include "qsat.cuh"
+#include "fcmp.cuh"
 
 namespace ctsmg {
 namespace canopy {
@@ -58,15 +59,15 @@ __device__ __forceinline__ void flag(Err& e, int code, int idx) { if (!e.code) {
 
 // quadraticMod.F90:17-74
 __device__ __forceinline__ bool quadratic(double a, double b, double c, double& r1, double& r2) {
-    if (a == 0.0) { r1 = r2 = 0.0; return false; }
+    if (!ic::ne0(a)) { r1 = r2 = 0.0; return false; }
     double root = b * b - 4.0 * a * c;
-    if (root < 0.0) {
-        if (-root < 3.0 * 2.220446049250313e-16) root = 0.0;
+    if (ic::lt0(root)) {
+        if (ic::gtn(root, -3.0 * 2.220446049250313e-16)) root = 0.0;
         else { r1 = r2 = 0.0; return false; }
     }
-    const double q = (b >= 0.0) ? -0.5 * (b + sqrt(root)) : -0.5 * (b - sqrt(root));
+    const double q = ic::ge0(b) ? -0.5 * (b + sqrt(root)) : -0.5 * (b - sqrt(root));
     r1 = q / a;
-    r2 = (q != 0.0) ? c / q : 1.e36;
+    r2 = ic::ne0(q) ? c / q : 1.e36;
     return true;
 }
 
@@ -109,23 +110,23 @@ __device__ double ci_func(double ci, const PsnCtx& x, PsnState& s, Err& e, int p
     LANE_PROBE(4);
     double r1, r2;
     if (x.c3) {
-        s.ac = x.vcmax_z * fmax(ci - x.cp, 0.0) / (ci + x.kco);
-        s.aj = x.je * fmax(ci - x.cp, 0.0) / (4.0 * ci + 8.0 * x.cp);
+        s.ac = x.vcmax_z * ic::max0(ci - x.cp) / (ci + x.kco);
+        s.aj = x.je * ic::max0(ci - x.cp) / (4.0 * ci + 8.0 * x.cp);
         s.ap = x.ap3;
     } else {
         s.ac = x.vcmax_z;
         s.aj = x.aj4;
-        s.ap = x.kp_z * fmax(ci, 0.0) / x.forc_pbot;
+        s.ap = x.kp_z * ic::max0(ci) / x.forc_pbot;
     }
     if (!quadratic(x.theta_cj, -(s.ac + s.aj), s.ac * s.aj, r1, r2)) flag(e, CTSMG_E_DISCRIMINANT, pidx);
     const double ai = fmin(r1, r2);
     if (!quadratic(x.theta_ip, -(ai + s.ap), ai * s.ap, r1, r2)) flag(e, CTSMG_E_DISCRIMINANT, pidx);
-    s.ag = fmax(0.0, fmin(r1, r2));
+    s.ag = ic::max0(fmin(r1, r2));
     s.an = s.ag - x.lmr_z;
-    if (s.an < 0.0) return 0.0;
+    if (ic::lt0(s.an)) return 0.0;
     LANE_PROBE(5);
     double cs = x.cair - x.c14gb * s.an * x.forc_pbot;
-    cs = fmax(cs, 1.e-06);
+    cs = ic::maxc(cs, 1.e-06);
     if (x.method == 1) {
         const double term = 1.6 * s.an / (cs / x.forc_pbot * 1.e06);
         const double st = x.m_slope * term;
@@ -311,7 +312,7 @@ __device__ PhaseOut photosynthesis(const CanopyArgs& A, const Patch& s, const Pa
     const bool c3 = s.c3 != 0;
     const double qe = c3 ? 0.0 : 0.05;
     double bbb = 0.0, mbb = 0.0;
-    if (method == 0) { bbb = fmax((c3 ? 10000.0 : 40000.0) * btran, 1.0); mbb = q.mbb; }
+    if (method == 0) { bbb = ic::maxc((c3 ? 10000.0 : 40000.0) * btran, 1.0); mbb = q.mbb; }
     const double nscaler = vcmaxcint;
     const double lmr25 = (c3 ? q.vcmax25top * P.leaf_mr_vcm : q.vcmax25top * 0.025) * nscaler;
     double lmr_z;
@@ -322,7 +323,7 @@ __device__ PhaseOut photosynthesis(const CanopyArgs& A, const Patch& s, const Pa
         lmr_z = lmr_z / T.lmr2;
     }
     double vcmax_z = 0.0, jmax_z = 0.0, tpu_z = 0.0, kp_z = 0.0;
-    if (par_z > 0.0) {
+    if (ic::gt0(par_z)) {
         const double vcmax25 = q.vcmax25top * nscaler, jmax25 = q.jmax25top * nscaler;
         const double tpu25 = P.tpu25ratio * q.vcmax25top * nscaler, kp25 = P.kp25ratio * q.vcmax25top * nscaler;
         if (c3) {
@@ -338,18 +339,18 @@ __device__ PhaseOut photosynthesis(const CanopyArgs& A, const Patch& s, const Pa
     }
     vcmax_z = vcmax_z * btran;
     lmr_z = lmr_z * btran;
-    if (P.light_inhibit && par_z > 0.0) lmr_z = lmr_z * 0.67;
+    if (P.light_inhibit && ic::gt0(par_z)) lmr_z = lmr_z * 0.67;
 
     const double rsmax0 = 2.e4;
     const double cf = q.cf;
     const double gb_mol = 1.0 / rb * cf;
     PhaseOut out;
     double rs_z, psn_z, ci_z;
-    if (par_z <= 0.0) {
+    if (ic::le0(par_z)) {
         st.ac = st.aj = st.ap = st.ag = 0.0;
         st.an = 0.0 - lmr_z;
         psn_z = 0.0;
-        rs_z = (method == 0) ? fmin(rsmax0, 1.0 / bbb * cf) : fmin(rsmax0, 1.0 / medlyn_int * cf);
+        rs_z = (method == 0) ? ic::minc(1.0 / bbb * cf, rsmax0) : ic::minc(1.0 / medlyn_int * cf, rsmax0);
         ci_z = 0.0;
         rh_leaf = 0.0;
         out.gs_mol_phase = cf / rs_z;
@@ -359,7 +360,7 @@ __device__ PhaseOut photosynthesis(const CanopyArgs& A, const Patch& s, const Pa
         if (method == 0) {
             rh_can = ceair / esat_tv;
         } else {
-            rh_can = fmax((esat_tv - ceair), 50.0) * 0.001;
+            rh_can = ic::maxc((esat_tv - ceair), 50.0) * 0.001;
             vpd_can = rh_can;
         }
         const double qabs = 0.5 * (1.0 - P.fnps) * par_z * 4.6;
@@ -375,16 +376,16 @@ __device__ PhaseOut photosynthesis(const CanopyArgs& A, const Patch& s, const Pa
 #pragma unroll 1
         while (rf.next(ci_func(rf.x, ctx, st, err, pidx))) {}
         if (rf.not_bracketed) flag(err, CTSMG_E_NOT_BRACKETED, pidx);
-        if (st.an < 0.0) st.gs_mol = (method == 0) ? bbb : medlyn_int;
+        if (ic::lt0(st.an)) st.gs_mol = (method == 0) ? bbb : medlyn_int;
         out.gs_mol_phase = st.gs_mol;
         ci_z = cair - st.an * forc_pbot * (1.4 * st.gs_mol + 1.6 * gb_mol) / (gb_mol * st.gs_mol);
-        ci_z = fmax(ci_z, 1.e-06);
-        rs_z = fmin(1.0 / (st.gs_mol / cf), rsmax0);
+        ci_z = ic::maxc(ci_z, 1.e-06);
+        rs_z = ic::minc(1.0 / (st.gs_mol / cf), rsmax0);
         psn_z = st.ag;
-        if (st.gs_mol < 0.0) flag(err, CTSMG_E_ARG, pidx);
+        if (ic::lt0(st.gs_mol)) flag(err, CTSMG_E_ARG, pidx);
         if (method == 0) rh_leaf = (gb_mol * ceair + st.gs_mol * esat_tv) / ((gb_mol + st.gs_mol) * esat_tv);
     }
-    if (lai_z > 0.0) {
+    if (ic::gt0(lai_z)) {
         out.psn = psn_z * lai_z / lai_z;
         out.lmr = lmr_z * lai_z / lai_z;
         out.rs = lai_z / (lai_z / (rb + rs_z)) - rb;
@@ -410,8 +411,9 @@ __device__ void friction_velocity(const Patch& s, const PatchK& K, int iter, dou
     // once per warp in a "slot" whose argument each lane selects for its own
     // branch, then the branches combine the slots' values: the arguments and
     // the arithmetic are the reference's, only the control flow differs.
-    const bool b1 = zeta < -zetam, b2 = !b1 && zeta < 0.0, b3 = !b1 && !b2 && zeta <= 1.0, b4 = !b1 && !b2 && !b3;
-    const bool tall = !(zldis - z0m <= 10.0);
+    const bool b1 = ic::ltn(zeta, -zetam), b2 = !b1 && ic::lt0(zeta), b3 = !b1 && !b2 && ic::lec(zeta, 1.0);
+    const bool b4 = !b1 && !b2 && !b3;
+    const bool tall = !ic::lec(zldis - z0m, 10.0);
     const double z10 = 10.0 + z0m;
     // the scalar profiles' heights and their branches (z0 = z0m in every call)
     const bool two = !(K.hgt_q == K.hgt_t);
@@ -422,7 +424,7 @@ __device__ void friction_velocity(const Patch& s, const PatchK& K, int iter, dou
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         zt[i] = zl[i] / obu;
-        tb[i] = (zt[i] < -zetat) ? 1 : (zt[i] < 0.0) ? 2 : (zt[i] <= 1.0) ? 3 : 4;
+        tb[i] = ic::ltn(zt[i], -zetat) ? 1 : ic::lt0(zt[i]) ? 2 : ic::lec(zt[i], 1.0) ? 3 : 4;
         if (i == 1 && !two) tb[i] = 0;
         any_t1 |= tb[i] == 1;
         any_t4 |= tb[i] == 4;
@@ -431,7 +433,7 @@ __device__ void friction_velocity(const Patch& s, const PatchK& K, int iter, dou
     double pz = 0.0, s2z0 = 0.0, st_z0 = 0.0, st_zeta = 0.0, st_z10 = 0.0, l_a = 0.0, l_b = 0.0, l_zeta = 0.0;
     double l_t1 = 0.0, p_vds = 0.0;
     if (b1) pz = xpow(-zeta, 0.333);
-    if (obu < 0.0) s2z0 = stab2(z0m / obu);
+    if (ic::lt0(obu)) s2z0 = stab2(z0m / obu);
     if (b1 || b2) st_z0 = stab1(z0m / obu);
     if (b2) st_zeta = stab1(zeta);
     if ((b1 || b2) && tall) st_z10 = stab1(z10 / obu);
@@ -443,13 +445,13 @@ __device__ void friction_velocity(const Patch& s, const PatchK& K, int iter, dou
     // took slot l_a for branch 1 (zl and zldis of opposite signs)
     double l_obu = l_a;
     if (b1 && any_t4) l_obu = xlog(obu / z0m);
-    if (zeta < 0.0) p_vds = xpow(300.0 / (-obu), 0.666);
+    if (ic::lt0(zeta)) p_vds = xpow(300.0 / (-obu), 0.666);
     LANE_PROBE(8);
     if (b1) ustar = VKC * um / (l_a - K.s1_zetam + st_z0 + 1.14 * (pz - K.pz_m));
     else if (b2) ustar = VKC * um / (K.lg_u - st_zeta + st_z0);
     else if (b3) ustar = VKC * um / (K.lg_u + 5.0 * zeta - 5.0 * z0m / obu);
     else ustar = VKC * um / (l_a + 5.0 - 5.0 * z0m / obu + (5.0 * l_zeta + zeta - 1.0));
-    vds = (zeta < 0.0) ? 2.e-3 * ustar * (1.0 + p_vds) : 2.e-3 * ustar;
+    vds = ic::lt0(zeta) ? 2.e-3 * ustar * (1.0 + p_vds) : 2.e-3 * ustar;
     if (!tall) {
         u10_clm = um;
     } else if (b1) {
@@ -483,18 +485,19 @@ __device__ void friction_velocity(const Patch& s, const PatchK& K, int iter, dou
     temp22m = temp12m;
     double fmnew;
     LANE_PROBE(2);
-    if (fmin(zeta, 1.0) < 0.0) {
+    const double zeta1 = ic::minc(zeta, 1.0);
+    if (ic::lt0(zeta1)) {
         LANE_PROBE(11);
-        const double tmp1 = xpow(1.0 - 16.0 * fmin(zeta, 1.0), 0.25);
+        const double tmp1 = xpow(1.0 - 16.0 * zeta1, 0.25);
         fmnew = 2.0 * xlog((1.0 + tmp1) / 2.0) + xlog((1.0 + tmp1 * tmp1) / 2.0) - 2.0 * xatan(tmp1) + 1.5707963;
     } else {
-        fmnew = -5.0 * fmin(zeta, 1.0);
+        fmnew = -5.0 * zeta1;
     }
     fm = (iter == 1) ? fmnew : 0.5 * (fm + fmnew);
-    double zeta10 = fmin(10.0 / obu, 1.0);
-    if (zeta == 0.0) zeta10 = 0.0;
+    double zeta10 = ic::minc(10.0 / obu, 1.0);
+    if (!ic::ne0(zeta)) zeta10 = 0.0;
     double fm10;
-    if (zeta10 < 0.0) {
+    if (ic::lt0(zeta10)) {
         const double tmp1 = xpow(1.0 - 16.0 * zeta10, 0.25);
         fm10 = 2.0 * xlog((1.0 + tmp1) / 2.0) + xlog((1.0 + tmp1 * tmp1) / 2.0) - 2.0 * xatan(tmp1) + 1.5707963;
     } else {
@@ -638,13 +641,13 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, const PatchK& K, Err& err, d
     const double svpts = s.el;
     const double eah = forc_pbot * s.qaf / 0.622;
     s.rhaf_last = eah / svpts;
-    s.vpd_last = fmax((svpts - eah), 50.0) * 0.001;
+    s.vpd_last = ic::maxc((svpts - eah), 50.0) * 0.001;
     const double thm = io.thm[p], btran = io.btran[p];
     const double laisun = io.laisun[p], laisha = io.laisha[p];
     const double oair = io.forc_po2[g], cair = io.forc_pco2[g];
     const double parsun = io.parsun_z[p], parsha = io.parsha_z[p];
     PsnTemp T;
-    psn_temp(A, s, K, forc_pbot, oair, parsun > 0.0 || parsha > 0.0, T);
+    psn_temp(A, s, K, forc_pbot, oair, ic::gt0(parsun) || ic::gt0(parsha), T);
     // sunlit then shaded phase (PhotosynthesisMod called with phase='sun' and
     // 'sha', CanopyFluxesMod.F90:1143-1169); a loop, so the phase body and
     // its root finder are compiled once
@@ -669,24 +672,24 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, const PatchK& K, Err& err, d
     const double wtga = s.wta0 + wtg0 + 0.0;
     s.wtal = s.wta0 + s.wtl0 + 0.0;
     const double fdry = io.fdry[p], fwet = io.fwet[p];
-    const double rppdry = (fdry > 0.0) ? fdry * rb * (laisun / (rb + s.sun.rs) + laisha / (rb + s.sha.rs)) / elai : 0.0;
+    const double rppdry = ic::gt0(fdry) ? fdry * rb * (laisun / (rb + s.sun.rs) + laisha / (rb + s.sha.rs)) / elai : 0.0;
     const double forc_rho = io.forc_rho[c], forc_q = io.forc_q[c], qg = io.qg[c], t_grnd = io.t_grnd[c];
     double efpot = forc_rho * ((elai + esai) / rb) * (s.qsatl - s.qaf);
     const double h2ocan = K.liqcan + K.snocan;
     double rpp;
-    if (efpot > 0.0) {
-        if (btran > 0.0) { s.qflx_tran_veg = efpot * rppdry; rpp = rppdry + fwet; }
+    if (ic::gt0(efpot)) {
+        if (ic::gt0(btran)) { s.qflx_tran_veg = efpot * rppdry; rpp = rppdry + fwet; }
         else { rpp = fwet; s.qflx_tran_veg = 0.0; }
         rpp = fmin(rpp, (s.qflx_tran_veg + h2ocan / dtime) / efpot);
     } else {
         rpp = 1.0;
         s.qflx_tran_veg = 0.0;
     }
-    const double fv = (double)io.frac_veg_nosno[p];
+    const double fv = fm::i2d(io.frac_veg_nosno[p]);
     const double wtaq = fv / s.raw_a;
     const double wtlq = fv * (elai + esai) / rb * rpp;
     const double rdl = K.one_m_edl / (0.004 * s.uaf);
-    s.wtgq = (s.delq < 0.0) ? fv / (raw_b + rdl) : fv / (raw_b + io.soilresis[c]);
+    s.wtgq = ic::lt0(s.delq) ? fv / (raw_b + rdl) : fv / (raw_b + io.soilresis[c]);
     const double wtsqi = 1.0 / (wtaq + wtlq + s.wtgq);
     const double wtgq0 = s.wtgq * wtsqi;
     s.wtlq0 = wtlq * wtsqi;
@@ -698,7 +701,7 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, const PatchK& K, Err& err, d
     const double efsh = dc1 * (wtga * s.t_veg - wtg0 * t_grnd - s.wta0 * thm - 0.0);
     s.efe = dc2 * (wtgaq * s.qsatl - wtgq0 * qg - s.wtaq0 * forc_q);
     double erre = 0.0;
-    if (s.efe * s.efeb < 0.0) {
+    if (ic::lt0(s.efe * s.efeb)) {
         const double efeold = s.efe;
         s.efe = 0.1 * efeold;
         erre = s.efe - efeold;
@@ -714,7 +717,7 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, const PatchK& K, Err& err, d
     const double dels = dt_veg;
     s.del = fabs(dels);
     s.err = 0.0;
-    if (s.del > 1.0) {
+    if (ic::gtc(s.del, 1.0)) {
         dt_veg = 1.0 * dels / s.del;
         s.t_veg = s.tlbef + dt_veg;
         const double tb3 = ipow3(s.tlbef);
@@ -725,8 +728,8 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, const PatchK& K, Err& err, d
     s.dt_veg = dt_veg;
     efpot = forc_rho * ((elai + esai) / rb) * (wtgaq * (s.qsatl + s.qsatldT * dt_veg) - wtgq0 * qg - s.wtaq0 * forc_q);
     s.qflx_evap_veg = rpp * efpot;
-    s.qflx_tran_veg = (efpot > 0.0 && btran > 0.0) ? efpot * rppdry : 0.0;
-    const double ecidif = fmax(0.0, s.qflx_evap_veg - s.qflx_tran_veg - h2ocan / dtime);
+    s.qflx_tran_veg = (ic::gt0(efpot) && ic::gt0(btran)) ? efpot * rppdry : 0.0;
+    const double ecidif = ic::max0(s.qflx_evap_veg - s.qflx_tran_veg - h2ocan / dtime);
     s.qflx_evap_veg = fmin(s.qflx_evap_veg, s.qflx_tran_veg + h2ocan / dtime);
     s.eflx_sh_veg = efsh + dc1 * wtga * dt_veg + s.err + erre + HVAP * ecidif;
     s.lw_leaf = 0.0 * io.emv[p] * SB * ipow3(s.tlbef) * (s.tlbef + 4.0 * dt_veg);
@@ -741,17 +744,18 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, const PatchK& K, Err& err, d
     const double forc_th = io.forc_th[c], thv = io.thv[c];
     const double thvstar = tstar * (1.0 + 0.61 * forc_q) + 0.61 * forc_th * qstar;
     double zeta = K.zldis * VKC * GRAV * thvstar / ((ustar * ustar) * thv);
-    if (zeta >= 0.0) {
-        zeta = fmin(P.zetamaxstable, fmax(zeta, 0.01));
-        s.um = fmax(K.ur, 0.1);
+    if (ic::ge0(zeta)) {
+        zeta = fmin(P.zetamaxstable, ic::maxc(zeta, 0.01));
+        s.um = ic::maxc(K.ur, 0.1);
     } else {
-        zeta = fmax(-100.0, fmin(zeta, -0.01));
-        const double wc = (ustar * thvstar > 0.0) ? 0.0 : 1.0 * xpow(-GRAV * ustar * thvstar * 1000.0 / thv, 0.333);
+        zeta = ic::ltn(zeta, -0.01) ? zeta : -0.01;
+        zeta = ic::gtn(zeta, -100.0) ? zeta : -100.0;
+        const double wc = ic::gt0(ustar * thvstar) ? 0.0 : 1.0 * xpow(-GRAV * ustar * thvstar * 1000.0 / thv, 0.333);
         s.um = sqrt(K.ur * K.ur + wc * wc);
     }
     s.zeta = zeta;
     s.obu = K.zldis / zeta;
-    if (s.obuold * s.obu < 0.0) s.nmozsgn = s.nmozsgn + 1;
+    if (ic::lt0(s.obuold * s.obu)) s.nmozsgn = s.nmozsgn + 1;
     if (s.nmozsgn >= 4) s.obu = K.zldis / (-0.01);
     s.obuold = s.obu;
     s.itlef = s.itlef + 1;
@@ -760,7 +764,7 @@ __device__ bool pass(const CanopyArgs& A, Patch& s, const PatchK& K, Err& err, d
         s.efeb = s.efe;
         const double det = fmax(s.del, del2);
         s.num_iter = s.itlef;
-        if (det < 0.01 && dele < 0.1) return true;
+        if (ic::ltc(det, 0.01) && ic::ltc(dele, 0.1)) return true;
     }
     return s.itlef > A.itmax;
 }

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include "ctsm_gpu.h"
 #include "ctsm_device.cuh"
+#include "fcmp.cuh"
 
 namespace ctsmg {
 
@@ -17,11 +18,11 @@ __device__ __forceinline__ void set_soil_water_fractions(const ctsmg_soilwater_i
         const double ws = io.watsat[g];
         const double dz_ext = io.dz[ix] + 0.0 / DENICE;
         const double a = io.h2osoi_ice[ix] + 0.0, q = a / (dz_ext * DENICE);
-        const double vol_ice = (q < ws) ? q : ws;
+        const double vol_ice = ic::lt(q, ws) ? q : ws;
         const double ep = ws - vol_ice;
-        ((double*)io.eff_porosity)[g] = (0.01 < ep) ? ep : 0.01;
+        ((double*)io.eff_porosity)[g] = ic::gtc(ep, 0.01) ? ep : 0.01;
         const double f = vol_ice / ws;
-        io.icefrac[g] = (f < 1.0) ? f : 1.0;
+        io.icefrac[g] = ic::ltc(f, 1.0) ? f : 1.0;
     }
 }
 
@@ -34,13 +35,13 @@ __device__ __forceinline__ void flexcn_column(const ctsmg_soilwater_io& io, int 
 #pragma unroll 1
     for (int j = 1; j <= NLEVSOI - 1; ++j) {
         const size_t ix = c + (size_t)(j - LS) * ld, ixn = ix + ld;
-        const double xs = carry < 0.0 ? watmin - carry : 0.0;
+        const double xs = ic::lt0(carry) ? watmin - carry : 0.0;
         liq[ix] = carry + xs;
         carry = liq[ixn] - xs;
         liq[ixn] = carry;
     }
     const size_t ib = c + (size_t)(NLEVSOI - LS) * ld;
-    const double xs = carry < watmin ? watmin - carry : 0.0;
+    const double xs = ic::ltc(carry, watmin) ? watmin - carry : 0.0;
     liq[ib] = carry + xs;
     io.wa[c] = io.wa[c] - xs;
 #pragma unroll 1

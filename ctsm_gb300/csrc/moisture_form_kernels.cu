@@ -31,7 +31,10 @@ namespace {
 constexpr double M_TO_MM = 1.e3;
 constexpr int N1 = NLEVSOI + 2;
 
-// std::max / std::min semantics ((a < b) ? b : a), as the oracle evaluates them
+// std::max / std::min semantics ((a < b) ? b : a), as the oracle evaluates
+// them.  Comparisons of the level loop against constants run on the integer
+// pipe (fcmp.cuh); these two-variable ones, outside it, stay FP64 compares,
+// which need fewer registers than their integer form.
 __device__ __forceinline__ double fmx(double a, double b) { return (a < b) ? b : a; }
 __device__ __forceinline__ double fmn(double a, double b) { return (b < a) ? b : a; }
 
@@ -54,10 +57,10 @@ __device__ __forceinline__ void suction(const ColView& k, int j, double s2, doub
 }
 
 __device__ __forceinline__ double rel_sat(const ColView& k, int j, double liq) {
-    const double vwc = fmx(liq, 1.0e-6) / (k.ss(k.io.dz, j) * DENH2O);
+    const double vwc = (ic::ltc(liq, 1.0e-6) ? 1.0e-6 : liq) / (k.ss(k.io.dz, j) * DENH2O);
     double s2 = vwc / k.g(k.io.watsat, j);
-    s2 = fmn(s2, 1.0);
-    return fmx(0.01, s2);
+    s2 = ic::gtc(s2, 1.0) ? 1.0 : s2;
+    return ic::gtc(s2, 0.01) ? s2 : 0.01;
 }
 } // namespace
 
@@ -92,7 +95,7 @@ __device__ __forceinline__ void mf_begin(MFLane<EXPENSIVE>& L, const ctsmg_soilw
     if (L.wt) {
 #pragma unroll 1
         for (int j = 1; j <= NLEVSOI; ++j)
-            if (L.zwt <= k.zi(j)) { L.jwt = j - 1; break; }
+            if (ic::le(L.zwt, k.zi(j))) { L.jwt = j - 1; break; }
     }
 #pragma unroll 1
     for (int j = 1; j <= L.nl; ++j) L.liq[j] = k.ss(io.h2osoi_liq, j);
@@ -141,15 +144,15 @@ __device__ int mf_trial(MFLane<EXPENSIVE>& L, const ctsmg_soilwater_io& io, cons
             s1 = 0.5 * (s2c + s2n);
             imped = pow10_dd(-P.e_ice * (0.5 * (k.g(io.icefrac, j) + k.g(io.icefrac, j + 1))));
         }
-        s1 = fmn(s1, 1.0);
-        s1 = fmx(0.01, s1);
+        s1 = ic::gtc(s1, 1.0) ? 1.0 : s1;
+        s1 = ic::gtc(s1, 0.01) ? s1 : 0.01;
         const double ws = k.g(io.watsat, j), bsw = k.g(io.bsw, j);
         const double hkj = imped * k.g(io.hksat, j) * fm::pow(s1, 2.0 * bsw + 3.0);
         const double dhkdw = (2.0 * bsw + 3.0) * hkj / s1;
         io.smp_l[L.c + (j - 1) * ld] = smp_c;
         io.hk_l[L.c + (j - 1) * ld] = hkj;
         if (wt && j == jwt + 1) {
-            L.vwc_q = fmx(L.liq[j], 1.0e-6) / (k.ss(io.dz, j) * DENH2O);
+            L.vwc_q = (ic::ltc(L.liq[j], 1.0e-6) ? 1.0e-6 : L.liq[j]) / (k.ss(io.dz, j) * DENH2O);
             L.imped_q = imped;
         }
         // flux out of the bottom of level j and its derivatives
@@ -193,8 +196,8 @@ __device__ int mf_trial(MFLane<EXPENSIVE>& L, const ctsmg_soilwater_io& io, cons
         } else {
             // dgtsv elimination step i = j-2 (0-based) on rows j-1 (pending) and j
             double dl = amx, dn = bmx, dun = cmx, bn = rmx;
-            if (fabs(d_p) >= fabs(dl)) {
-                if (d_p == 0.0) { *info = j - 1; return MF_SINGULAR; }
+            if (ic::abs_ge(d_p, dl)) {
+                if (!ic::ne0(d_p)) { *info = j - 1; return MF_SINGULAR; }
                 const double fact = dl / d_p;
                 dn = dn - fact * du_p;
                 bn = bn - fact * b_p;
@@ -218,7 +221,7 @@ __device__ int mf_trial(MFLane<EXPENSIVE>& L, const ctsmg_soilwater_io& io, cons
         qin = qo; dqidw0 = dq1; dqidw1 = dq2;
         s2c = s2n; smp_c = smp_n; dsmpdw_c = dsmpdw_n;
     }
-    if (d_p == 0.0) { *info = nl; return MF_SINGULAR; }
+    if (!ic::ne0(d_p)) { *info = nl; return MF_SINGULAR; }
     d[nl] = d_p; du[nl] = du_p; b[nl] = b_p;
     // back substitution (1-based rows here)
     b[nl] = b[nl] / d[nl];
@@ -276,7 +279,7 @@ __device__ void mf_finish(MFLane<EXPENSIVE>& L, const ctsmg_soilwater_io& io, co
 #pragma unroll 1
     for (int j = nl; j >= 2; --j) {
         const double cap = k.g(io.eff_porosity, j) * M_TO_MM * k.ss(io.dz, j);
-        const double over = fmx(L.liq[j] - cap, 0.0);
+        const double over = ic::lt0(L.liq[j] - cap) ? 0.0 : L.liq[j] - cap;
         L.liq[j] = fmn(cap, L.liq[j]);
         L.liq[j - 1] = L.liq[j - 1] + over;
     }
@@ -291,8 +294,9 @@ __device__ void mf_finish(MFLane<EXPENSIVE>& L, const ctsmg_soilwater_io& io, co
     if (L.wt && jwt < NLEVSOI) {
         const double zwt = L.zwt;
         const double wh_zwt = -k.g(io.sucsat, jwt + 1) - zwt * M_TO_MM;
-        double s1 = fmx(L.vwc_q / k.g(io.watsat, jwt + 1), 0.01);
-        s1 = fmn(1.0, s1);
+        double s1 = L.vwc_q / k.g(io.watsat, jwt + 1);
+        s1 = ic::ltc(s1, 0.01) ? 0.01 : s1;
+        s1 = ic::ltc(s1, 1.0) ? s1 : 1.0;
         const double ka = L.imped_q * k.g(io.hksat, jwt + 1) * fm::pow(s1, 2.0 * k.g(io.bsw, jwt + 1) + 3.0);
         const int jm = jwt > 1 ? jwt : 1;
         const double smp1 = fmx(io.smpmin[c], io.smp_l[c + (size_t)(jm - 1) * k.ld]);

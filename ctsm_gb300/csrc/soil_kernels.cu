@@ -62,9 +62,9 @@ __device__ __forceinline__ ZdLevel zd09_level(const ctsmg_soilwater_io& io, int 
     const Recip rws = recip(ws);
     // :649-665 ice fraction and liquid content
     const double vol_ice = ic::min(ws, divf(io.h2osoi_ice[ss_ix], dzj * DENICE));
-    L.icef = ic::min(1.0, divr(vol_ice, rws));
+    L.icef = ic::minc(divr(vol_ice, rws), 1.0);
     io.icefrac[g_ix] = L.icef;
-    L.vwc = divf(ic::max(io.h2osoi_liq[ss_ix], 1.0e-6), dzj * DENH2O);
+    L.vwc = divf(ic::maxc(io.h2osoi_liq[ss_ix], 1.0e-6), dzj * DENH2O);
     // :670-712 equilibrium volumetric water and matric potential: water table
     // above the layer, inside it, below it.  temp0 is the same expression in
     // the last two cases and tempi is only needed in the last, so each power
@@ -84,16 +84,16 @@ __device__ __forceinline__ ZdLevel zd09_level(const ctsmg_soilwater_io& io, int 
         double voleq1 = divf(divf(-ss * ws, omb), zwtmm - zimm_prev) * (tempi - temp0);
         veq = divf(voleq1 * (zwtmm - zimm_prev) + ws * (L.zimm - zwtmm), L.zimm - zimm_prev);
         veq = ic::min(ws, veq);
-        veq = ic::max(veq, 0.0);
+        veq = ic::max0(veq);
     } else {
         veq = divf(divf(-ss * ws, omb), L.zimm - zimm_prev) * (tempi - temp0);
-        veq = ic::max(veq, 0.0);
+        veq = ic::max0(veq);
         veq = ic::min(ws, veq);
     }
-    L.zq = ic::max(smpmin, -ss * fm::pow(ic::max(divr(veq, rws), 0.01), -bb));
+    L.zq = ic::max(smpmin, -ss * fm::pow(ic::maxc(divr(veq, rws), 0.01), -bb));
     // :740-760 node matric potential and its derivative
-    double s_node = ic::max(divr(L.vwc, rws), 0.01);
-    s_node = ic::min(1.0, s_node);
+    double s_node = ic::maxc(divr(L.vwc, rws), 0.01);
+    s_node = ic::minc(s_node, 1.0);
     const double sm = ic::max(smpmin, -ss * fm::pow(s_node, -bb));
     L.smp = sm;
     L.dsmpdw = divf(-bb * sm, L.vwc);
@@ -124,7 +124,7 @@ __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, d
     }
     // :649-665 water content at the water table (frozen case)
     double vwc_zwt = G(io.watsat, NLEVSOI);
-    if (ic::lt(SS(io.t_soisno, jwt + 1), TFRZ)) {
+    if (ic::ltc(SS(io.t_soisno, jwt + 1), TFRZ)) {
         vwc_zwt = fmax(SS(io.h2osoi_liq, NLEVSOI), 1.0e-6) / (SS(io.dz, NLEVSOI) * DENH2O);
 #pragma unroll 1
         for (int j = NLEVSOI; j <= NLEVGRND; ++j) {
@@ -171,7 +171,7 @@ __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, d
         ZdLevel nx = bottom ? cur : zd09_level(io, c, j + 1, cur.zimm, zwtmm, smpmin);
         // :716-737 interface conductivity and its derivative (jp = min(nlevsoi, j+1))
         const Recip rB = recip(cur.ws + nx.ws);
-        const double s1 = ic::min(1.0, divr(cur.vwc + nx.vwc, rB));
+        const double s1 = ic::minc(divr(cur.vwc + nx.vwc, rB), 1.0);
         const double s2 = cur.hks * fm::pow(s1, 2.0 * cur.bb + 2.0);
         const double imped = pow10_dd(-e_ice * (0.5 * (cur.icef + nx.icef)));
         const double hk = imped * s1 * s2;
@@ -243,7 +243,7 @@ __device__ void zd09_column(const ctsmg_soilwater_io& io, int c, double e_ice, d
         double& liq = io.h2osoi_liq[c + (size_t)(j - LS) * ld];
         double v = liq + rr[j] * (SS(io.dz, j) * 1.e3);
         liq = v;
-        if (ic::lt(v, 0.0)) deficit = deficit - v;
+        if (ic::lt0(v)) deficit = deficit - v;
     }
     double qcharge;
     if (jwt < NLEVSOI) {
@@ -332,9 +332,9 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
                 t = THK_BEDROCK;
             } else {
                 double satw = divf(divr(liq, R_DENH2O) + divr(ice, R_DENICE) + 0.0 / DENICE, dzj * ws);
-                satw = ic::min(1.0, satw);
-                if (ic::gt(satw, .1e-6)) {
-                    double dke = ic::ge(T[ssi(j)], TFRZ) ? ic::max(0.0, fm::log10(satw) + 1.0) : satw;
+                satw = ic::minc(satw, 1.0);
+                if (ic::gtc(satw, .1e-6)) {
+                    double dke = ic::gec(T[ssi(j)], TFRZ) ? ic::max0(fm::log10(satw) + 1.0) : satw;
                     const double xl = divf(liq, DENH2O * dzj);
                     double fl = divf(xl, xl + divf(ice, DENICE * dzj) + zero_over(DENICE * dzj));
                     double dksat = io.tkmg[gi(j)] * tkwat_tkice_pow(fl * ws, (1.0 - fl) * ws);
@@ -345,7 +345,7 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
             }
             cv = io.csol[gi(j)] * (1.0 - ws) * dzj + (ice * CPICE + liq * CPLIQ) + 0.0 * CPICE;
             if (j > nbedrock) cv = CSOL_BEDROCK * dzj;
-            if (j == 1 && ic::gt(io.h2osno_no_layers[c], 0.0)) cv = cv + CPICE * io.h2osno_no_layers[c];
+            if (j == 1 && ic::gt0(io.h2osno_no_layers[c])) cv = cv + CPICE * io.h2osno_no_layers[c];
         } else {
             const double liq = LIQ[ssi(j)], ice = ICE[ssi(j)];
             double b = divf(ice + liq, frac_sno * DZ(j));
@@ -353,10 +353,10 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
             if (snow_method == 0) {
                 t = TKAIR + (7.75e-5 * b + 1.105e-6 * b * b) * (TKICE - TKAIR);
             } else {
-                if (ic::le(b, 156.0)) t = sp(0.023f) + sp(0.234f) * (b / 1000);
+                if (ic::lec(b, 156.0)) t = sp(0.023f) + sp(0.234f) * (b / 1000);
                 else t = sp(0.138f) - sp(1.01f) * (b / 1000) + (sp(3.233f) * ((b / 1000) * (b / 1000)));
             }
-            cv = ic::gt(frac_sno, 0.0) ? ic::max(THIN_SFCLAYER, divr(CPLIQ * liq + CPICE * ice, rfsno)) : THIN_SFCLAYER;
+            cv = ic::gt0(frac_sno) ? ic::maxc(divr(CPLIQ * liq + CPICE * ice, rfsno), THIN_SFCLAYER) : THIN_SFCLAYER;
         }
         io.thk[ssi(j)] = t;
         double f;
@@ -398,7 +398,7 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
     double hs_soil = 0.0, hs_h2osfc = 0.0, dhsdT = 0.0, hs_top_snow = 0.0;
 #pragma unroll 1
     for (int p = p0; p < p0 + np; ++p) {
-        const double fv = (double)io.frac_veg_nosno[p];
+        const double fv = fm::i2d(io.frac_veg_nosno[p]);
         const double dl = io.dlrad[p], lw = (1.0 - fv) * emg * forc_lwrad;
         double gnet = io.sabg[p] + dl + lw - lwrad_emit - (io.eflx_sh_grnd[p] + io.qflx_evap_soi[p] * htvp);
         io.eflx_gnet[p] = gnet;
@@ -414,7 +414,7 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
     }
 #pragma unroll 1
     for (int p = p0; p < p0 + np; ++p) {
-        const double fv = (double)io.frac_veg_nosno[p];
+        const double fv = fm::i2d(io.frac_veg_nosno[p]);
         const double w = io.wtcol[p];
         const double* sl = io.sabg_lyr;
         const size_t ldp = io.ldp;
@@ -725,18 +725,18 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
         int imelt = 0;
         double tinc = 0.0, supercool = 0.0;
         if (j <= 0) {
-            if (ic::gt(wice0, 0.0) && ic::gt(tj, TFRZ)) { imelt = 1; tinc = TFRZ - tj; tj = TFRZ; }
-            if (ic::gt(wliq0, 0.0) && ic::lt(tj, TFRZ)) { imelt = 2; tinc = TFRZ - tj; tj = TFRZ; }
+            if (ic::gt0(wice0) && ic::gtc(tj, TFRZ)) { imelt = 1; tinc = TFRZ - tj; tj = TFRZ; }
+            if (ic::gt0(wliq0) && ic::ltc(tj, TFRZ)) { imelt = 2; tinc = TFRZ - tj; tj = TFRZ; }
         } else {
-            if (ic::gt(wice0, 0.0) && ic::gt(tj, TFRZ)) { imelt = 1; tinc = TFRZ - tj; tj = TFRZ; }
-            if (ic::lt(tj, TFRZ)) {
+            if (ic::gt0(wice0) && ic::gtc(tj, TFRZ)) { imelt = 1; tinc = TFRZ - tj; tj = TFRZ; }
+            if (ic::ltc(tj, TFRZ)) {
                 double smp = divf(HFUS * (TFRZ - tj), GRAV * tj) * 1000.0;
                 supercool = io.watsat[gi(j)] * fm::pow(divf(smp, io.sucsat[gi(j)]), divf(-1.0, io.bsw[gi(j)]));
                 supercool = supercool * DZ(j) * 1000.0;
             }
-            if (ic::gt(wliq0, supercool) && ic::lt(tj, TFRZ)) { imelt = 2; tinc = TFRZ - tj; tj = TFRZ; }
-            if (j == 1 && ic::gt(io.h2osno_no_layers[c], 0.0)) {
-                if (ic::gt(tj, TFRZ)) { imelt = 1; tinc = TFRZ - tj; tj = TFRZ; }
+            if (ic::gt(wliq0, supercool) && ic::ltc(tj, TFRZ)) { imelt = 2; tinc = TFRZ - tj; tj = TFRZ; }
+            if (j == 1 && ic::gt0(io.h2osno_no_layers[c])) {
+                if (ic::gtc(tj, TFRZ)) { imelt = 1; tinc = TFRZ - tj; tj = TFRZ; }
             }
         }
         const double fj = fact[L(j)];
@@ -753,8 +753,8 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
                 else hm = divf(-tinc, fj);
             }
         }
-        if (imelt == 1 && ic::lt(hm, 0.0)) { hm = 0.0; imelt = 0; }
-        if (imelt == 2 && ic::gt(hm, 0.0)) { hm = 0.0; imelt = 0; }
+        if (imelt == 1 && ic::lt0(hm)) { hm = 0.0; imelt = 0; }
+        if (imelt == 2 && ic::gt0(hm)) { hm = 0.0; imelt = 0; }
         double ice = wice0, liq = wliq0;
         if (imelt > 0 && ic::abs_gt0(hm)) {
             double xm = divr(hm * dtime, R_HFUS);
@@ -774,16 +774,16 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
                 }
             }
             double heatr = 0.0;
-            if (ic::gt(xm, 0.0)) {
-                ice = ic::max(0.0, wice0 - xm);
+            if (ic::gt0(xm)) {
+                ice = ic::max0(wice0 - xm);
                 if (j >= 1) heatr = hm - divr(HFUS * (0.0 - 0.0 + wice0 - ice), rdt);
                 else heatr = hm - divr(HFUS * (wice0 - ice), rdt);
-            } else if (ic::lt(xm, 0.0)) {
+            } else if (ic::lt0(xm)) {
                 if (j <= 0) ice = ic::min(wmass0, wice0 - xm);
                 else ice = ic::lt(wmass0 - 0.0, supercool) ? 0.0 : ic::min(wmass0 - 0.0 - supercool, wice0 - xm);
                 heatr = hm - divr(HFUS * (wice0 - ice), rdt);
             }
-            liq = ic::max(0.0, wmass0 - ice - 0.0);
+            liq = ic::max0(wmass0 - ice - 0.0);
             if (ic::abs_gt0(heatr)) {
                 if (j == snl + 1) {
                     if (j == 1) tj = tj + fj * heatr / (1.0 - (1.0 - frac_h2osfc) * fj * dhsdT);
@@ -792,22 +792,22 @@ __device__ int soiltemp_column(const ctsmg_soiltemp_io& io, int c, int begp, dou
                     tj = tj + fj * heatr / (1.0 - (1.0 - frac_sno - frac_h2osfc) * fj * dhsdT);
                 } else {
                     if (j > 0) tj = tj + fj * heatr;
-                    else if (ic::gt(frac_sno, 0.0)) tj = tj + divr(fj, rfsno) * heatr;
+                    else if (ic::gt0(frac_sno)) tj = tj + divr(fj, rfsno) * heatr;
                 }
                 if (j <= 0) {
-                    if (ic::gt(liq * ice, 0.0)) tj = TFRZ;
+                    if (ic::gt0(liq * ice)) tj = TFRZ;
                 }
             }
             if (j >= 1) xmf = xmf + divr(HFUS * (wice0 - ice), rdt) + zero_over(dtime);
             else xmf = xmf + divr(HFUS * (wice0 - ice), rdt);
             if (imelt == 1 && j < 1) {
-                double m = divr(ic::max(0.0, (wice0 - ice)), rdt);
+                double m = divr(ic::max0(wice0 - ice), rdt);
                 io.qflx_snomelt_lyr[ix] = m;
                 qflx_snomelt = qflx_snomelt + m;
                 io.snomelt_accum[c] = io.snomelt_accum[c] + m * dtime * 1.e-3;
             }
             if (imelt == 2 && j < 1) {
-                double f = divr(ic::max(0.0, (ice - wice0)), rdt);
+                double f = divr(ic::max0(ice - wice0), rdt);
                 io.qflx_snofrz_lyr[ix] = f;
                 qflx_snofrz = qflx_snofrz + f;
             }

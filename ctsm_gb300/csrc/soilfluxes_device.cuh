@@ -7,6 +7,7 @@
 #include <cstdint>
 #include "ctsm_gpu.h"
 #include "ctsm_device.cuh"
+#include "fastmath.cuh"
 
 namespace ctsmg {
 namespace sfx {
@@ -70,7 +71,7 @@ __device__ __forceinline__ void soilfluxes_patch(const ctsmg_soilfluxes_io& io, 
     const double emg = io.emg[c], forc_lwrad = io.forc_lwrad[c];
     const double lw_grnd = (fsno * p4(SS(io.tssbef, jtop)) + (1.0 - fsno - fh2o) * p4(SS(io.tssbef, 1)) +
                             fh2o * p4(th2o_bef));
-    const double fv = (double)(1 - io.frac_veg_nosno[p]);
+    const double fv = fm::i2d(1 - io.frac_veg_nosno[p]);
     const double esg = ((1.0 - fsno) * io.sabg_soil[p] + fsno * io.sabg_snow[p]) + io.dlrad[p] + fv * emg * forc_lwrad -
                        emg * SB * lw_grnd - emg * SB * p3(t_grnd0) * (4.0 * tinc) - (sh + ev * htvp);
     // totals and partitions (:375-393)

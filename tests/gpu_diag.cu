@@ -10,9 +10,11 @@
 //     reciprocal RN(1/b[i]) (3n doubles).
 //   ctsmg_diag_fcmp(n, a, b, out): the integer-pipe comparisons of fcmp.cuh
 //     beside the FP64 ones -- rows 0-7 a<b, a<=b, a>b, a>=b, a==b, a!=0,
-//     |a|>0 (IEEE; row 7 unused), rows 8-15 the same from fcmp.cuh, rows
-//     16-19 fmin(a,b), fmax(a,b), ic::min, ic::max, row 20 fm::i2d(i - n/2)
-//     (21n doubles).
+//     |a|>0 (IEEE), row 7 fmax(a, 0), rows 8-14 the same from fcmp.cuh, rows
+//     16-19 fmin(a,b), fmax(a,b), ic::min, ic::max, row 20 fm::i2d(i - n/2),
+//     rows 21-24 ic::ltc, lec, gtc, gec (b > 0) or ltn, -, gtn, - (b < 0),
+//     rows 25-28 ic::lt0, le0, gt0, ge0 of a, rows 29-31 ic::minc(a, b),
+//     ic::maxc(a, b) (b > 0), ic::max0(a) (32n doubles).
 // Host arrays in and out.  Built by tests/gpu_diag.py with nvcc for sm_103a.
 #include <cuda_runtime.h>
 #include <cstdint>
@@ -121,11 +123,16 @@ __global__ void diag_fcmp_kernel(int n, const double* __restrict__ a, const doub
     const double x = a[i], y = b[i];
     auto put = [&](int row, double v) { out[(size_t)row * n + i] = v; };
     put(0, x < y); put(1, x <= y); put(2, x > y); put(3, x >= y); put(4, x == y); put(5, x != 0.0);
-    put(6, fabs(x) > 0.0); put(7, 0.0);
+    put(6, fabs(x) > 0.0); put(7, fmax(x, 0.0));
     put(8, ic::lt(x, y)); put(9, ic::le(x, y)); put(10, ic::gt(x, y)); put(11, ic::ge(x, y));
     put(12, ic::eq(x, y)); put(13, ic::ne0(x)); put(14, ic::abs_gt0(x)); put(15, 0.0);
     put(16, fmin(x, y)); put(17, fmax(x, y)); put(18, ic::min(x, y)); put(19, ic::max(x, y));
     put(20, fm::i2d(i - n / 2));
+    const bool pos = y > 0.0;
+    put(21, pos ? ic::ltc(x, y) : ic::ltn(x, y)); put(22, pos ? ic::lec(x, y) : 0.0);
+    put(23, pos ? ic::gtc(x, y) : ic::gtn(x, y)); put(24, pos ? ic::gec(x, y) : 0.0);
+    put(25, ic::lt0(x)); put(26, ic::le0(x)); put(27, ic::gt0(x)); put(28, ic::ge0(x));
+    put(29, pos ? ic::minc(x, y) : 0.0); put(30, pos ? ic::maxc(x, y) : 0.0); put(31, ic::max0(x));
 }
 } // namespace ctsmg
 
@@ -134,14 +141,14 @@ extern "C" int32_t ctsmg_diag_fcmp(int32_t n, const double* a, const double* b, 
     if (n <= 0 || !a || !b || !out) return CTSMG_E_ARG;
     double* d = nullptr;
     const size_t nb = (size_t)n * 8;
-    cudaError_t e = cudaMalloc(&d, 23 * nb);
+    cudaError_t e = cudaMalloc(&d, 34 * nb);
     if (e == cudaSuccess) e = cudaMemcpy(d, a, nb, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(d + n, b, nb, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
         diag_fcmp_kernel<<<(n + 127) / 128, 128>>>(n, d, d + n, d + 2 * (size_t)n);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * (size_t)n, 21 * nb, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * (size_t)n, 32 * nb, cudaMemcpyDeviceToHost);
     if (d) cudaFree(d);
     return diag_fail(e);
 }

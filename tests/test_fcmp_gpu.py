@@ -3,7 +3,8 @@ against the device's FP64 instructions over random and edge-case pairs
 (signed zeros, subnormals, infinities, NaN of either sign, equal operands,
 the literals the soil kernels compare against): every comparison gives the
 same truth value, min / max the same value (a NaN operand yields the other
-operand, as fmin / fmax), and fm::i2d builds (double)k exactly."""
+operand, as fmin / fmax), the forms against a positive or negative constant
+or zero agree likewise, and fm::i2d builds (double)k exactly."""
 import numpy as np
 import pytest
 
@@ -40,9 +41,9 @@ def test_integer_pipe_comparisons_match_fp64(gpu_lib):
     P = C.POINTER(C.c_double)
     a, b = _pairs()
     n = a.size
-    out = np.zeros(21 * n)
+    out = np.zeros(32 * n)
     check(L.ctsmg_diag_fcmp(n, a.ctypes.data_as(P), b.ctypes.data_as(P), out.ctypes.data_as(P)))
-    o = out.reshape(21, n)
+    o = out.reshape(32, n)
     for k in range(7):
         assert np.array_equal(o[k], o[8 + k]), (k, a[o[k] != o[8 + k]][:4], b[o[k] != o[8 + k]][:4])
     with np.errstate(invalid="ignore"):
@@ -52,3 +53,18 @@ def test_integer_pipe_comparisons_match_fp64(gpu_lib):
         assert same.all(), (a[~same][:4], b[~same][:4])
     k = np.arange(n) - n // 2
     np.testing.assert_array_equal(o[20], k.astype(np.float64))
+    # the constant forms (a positive or negative second operand, and zero)
+    with np.errstate(invalid="ignore"):
+        pos, neg = b > 0, b < 0
+        np.testing.assert_array_equal(o[21][pos], (a < b)[pos]); np.testing.assert_array_equal(o[21][neg], (a < b)[neg])
+        np.testing.assert_array_equal(o[23][pos], (a > b)[pos]); np.testing.assert_array_equal(o[23][neg], (a > b)[neg])
+        np.testing.assert_array_equal(o[22][pos], (a <= b)[pos]); np.testing.assert_array_equal(o[24][pos], (a >= b)[pos])
+        for row, ref in ((25, a < 0), (26, a <= 0), (27, a > 0), (28, a >= 0)):
+            np.testing.assert_array_equal(o[row], ref.astype(float))
+    # min / max against the device's fmin / fmax (numpy's fmin returns NaN for
+    # a signalling-NaN operand on some hosts; the device's returns the other)
+    for mine, ieee in ((o[29], o[16]), (o[30], o[17])):
+        same = (mine[pos] == ieee[pos]) | (np.isnan(mine[pos]) & np.isnan(ieee[pos]))
+        assert same.all(), (a[pos][~same][:4], b[pos][~same][:4], mine[pos][~same][:4], ieee[pos][~same][:4])
+    same = (o[31] == o[7]) | (np.isnan(o[31]) & np.isnan(o[7]))
+    assert same.all(), (a[~same][:4], o[31][~same][:4], o[7][~same][:4])
