@@ -12,9 +12,9 @@ NLEVSNO, NLEVSOI, NLEVGRND = abi.NLEVSNO, abi.NLEVSOI, abi.NLEVGRND
 # included), FP64-pipe warp instructions (every FP64 instruction one issue
 # slot of the pipe, whatever its lanes) and DRAM bytes read + written.  The
 # full 524,288-column launch is scaled from it by columns.
-FLOPS_PER_COLUMN_STEP = (143180655 + 157036799 + 2 * 399076403) / 65536.0
-FP64_WARP_INST_PER_COLUMN_STEP = 29425746 / 65536.0
-TRAFFIC_PER_COLUMN_STEP = (571910656 + 339028736) / 65536.0
+FLOPS_PER_COLUMN_STEP = (150967449 + 161048536 + 2 * 403756673) / 65536.0
+FP64_WARP_INST_PER_COLUMN_STEP = 28241444 / 65536.0
+TRAFFIC_PER_COLUMN_STEP = (575314944 + 351197952) / 65536.0
 
 # FP64 floating-point operations per CanopyFluxes pass of one patch
 # (canopy_iterate_kernel: DADD + DMUL + 2 x DFMA executed over 262,144 patches
