@@ -21,6 +21,7 @@
 #include <cooperative_groups.h>
 #include "ctsm_device.cuh"
 #include "soil_math.cuh"
+#include "cr_div.cuh"
 #include "moisture_form_kernels.cuh"
 #include "moisture_form_device.cuh"
 #include "hydrology_device.cuh"
@@ -49,16 +50,19 @@ struct ColView {
 // Clapp-Hornberger suction and its derivative w.r.t. volumetric liquid water
 // (soil_suction, SoilWaterRetentionCurveClappHornberg1978Mod.F90:95-125; the
 // division by watsat is compute_hydraulic_properties' :1540)
-__device__ __forceinline__ void suction(const ColView& k, int j, double s2, double& smp, double& dsmpdw) {
+// Quotients go through cr_div.cuh (the IEEE quotient's bits but for a/b
+// within 2^-79 |a/b| of a rounding midpoint); rws is the level's 1/watsat.
+__device__ __forceinline__ void suction(const ColView& k, int j, double s2, const Recip& rws, double& smp,
+                                        double& dsmpdw) {
     const double bsw = k.g(k.io.bsw, j);
     smp = -k.g(k.io.sucsat, j) * fm::pow(s2, -bsw);
-    const double dsmpds = -bsw * smp / s2;
-    dsmpdw = dsmpds / k.g(k.io.watsat, j);
+    const double dsmpds = divf(-bsw * smp, s2);
+    dsmpdw = divr(dsmpds, rws);
 }
 
-__device__ __forceinline__ double rel_sat(const ColView& k, int j, double liq) {
-    const double vwc = (ic::ltc(liq, 1.0e-6) ? 1.0e-6 : liq) / (k.ss(k.io.dz, j) * DENH2O);
-    double s2 = vwc / k.g(k.io.watsat, j);
+__device__ __forceinline__ double rel_sat(const ColView& k, int j, double liq, const Recip& rws) {
+    const double vwc = divf(ic::ltc(liq, 1.0e-6) ? 1.0e-6 : liq, k.ss(k.io.dz, j) * DENH2O);
+    double s2 = divr(vwc, rws);
     s2 = ic::gtc(s2, 1.0) ? 1.0 : s2;
     return ic::gtc(s2, 0.01) ? s2 : 0.01;
 }
@@ -122,9 +126,10 @@ __device__ int mf_trial(MFLane<EXPENSIVE>& L, const ctsmg_soilwater_io& io, cons
     L.nsub = L.nsub + 1;
     const double dtsub = L.dtsub;
     // ---- level 1 suction, then stream the levels
-    double s2c = rel_sat(k, 1, L.liq[1]);
+    Recip rws_c = recip(k.g(io.watsat, 1));
+    double s2c = rel_sat(k, 1, L.liq[1], rws_c);
     double smp_c, dsmpdw_c;
-    suction(k, 1, s2c, smp_c, dsmpdw_c);
+    suction(k, 1, s2c, rws_c, smp_c, dsmpdw_c);
     double qin = L.qinfl, dqidw0 = 0.0, dqidw1 = 0.0;
     double hk_nl = 0.0, dhkdw_nl = 0.0, qo_nl = 0.0, dq1_nl = 0.0;
     // pending dgtsv row: d_p, du_p, b_p; its sub-diagonal arrives with the next row
@@ -132,9 +137,11 @@ __device__ int mf_trial(MFLane<EXPENSIVE>& L, const ctsmg_soilwater_io& io, cons
 #pragma unroll 1
     for (int j = 1; j <= nl; ++j) {
         double s2n = 0.0, smp_n = 0.0, dsmpdw_n = 0.0;
+        Recip rws_n = rws_c;
         if (j < nl) {
-            s2n = rel_sat(k, j + 1, L.liq[j + 1]);
-            suction(k, j + 1, s2n, smp_n, dsmpdw_n);
+            rws_n = recip(k.g(io.watsat, j + 1));
+            s2n = rel_sat(k, j + 1, L.liq[j + 1], rws_n);
+            suction(k, j + 1, s2n, rws_n, smp_n, dsmpdw_n);
         }
         double s1, imped;
         if (j == nl) {
@@ -146,38 +153,38 @@ __device__ int mf_trial(MFLane<EXPENSIVE>& L, const ctsmg_soilwater_io& io, cons
         }
         s1 = ic::gtc(s1, 1.0) ? 1.0 : s1;
         s1 = ic::gtc(s1, 0.01) ? s1 : 0.01;
-        const double ws = k.g(io.watsat, j), bsw = k.g(io.bsw, j);
+        const double bsw = k.g(io.bsw, j);
         const double hkj = imped * k.g(io.hksat, j) * fm::pow(s1, 2.0 * bsw + 3.0);
-        const double dhkdw = (2.0 * bsw + 3.0) * hkj / s1;
+        const double dhkdw = divf((2.0 * bsw + 3.0) * hkj, s1);
         io.smp_l[L.c + (j - 1) * ld] = smp_c;
         io.hk_l[L.c + (j - 1) * ld] = hkj;
         if (wt && j == jwt + 1) {
-            L.vwc_q = (ic::ltc(L.liq[j], 1.0e-6) ? 1.0e-6 : L.liq[j]) / (k.ss(io.dz, j) * DENH2O);
+            L.vwc_q = divf(ic::ltc(L.liq[j], 1.0e-6) ? 1.0e-6 : L.liq[j], k.ss(io.dz, j) * DENH2O);
             L.imped_q = imped;
         }
         // flux out of the bottom of level j and its derivatives
         double qo, dq1, dq2;
         if (j < nl) {
-            const double dhkds1 = 0.5 * dhkdw / ws;
-            const double dhkds2 = 0.5 * dhkdw / k.g(io.watsat, j + 1);
+            const double dhkds1 = divr(0.5 * dhkdw, rws_c);
+            const double dhkds2 = divr(0.5 * dhkdw, rws_n);
             const double num = smp_n - smp_c;
-            const double den = M_TO_MM * (k.ss(io.z, j + 1) - k.ss(io.z, j));
-            qo = -hkj * num / den + hkj;
-            dq1 = (hkj * dsmpdw_c - dhkds1 * num) / den + dhkds1;
-            dq2 = (-hkj * dsmpdw_n - dhkds2 * num) / den + dhkds2;
+            const Recip rden = recip(M_TO_MM * (k.ss(io.z, j + 1) - k.ss(io.z, j)));
+            qo = divr(-hkj * num, rden) + hkj;
+            dq1 = divr(hkj * dsmpdw_c - dhkds1 * num, rden) + dhkds1;
+            dq2 = divr(-hkj * dsmpdw_n - dhkds2 * num, rden) + dhkds2;
         } else if (P.lower_bc == 3) {            // bc_waterTable (nl == nlevsoi)
             if (NLEVSOI > jwt) {
                 qo = 0.0; dq1 = 0.0; dq2 = 0.0;
             } else {
-                const double dhkds1 = dhkdw / ws;
+                const double dhkds1 = divr(dhkdw, rws_c);
                 const double num = -smp_c;
-                const double den = M_TO_MM * (L.zwt - k.ss(io.z, j));
-                qo = -hkj * num / den + hkj;
-                dq1 = (hkj * dsmpdw_c - dhkds1 * num) / den + dhkds1;
+                const Recip rden = recip(M_TO_MM * (L.zwt - k.ss(io.z, j)));
+                qo = divr(-hkj * num, rden) + hkj;
+                dq1 = divr(hkj * dsmpdw_c - dhkds1 * num, rden) + dhkds1;
                 dq2 = 0.0;
             }
         } else if (P.lower_bc == 1) {            // bc_flux: free drainage
-            qo = hkj; dq1 = dhkdw / ws; dq2 = 0.0;
+            qo = hkj; dq1 = divr(dhkdw, rws_c); dq2 = 0.0;
         } else {                                 // bc_zero_flux
             qo = 0.0; dq1 = 0.0; dq2 = 0.0;
         }
@@ -185,7 +192,7 @@ __device__ int mf_trial(MFLane<EXPENSIVE>& L, const ctsmg_soilwater_io& io, cons
         if (EXPENSIVE) { L.dqodw1[j] = dq1; L.dqodw2[j] = dq2; }
         if (j == nl) { hk_nl = hkj; dhkdw_nl = dhkdw; qo_nl = qo; dq1_nl = dq1; }
         // tridiagonal row j
-        const double dt_dz = dtsub / (M_TO_MM * k.ss(io.dz, j));
+        const double dt_dz = divf(dtsub, M_TO_MM * k.ss(io.dz, j));
         const double amx = (j == 1) ? 0.0 : dqidw0 * dt_dz;
         const double bmx = -1.0 - (-dqidw1 + dq1) * dt_dz;
         const double cmx = (j == nl) ? 0.0 : -dq2 * dt_dz;
@@ -198,12 +205,12 @@ __device__ int mf_trial(MFLane<EXPENSIVE>& L, const ctsmg_soilwater_io& io, cons
             double dl = amx, dn = bmx, dun = cmx, bn = rmx;
             if (ic::abs_ge(d_p, dl)) {
                 if (!ic::ne0(d_p)) { *info = j - 1; return MF_SINGULAR; }
-                const double fact = dl / d_p;
+                const double fact = divf(dl, d_p);
                 dn = dn - fact * du_p;
                 bn = bn - fact * b_p;
                 dl2[j - 1] = 0.0;
             } else {
-                const double fact = d_p / dl;
+                const double fact = divf(d_p, dl);
                 d_p = dl;
                 const double temp = dn;
                 dn = du_p - fact * temp;
@@ -219,20 +226,20 @@ __device__ int mf_trial(MFLane<EXPENSIVE>& L, const ctsmg_soilwater_io& io, cons
         }
         // next level
         qin = qo; dqidw0 = dq1; dqidw1 = dq2;
-        s2c = s2n; smp_c = smp_n; dsmpdw_c = dsmpdw_n;
+        s2c = s2n; smp_c = smp_n; dsmpdw_c = dsmpdw_n; rws_c = rws_n;
     }
     if (!ic::ne0(d_p)) { *info = nl; return MF_SINGULAR; }
     d[nl] = d_p; du[nl] = du_p; b[nl] = b_p;
     // back substitution (1-based rows here)
-    b[nl] = b[nl] / d[nl];
-    if (nl > 1) b[nl - 1] = (b[nl - 1] - du[nl - 1] * b[nl]) / d[nl - 1];
+    b[nl] = divf(b[nl], d[nl]);
+    if (nl > 1) b[nl - 1] = divf(b[nl - 1] - du[nl - 1] * b[nl], d[nl - 1]);
 #pragma unroll 1
-    for (int i = nl - 2; i >= 1; --i) b[i] = (b[i] - du[i] * b[i + 1] - dl2[i] * b[i + 2]) / d[i];
+    for (int i = nl - 2; i >= 1; --i) b[i] = divf(b[i] - du[i] * b[i + 1] - dl2[i] * b[i + 2], d[i]);
     // ---- error estimate (:1306-1348)
     double errorMax = 0.0;
 #pragma unroll 1
     for (int j = 1; j <= nl; ++j) {
-        const double dt_dz = dtsub / (M_TO_MM * k.ss(io.dz, j));
+        const double dt_dz = divf(dtsub, M_TO_MM * k.ss(io.dz, j));
         const double qi = (j == 1) ? L.qinfl : qout_c[(j - 2) * ld];
         const double qo = qout_c[(j - 1) * ld];
         double fluxNet0;
@@ -243,7 +250,7 @@ __device__ int mf_trial(MFLane<EXPENSIVE>& L, const ctsmg_soilwater_io& io, cons
                                                : qo + L.dqodw1[j] * b[j] + L.dqodw2[j] * b[j + 1];
             fluxNet0 = qin_test - qout_test - k.g(io.qflx_rootsoi, j);
         } else {
-            fluxNet0 = b[j] / dt_dz;
+            fluxNet0 = divf(b[j], dt_dz);
         }
         // fluxNet1, the net flux at the start of the sub-step, as the row's rmx had it
         const double fn1 = qi - qo - k.g(io.qflx_rootsoi, j);
