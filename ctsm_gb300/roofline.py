@@ -19,10 +19,11 @@ TRAFFIC_PER_COLUMN_STEP = (575314944 + 351197952) / 65536.0
 # FP64 floating-point operations per CanopyFluxes pass of one patch
 # (canopy_iterate_kernel: DADD + DMUL + 2 x DFMA executed over 262,144 patches
 # of the canopy workload, 5.508 passes per patch on average), and DRAM bytes
-# per patch-step of that kernel from the 1-pass capture of the full
-# 2,097,152-patch launch.
+# per patch-step of that kernel from a capture of one launch over 262,144
+# patches of the same workload (3.5 GB of traffic, larger than L2), scaled to
+# the full launch by patches.
 CANOPY_FLOPS_PER_PASS = (489099825 + 889105990 + 2 * 2293152799) / (262144 * 5.507728576660156)
-CANOPY_TRAFFIC_PER_PATCH_STEP = (39389850624 + 15903046144) / 2097152.0
+CANOPY_TRAFFIC_PER_PATCH_STEP = (2404084224 + 1122854912) / 262144.0
 
 
 def _active_levels(kind, nsnow):
