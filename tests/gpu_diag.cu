@@ -10,7 +10,8 @@
 //     reciprocal RN(1/b[i]) (3n doubles).
 //   ctsmg_diag_fcmp(n, a, b, out): the integer-pipe comparisons of fcmp.cuh
 //     beside the FP64 ones -- rows 0-7 a<b, a<=b, a>b, a>=b, a==b, a!=0,
-//     |a|>0 (IEEE), row 7 fmax(a, 0), rows 8-14 the same from fcmp.cuh, rows
+//     |a|>0 (IEEE), row 7 fmax(a, 0), rows 8-14 the same from fcmp.cuh, row
+//     15 ic::abs_ge(a, b), rows
 //     16-19 fmin(a,b), fmax(a,b), ic::min, ic::max, row 20 fm::i2d(i - n/2),
 //     rows 21-24 ic::ltc, lec, gtc, gec (b > 0) or ltn, -, gtn, - (b < 0),
 //     rows 25-28 ic::lt0, le0, gt0, ge0 of a, rows 29-31 ic::minc(a, b),
@@ -125,7 +126,7 @@ __global__ void diag_fcmp_kernel(int n, const double* __restrict__ a, const doub
     put(0, x < y); put(1, x <= y); put(2, x > y); put(3, x >= y); put(4, x == y); put(5, x != 0.0);
     put(6, fabs(x) > 0.0); put(7, fmax(x, 0.0));
     put(8, ic::lt(x, y)); put(9, ic::le(x, y)); put(10, ic::gt(x, y)); put(11, ic::ge(x, y));
-    put(12, ic::eq(x, y)); put(13, ic::ne0(x)); put(14, ic::abs_gt0(x)); put(15, 0.0);
+    put(12, ic::eq(x, y)); put(13, ic::ne0(x)); put(14, ic::abs_gt0(x)); put(15, ic::abs_ge(x, y));
     put(16, fmin(x, y)); put(17, fmax(x, y)); put(18, ic::min(x, y)); put(19, ic::max(x, y));
     put(20, fm::i2d(i - n / 2));
     const bool pos = y > 0.0;

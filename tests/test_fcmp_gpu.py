@@ -48,6 +48,7 @@ def test_integer_pipe_comparisons_match_fp64(gpu_lib):
         assert np.array_equal(o[k], o[8 + k]), (k, a[o[k] != o[8 + k]][:4], b[o[k] != o[8 + k]][:4])
     with np.errstate(invalid="ignore"):
         np.testing.assert_array_equal(o[0], (a < b).astype(float))
+        np.testing.assert_array_equal(o[15], (np.abs(a) >= np.abs(b)).astype(float))
     for ieee, mine in ((o[16], o[18]), (o[17], o[19])):
         same = (ieee == mine) | (np.isnan(ieee) & np.isnan(mine))
         assert same.all(), (a[~same][:4], b[~same][:4])
