@@ -298,6 +298,12 @@ def soil_gate(A0, npatch, G, nsteps, G1, balance, identical, sensitivity_runs=4)
     one_c, one_c_bad = compare_states(G1, o1.S, GATE_CANCEL, bands=bands)
     one.update({k + " (conditioned)": v for k, v in one_c.items()})
     one_bad = one_bad | one_c_bad
+    # how much the conditioned outputs lean on their band: the plain relative
+    # error and the columns that exceed 1e-9 without it
+    band_use = {}
+    for k in GATE_CANCEL:
+        e_plain, bad_plain = compare_states(G1, o1.S, (k,))
+        band_use[k] = {"max_rel_err_without_band": e_plain[k], "columns_above_tol_without_band": int(bad_plain.sum())}
     del o1
     # (2)
     o = OracleSoilStepper(A0, track_water=True)
@@ -320,7 +326,7 @@ def soil_gate(A0, npatch, G, nsteps, G1, balance, identical, sensitivity_runs=4)
     finite = int(np.count_nonzero(~np.isfinite(G["t_soisno"]).all(axis=0) | ~np.isfinite(G["h2osoi_liq"]).all(axis=0)))
     gate = {"columns": int(o.n), "steps": int(nsteps), "tol": GATE_TOL,
             "one_step_from_evolved_state": {"max_rel_err": one, "columns_above_tol": int(one_bad.sum()),
-                                            "conditioned": list(GATE_CANCEL)},
+                                            "conditioned": list(GATE_CANCEL), "band_use": band_use},
             "trajectory": {"max_rel_err": traj, "columns_above_tol": int(traj_bad.sum()),
                            "oracle_self_sensitive_columns": int(sens.sum()),
                            "above_tol_and_sensitive": int((traj_bad & sens).sum()),

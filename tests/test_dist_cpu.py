@@ -103,6 +103,8 @@ def test_soil_gate_passes_on_oracle_states_and_flags_a_planted_error():
     assert gate["trajectory"]["columns_above_tol"] == 0 and gate["one_step_from_evolved_state"]["columns_above_tol"] == 0
     assert all(v == 0.0 for v in gate["trajectory"]["max_rel_err"].values())
     assert gate["balance"]["oracle_errh2o_max_mm"] < 1e-9
+    use = gate["one_step_from_evolved_state"]["band_use"]
+    assert set(use) == set(bench.GATE_CANCEL) and all(v["columns_above_tol_without_band"] == 0 for v in use.values())
     bad = copy.deepcopy(G1)
     bad["t_soisno"][-1, 100] *= 1.0 + 1e-7
     gate, _, _ = bench.soil_gate(A, npatch, G, 3, bad, zero, True, sensitivity_runs=1)
@@ -112,6 +114,7 @@ def test_soil_gate_passes_on_oracle_states_and_flags_a_planted_error():
     bad["xmf"][:] = bad["xmf"] * (1.0 + 1e-6) + 1.0
     gate, _, _ = bench.soil_gate(A, npatch, G, 3, bad, zero, True, sensitivity_runs=1)
     assert not gate["pass"] and gate["one_step_from_evolved_state"]["max_rel_err"]["xmf (conditioned)"] > 1e-9
+    assert gate["one_step_from_evolved_state"]["band_use"]["xmf"]["columns_above_tol_without_band"] > 0
     over = (np.full(512, 2e-5), np.zeros(512))
     gate, _, _ = bench.soil_gate(A, npatch, G, 3, G1, over, True, sensitivity_runs=1)
     assert not gate["pass"] and gate["balance"]["columns_above_stop"] == 512
