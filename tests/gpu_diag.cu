@@ -9,10 +9,10 @@
 //     the shared-reciprocal quotient of cr_div.cuh, out[2n+i] = its
 //     reciprocal RN(1/b[i]) (3n doubles).
 //   ctsmg_diag_fcmp(n, a, b, out): the integer-pipe comparisons of fcmp.cuh
-//     beside the FP64 ones -- rows 0-7 a<b, a<=b, a>b, a>=b, a==b, a!=0,
-//     |a|>0 (IEEE), row 7 fmax(a, 0), rows 8-14 the same from fcmp.cuh, row
-//     15 ic::abs_ge(a, b), rows
-//     16-19 fmin(a,b), fmax(a,b), ic::min, ic::max, row 20 fm::i2d(i - n/2),
+//     beside the FP64 ones -- rows 0-6 a<b, a<=b, a>b, a>=b, a==b, a!=0,
+//     |a|>0 (IEEE), row 7 fmax(a, 0), rows 8-14 the same seven from
+//     fcmp.cuh, row 15 ic::abs_ge(a, b), rows 16-19 fmin(a,b), fmax(a,b),
+//     ic::min, ic::max, row 20 fm::i2d(i - n/2),
 //     rows 21-24 ic::ltc, lec, gtc, gec (b > 0) or ltn, -, gtn, - (b < 0),
 //     rows 25-28 ic::lt0, le0, gt0, ge0 of a, rows 29-31 ic::minc(a, b),
 //     ic::maxc(a, b) (b > 0), ic::max0(a) (32n doubles).
