@@ -231,6 +231,33 @@ class SoilBatch:
         self.L.ctsmg_batch_load.argtypes = [C.c_void_p, C.c_char_p]
         check(self.L.ctsmg_batch_load(self.h, str(path).encode()))
 
+    def save_restart(self, path):
+        """The resident state's restart variables, in the reference's restart
+        layout, to a NetCDF-3 file at `path` (ctsm_gb300/restart.py); returns
+        the variable names written."""
+        import os
+        import tempfile
+        from . import restart
+        with tempfile.TemporaryDirectory() as d:
+            ck = os.path.join(d, "state.ckpt")
+            self.save(ck)
+            return restart.checkpoint_to_restart(restart.read_checkpoint(ck), path)
+
+    def load_restart(self, path):
+        """Replace the resident components that the restart file at `path`
+        holds variables for (and h2osoi_vol, formed from them); the others
+        keep their resident values.  Returns the variable names read."""
+        import os
+        import tempfile
+        from . import restart
+        with tempfile.TemporaryDirectory() as d:
+            ck = os.path.join(d, "state.ckpt")
+            self.save(ck)
+            merged, read = restart.restart_into_checkpoint(path, restart.read_checkpoint(ck))
+            restart.write_checkpoint(ck, merged)
+            self.load(ck)
+        return read
+
     def state_bytes(self):
         return int(self.L.ctsmg_batch_state_bytes(self.h))
 

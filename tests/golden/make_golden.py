@@ -9,6 +9,11 @@ reference whose path is the one required argument:
   pedotransfer.json      src/main/FuncPedotransferMod.F90:28,83-103 (the default
                          Cosby 1984 table 5) and the organic-soil mixing of
                          src/biogeophys/SoilStateInitTimeConstMod.F90:200-210,543-602
+  restart_vars.json      the restartvar declarations (name, type, dimensions,
+                         dimension order on file) of the path's prognostic
+                         state: TemperatureType.F90, WaterStateType.F90,
+                         WaterStateBulkType.F90, WaterDiagnosticBulkType.F90,
+                         SoilHydrologyType.F90, subgridRestMod.F90
 
     python tests/golden/make_golden.py <path of the reference checkout>
 """
@@ -124,10 +129,65 @@ def pedotransfer():
             "bsw": stmt("bsw_col(c,lev)", "bsw_sf"), "watsat": stmt("watsat_col(c,lev)    =", "watsat_sf")}
 
 
+RESTART_SOURCES = ("src/biogeophys/TemperatureType.F90", "src/biogeophys/WaterStateType.F90",
+                   "src/biogeophys/WaterStateBulkType.F90", "src/biogeophys/WaterDiagnosticBulkType.F90",
+                   "src/biogeophys/SoilHydrologyType.F90", "src/main/subgridRestMod.F90")
+RESTART_NAMES = ("T_SOISNO", "T_GRND", "TH2OSFC", "T_VEG", "H2OSOI_LIQ", "H2OSOI_ICE", "H2OSFC",
+                 "H2OSNO_NO_LAYERS", "WA", "ZWT", "ZWT_PERCH", "FROST_TABLE", "SNLSNO", "SNOW_DEPTH",
+                 "frac_sno_eff", "frac_sno", "FH2OSFC", "INT_SNOW", "SNOMELT_ACCUM", "LIQCAN", "SNOCAN")
+
+
+def _call_text(txt, start):
+    """The text of a Fortran call from `start` to its closing parenthesis
+    (parentheses inside quoted strings and comments do not count)."""
+    i = txt.index("(", start) + 1
+    depth, quote = 1, None
+    while depth:
+        c = txt[i]
+        if quote:
+            if c == quote:
+                quote = None
+        elif c in "'\"":
+            quote = c
+        elif c == "!":
+            i = txt.index("\n", i)
+            continue
+        elif c == "(":
+            depth += 1
+        elif c == ")":
+            depth -= 1
+        i += 1
+    return txt[start:i]
+
+
+def restart_vars():
+    out = {}
+    for rel in RESTART_SOURCES:
+        txt = read(rel)
+        for m in re.finditer(r"call\s+restartvar\s*\(", txt):
+            call = _call_text(txt, m.start())
+            flat = re.sub(r"&\s*(!.*)?\n\s*&?", " ", call)
+            vm = re.search(r"varname\s*=\s*(?:this%info%fname\(\s*)?'(\w+)'", flat)
+            if not vm or vm.group(1) not in RESTART_NAMES or vm.group(1) in out:
+                continue
+            def opt(key, pat=r"'(\w+)'"):
+                r = re.search(key + r"\s*=\s*" + pat, flat)
+                return r.group(1).strip() if r else None
+            out[vm.group(1)] = {"file": rel, "line": txt.count("\n", 0, m.start()) + 1,
+                                "xtype": opt("xtype", r"(\w+)"), "dim1name": opt("dim1name"),
+                                "dim2name": opt("dim2name"), "switchdim": opt("switchdim", r"(\.\w+\.)") == ".true.",
+                                "lowerb2": opt("lowerb2", r"([^,)]+)"), "upperb2": opt("upperb2", r"([^,)]+)")}
+    missing = [n for n in RESTART_NAMES if n not in out]
+    if missing:
+        sys.exit("restartvar declarations not found: %s" % missing)
+    return {"source": "restartvar calls of %s" % ", ".join(os.path.basename(r) for r in RESTART_SOURCES),
+            "vars": out}
+
+
 def main():
     for fname, fn in (("layer_table_20sl.json", layer_table), ("skip_steps.json", skip_steps),
                       ("quadratic_kat.json", quadratic), ("qsat_coeffs.json", qsat),
-                      ("pedotransfer.json", pedotransfer)):
+                      ("pedotransfer.json", pedotransfer), ("restart_vars.json", restart_vars)):
         with open(os.path.join(OUT, fname), "w") as f:
             json.dump(fn(), f, indent=1)
         print("wrote", fname)
